@@ -1,0 +1,186 @@
+"""ctypes binding of libfhg.so (include/fhg.h).
+
+The library is built in-tree by :mod:`fhhos4_gb300.build`; importing this module
+never falls back to anything else: a missing library raises ``ImportError`` with
+the build command, and every nonzero status raises :class:`FhgError`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .build import LIB
+
+FHG_OK = 0
+FHG_ERR_INVALID_ARG = -1
+FHG_ERR_CUDA = -2
+FHG_ERR_NOT_READY = -3
+FHG_ERR_SINGULAR_BLOCK = -4
+FHG_ERR_NOT_SPD = -5
+FHG_ERR_DIVERGED = -6
+FHG_ERR_NAN = -7
+FHG_ERR_TOO_LARGE = -8
+FHG_ERR_UNSUPPORTED = -9
+
+SMOOTHERS = {"bgs": 0, "rbgs": 1, "bj": 2, "bj23": 3}
+KRYLOV = {"fcg": 0, "cg": 1}
+PRECISION = {"fp64": 0, "fp32": 1}
+
+OP_SPMV, OP_RESIDUAL, OP_RESTRICT, OP_PROLONG_ADD = 0, 1, 2, 3
+OP_GS_FORWARD, OP_GS_BACKWARD, OP_JACOBI, OP_SYM_SPMV = 4, 5, 6, 7
+OP_COARSE_SOLVE, OP_VCYCLE = 8, 9
+
+# Every symbol include/fhg.h declares.
+EXPORTS = ["fhg_default_options", "fhg_create", "fhg_destroy", "fhg_last_error", "fhg_set_level",
+           "fhg_set_prolongation", "fhg_setup", "fhg_solve", "fhg_solve_device", "fhg_apply",
+           "fhg_time_op", "fhg_level_info", "fhg_get_permutation", "fhg_kernel_launches"]
+
+
+class FhgError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"fhg error {code}: {message}")
+        self.code = code
+
+
+class Options(C.Structure):
+    _fields_ = [("krylov", C.c_int), ("pre_smoother", C.c_int), ("post_smoother", C.c_int),
+                ("pre_iterations", C.c_int), ("post_iterations", C.c_int), ("omega", C.c_double),
+                ("tolerance", C.c_double), ("max_iterations", C.c_int), ("vcycle_precision", C.c_int),
+                ("colouring", C.c_int), ("use_graphs", C.c_int), ("autotune", C.c_int),
+                ("max_coarse_rows", C.c_int)]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("status", C.c_int), ("normalized_residual", C.c_double),
+                ("solve_ms", C.c_double)]
+
+
+_lib = None
+
+
+def load(path: str = LIB):
+    """Load libfhg.so (raises ImportError when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -m fhhos4_gb300.build`")
+    lib = C.CDLL(path)
+    P = C.POINTER
+    lib.fhg_default_options.argtypes = [P(Options)]
+    lib.fhg_default_options.restype = None
+    lib.fhg_create.argtypes = [P(C.c_void_p), C.c_int]
+    lib.fhg_destroy.argtypes = [C.c_void_p]
+    lib.fhg_destroy.restype = None
+    lib.fhg_last_error.argtypes = [C.c_void_p]
+    lib.fhg_last_error.restype = C.c_char_p
+    lib.fhg_set_level.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.fhg_set_prolongation.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.fhg_setup.argtypes = [C.c_void_p, C.c_int, P(Options)]
+    lib.fhg_solve.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, P(SolveInfo)]
+    lib.fhg_solve_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, P(SolveInfo)]
+    lib.fhg_apply.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.fhg_time_op.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_double)]
+    lib.fhg_level_info.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_longlong), P(C.c_int), P(C.c_int),
+                                   P(C.c_longlong)]
+    lib.fhg_get_permutation.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    lib.fhg_kernel_launches.argtypes = [C.c_void_p]
+    lib.fhg_kernel_launches.restype = C.c_longlong
+    _lib = lib
+    return lib
+
+
+def ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+class Context:
+    """Owns one fhg_ctx (one hierarchy on one GPU)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        self.h = C.c_void_p()
+        rc = self.lib.fhg_create(C.byref(self.h), device)
+        self._check(rc)
+
+    def _check(self, rc: int):
+        if rc != FHG_OK:
+            msg = self.lib.fhg_last_error(self.h).decode() if self.h else "no context"
+            raise FhgError(rc, msg)
+
+    def close(self):
+        if self.h:
+            self.lib.fhg_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- hierarchy -------------------------------------------------------
+    def set_level(self, level: int, block_size: int, A):
+        rp = np.ascontiguousarray(A.indptr, dtype=np.int32)
+        ci = np.ascontiguousarray(A.indices, dtype=np.int32)
+        va = np.ascontiguousarray(A.data, dtype=np.float64)
+        self._check(self.lib.fhg_set_level(self.h, level, block_size, A.shape[0], ptr(rp), ptr(ci), ptr(va)))
+
+    def set_prolongation(self, level: int, P):
+        rp = np.ascontiguousarray(P.indptr, dtype=np.int32)
+        ci = np.ascontiguousarray(P.indices, dtype=np.int32)
+        va = np.ascontiguousarray(P.data, dtype=np.float64)
+        self._check(self.lib.fhg_set_prolongation(self.h, level, P.shape[0], P.shape[1], ptr(rp), ptr(ci), ptr(va)))
+
+    def setup(self, nlevels: int, opts: Options):
+        self._check(self.lib.fhg_setup(self.h, nlevels, C.byref(opts)))
+
+    # -- solve -----------------------------------------------------------
+    def solve(self, b: np.ndarray, max_iterations: int):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.empty_like(b)
+        hist = np.zeros(max_iterations + 1)
+        info = SolveInfo()
+        rc = self.lib.fhg_solve(self.h, ptr(b), ptr(x), ptr(hist), C.byref(info))
+        return rc, x, hist[: info.iterations + 1].copy(), info
+
+    def solve_device(self, b_dev_ptr: int, x_dev_ptr: int, max_iterations: int):
+        hist = np.zeros(max_iterations + 1)
+        info = SolveInfo()
+        rc = self.lib.fhg_solve_device(self.h, C.c_void_p(b_dev_ptr), C.c_void_p(x_dev_ptr), ptr(hist),
+                                       C.byref(info))
+        return rc, hist[: info.iterations + 1].copy(), info
+
+    def apply(self, level: int, op: int, inp: np.ndarray, aux: np.ndarray | None, n_out: int):
+        inp = np.ascontiguousarray(inp, dtype=np.float64)
+        auxa = None if aux is None else np.ascontiguousarray(aux, dtype=np.float64)
+        out = np.empty(n_out)
+        self._check(self.lib.fhg_apply(self.h, level, op, ptr(inp), ptr(auxa), ptr(out)))
+        return out
+
+    def time_op(self, level: int, op: int, warmup: int = 3, reps: int = 20) -> float:
+        ms = C.c_double()
+        self._check(self.lib.fhg_time_op(self.h, level, op, warmup, reps, C.byref(ms)))
+        return ms.value
+
+    def level_info(self, level: int):
+        nb, nbl, nc, lanes, pb = C.c_int(), C.c_longlong(), C.c_int(), C.c_int(), C.c_longlong()
+        self._check(self.lib.fhg_level_info(self.h, level, C.byref(nb), C.byref(nbl), C.byref(nc), C.byref(lanes),
+                                            C.byref(pb)))
+        return dict(block_rows=nb.value, blocks=nbl.value, colours=nc.value, lanes=lanes.value, p_blocks=pb.value)
+
+    def permutation(self, level: int, nb: int) -> np.ndarray:
+        perm = np.empty(nb, dtype=np.int32)
+        self._check(self.lib.fhg_get_permutation(self.h, level, ptr(perm)))
+        return perm
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.fhg_kernel_launches(self.h))
+
+
+def default_options() -> Options:
+    o = Options()
+    load().fhg_default_options(C.byref(o))
+    return o

@@ -1,0 +1,1180 @@
+// libfhg host side: the C ABI of include/fhg.h.
+//
+// Setup (host, once; the reference's Multigrid::Setup, src/Solver/Multigrid/Multigrid.h:88-313):
+//   scalar CSR of every A_l, P_l  ->  face-block BSR  ->  greedy multicolouring of the block
+//   graph  ->  colour-grouped numbering  ->  pre-inverted diagonal blocks, R = P^T,
+//   symmetrised outer operator, dense inverse of the coarsest operator  ->  upload.
+// Solve (device only): FCG(1) or PCG preconditioned by one V-cycle from zero, Krylov
+// scalars on the device, one CUDA graph per iteration, one 8-byte read-back of the
+// normalised residual per iteration for the stopping test.
+#include "fhg.h"
+#include "fhg_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <thread>
+#include <vector>
+
+using fhg::BsrView;
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Host containers
+
+struct HostCsr {
+    int n_rows = 0, n_cols = 0;
+    std::vector<int> rowptr, colidx;
+    std::vector<double> vals;
+    bool set = false;
+};
+
+// Block values block-major, row-major inside a block (host form).
+struct HostBsr {
+    int nbr = 0, nbc = 0, bs = 0;
+    std::vector<int> rowptr, colidx;
+    std::vector<double> vals;
+    long long nnzb() const { return (long long)colidx.size(); }
+};
+
+template <class T>
+struct DevBsr {
+    BsrView<T> v;
+    T* vals = nullptr;
+    int* rowptr = nullptr;
+    int* colidx = nullptr;
+    bool owns_index = true;
+};
+
+struct Level {
+    int n = 0, nb = 0, bs = 0;
+    HostCsr A_in, P_in;
+    int ncolours = 0;
+    std::vector<int> colour_start;  // block-row offsets of every colour, ncolours + 1
+    std::vector<int> perm;          // new block row -> given block row
+    DevBsr<double> A, Ahat, P, R;
+    bool ahat_is_a = true;
+    DevBsr<float> A32, P32, R32;
+    double* dinv = nullptr;
+    float* dinv32 = nullptr;
+    int* perm_d = nullptr;
+    double *x = nullptr, *b = nullptr, *r = nullptr;
+    float *x32 = nullptr, *b32 = nullptr, *r32 = nullptr;
+    double* cinv = nullptr;  // coarsest only, n x n row-major
+    long long p_blocks = 0;
+};
+
+}  // namespace
+
+struct fhg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    std::vector<Level> levels;
+    int nlevels = 0;
+    fhg_options opts{};
+    bool ready = false;
+    // Krylov state (level-0 numbering after permutation)
+    double *kx = nullptr, *kr = nullptr, *kb = nullptr, *kz[2] = {nullptr, nullptr}, *kAd[2] = {nullptr, nullptr};
+    double* partials = nullptr;  // 8 * kReduceCtas
+    double* scal = nullptr;      // [0]=bnorm [1]=dAdp [2]=nr [3]=rz [4]=beta
+    double* hist_d = nullptr;
+    int* counter_d = nullptr;
+    double* nr_host = nullptr;   // pinned
+    double* io = nullptr;        // user-numbered I/O scratch (2 * n0)
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    long long graph_kernels[2] = {0, 0};
+    int graphs_built = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<void*> allocations;
+};
+
+namespace {
+
+int fail(fhg_ctx* c, int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail(ctx, FHG_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));       \
+    } while (0)
+
+template <class T>
+int dalloc(fhg_ctx* ctx, T** p, size_t count)
+{
+    void* q = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+    if (e != cudaSuccess)
+        return fail(ctx, FHG_ERR_CUDA, "cudaMalloc(%zu bytes) failed: %s", count * sizeof(T), cudaGetErrorString(e));
+    ctx->allocations.push_back(q);
+    *p = (T*)q;
+    return FHG_OK;
+}
+
+template <class T>
+int upload(fhg_ctx* ctx, T** p, const T* src, size_t count)
+{
+    int rc = dalloc(ctx, p, count);
+    if (rc) return rc;
+    if (count) CK(cudaMemcpy(*p, src, count * sizeof(T), cudaMemcpyHostToDevice));
+    return FHG_OK;
+}
+
+int check_csr(fhg_ctx* ctx, const char* what, int n_rows, int n_cols, const int* rp, const int* ci)
+{
+    if (rp[0] != 0) return fail(ctx, FHG_ERR_INVALID_ARG, "%s: rowptr[0] != 0", what);
+    for (int i = 0; i < n_rows; i++) {
+        if (rp[i + 1] < rp[i]) return fail(ctx, FHG_ERR_INVALID_ARG, "%s: rowptr decreases at row %d", what, i);
+        for (int p = rp[i]; p < rp[i + 1]; p++) {
+            if (ci[p] < 0 || ci[p] >= n_cols)
+                return fail(ctx, FHG_ERR_INVALID_ARG, "%s: column %d out of range in row %d", what, ci[p], i);
+            if (p > rp[i] && ci[p] <= ci[p - 1])
+                return fail(ctx, FHG_ERR_INVALID_ARG, "%s: columns not strictly ascending in row %d", what, i);
+        }
+    }
+    return FHG_OK;
+}
+
+// Scalar CSR -> BSR with square bs x bs blocks (missing entries of a stored block are 0).
+void csr_to_bsr(const HostCsr& A, int bs, HostBsr& B)
+{
+    B.bs = bs;
+    B.nbr = A.n_rows / bs;
+    B.nbc = A.n_cols / bs;
+    B.rowptr.assign(B.nbr + 1, 0);
+    std::vector<int> mark(B.nbc, -1);
+    for (int I = 0; I < B.nbr; I++) {
+        int cnt = 0;
+        for (int k = 0; k < bs; k++) {
+            const int i = I * bs + k;
+            for (int p = A.rowptr[i]; p < A.rowptr[i + 1]; p++) {
+                const int J = A.colidx[p] / bs;
+                if (mark[J] != I) { mark[J] = I; cnt++; }
+            }
+        }
+        B.rowptr[I + 1] = B.rowptr[I] + cnt;
+    }
+    B.colidx.assign(B.rowptr[B.nbr], 0);
+    B.vals.assign((size_t)B.rowptr[B.nbr] * bs * bs, 0.0);
+    std::fill(mark.begin(), mark.end(), -1);
+    std::vector<int> slot(B.nbc, 0);
+    std::vector<int> cols;
+    for (int I = 0; I < B.nbr; I++) {
+        cols.clear();
+        for (int k = 0; k < bs; k++) {
+            const int i = I * bs + k;
+            for (int p = A.rowptr[i]; p < A.rowptr[i + 1]; p++) {
+                const int J = A.colidx[p] / bs;
+                if (mark[J] != I) { mark[J] = I; cols.push_back(J); }
+            }
+        }
+        std::sort(cols.begin(), cols.end());
+        const int base = B.rowptr[I];
+        for (size_t q = 0; q < cols.size(); q++) {
+            B.colidx[base + q] = cols[q];
+            slot[cols[q]] = base + (int)q;
+        }
+        for (int k = 0; k < bs; k++) {
+            const int i = I * bs + k;
+            for (int p = A.rowptr[i]; p < A.rowptr[i + 1]; p++) {
+                const int j = A.colidx[p], J = j / bs;
+                B.vals[(size_t)slot[J] * bs * bs + k * bs + (j - J * bs)] = A.vals[p];
+            }
+        }
+    }
+}
+
+// Greedy colouring of the symmetric block graph in block-row order: colour(I) is the
+// smallest colour absent from the already-coloured neighbours of I (rows and columns of
+// the stored pattern). Same algorithm as the oracle's orc_greedy_colouring.
+int greedy_colouring(const HostBsr& B, std::vector<int>& colour)
+{
+    const int nb = B.nbr;
+    // transpose pattern
+    std::vector<int> trp(nb + 1, 0), tci(B.colidx.size());
+    for (int J : B.colidx) trp[J + 1]++;
+    for (int j = 0; j < nb; j++) trp[j + 1] += trp[j];
+    std::vector<int> fill(trp.begin(), trp.end() - 1);
+    for (int I = 0; I < nb; I++)
+        for (int p = B.rowptr[I]; p < B.rowptr[I + 1]; p++) tci[fill[B.colidx[p]]++] = I;
+    colour.assign(nb, -1);
+    std::vector<int> mark(nb + 1, -1);
+    int maxc = 0;
+    for (int I = 0; I < nb; I++) {
+        for (int p = B.rowptr[I]; p < B.rowptr[I + 1]; p++) {
+            const int J = B.colidx[p];
+            if (J != I && colour[J] >= 0) mark[colour[J]] = I;
+        }
+        for (int p = trp[I]; p < trp[I + 1]; p++) {
+            const int J = tci[p];
+            if (J != I && colour[J] >= 0) mark[colour[J]] = I;
+        }
+        int c = 0;
+        while (mark[c] == I) c++;
+        colour[I] = c;
+        maxc = std::max(maxc, c + 1);
+    }
+    return maxc;
+}
+
+// B' with rows perm_r (new -> old) and columns renumbered by iperm_c (old -> new).
+void permute_bsr(const HostBsr& B, const std::vector<int>& perm_r, const std::vector<int>& iperm_c, HostBsr& O)
+{
+    const int bs = B.bs, bb = bs * bs;
+    O.bs = bs; O.nbr = B.nbr; O.nbc = B.nbc;
+    O.rowptr.assign(O.nbr + 1, 0);
+    for (int I = 0; I < O.nbr; I++) {
+        const int src = perm_r[I];
+        O.rowptr[I + 1] = O.rowptr[I] + (B.rowptr[src + 1] - B.rowptr[src]);
+    }
+    O.colidx.resize(B.colidx.size());
+    O.vals.resize(B.vals.size());
+    std::vector<std::pair<int, int>> row;
+    for (int I = 0; I < O.nbr; I++) {
+        const int src = perm_r[I];
+        row.clear();
+        for (int p = B.rowptr[src]; p < B.rowptr[src + 1]; p++) row.emplace_back(iperm_c[B.colidx[p]], p);
+        std::sort(row.begin(), row.end());
+        int q = O.rowptr[I];
+        for (auto& e : row) {
+            O.colidx[q] = e.first;
+            std::memcpy(&O.vals[(size_t)q * bb], &B.vals[(size_t)e.second * bb], sizeof(double) * bb);
+            q++;
+        }
+    }
+}
+
+void transpose_bsr(const HostBsr& B, HostBsr& T)
+{
+    const int bs = B.bs, bb = bs * bs;
+    T.bs = bs; T.nbr = B.nbc; T.nbc = B.nbr;
+    T.rowptr.assign(T.nbr + 1, 0);
+    for (int J : B.colidx) T.rowptr[J + 1]++;
+    for (int j = 0; j < T.nbr; j++) T.rowptr[j + 1] += T.rowptr[j];
+    T.colidx.resize(B.colidx.size());
+    T.vals.resize(B.vals.size());
+    std::vector<int> fill(T.rowptr.begin(), T.rowptr.end() - 1);
+    for (int I = 0; I < B.nbr; I++)
+        for (int p = B.rowptr[I]; p < B.rowptr[I + 1]; p++) {
+            const int q = fill[B.colidx[p]]++;
+            T.colidx[q] = I;
+            for (int r = 0; r < bs; r++)
+                for (int c = 0; c < bs; c++) T.vals[(size_t)q * bb + c * bs + r] = B.vals[(size_t)p * bb + r * bs + c];
+        }
+}
+
+// tril(A) + tril(A,-1)^T: the operator A.selfadjointView<Eigen::Lower>() applies
+// (src/Solver/Krylov/FlexibleConjugateGradient.h:124).
+void symmetrise_lower(const HostCsr& A, HostCsr& S)
+{
+    const int n = A.n_rows;
+    std::vector<int> urp(n + 1, 0);
+    for (int i = 0; i < n; i++)
+        for (int p = A.rowptr[i]; p < A.rowptr[i + 1]; p++)
+            if (A.colidx[p] < i) urp[A.colidx[p] + 1]++;
+    for (int i = 0; i < n; i++) urp[i + 1] += urp[i];
+    std::vector<int> uci(urp[n]);
+    std::vector<double> uva(urp[n]);
+    std::vector<int> fill(urp.begin(), urp.end() - 1);
+    for (int i = 0; i < n; i++)
+        for (int p = A.rowptr[i]; p < A.rowptr[i + 1]; p++)
+            if (A.colidx[p] < i) {
+                const int q = fill[A.colidx[p]]++;
+                uci[q] = i;
+                uva[q] = A.vals[p];
+            }
+    S.n_rows = S.n_cols = n;
+    S.rowptr.assign(n + 1, 0);
+    S.colidx.clear(); S.vals.clear();
+    S.colidx.reserve(A.colidx.size());
+    S.vals.reserve(A.vals.size());
+    for (int i = 0; i < n; i++) {
+        for (int p = A.rowptr[i]; p < A.rowptr[i + 1] && A.colidx[p] <= i; p++) {
+            S.colidx.push_back(A.colidx[p]);
+            S.vals.push_back(A.vals[p]);
+        }
+        for (int q = urp[i]; q < urp[i + 1]; q++) {
+            S.colidx.push_back(uci[q]);
+            S.vals.push_back(uva[q]);
+        }
+        S.rowptr[i + 1] = (int)S.colidx.size();
+    }
+    S.set = true;
+}
+
+bool csr_equal(const HostCsr& A, const HostCsr& B)
+{
+    return A.rowptr == B.rowptr && A.colidx == B.colidx &&
+           std::memcmp(A.vals.data(), B.vals.data(), sizeof(double) * A.vals.size()) == 0;
+}
+
+// Inverse of a bs x bs block by Gauss-Jordan elimination with full pivoting (FP64).
+bool invert_block(const double* a_in, int n, double* inv)
+{
+    double a[64], b[64];
+    int rp[8], cp[8];
+    std::memcpy(a, a_in, sizeof(double) * n * n);
+    for (int i = 0; i < n * n; i++) b[i] = 0.0;
+    for (int i = 0; i < n; i++) b[i * n + i] = 1.0;
+    (void)rp; (void)cp;
+    int colperm[8];
+    for (int i = 0; i < n; i++) colperm[i] = i;
+    for (int k = 0; k < n; k++) {
+        int bi = k, bj = k;
+        double best = -1.0;
+        for (int i = k; i < n; i++)
+            for (int j = k; j < n; j++)
+                if (std::fabs(a[i * n + j]) > best) { best = std::fabs(a[i * n + j]); bi = i; bj = j; }
+        if (!(best > 0.0) || !std::isfinite(best)) return false;
+        if (bi != k)
+            for (int j = 0; j < n; j++) { std::swap(a[k * n + j], a[bi * n + j]); std::swap(b[k * n + j], b[bi * n + j]); }
+        if (bj != k) {
+            for (int i = 0; i < n; i++) std::swap(a[i * n + k], a[i * n + bj]);
+            std::swap(colperm[k], colperm[bj]);
+        }
+        const double piv = a[k * n + k];
+        for (int j = 0; j < n; j++) { a[k * n + j] /= piv; b[k * n + j] /= piv; }
+        for (int i = 0; i < n; i++) {
+            if (i == k) continue;
+            const double f = a[i * n + k];
+            if (f == 0.0) continue;
+            for (int j = 0; j < n; j++) { a[i * n + j] -= f * a[k * n + j]; b[i * n + j] -= f * b[k * n + j]; }
+        }
+    }
+    // a is now the column permutation Q^T of the identity: (A Q)^{-1} = b  =>  A^{-1} = Q b.
+    for (int k = 0; k < n; k++)
+        for (int j = 0; j < n; j++) inv[colperm[k] * n + j] = b[k * n + j];
+    return true;
+}
+
+// Dense Cholesky A = L L^T in place (lower), then A^{-1} = L^{-T} L^{-1}; multithreaded over columns.
+int dense_spd_inverse(std::vector<double>& a, int n, std::vector<double>& inv)
+{
+    const unsigned nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    for (int j = 0; j < n; j++) {
+        double d = a[(size_t)j * n + j];
+        for (int k = 0; k < j; k++) d -= a[(size_t)j * n + k] * a[(size_t)j * n + k];
+        if (!(d > 0.0) || !std::isfinite(d)) return 1;
+        const double ljj = std::sqrt(d);
+        a[(size_t)j * n + j] = ljj;
+        auto work = [&](int i0, int i1) {
+            for (int i = i0; i < i1; i++) {
+                double v = a[(size_t)i * n + j];
+                const double* ai = &a[(size_t)i * n];
+                const double* aj = &a[(size_t)j * n];
+                for (int k = 0; k < j; k++) v -= ai[k] * aj[k];
+                a[(size_t)i * n + j] = v / ljj;
+            }
+        };
+        const int rows = n - j - 1;
+        if (rows > 256 && nt > 1) {
+            std::vector<std::thread> th;
+            const int chunk = (rows + nt - 1) / nt;
+            for (unsigned t = 0; t < nt; t++) {
+                const int i0 = j + 1 + t * chunk, i1 = std::min(n, i0 + chunk);
+                if (i0 < i1) th.emplace_back(work, i0, i1);
+            }
+            for (auto& t : th) t.join();
+        } else {
+            work(j + 1, n);
+        }
+    }
+    inv.assign((size_t)n * n, 0.0);
+    auto cols = [&](int c0, int c1) {
+        std::vector<double> y(n);
+        for (int c = c0; c < c1; c++) {
+            for (int i = 0; i < n; i++) {
+                double v = (i == c) ? 1.0 : 0.0;
+                const double* ai = &a[(size_t)i * n];
+                for (int k = c; k < i; k++) v -= ai[k] * y[k];
+                y[i] = i < c ? 0.0 : v / ai[i];
+            }
+            for (int i = n - 1; i >= 0; i--) {
+                double v = y[i];
+                for (int k = i + 1; k < n; k++) v -= a[(size_t)k * n + i] * y[k];
+                y[i] = v / a[(size_t)i * n + i];
+            }
+            for (int i = 0; i < n; i++) inv[(size_t)i * n + c] = y[i];
+        }
+    };
+    if (n > 128 && nt > 1) {
+        std::vector<std::thread> th;
+        const int chunk = (n + nt - 1) / nt;
+        for (unsigned t = 0; t < nt; t++) {
+            const int c0 = t * chunk, c1 = std::min(n, c0 + chunk);
+            if (c0 < c1) th.emplace_back(cols, c0, c1);
+        }
+        for (auto& t : th) t.join();
+    } else {
+        cols(0, n);
+    }
+    return 0;
+}
+
+long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
+
+int default_lanes(const HostBsr& B)
+{
+    const double avg = B.nbr ? (double)B.nnzb() / B.nbr : 1.0;
+    if (avg <= 4.5) return 4;
+    if (avg <= 9.0) return 8;
+    if (avg <= 18.0) return 16;
+    return 32;
+}
+
+template <class T>
+int upload_bsr(fhg_ctx* ctx, const HostBsr& B, DevBsr<T>& D, const DevBsr<double>* share_index)
+{
+    const int bb = B.bs * B.bs;
+    const long long nnzb = B.nnzb();
+    const long long ld = round_up(std::max<long long>(nnzb, 1), 32);
+    std::vector<T> soa((size_t)ld * bb, T(0));
+    for (long long p = 0; p < nnzb; p++)
+        for (int e = 0; e < bb; e++) soa[(size_t)e * ld + p] = (T)B.vals[(size_t)p * bb + e];
+    int rc;
+    if (share_index) {
+        D.rowptr = share_index->rowptr;
+        D.colidx = share_index->colidx;
+        D.owns_index = false;
+    } else {
+        if ((rc = upload(ctx, &D.rowptr, B.rowptr.data(), B.rowptr.size()))) return rc;
+        if ((rc = upload(ctx, &D.colidx, B.colidx.data(), B.colidx.size()))) return rc;
+    }
+    if ((rc = upload(ctx, &D.vals, soa.data(), soa.size()))) return rc;
+    D.v.nbr = B.nbr; D.v.nbc = B.nbc; D.v.bs = B.bs; D.v.nnzb = nnzb; D.v.ld = ld;
+    D.v.rowptr = D.rowptr; D.v.colidx = D.colidx; D.v.vals = D.vals;
+    D.v.lanes = default_lanes(B);
+    return FHG_OK;
+}
+
+bool supported_bs(int bs) { return bs == 2 || bs == 3 || bs == 4 || bs == 6; }
+
+// ---------------------------------------------------------------------------
+// Device operations
+
+template <class T> struct LevelVecs;
+template <> struct LevelVecs<double> {
+    static double* x(Level& L) { return L.x; }
+    static double* b(Level& L) { return L.b; }
+    static double* r(Level& L) { return L.r; }
+    static const BsrView<double>& A(Level& L) { return L.A.v; }
+    static const BsrView<double>& P(Level& L) { return L.P.v; }
+    static const BsrView<double>& R(Level& L) { return L.R.v; }
+    static const double* dinv(Level& L) { return L.dinv; }
+};
+template <> struct LevelVecs<float> {
+    static float* x(Level& L) { return L.x32; }
+    static float* b(Level& L) { return L.b32; }
+    static float* r(Level& L) { return L.r32; }
+    static const BsrView<float>& A(Level& L) { return L.A32.v; }
+    static const BsrView<float>& P(Level& L) { return L.P32.v; }
+    static const BsrView<float>& R(Level& L) { return L.R32.v; }
+    static const float* dinv(Level& L) { return L.dinv32; }
+};
+
+template <class T>
+void smooth(fhg_ctx* ctx, int l, int code, int iters, const T* b, T* x)
+{
+    Level& L = ctx->levels[l];
+    using V = LevelVecs<T>;
+    cudaStream_t s = ctx->stream;
+    for (int it = 0; it < iters; it++) {
+        if (code == FHG_SMOOTHER_BGS) {
+            for (int c = 0; c < L.ncolours; c++)
+                fhg::launch_gs<T>(V::A(L), L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s);
+        } else if (code == FHG_SMOOTHER_RBGS) {
+            for (int c = L.ncolours - 1; c >= 0; c--)
+                fhg::launch_gs<T>(V::A(L), L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s);
+        } else {
+            const T omega = code == FHG_SMOOTHER_BJ23 ? T(2.0 / 3.0) : T(ctx->opts.omega);
+            T* tmp = V::r(L);
+            fhg::launch_jacobi<T>(V::A(L), V::dinv(L), L.nb, omega, b, x, tmp, s);
+            cudaMemcpyAsync(x, tmp, sizeof(T) * (size_t)L.n, cudaMemcpyDeviceToDevice, s);
+        }
+    }
+}
+
+// One V-cycle on level l from x = 0 (src/Solver/Multigrid/Multigrid.h:438-608).
+template <class T>
+void vcycle(fhg_ctx* ctx, int l, const T* b, T* x)
+{
+    Level& L = ctx->levels[l];
+    using V = LevelVecs<T>;
+    cudaStream_t s = ctx->stream;
+    if (l == ctx->nlevels - 1) {
+        fhg::launch_coarse<T>(L.n, L.cinv, b, x, s);
+        return;
+    }
+    Level& C = ctx->levels[l + 1];
+    cudaMemsetAsync(x, 0, sizeof(T) * (size_t)L.n, s);
+    smooth<T>(ctx, l, ctx->opts.pre_smoother, ctx->opts.pre_iterations, b, x);
+    fhg::launch_spmv<T>(V::A(L), fhg::kSpmvResidual, x, b, V::r(L), s);
+    fhg::launch_spmv<T>(V::R(L), fhg::kSpmvAssign, V::r(L), nullptr, V::b(C), s);
+    vcycle<T>(ctx, l + 1, V::b(C), V::x(C));
+    fhg::launch_spmv<T>(V::P(L), fhg::kSpmvAddTo, V::x(C), x, x, s);
+    smooth<T>(ctx, l, ctx->opts.post_smoother, ctx->opts.post_iterations, b, x);
+}
+
+// z = M r in the configured precision (level-0 numbering, FP64 in/out).
+void precondition(fhg_ctx* ctx, const double* r, double* z)
+{
+    Level& L = ctx->levels[0];
+    if (ctx->opts.vcycle_precision == FHG_PREC_FP32) {
+        fhg::launch_convert<double, float>(L.n, r, L.b32, ctx->stream);
+        vcycle<float>(ctx, 0, L.b32, L.x32);
+        fhg::launch_convert<float, double>(L.n, L.x32, z, ctx->stream);
+    } else {
+        vcycle<double>(ctx, 0, r, z);
+    }
+}
+
+double* part(fhg_ctx* ctx, int i) { return ctx->partials + (size_t)i * fhg::kReduceCtas; }
+
+// One FCG(1) iteration (src/Solver/Krylov/FlexibleConjugateGradient.h:80-162), parity p
+// selects the ping-pong buffers (z/d, Ad) of this iteration.
+void fcg_iteration(fhg_ctx* ctx, int p)
+{
+    const long long n = ctx->levels[0].n;
+    cudaStream_t s = ctx->stream;
+    double* z = ctx->kz[p];
+    double* dp = ctx->kz[1 - p];
+    double* Ad = ctx->kAd[p];
+    double* Adp = ctx->kAd[1 - p];
+    precondition(ctx, ctx->kr, z);
+    fhg::launch_dot(n, z, Adp, part(ctx, 0), s);
+    fhg::launch_fcg_direction(n, z, dp, part(ctx, 0), ctx->scal + 1, z, s);
+    const BsrView<double>& Ah = ctx->levels[0].ahat_is_a ? ctx->levels[0].A.v : ctx->levels[0].Ahat.v;
+    fhg::launch_spmv_dots(Ah, z, ctx->kr, Ad, part(ctx, 1), s);
+    // parts 1 = d.Ad, 2 = r.d
+    fhg::launch_krylov_step(n, ctx->kx, ctx->kr, z, Ad, part(ctx, 2), part(ctx, 1), ctx->scal + 1, part(ctx, 3), s);
+    fhg::launch_finalize_norm(part(ctx, 3), ctx->scal + 0, ctx->scal + 2, ctx->hist_d, ctx->counter_d,
+                              ctx->opts.max_iterations + 1, s);
+    cudaMemcpyAsync(ctx->nr_host, ctx->scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s);
+}
+
+// One PCG iteration (src/Solver/Krylov/ConjugateGradient.h:58-96); z, d, Ad = kz[0], kz[1], kAd[0].
+void cg_iteration(fhg_ctx* ctx)
+{
+    const long long n = ctx->levels[0].n;
+    cudaStream_t s = ctx->stream;
+    double* z = ctx->kz[0];
+    double* d = ctx->kz[1];
+    double* Ad = ctx->kAd[0];
+    fhg::launch_cg_direction(n, z, ctx->scal + 4, d, s);
+    fhg::launch_spmv_dots(ctx->levels[0].A.v, d, ctx->kr, Ad, part(ctx, 1), s);
+    fhg::launch_cg_step(n, ctx->kx, ctx->kr, d, Ad, ctx->scal + 3, part(ctx, 1), part(ctx, 3), s);
+    precondition(ctx, ctx->kr, z);
+    fhg::launch_dot(n, ctx->kr, z, part(ctx, 0), s);
+    fhg::launch_cg_beta(part(ctx, 0), ctx->scal + 3, ctx->scal + 4, s);
+    fhg::launch_finalize_norm(part(ctx, 3), ctx->scal + 0, ctx->scal + 2, ctx->hist_d, ctx->counter_d,
+                              ctx->opts.max_iterations + 1, s);
+    cudaMemcpyAsync(ctx->nr_host, ctx->scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s);
+}
+
+int build_graphs(fhg_ctx* ctx)
+{
+    const int ngraphs = ctx->opts.krylov == FHG_KRYLOV_CG ? 1 : 2;
+    for (int g = 0; g < ngraphs; g++) {
+        cudaGraph_t graph = nullptr;
+        const long long before = fhg::g_kernel_launches.load();
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        if (ctx->opts.krylov == FHG_KRYLOV_CG) cg_iteration(ctx);
+        else fcg_iteration(ctx, g);
+        CK(cudaStreamEndCapture(ctx->stream, &graph));
+        const long long after = fhg::g_kernel_launches.load();
+        fhg::g_kernel_launches -= (after - before);  // captured, not executed
+        ctx->graph_kernels[g] = after - before;
+        CK(cudaGraphInstantiate(&ctx->graph[g], graph, 0));
+        CK(cudaGraphDestroy(graph));
+    }
+    ctx->graphs_built = ngraphs;
+    return FHG_OK;
+}
+
+// Lanes-per-block-row autotuning of one operator: time y = A x for G = 4..32, keep the best.
+template <class T>
+int tune_lanes(fhg_ctx* ctx, BsrView<T>& v, const T* x, T* y)
+{
+    if (v.nbr == 0) return FHG_OK;
+    float best = 1e30f;
+    int bestG = v.lanes;
+    for (int G : {4, 8, 16, 32}) {
+        v.lanes = G;
+        for (int w = 0; w < 2; w++) fhg::launch_spmv<T>(v, fhg::kSpmvAssign, x, nullptr, y, ctx->stream);
+        CK(cudaEventRecord(ctx->ev0, ctx->stream));
+        const int reps = 5;
+        for (int r = 0; r < reps; r++) fhg::launch_spmv<T>(v, fhg::kSpmvAssign, x, nullptr, y, ctx->stream);
+        CK(cudaEventRecord(ctx->ev1, ctx->stream));
+        CK(cudaEventSynchronize(ctx->ev1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        if (ms < best) { best = ms; bestG = G; }
+    }
+    v.lanes = bestG;
+    return FHG_OK;
+}
+
+void free_all(fhg_ctx* ctx)
+{
+    for (int g = 0; g < 2; g++)
+        if (ctx->graph[g]) { cudaGraphExecDestroy(ctx->graph[g]); ctx->graph[g] = nullptr; }
+    ctx->graphs_built = 0;
+    for (void* p : ctx->allocations) cudaFree(p);
+    ctx->allocations.clear();
+    if (ctx->nr_host) { cudaFreeHost(ctx->nr_host); ctx->nr_host = nullptr; }
+    ctx->ready = false;
+}
+
+int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
+{
+    Level& L0 = ctx->levels[0];
+    const long long n = L0.n;
+    cudaStream_t s = ctx->stream;
+    const int maxit = ctx->opts.max_iterations;
+    // x = 0, r = b, ||b||, first-iteration placeholders (dp = 0, Adp = 0, d.Ad_prev = 1).
+    CK(cudaMemsetAsync(ctx->kx, 0, sizeof(double) * n, s));
+    CK(cudaMemcpyAsync(ctx->kr, ctx->kb, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    for (int q = 0; q < 2; q++) {
+        CK(cudaMemsetAsync(ctx->kz[q], 0, sizeof(double) * n, s));
+        CK(cudaMemsetAsync(ctx->kAd[q], 0, sizeof(double) * n, s));
+    }
+    fhg::launch_dot(n, ctx->kb, ctx->kb, part(ctx, 0), s);
+    fhg::launch_sqrt_sum(part(ctx, 0), ctx->scal + 0, s);
+    const double init[4] = {1.0, 1.0, 0.0, 0.0};  // dAdp, nr, rz, beta
+    CK(cudaMemcpyAsync(ctx->scal + 1, init, sizeof(init), cudaMemcpyHostToDevice, s));
+    const int one = 1;
+    CK(cudaMemcpyAsync(ctx->counter_d, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+    if (ctx->opts.krylov == FHG_KRYLOV_CG) {
+        // z = M r; d = 0 so that the first direction is z; rz = r.z
+        precondition(ctx, ctx->kr, ctx->kz[0]);
+        fhg::launch_dot(n, ctx->kr, ctx->kz[0], part(ctx, 0), s);
+        fhg::launch_sum(part(ctx, 0), ctx->scal + 3, s);
+    }
+    if (ctx->opts.use_graphs && !ctx->graphs_built) {
+        int rc = build_graphs(ctx);
+        if (rc) return rc;
+    }
+    CK(cudaEventRecord(ctx->ev0, s));
+    std::vector<double> hist(maxit + 1, 0.0);
+    hist[0] = 1.0;
+    double nr = 1.0;
+    int it = 0;
+    int status = FHG_OK;
+    while (!(it > 0 && (it >= maxit || nr < ctx->opts.tolerance))) {
+        const int p = it & 1;
+        if (ctx->opts.use_graphs) {
+            const int g = ctx->opts.krylov == FHG_KRYLOV_CG ? 0 : p;
+            CK(cudaGraphLaunch(ctx->graph[g], s));
+            fhg::g_kernel_launches += ctx->graph_kernels[g];
+        } else if (ctx->opts.krylov == FHG_KRYLOV_CG) {
+            cg_iteration(ctx);
+        } else {
+            fcg_iteration(ctx, p);
+        }
+        CK(cudaStreamSynchronize(s));
+        nr = *ctx->nr_host;
+        it++;
+        hist[it] = nr;
+        if (std::isinf(nr)) { status = fail(ctx, FHG_ERR_DIVERGED, "divergence of the solver"); break; }
+        if (std::isnan(nr)) { status = fail(ctx, FHG_ERR_NAN, "the residual is NaN."); break; }
+    }
+    CK(cudaEventRecord(ctx->ev1, s));
+    CK(cudaEventSynchronize(ctx->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    if (history)
+        for (int k = 0; k <= maxit; k++) history[k] = k <= it ? hist[k] : 0.0;
+    if (info) {
+        info->iterations = it;
+        info->status = status;
+        info->normalized_residual = nr;
+        info->solve_ms = ms;
+    }
+    return status;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+
+extern "C" {
+
+void fhg_default_options(fhg_options* o)
+{
+    std::memset(o, 0, sizeof(*o));
+    o->krylov = FHG_KRYLOV_FCG;
+    o->pre_smoother = FHG_SMOOTHER_BGS;
+    o->post_smoother = FHG_SMOOTHER_RBGS;
+    o->pre_iterations = 1;
+    o->post_iterations = 1;
+    o->omega = 1.0;
+    o->tolerance = 1e-8;
+    o->max_iterations = 200;
+    o->vcycle_precision = FHG_PREC_FP64;
+    o->colouring = 1;
+    o->use_graphs = 1;
+    o->autotune = 0;
+    o->max_coarse_rows = 8192;
+}
+
+int fhg_create(fhg_ctx** out, int device)
+{
+    if (!out) return FHG_ERR_INVALID_ARG;
+    *out = nullptr;
+    fhg_ctx* ctx = new fhg_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+    if (e != cudaSuccess) {
+        ctx->err = std::string("CUDA initialisation failed: ") + cudaGetErrorString(e);
+        *out = ctx;
+        return FHG_ERR_CUDA;
+    }
+    fhg_default_options(&ctx->opts);
+    *out = ctx;
+    return FHG_OK;
+}
+
+void fhg_destroy(fhg_ctx* ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    free_all(ctx);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* fhg_last_error(const fhg_ctx* ctx)
+{
+    return ctx ? ctx->err.c_str() : "null context";
+}
+
+int fhg_set_level(fhg_ctx* ctx, int level, int block_size, int n, const int* rowptr, const int* colidx,
+                  const double* vals)
+{
+    if (!ctx) return FHG_ERR_INVALID_ARG;
+    if (level < 0 || level > 63) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d out of range", level);
+    if (!supported_bs(block_size))
+        return fail(ctx, FHG_ERR_UNSUPPORTED, "block size %d not supported (2, 3, 4, 6)", block_size);
+    if (n <= 0 || n % block_size) return fail(ctx, FHG_ERR_INVALID_ARG, "n=%d is not a positive multiple of %d", n, block_size);
+    if (!rowptr || !colidx || (!vals && rowptr[n] > 0)) return fail(ctx, FHG_ERR_INVALID_ARG, "null CSR array");
+    int rc = check_csr(ctx, "A", n, n, rowptr, colidx);
+    if (rc) return rc;
+    if ((int)ctx->levels.size() <= level) ctx->levels.resize(level + 1);
+    Level& L = ctx->levels[level];
+    L.n = n; L.bs = block_size; L.nb = n / block_size;
+    L.A_in.n_rows = L.A_in.n_cols = n;
+    L.A_in.rowptr.assign(rowptr, rowptr + n + 1);
+    L.A_in.colidx.assign(colidx, colidx + rowptr[n]);
+    L.A_in.vals.assign(vals, vals + rowptr[n]);
+    L.A_in.set = true;
+    ctx->ready = false;
+    return FHG_OK;
+}
+
+int fhg_set_prolongation(fhg_ctx* ctx, int level, int n_fine, int n_coarse, const int* rowptr, const int* colidx,
+                         const double* vals)
+{
+    if (!ctx) return FHG_ERR_INVALID_ARG;
+    if (level < 0 || level > 63) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d out of range", level);
+    if (n_fine <= 0 || n_coarse <= 0) return fail(ctx, FHG_ERR_INVALID_ARG, "bad prolongation shape");
+    if (!rowptr || !colidx || (!vals && rowptr[n_fine] > 0)) return fail(ctx, FHG_ERR_INVALID_ARG, "null CSR array");
+    int rc = check_csr(ctx, "P", n_fine, n_coarse, rowptr, colidx);
+    if (rc) return rc;
+    if ((int)ctx->levels.size() <= level) ctx->levels.resize(level + 1);
+    Level& L = ctx->levels[level];
+    L.P_in.n_rows = n_fine; L.P_in.n_cols = n_coarse;
+    L.P_in.rowptr.assign(rowptr, rowptr + n_fine + 1);
+    L.P_in.colidx.assign(colidx, colidx + rowptr[n_fine]);
+    L.P_in.vals.assign(vals, vals + rowptr[n_fine]);
+    L.P_in.set = true;
+    ctx->ready = false;
+    return FHG_OK;
+}
+
+int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
+{
+    if (!ctx) return FHG_ERR_INVALID_ARG;
+    CK(cudaSetDevice(ctx->device));
+    free_all(ctx);
+    if (opts) ctx->opts = *opts;
+    fhg_options& o = ctx->opts;
+    if (o.max_coarse_rows <= 0) o.max_coarse_rows = 8192;
+    if (o.max_iterations < 0 || o.pre_iterations < 0 || o.post_iterations < 0)
+        return fail(ctx, FHG_ERR_INVALID_ARG, "negative iteration count");
+    if (o.pre_smoother < 0 || o.pre_smoother > 3 || o.post_smoother < 0 || o.post_smoother > 3)
+        return fail(ctx, FHG_ERR_INVALID_ARG, "unknown smoother code");
+    if (nlevels <= 0 || nlevels > (int)ctx->levels.size())
+        return fail(ctx, FHG_ERR_INVALID_ARG, "nlevels=%d but %zu levels were given", nlevels, ctx->levels.size());
+    ctx->nlevels = nlevels;
+    const int bs = ctx->levels[0].bs;
+    for (int l = 0; l < nlevels; l++) {
+        Level& L = ctx->levels[l];
+        if (!L.A_in.set) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d operator not set", l);
+        if (L.bs != bs) return fail(ctx, FHG_ERR_UNSUPPORTED, "level %d block size %d differs from %d", l, L.bs, bs);
+        if (l < nlevels - 1) {
+            if (!L.P_in.set) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d prolongation not set", l);
+            if (L.P_in.n_rows != L.n || L.P_in.n_cols != ctx->levels[l + 1].n)
+                return fail(ctx, FHG_ERR_INVALID_ARG, "level %d prolongation is %dx%d, expected %dx%d", l,
+                            L.P_in.n_rows, L.P_in.n_cols, L.n, ctx->levels[l + 1].n);
+        }
+    }
+    Level& LC = ctx->levels[nlevels - 1];
+    if (LC.n > o.max_coarse_rows)
+        return fail(ctx, FHG_ERR_TOO_LARGE, "coarsest level has %d rows, above the dense direct-solve limit %d", LC.n,
+                    o.max_coarse_rows);
+    const bool fp32 = o.vcycle_precision == FHG_PREC_FP32;
+    int rc;
+
+    // Block structure, colouring and permutation of every level.
+    std::vector<HostBsr> Ab(nlevels);
+    for (int l = 0; l < nlevels; l++) {
+        Level& L = ctx->levels[l];
+        csr_to_bsr(L.A_in, bs, Ab[l]);
+        L.perm.resize(L.nb);
+        std::iota(L.perm.begin(), L.perm.end(), 0);
+        if (l == nlevels - 1) {
+            L.ncolours = 0;
+            L.colour_start.assign(1, 0);
+        } else if (o.colouring) {
+            std::vector<int> colour;
+            L.ncolours = greedy_colouring(Ab[l], colour);
+            L.colour_start.assign(L.ncolours + 1, 0);
+            for (int c : colour) L.colour_start[c + 1]++;
+            for (int c = 0; c < L.ncolours; c++) L.colour_start[c + 1] += L.colour_start[c];
+            std::vector<int> fill(L.colour_start.begin(), L.colour_start.end() - 1);
+            for (int I = 0; I < L.nb; I++) L.perm[fill[colour[I]]++] = I;
+        } else {
+            // Given order, one block row per colour: the sequential sweep of the reference.
+            L.ncolours = L.nb;
+            L.colour_start.resize(L.nb + 1);
+            std::iota(L.colour_start.begin(), L.colour_start.end(), 0);
+        }
+    }
+    std::vector<std::vector<int>> iperm(nlevels);
+    for (int l = 0; l < nlevels; l++) {
+        Level& L = ctx->levels[l];
+        iperm[l].resize(L.nb);
+        for (int I = 0; I < L.nb; I++) iperm[l][L.perm[I]] = I;
+    }
+
+    for (int l = 0; l < nlevels; l++) {
+        Level& L = ctx->levels[l];
+        HostBsr Ap;
+        permute_bsr(Ab[l], L.perm, iperm[l], Ap);
+        Ab[l] = HostBsr();
+        if ((rc = upload_bsr<double>(ctx, Ap, L.A, nullptr))) return rc;
+        if (fp32 && (rc = upload_bsr<float>(ctx, Ap, L.A32, &L.A))) return rc;
+        if ((rc = upload(ctx, &L.perm_d, L.perm.data(), L.perm.size()))) return rc;
+        if (l < nlevels - 1) {
+            // Pre-inverted diagonal blocks (FP64, rounded for the FP32 copy).
+            const int bb = bs * bs;
+            std::vector<double> inv((size_t)L.nb * bb);
+            for (int I = 0; I < L.nb; I++) {
+                int pd = -1;
+                for (int p = Ap.rowptr[I]; p < Ap.rowptr[I + 1]; p++)
+                    if (Ap.colidx[p] == I) { pd = p; break; }
+                if (pd < 0 || !invert_block(&Ap.vals[(size_t)pd * bb], bs, &inv[(size_t)I * bb]))
+                    return fail(ctx, FHG_ERR_SINGULAR_BLOCK, "level %d: diagonal block %d is singular", l, L.perm[I]);
+            }
+            std::vector<double> soa((size_t)L.nb * bb);
+            for (int I = 0; I < L.nb; I++)
+                for (int e = 0; e < bb; e++) soa[(size_t)e * L.nb + I] = inv[(size_t)I * bb + e];
+            if ((rc = upload(ctx, &L.dinv, soa.data(), soa.size()))) return rc;
+            if (fp32) {
+                std::vector<float> s32(soa.begin(), soa.end());
+                if ((rc = upload(ctx, &L.dinv32, s32.data(), s32.size()))) return rc;
+            }
+            // Transfers: P' = Pi_l P Pi_{l+1}^T, R' = P'^T.
+            HostBsr Pb, Pp, Rp;
+            csr_to_bsr(L.P_in, bs, Pb);
+            permute_bsr(Pb, L.perm, iperm[l + 1], Pp);
+            Pb = HostBsr();
+            transpose_bsr(Pp, Rp);
+            L.p_blocks = Pp.nnzb();
+            if ((rc = upload_bsr<double>(ctx, Pp, L.P, nullptr))) return rc;
+            if ((rc = upload_bsr<double>(ctx, Rp, L.R, nullptr))) return rc;
+            if (fp32) {
+                if ((rc = upload_bsr<float>(ctx, Pp, L.P32, &L.P))) return rc;
+                if ((rc = upload_bsr<float>(ctx, Rp, L.R32, &L.R))) return rc;
+            }
+        }
+        if (l == 0) {
+            HostCsr S;
+            symmetrise_lower(L.A_in, S);
+            L.ahat_is_a = csr_equal(S, L.A_in);
+            if (!L.ahat_is_a) {
+                HostBsr Sb, Sp;
+                csr_to_bsr(S, bs, Sb);
+                permute_bsr(Sb, L.perm, iperm[0], Sp);
+                if ((rc = upload_bsr<double>(ctx, Sp, L.Ahat, nullptr))) return rc;
+            }
+        }
+        if (l == nlevels - 1) {
+            std::vector<double> dense((size_t)L.n * L.n, 0.0), inv;
+            for (int i = 0; i < L.n; i++)
+                for (int p = L.A_in.rowptr[i]; p < L.A_in.rowptr[i + 1]; p++)
+                    dense[(size_t)i * L.n + L.A_in.colidx[p]] = L.A_in.vals[p];
+            if (dense_spd_inverse(dense, L.n, inv))
+                return fail(ctx, FHG_ERR_NOT_SPD, "coarsest operator (%d rows) is not symmetric positive definite", L.n);
+            if ((rc = upload(ctx, &L.cinv, inv.data(), inv.size()))) return rc;
+        }
+        // Vectors.
+        if ((rc = dalloc(ctx, &L.x, L.n)) || (rc = dalloc(ctx, &L.b, L.n)) || (rc = dalloc(ctx, &L.r, L.n))) return rc;
+        if (fp32 && ((rc = dalloc(ctx, &L.x32, L.n)) || (rc = dalloc(ctx, &L.b32, L.n)) || (rc = dalloc(ctx, &L.r32, L.n))))
+            return rc;
+    }
+    const long long n0 = ctx->levels[0].n;
+    if ((rc = dalloc(ctx, &ctx->kx, n0)) || (rc = dalloc(ctx, &ctx->kr, n0)) || (rc = dalloc(ctx, &ctx->kb, n0)) ||
+        (rc = dalloc(ctx, &ctx->kz[0], n0)) || (rc = dalloc(ctx, &ctx->kz[1], n0)) ||
+        (rc = dalloc(ctx, &ctx->kAd[0], n0)) || (rc = dalloc(ctx, &ctx->kAd[1], n0)) ||
+        (rc = dalloc(ctx, &ctx->partials, (size_t)8 * fhg::kReduceCtas)) || (rc = dalloc(ctx, &ctx->scal, 8)) ||
+        (rc = dalloc(ctx, &ctx->hist_d, (size_t)o.max_iterations + 2)) || (rc = dalloc(ctx, &ctx->counter_d, 1)) ||
+        (rc = dalloc(ctx, &ctx->io, (size_t)2 * n0)))
+        return rc;
+    CK(cudaMallocHost(&ctx->nr_host, sizeof(double)));
+
+    if (o.autotune) {
+        for (int l = 0; l < nlevels; l++) {
+            Level& L = ctx->levels[l];
+            if ((rc = tune_lanes<double>(ctx, L.A.v, L.x, L.r))) return rc;
+            if (l < nlevels - 1) {
+                Level& C = ctx->levels[l + 1];
+                if ((rc = tune_lanes<double>(ctx, L.P.v, C.x, L.r))) return rc;
+                if ((rc = tune_lanes<double>(ctx, L.R.v, L.x, C.r))) return rc;
+            }
+            if (fp32) {
+                L.A32.v.lanes = L.A.v.lanes;
+                L.P32.v.lanes = L.P.v.lanes;
+                L.R32.v.lanes = L.R.v.lanes;
+            }
+        }
+        Level& L0 = ctx->levels[0];
+        if (!L0.ahat_is_a) L0.Ahat.v.lanes = L0.A.v.lanes;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->ready = true;
+    return FHG_OK;
+}
+
+int fhg_solve_device(fhg_ctx* ctx, const double* b_dev, double* x_dev, double* history, fhg_solve_info* info)
+{
+    if (!ctx) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
+    CK(cudaSetDevice(ctx->device));
+    Level& L0 = ctx->levels[0];
+    // b' = Pi_0 b
+    fhg::launch_permute<double>(L0.nb, L0.bs, L0.perm_d, b_dev, ctx->kb, true, ctx->stream);
+    int rc = run_solve(ctx, history, info);
+    // x = Pi_0^T x'
+    fhg::launch_permute<double>(L0.nb, L0.bs, L0.perm_d, ctx->kx, x_dev, false, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (rc == FHG_OK && e != cudaSuccess) return fail(ctx, FHG_ERR_CUDA, "solve: %s", cudaGetErrorString(e));
+    return rc;
+}
+
+int fhg_solve(fhg_ctx* ctx, const double* b, double* x, double* history, fhg_solve_info* info)
+{
+    if (!ctx) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
+    if (!b || !x) return fail(ctx, FHG_ERR_INVALID_ARG, "null vector");
+    CK(cudaSetDevice(ctx->device));
+    const long long n = ctx->levels[0].n;
+    CK(cudaMemcpyAsync(ctx->io, b, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    int rc = fhg_solve_device(ctx, ctx->io, ctx->io + n, history, info);
+    cudaError_t e = cudaMemcpyAsync(x, ctx->io + n, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (rc == FHG_OK && e != cudaSuccess) return fail(ctx, FHG_ERR_CUDA, "solve copy-out: %s", cudaGetErrorString(e));
+    return rc;
+}
+
+static int apply_device(fhg_ctx* ctx, int level, int op, double* in, double* aux, double* out)
+{
+    // in/aux/out already in the permuted numbering on the device.
+    Level& L = ctx->levels[level];
+    cudaStream_t s = ctx->stream;
+    const bool coarsest = level == ctx->nlevels - 1;
+    switch (op) {
+    case FHG_OP_SPMV: fhg::launch_spmv<double>(L.A.v, fhg::kSpmvAssign, in, nullptr, out, s); break;
+    case FHG_OP_RESIDUAL: fhg::launch_spmv<double>(L.A.v, fhg::kSpmvResidual, in, aux, out, s); break;
+    case FHG_OP_RESTRICT:
+        if (coarsest) return fail(ctx, FHG_ERR_INVALID_ARG, "no restriction on the coarsest level");
+        fhg::launch_spmv<double>(L.R.v, fhg::kSpmvAssign, in, nullptr, out, s);
+        break;
+    case FHG_OP_PROLONG_ADD:
+        if (coarsest) return fail(ctx, FHG_ERR_INVALID_ARG, "no prolongation on the coarsest level");
+        fhg::launch_spmv<double>(L.P.v, fhg::kSpmvAddTo, in, aux, out, s);
+        break;
+    case FHG_OP_GS_FORWARD:
+    case FHG_OP_GS_BACKWARD:
+    case FHG_OP_JACOBI: {
+        if (coarsest) return fail(ctx, FHG_ERR_INVALID_ARG, "no smoother on the coarsest level");
+        CK(cudaMemcpyAsync(out, in, sizeof(double) * L.n, cudaMemcpyDeviceToDevice, s));
+        const int code = op == FHG_OP_GS_FORWARD ? FHG_SMOOTHER_BGS
+                         : op == FHG_OP_GS_BACKWARD ? FHG_SMOOTHER_RBGS
+                                                    : (ctx->opts.pre_smoother == FHG_SMOOTHER_BJ23 ? FHG_SMOOTHER_BJ23 : FHG_SMOOTHER_BJ);
+        smooth<double>(ctx, level, code, 1, aux, out);
+        break;
+    }
+    case FHG_OP_SYM_SPMV: {
+        if (level != 0) return fail(ctx, FHG_ERR_INVALID_ARG, "symmetric operator exists on level 0 only");
+        fhg::launch_spmv_dots(L.ahat_is_a ? L.A.v : L.Ahat.v, in, in, out, part(ctx, 4), s);
+        break;
+    }
+    case FHG_OP_COARSE_SOLVE:
+        if (!coarsest) return fail(ctx, FHG_ERR_INVALID_ARG, "coarse solve on level %d (coarsest is %d)", level, ctx->nlevels - 1);
+        fhg::launch_coarse<double>(L.n, L.cinv, in, out, s);
+        break;
+    case FHG_OP_VCYCLE:
+        if (level != 0) return fail(ctx, FHG_ERR_INVALID_ARG, "V-cycle starts on level 0");
+        precondition(ctx, in, out);
+        break;
+    default: return fail(ctx, FHG_ERR_INVALID_ARG, "unknown op %d", op);
+    }
+    return FHG_OK;
+}
+
+static void op_levels(int level, int op, int* in_level, int* out_level)
+{
+    *in_level = level; *out_level = level;
+    if (op == FHG_OP_RESTRICT) *out_level = level + 1;
+    if (op == FHG_OP_PROLONG_ADD) *in_level = level + 1;
+}
+
+int fhg_apply(fhg_ctx* ctx, int level, int op, const double* in, const double* aux, double* out)
+{
+    if (!ctx) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
+    if (level < 0 || level >= ctx->nlevels) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d out of range", level);
+    CK(cudaSetDevice(ctx->device));
+    int li, lo;
+    op_levels(level, op, &li, &lo);
+    if (lo >= ctx->nlevels || li >= ctx->nlevels) return fail(ctx, FHG_ERR_INVALID_ARG, "operator leaves the hierarchy");
+    Level& Li = ctx->levels[li];
+    Level& Lo = ctx->levels[lo];
+    const bool need_aux = op == FHG_OP_RESIDUAL || op == FHG_OP_PROLONG_ADD || op == FHG_OP_GS_FORWARD ||
+                          op == FHG_OP_GS_BACKWARD || op == FHG_OP_JACOBI;
+    if (!in || !out || (need_aux && !aux)) return fail(ctx, FHG_ERR_INVALID_ARG, "null vector");
+    const int aux_level = op == FHG_OP_PROLONG_ADD ? lo : li;
+    Level& La = ctx->levels[aux_level];
+    const size_t mx = (size_t)std::max(std::max(Li.n, Lo.n), La.n);
+    double *t = nullptr;
+    int rc = dalloc(ctx, &t, 6 * mx);
+    if (rc) return rc;
+    double *din = t, *daux = t + mx, *dout = t + 2 * mx, *pin = t + 3 * mx, *paux = t + 4 * mx, *pout = t + 5 * mx;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(din, in, sizeof(double) * Li.n, cudaMemcpyHostToDevice, s));
+    fhg::launch_permute<double>(Li.nb, Li.bs, Li.perm_d, din, pin, true, s);
+    if (need_aux) {
+        CK(cudaMemcpyAsync(daux, aux, sizeof(double) * La.n, cudaMemcpyHostToDevice, s));
+        fhg::launch_permute<double>(La.nb, La.bs, La.perm_d, daux, paux, true, s);
+    }
+    if (op == FHG_OP_PROLONG_ADD) CK(cudaMemcpyAsync(pout, paux, sizeof(double) * Lo.n, cudaMemcpyDeviceToDevice, s));
+    rc = apply_device(ctx, level, op, pin, paux, op == FHG_OP_PROLONG_ADD ? pout : pout);
+    if (rc == FHG_OK) {
+        fhg::launch_permute<double>(Lo.nb, Lo.bs, Lo.perm_d, pout, dout, false, s);
+        cudaError_t e = cudaMemcpyAsync(out, dout, sizeof(double) * Lo.n, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = fail(ctx, FHG_ERR_CUDA, "apply: %s", cudaGetErrorString(e));
+    }
+    cudaStreamSynchronize(s);
+    ctx->allocations.erase(std::find(ctx->allocations.begin(), ctx->allocations.end(), (void*)t));
+    cudaFree(t);
+    return rc;
+}
+
+int fhg_time_op(fhg_ctx* ctx, int level, int op, int warmup, int reps, double* avg_ms)
+{
+    if (!ctx || !avg_ms || reps <= 0) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
+    if (level < 0 || level >= ctx->nlevels) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d out of range", level);
+    CK(cudaSetDevice(ctx->device));
+    int li, lo;
+    op_levels(level, op, &li, &lo);
+    if (lo >= ctx->nlevels || li >= ctx->nlevels) return fail(ctx, FHG_ERR_INVALID_ARG, "operator leaves the hierarchy");
+    Level& L = ctx->levels[level];
+    const size_t mx = (size_t)std::max(ctx->levels[li].n, ctx->levels[lo].n);
+    double* t = nullptr;
+    int rc = dalloc(ctx, &t, 3 * mx);
+    if (rc) return rc;
+    double *in = t, *aux = t + mx, *out = t + 2 * mx;
+    cudaStream_t s = ctx->stream;
+    // Inputs: the level's last V-cycle vectors (finite, representative values).
+    CK(cudaMemcpyAsync(in, ctx->levels[li].x, sizeof(double) * ctx->levels[li].n, cudaMemcpyDeviceToDevice, s));
+    const int la = op == FHG_OP_PROLONG_ADD ? lo : li;
+    CK(cudaMemcpyAsync(aux, ctx->levels[la].b, sizeof(double) * ctx->levels[la].n, cudaMemcpyDeviceToDevice, s));
+    auto one = [&]() -> int {
+        if (op == FHG_OP_GS_FORWARD || op == FHG_OP_GS_BACKWARD) {
+            if (level == ctx->nlevels - 1) return fail(ctx, FHG_ERR_INVALID_ARG, "no smoother on the coarsest level");
+            smooth<double>(ctx, level, op == FHG_OP_GS_FORWARD ? FHG_SMOOTHER_BGS : FHG_SMOOTHER_RBGS, 1, aux, in);
+            return FHG_OK;
+        }
+        return apply_device(ctx, level, op, in, aux, out);
+    };
+    (void)L;
+    for (int w = 0; w < warmup && rc == FHG_OK; w++) rc = one();
+    if (rc == FHG_OK) {
+        CK(cudaEventRecord(ctx->ev0, s));
+        for (int r = 0; r < reps && rc == FHG_OK; r++) rc = one();
+        CK(cudaEventRecord(ctx->ev1, s));
+        CK(cudaEventSynchronize(ctx->ev1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        *avg_ms = ms / reps;
+    }
+    cudaStreamSynchronize(s);
+    ctx->allocations.erase(std::find(ctx->allocations.begin(), ctx->allocations.end(), (void*)t));
+    cudaFree(t);
+    return rc;
+}
+
+int fhg_level_info(const fhg_ctx* ctx, int level, int* n_block_rows, long long* n_blocks, int* n_colours, int* lanes,
+                   long long* p_blocks)
+{
+    if (!ctx || !ctx->ready || level < 0 || level >= ctx->nlevels) return FHG_ERR_INVALID_ARG;
+    const Level& L = ctx->levels[level];
+    if (n_block_rows) *n_block_rows = L.nb;
+    if (n_blocks) *n_blocks = L.A.v.nnzb;
+    if (n_colours) *n_colours = L.ncolours;
+    if (lanes) *lanes = L.A.v.lanes;
+    if (p_blocks) *p_blocks = L.p_blocks;
+    return FHG_OK;
+}
+
+int fhg_get_permutation(const fhg_ctx* ctx, int level, int* perm)
+{
+    if (!ctx || !ctx->ready || level < 0 || level >= ctx->nlevels || !perm) return FHG_ERR_INVALID_ARG;
+    const Level& L = ctx->levels[level];
+    std::copy(L.perm.begin(), L.perm.end(), perm);
+    return FHG_OK;
+}
+
+long long fhg_kernel_launches(const fhg_ctx* ctx)
+{
+    (void)ctx;
+    return fhg::g_kernel_launches.load();
+}
+
+}  // extern "C"

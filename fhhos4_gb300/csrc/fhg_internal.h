@@ -1,0 +1,87 @@
+// Internal declarations shared by the host side (fhg_api.cu) and the kernels
+// (fhg_kernels.cu) of libfhg.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+
+namespace fhg {
+
+// Device block-sparse-row operator. Block values are stored entry-major
+// ("structure of arrays"): entry e = r*bs + c of stored block p lives at
+// vals[e * ld + p], ld = nnzb rounded up to a multiple of 32, so that the lanes of a
+// warp walking consecutive blocks read consecutive addresses for every entry.
+template <class T>
+struct BsrView {
+    int nbr = 0;          // block rows
+    int nbc = 0;          // block columns
+    int bs = 0;           // block size (square blocks)
+    int lanes = 8;        // lanes per block row (power of two, 4..32)
+    long long nnzb = 0;   // stored blocks
+    long long ld = 0;     // leading dimension of vals
+    const int* rowptr = nullptr;
+    const int* colidx = nullptr;
+    const T* vals = nullptr;
+};
+
+// Fixed number of CTAs of the reduction kernels: the partial-sum arrays they write
+// have exactly this many entries per quantity, and every consumer reduces them in the
+// same fixed order, so the Krylov scalars are bitwise reproducible run to run.
+constexpr int kReduceCtas = 608;   // 4 x 152 SMs
+constexpr int kReduceThreads = 256;
+
+// Process-wide count of kernels launched by this library.
+extern std::atomic<long long> g_kernel_launches;
+
+enum SpmvMode { kSpmvAssign = 0, kSpmvResidual = 1, kSpmvAddTo = 2 };
+
+template <class T>
+void launch_spmv(const BsrView<T>& A, int mode, const T* x, const T* aux, T* y, cudaStream_t s);
+template <class T>
+void launch_gs(const BsrView<T>& A, int row0, int row1, const T* dinv, long long dld,
+               const T* b, T* x, cudaStream_t s);
+template <class T>
+void launch_jacobi(const BsrView<T>& A, const T* dinv, long long dld, T omega, const T* b,
+                   const T* xold, T* xnew, cudaStream_t s);
+// Ad = A d with per-CTA partials of d.Ad (partials[0..kReduceCtas)) and r.d
+// (partials[kReduceCtas..2*kReduceCtas)).
+void launch_spmv_dots(const BsrView<double>& A, const double* d, const double* r, double* Ad,
+                      double* partials, cudaStream_t s);
+// x = Cinv b, Cinv dense n x n row-major FP64; b, x in T.
+template <class T>
+void launch_coarse(int n, const double* cinv, const T* b, T* x, cudaStream_t s);
+// partials[0..kReduceCtas) of sum a_i b_i.
+void launch_dot(long long n, const double* a, const double* b, double* partials, cudaStream_t s);
+// FCG(1) direction: s = sum(partials_zadp) / *dadp; d = z - s * dp (d may alias z).
+void launch_fcg_direction(long long n, const double* z, const double* dp, const double* partials_zadp,
+                          const double* dadp, double* d, cudaStream_t s);
+// FCG/CG step: alpha = num / den with num, den reduced from partials (num_off, den_off offsets);
+// x += alpha d; r -= alpha Ad; partials_rr = per-CTA sum r_i^2; *den_out = den (if not null).
+void launch_krylov_step(long long n, double* x, double* r, const double* d, const double* Ad,
+                        const double* partials_num, const double* partials_den, double* den_out,
+                        double* partials_rr, cudaStream_t s);
+// ||r|| / ||b||: reduces partials_rr, divides by *bnorm, writes *nr_out and hist[*counter],
+// then ++*counter.
+void launch_finalize_norm(const double* partials_rr, const double* bnorm, double* nr_out,
+                          double* hist, int* counter, int hist_len, cudaStream_t s);
+// *out = sqrt(sum partials).
+void launch_sqrt_sum(const double* partials, double* out, cudaStream_t s);
+// *out = sum partials.
+void launch_sum(const double* partials, double* out, cudaStream_t s);
+// CG direction: d = z + (*beta) d.
+void launch_cg_direction(long long n, const double* z, const double* beta, double* d, cudaStream_t s);
+// CG: rz_new = sum(partials); *beta = rz_new / *rz; *rz = rz_new.
+void launch_cg_beta(const double* partials, double* rz, double* beta, cudaStream_t s);
+// CG step numerator from a device scalar: alpha = *num / sum(partials_den).
+void launch_cg_step(long long n, double* x, double* r, const double* d, const double* Ad,
+                    const double* num, const double* partials_den, double* partials_rr, cudaStream_t s);
+
+template <class Tin, class Tout>
+void launch_convert(long long n, const Tin* in, Tout* out, cudaStream_t s);
+// gather: out[b*bs+c] = in[perm[b]*bs+c]; scatter: out[perm[b]*bs+c] = in[b*bs+c].
+template <class T>
+void launch_permute(int nb, int bs, const int* perm, const T* in, T* out, bool gather, cudaStream_t s);
+
+}  // namespace fhg

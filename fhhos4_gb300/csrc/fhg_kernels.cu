@@ -1,0 +1,584 @@
+// CUDA kernels of the fhhos4 solve phase for GB300 (sm_103a).
+//
+// Every kernel is memory-bound: block-sparse products over face-block operators
+// (bs = face DOFs: 2/3/4/6), colour sweeps of block Gauss-Seidel, and the FCG vector
+// updates. The design targets HBM bandwidth:
+//   * block values entry-major (vals[e*ld + p]) so a warp reading consecutive blocks
+//     issues fully coalesced 8-byte (FP64) or 4-byte (FP32) loads per entry;
+//   * a group of G lanes (G = 4..32, chosen per operator) per block row, partial sums
+//     reduced with warp shuffles;
+//   * reductions write fixed-size per-CTA partial arrays that every consumer reduces
+//     in the same order (bitwise reproducible Krylov scalars, no atomics);
+//   * Krylov scalars never leave the device: consumers read them from device memory,
+//     so one whole iteration can be replayed as a CUDA graph.
+#include "fhg_internal.h"
+
+#include <cmath>
+
+namespace fhg {
+
+std::atomic<long long> g_kernel_launches{0};
+
+namespace {
+
+constexpr int kThreads = 256;
+
+template <int G, class T>
+__device__ __forceinline__ T group_sum(T v)
+{
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
+    return v;
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum over the CTA; result valid in every thread. `sh` holds >= 33 doubles.
+__device__ __forceinline__ double block_sum(double v, double* sh)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        double t = lane < nw ? sh[lane] : 0.0;
+        t = warp_sum(t);
+        if (lane == 0) sh[32] = t;
+    }
+    __syncthreads();
+    return sh[32];
+}
+
+// Fixed-order reduction of a kReduceCtas-long partial array by one CTA.
+__device__ __forceinline__ double reduce_partials(const double* __restrict__ p, double* sh)
+{
+    double v = 0.0;
+    for (int i = threadIdx.x; i < kReduceCtas; i += blockDim.x) v += p[i];
+    return block_sum(v, sh);
+}
+
+// ---------------------------------------------------------------------------
+// y = A x  |  y = aux - A x  |  y = aux + A x      (aux may alias y)
+template <class T, int BS, int G, int MODE>
+__global__ void __launch_bounds__(kThreads) k_bsr_spmv(int nbr, const int* __restrict__ rowptr,
+                                                       const int* __restrict__ colidx,
+                                                       const T* __restrict__ vals, long long ld,
+                                                       const T* __restrict__ x, const T* aux, T* y)
+{
+    const int lane = threadIdx.x & (G - 1);
+    const int row = (int)(((long long)blockIdx.x * kThreads + threadIdx.x) / G);
+    T acc[BS];
+#pragma unroll
+    for (int r = 0; r < BS; r++) acc[r] = T(0);
+    if (row < nbr) {
+        const int p1 = rowptr[row + 1];
+        for (int p = rowptr[row] + lane; p < p1; p += G) {
+            const int col = colidx[p];
+            T xv[BS];
+#pragma unroll
+            for (int c = 0; c < BS; c++) xv[c] = x[(long long)col * BS + c];
+#pragma unroll
+            for (int r = 0; r < BS; r++)
+#pragma unroll
+                for (int c = 0; c < BS; c++) acc[r] = fma(vals[(long long)(r * BS + c) * ld + p], xv[c], acc[r]);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < BS; r++) acc[r] = group_sum<G>(acc[r]);
+    if (row < nbr) {
+#pragma unroll
+        for (int r = 0; r < BS; r++) {
+            if (lane == r % G) {
+                const long long i = (long long)row * BS + r;
+                if (MODE == kSpmvAssign) y[i] = acc[r];
+                else if (MODE == kSpmvResidual) y[i] = aux[i] - acc[r];
+                else y[i] = aux[i] + acc[r];
+            }
+        }
+    }
+}
+
+// One colour of block Gauss-Seidel: rows [row0, row1) are mutually uncoupled.
+// x_i <- D_i^{-1} (b_i - sum_{j != i} A_ij x_j)
+template <class T, int BS, int G>
+__global__ void __launch_bounds__(kThreads) k_bsr_gs(int row0, int row1, const int* __restrict__ rowptr,
+                                                     const int* __restrict__ colidx,
+                                                     const T* __restrict__ vals, long long ld,
+                                                     const T* __restrict__ dinv, long long dld,
+                                                     const T* __restrict__ b, T* x)
+{
+    const int lane = threadIdx.x & (G - 1);
+    const int row = row0 + (int)(((long long)blockIdx.x * kThreads + threadIdx.x) / G);
+    T acc[BS];
+#pragma unroll
+    for (int r = 0; r < BS; r++) acc[r] = T(0);
+    if (row < row1) {
+        const int p1 = rowptr[row + 1];
+        for (int p = rowptr[row] + lane; p < p1; p += G) {
+            const int col = colidx[p];
+            if (col == row) continue;
+            T xv[BS];
+#pragma unroll
+            for (int c = 0; c < BS; c++) xv[c] = x[(long long)col * BS + c];
+#pragma unroll
+            for (int r = 0; r < BS; r++)
+#pragma unroll
+                for (int c = 0; c < BS; c++) acc[r] = fma(vals[(long long)(r * BS + c) * ld + p], xv[c], acc[r]);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < BS; r++) acc[r] = group_sum<G>(acc[r]);
+    if (row < row1) {
+        T t[BS];
+#pragma unroll
+        for (int c = 0; c < BS; c++) t[c] = b[(long long)row * BS + c] - acc[c];
+#pragma unroll
+        for (int r = 0; r < BS; r++) {
+            if (lane == r % G) {
+                T v = T(0);
+#pragma unroll
+                for (int c = 0; c < BS; c++) v = fma(dinv[(long long)(r * BS + c) * dld + row], t[c], v);
+                x[(long long)row * BS + r] = v;
+            }
+        }
+    }
+}
+
+// Block Jacobi: xnew_i = D_i^{-1} (omega b_i + (1-omega) D_i xold_i - omega sum_{j!=i} A_ij xold_j)
+template <class T, int BS, int G>
+__global__ void __launch_bounds__(kThreads) k_bsr_jacobi(int nbr, const int* __restrict__ rowptr,
+                                                         const int* __restrict__ colidx,
+                                                         const T* __restrict__ vals, long long ld,
+                                                         const T* __restrict__ dinv, long long dld, T omega,
+                                                         const T* __restrict__ b, const T* __restrict__ xold,
+                                                         T* __restrict__ xnew)
+{
+    const int lane = threadIdx.x & (G - 1);
+    const int row = (int)(((long long)blockIdx.x * kThreads + threadIdx.x) / G);
+    T off[BS], dia[BS];
+#pragma unroll
+    for (int r = 0; r < BS; r++) { off[r] = T(0); dia[r] = T(0); }
+    if (row < nbr) {
+        const int p1 = rowptr[row + 1];
+        for (int p = rowptr[row] + lane; p < p1; p += G) {
+            const int col = colidx[p];
+            T xv[BS];
+#pragma unroll
+            for (int c = 0; c < BS; c++) xv[c] = xold[(long long)col * BS + c];
+            if (col == row) {
+#pragma unroll
+                for (int r = 0; r < BS; r++)
+#pragma unroll
+                    for (int c = 0; c < BS; c++) dia[r] = fma(vals[(long long)(r * BS + c) * ld + p], xv[c], dia[r]);
+            } else {
+#pragma unroll
+                for (int r = 0; r < BS; r++)
+#pragma unroll
+                    for (int c = 0; c < BS; c++) off[r] = fma(vals[(long long)(r * BS + c) * ld + p], xv[c], off[r]);
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < BS; r++) { off[r] = group_sum<G>(off[r]); dia[r] = group_sum<G>(dia[r]); }
+    if (row < nbr) {
+        T t[BS];
+#pragma unroll
+        for (int c = 0; c < BS; c++)
+            t[c] = omega * b[(long long)row * BS + c] + (T(1) - omega) * dia[c] - omega * off[c];
+#pragma unroll
+        for (int r = 0; r < BS; r++) {
+            if (lane == r % G) {
+                T v = T(0);
+#pragma unroll
+                for (int c = 0; c < BS; c++) v = fma(dinv[(long long)(r * BS + c) * dld + row], t[c], v);
+                xnew[(long long)row * BS + r] = v;
+            }
+        }
+    }
+}
+
+// Ad = A d, with per-CTA partials of d.Ad and r.d (fixed grid, grid-stride over block rows).
+template <int BS, int G>
+__global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots(int nbr, const int* __restrict__ rowptr,
+                                                                  const int* __restrict__ colidx,
+                                                                  const double* __restrict__ vals, long long ld,
+                                                                  const double* __restrict__ d,
+                                                                  const double* __restrict__ rvec,
+                                                                  double* __restrict__ Ad,
+                                                                  double* __restrict__ partials)
+{
+    __shared__ double sh[33];
+    const int lane = threadIdx.x & (G - 1);
+    // Loop bounds are uniform per warp (every lane runs the same shuffle rounds).
+    constexpr int kGroupsPerWarp = 32 / G;
+    const long long warp_id = ((long long)blockIdx.x * kReduceThreads + threadIdx.x) >> 5;
+    const long long warp_stride = (long long)kReduceCtas * kReduceThreads / 32 * kGroupsPerWarp;
+    const int group_in_warp = (threadIdx.x & 31) / G;
+    double dad = 0.0, rd = 0.0;
+    for (long long row0 = warp_id * kGroupsPerWarp; row0 < nbr; row0 += warp_stride) {
+        const int row = (int)(row0 + group_in_warp);
+        double acc[BS];
+#pragma unroll
+        for (int r = 0; r < BS; r++) acc[r] = 0.0;
+        const bool active = row < nbr;
+        if (active) {
+            const int p1 = rowptr[row + 1];
+            for (int p = rowptr[row] + lane; p < p1; p += G) {
+                const int col = colidx[p];
+                double xv[BS];
+#pragma unroll
+                for (int c = 0; c < BS; c++) xv[c] = d[(long long)col * BS + c];
+#pragma unroll
+                for (int r = 0; r < BS; r++)
+#pragma unroll
+                    for (int c = 0; c < BS; c++) acc[r] = fma(vals[(long long)(r * BS + c) * ld + p], xv[c], acc[r]);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < BS; r++) acc[r] = group_sum<G>(acc[r]);
+        if (active) {
+#pragma unroll
+            for (int r = 0; r < BS; r++) {
+                if (lane == r % G) {
+                    const long long i = (long long)row * BS + r;
+                    Ad[i] = acc[r];
+                    const double di = d[i];
+                    dad = fma(di, acc[r], dad);
+                    rd = fma(rvec[i], di, rd);
+                }
+            }
+        }
+    }
+    const double s1 = block_sum(dad, sh);
+    const double s2 = block_sum(rd, sh);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = s1;
+        partials[kReduceCtas + blockIdx.x] = s2;
+    }
+}
+
+// x = Cinv b, one warp per row, FP64 accumulation.
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_coarse(int n, const double* __restrict__ cinv,
+                                                     const T* __restrict__ b, T* __restrict__ x)
+{
+    const int lane = threadIdx.x & 31;
+    const int row = (blockIdx.x * kThreads + threadIdx.x) >> 5;
+    if (row >= n) return;  // whole warps exit together
+    const double* a = cinv + (long long)row * n;
+    double acc = 0.0;
+    for (int j = lane; j < n; j += 32) acc = fma(a[j], (double)b[j], acc);
+    acc = warp_sum(acc);
+    if (lane == 0) x[row] = (T)acc;
+}
+
+__global__ void __launch_bounds__(kReduceThreads) k_dot(long long n, const double* __restrict__ a,
+                                                        const double* __restrict__ b, double* __restrict__ partials)
+{
+    __shared__ double sh[33];
+    double v = 0.0;
+    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads)
+        v = fma(a[i], b[i], v);
+    v = block_sum(v, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v;
+}
+
+__global__ void __launch_bounds__(kReduceThreads) k_fcg_direction(long long n, const double* z, const double* __restrict__ dp,
+                                                                  const double* __restrict__ partials,
+                                                                  const double* __restrict__ dadp, double* d)
+{
+    __shared__ double sh[33];
+    const double s = reduce_partials(partials, sh) / *dadp;
+    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads)
+        d[i] = z[i] - s * dp[i];
+}
+
+__global__ void __launch_bounds__(kReduceThreads) k_krylov_step(long long n, double* __restrict__ x, double* __restrict__ r,
+                                                                const double* __restrict__ d, const double* __restrict__ Ad,
+                                                                const double* __restrict__ pnum, const double* __restrict__ pden,
+                                                                double* __restrict__ den_out, double* __restrict__ prr)
+{
+    __shared__ double sh[33];
+    const double num = reduce_partials(pnum, sh);
+    const double den = reduce_partials(pden, sh);
+    const double alpha = num / den;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && den_out) *den_out = den;
+    double rr = 0.0;
+    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads) {
+        x[i] = x[i] + alpha * d[i];
+        const double ri = r[i] - alpha * Ad[i];
+        r[i] = ri;
+        rr = fma(ri, ri, rr);
+    }
+    rr = block_sum(rr, sh);
+    if (threadIdx.x == 0) prr[blockIdx.x] = rr;
+}
+
+__global__ void __launch_bounds__(kReduceThreads) k_cg_step(long long n, double* __restrict__ x, double* __restrict__ r,
+                                                            const double* __restrict__ d, const double* __restrict__ Ad,
+                                                            const double* __restrict__ num, const double* __restrict__ pden,
+                                                            double* __restrict__ prr)
+{
+    __shared__ double sh[33];
+    const double den = reduce_partials(pden, sh);
+    const double alpha = *num / den;
+    double rr = 0.0;
+    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads) {
+        x[i] = x[i] + alpha * d[i];
+        const double ri = r[i] - alpha * Ad[i];
+        r[i] = ri;
+        rr = fma(ri, ri, rr);
+    }
+    rr = block_sum(rr, sh);
+    if (threadIdx.x == 0) prr[blockIdx.x] = rr;
+}
+
+__global__ void __launch_bounds__(kReduceThreads) k_cg_direction(long long n, const double* __restrict__ z,
+                                                                 const double* __restrict__ beta, double* __restrict__ d)
+{
+    const double bt = *beta;
+    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads)
+        d[i] = z[i] + bt * d[i];
+}
+
+__global__ void __launch_bounds__(kReduceThreads) k_finalize_norm(const double* __restrict__ prr, const double* __restrict__ bnorm,
+                                                                  double* nr_out, double* hist, int* counter, int hist_len)
+{
+    __shared__ double sh[33];
+    const double rn = sqrt(reduce_partials(prr, sh));
+    if (threadIdx.x == 0) {
+        const double bn = *bnorm;
+        const double nr = bn > 0.0 ? rn / bn : rn;
+        *nr_out = nr;
+        const int k = *counter;
+        if (k < hist_len) hist[k] = nr;
+        *counter = k + 1;
+    }
+}
+
+__global__ void __launch_bounds__(kReduceThreads) k_sqrt_sum(const double* __restrict__ p, double* out)
+{
+    __shared__ double sh[33];
+    const double v = reduce_partials(p, sh);
+    if (threadIdx.x == 0) *out = sqrt(v);
+}
+
+__global__ void __launch_bounds__(kReduceThreads) k_sum(const double* __restrict__ p, double* out)
+{
+    __shared__ double sh[33];
+    const double v = reduce_partials(p, sh);
+    if (threadIdx.x == 0) *out = v;
+}
+
+__global__ void __launch_bounds__(kReduceThreads) k_cg_beta(const double* __restrict__ p, double* rz, double* beta)
+{
+    __shared__ double sh[33];
+    const double v = reduce_partials(p, sh);
+    if (threadIdx.x == 0) {
+        *beta = v / *rz;
+        *rz = v;
+    }
+}
+
+template <class Tin, class Tout>
+__global__ void __launch_bounds__(kThreads) k_convert(long long n, const Tin* __restrict__ in, Tout* __restrict__ out)
+{
+    const long long i = (long long)blockIdx.x * kThreads + threadIdx.x;
+    if (i < n) out[i] = (Tout)in[i];
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_permute(int nb, int bs, const int* __restrict__ perm,
+                                                      const T* __restrict__ in, T* __restrict__ out, int gather)
+{
+    const long long i = (long long)blockIdx.x * kThreads + threadIdx.x;
+    if (i >= (long long)nb * bs) return;
+    const int blk = (int)(i / bs), c = (int)(i - (long long)blk * bs);
+    const long long o = (long long)perm[blk] * bs + c;
+    if (gather) out[i] = in[o];
+    else out[o] = in[i];
+}
+
+inline unsigned grid_for(long long work, int per_cta)
+{
+    long long g = (work + per_cta - 1) / per_cta;
+    return (unsigned)(g > 0 ? g : 1);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Dispatch on (block size, lanes per block row).
+#define FHG_DISPATCH_BS_G(BSV, GV, ...)                                              \
+    switch (BSV) {                                                                    \
+    case 2: FHG_DISPATCH_G(2, GV, __VA_ARGS__); break;                                       \
+    case 3: FHG_DISPATCH_G(3, GV, __VA_ARGS__); break;                                       \
+    case 4: FHG_DISPATCH_G(4, GV, __VA_ARGS__); break;                                       \
+    case 6: FHG_DISPATCH_G(6, GV, __VA_ARGS__); break;                                       \
+    default: break;                                                                   \
+    }
+#define FHG_DISPATCH_G(BS_, GV, ...)                                                 \
+    switch (GV) {                                                                     \
+    case 4: { constexpr int BS = BS_, G = 4; __VA_ARGS__; } break;                          \
+    case 8: { constexpr int BS = BS_, G = 8; __VA_ARGS__; } break;                          \
+    case 16: { constexpr int BS = BS_, G = 16; __VA_ARGS__; } break;                        \
+    default: { constexpr int BS = BS_, G = 32; __VA_ARGS__; } break;                        \
+    }
+
+template <class T>
+void launch_spmv(const BsrView<T>& A, int mode, const T* x, const T* aux, T* y, cudaStream_t s)
+{
+    if (A.nbr == 0) return;
+    const unsigned grid = grid_for((long long)A.nbr * A.lanes, kThreads);
+    FHG_DISPATCH_BS_G(A.bs, A.lanes, {
+        if (mode == kSpmvAssign)
+            k_bsr_spmv<T, BS, G, kSpmvAssign><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
+        else if (mode == kSpmvResidual)
+            k_bsr_spmv<T, BS, G, kSpmvResidual><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
+        else
+            k_bsr_spmv<T, BS, G, kSpmvAddTo><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
+    });
+    g_kernel_launches++;
+}
+
+template <class T>
+void launch_gs(const BsrView<T>& A, int row0, int row1, const T* dinv, long long dld, const T* b, T* x, cudaStream_t s)
+{
+    if (row1 <= row0) return;
+    const unsigned grid = grid_for((long long)(row1 - row0) * A.lanes, kThreads);
+    FHG_DISPATCH_BS_G(A.bs, A.lanes, {
+        k_bsr_gs<T, BS, G><<<grid, kThreads, 0, s>>>(row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, b, x);
+    });
+    g_kernel_launches++;
+}
+
+template <class T>
+void launch_jacobi(const BsrView<T>& A, const T* dinv, long long dld, T omega, const T* b, const T* xold, T* xnew,
+                   cudaStream_t s)
+{
+    if (A.nbr == 0) return;
+    const unsigned grid = grid_for((long long)A.nbr * A.lanes, kThreads);
+    FHG_DISPATCH_BS_G(A.bs, A.lanes, {
+        k_bsr_jacobi<T, BS, G><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, omega, b,
+                                                         xold, xnew);
+    });
+    g_kernel_launches++;
+}
+
+void launch_spmv_dots(const BsrView<double>& A, const double* d, const double* r, double* Ad, double* partials,
+                      cudaStream_t s)
+{
+    FHG_DISPATCH_BS_G(A.bs, A.lanes, {
+        k_bsr_spmv_dots<BS, G><<<kReduceCtas, kReduceThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, d, r,
+                                                                      Ad, partials);
+    });
+    g_kernel_launches++;
+}
+
+template <class T>
+void launch_coarse(int n, const double* cinv, const T* b, T* x, cudaStream_t s)
+{
+    k_coarse<T><<<grid_for((long long)n * 32, kThreads), kThreads, 0, s>>>(n, cinv, b, x);
+    g_kernel_launches++;
+}
+
+void launch_dot(long long n, const double* a, const double* b, double* partials, cudaStream_t s)
+{
+    k_dot<<<kReduceCtas, kReduceThreads, 0, s>>>(n, a, b, partials);
+    g_kernel_launches++;
+}
+
+void launch_fcg_direction(long long n, const double* z, const double* dp, const double* partials_zadp,
+                          const double* dadp, double* d, cudaStream_t s)
+{
+    k_fcg_direction<<<kReduceCtas, kReduceThreads, 0, s>>>(n, z, dp, partials_zadp, dadp, d);
+    g_kernel_launches++;
+}
+
+void launch_krylov_step(long long n, double* x, double* r, const double* d, const double* Ad,
+                        const double* partials_num, const double* partials_den, double* den_out,
+                        double* partials_rr, cudaStream_t s)
+{
+    k_krylov_step<<<kReduceCtas, kReduceThreads, 0, s>>>(n, x, r, d, Ad, partials_num, partials_den, den_out,
+                                                         partials_rr);
+    g_kernel_launches++;
+}
+
+void launch_cg_step(long long n, double* x, double* r, const double* d, const double* Ad, const double* num,
+                    const double* partials_den, double* partials_rr, cudaStream_t s)
+{
+    k_cg_step<<<kReduceCtas, kReduceThreads, 0, s>>>(n, x, r, d, Ad, num, partials_den, partials_rr);
+    g_kernel_launches++;
+}
+
+void launch_cg_direction(long long n, const double* z, const double* beta, double* d, cudaStream_t s)
+{
+    k_cg_direction<<<kReduceCtas, kReduceThreads, 0, s>>>(n, z, beta, d);
+    g_kernel_launches++;
+}
+
+void launch_cg_beta(const double* partials, double* rz, double* beta, cudaStream_t s)
+{
+    k_cg_beta<<<1, kReduceThreads, 0, s>>>(partials, rz, beta);
+    g_kernel_launches++;
+}
+
+void launch_finalize_norm(const double* partials_rr, const double* bnorm, double* nr_out, double* hist, int* counter,
+                          int hist_len, cudaStream_t s)
+{
+    k_finalize_norm<<<1, kReduceThreads, 0, s>>>(partials_rr, bnorm, nr_out, hist, counter, hist_len);
+    g_kernel_launches++;
+}
+
+void launch_sqrt_sum(const double* partials, double* out, cudaStream_t s)
+{
+    k_sqrt_sum<<<1, kReduceThreads, 0, s>>>(partials, out);
+    g_kernel_launches++;
+}
+
+void launch_sum(const double* partials, double* out, cudaStream_t s)
+{
+    k_sum<<<1, kReduceThreads, 0, s>>>(partials, out);
+    g_kernel_launches++;
+}
+
+template <class Tin, class Tout>
+void launch_convert(long long n, const Tin* in, Tout* out, cudaStream_t s)
+{
+    if (n == 0) return;
+    k_convert<Tin, Tout><<<grid_for(n, kThreads), kThreads, 0, s>>>(n, in, out);
+    g_kernel_launches++;
+}
+
+template <class T>
+void launch_permute(int nb, int bs, const int* perm, const T* in, T* out, bool gather, cudaStream_t s)
+{
+    if (nb == 0) return;
+    k_permute<T><<<grid_for((long long)nb * bs, kThreads), kThreads, 0, s>>>(nb, bs, perm, in, out, gather ? 1 : 0);
+    g_kernel_launches++;
+}
+
+template void launch_spmv<double>(const BsrView<double>&, int, const double*, const double*, double*, cudaStream_t);
+template void launch_spmv<float>(const BsrView<float>&, int, const float*, const float*, float*, cudaStream_t);
+template void launch_gs<double>(const BsrView<double>&, int, int, const double*, long long, const double*, double*,
+                                cudaStream_t);
+template void launch_gs<float>(const BsrView<float>&, int, int, const float*, long long, const float*, float*,
+                               cudaStream_t);
+template void launch_jacobi<double>(const BsrView<double>&, const double*, long long, double, const double*,
+                                    const double*, double*, cudaStream_t);
+template void launch_jacobi<float>(const BsrView<float>&, const float*, long long, float, const float*, const float*,
+                                   float*, cudaStream_t);
+template void launch_coarse<double>(int, const double*, const double*, double*, cudaStream_t);
+template void launch_coarse<float>(int, const double*, const float*, float*, cudaStream_t);
+template void launch_convert<double, float>(long long, const double*, float*, cudaStream_t);
+template void launch_convert<float, double>(long long, const float*, double*, cudaStream_t);
+template void launch_permute<double>(int, int, const int*, const double*, double*, bool, cudaStream_t);
+template void launch_permute<float>(int, int, const int*, const float*, float*, bool, cudaStream_t);
+
+}  // namespace fhg

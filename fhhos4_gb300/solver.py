@@ -1,0 +1,234 @@
+"""Python mirror of the reference's solver interface for the solve phase.
+
+Names, attributes and defaults follow fhhos4's C++ classes so that code written
+against them reads the same:
+
+* ``IterativeSolver`` (src/Solver/IterativeSolver.h:6-191): ``Tolerance``,
+  ``MaxIterations``, ``IterationCount``, ``OnIterationEnd``, ``Setup(A)``,
+  ``Solve(b, initialGuessCode="0")``.
+* ``Multigrid`` (src/Solver/Multigrid/Multigrid.h:7-46): cycle and smoother fields; its
+  levels are the operators and prolongations that ``LevelForHHO`` builds
+  (src/Solver/Multigrid/MultigridForHHO/LevelForHHO.h:72-213), given here with
+  ``SetHierarchy``.
+* ``SolverPreconditioner`` (src/Solver/Preconditioner.h:100-118): one V-cycle per
+  application.
+* ``FlexibleConjugateGradient(truncation=1)`` (src/Solver/Krylov/FlexibleConjugateGradient.h)
+  and ``ConjugateGradient`` (src/Solver/Krylov/ConjugateGradient.h).
+
+Everything runs in libfhg on the GPU; there is no CPU path. The reference reports
+errors with ``Utils::FatalError`` (print + exit); here the same conditions raise
+:class:`fhhos4_gb300._native.FhgError` with the reference's message.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Callable, List, Optional
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _native as N
+
+
+def as_eigen_csr(A) -> sp.csr_matrix:
+    """Row-major CSR with int32 indices, sorted and duplicate-free (Eigen compressed form)."""
+    A = sp.csr_matrix(A)
+    A.sum_duplicates()
+    A.sort_indices()
+    return sp.csr_matrix((A.data.astype(np.float64), A.indices.astype(np.int32), A.indptr.astype(np.int32)),
+                         shape=A.shape)
+
+
+@dataclass
+class IterationResult:
+    """The fields of IterationResult (src/Solver/IterationResult.h:23-33) the solve phase fills."""
+    IterationNumber: int = 0
+    NormalizedResidualNorm: float = -1.0
+    PreviousNormalizedResidualNorm: float = -1.0
+    IterationConvRate: float = 0.0
+    AsymptoticConvRate: float = 0.0
+
+
+class IterativeSolver:
+    def __init__(self):
+        self.Tolerance = 1e-3
+        self.MaxIterations = 200
+        self.IterationCount = 0
+        self.PrintIterationResults = False
+        self.OnIterationEnd: Optional[Callable[[IterationResult], None]] = None
+        self.LastIterationResult = IterationResult()
+        self.Matrix = None
+        self.SolveTimeMs = 0.0
+        self.History = np.zeros(0)
+
+    def Setup(self, A):
+        self.Matrix = as_eigen_csr(A)
+
+
+class Multigrid(IterativeSolver):
+    """Geometric multigrid (V-cycle) over a given hierarchy, executed by libfhg."""
+
+    def __init__(self, nLevels: int = 0):
+        super().__init__()
+        self.Cycle = "V"
+        self.WLoops = 1
+        self.PreSmootherCode = "bgs"
+        self.PostSmootherCode = "rbgs"
+        self.PreSmoothingIterations = 1
+        self.PostSmoothingIterations = 1
+        self.RelaxationParameter = 1.0
+        self.BlockSizeForBlockSmoothers = -1
+        self.MatrixMaxSizeForCoarsestLevel = 1000
+        # GB300 knobs
+        self.VCyclePrecision = "fp64"
+        self.Colouring = True
+        self.Autotune = False
+        self.MaxCoarseRows = 8192
+        self._As: List[sp.csr_matrix] = []
+        self._Ps: List[sp.csr_matrix] = []
+        self._nLevels = nLevels
+
+    def SetHierarchy(self, As, Ps):
+        """A_0..A_{L-1} and P_0..P_{L-2} (P_l: level l rows, level l+1 columns), as built on the host."""
+        if len(Ps) != len(As) - 1:
+            raise ValueError("need one prolongation per level except the coarsest")
+        self._As = [as_eigen_csr(A) for A in As]
+        self._Ps = [as_eigen_csr(P) for P in Ps]
+        self._nLevels = len(As)
+
+    def NumberOfLevels(self) -> int:
+        return self._nLevels
+
+    def _check_supported(self):
+        if self.Cycle != "V" or self.WLoops != 1:
+            raise NotImplementedError("only the V-cycle (Cycle='V', WLoops=1) runs on the GPU")
+        for code in (self.PreSmootherCode, self.PostSmootherCode):
+            if code not in N.SMOOTHERS:
+                raise NotImplementedError(f"smoother '{code}' (GPU smoothers: {sorted(N.SMOOTHERS)})")
+        if self.VCyclePrecision not in N.PRECISION:
+            raise ValueError(f"unknown precision {self.VCyclePrecision}")
+
+
+class SolverPreconditioner:
+    """One application = one V-cycle from zero (Preconditioner.h:107-118,162-167)."""
+
+    def __init__(self, solver: Optional[Multigrid] = None):
+        self._solver = solver
+        if solver is not None:
+            solver.MaxIterations = 1
+
+
+class _KrylovOnGpu(IterativeSolver):
+    _krylov = "fcg"
+
+    def __init__(self):
+        super().__init__()
+        self.Precond = SolverPreconditioner()
+        self.Device = 0
+        self.UseGraphs = True
+        self._ctx: Optional[N.Context] = None
+
+    def _options(self, mg: Multigrid) -> N.Options:
+        o = N.default_options()
+        o.krylov = N.KRYLOV[self._krylov]
+        o.pre_smoother = N.SMOOTHERS[mg.PreSmootherCode]
+        o.post_smoother = N.SMOOTHERS[mg.PostSmootherCode]
+        o.pre_iterations = mg.PreSmoothingIterations
+        o.post_iterations = mg.PostSmoothingIterations
+        o.omega = mg.RelaxationParameter
+        o.tolerance = self.Tolerance
+        o.max_iterations = self.MaxIterations
+        o.vcycle_precision = N.PRECISION[mg.VCyclePrecision]
+        o.colouring = 1 if mg.Colouring else 0
+        o.use_graphs = 1 if self.UseGraphs else 0
+        o.autotune = 1 if mg.Autotune else 0
+        o.max_coarse_rows = mg.MaxCoarseRows
+        return o
+
+    def Setup(self, A):
+        """FlexibleConjugateGradient::Setup (FlexibleConjugateGradient.h:32-37): the operator and the
+        preconditioner's whole hierarchy go to the GPU."""
+        super().Setup(A)
+        mg = self.Precond._solver
+        if mg is None:
+            raise NotImplementedError("the GPU Krylov solvers need the multigrid preconditioner")
+        mg._check_supported()
+        if not mg._As:
+            raise ValueError("Multigrid.SetHierarchy must be called before Setup")
+        if mg._As[0].shape != self.Matrix.shape:
+            raise ValueError("the finest multigrid level is not the system matrix")
+        bs = mg.BlockSizeForBlockSmoothers
+        if bs <= 0:
+            raise ValueError("BlockSizeForBlockSmoothers must be set (face DOFs)")
+        if self._ctx is None:
+            self._ctx = N.Context(self.Device)
+        self._ctx.set_level(0, bs, self.Matrix)
+        for l in range(1, len(mg._As)):
+            self._ctx.set_level(l, bs, mg._As[l])
+        for l, P in enumerate(mg._Ps):
+            self._ctx.set_prolongation(l, P)
+        self._ctx.setup(len(mg._As), self._options(mg))
+
+    def Solve(self, b, initialGuessCode: str = "0"):
+        """IterativeSolver::Solve(b, "0") (IterativeSolver.h:55-73)."""
+        if initialGuessCode != "0":
+            raise NotImplementedError("the GPU solve starts from x = 0 (initial guess code \"0\")")
+        if self._ctx is None:
+            raise N.FhgError(N.FHG_ERR_NOT_READY, "Setup has not been called")
+        rc, x, hist, info = self._ctx.solve(np.asarray(b, dtype=np.float64), self.MaxIterations)
+        self.IterationCount = info.iterations
+        self.SolveTimeMs = info.solve_ms
+        self.History = hist
+        prev = -1.0
+        rates: List[float] = []
+        for k, nr in enumerate(hist):
+            r = IterationResult(IterationNumber=k, NormalizedResidualNorm=float(nr), PreviousNormalizedResidualNorm=prev)
+            if prev != -1.0:
+                r.IterationConvRate = nr / prev
+                rates = (rates + [r.IterationConvRate])[-5:]
+                r.AsymptoticConvRate = float(np.prod(rates) ** (1.0 / len(rates)))
+            if self.OnIterationEnd:
+                self.OnIterationEnd(r)
+            self.LastIterationResult = r
+            prev = nr
+        if rc != N.FHG_OK:
+            self._ctx._check(rc)
+        return x
+
+    def Context(self) -> N.Context:
+        return self._ctx
+
+
+class FlexibleConjugateGradient(_KrylovOnGpu):
+    _krylov = "fcg"
+
+    def __init__(self, truncation: int = 1, restart: bool = False):
+        super().__init__()
+        if truncation != 1 or restart:
+            raise NotImplementedError("FCG(1) without restart is the configuration on the GPU")
+        self.Truncation = truncation
+        self.Restart = restart
+
+
+class ConjugateGradient(_KrylovOnGpu):
+    _krylov = "cg"
+
+
+def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: str = "bgs", post: str = "rbgs",
+           precision: str = "fp64", krylov: str = "fcg", device: int = 0, autotune: bool = False,
+           use_graphs: bool = True):
+    """SolverFactory-style construction of "-s fcgmg -cycle V,1,1" (src/Solver/SolverFactory.h:156-200)."""
+    mg = Multigrid(len(As))
+    mg.SetHierarchy(As, Ps)
+    mg.BlockSizeForBlockSmoothers = block_size
+    mg.PreSmootherCode, mg.PostSmootherCode = pre, post
+    mg.VCyclePrecision = precision
+    mg.Autotune = autotune
+    solver = FlexibleConjugateGradient(1) if krylov == "fcg" else ConjugateGradient()
+    solver.Precond = SolverPreconditioner(mg)
+    solver.Tolerance = tol
+    solver.MaxIterations = maxit
+    solver.Device = device
+    solver.UseGraphs = use_graphs
+    solver.Setup(As[0])
+    return solver

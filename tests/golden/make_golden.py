@@ -1,0 +1,142 @@
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+Runs the reference harness (oracle/_ref/ref_driver, compiled from the reference
+checkout by ``make -C oracle ref``) and stores, per case, in a compressed .npz:
+
+* the whole multigrid hierarchy the reference builds (A_l, P_l as CSR) and b;
+* the reference FCG(1)+V(1,1) residual history and solution in its natural
+  block-Gauss-Seidel order (``hist_natural``, ``x_natural``);
+* the colour permutation of every level computed by the oracle's greedy
+  colouring, and the reference's own classes re-run on the colour-permuted
+  hierarchy (``hist_colour``, ``x_colour`` in the permuted numbering), for
+  block GS (bgs/rbgs), block Jacobi (bj23) and PCG (``cg``).
+
+Only ``hist_*`` summaries are kept for the large cases (``--histories-only``).
+
+Usage:  python tests/golden/make_golden.py [case ...] [--histories-only]
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+import scipy.sparse as sp
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import oracle as O  # noqa: E402
+
+GOLDEN = os.path.dirname(os.path.abspath(__file__))
+
+# name -> (dim, n, k)
+CASES = {
+    "tri2d_n8_k1": (2, 8, 1),
+    "tri2d_n32_k1": (2, 32, 1),      # 2D Poisson, 2048 triangles, k=1
+    "tri2d_n50_k1": (2, 50, 1),      # odd coarse n (25): hierarchy stops early, large coarsest
+    "tri2d_n16_k2": (2, 16, 2),      # block size 3
+    "tet3d_n4_k1": (3, 4, 1),
+    "tet3d_n8_k1": (3, 8, 1),
+    "tet3d_n4_k2": (3, 4, 2),        # block size 6
+}
+LARGE = {
+    "tet3d_n16_k1": (3, 16, 1),
+    "tet3d_n32_k1": (3, 32, 1),
+    "tet3d_n64_k1": (3, 64, 1),
+}
+
+
+def load_csr(prefix):
+    sh = np.fromfile(prefix + "_shape.i32", dtype=np.int32)
+    rp = np.fromfile(prefix + "_rowptr.i32", dtype=np.int32)
+    ci = np.fromfile(prefix + "_colidx.i32", dtype=np.int32)
+    va = np.fromfile(prefix + "_vals.f64")
+    return sp.csr_matrix((va, ci, rp), shape=(int(sh[0]), int(sh[1])))
+
+
+def dump_csr(prefix, A):
+    A = O.as_csr(A)
+    np.asarray(A.shape, dtype=np.int32).tofile(prefix + "_shape.i32")
+    A.indptr.astype(np.int32).tofile(prefix + "_rowptr.i32")
+    A.indices.astype(np.int32).tofile(prefix + "_colidx.i32")
+    A.data.astype(np.float64).tofile(prefix + "_vals.f64")
+
+
+def ref_gen(dim, n, k, out):
+    subprocess.run([O.REF_DRIVER, "gen", str(dim), str(n), str(k), out], check=True)
+    meta = json.load(open(os.path.join(out, "meta.json")))
+    L = meta["levels"]
+    As = [load_csr(f"{out}/L{l}_A") for l in range(L)]
+    Ps = [load_csr(f"{out}/L{l}_P") for l in range(L - 1)]
+    b = np.fromfile(f"{out}/b.f64")
+    return meta, As, Ps, b, np.fromfile(f"{out}/history.f64"), np.fromfile(f"{out}/x.f64")
+
+
+def ref_solve(As, Ps, b, bs, work, smoothers="bgs,rbgs", krylov="fcg"):
+    os.makedirs(work, exist_ok=True)
+    np.asarray([len(As), bs], dtype=np.int32).tofile(f"{work}/levels.i32")
+    for l, A in enumerate(As):
+        dump_csr(f"{work}/L{l}_A", A)
+    for l, P in enumerate(Ps):
+        dump_csr(f"{work}/L{l}_P", P)
+    np.asarray(b, dtype=np.float64).tofile(f"{work}/b.f64")
+    subprocess.run([O.REF_DRIVER, "solve", work, "--smoothers", smoothers, "--krylov", krylov], check=True)
+    return np.fromfile(f"{work}/out_history.f64"), np.fromfile(f"{work}/out_x.f64")
+
+
+def make_case(name, dim, n, k, histories_only=False):
+    with tempfile.TemporaryDirectory() as tmp:
+        gen = os.path.join(tmp, "gen")
+        os.makedirs(gen)
+        meta, As, Ps, b, hist_nat, x_nat = ref_gen(dim, n, k, gen)
+        bs = meta["block_size"]
+        perms, ncol = O.colour_perms(As, bs)
+        Ac, Pc, bc = O.permute_hierarchy(As, Ps, b, bs, perms)
+        hist_col, x_col = ref_solve(Ac, Pc, bc, bs, os.path.join(tmp, "col"))
+        hist_bj, x_bj = ref_solve(Ac, Pc, bc, bs, os.path.join(tmp, "bj"), smoothers="bj23,bj23")
+        hist_cg, x_cg = ref_solve(Ac, Pc, bc, bs, os.path.join(tmp, "cg"), krylov="cg")
+        out = dict(
+            dim=dim, n=n, k=k, block_size=bs, levels=len(As),
+            hist_natural=hist_nat, hist_colour=hist_col, hist_bj23=hist_bj, hist_cg=hist_cg,
+            ncolours=np.asarray(ncol, dtype=np.int32),
+            level_rows=np.asarray([A.shape[0] for A in As], dtype=np.int64),
+            level_nnz=np.asarray([A.nnz for A in As], dtype=np.int64),
+            p_nnz=np.asarray([P.nnz for P in Ps], dtype=np.int64),
+            b_norm=np.linalg.norm(b), x_natural_norm=np.linalg.norm(x_nat),
+            setup_s=meta.get("setup_s", 0.0), solve_s=meta.get("solve_s", 0.0),
+        )
+        if not histories_only:
+            out.update(b=b, x_natural=x_nat, x_colour=x_col, x_bj23=x_bj, x_cg=x_cg)
+            for l, A in enumerate(As):
+                A = O.as_csr(A)
+                out[f"A{l}_indptr"], out[f"A{l}_indices"], out[f"A{l}_data"] = A.indptr, A.indices, A.data
+                out[f"perm{l}"] = perms[l]
+            for l, P in enumerate(Ps):
+                P = O.as_csr(P)
+                out[f"P{l}_indptr"], out[f"P{l}_indices"], out[f"P{l}_data"] = P.indptr, P.indices, P.data
+                out[f"P{l}_shape"] = np.asarray(P.shape, dtype=np.int64)
+        path = os.path.join(GOLDEN, name + ".npz")
+        np.savez_compressed(path, **out)
+        print(f"{name}: levels={len(As)} N={As[0].shape[0]} nnz={As[0].nnz} iters nat/col/bj/cg="
+              f"{len(hist_nat)-1}/{len(hist_col)-1}/{len(hist_bj)-1}/{len(hist_cg)-1} "
+              f"size={os.path.getsize(path)/1e6:.2f} MB", flush=True)
+
+
+def main(argv):
+    histories_only = "--histories-only" in argv
+    names = [a for a in argv if not a.startswith("--")]
+    table = dict(CASES, **LARGE)
+    if not names:
+        names = list(CASES)
+    if not os.path.exists(O.REF_DRIVER):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+    for name in names:
+        dim, n, k = table[name]
+        make_case(name, dim, n, k, histories_only or name in LARGE)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -1,0 +1,245 @@
+"""Parity of the CUDA path (libfhg through its C ABI) with the reference and the oracle.
+
+Solve level: iteration counts exact, normalised residual histories within 1e-10 relative per
+iteration (absolute floor 1e-13), solutions within 1e-10 relative L2, against the reference's
+own classes run on the colour-permuted hierarchy (tests/golden/). Kernel level: every operator
+of every level against the oracle. Integer work (colour permutation): bit-exact.
+"""
+import importlib
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import oracle as O
+from _golden import FULL_CASES, Case, available
+from test_oracle import HIST_ATOL, X_RTOL, check_bj23_history, hist_close
+
+pytestmark = pytest.mark.gpu
+
+B = importlib.import_module("fhhos4_gb300.build")
+
+
+@pytest.fixture(scope="session", autouse=True)
+def built_library():
+    if not os.path.exists(B.LIB):
+        B.build()
+    from fhhos4_gb300 import _native as N
+    N.load()
+
+
+@pytest.fixture(scope="module", params=available(FULL_CASES))
+def case(request):
+    return Case(request.param)
+
+
+def S():
+    from fhhos4_gb300 import solver
+    return solver
+
+
+def scalar_perm(perm, bs):
+    return (np.asarray(perm)[:, None] * bs + np.arange(bs)[None, :]).ravel()
+
+
+def true_rel_residual(A, b, x):
+    return np.linalg.norm(b - A @ x) / np.linalg.norm(b)
+
+
+# ---------------------------------------------------------------------------- solves
+@pytest.mark.parametrize("graphs", [True, False])
+def test_fcg_mg_matches_reference_colour_order(case, graphs):
+    solver = S().fcg_mg(case.As, case.Ps, case.bs, use_graphs=graphs)
+    hist = []
+    solver.OnIterationEnd = lambda r: hist.append(r.NormalizedResidualNorm)
+    x = solver.Solve(case.b)
+    ref = case["hist_colour"]
+    assert solver.IterationCount == len(ref) - 1
+    assert hist_close(hist, ref), (np.asarray(hist), ref)
+    xc = case["x_colour"]
+    sp_ = scalar_perm(case.perms[0], case.bs)
+    assert np.linalg.norm(x[sp_] - xc) / np.linalg.norm(xc) < X_RTOL
+    # the colour permutation the GPU used is the oracle's, bit for bit
+    ctx = solver.Context()
+    for l in range(case.levels - 1):
+        nb = case.As[l].shape[0] // case.bs
+        assert np.array_equal(ctx.permutation(l, nb), case.perms[l])
+
+
+def test_fcg_mg_on_the_permuted_hierarchy_is_the_reference_run(case):
+    # The exact inputs the reference harness received; greedy colouring of a colour-grouped
+    # matrix is the identity, so the GPU sweeps the rows in the same order.
+    Ac, Pc, bc = O.permute_hierarchy(case.As, case.Ps, case.b, case.bs, case.perms)
+    solver = S().fcg_mg(Ac, Pc, case.bs)
+    x = solver.Solve(bc)
+    ref = case["hist_colour"]
+    assert solver.IterationCount == len(ref) - 1
+    assert hist_close(solver.History, ref)
+    assert np.linalg.norm(x - case["x_colour"]) / np.linalg.norm(case["x_colour"]) < X_RTOL
+    ctx = solver.Context()
+    for l in range(case.levels - 1):
+        nb = Ac[l].shape[0] // case.bs
+        assert np.array_equal(ctx.permutation(l, nb), np.arange(nb))
+
+
+def test_pcg_mg_matches_reference(case):
+    solver = S().fcg_mg(case.As, case.Ps, case.bs, krylov="cg")
+    x = solver.Solve(case.b)
+    ref = case["hist_cg"]
+    assert solver.IterationCount == len(ref) - 1
+    assert hist_close(solver.History, ref)
+    sp_ = scalar_perm(case.perms[0], case.bs)
+    assert np.linalg.norm(x[sp_] - case["x_cg"]) / np.linalg.norm(case["x_cg"]) < X_RTOL
+
+
+def test_block_jacobi_smoother_matches_reference(case):
+    solver = S().fcg_mg(case.As, case.Ps, case.bs, pre="bj23", post="bj23")
+    solver.Solve(case.b)
+    check_bj23_history(solver.History, np.asarray(case["hist_bj23"]))
+
+
+def test_solves_are_bitwise_reproducible(case):
+    solver = S().fcg_mg(case.As, case.Ps, case.bs)
+    x1 = solver.Solve(case.b)
+    h1 = solver.History.copy()
+    x2 = solver.Solve(case.b)
+    assert np.array_equal(x1, x2) and np.array_equal(h1, solver.History)
+
+
+def test_fp32_vcycle_reaches_fp64_tolerance(case):
+    ref_iters = len(case["hist_colour"]) - 1
+    solver = S().fcg_mg(case.As, case.Ps, case.bs, precision="fp32")
+    x = solver.Solve(case.b)
+    assert solver.History[-1] < 1e-8
+    assert solver.IterationCount <= ref_iters + 3
+    assert true_rel_residual(case.As[0], case.b, x) < 5e-8
+    xr = case["x_natural"]
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-6
+
+
+def test_autotuned_lanes_give_the_same_solve(case):
+    solver = S().fcg_mg(case.As, case.Ps, case.bs, autotune=True)
+    solver.Solve(case.b)
+    ref = case["hist_colour"]
+    assert solver.IterationCount == len(ref) - 1
+    assert hist_close(solver.History, ref)
+
+
+# ---------------------------------------------------------------------------- kernels
+def _ctx(case):
+    solver = S().fcg_mg(case.As, case.Ps, case.bs)
+    return solver, solver.Context()
+
+
+def test_operators_of_every_level(case):
+    from fhhos4_gb300 import _native as N
+    solver, ctx = _ctx(case)
+    rng = np.random.default_rng(7)
+    for l, A in enumerate(case.As):
+        n = A.shape[0]
+        x = rng.standard_normal(n)
+        b = rng.standard_normal(n)
+        scale = np.abs(A).max() * np.linalg.norm(x)
+        y = ctx.apply(l, N.OP_SPMV, x, None, n)
+        assert np.linalg.norm(y - O.spmv(A, x)) <= 1e-14 * scale * 10
+        r = ctx.apply(l, N.OP_RESIDUAL, x, b, n)
+        assert np.linalg.norm(r - O.residual(A, b, x)) <= 1e-14 * (scale + np.linalg.norm(b)) * 10
+        if l < case.levels - 1:
+            P = case.Ps[l]
+            nc = P.shape[1]
+            R = O.as_csr(P.T)
+            rc = ctx.apply(l, N.OP_RESTRICT, x, None, nc)
+            assert np.linalg.norm(rc - O.spmv(R, x)) <= 1e-13 * np.abs(P).max() * np.linalg.norm(x) * 10
+            e = rng.standard_normal(nc)
+            xp = ctx.apply(l, N.OP_PROLONG_ADD, e, x, n)
+            assert np.linalg.norm(xp - (x + O.spmv(P, e))) <= 1e-13 * (np.linalg.norm(x) + np.abs(P).max() * np.linalg.norm(e)) * 10
+            # smoothers: the GPU sweeps in colour order; the oracle sweeps the permuted matrix
+            s = scalar_perm(ctx.permutation(l, n // case.bs), case.bs)
+            Ap = O.as_csr(A[s][:, s])
+            for op, backward in ((N.OP_GS_FORWARD, False), (N.OP_GS_BACKWARD, True)):
+                g = ctx.apply(l, op, x, b, n)
+                ref = np.empty(n)
+                ref[s] = O.block_gs(Ap, case.bs, b[s], x[s], backward=backward)
+                assert np.linalg.norm(g - ref) <= 1e-11 * np.linalg.norm(ref)
+            j = ctx.apply(l, N.OP_JACOBI, x, b, n)
+            assert np.linalg.norm(j - O.block_jacobi(A, case.bs, 1.0, b, x)) <= 1e-11 * np.linalg.norm(j)
+        else:
+            xs = ctx.apply(l, N.OP_COARSE_SOLVE, b, None, n)
+            ref = np.linalg.solve(A.toarray(), b)
+            assert np.linalg.norm(xs - ref) <= 1e-10 * np.linalg.norm(ref)
+    A0 = case.As[0]
+    x = rng.standard_normal(A0.shape[0])
+    ys = ctx.apply(0, N.OP_SYM_SPMV, x, None, A0.shape[0])
+    assert np.linalg.norm(ys - O.spmv_sym_lower(A0, x)) <= 1e-13 * np.abs(A0).max() * np.linalg.norm(x) * 10
+
+
+def test_kernel_launches_are_counted(case):
+    solver, ctx = _ctx(case)
+    before = ctx.kernel_launches()
+    solver.Solve(case.b)
+    assert ctx.kernel_launches() > before + solver.IterationCount
+
+
+# ---------------------------------------------------------------------------- errors
+def _tiny():
+    c = Case("tet3d_n4_k1")
+    return c
+
+
+def test_nan_rhs_reports_the_reference_message():
+    from fhhos4_gb300 import _native as N
+    c = _tiny()
+    solver = S().fcg_mg(c.As, c.Ps, c.bs)
+    b = c.b.copy()
+    b[5] = np.nan
+    with pytest.raises(N.FhgError) as ei:
+        solver.Solve(b)
+    assert ei.value.code in (N.FHG_ERR_NAN, N.FHG_ERR_DIVERGED)
+
+
+def test_singular_diagonal_block_is_rejected():
+    from fhhos4_gb300 import _native as N
+    c = _tiny()
+    A = c.As[0].tolil()
+    A[0, :] = 0.0
+    A[:, 0] = 0.0
+    A = sp.csr_matrix(A)
+    A.eliminate_zeros()
+    with pytest.raises(N.FhgError) as ei:
+        S().fcg_mg([A] + c.As[1:], c.Ps, c.bs)
+    assert ei.value.code == N.FHG_ERR_SINGULAR_BLOCK
+
+
+def test_invalid_inputs_are_rejected():
+    from fhhos4_gb300 import _native as N
+    c = _tiny()
+    ctx = N.Context(0)
+    with pytest.raises(N.FhgError) as ei:
+        ctx.set_level(0, 5, c.As[0])
+    assert ei.value.code == N.FHG_ERR_UNSUPPORTED
+    with pytest.raises(N.FhgError) as ei:
+        ctx.setup(2, N.default_options())
+    assert ei.value.code == N.FHG_ERR_INVALID_ARG
+    ctx.set_level(0, c.bs, c.As[0])
+    ctx.set_level(1, c.bs, c.As[1])
+    with pytest.raises(N.FhgError):
+        ctx.setup(2, N.default_options())          # P_0 missing
+    ctx.set_prolongation(0, c.Ps[0])
+    o = N.default_options()
+    o.max_coarse_rows = 10
+    with pytest.raises(N.FhgError) as ei:
+        ctx.setup(2, o)
+    assert ei.value.code == N.FHG_ERR_TOO_LARGE
+    rc, x, hist, info = ctx.solve(c.b, 10)
+    assert rc == N.FHG_ERR_NOT_READY
+    ctx.setup(2, N.default_options())
+    rc, x, hist, info = ctx.solve(c.b, 200)
+    assert rc == N.FHG_OK and info.iterations > 0
+    bad = sp.csr_matrix(c.As[0])
+    bad.indices = bad.indices.copy()
+    bad.indices[0] = bad.shape[0] + 3
+    with pytest.raises(N.FhgError) as ei:
+        ctx.set_level(0, c.bs, bad)
+    assert ei.value.code == N.FHG_ERR_INVALID_ARG
+    ctx.close()

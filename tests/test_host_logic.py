@@ -1,0 +1,53 @@
+"""Host-side logic of the Python mirror that needs no GPU: option mapping, argument checks,
+unsupported configurations failing loudly."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from fhhos4_gb300 import _native as N
+from fhhos4_gb300 import solver as S
+
+
+def test_as_eigen_csr_is_canonical():
+    A = sp.coo_matrix((np.array([1.0, 2.0, 3.0]), (np.array([1, 0, 1]), np.array([0, 1, 0]))), shape=(2, 2))
+    C = S.as_eigen_csr(A)
+    assert C.indptr.dtype == np.int32 and C.indices.dtype == np.int32
+    assert C[1, 0] == 4.0 and C.nnz == 2
+
+
+def test_reference_defaults_are_mirrored():
+    fcg = S.FlexibleConjugateGradient()
+    assert fcg.Truncation == 1 and not fcg.Restart
+    mg = S.Multigrid()
+    assert (mg.PreSmootherCode, mg.PostSmootherCode) == ("bgs", "rbgs")
+    assert (mg.PreSmoothingIterations, mg.PostSmoothingIterations) == (1, 1)
+    assert mg.Cycle == "V" and mg.MatrixMaxSizeForCoarsestLevel == 1000
+    assert fcg.MaxIterations == 200
+
+
+def test_unsupported_configurations_fail_loudly():
+    with pytest.raises(NotImplementedError):
+        S.FlexibleConjugateGradient(truncation=2)
+    mg = S.Multigrid()
+    mg.Cycle = "W"
+    with pytest.raises(NotImplementedError):
+        mg._check_supported()
+    mg.Cycle = "V"
+    mg.PreSmootherCode = "hbgs"
+    with pytest.raises(NotImplementedError):
+        mg._check_supported()
+    fcg = S.FlexibleConjugateGradient()
+    with pytest.raises(NotImplementedError):
+        fcg.Setup(sp.identity(4, format="csr"))   # no multigrid preconditioner
+
+
+def test_hierarchy_shape_checks():
+    mg = S.Multigrid()
+    with pytest.raises(ValueError):
+        mg.SetHierarchy([sp.identity(6)], [sp.identity(6)])
+
+
+def test_option_codes_match_header():
+    assert N.SMOOTHERS == {"bgs": 0, "rbgs": 1, "bj": 2, "bj23": 3}
+    assert N.KRYLOV == {"fcg": 0, "cg": 1}
+    assert N.PRECISION == {"fp64": 0, "fp32": 1}
