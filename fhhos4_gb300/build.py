@@ -16,7 +16,9 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libfhg.so")
+HHO_LIB = os.path.join(OUT_DIR, "libfhg_hho.so")
 SOURCES = ["fhg_kernels.cu", "fhg_api.cu"]
+HHO_SOURCES = ["hho_gen.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -49,8 +51,20 @@ def build(verbose: bool = False, extra=()) -> str:
             print(r.stderr, flush=True)
         return obj
 
-    with cf.ThreadPoolExecutor(len(SOURCES)) as ex:
+    def build_hho():
+        cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+        tmp = HHO_LIB + ".tmp"
+        cmd = [cxx, "-std=c++17", "-O3", "-fPIC", "-shared", "-w", "-o", tmp,
+               *[os.path.join(CSRC, s) for s in HHO_SOURCES], "-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"host generator build failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, HHO_LIB)
+
+    with cf.ThreadPoolExecutor(len(SOURCES) + 1) as ex:
+        hho = ex.submit(build_hho)
         objs = list(ex.map(compile_one, SOURCES))
+        hho.result()
     tmp = LIB + ".tmp"
     cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -1,0 +1,1252 @@
+// Host-side producer of the multigrid hierarchy the solve phase consumes: the statically
+// condensed HHO face system A_l, right-hand side b and prolongations P_l of fhhos4's
+// geometric h-multigrid, for the in-house meshes of the unit square (2 triangles per cell)
+// and the unit cube (6 tetrahedra per cube).
+//
+// It reproduces the reference's discretisation so that the system is the reference's own
+// (up to rounding):
+//   * mesh numbering: Square_TriangularMesh::Build (src/Mesher/InHouse/Square_TriangularMesh.h:113-233),
+//     Cube_CartesianTetrahedralMesh::Build (src/Mesher/InHouse/Cube_CartesianTetrahedralMesh.h:24-104),
+//     faces renumbered interior-first (src/Mesh/Mesh.h:331-340);
+//   * standard coarsening links (Square_TriangularMesh.h:368-400, Cube_CartesianTetrahedralMesh.h:120-162,
+//     Mesh.h:696-732);
+//   * face bases: Legendre on edges (2D), monomials in the face's reference coordinates
+//     orthogonalised once by Gram-Schmidt (3D) (src/Discretizations/HHO/Diff_HHOFace.h:55-70,
+//     src/FunctionalBasis/Orthogonal/OrthogonalBasis.h:96-114);
+//   * HHO reconstruction, "hho" stabilisation, static condensation and condensed RHS
+//     (src/Discretizations/HHO/Diff_HHOElement.h:303-470, Diffusion_HHO.h:600-640);
+//   * prolongation P = Pi_f I_c with heterogeneous face weights and R = P^T
+//     (src/Solver/Multigrid/MultigridForHHO/LevelForHHO.h:182-213,743-954).
+// Cell bases are this file's own (orthonormalised scaled monomials): the condensed operator
+// and P do not depend on that choice. Integrals are exact (collapsed Gauss-Legendre rules)
+// except the source term, integrated with a high-order rule.
+#include "hho_gen.h"
+
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+
+// ---------------------------------------------------------------------------
+// Small dense helpers (row-major)
+
+struct Mat {
+    int r = 0, c = 0;
+    std::vector<double> a;
+    Mat() {}
+    Mat(int r_, int c_) : r(r_), c(c_), a((size_t)r_ * c_, 0.0) {}
+    double& operator()(int i, int j) { return a[(size_t)i * c + j]; }
+    double operator()(int i, int j) const { return a[(size_t)i * c + j]; }
+};
+
+Mat matmul(const Mat& A, const Mat& B)
+{
+    Mat C(A.r, B.c);
+    for (int i = 0; i < A.r; i++)
+        for (int k = 0; k < A.c; k++) {
+            const double v = A(i, k);
+            if (v == 0.0) continue;
+            for (int j = 0; j < B.c; j++) C(i, j) += v * B(k, j);
+        }
+    return C;
+}
+
+Mat transpose(const Mat& A)
+{
+    Mat T(A.c, A.r);
+    for (int i = 0; i < A.r; i++)
+        for (int j = 0; j < A.c; j++) T(j, i) = A(i, j);
+    return T;
+}
+
+// Solve A X = B (A square) by LU with partial pivoting; returns false if singular.
+bool solve(Mat A, Mat& B)
+{
+    const int n = A.r;
+    std::vector<int> piv(n);
+    for (int k = 0; k < n; k++) {
+        int p = k;
+        for (int i = k + 1; i < n; i++)
+            if (std::fabs(A(i, k)) > std::fabs(A(p, k))) p = i;
+        if (A(p, k) == 0.0) return false;
+        if (p != k) {
+            for (int j = 0; j < n; j++) std::swap(A(k, j), A(p, j));
+            for (int j = 0; j < B.c; j++) std::swap(B(k, j), B(p, j));
+        }
+        for (int i = k + 1; i < n; i++) {
+            const double f = A(i, k) / A(k, k);
+            if (f == 0.0) continue;
+            for (int j = k; j < n; j++) A(i, j) -= f * A(k, j);
+            for (int j = 0; j < B.c; j++) B(i, j) -= f * B(k, j);
+        }
+    }
+    for (int i = n - 1; i >= 0; i--)
+        for (int j = 0; j < B.c; j++) {
+            double v = B(i, j);
+            for (int k = i + 1; k < n; k++) v -= A(i, k) * B(k, j);
+            B(i, j) = v / A(i, i);
+        }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Quadrature: Gauss-Legendre on [0,1] and collapsed rules on the reference simplex.
+
+void gauss_legendre01(int m, std::vector<double>& x, std::vector<double>& w)
+{
+    x.resize(m);
+    w.resize(m);
+    for (int i = 0; i < m; i++) {
+        long double z = std::cos(kPi * (i + 0.75L) / (m + 0.5L)), pp = 0;
+        for (int it = 0; it < 100; it++) {
+            long double p1 = 1, p2 = 0;
+            for (int j = 1; j <= m; j++) {
+                const long double p3 = p2;
+                p2 = p1;
+                p1 = ((2 * j - 1) * z * p2 - (j - 1) * p3) / j;
+            }
+            pp = m * (z * p1 - p2) / (z * z - 1);
+            const long double dz = p1 / pp;
+            z -= dz;
+            if (std::fabs((double)dz) < 1e-19) break;
+        }
+        x[i] = (double)((1 - z) / 2);
+        w[i] = (double)(1 / ((1 - z * z) * pp * pp));
+    }
+}
+
+struct RefRule {
+    std::vector<std::array<double, 3>> p;  // reference simplex coordinates
+    std::vector<double> w;                 // weights summing to the reference measure
+};
+
+// Exact for polynomials of degree <= 2m-1-(dim-1) on the reference simplex.
+RefRule simplex_rule(int dim, int m)
+{
+    std::vector<double> x, w;
+    gauss_legendre01(m, x, w);
+    RefRule R;
+    if (dim == 1) {
+        for (int i = 0; i < m; i++) { R.p.push_back({x[i], 0, 0}); R.w.push_back(w[i]); }
+    } else if (dim == 2) {
+        for (int i = 0; i < m; i++)
+            for (int j = 0; j < m; j++) {
+                const double a = x[i], b = x[j];
+                R.p.push_back({a * (1 - b), b, 0});
+                R.w.push_back(w[i] * w[j] * (1 - b));
+            }
+    } else {
+        for (int i = 0; i < m; i++)
+            for (int j = 0; j < m; j++)
+                for (int k = 0; k < m; k++) {
+                    const double a = x[i], b = x[j], c = x[k];
+                    R.p.push_back({a * (1 - b) * (1 - c), b * (1 - c), c});
+                    R.w.push_back(w[i] * w[j] * w[k] * (1 - b) * (1 - c) * (1 - c));
+                }
+    }
+    return R;
+}
+
+// ---------------------------------------------------------------------------
+// Meshes
+
+struct Mesh {
+    int dim = 2, n = 0;
+    std::vector<std::array<double, 3>> vx;
+    std::vector<std::array<int, 4>> el;        // vertices (dim+1)
+    std::vector<std::array<int, 3>> fv;        // face vertices in the face's own order (dim)
+    std::vector<int> fe1, fe2;                 // face elements (fe2 = -1 on the boundary)
+    std::vector<std::array<int, 4>> ef;        // element faces (dim+1)
+    std::vector<int> efn;                      // faces added so far per element (build only)
+    std::vector<int> interior_order;           // faces in the order they became interior
+    std::vector<int> number;                   // face -> unknown block (-1: Dirichlet face)
+    int n_interior = 0;
+    std::vector<int> coarser;                  // element -> coarser element (standard coarsening)
+    std::vector<int> removed;                  // face -> 1 if interior to a coarse element
+    std::vector<std::array<double, 9>> K;      // diffusion tensor per element (row-major dim x dim)
+};
+
+void add_face_to_element(Mesh& M, int e, int f) { M.ef[e][M.efn[e]++] = f; }
+
+void finalize_numbering(Mesh& M)
+{
+    M.number.assign(M.fv.size(), -1);
+    int k = 0;
+    for (int f : M.interior_order) M.number[f] = k++;
+    M.n_interior = k;
+}
+
+Mesh build_tri(int n)
+{
+    Mesh M;
+    M.dim = 2; M.n = n;
+    const double h = 1.0 / n;
+    for (int iy = 0; iy <= n; iy++)
+        for (int ix = 0; ix <= n; ix++) M.vx.push_back({ix * h, iy * h, 0.0});
+    auto V = [&](int ix, int iy) { return iy * (n + 1) + ix; };
+    auto E = [&](int ix, int iy) { return (iy * n + ix) * 2; };
+    M.el.resize((size_t)2 * n * n);
+    for (int iy = 0; iy < n; iy++)
+        for (int ix = 0; ix < n; ix++) {
+            const int bl = V(ix, iy), tl = V(ix, iy + 1), tr = V(ix + 1, iy + 1), br = V(ix + 1, iy);
+            M.el[E(ix, iy)] = {bl, br, tl, -1};       // lower (V1, V2, V3)
+            M.el[E(ix, iy) + 1] = {tl, br, tr, -1};   // upper
+        }
+    M.ef.assign(M.el.size(), {-1, -1, -1, -1});
+    M.efn.assign(M.el.size(), 0);
+    auto face = [&](int a, int b, int e1, int e2) {
+        const int f = (int)M.fv.size();
+        M.fv.push_back({a, b, -1});
+        M.fe1.push_back(e1);
+        M.fe2.push_back(e2);
+        add_face_to_element(M, e1, f);
+        if (e2 >= 0) { add_face_to_element(M, e2, f); M.interior_order.push_back(f); }
+        return f;
+    };
+    for (int ix = 0; ix < n; ix++) {
+        const int lo = E(ix, 0);
+        face(M.el[lo][0], M.el[lo][1], lo, -1);                 // south: lower V1-V2
+        const int up = E(ix, n - 1) + 1;
+        face(M.el[up][0], M.el[up][2], up, -1);                 // north: upper V1-V3
+    }
+    for (int iy = 0; iy < n; iy++) {
+        const int lo = E(0, iy);
+        face(M.el[lo][2], M.el[lo][0], lo, -1);                 // west: lower V3-V1
+        const int up = E(n - 1, iy) + 1;
+        face(M.el[up][1], M.el[up][2], up, -1);                 // east: upper V2-V3
+    }
+    for (int iy = 0; iy < n; iy++)
+        for (int ix = 0; ix < n; ix++) {
+            const int lo = E(ix, iy), up = lo + 1;
+            face(M.el[lo][2], M.el[lo][1], lo, up);              // diagonal: lower V3-V2
+            if (ix != n - 1) {
+                const int ea = E(ix + 1, iy);
+                face(M.el[ea][2], M.el[ea][0], up, ea);          // east neighbour V3-V1
+            }
+            if (iy != n - 1) {
+                const int no = E(ix, iy + 1);
+                face(M.el[no][0], M.el[no][1], up, no);          // north neighbour V1-V2
+            }
+        }
+    finalize_numbering(M);
+    return M;
+}
+
+struct TriKey {
+    int a, b, c;
+    bool operator==(const TriKey& o) const { return a == o.a && b == o.b && c == o.c; }
+};
+struct TriKeyHash {
+    size_t operator()(const TriKey& k) const
+    {
+        return ((size_t)k.a * 73856093u) ^ ((size_t)k.b * 19349663u) ^ ((size_t)k.c * 83492791u);
+    }
+};
+
+Mesh build_tet(int n)
+{
+    Mesh M;
+    M.dim = 3; M.n = n;
+    const double h = 1.0 / n;
+    for (int iz = 0; iz <= n; iz++)
+        for (int iy = 0; iy <= n; iy++)
+            for (int ix = 0; ix <= n; ix++) M.vx.push_back({ix * h, iy * h, iz * h});
+    auto V = [&](int ix, int iy, int iz) { return (iz * (n + 1) + iy) * (n + 1) + ix; };
+    const size_t ne = (size_t)6 * n * n * n;
+    M.el.reserve(ne);
+    M.ef.assign(ne, {-1, -1, -1, -1});
+    M.efn.assign(ne, 0);
+    std::unordered_map<TriKey, int, TriKeyHash> lookup;
+    lookup.reserve((size_t)14 * n * n * n);
+    auto key = [](int a, int b, int c) {
+        int v[3] = {a, b, c};
+        std::sort(v, v + 3);
+        return TriKey{v[0], v[1], v[2]};
+    };
+    auto new_face = [&](int a, int b, int c, int e1, int e2) {
+        const int f = (int)M.fv.size();
+        M.fv.push_back({a, b, c});
+        M.fe1.push_back(e1);
+        M.fe2.push_back(e2);
+        return f;
+    };
+    // CreateFaceIfNeeded (TetrahedralMesh.h:263-283)
+    auto face_if_needed = [&](int e, int a, int b, int c) {
+        auto k = key(a, b, c);
+        auto it = lookup.find(k);
+        int f;
+        if (it == lookup.end()) {
+            f = new_face(a, b, c, e, -1);
+            lookup.emplace(k, f);
+        } else {
+            f = it->second;
+            M.fe2[f] = e;
+            M.interior_order.push_back(f);
+        }
+        add_face_to_element(M, e, f);
+    };
+    // CreateInteriorFace (TetrahedralMesh.h:285-299)
+    auto interior_face = [&](int e1, int e2, int a, int b, int c) {
+        const int f = new_face(a, b, c, e1, e2);
+        lookup.emplace(key(a, b, c), f);
+        M.interior_order.push_back(f);
+        add_face_to_element(M, e1, f);
+        add_face_to_element(M, e2, f);
+    };
+    for (int iz = 0; iz < n; iz++)
+        for (int iy = 0; iy < n; iy++)
+            for (int ix = 0; ix < n; ix++) {
+                const int v000 = V(ix, iy, iz), v100 = V(ix + 1, iy, iz), v110 = V(ix + 1, iy + 1, iz),
+                          v111 = V(ix + 1, iy + 1, iz + 1), v101 = V(ix + 1, iy, iz + 1), v010 = V(ix, iy + 1, iz),
+                          v011 = V(ix, iy + 1, iz + 1), v001 = V(ix, iy, iz + 1);
+                const int t0 = (int)M.el.size();
+                M.el.push_back({v010, v110, v111, v100});
+                M.el.push_back({v111, v010, v100, v000});
+                M.el.push_back({v000, v100, v111, v101});
+                M.el.push_back({v111, v010, v000, v011});
+                M.el.push_back({v101, v111, v000, v011});
+                M.el.push_back({v101, v000, v001, v011});
+                const int t1 = t0 + 1, t2 = t0 + 2, t3 = t0 + 3, t4 = t0 + 4, t5 = t0 + 5;
+                face_if_needed(t0, v010, v111, v110);
+                face_if_needed(t0, v010, v110, v100);
+                interior_face(t0, t1, v010, v100, v111);
+                face_if_needed(t0, v100, v110, v111);
+                interior_face(t1, t3, v111, v010, v000);
+                interior_face(t1, t2, v111, v000, v100);
+                face_if_needed(t1, v000, v010, v100);
+                face_if_needed(t2, v000, v100, v101);
+                interior_face(t2, t4, v000, v101, v111);
+                face_if_needed(t2, v101, v100, v111);
+                face_if_needed(t3, v111, v010, v011);
+                interior_face(t3, t4, v111, v011, v000);
+                face_if_needed(t3, v011, v010, v000);
+                face_if_needed(t4, v101, v111, v011);
+                interior_face(t4, t5, v101, v011, v000);
+                face_if_needed(t5, v101, v001, v000);
+                face_if_needed(t5, v101, v011, v001);
+                face_if_needed(t5, v011, v000, v001);
+            }
+    finalize_numbering(M);
+    return M;
+}
+
+std::array<double, 3> centroid(const Mesh& M, int e)
+{
+    std::array<double, 3> c{0, 0, 0};
+    for (int i = 0; i <= M.dim; i++)
+        for (int d = 0; d < 3; d++) c[d] += M.vx[M.el[e][i]][d];
+    for (int d = 0; d < 3; d++) c[d] /= (M.dim + 1);
+    return c;
+}
+
+double simplex_volume(const Mesh& M, const std::array<double, 3>* P, int dim)
+{
+    if (dim == 2) {
+        return 0.5 * std::fabs((P[1][0] - P[0][0]) * (P[2][1] - P[0][1]) - (P[2][0] - P[0][0]) * (P[1][1] - P[0][1]));
+    }
+    double a[3], b[3], c[3];
+    for (int d = 0; d < 3; d++) { a[d] = P[1][d] - P[0][d]; b[d] = P[2][d] - P[0][d]; c[d] = P[3][d] - P[0][d]; }
+    const double det = a[0] * (b[1] * c[2] - b[2] * c[1]) - a[1] * (b[0] * c[2] - b[2] * c[0]) + a[2] * (b[0] * c[1] - b[1] * c[0]);
+    (void)M;
+    return std::fabs(det) / 6.0;
+}
+
+// Tetrahedron/Triangle::Contains: barycentric coordinates from sub-volumes, tolerance 1e-4
+// (src/Geometry/3D/Tetrahedron.h:147-161, Utils::Eps).
+bool contains(const Mesh& M, int e, const std::array<double, 3>& p)
+{
+    const int nv = M.dim + 1;
+    std::array<double, 3> P[4];
+    for (int i = 0; i < nv; i++) P[i] = M.vx[M.el[e][i]];
+    const double vol = simplex_volume(M, P, M.dim);
+    const double tol = 1e-4;
+    double sum = 0;
+    for (int i = 0; i < nv; i++) {
+        std::array<double, 3> Q[4];
+        for (int j = 0; j < nv; j++) Q[j] = P[j];
+        Q[i] = p;
+        const double l = simplex_volume(M, Q, M.dim) / vol;
+        if (!(l + tol > 0 && l < 1 + tol)) return false;
+        sum += l;
+    }
+    return std::fabs(sum - 1) < tol;
+}
+
+// Standard coarsening links: fine element -> coarse element containing its centre, searched
+// among the coarse simplices of the coarse cell that holds the fine cell.
+void link_coarse(Mesh& F, const Mesh& C)
+{
+    const int per = F.dim == 2 ? 2 : 6;
+    F.coarser.assign(F.el.size(), -1);
+    const int n = F.n, nc = C.n;
+    for (size_t e = 0; e < F.el.size(); e++) {
+        const int cell = (int)(e / per);
+        int ix, iy, iz = 0;
+        if (F.dim == 2) { ix = cell % n; iy = cell / n; }
+        else { ix = cell % n; iy = (cell / n) % n; iz = cell / (n * n); }
+        const int ccell = F.dim == 2 ? (iy / 2) * nc + ix / 2 : ((iz / 2) * nc + iy / 2) * nc + ix / 2;
+        const auto c = centroid(F, (int)e);
+        for (int j = 0; j < per; j++) {
+            const int ce = ccell * per + j;
+            if (contains(C, ce, c)) { F.coarser[e] = ce; break; }
+        }
+    }
+    F.removed.assign(F.fv.size(), 0);
+    for (size_t f = 0; f < F.fv.size(); f++)
+        if (F.fe2[f] >= 0) F.removed[f] = F.coarser[F.fe1[f]] == F.coarser[F.fe2[f]];
+}
+
+// ---------------------------------------------------------------------------
+// Polynomial spaces
+
+// Exponents of the monomials of total degree <= p, ordered by degree.
+std::vector<std::array<int, 3>> exponents(int dim, int p)
+{
+    std::vector<std::array<int, 3>> ex;
+    for (int deg = 0; deg <= p; deg++) {
+        if (dim == 1) ex.push_back({deg, 0, 0});
+        else if (dim == 2)
+            for (int j = 0; j <= deg; j++) ex.push_back({deg - j, j, 0});
+        else
+            for (int c = 0; c <= deg; c++)
+                for (int b = 0; b <= deg - c; b++) ex.push_back({deg - b - c, b, c});
+    }
+    return ex;
+}
+
+double ipow(double x, int k)
+{
+    double r = 1;
+    for (int i = 0; i < k; i++) r *= x;
+    return r;
+}
+
+double legendre(int n, double x)
+{
+    if (n == 0) return 1;
+    if (n == 1) return x;
+    double p0 = 1, p1 = x;
+    for (int j = 2; j <= n; j++) {
+        const double p2 = ((2 * j - 1) * x * p1 - (j - 1) * p0) / j;
+        p0 = p1;
+        p1 = p2;
+    }
+    return p1;
+}
+
+// Cell basis: scaled monomials ((x - xT)/hT)^alpha orthonormalised in L2(T) (two sweeps).
+struct CellBasis {
+    int dim = 0, nR = 0;
+    std::vector<std::array<int, 3>> ex;
+    std::array<double, 3> xc{0, 0, 0};
+    double hs = 1;
+    Mat coef;  // nR x nR: phi_i = sum_j coef(i,j) m_j
+    void eval_monomials(const double* x, double* m, double* gm /* nR x 3 or null */) const
+    {
+        double y[3] = {0, 0, 0};
+        for (int d = 0; d < dim; d++) y[d] = (x[d] - xc[d]) / hs;
+        for (int j = 0; j < nR; j++) {
+            const auto& e = ex[j];
+            m[j] = ipow(y[0], e[0]) * ipow(y[1], e[1]) * ipow(y[2], e[2]);
+            if (gm) {
+                for (int d = 0; d < 3; d++) {
+                    double g = 0;
+                    if (d < dim && e[d] > 0) {
+                        g = e[d] / hs;
+                        for (int q = 0; q < 3; q++) g *= ipow(y[q], e[q] - (q == d ? 1 : 0));
+                    }
+                    gm[j * 3 + d] = g;
+                }
+            }
+        }
+    }
+    void eval(const double* x, double* v, double* g) const
+    {
+        double m[64], gm[192];
+        eval_monomials(x, m, g ? gm : nullptr);
+        for (int i = 0; i < nR; i++) {
+            double s = 0, gx = 0, gy = 0, gz = 0;
+            for (int j = 0; j <= i; j++) {
+                const double c = coef(i, j);
+                s += c * m[j];
+                if (g) { gx += c * gm[j * 3]; gy += c * gm[j * 3 + 1]; gz += c * gm[j * 3 + 2]; }
+            }
+            v[i] = s;
+            if (g) { g[i * 3] = gx; g[i * 3 + 1] = gy; g[i * 3 + 2] = gz; }
+        }
+    }
+};
+
+// Physical quadrature points of an element / face.
+struct QPts {
+    std::vector<std::array<double, 3>> x;
+    std::vector<std::array<double, 2>> ref;  // face reference coordinates (t[, u])
+    std::vector<double> w;
+};
+
+struct Rules {
+    RefRule cell, cell_rhs, face;
+};
+
+QPts element_points(const Mesh& M, int e, const RefRule& R)
+{
+    QPts Q;
+    const int dim = M.dim;
+    const auto& X0 = M.vx[M.el[e][0]];
+    double J[3][3] = {{0}};
+    for (int c = 0; c < dim; c++)
+        for (int d = 0; d < dim; d++) J[d][c] = M.vx[M.el[e][c + 1]][d] - X0[d];
+    double det;
+    if (dim == 2) det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    else
+        det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+              J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    det = std::fabs(det);
+    for (size_t q = 0; q < R.w.size(); q++) {
+        std::array<double, 3> x{0, 0, 0};
+        for (int d = 0; d < dim; d++) {
+            x[d] = X0[d];
+            for (int c = 0; c < dim; c++) x[d] += J[d][c] * R.p[q][c];
+        }
+        Q.x.push_back(x);
+        Q.w.push_back(R.w[q] * det);
+    }
+    return Q;
+}
+
+// Face points in the face's own reference coordinates: 2D edges t in [-1,1] with
+// x = (v2-v1)/2 t + (v2+v1)/2 (src/Geometry/2D/Segment.h:117-128); 3D triangles
+// x = v1 + (v2-v1) t + (v3-v1) u (src/Geometry/3D/TriangleIn3D.h:152-162).
+QPts face_points(const Mesh& M, int f, const RefRule& R1, const RefRule& R2, double& measure, double& diameter)
+{
+    QPts Q;
+    if (M.dim == 2) {
+        const auto& a = M.vx[M.fv[f][0]];
+        const auto& b = M.vx[M.fv[f][1]];
+        const double len = std::hypot(b[0] - a[0], b[1] - a[1]);
+        measure = diameter = len;
+        for (size_t q = 0; q < R1.w.size(); q++) {
+            const double t = 2 * R1.p[q][0] - 1;  // [0,1] -> [-1,1]
+            Q.x.push_back({(b[0] - a[0]) / 2 * t + (b[0] + a[0]) / 2, (b[1] - a[1]) / 2 * t + (b[1] + a[1]) / 2, 0});
+            Q.ref.push_back({t, 0});
+            Q.w.push_back(R1.w[q] * len);
+        }
+    } else {
+        const auto& a = M.vx[M.fv[f][0]];
+        const auto& b = M.vx[M.fv[f][1]];
+        const auto& c = M.vx[M.fv[f][2]];
+        double ab[3], ac[3], bc[3];
+        for (int d = 0; d < 3; d++) { ab[d] = b[d] - a[d]; ac[d] = c[d] - a[d]; bc[d] = c[d] - b[d]; }
+        const double cr[3] = {ab[1] * ac[2] - ab[2] * ac[1], ab[2] * ac[0] - ab[0] * ac[2], ab[0] * ac[1] - ab[1] * ac[0]};
+        measure = 0.5 * std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+        auto nrm = [](const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
+        diameter = std::max({nrm(ab), nrm(ac), nrm(bc)});
+        for (size_t q = 0; q < R2.w.size(); q++) {
+            const double t = R2.p[q][0], u = R2.p[q][1];
+            Q.x.push_back({a[0] + ab[0] * t + ac[0] * u, a[1] + ab[1] * t + ac[1] * u, a[2] + ab[2] * t + ac[2] * u});
+            Q.ref.push_back({t, u});
+            Q.w.push_back(R2.w[q] * 2 * measure);
+        }
+    }
+    return Q;
+}
+
+// Reference face basis of one face: values at the face points (nf x nq) and the face mass matrix.
+struct FaceBasis {
+    int nf = 0;
+    Mat vals;  // nf x nq
+    Mat mass;  // nf x nf
+    Mat mass_inv;
+};
+
+FaceBasis face_basis(int dim, int k, const QPts& Q)
+{
+    FaceBasis B;
+    const int nq = (int)Q.w.size();
+    if (dim == 2) {
+        // LegendreBasis1D, not orthogonalised (src/FunctionalBasis/Legendre/Legendre1D.h:37-45)
+        B.nf = k + 1;
+        B.vals = Mat(B.nf, nq);
+        for (int i = 0; i < B.nf; i++)
+            for (int q = 0; q < nq; q++) B.vals(i, q) = legendre(i, Q.ref[q][0]);
+    } else {
+        // MonomialBasis2D in (t, u), Gram-Schmidt once, not normalised (OrthogonalBasis.h:96-114)
+        auto ex = exponents(2, k);
+        B.nf = (int)ex.size();
+        B.vals = Mat(B.nf, nq);
+        std::vector<double> norm2(B.nf);
+        for (int i = 0; i < B.nf; i++) {
+            for (int q = 0; q < nq; q++) B.vals(i, q) = ipow(Q.ref[q][0], ex[i][0]) * ipow(Q.ref[q][1], ex[i][1]);
+            for (int j = 0; j < i; j++) {
+                double ip = 0;
+                for (int q = 0; q < nq; q++) ip += Q.w[q] * B.vals(i, q) * B.vals(j, q);
+                const double c = ip / norm2[j];
+                for (int q = 0; q < nq; q++) B.vals(i, q) -= c * B.vals(j, q);
+            }
+            double n2 = 0;
+            for (int q = 0; q < nq; q++) n2 += Q.w[q] * B.vals(i, q) * B.vals(i, q);
+            norm2[i] = n2;
+        }
+    }
+    B.mass = Mat(B.nf, B.nf);
+    for (int i = 0; i < B.nf; i++)
+        for (int j = 0; j < B.nf; j++) {
+            double s = 0;
+            for (int q = 0; q < nq; q++) s += Q.w[q] * B.vals(i, q) * B.vals(j, q);
+            B.mass(i, j) = s;
+        }
+    if (dim == 3) {
+        // orthogonal basis: the reference applies diag(NormSquare)
+        for (int i = 0; i < B.nf; i++)
+            for (int j = 0; j < B.nf; j++)
+                if (i != j) B.mass(i, j) = 0.0;
+    }
+    B.mass_inv = Mat(B.nf, B.nf);
+    for (int i = 0; i < B.nf; i++) B.mass_inv(i, i) = 1.0;
+    solve(B.mass, B.mass_inv);
+    return B;
+}
+
+// ---------------------------------------------------------------------------
+// Element operators
+
+struct ElementOps {
+    CellBasis basis;
+    int nC = 0, nR = 0, nf = 0, nF = 0;
+    Mat P;       // nR x (nC + nF nf) reconstruction
+    Mat A;       // (nC + nF nf)^2 local operator
+    Mat schur;   // (nF nf)^2 condensed
+    Mat solve_cells;  // nC x nF nf: -A_TT^{-1} A_TF
+    Mat interp;  // nR x nF nf: P [solve_cells; I] (ReconstructionFromFacesMatrix)
+    std::vector<double> bT;    // nC: (f, c_j)_T
+    std::vector<double> bF;    // nF nf: condensed RHS contribution
+    bool ok = true;
+};
+
+struct Params {
+    int dim, k;
+    int source;  // 0: d pi^2 prod sin(pi x_i); 1: 1
+};
+
+double source_value(const Params& p, const std::array<double, 3>& x)
+{
+    if (p.source == 1) return 1.0;
+    if (p.dim == 2) return 2 * kPi * kPi * std::sin(kPi * x[0]) * std::sin(kPi * x[1]);
+    return 3 * kPi * kPi * std::sin(kPi * x[0]) * std::sin(kPi * x[1]) * std::sin(kPi * x[2]);
+}
+
+// Outward unit normal of face f of element e.
+std::array<double, 3> outer_normal(const Mesh& M, int e, int f)
+{
+    std::array<double, 3> n{0, 0, 0};
+    const auto& a = M.vx[M.fv[f][0]];
+    const auto& b = M.vx[M.fv[f][1]];
+    if (M.dim == 2) {
+        n = {b[1] - a[1], -(b[0] - a[0]), 0};
+    } else {
+        const auto& c = M.vx[M.fv[f][2]];
+        const double ab[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, ac[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+        n = {ab[1] * ac[2] - ab[2] * ac[1], ab[2] * ac[0] - ab[0] * ac[2], ab[0] * ac[1] - ab[1] * ac[0]};
+    }
+    const double len = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (auto& v : n) v /= len;
+    const auto ce = centroid(M, e);
+    double s = 0;
+    for (int d = 0; d < 3; d++) s += n[d] * (a[d] - ce[d]);
+    if (s < 0)
+        for (auto& v : n) v = -v;
+    return n;
+}
+
+void Kgrad(const std::array<double, 9>& K, int dim, const double* g, double* out)
+{
+    for (int i = 0; i < 3; i++) out[i] = 0;
+    for (int i = 0; i < dim; i++)
+        for (int j = 0; j < dim; j++) out[i] += K[i * dim + j] * g[j];
+}
+
+double nKn(const std::array<double, 9>& K, int dim, const std::array<double, 3>& n)
+{
+    double s = 0;
+    for (int i = 0; i < dim; i++)
+        for (int j = 0; j < dim; j++) s += n[i] * K[i * dim + j] * n[j];
+    return s;
+}
+
+ElementOps element_ops(const Mesh& M, int e, const Params& prm, const Rules& rules, bool want_interp)
+{
+    ElementOps O;
+    const int dim = M.dim, k = prm.k;
+    const auto& K = M.K[e];
+    CellBasis& B = O.basis;
+    B.dim = dim;
+    B.ex = exponents(dim, k + 1);
+    B.nR = (int)B.ex.size();
+    B.xc = centroid(M, e);
+    double hmax = 0;
+    for (int i = 0; i <= dim; i++)
+        for (int j = i + 1; j <= dim; j++) {
+            double s = 0;
+            for (int d = 0; d < 3; d++) s += std::pow(M.vx[M.el[e][i]][d] - M.vx[M.el[e][j]][d], 2);
+            hmax = std::max(hmax, std::sqrt(s));
+        }
+    B.hs = hmax;
+    O.nR = B.nR;
+    O.nC = (int)exponents(dim, k).size();
+    O.nF = dim + 1;
+    const QPts QE = element_points(M, e, rules.cell);
+    const int nq = (int)QE.w.size();
+    // Orthonormalise the scaled monomials (modified Gram-Schmidt, two sweeps).
+    {
+        Mat mv(B.nR, nq);
+        double m[64];
+        for (int q = 0; q < nq; q++) {
+            B.eval_monomials(QE.x[q].data(), m, nullptr);
+            for (int j = 0; j < B.nR; j++) mv(j, q) = m[j];
+        }
+        B.coef = Mat(B.nR, B.nR);
+        Mat vals(B.nR, nq);
+        for (int i = 0; i < B.nR; i++) {
+            B.coef(i, i) = 1.0;
+            for (int q = 0; q < nq; q++) vals(i, q) = mv(i, q);
+            for (int sweep = 0; sweep < 2; sweep++)
+                for (int j = 0; j < i; j++) {
+                    double ip = 0;
+                    for (int q = 0; q < nq; q++) ip += QE.w[q] * vals(i, q) * vals(j, q);
+                    for (int q = 0; q < nq; q++) vals(i, q) -= ip * vals(j, q);
+                    for (int c = 0; c <= j; c++) B.coef(i, c) -= ip * B.coef(j, c);
+                }
+            double n2 = 0;
+            for (int q = 0; q < nq; q++) n2 += QE.w[q] * vals(i, q) * vals(i, q);
+            const double inv = 1.0 / std::sqrt(n2);
+            for (int q = 0; q < nq; q++) vals(i, q) *= inv;
+            for (int c = 0; c <= i; c++) B.coef(i, c) *= inv;
+        }
+    }
+    const int nR = O.nR, nC = O.nC;
+    // Stiffness S and mean values.
+    Mat S(nR, nR);
+    std::vector<double> mean(nR, 0.0);
+    {
+        double v[64], g[192], kg[3];
+        for (int q = 0; q < nq; q++) {
+            B.eval(QE.x[q].data(), v, g);
+            for (int i = 0; i < nR; i++) {
+                mean[i] += QE.w[q] * v[i];
+                Kgrad(K, dim, &g[i * 3], kg);
+                for (int j = 0; j < nR; j++) S(i, j) += QE.w[q] * (kg[0] * g[j * 3] + kg[1] * g[j * 3 + 1] + kg[2] * g[j * 3 + 2]);
+            }
+        }
+    }
+    // Faces: points, bases, normals.
+    struct FaceData { QPts Q; FaceBasis FB; std::array<double, 3> n; double measure, diam; Mat cellvals; Mat gradn; };
+    std::vector<FaceData> FD(O.nF);
+    for (int lf = 0; lf < O.nF; lf++) {
+        const int f = M.ef[e][lf];
+        FaceData& D = FD[lf];
+        D.Q = face_points(M, f, rules.face, rules.face, D.measure, D.diam);
+        D.FB = face_basis(dim, k, D.Q);
+        D.n = outer_normal(M, e, f);
+        const int nfq = (int)D.Q.w.size();
+        D.cellvals = Mat(nR, nfq);
+        D.gradn = Mat(nR, nfq);
+        double v[64], g[192], kg[3];
+        for (int q = 0; q < nfq; q++) {
+            B.eval(D.Q.x[q].data(), v, g);
+            for (int i = 0; i < nR; i++) {
+                D.cellvals(i, q) = v[i];
+                Kgrad(K, dim, &g[i * 3], kg);
+                D.gradn(i, q) = kg[0] * D.n[0] + kg[1] * D.n[1] + kg[2] * D.n[2];
+            }
+        }
+    }
+    O.nf = FD[0].FB.nf;
+    const int nf = O.nf, nF = O.nF, nH = nC + nF * nf;
+    // Reconstruction: [S L; L^T 0] [P; lambda] = [rhs; mean condition]
+    Mat sys(nR + 1, nR + 1), rhs(nR + 1, nH);
+    for (int i = 0; i < nR; i++) {
+        for (int j = 0; j < nR; j++) sys(i, j) = S(i, j);
+        sys(i, nR) = mean[i];
+        sys(nR, i) = mean[i];
+    }
+    for (int i = 0; i < nR; i++) {
+        for (int j = 0; j < nC; j++) {
+            double v = S(i, j);  // hierarchical orthonormal basis: c_j = r_j
+            for (int lf = 0; lf < nF; lf++) {
+                const FaceData& D = FD[lf];
+                for (size_t q = 0; q < D.Q.w.size(); q++) v -= D.Q.w[q] * D.gradn(i, q) * D.cellvals(j, q);
+            }
+            rhs(i, j) = v;
+        }
+        for (int lf = 0; lf < nF; lf++) {
+            const FaceData& D = FD[lf];
+            for (int a = 0; a < nf; a++) {
+                double v = 0;
+                for (size_t q = 0; q < D.Q.w.size(); q++) v += D.Q.w[q] * D.gradn(i, q) * D.FB.vals(a, q);
+                rhs(i, nC + lf * nf + a) = v;
+            }
+        }
+    }
+    for (int j = 0; j < nC; j++) rhs(nR, j) = mean[j];
+    if (!solve(sys, rhs)) { O.ok = false; return O; }
+    O.P = Mat(nR, nH);
+    for (int i = 0; i < nR; i++)
+        for (int j = 0; j < nH; j++) O.P(i, j) = rhs(i, j);
+    // Consistency: P^T S P.
+    Mat Acons = matmul(transpose(O.P), matmul(S, O.P));
+    // Stabilisation (Diff_HHOElement.h:378-413).
+    Mat Astab(nH, nH);
+    Mat Dt(nC, nH);
+    for (int i = 0; i < nC; i++)
+        for (int j = 0; j < nH; j++) Dt(i, j) = O.P(i, j) - (i == j ? 1.0 : 0.0);
+    for (int lf = 0; lf < nF; lf++) {
+        const FaceData& D = FD[lf];
+        const int nfq = (int)D.Q.w.size();
+        Mat tr(nf, nR);  // M_F^{-1} (phi_a, r_j)_F
+        {
+            Mat m(nf, nR);
+            for (int a = 0; a < nf; a++)
+                for (int j = 0; j < nR; j++) {
+                    double s = 0;
+                    for (int q = 0; q < nfq; q++) s += D.Q.w[q] * D.FB.vals(a, q) * D.cellvals(j, q);
+                    m(a, j) = s;
+                }
+            tr = matmul(D.FB.mass_inv, m);
+        }
+        Mat Df = matmul(tr, O.P);
+        for (int a = 0; a < nf; a++) Df(a, nC + lf * nf + a) -= 1.0;
+        Mat trT(nf, nC);
+        for (int a = 0; a < nf; a++)
+            for (int j = 0; j < nC; j++) trT(a, j) = tr(a, j);
+        Mat diff = matmul(trT, Dt);
+        for (int a = 0; a < nf; a++)
+            for (int j = 0; j < nH; j++) diff(a, j) = Df(a, j) - diff(a, j);
+        const double coeff = nKn(K, dim, D.n) / D.diam;
+        Mat md = matmul(D.FB.mass, diff);
+        for (int i = 0; i < nH; i++)
+            for (int j = 0; j < nH; j++) {
+                double s = 0;
+                for (int a = 0; a < nf; a++) s += diff(a, i) * md(a, j);
+                Astab(i, j) += s * coeff;
+            }
+    }
+    O.A = Mat(nH, nH);
+    for (size_t i = 0; i < O.A.a.size(); i++) O.A.a[i] = Acons.a[i] + Astab.a[i];
+    // Static condensation.
+    const int nFF = nF * nf;
+    Mat Att(nC, nC), Atf(nC, nFF);
+    for (int i = 0; i < nC; i++) {
+        for (int j = 0; j < nC; j++) Att(i, j) = O.A(i, j);
+        for (int j = 0; j < nFF; j++) Atf(i, j) = O.A(i, nC + j);
+    }
+    // RHS (f, c_j)_T with a high-order rule.
+    O.bT.assign(nC, 0.0);
+    {
+        const QPts QR = element_points(M, e, rules.cell_rhs);
+        double v[64];
+        for (size_t q = 0; q < QR.w.size(); q++) {
+            B.eval(QR.x[q].data(), v, nullptr);
+            const double fv = source_value(prm, QR.x[q]);
+            for (int j = 0; j < nC; j++) O.bT[j] += QR.w[q] * fv * v[j];
+        }
+    }
+    Mat X = Atf;  // A_TT^{-1} A_TF
+    Mat rhsb(nC, 1);
+    for (int j = 0; j < nC; j++) rhsb(j, 0) = O.bT[j];
+    if (!solve(Att, X) || !solve(Att, rhsb)) { O.ok = false; return O; }
+    O.schur = Mat(nFF, nFF);
+    for (int i = 0; i < nFF; i++)
+        for (int j = 0; j < nFF; j++) {
+            double s = O.A(nC + i, nC + j);
+            for (int c = 0; c < nC; c++) s -= Atf(c, i) * X(c, j);
+            O.schur(i, j) = s;
+        }
+    O.bF.assign(nFF, 0.0);
+    for (int i = 0; i < nFF; i++) {
+        double s = 0;
+        for (int c = 0; c < nC; c++) s += Atf(c, i) * rhsb(c, 0);
+        O.bF[i] = -s;
+    }
+    if (want_interp) {
+        O.solve_cells = Mat(nC, nFF);
+        for (int i = 0; i < nC; i++)
+            for (int j = 0; j < nFF; j++) O.solve_cells(i, j) = -X(i, j);
+        Mat H(nH, nFF);
+        for (int i = 0; i < nC; i++)
+            for (int j = 0; j < nFF; j++) H(i, j) = O.solve_cells(i, j);
+        for (int j = 0; j < nFF; j++) H(nC + j, j) = 1.0;
+        O.interp = matmul(O.P, H);
+        O.A = Mat();
+    } else {
+        O.P = Mat();
+        O.A = Mat();
+    }
+    return O;
+}
+
+// ---------------------------------------------------------------------------
+// Parallel loop
+
+void parallel_for(size_t n, int threads, const std::function<void(size_t, size_t)>& body)
+{
+    if (threads <= 1 || n < 256) { body(0, n); return; }
+    std::vector<std::thread> th;
+    std::atomic<size_t> next{0};
+    const size_t chunk = std::max<size_t>(64, n / (threads * 16));
+    for (int t = 0; t < threads; t++)
+        th.emplace_back([&]() {
+            for (;;) {
+                const size_t s = next.fetch_add(chunk);
+                if (s >= n) break;
+                body(s, std::min(n, s + chunk));
+            }
+        });
+    for (auto& t : th) t.join();
+}
+
+// ---------------------------------------------------------------------------
+// Levels
+
+struct Level {
+    Mesh mesh;
+    std::vector<ElementOps> ops;
+    int n_rows = 0;
+    std::vector<int> A_rowptr, A_colidx;
+    std::vector<double> A_vals;
+    std::vector<double> b;
+    std::vector<int> P_rowptr, P_colidx;
+    std::vector<double> P_vals;
+    int P_cols = 0;
+};
+
+// Global condensed operator and RHS of one level.
+void assemble(Level& L, const Params& prm, int threads, bool want_rhs)
+{
+    Mesh& M = L.mesh;
+    const int nf = (int)L.ops[0].nf, nF = M.dim + 1;
+    const int nI = M.n_interior;
+    L.n_rows = nI * nf;
+    // Block pattern: faces of the elements of each interior face.
+    std::vector<std::array<int, 8>> cols(nI);
+    std::vector<int> ncols(nI, 0);
+    std::vector<int> face_of(nI);
+    for (size_t f = 0; f < M.fv.size(); f++)
+        if (M.number[f] >= 0) face_of[M.number[f]] = (int)f;
+    parallel_for(nI, threads, [&](size_t s, size_t e) {
+        for (size_t I = s; I < e; I++) {
+            const int f = face_of[I];
+            std::array<int, 8> c;
+            int nc = 0;
+            for (int side = 0; side < 2; side++) {
+                const int el = side == 0 ? M.fe1[f] : M.fe2[f];
+                for (int lf = 0; lf < nF; lf++) {
+                    const int g = M.number[M.ef[el][lf]];
+                    if (g < 0) continue;
+                    bool seen = false;
+                    for (int q = 0; q < nc; q++) seen |= c[q] == g;
+                    if (!seen) c[nc++] = g;
+                }
+            }
+            std::sort(c.begin(), c.begin() + nc);
+            cols[I] = c;
+            ncols[I] = nc;
+        }
+    });
+    L.A_rowptr.assign((size_t)L.n_rows + 1, 0);
+    for (int I = 0; I < nI; I++)
+        for (int a = 0; a < nf; a++) L.A_rowptr[(size_t)I * nf + a + 1] = ncols[I] * nf;
+    for (int r = 0; r < L.n_rows; r++) L.A_rowptr[r + 1] += L.A_rowptr[r];
+    L.A_colidx.assign(L.A_rowptr[L.n_rows], 0);
+    L.A_vals.assign(L.A_rowptr[L.n_rows], 0.0);
+    if (want_rhs) L.b.assign(L.n_rows, 0.0);
+    parallel_for(nI, threads, [&](size_t s, size_t e) {
+        for (size_t I = s; I < e; I++) {
+            const int f = face_of[I];
+            for (int a = 0; a < nf; a++) {
+                const size_t row = (size_t)I * nf + a;
+                int p = L.A_rowptr[row];
+                for (int q = 0; q < ncols[I]; q++)
+                    for (int bb = 0; bb < nf; bb++) L.A_colidx[p++] = cols[I][q] * nf + bb;
+            }
+            for (int side = 0; side < 2; side++) {
+                const int el = side == 0 ? M.fe1[f] : M.fe2[f];
+                const ElementOps& O = L.ops[el];
+                int lfi = -1;
+                for (int lf = 0; lf < nF; lf++)
+                    if (M.ef[el][lf] == f) lfi = lf;
+                for (int lf = 0; lf < nF; lf++) {
+                    const int g = M.number[M.ef[el][lf]];
+                    if (g < 0) continue;
+                    int q = 0;
+                    while (cols[I][q] != g) q++;
+                    for (int a = 0; a < nf; a++) {
+                        const size_t row = (size_t)I * nf + a;
+                        double* dst = &L.A_vals[L.A_rowptr[row] + q * nf];
+                        for (int bb = 0; bb < nf; bb++) dst[bb] += O.schur(lfi * nf + a, lf * nf + bb);
+                    }
+                }
+                if (want_rhs)
+                    for (int a = 0; a < nf; a++) L.b[(size_t)I * nf + a] += O.bF[lfi * nf + a];
+            }
+        }
+    });
+}
+
+// P (fine faces x coarse faces) of LevelForHHO::SetupProlongation_H with CellInterp_Trace.
+void prolongation(Level& F, const Level& C, const Params& prm, const Rules& rules, int threads)
+{
+    const Mesh& M = F.mesh;
+    const Mesh& MC = C.mesh;
+    const int dim = M.dim, nf = C.ops[0].nf, nFc = dim + 1;
+    const int nI = M.n_interior;
+    std::vector<int> face_of(nI);
+    for (size_t f = 0; f < M.fv.size(); f++)
+        if (M.number[f] >= 0) face_of[M.number[f]] = (int)f;
+    std::vector<std::array<int, 8>> cols(nI);
+    std::vector<int> ncols(nI, 0);
+    auto coarse_elems = [&](int f, int* ce, double* w, int& nce) {
+        const int e1 = M.fe1[f], e2 = M.fe2[f];
+        if (M.removed[f]) { ce[0] = M.coarser[e1]; w[0] = 1.0; nce = 1; return; }
+        const auto n1 = outer_normal(M, e1, f);
+        const auto n2 = outer_normal(M, e2, f);
+        const double k1 = nKn(M.K[e1], dim, n1), k2 = nKn(M.K[e2], dim, n2);
+        ce[0] = M.coarser[e1]; w[0] = k1 / (k1 + k2);
+        ce[1] = M.coarser[e2]; w[1] = k2 / (k1 + k2);
+        nce = 2;
+    };
+    parallel_for(nI, threads, [&](size_t s, size_t e) {
+        for (size_t I = s; I < e; I++) {
+            const int f = face_of[I];
+            int ce[2], nce;
+            double w[2];
+            coarse_elems(f, ce, w, nce);
+            std::array<int, 8> c;
+            int nc = 0;
+            for (int t = 0; t < nce; t++)
+                for (int lf = 0; lf < nFc; lf++) {
+                    const int g = MC.number[MC.ef[ce[t]][lf]];
+                    if (g < 0) continue;
+                    bool seen = false;
+                    for (int q = 0; q < nc; q++) seen |= c[q] == g;
+                    if (!seen) c[nc++] = g;
+                }
+            std::sort(c.begin(), c.begin() + nc);
+            cols[I] = c;
+            ncols[I] = nc;
+        }
+    });
+    F.P_cols = C.n_rows;
+    F.P_rowptr.assign((size_t)nI * nf + 1, 0);
+    for (int I = 0; I < nI; I++)
+        for (int a = 0; a < nf; a++) F.P_rowptr[(size_t)I * nf + a + 1] = ncols[I] * nf;
+    for (size_t r = 0; r < (size_t)nI * nf; r++) F.P_rowptr[r + 1] += F.P_rowptr[r];
+    F.P_colidx.assign(F.P_rowptr.back(), 0);
+    F.P_vals.assign(F.P_rowptr.back(), 0.0);
+    parallel_for(nI, threads, [&](size_t s, size_t e) {
+        for (size_t I = s; I < e; I++) {
+            const int f = face_of[I];
+            for (int a = 0; a < nf; a++) {
+                int p = F.P_rowptr[(size_t)I * nf + a];
+                for (int q = 0; q < ncols[I]; q++)
+                    for (int bb = 0; bb < nf; bb++) F.P_colidx[p++] = cols[I][q] * nf + bb;
+            }
+            int ce[2], nce;
+            double w[2];
+            coarse_elems(f, ce, w, nce);
+            double measure, diam;
+            const QPts Q = face_points(M, f, rules.face, rules.face, measure, diam);
+            const FaceBasis FB = face_basis(dim, prm.k, Q);
+            const int nfq = (int)Q.w.size();
+            for (int t = 0; t < nce; t++) {
+                const ElementOps& O = C.ops[ce[t]];
+                const int nR = O.nR;
+                // Trace of the coarse reconstruction basis on the fine face: M_f^{-1} (phi_a, r_j)_f
+                Mat m(nf, nR);
+                double v[64];
+                for (int q = 0; q < nfq; q++) {
+                    O.basis.eval(Q.x[q].data(), v, nullptr);
+                    for (int a = 0; a < nf; a++)
+                        for (int j = 0; j < nR; j++) m(a, j) += Q.w[q] * FB.vals(a, q) * v[j];
+                }
+                Mat tr = matmul(FB.mass_inv, m);
+                Mat contrib = matmul(tr, O.interp);  // nf x (nFc nf)
+                for (int lf = 0; lf < nFc; lf++) {
+                    const int g = MC.number[MC.ef[ce[t]][lf]];
+                    if (g < 0) continue;
+                    int q = 0;
+                    while (cols[I][q] != g) q++;
+                    for (int a = 0; a < nf; a++) {
+                        double* dst = &F.P_vals[F.P_rowptr[(size_t)I * nf + a] + q * nf];
+                        for (int bb = 0; bb < nf; bb++) dst[bb] += w[t] * contrib(a, lf * nf + bb);
+                    }
+                }
+            }
+        }
+    });
+}
+
+void set_coefficients(Mesh& M, const fhg_hho_params& p)
+{
+    const int dim = M.dim;
+    M.K.assign(M.el.size(), {0, 0, 0, 0, 0, 0, 0, 0, 0});
+    for (size_t e = 0; e < M.el.size(); e++) {
+        auto& K = M.K[e];
+        double kappa = 1.0;
+        const auto c = centroid(M, (int)e);
+        if (p.coefficient == FHG_HHO_CHECKERBOARD) {
+            const int m = p.checker_blocks > 0 ? p.checker_blocks : 4;
+            int parity = 0;
+            for (int d = 0; d < dim; d++) parity += std::min(m - 1, (int)std::floor(c[d] * m));
+            kappa = (parity % 2 == 0) ? 1.0 : p.contrast;
+        }
+        for (int i = 0; i < dim; i++) K[i * dim + i] = kappa;
+    }
+}
+
+}  // namespace
+
+// ===========================================================================
+
+struct fhg_hho {
+    std::vector<Level> levels;
+    std::string err;
+    int block_size = 0;
+};
+
+extern "C" {
+
+void fhg_hho_default_params(fhg_hho_params* p)
+{
+    std::memset(p, 0, sizeof(*p));
+    p->dim = 3;
+    p->n = 8;
+    p->k = 1;
+    p->max_coarse_rows = 1000;
+    p->max_levels = 0;
+    p->source = FHG_HHO_SOURCE_SINE;
+    p->coefficient = FHG_HHO_IDENTITY;
+    p->contrast = 1.0;
+    p->checker_blocks = 4;
+    p->threads = 0;
+}
+
+int fhg_hho_create(fhg_hho** out, const fhg_hho_params* p)
+{
+    if (!out || !p) return -1;
+    fhg_hho* H = new fhg_hho();
+    *out = H;
+    if ((p->dim != 2 && p->dim != 3) || p->n < 1 || p->k < 1 || p->k > 3) {
+        H->err = "unsupported dim/n/k (dim 2 or 3, n >= 1, k in 1..3)";
+        return -1;
+    }
+    const int threads = p->threads > 0 ? p->threads : (int)std::max(1u, std::thread::hardware_concurrency());
+    Params prm{p->dim, p->k, p->source == FHG_HHO_SOURCE_ONE ? 1 : 0};
+    Rules rules;
+    // cell: exact to degree 2k+2 (mass of P_{k+1}); face: degree 2k+1; RHS: high order.
+    const int dim = p->dim;
+    rules.cell = simplex_rule(dim, (2 * p->k + 2 + dim + 1) / 2 + 1);
+    rules.cell_rhs = simplex_rule(dim, 6);
+    rules.face = simplex_rule(dim - 1, (2 * p->k + 2 + dim) / 2 + 1);
+    // Level hierarchy: standard coarsening while the system is above max_coarse_rows
+    // (Multigrid::CoarseLevelNeeded, src/Solver/Multigrid/Multigrid.h:419-427) and n is even.
+    int n = p->n;
+    std::vector<int> ns;
+    ns.push_back(n);
+    const int nf = dim == 2 ? p->k + 1 : (p->k + 1) * (p->k + 2) / 2;
+    H->block_size = nf;
+    auto rows_of = [&](int m) -> long long {
+        const long long faces = dim == 2 ? (long long)3 * m * m + 2 * m : (long long)12 * m * m * m + 6 * m * m;
+        const long long bfaces = dim == 2 ? 4LL * m : 12LL * m * m;
+        return (faces - bfaces) * nf;
+    };
+    while (true) {
+        const int cur = ns.back();
+        if (p->max_levels > 0 && (int)ns.size() >= p->max_levels) break;
+        if (p->max_levels <= 0 && rows_of(cur) <= p->max_coarse_rows) break;
+        if (cur % 2 != 0 || cur / 2 < 1) break;
+        if (rows_of(cur / 2) == 0) break;
+        ns.push_back(cur / 2);
+    }
+    H->levels.resize(ns.size());
+    for (size_t l = 0; l < ns.size(); l++) {
+        H->levels[l].mesh = dim == 2 ? build_tri(ns[l]) : build_tet(ns[l]);
+        set_coefficients(H->levels[l].mesh, *p);
+    }
+    for (size_t l = 0; l + 1 < ns.size(); l++) link_coarse(H->levels[l].mesh, H->levels[l + 1].mesh);
+    for (size_t l = 0; l < ns.size(); l++) {
+        Level& L = H->levels[l];
+        const size_t ne = L.mesh.el.size();
+        L.ops.resize(ne);
+        std::atomic<int> bad{0};
+        const bool want_interp = l > 0;
+        parallel_for(ne, threads, [&](size_t s, size_t e) {
+            for (size_t i = s; i < e; i++) {
+                L.ops[i] = element_ops(L.mesh, (int)i, prm, rules, want_interp);
+                if (!L.ops[i].ok) bad++;
+            }
+        });
+        if (bad) { H->err = "singular local HHO system"; return -2; }
+        assemble(L, prm, threads, l == 0);
+        if (l > 0) prolongation(H->levels[l - 1], L, prm, rules, threads);
+        if (l > 0) {
+            // fine-level element data no longer needed
+            std::vector<ElementOps>().swap(H->levels[l - 1].ops);
+        }
+    }
+    std::vector<ElementOps>().swap(H->levels.back().ops);
+    return 0;
+}
+
+void fhg_hho_destroy(fhg_hho* h) { delete h; }
+
+const char* fhg_hho_last_error(const fhg_hho* h) { return h ? h->err.c_str() : "null handle"; }
+
+int fhg_hho_num_levels(const fhg_hho* h) { return h ? (int)h->levels.size() : 0; }
+
+int fhg_hho_block_size(const fhg_hho* h) { return h ? h->block_size : 0; }
+
+int fhg_hho_level(const fhg_hho* h, int l, int* n_rows, long long* nnz, const int** rowptr, const int** colidx,
+                  const double** vals)
+{
+    if (!h || l < 0 || l >= (int)h->levels.size()) return -1;
+    const Level& L = h->levels[l];
+    if (n_rows) *n_rows = L.n_rows;
+    if (nnz) *nnz = (long long)L.A_colidx.size();
+    if (rowptr) *rowptr = L.A_rowptr.data();
+    if (colidx) *colidx = L.A_colidx.data();
+    if (vals) *vals = L.A_vals.data();
+    return 0;
+}
+
+int fhg_hho_prolongation(const fhg_hho* h, int l, int* n_rows, int* n_cols, long long* nnz, const int** rowptr,
+                         const int** colidx, const double** vals)
+{
+    if (!h || l < 0 || l + 1 >= (int)h->levels.size()) return -1;
+    const Level& L = h->levels[l];
+    if (n_rows) *n_rows = L.n_rows;
+    if (n_cols) *n_cols = L.P_cols;
+    if (nnz) *nnz = (long long)L.P_colidx.size();
+    if (rowptr) *rowptr = L.P_rowptr.data();
+    if (colidx) *colidx = L.P_colidx.data();
+    if (vals) *vals = L.P_vals.data();
+    return 0;
+}
+
+int fhg_hho_rhs(const fhg_hho* h, const double** b)
+{
+    if (!h || h->levels.empty()) return -1;
+    *b = h->levels[0].b.data();
+    return 0;
+}
+
+}  // extern "C"

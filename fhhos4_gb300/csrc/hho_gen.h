@@ -1,0 +1,45 @@
+// C API of the host hierarchy producer (hho_gen.cpp): the condensed HHO face system and the
+// geometric multigrid hierarchy of fhhos4's in-house square/cube meshes. Arrays returned by
+// the accessors are owned by the handle and stay valid until fhg_hho_destroy.
+#ifndef FHG_HHO_GEN_H
+#define FHG_HHO_GEN_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FHG_HHO_SOURCE_SINE 0      /* f = d pi^2 prod sin(pi x_i), u = prod sin(pi x_i) */
+#define FHG_HHO_SOURCE_ONE 1       /* f = 1 */
+#define FHG_HHO_IDENTITY 0         /* K = I */
+#define FHG_HHO_CHECKERBOARD 1     /* isotropic, m^d checkerboard alternating 1 and `contrast` */
+
+typedef struct {
+    int dim;              /* 2: unit square, 2 triangles per cell; 3: unit cube, 6 tetrahedra per cube */
+    int n;                /* cells per direction */
+    int k;                /* face polynomial degree (1..3) */
+    int max_coarse_rows;  /* coarsen while the level has more rows (MatrixMaxSizeForCoarsestLevel) */
+    int max_levels;       /* > 0: fixed number of levels instead */
+    int source;           /* FHG_HHO_SOURCE_* */
+    int coefficient;      /* FHG_HHO_IDENTITY / FHG_HHO_CHECKERBOARD */
+    double contrast;
+    int checker_blocks;   /* m (4) */
+    int threads;          /* 0: all hardware threads */
+} fhg_hho_params;
+
+typedef struct fhg_hho fhg_hho;
+
+void fhg_hho_default_params(fhg_hho_params* p);
+int fhg_hho_create(fhg_hho** h, const fhg_hho_params* p);
+void fhg_hho_destroy(fhg_hho* h);
+const char* fhg_hho_last_error(const fhg_hho* h);
+int fhg_hho_num_levels(const fhg_hho* h);
+int fhg_hho_block_size(const fhg_hho* h);
+int fhg_hho_level(const fhg_hho* h, int level, int* n_rows, long long* nnz, const int** rowptr,
+                  const int** colidx, const double** vals);
+int fhg_hho_prolongation(const fhg_hho* h, int level, int* n_rows, int* n_cols, long long* nnz,
+                         const int** rowptr, const int** colidx, const double** vals);
+int fhg_hho_rhs(const fhg_hho* h, const double** b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,130 @@
+"""ctypes front end of the host hierarchy producer (csrc/hho_gen.cpp, libfhg_hho.so).
+
+``generate(dim, n, k, ...)`` returns the condensed HHO face operators ``As``, prolongations
+``Ps``, right-hand side ``b`` and block size of fhhos4's geometric multigrid hierarchy on the
+in-house unit-square (2 triangles per cell) or unit-cube (6 tetrahedra per cube) mesh.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+import scipy.sparse as sp
+
+from .build import HHO_LIB
+
+SOURCE = {"sine": 0, "one": 1}
+COEFFICIENT = {"identity": 0, "checkerboard": 1}
+
+
+class Params(C.Structure):
+    _fields_ = [("dim", C.c_int), ("n", C.c_int), ("k", C.c_int), ("max_coarse_rows", C.c_int),
+                ("max_levels", C.c_int), ("source", C.c_int), ("coefficient", C.c_int), ("contrast", C.c_double),
+                ("checker_blocks", C.c_int), ("threads", C.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(HHO_LIB):
+            raise ImportError(f"{HHO_LIB} is missing: build it with `python -m fhhos4_gb300.build`")
+        L = C.CDLL(HHO_LIB)
+        P = C.POINTER
+        L.fhg_hho_default_params.argtypes = [P(Params)]
+        L.fhg_hho_create.argtypes = [P(C.c_void_p), P(Params)]
+        L.fhg_hho_destroy.argtypes = [C.c_void_p]
+        L.fhg_hho_last_error.argtypes = [C.c_void_p]
+        L.fhg_hho_last_error.restype = C.c_char_p
+        L.fhg_hho_num_levels.argtypes = [C.c_void_p]
+        L.fhg_hho_block_size.argtypes = [C.c_void_p]
+        L.fhg_hho_level.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_longlong), P(P(C.c_int)),
+                                    P(P(C.c_int)), P(P(C.c_double))]
+        L.fhg_hho_prolongation.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int), P(C.c_longlong),
+                                           P(P(C.c_int)), P(P(C.c_int)), P(P(C.c_double))]
+        L.fhg_hho_rhs.argtypes = [C.c_void_p, P(P(C.c_double))]
+        _lib = L
+    return _lib
+
+
+def _arr(ptr, n, dtype):
+    if n == 0:
+        return np.zeros(0, dtype=dtype)
+    return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+
+
+class Hierarchy:
+    """Owns one generated hierarchy; arrays are copied out into numpy."""
+
+    def __init__(self, dim: int, n: int, k: int = 1, max_coarse_rows: int = 1000, max_levels: int = 0,
+                 source: str = "sine", coefficient: str = "identity", contrast: float = 1.0, checker_blocks: int = 4,
+                 threads: int = 0):
+        L = lib()
+        p = Params()
+        L.fhg_hho_default_params(C.byref(p))
+        p.dim, p.n, p.k = dim, n, k
+        p.max_coarse_rows, p.max_levels = max_coarse_rows, max_levels
+        p.source, p.coefficient = SOURCE[source], COEFFICIENT[coefficient]
+        p.contrast, p.checker_blocks, p.threads = contrast, checker_blocks, threads
+        self.h = C.c_void_p()
+        rc = L.fhg_hho_create(C.byref(self.h), C.byref(p))
+        if rc != 0:
+            msg = L.fhg_hho_last_error(self.h).decode()
+            L.fhg_hho_destroy(self.h)
+            raise RuntimeError(f"hierarchy generation failed: {msg}")
+        self.levels = L.fhg_hho_num_levels(self.h)
+        self.block_size = L.fhg_hho_block_size(self.h)
+
+    def A(self, l: int) -> sp.csr_matrix:
+        L = lib()
+        n, nnz = C.c_int(), C.c_longlong()
+        rp, ci, va = C.POINTER(C.c_int)(), C.POINTER(C.c_int)(), C.POINTER(C.c_double)()
+        L.fhg_hho_level(self.h, l, C.byref(n), C.byref(nnz), C.byref(rp), C.byref(ci), C.byref(va))
+        return sp.csr_matrix((_arr(va, nnz.value, np.float64), _arr(ci, nnz.value, np.int32),
+                              _arr(rp, n.value + 1, np.int32)), shape=(n.value, n.value))
+
+    def P(self, l: int) -> sp.csr_matrix:
+        L = lib()
+        nr, nc, nnz = C.c_int(), C.c_int(), C.c_longlong()
+        rp, ci, va = C.POINTER(C.c_int)(), C.POINTER(C.c_int)(), C.POINTER(C.c_double)()
+        L.fhg_hho_prolongation(self.h, l, C.byref(nr), C.byref(nc), C.byref(nnz), C.byref(rp), C.byref(ci),
+                               C.byref(va))
+        return sp.csr_matrix((_arr(va, nnz.value, np.float64), _arr(ci, nnz.value, np.int32),
+                              _arr(rp, nr.value + 1, np.int32)), shape=(nr.value, nc.value))
+
+    def b(self) -> np.ndarray:
+        L = lib()
+        p = C.POINTER(C.c_double)()
+        L.fhg_hho_rhs(self.h, C.byref(p))
+        n = self.A_rows(0)
+        return _arr(p, n, np.float64)
+
+    def A_rows(self, l: int) -> int:
+        n = C.c_int()
+        lib().fhg_hho_level(self.h, l, C.byref(n), None, None, None, None)
+        return n.value
+
+    def close(self):
+        if self.h:
+            lib().fhg_hho_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def generate(dim: int, n: int, k: int = 1, **kw):
+    """(As, Ps, b, block_size) of the hierarchy."""
+    H = Hierarchy(dim, n, k, **kw)
+    As = [H.A(l) for l in range(H.levels)]
+    Ps = [H.P(l) for l in range(H.levels - 1)]
+    b = H.b()
+    bs = H.block_size
+    H.close()
+    return As, Ps, b, bs
