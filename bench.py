@@ -1,0 +1,436 @@
+#!/usr/bin/env python3
+"""Headline benchmark of the fhhos4 solve phase on GB300.
+
+Workload: the reference's "plain method at scale" problem: 3D Poisson on the unit cube,
+64^3 cubes x 6 tetrahedra, HHO k=1 (3 DOFs per face, 9,363,456 unknowns), identity tensor,
+f = 3 pi^2 prod sin(pi x_i), homogeneous Dirichlet; FCG(1) preconditioned by one geometric
+multigrid V(1,1) cycle with block Gauss-Seidel (bgs/rbgs), coarsest direct solve, stop at
+1e-8 relative residual. The hierarchy is produced on the host by fhhos4_gb300.hho (the
+reference's discretisation, validated against it) and uploaded once.
+
+One step = one complete solve to 1e-8 with b resident in HBM. `value` = seconds per solve of
+the fastest method that reaches 1e-8 FP64 relative residual (FP32 V-cycle inside FP64 FCG);
+the plain FP64 GPU solve (the reference's method, same iteration count) is reported beside it.
+`e2e` = the same solve through the C ABI with host buffers (H2D of b, D2H of x inside the
+timed region).
+
+--impl reference times the reference's CPU algorithm (the oracle restatement, natural block-GS
+order, OpenMP row-parallel products) on the host cores, one step = one FCG iteration, scaled
+to the reference's iteration count.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "s to 1e-8 FP64 rel residual: learned+FP32 MG-FCG vs plain FP64; SpMV GB/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--dim", type=int, default=3)
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--k", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-iterations", type=int, default=2)
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------- distributed
+class Dist:
+    """One process per GPU (torchrun); replicas: every rank solves its own copy."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local_rank)
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during a timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        # "under load": samples within 40% of the highest power seen
+        pmax = max(power)
+        loaded = [s for s, p in zip(sm, power) if p >= 0.6 * pmax] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_max": pmax}
+
+
+def measured_hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def committed_traffic():
+    """dram bytes per launch of the profiled kernels (profiles/traffic.json), if committed."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+# --------------------------------------------------------------------------- workload
+def workload_config(args):
+    name = (f"{'3D tet' if args.dim == 3 else '2D tri'} {args.n}^{args.dim} HHO k={args.k} Poisson, "
+            "FCG(1)+geometric MG V(1,1) bgs/rbgs, tol 1e-8")
+    return {"workload": name, "dim": args.dim, "n": args.n, "k": args.k, "mesh": "stetra" if args.dim == 3 else "stri",
+            "krylov": "FCG(1)", "cycle": "V(1,1)", "smoothers": "bgs/rbgs (multicolour order)",
+            "coarse": "FP64 dense inverse of the coarsest operator",
+            "l2": "inputs larger than L2 (fine operator alone is > 1 GB)"}
+
+
+def generate(args):
+    from fhhos4_gb300 import hho
+    t0 = time.perf_counter()
+    As, Ps, b, bs = hho.generate(args.dim, args.n, args.k)
+    return As, Ps, b, bs, time.perf_counter() - t0
+
+
+def reference_iterations(args):
+    """Iterations of the reference (natural order) and of the reference in colour order, from the
+    committed reference histories when present."""
+    try:
+        z = np.load(os.path.join(ROOT, "tests", "golden", f"tet3d_n{args.n}_k{args.k}.npz"))
+        return len(z["hist_natural"]) - 1, len(z["hist_colour"]) - 1
+    except (OSError, KeyError):
+        return None, None
+
+
+def cpu_sample(As, Ps, b, bs, iters: int, threads: int):
+    """Seconds per FCG iteration of the oracle restatement (setup excluded) on `threads` cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.set_threads(threads)
+    x, hist, it, rc = O.fcgmg_solve(As, Ps, b, bs, maxit=iters, tol=0.0)
+    setup_s, iter_s = O.last_timing()
+    return iter_s / max(it, 1), setup_s, it
+
+
+def bytes_spmv(nnzb, nb_rows, n_in, n_out, bs, p, residual=False, add=False):
+    """Algorithmic bytes of one BSR product: values + column indices + row pointers + x read once
+    + y written (+ b or the added vector read)."""
+    b = nnzb * bs * bs * p + nnzb * 4 + (nb_rows + 1) * 4 + n_in * p + n_out * p
+    if residual or add:
+        b += n_out * p
+    return b
+
+
+def run_ours(args, dist: Dist):
+    import torch
+    from fhhos4_gb300 import _native as N
+
+    dev = dist.local_rank
+    torch.cuda.set_device(dev)
+    As, Ps, b, bs, gen_s = generate(args)
+    n0 = As[0].shape[0]
+    ctx = N.Context(dev)
+    t0 = time.perf_counter()
+    for l, A in enumerate(As):
+        ctx.set_level(l, bs, A)
+    for l, P in enumerate(Ps):
+        ctx.set_prolongation(l, P)
+    o = N.default_options()
+    o.vcycle_precision = N.PRECISION["fp32"]   # keeps FP64 and FP32 copies
+    o.autotune = 1
+    o.max_iterations = 200
+    ctx.setup(len(As), o)
+    setup_s = time.perf_counter() - t0
+    info0 = ctx.level_info(0)
+
+    b_dev = torch.from_numpy(b).to(f"cuda:{dev}")
+    x_dev = torch.empty_like(b_dev)
+    torch.cuda.synchronize()
+
+    def solve_device():
+        rc, hist, info = ctx.solve_device(b_dev.data_ptr(), x_dev.data_ptr(), o.max_iterations)
+        if rc != 0:
+            ctx._check(rc)
+        return hist, info
+
+    def true_residual():
+        x = x_dev.cpu().numpy()
+        r = ctx.apply(0, N.OP_RESIDUAL, x, b, n0)
+        return float(np.linalg.norm(r) / np.linalg.norm(b))
+
+    results = {}
+    launches = {}
+    clocks = {}
+    for prec in ("fp64", "fp32"):
+        ctx.set_vcycle_precision(prec)
+        for _ in range(args.warmup):
+            solve_device()
+        dist.barrier()
+        torch.cuda.synchronize()
+        sampler = ClockSampler(dev)
+        sampler.start()
+        k0 = ctx.kernel_launches()
+        times, iters = [], []
+        for _ in range(args.steps):
+            hist, info = solve_device()
+            times.append(info.solve_ms / 1e3)
+            iters.append(info.iterations)
+        torch.cuda.synchronize()
+        launches[prec] = ctx.kernel_launches() - k0
+        clocks[prec] = sampler.stop()
+        dist.barrier()
+        t_step = dist.max(float(np.mean(times)))
+        results[prec] = dict(s=t_step, iterations=iters[-1], history=hist, true_rel_residual=true_residual(),
+                             final=float(hist[-1]))
+
+    # End to end through the public C ABI with pinned host buffers (H2D b, solve, D2H x).
+    ctx.set_vcycle_precision("fp32")
+    b_host = torch.from_numpy(b).pin_memory()
+    x_host = torch.empty_like(b_host).pin_memory()
+    lib = N.load()
+    import ctypes as C
+
+    def solve_host():
+        info = N.SolveInfo()
+        rc = lib.fhg_solve(ctx.h, C.c_void_p(b_host.data_ptr()), C.c_void_p(x_host.data_ptr()), None, C.byref(info))
+        if rc != 0:
+            ctx._check(rc)
+        return info
+
+    for _ in range(args.warmup):
+        solve_host()
+    dist.barrier()
+    e2e_times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        solve_host()
+        e2e_times.append(time.perf_counter() - t)
+    e2e_s = dist.max(float(np.mean(e2e_times)))
+
+    # Per-kernel device timing on level 0 (CUDA events on the library's stream).
+    p32, p64 = 4, 8
+    info1 = ctx.level_info(1) if len(As) > 1 else None
+    nb0, nnzb0 = info0["block_rows"], info0["blocks"]
+    n1 = As[1].shape[0] if len(As) > 1 else 0
+    kernels = {}
+
+    def add_kernel(name, op, prec, bytes_):
+        ms = ctx.time_op(0, op, prec, warmup=3, reps=20)
+        kernels[name] = {"ms": ms, "bytes": bytes_, "gbs": bytes_ / (ms * 1e-3) / 1e9}
+
+    for prec, p in (("fp32", p32), ("fp64", p64)):
+        add_kernel(f"bsr_spmv_{prec}", N.OP_SPMV, prec, bytes_spmv(nnzb0, nb0, n0, n0, bs, p))
+        gs_bytes = bytes_spmv(nnzb0, nb0, n0, n0, bs, p) + nb0 * bs * bs * p + n0 * p   # + D^-1 + b
+        add_kernel(f"bsr_gs_sweep_{prec}", N.OP_GS_FORWARD, prec, gs_bytes)
+        if info1:
+            pb = info0["p_blocks"]
+            add_kernel(f"bsr_restrict_{prec}", N.OP_RESTRICT, prec, bytes_spmv(pb, n1 // bs, n0, n1, bs, p))
+            add_kernel(f"bsr_prolong_add_{prec}", N.OP_PROLONG_ADD, prec,
+                       bytes_spmv(pb, nb0, n1, n0, bs, p, add=True))
+    # Dominant kernel of the headline (FP32 V-cycle) solve: two GS sweeps per iteration on level 0.
+    ncol = info0["colours"]
+    dom = "bsr_gs_sweep_fp32"
+    hbm, hbm_kind = measured_hbm_peak()
+    traffic = committed_traffic().get(dom)
+    ach = kernels[dom]["gbs"]
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(ach / hbm, 4), "peak_kind": f"of {hbm_kind}",
+                "traffic": traffic,
+                "algorithmic_bytes_per_launch": kernels[dom]["bytes"] / max(ncol, 1),
+                "launches_per_sweep": ncol,
+                "spmv_fp64_frac": round(kernels["bsr_spmv_fp64"]["gbs"] / hbm, 4),
+                "spmv_fp32_frac": round(kernels["bsr_spmv_fp32"]["gbs"] / hbm, 4)}
+
+    cpu = None
+    ref_nat, ref_col = reference_iterations(args)
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        per_it, cpu_setup, k = cpu_sample(As, Ps, b, bs, args.cpu_sample_iterations, threads)
+        its = ref_nat or results["fp64"]["iterations"]
+        cpu = {"value": round(per_it * its, 3), "unit": "s", "cores": threads, "kind": "port",
+               "sample": (f"{k} FCG(1)+V(1,1) iterations of this {n0}-unknown solve by the oracle restatement "
+                          f"(natural block-GS order, OpenMP row-parallel products), {per_it:.3f} s/iteration "
+                          f"x {its} reference iterations; setup {cpu_setup:.1f} s excluded")}
+
+    clk = clocks["fp32"]
+    value = results["fp32"]["s"]
+    line = {
+        "metric": METRIC,
+        "value": round(value, 6),
+        "unit": "s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(value * 1e3, 3),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64 (Krylov) / f32 (V-cycle)",
+        "data": "synthetic: the reference's own 64^3 tetrahedral HHO system, generated on the host",
+        "config": dict(workload_config(args), parallelism=f"replicas x{dist.world}", method="FP32 V-cycle in FP64 FCG",
+                       unknowns=n0, levels=len(As), colours_level0=ncol),
+        "plain_fp64": {"s": round(results["fp64"]["s"], 6), "iterations": results["fp64"]["iterations"],
+                       "true_rel_residual": results["fp64"]["true_rel_residual"],
+                       "reference_iterations_colour_order": ref_col},
+        "fp32_vcycle": {"s": round(results["fp32"]["s"], 6), "iterations": results["fp32"]["iterations"],
+                        "true_rel_residual": results["fp32"]["true_rel_residual"]},
+        "speedup_vs_plain_fp64": round(results["fp64"]["s"] / value, 3),
+        "dofs_per_s": round(n0 * dist.world / value, 1),
+        "e2e": {"value": round(e2e_s, 6), "unit": "s", "h2d_bytes_per_step": int(n0 * 8),
+                "d2h_bytes_per_step": int(n0 * 8)},
+        "roofline": roofline,
+        "kernels": {k: {"ms": round(v["ms"], 4), "gbs": round(v["gbs"], 1), "frac": round(v["gbs"] / hbm, 4)}
+                    for k, v in kernels.items()},
+        "gpu_launches": int(launches["fp32"]),
+        "clocks": clk,
+        "setup_s": {"hierarchy_generation": round(gen_s, 2), "gpu_setup": round(setup_s, 2)},
+        "cpu_baseline": cpu,
+    }
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def run_reference(args, dist: Dist):
+    if dist.rank != 0:
+        return
+    As, Ps, b, bs, gen_s = generate(args)
+    threads = os.cpu_count() or 1
+    ref_nat, _ = reference_iterations(args)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.set_threads(threads)
+    if args.warmup > 0:
+        O.fcgmg_solve(As, Ps, b, bs, maxit=args.warmup, tol=0.0)
+    x, hist, it, rc = O.fcgmg_solve(As, Ps, b, bs, maxit=args.steps, tol=0.0)
+    setup_s, iter_s = O.last_timing()
+    per_it = iter_s / max(it, 1)
+    its = ref_nat if ref_nat else 35
+    value = per_it * its
+    n0 = As[0].shape[0]
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": "s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(per_it * 1e3, 2), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+        "data": "synthetic: the reference's own 64^3 tetrahedral HHO system, generated on the host",
+        "config": dict(workload_config(args), parallelism="host cores", unknowns=n0),
+        "cpu_baseline": {"value": round(value, 4), "unit": "s", "cores": threads, "kind": "port",
+                         "sample": (f"{it} FCG(1)+V(1,1) iterations (one per step) of the {n0}-unknown solve by the "
+                                    f"oracle restatement of the reference (natural block-GS order, OpenMP "
+                                    f"row-parallel products), {per_it:.3f} s/iteration x {its} reference iterations")},
+        "e2e": {"value": round(value, 4), "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "setup_s": {"hierarchy_generation": round(gen_s, 2), "oracle_setup": round(setup_s, 2)},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

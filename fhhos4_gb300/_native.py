@@ -35,7 +35,8 @@ OP_COARSE_SOLVE, OP_VCYCLE = 8, 9
 # Every symbol include/fhg.h declares.
 EXPORTS = ["fhg_default_options", "fhg_create", "fhg_destroy", "fhg_last_error", "fhg_set_level",
            "fhg_set_prolongation", "fhg_setup", "fhg_solve", "fhg_solve_device", "fhg_apply",
-           "fhg_time_op", "fhg_level_info", "fhg_get_permutation", "fhg_kernel_launches"]
+           "fhg_time_op", "fhg_set_vcycle_precision", "fhg_level_info", "fhg_get_permutation",
+           "fhg_kernel_launches"]
 
 
 class FhgError(RuntimeError):
@@ -82,7 +83,8 @@ def load(path: str = LIB):
     lib.fhg_solve.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, P(SolveInfo)]
     lib.fhg_solve_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, P(SolveInfo)]
     lib.fhg_apply.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
-    lib.fhg_time_op.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_double)]
+    lib.fhg_time_op.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_double)]
+    lib.fhg_set_vcycle_precision.argtypes = [C.c_void_p, C.c_int]
     lib.fhg_level_info.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_longlong), P(C.c_int), P(C.c_int),
                                    P(C.c_longlong)]
     lib.fhg_get_permutation.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
@@ -160,10 +162,13 @@ class Context:
         self._check(self.lib.fhg_apply(self.h, level, op, ptr(inp), ptr(auxa), ptr(out)))
         return out
 
-    def time_op(self, level: int, op: int, warmup: int = 3, reps: int = 20) -> float:
+    def time_op(self, level: int, op: int, precision: str = "fp64", warmup: int = 3, reps: int = 20) -> float:
         ms = C.c_double()
-        self._check(self.lib.fhg_time_op(self.h, level, op, warmup, reps, C.byref(ms)))
+        self._check(self.lib.fhg_time_op(self.h, level, op, PRECISION[precision], warmup, reps, C.byref(ms)))
         return ms.value
+
+    def set_vcycle_precision(self, precision: str):
+        self._check(self.lib.fhg_set_vcycle_precision(self.h, PRECISION[precision]))
 
     def level_info(self, level: int):
         nb, nbl, nc, lanes, pb = C.c_int(), C.c_longlong(), C.c_int(), C.c_int(), C.c_longlong()

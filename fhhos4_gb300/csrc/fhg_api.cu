@@ -671,7 +671,6 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
         int rc = build_graphs(ctx);
         if (rc) return rc;
     }
-    CK(cudaEventRecord(ctx->ev0, s));
     std::vector<double> hist(maxit + 1, 0.0);
     hist[0] = 1.0;
     double nr = 1.0;
@@ -695,17 +694,12 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
         if (std::isinf(nr)) { status = fail(ctx, FHG_ERR_DIVERGED, "divergence of the solver"); break; }
         if (std::isnan(nr)) { status = fail(ctx, FHG_ERR_NAN, "the residual is NaN."); break; }
     }
-    CK(cudaEventRecord(ctx->ev1, s));
-    CK(cudaEventSynchronize(ctx->ev1));
-    float ms = 0;
-    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     if (history)
         for (int k = 0; k <= maxit; k++) history[k] = k <= it ? hist[k] : 0.0;
     if (info) {
         info->iterations = it;
         info->status = status;
         info->normalized_residual = nr;
-        info->solve_ms = ms;
     }
     return status;
 }
@@ -985,13 +979,18 @@ int fhg_solve_device(fhg_ctx* ctx, const double* b_dev, double* x_dev, double* h
     if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
     CK(cudaSetDevice(ctx->device));
     Level& L0 = ctx->levels[0];
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
     // b' = Pi_0 b
     fhg::launch_permute<double>(L0.nb, L0.bs, L0.perm_d, b_dev, ctx->kb, true, ctx->stream);
     int rc = run_solve(ctx, history, info);
     // x = Pi_0^T x'
     fhg::launch_permute<double>(L0.nb, L0.bs, L0.perm_d, ctx->kx, x_dev, false, ctx->stream);
-    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    cudaError_t e = cudaEventSynchronize(ctx->ev1);
     if (rc == FHG_OK && e != cudaSuccess) return fail(ctx, FHG_ERR_CUDA, "solve: %s", cudaGetErrorString(e));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    if (info) info->solve_ms = ms;
     return rc;
 }
 
@@ -1010,50 +1009,64 @@ int fhg_solve(fhg_ctx* ctx, const double* b, double* x, double* history, fhg_sol
     return rc;
 }
 
-static int apply_device(fhg_ctx* ctx, int level, int op, double* in, double* aux, double* out)
+extern "C++" {
+template <class T>
+static int apply_device_t(fhg_ctx* ctx, int level, int op, T* in, T* aux, T* out)
 {
     // in/aux/out already in the permuted numbering on the device.
+    using V = LevelVecs<T>;
     Level& L = ctx->levels[level];
     cudaStream_t s = ctx->stream;
     const bool coarsest = level == ctx->nlevels - 1;
     switch (op) {
-    case FHG_OP_SPMV: fhg::launch_spmv<double>(L.A.v, fhg::kSpmvAssign, in, nullptr, out, s); break;
-    case FHG_OP_RESIDUAL: fhg::launch_spmv<double>(L.A.v, fhg::kSpmvResidual, in, aux, out, s); break;
+    case FHG_OP_SPMV: fhg::launch_spmv<T>(V::A(L), fhg::kSpmvAssign, in, nullptr, out, s); break;
+    case FHG_OP_RESIDUAL: fhg::launch_spmv<T>(V::A(L), fhg::kSpmvResidual, in, aux, out, s); break;
     case FHG_OP_RESTRICT:
         if (coarsest) return fail(ctx, FHG_ERR_INVALID_ARG, "no restriction on the coarsest level");
-        fhg::launch_spmv<double>(L.R.v, fhg::kSpmvAssign, in, nullptr, out, s);
+        fhg::launch_spmv<T>(V::R(L), fhg::kSpmvAssign, in, nullptr, out, s);
         break;
     case FHG_OP_PROLONG_ADD:
         if (coarsest) return fail(ctx, FHG_ERR_INVALID_ARG, "no prolongation on the coarsest level");
-        fhg::launch_spmv<double>(L.P.v, fhg::kSpmvAddTo, in, aux, out, s);
+        fhg::launch_spmv<T>(V::P(L), fhg::kSpmvAddTo, in, aux, out, s);
         break;
     case FHG_OP_GS_FORWARD:
     case FHG_OP_GS_BACKWARD:
     case FHG_OP_JACOBI: {
         if (coarsest) return fail(ctx, FHG_ERR_INVALID_ARG, "no smoother on the coarsest level");
-        CK(cudaMemcpyAsync(out, in, sizeof(double) * L.n, cudaMemcpyDeviceToDevice, s));
+        if (out != in) CK(cudaMemcpyAsync(out, in, sizeof(T) * L.n, cudaMemcpyDeviceToDevice, s));
         const int code = op == FHG_OP_GS_FORWARD ? FHG_SMOOTHER_BGS
                          : op == FHG_OP_GS_BACKWARD ? FHG_SMOOTHER_RBGS
                                                     : (ctx->opts.pre_smoother == FHG_SMOOTHER_BJ23 ? FHG_SMOOTHER_BJ23 : FHG_SMOOTHER_BJ);
-        smooth<double>(ctx, level, code, 1, aux, out);
-        break;
-    }
-    case FHG_OP_SYM_SPMV: {
-        if (level != 0) return fail(ctx, FHG_ERR_INVALID_ARG, "symmetric operator exists on level 0 only");
-        fhg::launch_spmv_dots(L.ahat_is_a ? L.A.v : L.Ahat.v, in, in, out, part(ctx, 4), s);
+        smooth<T>(ctx, level, code, 1, aux, out);
         break;
     }
     case FHG_OP_COARSE_SOLVE:
         if (!coarsest) return fail(ctx, FHG_ERR_INVALID_ARG, "coarse solve on level %d (coarsest is %d)", level, ctx->nlevels - 1);
-        fhg::launch_coarse<double>(L.n, L.cinv, in, out, s);
+        fhg::launch_coarse<T>(L.n, L.cinv, in, out, s);
         break;
-    case FHG_OP_VCYCLE:
-        if (level != 0) return fail(ctx, FHG_ERR_INVALID_ARG, "V-cycle starts on level 0");
-        precondition(ctx, in, out);
-        break;
-    default: return fail(ctx, FHG_ERR_INVALID_ARG, "unknown op %d", op);
+    default: return fail(ctx, FHG_ERR_INVALID_ARG, "op %d not available here", op);
     }
     return FHG_OK;
+}
+
+}  // extern "C++"
+
+static int apply_device(fhg_ctx* ctx, int level, int op, double* in, double* aux, double* out)
+{
+    Level& L = ctx->levels[level];
+    cudaStream_t s = ctx->stream;
+    if (op == FHG_OP_SYM_SPMV) {
+        if (level != 0) return fail(ctx, FHG_ERR_INVALID_ARG, "symmetric operator exists on level 0 only");
+        fhg::launch_spmv_dots(L.ahat_is_a ? L.A.v : L.Ahat.v, in, in, out, part(ctx, 4), s);
+        return FHG_OK;
+    }
+    if (op == FHG_OP_VCYCLE) {
+        if (level != 0) return fail(ctx, FHG_ERR_INVALID_ARG, "V-cycle starts on level 0");
+        precondition(ctx, in, out);
+        return FHG_OK;
+    }
+    if (op < 0 || op > FHG_OP_VCYCLE) return fail(ctx, FHG_ERR_INVALID_ARG, "unknown op %d", op);
+    return apply_device_t<double>(ctx, level, op, in, aux, out);
 }
 
 static void op_levels(int level, int op, int* in_level, int* out_level)
@@ -1105,35 +1118,36 @@ int fhg_apply(fhg_ctx* ctx, int level, int op, const double* in, const double* a
     return rc;
 }
 
-int fhg_time_op(fhg_ctx* ctx, int level, int op, int warmup, int reps, double* avg_ms)
+extern "C++" {
+template <class T>
+static int time_op_t(fhg_ctx* ctx, int level, int op, int warmup, int reps, double* avg_ms)
 {
-    if (!ctx || !avg_ms || reps <= 0) return FHG_ERR_INVALID_ARG;
-    if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
-    if (level < 0 || level >= ctx->nlevels) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d out of range", level);
-    CK(cudaSetDevice(ctx->device));
     int li, lo;
     op_levels(level, op, &li, &lo);
     if (lo >= ctx->nlevels || li >= ctx->nlevels) return fail(ctx, FHG_ERR_INVALID_ARG, "operator leaves the hierarchy");
-    Level& L = ctx->levels[level];
     const size_t mx = (size_t)std::max(ctx->levels[li].n, ctx->levels[lo].n);
-    double* t = nullptr;
+    T* t = nullptr;
     int rc = dalloc(ctx, &t, 3 * mx);
     if (rc) return rc;
-    double *in = t, *aux = t + mx, *out = t + 2 * mx;
+    T *in = t, *aux = t + mx, *out = t + 2 * mx;
     cudaStream_t s = ctx->stream;
-    // Inputs: the level's last V-cycle vectors (finite, representative values).
-    CK(cudaMemcpyAsync(in, ctx->levels[li].x, sizeof(double) * ctx->levels[li].n, cudaMemcpyDeviceToDevice, s));
+    // Inputs: the level's last V-cycle vectors (finite, representative values), converted.
     const int la = op == FHG_OP_PROLONG_ADD ? lo : li;
-    CK(cudaMemcpyAsync(aux, ctx->levels[la].b, sizeof(double) * ctx->levels[la].n, cudaMemcpyDeviceToDevice, s));
+    if (sizeof(T) == sizeof(double)) {
+        CK(cudaMemcpyAsync(in, ctx->levels[li].x, sizeof(T) * ctx->levels[li].n, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(aux, ctx->levels[la].b, sizeof(T) * ctx->levels[la].n, cudaMemcpyDeviceToDevice, s));
+    } else {
+        fhg::launch_convert<double, float>(ctx->levels[li].n, ctx->levels[li].x, (float*)in, s);
+        fhg::launch_convert<double, float>(ctx->levels[la].n, ctx->levels[la].b, (float*)aux, s);
+    }
     auto one = [&]() -> int {
         if (op == FHG_OP_GS_FORWARD || op == FHG_OP_GS_BACKWARD) {
             if (level == ctx->nlevels - 1) return fail(ctx, FHG_ERR_INVALID_ARG, "no smoother on the coarsest level");
-            smooth<double>(ctx, level, op == FHG_OP_GS_FORWARD ? FHG_SMOOTHER_BGS : FHG_SMOOTHER_RBGS, 1, aux, in);
+            smooth<T>(ctx, level, op == FHG_OP_GS_FORWARD ? FHG_SMOOTHER_BGS : FHG_SMOOTHER_RBGS, 1, aux, in);
             return FHG_OK;
         }
-        return apply_device(ctx, level, op, in, aux, out);
+        return apply_device_t<T>(ctx, level, op, in, aux, out);
     };
-    (void)L;
     for (int w = 0; w < warmup && rc == FHG_OK; w++) rc = one();
     if (rc == FHG_OK) {
         CK(cudaEventRecord(ctx->ev0, s));
@@ -1148,6 +1162,56 @@ int fhg_time_op(fhg_ctx* ctx, int level, int op, int warmup, int reps, double* a
     ctx->allocations.erase(std::find(ctx->allocations.begin(), ctx->allocations.end(), (void*)t));
     cudaFree(t);
     return rc;
+}
+
+}  // extern "C++"
+
+int fhg_time_op(fhg_ctx* ctx, int level, int op, int precision, int warmup, int reps, double* avg_ms)
+{
+    if (!ctx || !avg_ms || reps <= 0) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
+    if (level < 0 || level >= ctx->nlevels) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d out of range", level);
+    CK(cudaSetDevice(ctx->device));
+    if (op == FHG_OP_SYM_SPMV || op == FHG_OP_VCYCLE) {
+        if (precision != FHG_PREC_FP64) return fail(ctx, FHG_ERR_INVALID_ARG, "op %d is timed in FP64 only", op);
+        const size_t n0 = ctx->levels[0].n;
+        double* t = nullptr;
+        int rc = dalloc(ctx, &t, 2 * n0);
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(t, ctx->kr, sizeof(double) * n0, cudaMemcpyDeviceToDevice, ctx->stream));
+        for (int w = 0; w < warmup && rc == FHG_OK; w++) rc = apply_device(ctx, level, op, t, nullptr, t + n0);
+        CK(cudaEventRecord(ctx->ev0, ctx->stream));
+        for (int r = 0; r < reps && rc == FHG_OK; r++) rc = apply_device(ctx, level, op, t, nullptr, t + n0);
+        CK(cudaEventRecord(ctx->ev1, ctx->stream));
+        CK(cudaEventSynchronize(ctx->ev1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        *avg_ms = ms / reps;
+        ctx->allocations.erase(std::find(ctx->allocations.begin(), ctx->allocations.end(), (void*)t));
+        cudaFree(t);
+        return rc;
+    }
+    if (precision == FHG_PREC_FP32) {
+        if (!ctx->levels[0].A32.vals) return fail(ctx, FHG_ERR_NOT_READY, "FP32 operators were not built at setup");
+        return time_op_t<float>(ctx, level, op, warmup, reps, avg_ms);
+    }
+    return time_op_t<double>(ctx, level, op, warmup, reps, avg_ms);
+}
+
+int fhg_set_vcycle_precision(fhg_ctx* ctx, int precision)
+{
+    if (!ctx) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
+    if (precision != FHG_PREC_FP64 && precision != FHG_PREC_FP32) return fail(ctx, FHG_ERR_INVALID_ARG, "unknown precision");
+    if (precision == FHG_PREC_FP32 && !ctx->levels[0].A32.vals)
+        return fail(ctx, FHG_ERR_NOT_READY, "FP32 operators were not built: set up with FHG_PREC_FP32");
+    if (ctx->opts.vcycle_precision != precision) {
+        for (int g = 0; g < 2; g++)
+            if (ctx->graph[g]) { cudaGraphExecDestroy(ctx->graph[g]); ctx->graph[g] = nullptr; }
+        ctx->graphs_built = 0;
+        ctx->opts.vcycle_precision = precision;
+    }
+    return FHG_OK;
 }
 
 int fhg_level_info(const fhg_ctx* ctx, int level, int* n_block_rows, long long* n_blocks, int* n_colours, int* lanes,

@@ -125,9 +125,15 @@ int fhg_solve_device(fhg_ctx* ctx, const double* b_dev, double* x_dev, double* h
 #define FHG_OP_VCYCLE 9       /* out = one V-cycle from zero on rhs in (Preconditioner.h:162-167), level 0 */
 int fhg_apply(fhg_ctx* ctx, int level, int op, const double* in, const double* aux, double* out);
 
-/* Device timing of one operator (same ops; vectors left in device memory): average ms per
- * launch over `reps` back-to-back launches after `warmup`, CUDA events on the context stream. */
-int fhg_time_op(fhg_ctx* ctx, int level, int op, int warmup, int reps, double* avg_ms);
+/* Device timing of one operator (same ops; vectors left in device memory) in FHG_PREC_FP64 or
+ * FHG_PREC_FP32 (the V-cycle copies): average ms per application over `reps` back-to-back
+ * applications after `warmup`, CUDA events on the context stream. A block-GS sweep is all of
+ * its colour launches. */
+int fhg_time_op(fhg_ctx* ctx, int level, int op, int precision, int warmup, int reps, double* avg_ms);
+
+/* Switch the V-cycle precision of a set-up context (FP32 needs a setup with FHG_PREC_FP32,
+ * which keeps both copies). The outer Krylov iteration stays FP64. */
+int fhg_set_vcycle_precision(fhg_ctx* ctx, int precision);
 
 /* Sizes of level `level` after setup: block rows, stored blocks of A, colours, lanes per block row
  * of the A operator, stored blocks of P (0 on the coarsest). */
@@ -137,7 +143,7 @@ int fhg_level_info(const fhg_ctx* ctx, int level, int* n_block_rows, long long* 
 /* The colour permutation of `level` after setup: perm[new_block_row] = given_block_row. */
 int fhg_get_permutation(const fhg_ctx* ctx, int level, int* perm);
 
-/* Number of kernels this context has launched since creation (its own kernels only). */
+/* Number of kernels this library has launched in this process (graph replays included). */
 long long fhg_kernel_launches(const fhg_ctx* ctx);
 
 #ifdef __cplusplus

@@ -25,12 +25,44 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static double now_s(void)
+{
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return t.tv_sec + 1e-9 * t.tv_nsec;
+}
+
+void orc_set_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+int orc_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
 
 /* ------------------------------------------------------------------------- */
 /* Sparse products                                                           */
 
+/* Rows are independent: with OpenMP (the reference's Eigen built with -fopenmp parallelises
+ * row-major SpMV the same way, SparseDenseProduct.h:39-58) each row keeps its sequential sum. */
 void orc_spmv(const orc_csr* A, const double* x, double* y)
 {
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < A->n_rows; i++) {
         double t = 0.0;
         for (int p = A->rowptr[i]; p < A->rowptr[i + 1]; p++)
@@ -41,6 +73,7 @@ void orc_spmv(const orc_csr* A, const double* x, double* y)
 
 void orc_residual(const orc_csr* A, const double* b, const double* x, double* r)
 {
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < A->n_rows; i++) {
         double t = 0.0;
         for (int p = A->rowptr[i]; p < A->rowptr[i + 1]; p++)
@@ -382,10 +415,19 @@ static double dot(const double* a, const double* b, int n)
     return s;
 }
 
+static double g_setup_s = 0.0, g_iter_s = 0.0;
+
+void orc_last_timing(double* setup_s, double* iterations_s)
+{
+    *setup_s = g_setup_s;
+    *iterations_s = g_iter_s;
+}
+
 int orc_fcgmg_solve(int nlevels, int bs, const orc_csr* A, const orc_csr* P,
                     const double* b, double* x, const orc_options* opt,
                     double* history, int* iterations)
 {
+    const double t0 = now_s();
     orc_mg mg;
     memset(&mg, 0, sizeof(mg));
     mg.nlevels = nlevels; mg.bs = bs; mg.A = A; mg.P = P; mg.opt = opt;
@@ -412,6 +454,8 @@ int orc_fcgmg_solve(int nlevels, int bs, const orc_csr* A, const orc_csr* P,
     }
     if (ldlt_setup(&mg.coarse, &A[nlevels - 1])) rc = 3;
 
+    const double t1 = now_s();
+    g_setup_s = t1 - t0;
     int n = A[0].n_rows;
     double* r = (double*)malloc(sizeof(double) * (size_t)n);
     double* z = (double*)malloc(sizeof(double) * (size_t)n);
@@ -475,6 +519,7 @@ int orc_fcgmg_solve(int nlevels, int bs, const orc_csr* A, const orc_csr* P,
         }
     }
     *iterations = it;
+    g_iter_s = now_s() - t1;
 
     free(r); free(z); free(d); free(Ad); free(dp); free(Adp);
     for (int l = 0; l + 1 < nlevels; l++) {

@@ -63,6 +63,13 @@ int orc_fcgmg_solve(int nlevels, int bs, const orc_csr* A, const orc_csr* P,
                     const double* b, double* x, const orc_options* opt,
                     double* history, int* iterations);
 
+/* Wall seconds of the last orc_fcgmg_solve: setup (transposes, diagonal LU, coarse LDL^T)
+ * and the Krylov iterations. */
+void orc_last_timing(double* setup_s, double* iterations_s);
+/* OpenMP threads of the row-parallel products (1 without OpenMP). */
+void orc_set_threads(int n);
+int orc_max_threads(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -134,6 +134,21 @@ def colour_permutation(colour, ncolours):
     return perm
 
 
+def set_threads(n: int):
+    lib().orc_set_threads(C.c_int(n))
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())
+
+
+def last_timing():
+    """(setup seconds, iteration seconds) of the last fcgmg_solve."""
+    s, i = C.c_double(), C.c_double()
+    lib().orc_last_timing(C.byref(s), C.byref(i))
+    return s.value, i.value
+
+
 def fcgmg_solve(As, Ps, b, bs, pre="bgs", post="rbgs", krylov="fcg", tol=1e-8, maxit=200,
                 pre_iterations=1, post_iterations=1):
     """Returns (x, history, iterations, status)."""
