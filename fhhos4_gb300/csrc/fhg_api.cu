@@ -489,19 +489,24 @@ template <> struct LevelVecs<float> {
     static const float* dinv(Level& L) { return L.dinv32; }
 };
 
+// `from_zero`: x holds zeros on entry (the pre-smoothing of a V-cycle), so the first GS sweep
+// skips the blocks that multiply not-yet-updated entries.
 template <class T>
-void smooth(fhg_ctx* ctx, int l, int code, int iters, const T* b, T* x)
+void smooth(fhg_ctx* ctx, int l, int code, int iters, const T* b, T* x, bool from_zero = false)
 {
     Level& L = ctx->levels[l];
     using V = LevelVecs<T>;
     cudaStream_t s = ctx->stream;
     for (int it = 0; it < iters; it++) {
+        const bool zero = from_zero && it == 0;
         if (code == FHG_SMOOTHER_BGS) {
             for (int c = 0; c < L.ncolours; c++)
-                fhg::launch_gs<T>(V::A(L), L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s);
+                fhg::launch_gs<T>(V::A(L), L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s, 0,
+                                  zero ? L.colour_start[c + 1] : 0x7fffffff);
         } else if (code == FHG_SMOOTHER_RBGS) {
             for (int c = L.ncolours - 1; c >= 0; c--)
-                fhg::launch_gs<T>(V::A(L), L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s);
+                fhg::launch_gs<T>(V::A(L), L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s,
+                                  zero ? L.colour_start[c] : 0, 0x7fffffff);
         } else {
             const T omega = code == FHG_SMOOTHER_BJ23 ? T(2.0 / 3.0) : T(ctx->opts.omega);
             T* tmp = V::r(L);
@@ -523,8 +528,11 @@ void vcycle(fhg_ctx* ctx, int l, const T* b, T* x)
         return;
     }
     Level& C = ctx->levels[l + 1];
-    cudaMemsetAsync(x, 0, sizeof(T) * (size_t)L.n, s);
-    smooth<T>(ctx, l, ctx->opts.pre_smoother, ctx->opts.pre_iterations, b, x);
+    // A zero-start GS sweep writes every entry before any is read: no clearing needed then.
+    const int pre = ctx->opts.pre_smoother;
+    const bool gs_pre = (pre == FHG_SMOOTHER_BGS || pre == FHG_SMOOTHER_RBGS) && ctx->opts.pre_iterations > 0;
+    if (!gs_pre) cudaMemsetAsync(x, 0, sizeof(T) * (size_t)L.n, s);
+    smooth<T>(ctx, l, pre, ctx->opts.pre_iterations, b, x, gs_pre);
     fhg::launch_spmv<T>(V::A(L), fhg::kSpmvResidual, x, b, V::r(L), s);
     fhg::launch_spmv<T>(V::R(L), fhg::kSpmvAssign, V::r(L), nullptr, V::b(C), s);
     vcycle<T>(ctx, l + 1, V::b(C), V::x(C));
@@ -557,13 +565,24 @@ void fcg_iteration(fhg_ctx* ctx, int p)
     double* dp = ctx->kz[1 - p];
     double* Ad = ctx->kAd[p];
     double* Adp = ctx->kAd[1 - p];
-    precondition(ctx, ctx->kr, z);
-    fhg::launch_dot(n, z, Adp, part(ctx, 0), s);
-    fhg::launch_fcg_direction(n, z, dp, part(ctx, 0), ctx->scal + 1, z, s);
-    const BsrView<double>& Ah = ctx->levels[0].ahat_is_a ? ctx->levels[0].A.v : ctx->levels[0].Ahat.v;
+    Level& L0 = ctx->levels[0];
+    const bool fp32 = ctx->opts.vcycle_precision == FHG_PREC_FP32;
+    if (fp32) {
+        // V-cycle on the FP32 copy of r written by the previous step; z stays FP32 and is
+        // widened inside the direction update.
+        vcycle<float>(ctx, 0, L0.b32, L0.x32);
+        fhg::launch_dot_mixed(n, L0.x32, Adp, part(ctx, 0), s);
+        fhg::launch_fcg_direction_mixed(n, L0.x32, dp, part(ctx, 0), ctx->scal + 1, z, s);
+    } else {
+        precondition(ctx, ctx->kr, z);
+        fhg::launch_dot(n, z, Adp, part(ctx, 0), s);
+        fhg::launch_fcg_direction(n, z, dp, part(ctx, 0), ctx->scal + 1, z, s);
+    }
+    const BsrView<double>& Ah = L0.ahat_is_a ? L0.A.v : L0.Ahat.v;
     fhg::launch_spmv_dots(Ah, z, ctx->kr, Ad, part(ctx, 1), s);
     // parts 1 = d.Ad, 2 = r.d
-    fhg::launch_krylov_step(n, ctx->kx, ctx->kr, z, Ad, part(ctx, 2), part(ctx, 1), ctx->scal + 1, part(ctx, 3), s);
+    fhg::launch_krylov_step(n, ctx->kx, ctx->kr, z, Ad, part(ctx, 2), part(ctx, 1), ctx->scal + 1, part(ctx, 3), s,
+                            fp32 ? L0.b32 : nullptr);
     fhg::launch_finalize_norm(part(ctx, 3), ctx->scal + 0, ctx->scal + 2, ctx->hist_d, ctx->counter_d,
                               ctx->opts.max_iterations + 1, s);
     cudaMemcpyAsync(ctx->nr_host, ctx->scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s);
@@ -661,6 +680,8 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
     CK(cudaMemcpyAsync(ctx->scal + 1, init, sizeof(init), cudaMemcpyHostToDevice, s));
     const int one = 1;
     CK(cudaMemcpyAsync(ctx->counter_d, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+    if (ctx->opts.krylov == FHG_KRYLOV_FCG && ctx->opts.vcycle_precision == FHG_PREC_FP32)
+        fhg::launch_convert<double, float>(n, ctx->kr, L0.b32, s);  // FP32 copy of r = b
     if (ctx->opts.krylov == FHG_KRYLOV_CG) {
         // z = M r; d = 0 so that the first direction is z; rz = r.z
         precondition(ctx, ctx->kr, ctx->kz[0]);

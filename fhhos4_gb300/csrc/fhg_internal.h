@@ -39,9 +39,10 @@ enum SpmvMode { kSpmvAssign = 0, kSpmvResidual = 1, kSpmvAddTo = 2 };
 
 template <class T>
 void launch_spmv(const BsrView<T>& A, int mode, const T* x, const T* aux, T* y, cudaStream_t s);
+// col_lo/col_hi: block columns outside [col_lo, col_hi) are skipped (zero-start sweeps).
 template <class T>
 void launch_gs(const BsrView<T>& A, int row0, int row1, const T* dinv, long long dld,
-               const T* b, T* x, cudaStream_t s);
+               const T* b, T* x, cudaStream_t s, int col_lo = 0, int col_hi = 0x7fffffff);
 template <class T>
 void launch_jacobi(const BsrView<T>& A, const T* dinv, long long dld, T omega, const T* b,
                    const T* xold, T* xnew, cudaStream_t s);
@@ -59,9 +60,14 @@ void launch_fcg_direction(long long n, const double* z, const double* dp, const 
                           const double* dadp, double* d, cudaStream_t s);
 // FCG/CG step: alpha = num / den with num, den reduced from partials (num_off, den_off offsets);
 // x += alpha d; r -= alpha Ad; partials_rr = per-CTA sum r_i^2; *den_out = den (if not null).
+// r32 (optional): FP32 copy of the updated r, the next V-cycle's right-hand side.
 void launch_krylov_step(long long n, double* x, double* r, const double* d, const double* Ad,
                         const double* partials_num, const double* partials_den, double* den_out,
-                        double* partials_rr, cudaStream_t s);
+                        double* partials_rr, cudaStream_t s, float* r32 = nullptr);
+// FP32 preconditioned residual z into the FP64 FCG: partials of z.Adp; d = z - s dp.
+void launch_dot_mixed(long long n, const float* a, const double* b, double* partials, cudaStream_t s);
+void launch_fcg_direction_mixed(long long n, const float* z, const double* dp, const double* partials_zadp,
+                                const double* dadp, double* d, cudaStream_t s);
 // ||r|| / ||b||: reduces partials_rr, divides by *bnorm, writes *nr_out and hist[*counter],
 // then ++*counter.
 void launch_finalize_norm(const double* partials_rr, const double* bnorm, double* nr_out,

@@ -106,12 +106,16 @@ __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int nbr, const int* __res
 
 // One colour of block Gauss-Seidel: rows [row0, row1) are mutually uncoupled.
 // x_i <- D_i^{-1} (b_i - sum_{j != i} A_ij x_j)
+// Columns outside [col_lo, col_hi) are skipped: in a sweep that starts from x = 0 they hold
+// zeros not yet overwritten (later colours of a forward sweep, earlier ones of a backward
+// sweep), so skipping them changes no bit of the result and saves their loads. Block columns
+// are sorted, so the skipped ones form a head and a tail of each row.
 template <class T, int BS, int G>
 __global__ void __launch_bounds__(kThreads) k_bsr_gs(int row0, int row1, const int* __restrict__ rowptr,
                                                      const int* __restrict__ colidx,
                                                      const T* __restrict__ vals, long long ld,
                                                      const T* __restrict__ dinv, long long dld,
-                                                     const T* __restrict__ b, T* x)
+                                                     const T* __restrict__ b, T* x, int col_lo, int col_hi)
 {
     const int lane = threadIdx.x & (G - 1);
     const int row = row0 + (int)(((long long)blockIdx.x * kThreads + threadIdx.x) / G);
@@ -122,7 +126,8 @@ __global__ void __launch_bounds__(kThreads) k_bsr_gs(int row0, int row1, const i
         const int p1 = rowptr[row + 1];
         for (int p = rowptr[row] + lane; p < p1; p += G) {
             const int col = colidx[p];
-            if (col == row) continue;
+            if (col >= col_hi) break;
+            if (col == row || col < col_lo) continue;
             T xv[BS];
 #pragma unroll
             for (int c = 0; c < BS; c++) xv[c] = x[(long long)col * BS + c];
@@ -289,6 +294,28 @@ __global__ void __launch_bounds__(kReduceThreads) k_dot(long long n, const doubl
     if (threadIdx.x == 0) partials[blockIdx.x] = v;
 }
 
+__global__ void __launch_bounds__(kReduceThreads) k_dot_mixed(long long n, const float* __restrict__ a,
+                                                              const double* __restrict__ b, double* __restrict__ partials)
+{
+    __shared__ double sh[33];
+    double v = 0.0;
+    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads)
+        v = fma((double)a[i], b[i], v);
+    v = block_sum(v, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v;
+}
+
+__global__ void __launch_bounds__(kReduceThreads) k_fcg_direction_mixed(long long n, const float* __restrict__ z,
+                                                                        const double* __restrict__ dp,
+                                                                        const double* __restrict__ partials,
+                                                                        const double* __restrict__ dadp, double* __restrict__ d)
+{
+    __shared__ double sh[33];
+    const double s = reduce_partials(partials, sh) / *dadp;
+    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads)
+        d[i] = (double)z[i] - s * dp[i];
+}
+
 __global__ void __launch_bounds__(kReduceThreads) k_fcg_direction(long long n, const double* z, const double* __restrict__ dp,
                                                                   const double* __restrict__ partials,
                                                                   const double* __restrict__ dadp, double* d)
@@ -302,7 +329,8 @@ __global__ void __launch_bounds__(kReduceThreads) k_fcg_direction(long long n, c
 __global__ void __launch_bounds__(kReduceThreads) k_krylov_step(long long n, double* __restrict__ x, double* __restrict__ r,
                                                                 const double* __restrict__ d, const double* __restrict__ Ad,
                                                                 const double* __restrict__ pnum, const double* __restrict__ pden,
-                                                                double* __restrict__ den_out, double* __restrict__ prr)
+                                                                double* __restrict__ den_out, double* __restrict__ prr,
+                                                                float* __restrict__ r32)
 {
     __shared__ double sh[33];
     const double num = reduce_partials(pnum, sh);
@@ -314,6 +342,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_krylov_step(long long n, dou
         x[i] = x[i] + alpha * d[i];
         const double ri = r[i] - alpha * Ad[i];
         r[i] = ri;
+        if (r32) r32[i] = (float)ri;
         rr = fma(ri, ri, rr);
     }
     rr = block_sum(rr, sh);
@@ -448,12 +477,14 @@ void launch_spmv(const BsrView<T>& A, int mode, const T* x, const T* aux, T* y, 
 }
 
 template <class T>
-void launch_gs(const BsrView<T>& A, int row0, int row1, const T* dinv, long long dld, const T* b, T* x, cudaStream_t s)
+void launch_gs(const BsrView<T>& A, int row0, int row1, const T* dinv, long long dld, const T* b, T* x, cudaStream_t s,
+               int col_lo, int col_hi)
 {
     if (row1 <= row0) return;
     const unsigned grid = grid_for((long long)(row1 - row0) * A.lanes, kThreads);
     FHG_DISPATCH_BS_G(A.bs, A.lanes, {
-        k_bsr_gs<T, BS, G><<<grid, kThreads, 0, s>>>(row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, b, x);
+        k_bsr_gs<T, BS, G><<<grid, kThreads, 0, s>>>(row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, b, x,
+                                                     col_lo, col_hi);
     });
     g_kernel_launches++;
 }
@@ -503,10 +534,23 @@ void launch_fcg_direction(long long n, const double* z, const double* dp, const 
 
 void launch_krylov_step(long long n, double* x, double* r, const double* d, const double* Ad,
                         const double* partials_num, const double* partials_den, double* den_out,
-                        double* partials_rr, cudaStream_t s)
+                        double* partials_rr, cudaStream_t s, float* r32)
 {
     k_krylov_step<<<kReduceCtas, kReduceThreads, 0, s>>>(n, x, r, d, Ad, partials_num, partials_den, den_out,
-                                                         partials_rr);
+                                                         partials_rr, r32);
+    g_kernel_launches++;
+}
+
+void launch_dot_mixed(long long n, const float* a, const double* b, double* partials, cudaStream_t s)
+{
+    k_dot_mixed<<<kReduceCtas, kReduceThreads, 0, s>>>(n, a, b, partials);
+    g_kernel_launches++;
+}
+
+void launch_fcg_direction_mixed(long long n, const float* z, const double* dp, const double* partials_zadp,
+                                const double* dadp, double* d, cudaStream_t s)
+{
+    k_fcg_direction_mixed<<<kReduceCtas, kReduceThreads, 0, s>>>(n, z, dp, partials_zadp, dadp, d);
     g_kernel_launches++;
 }
 
@@ -567,9 +611,9 @@ void launch_permute(int nb, int bs, const int* perm, const T* in, T* out, bool g
 template void launch_spmv<double>(const BsrView<double>&, int, const double*, const double*, double*, cudaStream_t);
 template void launch_spmv<float>(const BsrView<float>&, int, const float*, const float*, float*, cudaStream_t);
 template void launch_gs<double>(const BsrView<double>&, int, int, const double*, long long, const double*, double*,
-                                cudaStream_t);
+                                cudaStream_t, int, int);
 template void launch_gs<float>(const BsrView<float>&, int, int, const float*, long long, const float*, float*,
-                               cudaStream_t);
+                               cudaStream_t, int, int);
 template void launch_jacobi<double>(const BsrView<double>&, const double*, long long, double, const double*,
                                     const double*, double*, cudaStream_t);
 template void launch_jacobi<float>(const BsrView<float>&, const float*, long long, float, const float*, const float*,

@@ -26,6 +26,7 @@
 #include <array>
 #include <atomic>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <functional>
 #include <string>
@@ -1095,21 +1096,73 @@ void prolongation(Level& F, const Level& C, const Params& prm, const Rules& rule
     });
 }
 
+uint64_t splitmix64(uint64_t& s)
+{
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+double uniform01(uint64_t& s) { return (splitmix64(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+// Tensor of one coefficient block (bx, by, bz) of the field: a pure function of the seed and
+// the block index, so every level of the hierarchy sees the same field.
+std::array<double, 9> block_tensor(const fhg_hho_params& p, int dim, int bx, int by, int bz)
+{
+    std::array<double, 9> K{0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int m = p.checker_blocks > 0 ? p.checker_blocks : 4;
+    uint64_t s = p.seed * 0x100000001B3ull + (uint64_t)((bz * m + by) * m + bx) + 1;
+    if (p.coefficient == FHG_HHO_CHECKERBOARD) {
+        const double kappa = ((bx + by + bz) % 2 == 0) ? 1.0 : p.contrast;
+        for (int i = 0; i < dim; i++) K[i * dim + i] = kappa;
+    } else if (p.coefficient == FHG_HHO_LOGNORMAL_PATCHES) {
+        const double lc = std::log(p.contrast > 1 ? p.contrast : 1.0);
+        const double kappa = std::exp(-lc + 2 * lc * uniform01(s));
+        for (int i = 0; i < dim; i++) K[i * dim + i] = kappa;
+    } else if (p.coefficient == FHG_HHO_ANISOTROPIC) {
+        const double emin = p.eps_min > 0 ? p.eps_min : 1e-3;
+        const double eps = std::exp(std::log(emin) * (1.0 - uniform01(s)));
+        double R[3][3];
+        if (dim == 3) {
+            // uniform random rotation from a unit quaternion (Shoemake)
+            const double u1 = uniform01(s), u2 = uniform01(s), u3 = uniform01(s);
+            const double a = std::sqrt(1 - u1), b = std::sqrt(u1);
+            const double q0 = a * std::sin(2 * kPi * u2), q1 = a * std::cos(2 * kPi * u2);
+            const double q2 = b * std::sin(2 * kPi * u3), q3 = b * std::cos(2 * kPi * u3);
+            const double w = q0, x = q1, y = q2, z = q3;
+            R[0][0] = 1 - 2 * (y * y + z * z); R[0][1] = 2 * (x * y - z * w); R[0][2] = 2 * (x * z + y * w);
+            R[1][0] = 2 * (x * y + z * w); R[1][1] = 1 - 2 * (x * x + z * z); R[1][2] = 2 * (y * z - x * w);
+            R[2][0] = 2 * (x * z - y * w); R[2][1] = 2 * (y * z + x * w); R[2][2] = 1 - 2 * (x * x + y * y);
+        } else {
+            const double th = 2 * kPi * uniform01(s);
+            R[0][0] = std::cos(th); R[0][1] = -std::sin(th); R[1][0] = std::sin(th); R[1][1] = std::cos(th);
+        }
+        double D[3] = {1, 1, 1};
+        D[dim - 1] = eps;
+        for (int i = 0; i < dim; i++)
+            for (int j = 0; j < dim; j++) {
+                double v = 0;
+                for (int q = 0; q < dim; q++) v += R[i][q] * D[q] * R[j][q];
+                K[i * dim + j] = v;
+            }
+    } else {
+        for (int i = 0; i < dim; i++) K[i * dim + i] = 1.0;
+    }
+    return K;
+}
+
+// Coefficient of every element: the tensor of the block holding its centre (per-element
+// tensors keyed on the element centre, on every level).
 void set_coefficients(Mesh& M, const fhg_hho_params& p)
 {
     const int dim = M.dim;
+    const int m = p.checker_blocks > 0 ? p.checker_blocks : 4;
     M.K.assign(M.el.size(), {0, 0, 0, 0, 0, 0, 0, 0, 0});
     for (size_t e = 0; e < M.el.size(); e++) {
-        auto& K = M.K[e];
-        double kappa = 1.0;
         const auto c = centroid(M, (int)e);
-        if (p.coefficient == FHG_HHO_CHECKERBOARD) {
-            const int m = p.checker_blocks > 0 ? p.checker_blocks : 4;
-            int parity = 0;
-            for (int d = 0; d < dim; d++) parity += std::min(m - 1, (int)std::floor(c[d] * m));
-            kappa = (parity % 2 == 0) ? 1.0 : p.contrast;
-        }
-        for (int i = 0; i < dim; i++) K[i * dim + i] = kappa;
+        int bi[3] = {0, 0, 0};
+        for (int d = 0; d < dim; d++) bi[d] = std::min(m - 1, std::max(0, (int)std::floor(c[d] * m)));
+        M.K[e] = block_tensor(p, dim, bi[0], bi[1], bi[2]);
     }
 }
 
@@ -1138,6 +1191,8 @@ void fhg_hho_default_params(fhg_hho_params* p)
     p->contrast = 1.0;
     p->checker_blocks = 4;
     p->threads = 0;
+    p->eps_min = 1e-3;
+    p->seed = 20261203ull;
 }
 
 int fhg_hho_create(fhg_hho** out, const fhg_hho_params* p)

@@ -11,6 +11,10 @@ extern "C" {
 #define FHG_HHO_SOURCE_ONE 1       /* f = 1 */
 #define FHG_HHO_IDENTITY 0         /* K = I */
 #define FHG_HHO_CHECKERBOARD 1     /* isotropic, m^d checkerboard alternating 1 and `contrast` */
+#define FHG_HHO_ANISOTROPIC 2      /* per m^d block: R diag(1,..,1,eps) R^T, eps log-uniform in
+                                      [eps_min, 1], R a random rotation (seeded splitmix64) */
+#define FHG_HHO_LOGNORMAL_PATCHES 3 /* isotropic, per m^d block kappa log-uniform in
+                                      [1/contrast, contrast] (seeded) */
 
 typedef struct {
     int dim;              /* 2: unit square, 2 triangles per cell; 3: unit cube, 6 tetrahedra per cube */
@@ -23,6 +27,8 @@ typedef struct {
     double contrast;
     int checker_blocks;   /* m (4) */
     int threads;          /* 0: all hardware threads */
+    double eps_min;       /* FHG_HHO_ANISOTROPIC: smallest eps (1e-3) */
+    unsigned long long seed; /* coefficient fields and random sources */
 } fhg_hho_params;
 
 typedef struct fhg_hho fhg_hho;

@@ -15,13 +15,14 @@ import scipy.sparse as sp
 from .build import HHO_LIB
 
 SOURCE = {"sine": 0, "one": 1}
-COEFFICIENT = {"identity": 0, "checkerboard": 1}
+COEFFICIENT = {"identity": 0, "checkerboard": 1, "anisotropic": 2, "lognormal_patches": 3}
 
 
 class Params(C.Structure):
     _fields_ = [("dim", C.c_int), ("n", C.c_int), ("k", C.c_int), ("max_coarse_rows", C.c_int),
                 ("max_levels", C.c_int), ("source", C.c_int), ("coefficient", C.c_int), ("contrast", C.c_double),
-                ("checker_blocks", C.c_int), ("threads", C.c_int)]
+                ("checker_blocks", C.c_int), ("threads", C.c_int), ("eps_min", C.c_double),
+                ("seed", C.c_ulonglong)]
 
 
 _lib = None
@@ -61,7 +62,7 @@ class Hierarchy:
 
     def __init__(self, dim: int, n: int, k: int = 1, max_coarse_rows: int = 1000, max_levels: int = 0,
                  source: str = "sine", coefficient: str = "identity", contrast: float = 1.0, checker_blocks: int = 4,
-                 threads: int = 0):
+                 threads: int = 0, eps_min: float = 1e-3, seed: int = 20261203):
         L = lib()
         p = Params()
         L.fhg_hho_default_params(C.byref(p))
@@ -69,6 +70,7 @@ class Hierarchy:
         p.max_coarse_rows, p.max_levels = max_coarse_rows, max_levels
         p.source, p.coefficient = SOURCE[source], COEFFICIENT[coefficient]
         p.contrast, p.checker_blocks, p.threads = contrast, checker_blocks, threads
+        p.eps_min, p.seed = eps_min, seed
         self.h = C.c_void_p()
         rc = L.fhg_hho_create(C.byref(self.h), C.byref(p))
         if rc != 0:
