@@ -312,6 +312,10 @@ def run_ours(args, dist: Dist):
         ms = ctx.time_op(0, op, prec, warmup=3, reps=20)
         kernels[name] = {"ms": ms, "bytes": bytes_, "gbs": bytes_ / (ms * 1e-3) / 1e9}
 
+    # outer FCG operator: FP64 and double-FP32 (values as FP32 pairs, d as an FP32 pair, r.d, d.Ad)
+    outer_bytes = bytes_spmv(nnzb0, nb0, n0, n0, bs, 8) + n0 * 8 * 2   # + d (own rows) and r for the dots
+    add_kernel("bsr_outer_dots_fp64", N.OP_SYM_SPMV, "fp64", outer_bytes)
+    add_kernel("bsr_outer_dots_df", N.OP_SYM_SPMV, "fp32", outer_bytes)
     for prec, p in (("fp32", p32), ("fp64", p64)):
         add_kernel(f"bsr_spmv_{prec}", N.OP_SPMV, prec, bytes_spmv(nnzb0, nb0, n0, n0, bs, p))
         gs_bytes = bytes_spmv(nnzb0, nb0, n0, n0, bs, p) + nb0 * bs * bs * p + n0 * p   # + D^-1 + b

@@ -61,6 +61,8 @@ struct Level {
     DevBsr<double> A, Ahat, P, R;
     bool ahat_is_a = true;
     DevBsr<float> A32, P32, R32;
+    DevBsr<float> Ahat_hi;      // level 0, FP32 V-cycle: outer operator as an FP32 pair (hi part)
+    float* ahat_lo = nullptr;   // (lo part, same layout)
     double* dinv = nullptr;
     float* dinv32 = nullptr;
     int* perm_d = nullptr;
@@ -88,6 +90,7 @@ struct fhg_ctx {
     int* counter_d = nullptr;
     double* nr_host = nullptr;   // pinned
     double* io = nullptr;        // user-numbered I/O scratch (2 * n0)
+    float *dhi = nullptr, *dlo = nullptr;  // FP32 pair of the search direction (double-FP32 outer product)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     long long graph_kernels[2] = {0, 0};
     int graphs_built = 0;
@@ -464,6 +467,32 @@ int upload_bsr(fhg_ctx* ctx, const HostBsr& B, DevBsr<T>& D, const DevBsr<double
     return FHG_OK;
 }
 
+// Outer operator as an FP32 pair: hi = fl32(a), lo = fl32(a - hi), entry-major like upload_bsr.
+int upload_bsr_split(fhg_ctx* ctx, const HostBsr& B, DevBsr<float>& D, float** lo_out, const DevBsr<double>& share_index)
+{
+    const int bb = B.bs * B.bs;
+    const long long nnzb = B.nnzb();
+    const long long ld = round_up(std::max<long long>(nnzb, 1), 32);
+    std::vector<float> hi((size_t)ld * bb, 0.f), lo((size_t)ld * bb, 0.f);
+    for (long long p = 0; p < nnzb; p++)
+        for (int e = 0; e < bb; e++) {
+            const double v = B.vals[(size_t)p * bb + e];
+            const float h = (float)v;
+            hi[(size_t)e * ld + p] = h;
+            lo[(size_t)e * ld + p] = (float)(v - (double)h);
+        }
+    int rc;
+    D.rowptr = share_index.rowptr;
+    D.colidx = share_index.colidx;
+    D.owns_index = false;
+    if ((rc = upload(ctx, &D.vals, hi.data(), hi.size()))) return rc;
+    if ((rc = upload(ctx, lo_out, lo.data(), lo.size()))) return rc;
+    D.v.nbr = B.nbr; D.v.nbc = B.nbc; D.v.bs = B.bs; D.v.nnzb = nnzb; D.v.ld = ld;
+    D.v.rowptr = D.rowptr; D.v.colidx = D.colidx; D.v.vals = D.vals;
+    D.v.lanes = share_index.v.lanes;
+    return FHG_OK;
+}
+
 bool supported_bs(int bs) { return bs == 2 || bs == 3 || bs == 4 || bs == 6; }
 
 // ---------------------------------------------------------------------------
@@ -567,19 +596,25 @@ void fcg_iteration(fhg_ctx* ctx, int p)
     double* Adp = ctx->kAd[1 - p];
     Level& L0 = ctx->levels[0];
     const bool fp32 = ctx->opts.vcycle_precision == FHG_PREC_FP32;
+    const bool split = fp32 && L0.ahat_lo && ctx->dhi;
     if (fp32) {
         // V-cycle on the FP32 copy of r written by the previous step; z stays FP32 and is
         // widened inside the direction update.
         vcycle<float>(ctx, 0, L0.b32, L0.x32);
         fhg::launch_dot_mixed(n, L0.x32, Adp, part(ctx, 0), s);
-        fhg::launch_fcg_direction_mixed(n, L0.x32, dp, part(ctx, 0), ctx->scal + 1, z, s);
+        fhg::launch_fcg_direction_mixed(n, L0.x32, dp, part(ctx, 0), ctx->scal + 1, z, s, split ? ctx->dhi : nullptr,
+                                        split ? ctx->dlo : nullptr);
     } else {
         precondition(ctx, ctx->kr, z);
         fhg::launch_dot(n, z, Adp, part(ctx, 0), s);
         fhg::launch_fcg_direction(n, z, dp, part(ctx, 0), ctx->scal + 1, z, s);
     }
-    const BsrView<double>& Ah = L0.ahat_is_a ? L0.A.v : L0.Ahat.v;
-    fhg::launch_spmv_dots(Ah, z, ctx->kr, Ad, part(ctx, 1), s);
+    if (split) {
+        fhg::launch_spmv_dots_df(L0.Ahat_hi.v, L0.ahat_lo, ctx->dhi, ctx->dlo, z, ctx->kr, Ad, part(ctx, 1), s);
+    } else {
+        const BsrView<double>& Ah = L0.ahat_is_a ? L0.A.v : L0.Ahat.v;
+        fhg::launch_spmv_dots(Ah, z, ctx->kr, Ad, part(ctx, 1), s);
+    }
     // parts 1 = d.Ad, 2 = r.d
     fhg::launch_krylov_step(n, ctx->kx, ctx->kr, z, Ad, part(ctx, 2), part(ctx, 1), ctx->scal + 1, part(ctx, 3), s,
                             fp32 ? L0.b32 : nullptr);
@@ -748,6 +783,7 @@ void fhg_default_options(fhg_options* o)
     o->use_graphs = 1;
     o->autotune = 0;
     o->max_coarse_rows = 8192;
+    o->outer_split = 1;
 }
 
 int fhg_create(fhg_ctx** out, int device)
@@ -940,11 +976,15 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
             HostCsr S;
             symmetrise_lower(L.A_in, S);
             L.ahat_is_a = csr_equal(S, L.A_in);
+            const bool split = fp32 && o.outer_split;
             if (!L.ahat_is_a) {
                 HostBsr Sb, Sp;
                 csr_to_bsr(S, bs, Sb);
                 permute_bsr(Sb, L.perm, iperm[0], Sp);
                 if ((rc = upload_bsr<double>(ctx, Sp, L.Ahat, nullptr))) return rc;
+                if (split && (rc = upload_bsr_split(ctx, Sp, L.Ahat_hi, &L.ahat_lo, L.Ahat))) return rc;
+            } else if (split && (rc = upload_bsr_split(ctx, Ap, L.Ahat_hi, &L.ahat_lo, L.A))) {
+                return rc;
             }
         }
         if (l == nlevels - 1) {
@@ -969,6 +1009,7 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         (rc = dalloc(ctx, &ctx->hist_d, (size_t)o.max_iterations + 2)) || (rc = dalloc(ctx, &ctx->counter_d, 1)) ||
         (rc = dalloc(ctx, &ctx->io, (size_t)2 * n0)))
         return rc;
+    if (fp32 && o.outer_split && ((rc = dalloc(ctx, &ctx->dhi, n0)) || (rc = dalloc(ctx, &ctx->dlo, n0)))) return rc;
     CK(cudaMallocHost(&ctx->nr_host, sizeof(double)));
 
     if (o.autotune) {
@@ -988,6 +1029,7 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         }
         Level& L0 = ctx->levels[0];
         if (!L0.ahat_is_a) L0.Ahat.v.lanes = L0.A.v.lanes;
+        if (L0.ahat_lo) L0.Ahat_hi.v.lanes = L0.A.v.lanes;
     }
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->ready = true;
@@ -1194,15 +1236,31 @@ int fhg_time_op(fhg_ctx* ctx, int level, int op, int precision, int warmup, int 
     if (level < 0 || level >= ctx->nlevels) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d out of range", level);
     CK(cudaSetDevice(ctx->device));
     if (op == FHG_OP_SYM_SPMV || op == FHG_OP_VCYCLE) {
-        if (precision != FHG_PREC_FP64) return fail(ctx, FHG_ERR_INVALID_ARG, "op %d is timed in FP64 only", op);
-        const size_t n0 = ctx->levels[0].n;
+        Level& L0 = ctx->levels[0];
+        const bool split = op == FHG_OP_SYM_SPMV && precision == FHG_PREC_FP32;
+        if (precision != FHG_PREC_FP64 && !split) return fail(ctx, FHG_ERR_INVALID_ARG, "op %d is timed in FP64 only", op);
+        if (split && (!L0.ahat_lo || !ctx->dhi))
+            return fail(ctx, FHG_ERR_NOT_READY, "the double-FP32 outer operator was not built at setup");
+        const size_t n0 = L0.n;
         double* t = nullptr;
         int rc = dalloc(ctx, &t, 2 * n0);
         if (rc) return rc;
         CK(cudaMemcpyAsync(t, ctx->kr, sizeof(double) * n0, cudaMemcpyDeviceToDevice, ctx->stream));
-        for (int w = 0; w < warmup && rc == FHG_OK; w++) rc = apply_device(ctx, level, op, t, nullptr, t + n0);
+        if (split) {
+            fhg::launch_convert<double, float>(n0, t, ctx->dhi, ctx->stream);
+            CK(cudaMemsetAsync(ctx->dlo, 0, sizeof(float) * n0, ctx->stream));
+        }
+        auto one = [&]() -> int {
+            if (split) {
+                fhg::launch_spmv_dots_df(L0.Ahat_hi.v, L0.ahat_lo, ctx->dhi, ctx->dlo, t, t, t + n0, part(ctx, 4),
+                                         ctx->stream);
+                return FHG_OK;
+            }
+            return apply_device(ctx, level, op, t, nullptr, t + n0);
+        };
+        for (int w = 0; w < warmup && rc == FHG_OK; w++) rc = one();
         CK(cudaEventRecord(ctx->ev0, ctx->stream));
-        for (int r = 0; r < reps && rc == FHG_OK; r++) rc = apply_device(ctx, level, op, t, nullptr, t + n0);
+        for (int r = 0; r < reps && rc == FHG_OK; r++) rc = one();
         CK(cudaEventRecord(ctx->ev1, ctx->stream));
         CK(cudaEventSynchronize(ctx->ev1));
         float ms = 0;

@@ -66,8 +66,13 @@ void launch_krylov_step(long long n, double* x, double* r, const double* d, cons
                         double* partials_rr, cudaStream_t s, float* r32 = nullptr);
 // FP32 preconditioned residual z into the FP64 FCG: partials of z.Adp; d = z - s dp.
 void launch_dot_mixed(long long n, const float* a, const double* b, double* partials, cudaStream_t s);
+// (dhi, dlo optional: FP32 pair of d for the double-FP32 outer product)
 void launch_fcg_direction_mixed(long long n, const float* z, const double* dp, const double* partials_zadp,
-                                const double* dadp, double* d, cudaStream_t s);
+                                const double* dadp, double* d, cudaStream_t s, float* dhi = nullptr,
+                                float* dlo = nullptr);
+// Ad = Â d in double-FP32 arithmetic (Â = hi + lo, d = dhi + dlo), partials as launch_spmv_dots.
+void launch_spmv_dots_df(const BsrView<float>& Ahi, const float* vlo, const float* dhi, const float* dlo,
+                         const double* d, const double* r, double* Ad, double* partials, cudaStream_t s);
 // ||r|| / ||b||: reduces partials_rr, divides by *bnorm, writes *nr_out and hist[*counter],
 // then ++*counter.
 void launch_finalize_norm(const double* partials_rr, const double* bnorm, double* nr_out,

@@ -64,6 +64,73 @@ __device__ __forceinline__ double reduce_partials(const double* __restrict__ p, 
 }
 
 // ---------------------------------------------------------------------------
+// Row accumulation: acc[r] += sum over this lane's blocks of (A_block x_col)[r].
+// `sel(col)` returns 0 (skip the block), 1 (use it) or 2 (stop: columns are sorted, nothing
+// after it is used). For bs <= 3 each lane walks two blocks per step so that the loads of
+// both (column index, bs^2 values, bs entries of x) are in flight together; the
+// accumulation order stays block by block.
+template <class T, int BS, int G, class Sel>
+__device__ __forceinline__ void accumulate_row(int p0, int p1, int lane, const int* __restrict__ colidx,
+                                               const T* __restrict__ vals, long long ld, const T* x, T* acc,
+                                               Sel sel)
+{
+    if constexpr (BS <= 3) {
+        for (int p = p0 + lane; p < p1; p += 2 * G) {
+            const int q = p + G;
+            const int ca = colidx[p];
+            const int cb = q < p1 ? colidx[q] : -1;
+            const int ua = sel(ca);
+            if (ua == 2) break;
+            const int ub = cb >= 0 ? sel(cb) : 0;
+            T va[BS * BS], vb[BS * BS], xa[BS], xb[BS];
+            if (ua == 1) {
+#pragma unroll
+                for (int e = 0; e < BS * BS; e++) va[e] = vals[(long long)e * ld + p];
+#pragma unroll
+                for (int c = 0; c < BS; c++) xa[c] = x[(long long)ca * BS + c];
+            }
+            if (ub == 1) {
+#pragma unroll
+                for (int e = 0; e < BS * BS; e++) vb[e] = vals[(long long)e * ld + q];
+#pragma unroll
+                for (int c = 0; c < BS; c++) xb[c] = x[(long long)cb * BS + c];
+            }
+            if (ua == 1) {
+#pragma unroll
+                for (int r = 0; r < BS; r++)
+#pragma unroll
+                    for (int c = 0; c < BS; c++) acc[r] = fma(va[r * BS + c], xa[c], acc[r]);
+            }
+            if (ub == 1) {
+#pragma unroll
+                for (int r = 0; r < BS; r++)
+#pragma unroll
+                    for (int c = 0; c < BS; c++) acc[r] = fma(vb[r * BS + c], xb[c], acc[r]);
+            }
+            if (ub == 2) break;
+        }
+    } else {
+        for (int p = p0 + lane; p < p1; p += G) {
+            const int col = colidx[p];
+            const int u = sel(col);
+            if (u == 2) break;
+            if (u == 0) continue;
+            T xv[BS];
+#pragma unroll
+            for (int c = 0; c < BS; c++) xv[c] = x[(long long)col * BS + c];
+#pragma unroll
+            for (int r = 0; r < BS; r++)
+#pragma unroll
+                for (int c = 0; c < BS; c++) acc[r] = fma(vals[(long long)(r * BS + c) * ld + p], xv[c], acc[r]);
+        }
+    }
+}
+
+struct UseAll {
+    __device__ __forceinline__ int operator()(int) const { return 1; }
+};
+
+// ---------------------------------------------------------------------------
 // y = A x  |  y = aux - A x  |  y = aux + A x      (aux may alias y)
 template <class T, int BS, int G, int MODE>
 __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int nbr, const int* __restrict__ rowptr,
@@ -76,19 +143,7 @@ __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int nbr, const int* __res
     T acc[BS];
 #pragma unroll
     for (int r = 0; r < BS; r++) acc[r] = T(0);
-    if (row < nbr) {
-        const int p1 = rowptr[row + 1];
-        for (int p = rowptr[row] + lane; p < p1; p += G) {
-            const int col = colidx[p];
-            T xv[BS];
-#pragma unroll
-            for (int c = 0; c < BS; c++) xv[c] = x[(long long)col * BS + c];
-#pragma unroll
-            for (int r = 0; r < BS; r++)
-#pragma unroll
-                for (int c = 0; c < BS; c++) acc[r] = fma(vals[(long long)(r * BS + c) * ld + p], xv[c], acc[r]);
-        }
-    }
+    if (row < nbr) accumulate_row<T, BS, G>(rowptr[row], rowptr[row + 1], lane, colidx, vals, ld, x, acc, UseAll());
 #pragma unroll
     for (int r = 0; r < BS; r++) acc[r] = group_sum<G>(acc[r]);
     if (row < nbr) {
@@ -123,19 +178,11 @@ __global__ void __launch_bounds__(kThreads) k_bsr_gs(int row0, int row1, const i
 #pragma unroll
     for (int r = 0; r < BS; r++) acc[r] = T(0);
     if (row < row1) {
-        const int p1 = rowptr[row + 1];
-        for (int p = rowptr[row] + lane; p < p1; p += G) {
-            const int col = colidx[p];
-            if (col >= col_hi) break;
-            if (col == row || col < col_lo) continue;
-            T xv[BS];
-#pragma unroll
-            for (int c = 0; c < BS; c++) xv[c] = x[(long long)col * BS + c];
-#pragma unroll
-            for (int r = 0; r < BS; r++)
-#pragma unroll
-                for (int c = 0; c < BS; c++) acc[r] = fma(vals[(long long)(r * BS + c) * ld + p], xv[c], acc[r]);
-        }
+        auto sel = [row, col_lo, col_hi](int col) -> int {
+            if (col >= col_hi) return 2;
+            return (col == row || col < col_lo) ? 0 : 1;
+        };
+        accumulate_row<T, BS, G>(rowptr[row], rowptr[row + 1], lane, colidx, vals, ld, x, acc, sel);
     }
 #pragma unroll
     for (int r = 0; r < BS; r++) acc[r] = group_sum<G>(acc[r]);
@@ -232,19 +279,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots(int nbr, const
 #pragma unroll
         for (int r = 0; r < BS; r++) acc[r] = 0.0;
         const bool active = row < nbr;
-        if (active) {
-            const int p1 = rowptr[row + 1];
-            for (int p = rowptr[row] + lane; p < p1; p += G) {
-                const int col = colidx[p];
-                double xv[BS];
-#pragma unroll
-                for (int c = 0; c < BS; c++) xv[c] = d[(long long)col * BS + c];
-#pragma unroll
-                for (int r = 0; r < BS; r++)
-#pragma unroll
-                    for (int c = 0; c < BS; c++) acc[r] = fma(vals[(long long)(r * BS + c) * ld + p], xv[c], acc[r]);
-            }
-        }
+        if (active) accumulate_row<double, BS, G>(rowptr[row], rowptr[row + 1], lane, colidx, vals, ld, d, acc, UseAll());
 #pragma unroll
         for (int r = 0; r < BS; r++) acc[r] = group_sum<G>(acc[r]);
         if (active) {
@@ -262,6 +297,99 @@ __global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots(int nbr, const
     }
     const double s1 = block_sum(dad, sh);
     const double s2 = block_sum(rd, sh);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = s1;
+        partials[kReduceCtas + blockIdx.x] = s2;
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// Ad = Â d in double-FP32 ("double-single") arithmetic on the FP32 pipe, with per-CTA partials
+// of d.Ad and r.d in FP64. Â = a_hi + a_lo and d = d_hi + d_lo are FP32 pairs (a_lo, d_lo the
+// FP32-rounded remainders); every product a_hi*d_hi is split exactly with an FMA, the cross
+// terms a_hi*d_lo + a_lo*d_hi are added in FP32, a_lo*d_lo (2^-48 relative) is dropped, and the
+// running sum is a (hi, lo) FP32 pair kept exact with TwoSum. Relative accuracy of every term
+// ~2^-47: the result carries FP64-class accuracy (a few units in 1e-14) while the FP64 pipe,
+// 56x slower than FP32 on GB300, only adds the final pair and the two dot products.
+__device__ __forceinline__ void df_add(float& sh, float& sl, float ph, float pl)
+{
+    const float s = sh + ph;
+    const float bv = s - sh;
+    const float err = (sh - (s - bv)) + (ph - bv);
+    sl = sl + (err + pl);
+    sh = s;
+}
+
+template <int BS, int G>
+__global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots_df(int nbr, const int* __restrict__ rowptr,
+                                                                     const int* __restrict__ colidx,
+                                                                     const float* __restrict__ vhi,
+                                                                     const float* __restrict__ vlo, long long ld,
+                                                                     const float* __restrict__ dhi,
+                                                                     const float* __restrict__ dlo,
+                                                                     const double* __restrict__ d,
+                                                                     const double* __restrict__ rvec,
+                                                                     double* __restrict__ Ad,
+                                                                     double* __restrict__ partials)
+{
+    __shared__ double sh_red[33];
+    const int lane = threadIdx.x & (G - 1);
+    constexpr int kGroupsPerWarp = 32 / G;
+    const long long warp_id = ((long long)blockIdx.x * kReduceThreads + threadIdx.x) >> 5;
+    const long long warp_stride = (long long)kReduceCtas * kReduceThreads / 32 * kGroupsPerWarp;
+    const int group_in_warp = (threadIdx.x & 31) / G;
+    double dad = 0.0, rd = 0.0;
+    for (long long row0 = warp_id * kGroupsPerWarp; row0 < nbr; row0 += warp_stride) {
+        const int row = (int)(row0 + group_in_warp);
+        float hi[BS], lo[BS];
+#pragma unroll
+        for (int r = 0; r < BS; r++) { hi[r] = 0.f; lo[r] = 0.f; }
+        if (row < nbr) {
+            const int p1 = rowptr[row + 1];
+            for (int p = rowptr[row] + lane; p < p1; p += G) {
+                const int col = colidx[p];
+                float xh[BS], xl[BS];
+#pragma unroll
+                for (int c = 0; c < BS; c++) { xh[c] = dhi[(long long)col * BS + c]; xl[c] = dlo[(long long)col * BS + c]; }
+#pragma unroll
+                for (int r = 0; r < BS; r++)
+#pragma unroll
+                    for (int c = 0; c < BS; c++) {
+                        const float ah = vhi[(long long)(r * BS + c) * ld + p];
+                        const float al = vlo[(long long)(r * BS + c) * ld + p];
+                        const float ph = ah * xh[c];
+                        const float pe = fmaf(ah, xh[c], -ph);
+                        const float cross = fmaf(ah, xl[c], al * xh[c]);
+                        df_add(hi[r], lo[r], ph, pe + cross);
+                    }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < BS; r++) {
+#pragma unroll
+            for (int o = G / 2; o > 0; o >>= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, hi[r], o, G);
+                const float ol = __shfl_xor_sync(0xffffffffu, lo[r], o, G);
+                df_add(hi[r], lo[r], oh, ol);
+            }
+        }
+        if (row < nbr) {
+#pragma unroll
+            for (int r = 0; r < BS; r++) {
+                if (lane == r % G) {
+                    const long long i = (long long)row * BS + r;
+                    const double v = (double)hi[r] + (double)lo[r];
+                    Ad[i] = v;
+                    const double di = d[i];
+                    dad = fma(di, v, dad);
+                    rd = fma(rvec[i], di, rd);
+                }
+            }
+        }
+    }
+    const double s1 = block_sum(dad, sh_red);
+    const double s2 = block_sum(rd, sh_red);
     if (threadIdx.x == 0) {
         partials[blockIdx.x] = s1;
         partials[kReduceCtas + blockIdx.x] = s2;
@@ -308,12 +436,20 @@ __global__ void __launch_bounds__(kReduceThreads) k_dot_mixed(long long n, const
 __global__ void __launch_bounds__(kReduceThreads) k_fcg_direction_mixed(long long n, const float* __restrict__ z,
                                                                         const double* __restrict__ dp,
                                                                         const double* __restrict__ partials,
-                                                                        const double* __restrict__ dadp, double* __restrict__ d)
+                                                                        const double* __restrict__ dadp, double* __restrict__ d,
+                                                                        float* __restrict__ dhi, float* __restrict__ dlo)
 {
     __shared__ double sh[33];
     const double s = reduce_partials(partials, sh) / *dadp;
-    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads)
-        d[i] = (double)z[i] - s * dp[i];
+    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads) {
+        const double v = (double)z[i] - s * dp[i];
+        d[i] = v;
+        if (dhi) {
+            const float h = (float)v;
+            dhi[i] = h;
+            dlo[i] = (float)(v - (double)h);
+        }
+    }
 }
 
 __global__ void __launch_bounds__(kReduceThreads) k_fcg_direction(long long n, const double* z, const double* __restrict__ dp,
@@ -548,9 +684,19 @@ void launch_dot_mixed(long long n, const float* a, const double* b, double* part
 }
 
 void launch_fcg_direction_mixed(long long n, const float* z, const double* dp, const double* partials_zadp,
-                                const double* dadp, double* d, cudaStream_t s)
+                                const double* dadp, double* d, cudaStream_t s, float* dhi, float* dlo)
 {
-    k_fcg_direction_mixed<<<kReduceCtas, kReduceThreads, 0, s>>>(n, z, dp, partials_zadp, dadp, d);
+    k_fcg_direction_mixed<<<kReduceCtas, kReduceThreads, 0, s>>>(n, z, dp, partials_zadp, dadp, d, dhi, dlo);
+    g_kernel_launches++;
+}
+
+void launch_spmv_dots_df(const BsrView<float>& Ahi, const float* vlo, const float* dhi, const float* dlo,
+                         const double* d, const double* r, double* Ad, double* partials, cudaStream_t s)
+{
+    FHG_DISPATCH_BS_G(Ahi.bs, Ahi.lanes, {
+        k_bsr_spmv_dots_df<BS, G><<<kReduceCtas, kReduceThreads, 0, s>>>(Ahi.nbr, Ahi.rowptr, Ahi.colidx, Ahi.vals, vlo,
+                                                                         Ahi.ld, dhi, dlo, d, r, Ad, partials);
+    });
     g_kernel_launches++;
 }
 

@@ -126,6 +126,9 @@ class _KrylovOnGpu(IterativeSolver):
         self.Precond = SolverPreconditioner()
         self.Device = 0
         self.UseGraphs = True
+        # FP32 V-cycle only: apply the outer operator in double-FP32 arithmetic (FP64-class
+        # accuracy on the FP32 pipe) instead of native FP64.
+        self.OuterSplit = True
         self._ctx: Optional[N.Context] = None
 
     def _options(self, mg: Multigrid) -> N.Options:
@@ -143,6 +146,7 @@ class _KrylovOnGpu(IterativeSolver):
         o.use_graphs = 1 if self.UseGraphs else 0
         o.autotune = 1 if mg.Autotune else 0
         o.max_coarse_rows = mg.MaxCoarseRows
+        o.outer_split = 1 if self.OuterSplit else 0
         return o
 
     def Setup(self, A):
@@ -216,7 +220,7 @@ class ConjugateGradient(_KrylovOnGpu):
 
 def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: str = "bgs", post: str = "rbgs",
            precision: str = "fp64", krylov: str = "fcg", device: int = 0, autotune: bool = False,
-           use_graphs: bool = True):
+           use_graphs: bool = True, outer_split: bool = True):
     """SolverFactory-style construction of "-s fcgmg -cycle V,1,1" (src/Solver/SolverFactory.h:156-200)."""
     mg = Multigrid(len(As))
     mg.SetHierarchy(As, Ps)
@@ -230,5 +234,6 @@ def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: st
     solver.MaxIterations = maxit
     solver.Device = device
     solver.UseGraphs = use_graphs
+    solver.OuterSplit = outer_split
     solver.Setup(As[0])
     return solver

@@ -107,15 +107,27 @@ def test_solves_are_bitwise_reproducible(case):
     assert np.array_equal(x1, x2) and np.array_equal(h1, solver.History)
 
 
-def test_fp32_vcycle_reaches_fp64_tolerance(case):
+@pytest.mark.parametrize("outer_split", [True, False])
+def test_fp32_vcycle_reaches_fp64_tolerance(case, outer_split):
     ref_iters = len(case["hist_colour"]) - 1
-    solver = S().fcg_mg(case.As, case.Ps, case.bs, precision="fp32")
+    solver = S().fcg_mg(case.As, case.Ps, case.bs, precision="fp32", outer_split=outer_split)
     x = solver.Solve(case.b)
     assert solver.History[-1] < 1e-8
     assert solver.IterationCount <= ref_iters + 3
     assert true_rel_residual(case.As[0], case.b, x) < 5e-8
     xr = case["x_natural"]
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-6
+
+
+def test_double_fp32_outer_product_tracks_fp64(case):
+    # The double-FP32 outer product (FP64-class accuracy) changes the FP32-V-cycle solve by
+    # rounding only: same iterations, histories within 1e-8 relative.
+    a = S().fcg_mg(case.As, case.Ps, case.bs, precision="fp32", outer_split=True)
+    a.Solve(case.b)
+    b = S().fcg_mg(case.As, case.Ps, case.bs, precision="fp32", outer_split=False)
+    b.Solve(case.b)
+    assert a.IterationCount == b.IterationCount
+    assert np.all(np.abs(a.History - b.History) <= 1e-8 * b.History + 1e-13)
 
 
 def test_autotuned_lanes_give_the_same_solve(case):
