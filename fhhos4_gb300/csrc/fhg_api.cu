@@ -56,6 +56,9 @@ struct Level {
     int n = 0, nb = 0, bs = 0;
     HostCsr A_in, P_in;
     int ncolours = 0;
+    int gs_lanes = 0;              // lanes per block row of the GS/Jacobi sweeps (0: those of A)
+    int gs_unroll = 1;             // blocks per lane step of the GS sweeps
+    int outer_lanes = 0;           // level 0: lanes of the FP64 outer product (0: those of its view)
     std::vector<int> colour_start;  // block-row offsets of every colour, ncolours + 1
     std::vector<int> perm;          // new block row -> given block row
     DevBsr<double> A, Ahat, P, R;
@@ -526,20 +529,22 @@ void smooth(fhg_ctx* ctx, int l, int code, int iters, const T* b, T* x, bool fro
     Level& L = ctx->levels[l];
     using V = LevelVecs<T>;
     cudaStream_t s = ctx->stream;
+    BsrView<T> A = V::A(L);
+    if (L.gs_lanes) { A.lanes = L.gs_lanes; A.unroll = L.gs_unroll; }
     for (int it = 0; it < iters; it++) {
         const bool zero = from_zero && it == 0;
         if (code == FHG_SMOOTHER_BGS) {
             for (int c = 0; c < L.ncolours; c++)
-                fhg::launch_gs<T>(V::A(L), L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s, 0,
+                fhg::launch_gs<T>(A, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s, 0,
                                   zero ? L.colour_start[c + 1] : 0x7fffffff);
         } else if (code == FHG_SMOOTHER_RBGS) {
             for (int c = L.ncolours - 1; c >= 0; c--)
-                fhg::launch_gs<T>(V::A(L), L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s,
+                fhg::launch_gs<T>(A, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s,
                                   zero ? L.colour_start[c] : 0, 0x7fffffff);
         } else {
             const T omega = code == FHG_SMOOTHER_BJ23 ? T(2.0 / 3.0) : T(ctx->opts.omega);
             T* tmp = V::r(L);
-            fhg::launch_jacobi<T>(V::A(L), V::dinv(L), L.nb, omega, b, x, tmp, s);
+            fhg::launch_jacobi<T>(A, V::dinv(L), L.nb, omega, b, x, tmp, s);
             cudaMemcpyAsync(x, tmp, sizeof(T) * (size_t)L.n, cudaMemcpyDeviceToDevice, s);
         }
     }
@@ -612,7 +617,8 @@ void fcg_iteration(fhg_ctx* ctx, int p)
     if (split) {
         fhg::launch_spmv_dots_df(L0.Ahat_hi.v, L0.ahat_lo, ctx->dhi, ctx->dlo, z, ctx->kr, Ad, part(ctx, 1), s);
     } else {
-        const BsrView<double>& Ah = L0.ahat_is_a ? L0.A.v : L0.Ahat.v;
+        BsrView<double> Ah = L0.ahat_is_a ? L0.A.v : L0.Ahat.v;
+        if (L0.outer_lanes) Ah.lanes = L0.outer_lanes;
         fhg::launch_spmv_dots(Ah, z, ctx->kr, Ad, part(ctx, 1), s);
     }
     // parts 1 = d.Ad, 2 = r.d
@@ -662,26 +668,73 @@ int build_graphs(fhg_ctx* ctx)
     return FHG_OK;
 }
 
-// Lanes-per-block-row autotuning of one operator: time y = A x for G = 4..32, keep the best.
-template <class T>
-int tune_lanes(fhg_ctx* ctx, BsrView<T>& v, const T* x, T* y)
+// Autotuning of the launch shape of one operator: lanes per block row G in {4, 8, 16, 32} and
+// blocks per lane step U in {1, 2} (U = 2 for bs <= 3 only), timed with the launch that will
+// run; the fastest pair is kept. `run(G, U)` launches the operator once.
+template <class F>
+int tune(fhg_ctx* ctx, int bs, int& lanes, int& unroll, F run)
 {
-    if (v.nbr == 0) return FHG_OK;
     float best = 1e30f;
-    int bestG = v.lanes;
-    for (int G : {4, 8, 16, 32}) {
-        v.lanes = G;
-        for (int w = 0; w < 2; w++) fhg::launch_spmv<T>(v, fhg::kSpmvAssign, x, nullptr, y, ctx->stream);
-        CK(cudaEventRecord(ctx->ev0, ctx->stream));
-        const int reps = 5;
-        for (int r = 0; r < reps; r++) fhg::launch_spmv<T>(v, fhg::kSpmvAssign, x, nullptr, y, ctx->stream);
-        CK(cudaEventRecord(ctx->ev1, ctx->stream));
-        CK(cudaEventSynchronize(ctx->ev1));
-        float ms = 0;
-        CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-        if (ms < best) { best = ms; bestG = G; }
+    int bestG = lanes, bestU = unroll;
+    for (int U : {1, 2}) {
+        if (U == 2 && bs > 3) continue;
+        for (int G : {4, 8, 16, 32}) {
+            for (int w = 0; w < 2; w++) run(G, U);
+            CK(cudaEventRecord(ctx->ev0, ctx->stream));
+            const int reps = 8;
+            for (int r = 0; r < reps; r++) run(G, U);
+            CK(cudaEventRecord(ctx->ev1, ctx->stream));
+            CK(cudaEventSynchronize(ctx->ev1));
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+            if (ms < best) { best = ms; bestG = G; bestU = U; }
+        }
     }
-    v.lanes = bestG;
+    lanes = bestG;
+    unroll = bestU;
+    return FHG_OK;
+}
+
+template <class T>
+int tune_level(fhg_ctx* ctx, int l)
+{
+    using V = LevelVecs<T>;
+    Level& L = ctx->levels[l];
+    cudaStream_t s = ctx->stream;
+    BsrView<T>& A = const_cast<BsrView<T>&>(V::A(L));
+    const int bs = A.bs;
+    CK(cudaMemsetAsync(V::x(L), 0, sizeof(T) * L.n, s));
+    CK(cudaMemsetAsync(V::b(L), 0, sizeof(T) * L.n, s));
+    int rc = tune(ctx, bs, A.lanes, A.unroll, [&](int G, int U) {
+        BsrView<T> v = A; v.lanes = G; v.unroll = U;
+        fhg::launch_spmv<T>(v, fhg::kSpmvResidual, V::x(L), V::b(L), V::r(L), s);
+    });
+    if (rc) return rc;
+    if (l < ctx->nlevels - 1) {
+        Level& C = ctx->levels[l + 1];
+        int g = A.lanes, gu = A.unroll;
+        rc = tune(ctx, bs, g, gu, [&](int G, int U) {
+            BsrView<T> v = A; v.lanes = G; v.unroll = U;
+            for (int c = 0; c < L.ncolours; c++)
+                fhg::launch_gs<T>(v, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, V::b(L), V::x(L), s);
+        });
+        if (rc) return rc;
+        L.gs_lanes = g;
+        L.gs_unroll = gu;
+        BsrView<T>& P = const_cast<BsrView<T>&>(V::P(L));
+        BsrView<T>& R = const_cast<BsrView<T>&>(V::R(L));
+        CK(cudaMemsetAsync(V::x(C), 0, sizeof(T) * C.n, s));
+        if ((rc = tune(ctx, bs, P.lanes, P.unroll, [&](int G, int U) {
+                 BsrView<T> v = P; v.lanes = G; v.unroll = U;
+                 fhg::launch_spmv<T>(v, fhg::kSpmvAddTo, V::x(C), V::r(L), V::r(L), s);
+             })))
+            return rc;
+        if ((rc = tune(ctx, bs, R.lanes, R.unroll, [&](int G, int U) {
+                 BsrView<T> v = R; v.lanes = G; v.unroll = U;
+                 fhg::launch_spmv<T>(v, fhg::kSpmvAssign, V::r(L), nullptr, V::b(C), s);
+             })))
+            return rc;
+    }
     return FHG_OK;
 }
 
@@ -1013,23 +1066,44 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
     CK(cudaMallocHost(&ctx->nr_host, sizeof(double)));
 
     if (o.autotune) {
+        // Tune in the precision the V-cycle runs in (the FP64 copies keep the FP32 choices,
+        // the same access pattern); the outer operators on their own launches.
         for (int l = 0; l < nlevels; l++) {
             Level& L = ctx->levels[l];
-            if ((rc = tune_lanes<double>(ctx, L.A.v, L.x, L.r))) return rc;
-            if (l < nlevels - 1) {
-                Level& C = ctx->levels[l + 1];
-                if ((rc = tune_lanes<double>(ctx, L.P.v, C.x, L.r))) return rc;
-                if ((rc = tune_lanes<double>(ctx, L.R.v, L.x, C.r))) return rc;
-            }
             if (fp32) {
-                L.A32.v.lanes = L.A.v.lanes;
-                L.P32.v.lanes = L.P.v.lanes;
-                L.R32.v.lanes = L.R.v.lanes;
+                if ((rc = tune_level<float>(ctx, l))) return rc;
+                L.A.v.lanes = L.A32.v.lanes;
+                L.A.v.unroll = L.A32.v.unroll;
+                if (l < nlevels - 1) {
+                    L.P.v.lanes = L.P32.v.lanes; L.P.v.unroll = L.P32.v.unroll;
+                    L.R.v.lanes = L.R32.v.lanes; L.R.v.unroll = L.R32.v.unroll;
+                }
+            } else {
+                if ((rc = tune_level<double>(ctx, l))) return rc;
             }
         }
         Level& L0 = ctx->levels[0];
-        if (!L0.ahat_is_a) L0.Ahat.v.lanes = L0.A.v.lanes;
-        if (L0.ahat_lo) L0.Ahat_hi.v.lanes = L0.A.v.lanes;
+        BsrView<double>& Ah = L0.ahat_is_a ? L0.A.v : L0.Ahat.v;
+        int g = Ah.lanes, gu = 1;
+        CK(cudaMemsetAsync(ctx->kz[0], 0, sizeof(double) * L0.n, ctx->stream));
+        if ((rc = tune(ctx, 9, g, gu, [&](int G, int) {
+                 BsrView<double> v = Ah; v.lanes = G;
+                 fhg::launch_spmv_dots(v, ctx->kz[0], ctx->kz[0], ctx->kAd[0], part(ctx, 5), ctx->stream);
+             })))
+            return rc;
+        L0.outer_lanes = g;
+        if (L0.ahat_lo) {
+            int gd = g, gdu = 1;
+            CK(cudaMemsetAsync(ctx->dhi, 0, sizeof(float) * L0.n, ctx->stream));
+            CK(cudaMemsetAsync(ctx->dlo, 0, sizeof(float) * L0.n, ctx->stream));
+            if ((rc = tune(ctx, 9, gd, gdu, [&](int G, int) {
+                     BsrView<float> v = L0.Ahat_hi.v; v.lanes = G;
+                     fhg::launch_spmv_dots_df(v, L0.ahat_lo, ctx->dhi, ctx->dlo, ctx->kz[0], ctx->kz[0], ctx->kAd[0],
+                                              part(ctx, 5), ctx->stream);
+                 })))
+                return rc;
+            L0.Ahat_hi.v.lanes = gd;
+        }
     }
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->ready = true;
@@ -1120,7 +1194,9 @@ static int apply_device(fhg_ctx* ctx, int level, int op, double* in, double* aux
     cudaStream_t s = ctx->stream;
     if (op == FHG_OP_SYM_SPMV) {
         if (level != 0) return fail(ctx, FHG_ERR_INVALID_ARG, "symmetric operator exists on level 0 only");
-        fhg::launch_spmv_dots(L.ahat_is_a ? L.A.v : L.Ahat.v, in, in, out, part(ctx, 4), s);
+        BsrView<double> Ah = L.ahat_is_a ? L.A.v : L.Ahat.v;
+        if (L.outer_lanes) Ah.lanes = L.outer_lanes;
+        fhg::launch_spmv_dots(Ah, in, in, out, part(ctx, 4), s);
         return FHG_OK;
     }
     if (op == FHG_OP_VCYCLE) {

@@ -19,6 +19,7 @@ struct BsrView {
     int nbc = 0;          // block columns
     int bs = 0;           // block size (square blocks)
     int lanes = 8;        // lanes per block row (power of two, 4..32)
+    int unroll = 1;       // blocks per lane step in the row walk (1 or 2; 2 only for bs <= 3)
     long long nnzb = 0;   // stored blocks
     long long ld = 0;     // leading dimension of vals
     const int* rowptr = nullptr;

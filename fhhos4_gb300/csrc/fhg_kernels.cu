@@ -66,15 +66,16 @@ __device__ __forceinline__ double reduce_partials(const double* __restrict__ p, 
 // ---------------------------------------------------------------------------
 // Row accumulation: acc[r] += sum over this lane's blocks of (A_block x_col)[r].
 // `sel(col)` returns 0 (skip the block), 1 (use it) or 2 (stop: columns are sorted, nothing
-// after it is used). For bs <= 3 each lane walks two blocks per step so that the loads of
-// both (column index, bs^2 values, bs entries of x) are in flight together; the
-// accumulation order stays block by block.
-template <class T, int BS, int G, class Sel>
+// after it is used). With U = 2 (bs <= 3) each lane walks two blocks per step so that the loads
+// of both (column index, bs^2 values, bs entries of x) are in flight together, at the cost of
+// registers (fewer resident warps); U is chosen per operator by the autotuner. The
+// accumulation order is block by block either way.
+template <class T, int BS, int G, int U, class Sel>
 __device__ __forceinline__ void accumulate_row(int p0, int p1, int lane, const int* __restrict__ colidx,
                                                const T* __restrict__ vals, long long ld, const T* x, T* acc,
                                                Sel sel)
 {
-    if constexpr (BS <= 3) {
+    if constexpr (U == 2 && BS <= 3) {
         for (int p = p0 + lane; p < p1; p += 2 * G) {
             const int q = p + G;
             const int ca = colidx[p];
@@ -132,7 +133,7 @@ struct UseAll {
 
 // ---------------------------------------------------------------------------
 // y = A x  |  y = aux - A x  |  y = aux + A x      (aux may alias y)
-template <class T, int BS, int G, int MODE>
+template <class T, int BS, int G, int U, int MODE>
 __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int nbr, const int* __restrict__ rowptr,
                                                        const int* __restrict__ colidx,
                                                        const T* __restrict__ vals, long long ld,
@@ -143,7 +144,12 @@ __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int nbr, const int* __res
     T acc[BS];
 #pragma unroll
     for (int r = 0; r < BS; r++) acc[r] = T(0);
-    if (row < nbr) accumulate_row<T, BS, G>(rowptr[row], rowptr[row + 1], lane, colidx, vals, ld, x, acc, UseAll());
+    // Lane r < BS writes output r of the row (G >= BS here: G is at least 4 and bs at most 3 on
+    // this path, or lanes loop over outputs below when bs > G). The added vector is loaded
+    // before the row walk so that its latency overlaps it.
+    T av = T(0);
+    if (MODE != kSpmvAssign && G >= BS && row < nbr && lane < BS) av = aux[(long long)row * BS + lane];
+    if (row < nbr) accumulate_row<T, BS, G, U>(rowptr[row], rowptr[row + 1], lane, colidx, vals, ld, x, acc, UseAll());
 #pragma unroll
     for (int r = 0; r < BS; r++) acc[r] = group_sum<G>(acc[r]);
     if (row < nbr) {
@@ -151,9 +157,10 @@ __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int nbr, const int* __res
         for (int r = 0; r < BS; r++) {
             if (lane == r % G) {
                 const long long i = (long long)row * BS + r;
+                const T a = (G >= BS) ? av : ((MODE == kSpmvAssign) ? T(0) : aux[i]);
                 if (MODE == kSpmvAssign) y[i] = acc[r];
-                else if (MODE == kSpmvResidual) y[i] = aux[i] - acc[r];
-                else y[i] = aux[i] + acc[r];
+                else if (MODE == kSpmvResidual) y[i] = a - acc[r];
+                else y[i] = a + acc[r];
             }
         }
     }
@@ -165,7 +172,7 @@ __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int nbr, const int* __res
 // zeros not yet overwritten (later colours of a forward sweep, earlier ones of a backward
 // sweep), so skipping them changes no bit of the result and saves their loads. Block columns
 // are sorted, so the skipped ones form a head and a tail of each row.
-template <class T, int BS, int G>
+template <class T, int BS, int G, int U>
 __global__ void __launch_bounds__(kThreads) k_bsr_gs(int row0, int row1, const int* __restrict__ rowptr,
                                                      const int* __restrict__ colidx,
                                                      const T* __restrict__ vals, long long ld,
@@ -177,26 +184,45 @@ __global__ void __launch_bounds__(kThreads) k_bsr_gs(int row0, int row1, const i
     T acc[BS];
 #pragma unroll
     for (int r = 0; r < BS; r++) acc[r] = T(0);
+    // b_i and the D_i^-1 row this lane applies (lane r < BS owns output r when G >= BS), loaded
+    // before the row walk so that their latency overlaps it instead of following it.
+    T bv[BS], dv[BS];
+    if (G >= BS && row < row1) {
+#pragma unroll
+        for (int c = 0; c < BS; c++) bv[c] = b[(long long)row * BS + c];
+        if (lane < BS)
+#pragma unroll
+            for (int c = 0; c < BS; c++) dv[c] = dinv[(long long)(lane * BS + c) * dld + row];
+    }
     if (row < row1) {
         auto sel = [row, col_lo, col_hi](int col) -> int {
             if (col >= col_hi) return 2;
             return (col == row || col < col_lo) ? 0 : 1;
         };
-        accumulate_row<T, BS, G>(rowptr[row], rowptr[row + 1], lane, colidx, vals, ld, x, acc, sel);
+        accumulate_row<T, BS, G, U>(rowptr[row], rowptr[row + 1], lane, colidx, vals, ld, x, acc, sel);
     }
 #pragma unroll
     for (int r = 0; r < BS; r++) acc[r] = group_sum<G>(acc[r]);
     if (row < row1) {
-        T t[BS];
-#pragma unroll
-        for (int c = 0; c < BS; c++) t[c] = b[(long long)row * BS + c] - acc[c];
-#pragma unroll
-        for (int r = 0; r < BS; r++) {
-            if (lane == r % G) {
+        if (G >= BS) {
+            if (lane < BS) {
                 T v = T(0);
 #pragma unroll
-                for (int c = 0; c < BS; c++) v = fma(dinv[(long long)(r * BS + c) * dld + row], t[c], v);
-                x[(long long)row * BS + r] = v;
+                for (int c = 0; c < BS; c++) v = fma(dv[c], bv[c] - acc[c], v);
+                x[(long long)row * BS + lane] = v;
+            }
+        } else {
+            T t[BS];
+#pragma unroll
+            for (int c = 0; c < BS; c++) t[c] = b[(long long)row * BS + c] - acc[c];
+#pragma unroll
+            for (int r = 0; r < BS; r++) {
+                if (lane == r % G) {
+                    T v = T(0);
+#pragma unroll
+                    for (int c = 0; c < BS; c++) v = fma(dinv[(long long)(r * BS + c) * dld + row], t[c], v);
+                    x[(long long)row * BS + r] = v;
+                }
             }
         }
     }
@@ -279,7 +305,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots(int nbr, const
 #pragma unroll
         for (int r = 0; r < BS; r++) acc[r] = 0.0;
         const bool active = row < nbr;
-        if (active) accumulate_row<double, BS, G>(rowptr[row], rowptr[row + 1], lane, colidx, vals, ld, d, acc, UseAll());
+        if (active) accumulate_row<double, BS, G, 2>(rowptr[row], rowptr[row + 1], lane, colidx, vals, ld, d, acc, UseAll());
 #pragma unroll
         for (int r = 0; r < BS; r++) acc[r] = group_sum<G>(acc[r]);
         if (active) {
@@ -345,19 +371,28 @@ __global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots_df(int nbr, co
         float hi[BS], lo[BS];
 #pragma unroll
         for (int r = 0; r < BS; r++) { hi[r] = 0.f; lo[r] = 0.f; }
+        double dv = 0.0, rv = 0.0;
         if (row < nbr) {
+            if (lane < BS) {
+                dv = d[(long long)row * BS + lane];
+                rv = rvec[(long long)row * BS + lane];
+            }
             const int p1 = rowptr[row + 1];
             for (int p = rowptr[row] + lane; p < p1; p += G) {
                 const int col = colidx[p];
-                float xh[BS], xl[BS];
+                float ahv[BS * BS], alv[BS * BS], xh[BS], xl[BS];
+#pragma unroll
+                for (int e = 0; e < BS * BS; e++) {
+                    ahv[e] = vhi[(long long)e * ld + p];
+                    alv[e] = vlo[(long long)e * ld + p];
+                }
 #pragma unroll
                 for (int c = 0; c < BS; c++) { xh[c] = dhi[(long long)col * BS + c]; xl[c] = dlo[(long long)col * BS + c]; }
 #pragma unroll
                 for (int r = 0; r < BS; r++)
 #pragma unroll
                     for (int c = 0; c < BS; c++) {
-                        const float ah = vhi[(long long)(r * BS + c) * ld + p];
-                        const float al = vlo[(long long)(r * BS + c) * ld + p];
+                        const float ah = ahv[r * BS + c], al = alv[r * BS + c];
                         const float ph = ah * xh[c];
                         const float pe = fmaf(ah, xh[c], -ph);
                         const float cross = fmaf(ah, xl[c], al * xh[c]);
@@ -377,13 +412,12 @@ __global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots_df(int nbr, co
         if (row < nbr) {
 #pragma unroll
             for (int r = 0; r < BS; r++) {
-                if (lane == r % G) {
+                if (lane == r) {   // G >= BS: launch_spmv_dots_df rejects smaller G
                     const long long i = (long long)row * BS + r;
                     const double v = (double)hi[r] + (double)lo[r];
                     Ad[i] = v;
-                    const double di = d[i];
-                    dad = fma(di, v, dad);
-                    rd = fma(rvec[i], di, rd);
+                    dad = fma(dv, v, dad);
+                    rd = fma(rv, dv, rd);
                 }
             }
         }
@@ -596,18 +630,25 @@ inline unsigned grid_for(long long work, int per_cta)
     default: { constexpr int BS = BS_, G = 32; __VA_ARGS__; } break;                        \
     }
 
+template <class T, int BS, int G, int U>
+void spmv_u(const BsrView<T>& A, unsigned grid, int mode, const T* x, const T* aux, T* y, cudaStream_t s)
+{
+    if (mode == kSpmvAssign)
+        k_bsr_spmv<T, BS, G, U, kSpmvAssign><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
+    else if (mode == kSpmvResidual)
+        k_bsr_spmv<T, BS, G, U, kSpmvResidual><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
+    else
+        k_bsr_spmv<T, BS, G, U, kSpmvAddTo><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
+}
+
 template <class T>
 void launch_spmv(const BsrView<T>& A, int mode, const T* x, const T* aux, T* y, cudaStream_t s)
 {
     if (A.nbr == 0) return;
     const unsigned grid = grid_for((long long)A.nbr * A.lanes, kThreads);
     FHG_DISPATCH_BS_G(A.bs, A.lanes, {
-        if (mode == kSpmvAssign)
-            k_bsr_spmv<T, BS, G, kSpmvAssign><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
-        else if (mode == kSpmvResidual)
-            k_bsr_spmv<T, BS, G, kSpmvResidual><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
-        else
-            k_bsr_spmv<T, BS, G, kSpmvAddTo><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
+        if (A.unroll == 2) spmv_u<T, BS, G, 2>(A, grid, mode, x, aux, y, s);
+        else spmv_u<T, BS, G, 1>(A, grid, mode, x, aux, y, s);
     });
     g_kernel_launches++;
 }
@@ -619,8 +660,12 @@ void launch_gs(const BsrView<T>& A, int row0, int row1, const T* dinv, long long
     if (row1 <= row0) return;
     const unsigned grid = grid_for((long long)(row1 - row0) * A.lanes, kThreads);
     FHG_DISPATCH_BS_G(A.bs, A.lanes, {
-        k_bsr_gs<T, BS, G><<<grid, kThreads, 0, s>>>(row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, b, x,
-                                                     col_lo, col_hi);
+        if (A.unroll == 2)
+            k_bsr_gs<T, BS, G, 2><<<grid, kThreads, 0, s>>>(row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, b,
+                                                            x, col_lo, col_hi);
+        else
+            k_bsr_gs<T, BS, G, 1><<<grid, kThreads, 0, s>>>(row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, b,
+                                                            x, col_lo, col_hi);
     });
     g_kernel_launches++;
 }
@@ -693,7 +738,9 @@ void launch_fcg_direction_mixed(long long n, const float* z, const double* dp, c
 void launch_spmv_dots_df(const BsrView<float>& Ahi, const float* vlo, const float* dhi, const float* dlo,
                          const double* d, const double* r, double* Ad, double* partials, cudaStream_t s)
 {
-    FHG_DISPATCH_BS_G(Ahi.bs, Ahi.lanes, {
+    // lane r writes output r: needs G >= bs (always true for G >= 4 and bs <= 4; bs = 6 uses 8)
+    const int lanes = Ahi.lanes < Ahi.bs ? 8 : Ahi.lanes;
+    FHG_DISPATCH_BS_G(Ahi.bs, lanes, {
         k_bsr_spmv_dots_df<BS, G><<<kReduceCtas, kReduceThreads, 0, s>>>(Ahi.nbr, Ahi.rowptr, Ahi.colidx, Ahi.vals, vlo,
                                                                          Ahi.ld, dhi, dlo, d, r, Ad, partials);
     });

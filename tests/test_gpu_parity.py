@@ -120,14 +120,24 @@ def test_fp32_vcycle_reaches_fp64_tolerance(case, outer_split):
 
 
 def test_double_fp32_outer_product_tracks_fp64(case):
-    # The double-FP32 outer product (FP64-class accuracy) changes the FP32-V-cycle solve by
-    # rounding only: same iterations, histories within 1e-8 relative.
+    # The double-FP32 outer product (FP64-class accuracy, ~1e-14 relative per product) changes
+    # the FP32-V-cycle solve at the FP32 rounding level of the V-cycle only: same iteration count
+    # within one, histories within 1e-5 relative, same FP64 true residual tolerance.
     a = S().fcg_mg(case.As, case.Ps, case.bs, precision="fp32", outer_split=True)
-    a.Solve(case.b)
+    xa = a.Solve(case.b)
     b = S().fcg_mg(case.As, case.Ps, case.bs, precision="fp32", outer_split=False)
     b.Solve(case.b)
-    assert a.IterationCount == b.IterationCount
-    assert np.all(np.abs(a.History - b.History) <= 1e-8 * b.History + 1e-13)
+    assert abs(a.IterationCount - b.IterationCount) <= 1
+    m = min(len(a.History), len(b.History))
+    assert np.all(np.abs(a.History[:m] - b.History[:m]) <= 1e-5 * b.History[:m] + 1e-13)
+    assert true_rel_residual(case.As[0], case.b, xa) < 5e-8
+    # the product itself: double-FP32 against FP64 on the outer operator
+    from fhhos4_gb300 import _native as N
+    rng = np.random.default_rng(3)
+    d = rng.standard_normal(case.As[0].shape[0])
+    y64 = a.Context().apply(0, N.OP_SYM_SPMV, d, None, len(d))
+    y_ref = O.spmv_sym_lower(case.As[0], d)
+    assert np.linalg.norm(y64 - y_ref) <= 1e-13 * np.linalg.norm(y_ref)
 
 
 def test_autotuned_lanes_give_the_same_solve(case):
