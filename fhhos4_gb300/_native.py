@@ -36,7 +36,9 @@ OP_COARSE_SOLVE, OP_VCYCLE = 8, 9
 EXPORTS = ["fhg_default_options", "fhg_create", "fhg_destroy", "fhg_last_error", "fhg_set_level",
            "fhg_set_prolongation", "fhg_setup", "fhg_solve", "fhg_solve_device", "fhg_apply",
            "fhg_time_op", "fhg_set_vcycle_precision", "fhg_level_info", "fhg_get_permutation",
-           "fhg_kernel_launches"]
+           "fhg_kernel_launches", "fhg_residual_norm_noalloc"]
+
+FHG_NOALLOC_MAX_PARTIALS = 131072
 
 
 class FhgError(RuntimeError):
@@ -90,6 +92,8 @@ def load(path: str = LIB):
     lib.fhg_get_permutation.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
     lib.fhg_kernel_launches.argtypes = [C.c_void_p]
     lib.fhg_kernel_launches.restype = C.c_longlong
+    lib.fhg_residual_norm_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     _lib = lib
     return lib
 

@@ -149,6 +149,26 @@ int fhg_get_permutation(const fhg_ctx* ctx, int level, int* perm);
 /* Number of kernels this library has launched in this process (graph replays included). */
 long long fhg_kernel_launches(const fhg_ctx* ctx);
 
+/* Residual 2-norm ||b - A x|| of a face-block system, computed without allocating any memory.
+ * No counterpart in the reference: it exists for callers that cannot call cudaMalloc when they
+ * check a solution (while capturing a stream into a CUDA graph, or when every byte of device
+ * memory is owned by the caller's own pool or budget). The caller passes, in device memory it
+ * owns: the operator in libfhg's block layout (rowptr[n_block_rows+1], block colidx, values
+ * entry-major: entry r*bs+c of block p at vals[(r*bs+c)*ld + p], ld >= number of blocks), x, b
+ * (n_block_rows*block_size doubles each) and norm_out (one double, written on `stream`; NULL =
+ * the default stream). `lanes` (4, 8, 16, 32) is the number of lanes per block row.
+ * The per-block partial sums live in a fixed array inside the library, FHG_NOALLOC_MAX_PARTIALS
+ * doubles (1 MiB) on every GPU that loads it, held until the process exits; one partial sum per
+ * 256/lanes block rows, so n_block_rows may be at most FHG_NOALLOC_MAX_PARTIALS*256/lanes
+ * (4,194,304 block rows at 8 lanes): larger sizes return FHG_ERR_TOO_LARGE and launch nothing.
+ * The first call on a device looks up the array's device address on that device (make it before
+ * any stream capture). Calls share the array: two calls that overlap on the GPU race on it.
+ * Makes the device current for the call and restores the caller's current device. */
+#define FHG_NOALLOC_MAX_PARTIALS 131072
+int fhg_residual_norm_noalloc(int device, int n_block_rows, int block_size, int lanes,
+                              const int* rowptr, const int* colidx, const double* vals, long long ld,
+                              const double* x, const double* b, double* norm_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
