@@ -47,6 +47,11 @@ def parse():
     ap.add_argument("--dim", type=int, default=3)
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--k", type=int, default=1)
+    ap.add_argument("--coefficient", default="identity", choices=["identity", "checkerboard", "anisotropic",
+                                                                  "lognormal_patches"])
+    ap.add_argument("--contrast", type=float, default=1e6)
+    ap.add_argument("--source", default="sine", choices=["sine", "one"])
+    ap.add_argument("--max-coarse-rows", type=int, default=1000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-iterations", type=int, default=2)
     return ap.parse_args()
@@ -171,8 +176,10 @@ def committed_traffic():
 
 # --------------------------------------------------------------------------- workload
 def workload_config(args):
-    name = (f"{'3D tet' if args.dim == 3 else '2D tri'} {args.n}^{args.dim} HHO k={args.k} Poisson, "
-            "FCG(1)+geometric MG V(1,1) bgs/rbgs, tol 1e-8")
+    coef = "identity tensor" if args.coefficient == "identity" else (
+        f"{args.coefficient} coefficient (contrast {args.contrast:g})")
+    name = (f"{'3D tet' if args.dim == 3 else '2D tri'} {args.n}^{args.dim} HHO k={args.k} diffusion, {coef}, "
+            f"f={'sine' if args.source == 'sine' else '1'}, FCG(1)+geometric MG V(1,1) bgs/rbgs, tol 1e-8")
     return {"workload": name, "dim": args.dim, "n": args.n, "k": args.k, "mesh": "stetra" if args.dim == 3 else "stri",
             "krylov": "FCG(1)", "cycle": "V(1,1)", "smoothers": "bgs/rbgs (multicolour order)",
             "coarse": "FP64 dense inverse of the coarsest operator",
@@ -182,13 +189,16 @@ def workload_config(args):
 def generate(args):
     from fhhos4_gb300 import hho
     t0 = time.perf_counter()
-    As, Ps, b, bs = hho.generate(args.dim, args.n, args.k)
+    As, Ps, b, bs = hho.generate(args.dim, args.n, args.k, coefficient=args.coefficient, contrast=args.contrast,
+                                 source=args.source, max_coarse_rows=args.max_coarse_rows)
     return As, Ps, b, bs, time.perf_counter() - t0
 
 
 def reference_iterations(args):
     """Iterations of the reference (natural order) and of the reference in colour order, from the
     committed reference histories when present."""
+    if args.coefficient != "identity" or args.source != "sine" or args.dim != 3:
+        return None, None
     try:
         z = np.load(os.path.join(ROOT, "tests", "golden", f"tet3d_n{args.n}_k{args.k}.npz"))
         return len(z["hist_natural"]) - 1, len(z["hist_colour"]) - 1
@@ -364,7 +374,8 @@ def run_ours(args, dist: Dist):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64 (Krylov) / f32 (V-cycle)",
-        "data": "synthetic: the reference's own 64^3 tetrahedral HHO system, generated on the host",
+        "data": (f"synthetic: the reference's own {args.n}^{args.dim} HHO system ({args.coefficient} coefficient), "
+                 "generated on the host"),
         "config": dict(workload_config(args), parallelism=f"replicas x{dist.world}", method="FP32 V-cycle in FP64 FCG",
                        unknowns=n0, levels=len(As), colours_level0=ncol),
         "plain_fp64": {"s": round(results["fp64"]["s"], 6), "iterations": results["fp64"]["iterations"],
@@ -410,7 +421,8 @@ def run_reference(args, dist: Dist):
         "metric": METRIC, "value": round(value, 4), "unit": "s", "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(per_it * 1e3, 2), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
-        "data": "synthetic: the reference's own 64^3 tetrahedral HHO system, generated on the host",
+        "data": (f"synthetic: the reference's own {args.n}^{args.dim} HHO system ({args.coefficient} coefficient), "
+                 "generated on the host"),
         "config": dict(workload_config(args), parallelism="host cores", unknowns=n0),
         "cpu_baseline": {"value": round(value, 4), "unit": "s", "cores": threads, "kind": "port",
                          "sample": (f"{it} FCG(1)+V(1,1) iterations (one per step) of the {n0}-unknown solve by the "

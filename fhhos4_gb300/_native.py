@@ -24,7 +24,7 @@ FHG_ERR_NAN = -7
 FHG_ERR_TOO_LARGE = -8
 FHG_ERR_UNSUPPORTED = -9
 
-SMOOTHERS = {"bgs": 0, "rbgs": 1, "bj": 2, "bj23": 3}
+SMOOTHERS = {"bgs": 0, "rbgs": 1, "bj": 2, "bj23": 3, "sbgs": 4, "abgs": 5, "rabgs": 6}
 KRYLOV = {"fcg": 0, "cg": 1}
 PRECISION = {"fp64": 0, "fp32": 1}
 
@@ -52,7 +52,7 @@ class Options(C.Structure):
                 ("pre_iterations", C.c_int), ("post_iterations", C.c_int), ("omega", C.c_double),
                 ("tolerance", C.c_double), ("max_iterations", C.c_int), ("vcycle_precision", C.c_int),
                 ("colouring", C.c_int), ("use_graphs", C.c_int), ("autotune", C.c_int),
-                ("max_coarse_rows", C.c_int), ("outer_split", C.c_int)]
+                ("max_coarse_rows", C.c_int), ("outer_split", C.c_int), ("w_loops", C.c_int)]
 
 
 class SolveInfo(C.Structure):

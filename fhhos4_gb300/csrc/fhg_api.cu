@@ -531,16 +531,31 @@ void smooth(fhg_ctx* ctx, int l, int code, int iters, const T* b, T* x, bool fro
     cudaStream_t s = ctx->stream;
     BsrView<T> A = V::A(L);
     if (L.gs_lanes) { A.lanes = L.gs_lanes; A.unroll = L.gs_unroll; }
+    auto forward = [&](bool zero) {
+        for (int c = 0; c < L.ncolours; c++)
+            fhg::launch_gs<T>(A, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s, 0,
+                              zero ? L.colour_start[c + 1] : 0x7fffffff);
+    };
+    auto backward = [&](bool zero) {
+        for (int c = L.ncolours - 1; c >= 0; c--)
+            fhg::launch_gs<T>(A, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s,
+                              zero ? L.colour_start[c] : 0, 0x7fffffff);
+    };
     for (int it = 0; it < iters; it++) {
         const bool zero = from_zero && it == 0;
+        // BlockGaussSeidel directions (src/Solver/FixedPoint/BlockGaussSeidel.h:84-120); the
+        // alternating ones switch by iteration parity, IterationCount restarting at every smoothing.
         if (code == FHG_SMOOTHER_BGS) {
-            for (int c = 0; c < L.ncolours; c++)
-                fhg::launch_gs<T>(A, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s, 0,
-                                  zero ? L.colour_start[c + 1] : 0x7fffffff);
+            forward(zero);
         } else if (code == FHG_SMOOTHER_RBGS) {
-            for (int c = L.ncolours - 1; c >= 0; c--)
-                fhg::launch_gs<T>(A, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s,
-                                  zero ? L.colour_start[c] : 0, 0x7fffffff);
+            backward(zero);
+        } else if (code == FHG_SMOOTHER_SBGS) {
+            forward(zero);
+            backward(false);
+        } else if (code == FHG_SMOOTHER_ABGS) {
+            if (it % 2 == 0) forward(zero); else backward(false);
+        } else if (code == FHG_SMOOTHER_RABGS) {
+            if (it % 2 == 0) backward(zero); else forward(false);
         } else {
             const T omega = code == FHG_SMOOTHER_BJ23 ? T(2.0 / 3.0) : T(ctx->opts.omega);
             T* tmp = V::r(L);
@@ -550,9 +565,13 @@ void smooth(fhg_ctx* ctx, int l, int code, int iters, const T* b, T* x, bool fro
     }
 }
 
-// One V-cycle on level l from x = 0 (src/Solver/Multigrid/Multigrid.h:438-608).
+bool is_gs(int code) { return code != FHG_SMOOTHER_BJ && code != FHG_SMOOTHER_BJ23; }
+
+// One multigrid cycle on level l (src/Solver/Multigrid/Multigrid.h:438-608): V for w_loops = 1,
+// W for 2 (the coarse correction repeated, except directly above the coarsest level). x is the
+// initial guess, zero when x_zero.
 template <class T>
-void vcycle(fhg_ctx* ctx, int l, const T* b, T* x)
+void mg_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
 {
     Level& L = ctx->levels[l];
     using V = LevelVecs<T>;
@@ -564,15 +583,22 @@ void vcycle(fhg_ctx* ctx, int l, const T* b, T* x)
     Level& C = ctx->levels[l + 1];
     // A zero-start GS sweep writes every entry before any is read: no clearing needed then.
     const int pre = ctx->opts.pre_smoother;
-    const bool gs_pre = (pre == FHG_SMOOTHER_BGS || pre == FHG_SMOOTHER_RBGS) && ctx->opts.pre_iterations > 0;
-    if (!gs_pre) cudaMemsetAsync(x, 0, sizeof(T) * (size_t)L.n, s);
-    smooth<T>(ctx, l, pre, ctx->opts.pre_iterations, b, x, gs_pre);
+    const bool gs_zero = x_zero && is_gs(pre) && ctx->opts.pre_iterations > 0;
+    if (x_zero && !gs_zero) cudaMemsetAsync(x, 0, sizeof(T) * (size_t)L.n, s);
+    smooth<T>(ctx, l, pre, ctx->opts.pre_iterations, b, x, gs_zero);
     fhg::launch_spmv<T>(V::A(L), fhg::kSpmvResidual, x, b, V::r(L), s);
     fhg::launch_spmv<T>(V::R(L), fhg::kSpmvAssign, V::r(L), nullptr, V::b(C), s);
-    vcycle<T>(ctx, l + 1, V::b(C), V::x(C));
+    const int loops = ctx->opts.w_loops > 1 ? ctx->opts.w_loops : 1;
+    for (int w = 0; w < loops; w++) {
+        mg_cycle<T>(ctx, l + 1, V::b(C), V::x(C), w == 0);
+        if (l + 1 == ctx->nlevels - 1) break;
+    }
     fhg::launch_spmv<T>(V::P(L), fhg::kSpmvAddTo, V::x(C), x, x, s);
     smooth<T>(ctx, l, ctx->opts.post_smoother, ctx->opts.post_iterations, b, x);
 }
+
+template <class T>
+void vcycle(fhg_ctx* ctx, int l, const T* b, T* x) { mg_cycle<T>(ctx, l, b, x, true); }
 
 // z = M r in the configured precision (level-0 numbering, FP64 in/out).
 void precondition(fhg_ctx* ctx, const double* r, double* z)
@@ -837,6 +863,7 @@ void fhg_default_options(fhg_options* o)
     o->autotune = 0;
     o->max_coarse_rows = 8192;
     o->outer_split = 1;
+    o->w_loops = 1;
 }
 
 int fhg_create(fhg_ctx** out, int device)
@@ -928,8 +955,9 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
     if (o.max_coarse_rows <= 0) o.max_coarse_rows = 8192;
     if (o.max_iterations < 0 || o.pre_iterations < 0 || o.post_iterations < 0)
         return fail(ctx, FHG_ERR_INVALID_ARG, "negative iteration count");
-    if (o.pre_smoother < 0 || o.pre_smoother > 3 || o.post_smoother < 0 || o.post_smoother > 3)
+    if (o.pre_smoother < 0 || o.pre_smoother > 6 || o.post_smoother < 0 || o.post_smoother > 6)
         return fail(ctx, FHG_ERR_INVALID_ARG, "unknown smoother code");
+    if (o.w_loops < 1) o.w_loops = 1;
     if (nlevels <= 0 || nlevels > (int)ctx->levels.size())
         return fail(ctx, FHG_ERR_INVALID_ARG, "nlevels=%d but %zu levels were given", nlevels, ctx->levels.size());
     ctx->nlevels = nlevels;

@@ -631,6 +631,7 @@ struct ElementOps {
     Mat interp;  // nR x nF nf: P [solve_cells; I] (ReconstructionFromFacesMatrix)
     std::vector<double> bT;    // nC: (f, c_j)_T
     std::vector<double> bF;    // nF nf: condensed RHS contribution
+    std::vector<double> cell_rhs;  // nC: A_TT^{-1} b_T (cell unknowns = cell_rhs + solve_cells x_F)
     bool ok = true;
 };
 
@@ -872,6 +873,8 @@ ElementOps element_ops(const Mesh& M, int e, const Params& prm, const Rules& rul
             for (int c = 0; c < nC; c++) s -= Atf(c, i) * X(c, j);
             O.schur(i, j) = s;
         }
+    O.cell_rhs.assign(nC, 0.0);
+    for (int c = 0; c < nC; c++) O.cell_rhs[c] = rhsb(c, 0);
     O.bF.assign(nFF, 0.0);
     for (int i = 0; i < nFF; i++) {
         double s = 0;
@@ -1174,6 +1177,9 @@ struct fhg_hho {
     std::vector<Level> levels;
     std::string err;
     int block_size = 0;
+    Params prm{2, 1, 0};
+    Rules rules;
+    int threads = 1;
 };
 
 extern "C" {
@@ -1207,6 +1213,8 @@ int fhg_hho_create(fhg_hho** out, const fhg_hho_params* p)
     const int threads = p->threads > 0 ? p->threads : (int)std::max(1u, std::thread::hardware_concurrency());
     Params prm{p->dim, p->k, p->source == FHG_HHO_SOURCE_ONE ? 1 : 0};
     Rules rules;
+    H->prm = prm;
+    H->threads = threads;
     // cell: exact to degree 2k+2 (mass of P_{k+1}); face: degree 2k+1; RHS: high order.
     const int dim = p->dim;
     rules.cell = simplex_rule(dim, (2 * p->k + 2 + dim + 1) / 2 + 1);
@@ -1259,6 +1267,7 @@ int fhg_hho_create(fhg_hho** out, const fhg_hho_params* p)
         }
     }
     std::vector<ElementOps>().swap(H->levels.back().ops);
+    H->rules = rules;
     return 0;
 }
 
@@ -1294,6 +1303,63 @@ int fhg_hho_prolongation(const fhg_hho* h, int l, int* n_rows, int* n_cols, long
     if (rowptr) *rowptr = L.P_rowptr.data();
     if (colidx) *colidx = L.P_colidx.data();
     if (vals) *vals = L.P_vals.data();
+    return 0;
+}
+
+// Relative L2 error of the k+1 reconstruction of a face solution against the exact solution
+// u = prod sin(pi x_i) of the sine source: cell unknowns recovered element by element
+// (Diffusion_HHO::HybridCoeffsBySolvingCellUnknowns, src/Discretizations/HHO/Diffusion_HHO.h:855-882),
+// reconstruction P [x_T; x_F] (ReconstructHigherOrderApproximationFromHybridCoeffs, :896-912), error
+// sqrt(sum_T |u_h - u|^2_T) / sqrt(sum_T |u|^2_T) (Diffusion_HHO::L2Error, :120-150).
+int fhg_hho_l2_error(const fhg_hho* h, const double* x, double* rel_error)
+{
+    if (!h || !x || !rel_error || h->levels.empty()) return -1;
+    if (h->prm.source != 0) return -2;  // no closed-form solution for this source
+    const Level& L = h->levels[0];
+    const Mesh& M = L.mesh;
+    const int dim = M.dim, nF = dim + 1, nf = h->block_size;
+    const size_t ne = M.el.size();
+    const int nthreads = std::max(1, h->threads);
+    const size_t chunk = (ne + nthreads - 1) / nthreads;
+    std::vector<double> err(nthreads, 0.0), nrm(nthreads, 0.0);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthreads; t++)
+        th.emplace_back([&, t]() {
+            const size_t e0 = t * chunk, e1 = std::min(ne, e0 + chunk);
+            for (size_t e = e0; e < e1; e++) {
+                const ElementOps O = element_ops(M, (int)e, h->prm, h->rules, true);
+                const int nC = O.nC, nR = O.nR, nFF = nF * nf;
+                std::vector<double> hyb(nC + nFF, 0.0);
+                for (int lf = 0; lf < nF; lf++) {
+                    const int g = M.number[M.ef[e][lf]];
+                    if (g < 0) continue;
+                    for (int a = 0; a < nf; a++) hyb[nC + lf * nf + a] = x[(size_t)g * nf + a];
+                }
+                for (int c = 0; c < nC; c++) {
+                    double v = O.cell_rhs[c];
+                    for (int j = 0; j < nFF; j++) v += O.solve_cells(c, j) * hyb[nC + j];
+                    hyb[c] = v;
+                }
+                std::vector<double> coef(nR, 0.0);
+                for (int i = 0; i < nR; i++)
+                    for (int j = 0; j < nC + nFF; j++) coef[i] += O.P(i, j) * hyb[j];
+                const QPts Q = element_points(M, (int)e, h->rules.cell_rhs);
+                double vals[64];
+                for (size_t q = 0; q < Q.w.size(); q++) {
+                    O.basis.eval(Q.x[q].data(), vals, nullptr);
+                    double uh = 0;
+                    for (int i = 0; i < nR; i++) uh += coef[i] * vals[i];
+                    double u = 1.0;
+                    for (int d = 0; d < dim; d++) u *= std::sin(kPi * Q.x[q][d]);
+                    err[t] += Q.w[q] * (uh - u) * (uh - u);
+                    nrm[t] += Q.w[q] * u * u;
+                }
+            }
+        });
+    for (auto& t : th) t.join();
+    double E = 0, U = 0;
+    for (int t = 0; t < nthreads; t++) { E += err[t]; U += nrm[t]; }
+    *rel_error = U > 0 ? std::sqrt(E) / std::sqrt(U) : std::sqrt(E);
     return 0;
 }
 

@@ -44,6 +44,9 @@ int fhg_hho_level(const fhg_hho* h, int level, int* n_rows, long long* nnz, cons
 int fhg_hho_prolongation(const fhg_hho* h, int level, int* n_rows, int* n_cols, long long* nnz,
                          const int** rowptr, const int** colidx, const double** vals);
 int fhg_hho_rhs(const fhg_hho* h, const double** b);
+/* Relative L2 error of the reconstruction of face solution x (level-0 numbering) against the
+ * exact solution of the sine source; -2 for sources without a closed form. */
+int fhg_hho_l2_error(const fhg_hho* h, const double* x, double* rel_error);
 
 #ifdef __cplusplus
 }

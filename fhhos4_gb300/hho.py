@@ -47,6 +47,7 @@ def lib():
         L.fhg_hho_prolongation.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int), P(C.c_longlong),
                                            P(P(C.c_int)), P(P(C.c_int)), P(P(C.c_double))]
         L.fhg_hho_rhs.argtypes = [C.c_void_p, P(P(C.c_double))]
+        L.fhg_hho_l2_error.argtypes = [C.c_void_p, C.c_void_p, P(C.c_double)]
         _lib = L
     return _lib
 
@@ -103,6 +104,16 @@ class Hierarchy:
         L.fhg_hho_rhs(self.h, C.byref(p))
         n = self.A_rows(0)
         return _arr(p, n, np.float64)
+
+    def l2_error(self, x) -> float:
+        """Relative L2 error of the k+1 reconstruction of face solution x against the exact solution
+        (sine source only), as the reference's Diffusion_HHO::L2Error."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = C.c_double()
+        rc = lib().fhg_hho_l2_error(self.h, C.c_void_p(x.ctypes.data), C.byref(out))
+        if rc != 0:
+            raise RuntimeError("no exact solution for this source" if rc == -2 else "l2_error failed")
+        return out.value
 
     def A_rows(self, l: int) -> int:
         n = C.c_int()

@@ -100,8 +100,10 @@ class Multigrid(IterativeSolver):
         return self._nLevels
 
     def _check_supported(self):
-        if self.Cycle != "V" or self.WLoops != 1:
-            raise NotImplementedError("only the V-cycle (Cycle='V', WLoops=1) runs on the GPU")
+        if self.Cycle not in ("V", "W"):
+            raise NotImplementedError("V- and W-cycles run on the GPU (Cycle='V' or 'W')")
+        if self.Cycle == "W" and self.WLoops < 2:
+            self.WLoops = 2
         for code in (self.PreSmootherCode, self.PostSmootherCode):
             if code not in N.SMOOTHERS:
                 raise NotImplementedError(f"smoother '{code}' (GPU smoothers: {sorted(N.SMOOTHERS)})")
@@ -147,6 +149,7 @@ class _KrylovOnGpu(IterativeSolver):
         o.autotune = 1 if mg.Autotune else 0
         o.max_coarse_rows = mg.MaxCoarseRows
         o.outer_split = 1 if self.OuterSplit else 0
+        o.w_loops = mg.WLoops if mg.Cycle == "W" else 1
         return o
 
     def Setup(self, A):
@@ -220,7 +223,7 @@ class ConjugateGradient(_KrylovOnGpu):
 
 def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: str = "bgs", post: str = "rbgs",
            precision: str = "fp64", krylov: str = "fcg", device: int = 0, autotune: bool = False,
-           use_graphs: bool = True, outer_split: bool = True):
+           use_graphs: bool = True, outer_split: bool = True, cycle: str = "V"):
     """SolverFactory-style construction of "-s fcgmg -cycle V,1,1" (src/Solver/SolverFactory.h:156-200)."""
     mg = Multigrid(len(As))
     mg.SetHierarchy(As, Ps)
@@ -228,6 +231,8 @@ def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: st
     mg.PreSmootherCode, mg.PostSmootherCode = pre, post
     mg.VCyclePrecision = precision
     mg.Autotune = autotune
+    mg.Cycle = cycle
+    mg.WLoops = 2 if cycle == "W" else 1
     solver = FlexibleConjugateGradient(1) if krylov == "fcg" else ConjugateGradient()
     solver.Precond = SolverPreconditioner(mg)
     solver.Tolerance = tol

@@ -40,6 +40,9 @@ extern "C" {
 #define FHG_SMOOTHER_RBGS 1   /* "rbgs": block Gauss-Seidel, backward (reverse colour order) */
 #define FHG_SMOOTHER_BJ 2     /* "bj": block Jacobi, relaxation omega */
 #define FHG_SMOOTHER_BJ23 3   /* "bj23": block Jacobi, omega = 2/3 */
+#define FHG_SMOOTHER_SBGS 4   /* "sbgs": symmetric block Gauss-Seidel (forward then backward) */
+#define FHG_SMOOTHER_ABGS 5   /* "abgs": alternating block Gauss-Seidel, forward first */
+#define FHG_SMOOTHER_RABGS 6  /* "rabgs": alternating block Gauss-Seidel, backward first */
 
 /* Krylov codes: "fcg" = FlexibleConjugateGradient(1) (src/Solver/Krylov/FlexibleConjugateGradient.h:21-25),
  * "cg" = ConjugateGradient (src/Solver/Krylov/ConjugateGradient.h:6-104). */
@@ -71,6 +74,7 @@ typedef struct {
     int outer_split;            /* FP32 V-cycle only: 1 = the outer FCG operator product in double-FP32
                                    arithmetic (FP32 pairs, ~2^-47 relative per term, on the FP32 pipe);
                                    0 = native FP64. GB300's FP64 pipe is 56x slower than FP32. */
+    int w_loops;                /* Multigrid::WLoops: 1 = V-cycle, 2 = W-cycle ("-cycle W,..", main.cpp:1179-1215) */
 } fhg_options;
 
 typedef struct {

@@ -381,32 +381,53 @@ typedef struct {
     double** tmp;
 } orc_mg;
 
+/* One smoother application of `iters` iterations: BlockGaussSeidel::ExecuteOneIteration's
+ * directions (BlockGaussSeidel.h:84-120): symmetric = forward then backward; alternating =
+ * forward/backward by iteration parity (IterationCount restarts at 0 in every Solve). */
 static void smooth(orc_mg* mg, int l, int code, int iters, const double* b, double* x)
 {
     for (int s = 0; s < iters; s++) {
-        if (code == ORC_BJ) jacobi_sweep(&mg->A[l], &mg->D[l], mg->opt->omega, b, x, mg->tmp[l]);
-        else gs_sweep(&mg->A[l], &mg->D[l], b, x, code == ORC_BGS_BACKWARD);
+        switch (code) {
+        case ORC_BJ: jacobi_sweep(&mg->A[l], &mg->D[l], mg->opt->omega, b, x, mg->tmp[l]); break;
+        case ORC_BGS_FORWARD: gs_sweep(&mg->A[l], &mg->D[l], b, x, 0); break;
+        case ORC_BGS_BACKWARD: gs_sweep(&mg->A[l], &mg->D[l], b, x, 1); break;
+        case ORC_BGS_SYMMETRIC:
+            gs_sweep(&mg->A[l], &mg->D[l], b, x, 0);
+            gs_sweep(&mg->A[l], &mg->D[l], b, x, 1);
+            break;
+        case ORC_BGS_ALTERNATING_FORWARD_FIRST: gs_sweep(&mg->A[l], &mg->D[l], b, x, s % 2); break;
+        default: gs_sweep(&mg->A[l], &mg->D[l], b, x, 1 - s % 2); break;
+        }
     }
 }
 
-static void vcycle(orc_mg* mg, int l, const double* b, double* x)
+/* Multigrid::MultigridCycle (Multigrid.h:438-608) for V (WLoops 1) and W (WLoops 2): x is the
+ * initial guess (zero when x_zero); the coarse correction loops WLoops times except directly
+ * above the coarsest level. */
+static void cycle(orc_mg* mg, int l, const double* b, double* x, int x_zero)
 {
     int n = mg->A[l].n_rows;
     if (l == mg->nlevels - 1) {
         ldlt_solve(&mg->coarse, b, x);
         return;
     }
-    memset(x, 0, sizeof(double) * (size_t)n);
+    if (x_zero) memset(x, 0, sizeof(double) * (size_t)n);
     smooth(mg, l, mg->opt->pre_smoother, mg->opt->pre_iterations, b, x);
     orc_residual(&mg->A[l], b, x, mg->r[l]);
     orc_spmv(&mg->R[l], mg->r[l], mg->rc[l]);
     int nc = mg->A[l + 1].n_rows;
     memset(mg->ec[l], 0, sizeof(double) * (size_t)nc);
-    vcycle(mg, l + 1, mg->rc[l], mg->ec[l]);
+    const int loops = mg->opt->w_loops > 1 ? mg->opt->w_loops : 1;
+    for (int w = 0; w < loops; w++) {
+        cycle(mg, l + 1, mg->rc[l], mg->ec[l], w == 0);
+        if (l + 1 == mg->nlevels - 1) break;
+    }
     orc_spmv(&mg->P[l], mg->ec[l], mg->r[l]);
     for (int i = 0; i < n; i++) x[i] += mg->r[l][i];
     smooth(mg, l, mg->opt->post_smoother, mg->opt->post_iterations, b, x);
 }
+
+static void vcycle(orc_mg* mg, int l, const double* b, double* x) { cycle(mg, l, b, x, 1); }
 
 static double dot(const double* a, const double* b, int n)
 {

@@ -21,7 +21,8 @@ typedef struct {
     const double* vals;  /* nnz */
 } orc_csr;
 
-enum { ORC_BGS_FORWARD = 0, ORC_BGS_BACKWARD = 1, ORC_BJ = 2 };
+enum { ORC_BGS_FORWARD = 0, ORC_BGS_BACKWARD = 1, ORC_BJ = 2, ORC_BGS_SYMMETRIC = 3,
+       ORC_BGS_ALTERNATING_FORWARD_FIRST = 4, ORC_BGS_ALTERNATING_BACKWARD_FIRST = 5 };
 enum { ORC_KRYLOV_FCG = 0, ORC_KRYLOV_CG = 1 };
 
 typedef struct {
@@ -31,6 +32,7 @@ typedef struct {
     int krylov;                        /* ORC_KRYLOV_FCG (FCG(1)) or ORC_KRYLOV_CG */
     double tolerance;
     int max_iterations;
+    int w_loops;                       /* Multigrid::WLoops: 1 V-cycle, 2 W-cycle */
 } orc_options;
 
 /* y = A x, one sequential sum per row in column order (Eigen SparseDenseProduct.h:34-70). */

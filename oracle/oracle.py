@@ -18,10 +18,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
 
-BGS_FORWARD, BGS_BACKWARD, BJ = 0, 1, 2
+BGS_FORWARD, BGS_BACKWARD, BJ, SBGS, ABGS, RABGS = 0, 1, 2, 3, 4, 5
 KRYLOV_FCG, KRYLOV_CG = 0, 1
 SMOOTHER_CODES = {"bgs": (BGS_FORWARD, 1.0), "rbgs": (BGS_BACKWARD, 1.0),
-                  "bj": (BJ, 1.0), "bj23": (BJ, 2.0 / 3.0)}
+                  "bj": (BJ, 1.0), "bj23": (BJ, 2.0 / 3.0), "sbgs": (SBGS, 1.0),
+                  "abgs": (ABGS, 1.0), "rabgs": (RABGS, 1.0)}
 
 
 class _CSR(C.Structure):
@@ -33,7 +34,7 @@ class _CSR(C.Structure):
 class _Opts(C.Structure):
     _fields_ = [("pre_smoother", C.c_int), ("post_smoother", C.c_int), ("omega", C.c_double),
                 ("pre_iterations", C.c_int), ("post_iterations", C.c_int), ("krylov", C.c_int),
-                ("tolerance", C.c_double), ("max_iterations", C.c_int)]
+                ("tolerance", C.c_double), ("max_iterations", C.c_int), ("w_loops", C.c_int)]
 
 
 _lib = None
@@ -150,7 +151,7 @@ def last_timing():
 
 
 def fcgmg_solve(As, Ps, b, bs, pre="bgs", post="rbgs", krylov="fcg", tol=1e-8, maxit=200,
-                pre_iterations=1, post_iterations=1):
+                pre_iterations=1, post_iterations=1, cycle="V"):
     """Returns (x, history, iterations, status)."""
     keep: list = []
     nl = len(As)
@@ -159,7 +160,7 @@ def fcgmg_solve(As, Ps, b, bs, pre="bgs", post="rbgs", krylov="fcg", tol=1e-8, m
     pc, om = SMOOTHER_CODES[pre]
     qc, om2 = SMOOTHER_CODES[post]
     opts = _Opts(pc, qc, om if pc == BJ else om2, pre_iterations, post_iterations,
-                 KRYLOV_CG if krylov == "cg" else KRYLOV_FCG, tol, maxit)
+                 KRYLOV_CG if krylov == "cg" else KRYLOV_FCG, tol, maxit, 2 if cycle == "W" else 1)
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.zeros(As[0].shape[0])
     hist = np.zeros(maxit + 1)

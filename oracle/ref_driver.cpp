@@ -12,7 +12,7 @@
 //         residual history captured through IterativeSolver::OnIterationEnd
 //         (src/Solver/IterativeSolver.h:224-227) and the solution x.
 //
-//   solve <dir> [--smoothers pre,post] [--krylov fcg|cg] [--tol t] [--maxit m]
+//   solve <dir> [--smoothers pre,post] [--krylov fcg|cg] [--cycle V|W] [--tol t] [--maxit m]
 //         Reads a hierarchy (possibly re-ordered by the caller) from <dir>, feeds it
 //         to the reference's own Multigrid / BlockGaussSeidel / EigenSparseCholesky /
 //         FlexibleConjugateGradient classes through a Level subclass that only
@@ -232,6 +232,12 @@ static int RunGen(int n, int k, const std::string& outdir, const std::string& pr
 		WriteArray(outdir + "/x.f64", x.data(), (size_t)x.rows());
 		WriteArray(outdir + "/history.f64", hist.data(), hist.size());
 		meta << ", \"iterations\": " << fcg->IterationCount << ", \"solve_s\": " << t.Elapsed().InSeconds();
+		// Post-processing as Program_Diffusion_HHO::Execute (src/Program/Program_Diffusion_HHO.h:319-390):
+		// cell unknowns, k+1 reconstruction, relative L2 error against the exact solution.
+		Vector recon = pb->ReconstructHigherOrderApproximationFromFaceCoeffs(x);
+		double l2 = pb->L2Error(tc->ExactSolution, recon);
+		meta.precision(17);
+		meta << ", \"l2_error\": " << l2;
 	}
 	meta << "}\n";
 	WriteText(outdir + "/meta.json", meta.str());
@@ -275,7 +281,7 @@ protected:
 	Level* CreateCoarseLevel(Level* fineLevel, CoarseningType, int) override { return levels[fineLevel->Number + 1]; }
 };
 
-static int RunSolve(const std::string& dir, const std::string& pre, const std::string& post, const std::string& krylov, double tol, int maxit)
+static int RunSolve(const std::string& dir, const std::string& pre, const std::string& post, const std::string& krylov, double tol, int maxit, char cycle)
 {
 	auto meta = ReadArray<int>(dir + "/levels.i32"); // [nLevels, blockSize]
 	int nLevels = meta[0], bs = meta[1];
@@ -292,8 +298,9 @@ static int RunSolve(const std::string& dir, const std::string& pre, const std::s
 		mg->levels.push_back(lev);
 	}
 	// Parameters as SolverFactory::SetMultigridParameters (src/Solver/SolverFactory.h:236-310).
-	mg->Cycle = 'V';
-	mg->WLoops = 1;
+	// "-cycle V,1,1" / "-cycle W,1,1" (src/main.cpp:1179-1215)
+	mg->Cycle = cycle;
+	mg->WLoops = cycle == 'W' ? 2 : 1;
 	mg->PreSmootherCode = pre;
 	mg->PostSmootherCode = post;
 	mg->PreSmoothingIterations = 1;
@@ -345,6 +352,7 @@ int main(int argc, char** argv)
 	if (argc < 2) { fprintf(stderr, "usage: ref_driver gen|solve ...\n"); return 1; }
 	std::string mode = argv[1];
 	std::string pre = "bgs", post = "rbgs", krylov = "fcg";
+	char cycle = 'V';
 	double tol = 1e-8;
 	int maxit = 200;
 	bool solve = true;
@@ -357,6 +365,7 @@ int main(int argc, char** argv)
 		else if (a == "--tol" && i + 1 < argc) tol = atof(argv[++i]);
 		else if (a == "--maxit" && i + 1 < argc) maxit = atoi(argv[++i]);
 		else if (a == "--no-solve") solve = false;
+		else if (a == "--cycle" && i + 1 < argc) cycle = argv[++i][0];
 		else pos.push_back(a);
 	}
 	std::cout.setstate(std::ios_base::failbit); // the reference logs to stdout; keep it quiet
@@ -368,7 +377,7 @@ int main(int argc, char** argv)
 		else rc = RunGen<3>(n, k, pos[3], pre, post, solve);
 	}
 	else if (mode == "solve" && pos.size() == 1)
-		rc = RunSolve(pos[0], pre, post, krylov, tol, maxit);
+		rc = RunSolve(pos[0], pre, post, krylov, tol, maxit, cycle);
 	else
 		fprintf(stderr, "bad arguments\n");
 	std::cout.clear();

@@ -9,7 +9,8 @@ checkout by ``make -C oracle ref``) and stores, per case, in a compressed .npz:
 * the colour permutation of every level computed by the oracle's greedy
   colouring, and the reference's own classes re-run on the colour-permuted
   hierarchy (``hist_colour``, ``x_colour`` in the permuted numbering), for
-  block GS (bgs/rbgs), block Jacobi (bj23) and PCG (``cg``).
+  block GS (bgs/rbgs), block Jacobi (bj23), PCG (``cg``), the W-cycle (``w``), symmetric block
+  GS (``sbgs``) and alternating block GS (``abgs``/``rabgs``).
 
 Only ``hist_*`` summaries are kept for the large cases (``--histories-only``).
 
@@ -75,7 +76,7 @@ def ref_gen(dim, n, k, out):
     return meta, As, Ps, b, np.fromfile(f"{out}/history.f64"), np.fromfile(f"{out}/x.f64")
 
 
-def ref_solve(As, Ps, b, bs, work, smoothers="bgs,rbgs", krylov="fcg"):
+def ref_solve(As, Ps, b, bs, work, smoothers="bgs,rbgs", krylov="fcg", cycle="V"):
     os.makedirs(work, exist_ok=True)
     np.asarray([len(As), bs], dtype=np.int32).tofile(f"{work}/levels.i32")
     for l, A in enumerate(As):
@@ -83,7 +84,8 @@ def ref_solve(As, Ps, b, bs, work, smoothers="bgs,rbgs", krylov="fcg"):
     for l, P in enumerate(Ps):
         dump_csr(f"{work}/L{l}_P", P)
     np.asarray(b, dtype=np.float64).tofile(f"{work}/b.f64")
-    subprocess.run([O.REF_DRIVER, "solve", work, "--smoothers", smoothers, "--krylov", krylov], check=True)
+    subprocess.run([O.REF_DRIVER, "solve", work, "--smoothers", smoothers, "--krylov", krylov, "--cycle", cycle],
+                   check=True)
     return np.fromfile(f"{work}/out_history.f64"), np.fromfile(f"{work}/out_x.f64")
 
 
@@ -98,18 +100,24 @@ def make_case(name, dim, n, k, histories_only=False):
         hist_col, x_col = ref_solve(Ac, Pc, bc, bs, os.path.join(tmp, "col"))
         hist_bj, x_bj = ref_solve(Ac, Pc, bc, bs, os.path.join(tmp, "bj"), smoothers="bj23,bj23")
         hist_cg, x_cg = ref_solve(Ac, Pc, bc, bs, os.path.join(tmp, "cg"), krylov="cg")
+        hist_w, x_w = ref_solve(Ac, Pc, bc, bs, os.path.join(tmp, "w"), cycle="W")
+        hist_sbgs, x_sbgs = ref_solve(Ac, Pc, bc, bs, os.path.join(tmp, "sbgs"), smoothers="sbgs,sbgs")
+        hist_abgs, x_abgs = ref_solve(Ac, Pc, bc, bs, os.path.join(tmp, "abgs"), smoothers="abgs,rabgs")
         out = dict(
             dim=dim, n=n, k=k, block_size=bs, levels=len(As),
             hist_natural=hist_nat, hist_colour=hist_col, hist_bj23=hist_bj, hist_cg=hist_cg,
+            hist_w=hist_w, hist_sbgs=hist_sbgs, hist_abgs=hist_abgs,
             ncolours=np.asarray(ncol, dtype=np.int32),
             level_rows=np.asarray([A.shape[0] for A in As], dtype=np.int64),
             level_nnz=np.asarray([A.nnz for A in As], dtype=np.int64),
             p_nnz=np.asarray([P.nnz for P in Ps], dtype=np.int64),
             b_norm=np.linalg.norm(b), x_natural_norm=np.linalg.norm(x_nat),
             setup_s=meta.get("setup_s", 0.0), solve_s=meta.get("solve_s", 0.0),
+            l2_error=meta.get("l2_error", float("nan")),
         )
         if not histories_only:
-            out.update(b=b, x_natural=x_nat, x_colour=x_col, x_bj23=x_bj, x_cg=x_cg)
+            out.update(b=b, x_natural=x_nat, x_colour=x_col, x_bj23=x_bj, x_cg=x_cg, x_w=x_w, x_sbgs=x_sbgs,
+                       x_abgs=x_abgs)
             for l, A in enumerate(As):
                 A = O.as_csr(A)
                 out[f"A{l}_indptr"], out[f"A{l}_indices"], out[f"A{l}_data"] = A.indptr, A.indices, A.data

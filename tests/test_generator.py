@@ -72,3 +72,16 @@ def test_generated_16cube_reproduces_reference_history(name):
     ref = np.asarray(c["hist_colour"])
     assert rc == 0 and it == len(ref) - 1
     assert hist_close(hist, ref)
+
+
+def test_l2_error_post_processing_matches_reference(case, generated):
+    # Cell recovery + k+1 reconstruction + relative L2 error against the exact solution, applied to
+    # the reference's own solution: equal to the reference's L2Error up to the two quadratures
+    # (exact to rounding on triangles; degree-8 rule on tetrahedra, larger gap on the coarsest mesh).
+    from fhhos4_gb300 import hho
+    ref = float(case["l2_error"])
+    H = hho.Hierarchy(case.dim, case.n, case.k)
+    e = H.l2_error(case["x_natural"])
+    H.close()
+    tol = 1e-8 if case.dim == 2 else (1e-3 if case.n <= 4 else 1e-5)
+    assert abs(e - ref) <= tol * ref

@@ -93,6 +93,19 @@ def test_pcg_mg_matches_reference(case):
     assert np.linalg.norm(x[sp_] - case["x_cg"]) / np.linalg.norm(case["x_cg"]) < X_RTOL
 
 
+@pytest.mark.parametrize("variant,pre,post,cycle", [("w", "bgs", "rbgs", "W"), ("sbgs", "sbgs", "sbgs", "V"),
+                                                   ("abgs", "abgs", "rabgs", "V")])
+def test_cycles_and_smoothers_match_reference(case, variant, pre, post, cycle):
+    solver = S().fcg_mg(case.As, case.Ps, case.bs, pre=pre, post=post, cycle=cycle)
+    x = solver.Solve(case.b)
+    ref = case[f"hist_{variant}"]
+    assert solver.IterationCount == len(ref) - 1
+    assert hist_close(solver.History, ref)
+    sp_ = scalar_perm(case.perms[0], case.bs)
+    xr = case[f"x_{variant}"]
+    assert np.linalg.norm(x[sp_] - xr) / np.linalg.norm(xr) < X_RTOL
+
+
 def test_block_jacobi_smoother_matches_reference(case):
     solver = S().fcg_mg(case.As, case.Ps, case.bs, pre="bj23", post="bj23")
     solver.Solve(case.b)

@@ -29,7 +29,7 @@ def test_unsupported_configurations_fail_loudly():
     with pytest.raises(NotImplementedError):
         S.FlexibleConjugateGradient(truncation=2)
     mg = S.Multigrid()
-    mg.Cycle = "W"
+    mg.Cycle = "K"
     with pytest.raises(NotImplementedError):
         mg._check_supported()
     mg.Cycle = "V"
@@ -48,6 +48,6 @@ def test_hierarchy_shape_checks():
 
 
 def test_option_codes_match_header():
-    assert N.SMOOTHERS == {"bgs": 0, "rbgs": 1, "bj": 2, "bj23": 3}
+    assert N.SMOOTHERS == {"bgs": 0, "rbgs": 1, "bj": 2, "bj23": 3, "sbgs": 4, "abgs": 5, "rabgs": 6}
     assert N.KRYLOV == {"fcg": 0, "cg": 1}
     assert N.PRECISION == {"fp64": 0, "fp32": 1}

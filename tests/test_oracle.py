@@ -40,12 +40,19 @@ def test_natural_order_history_matches_reference(case):
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < X_RTOL
 
 
-@pytest.mark.parametrize("variant,smoothers,krylov", [("colour", ("bgs", "rbgs"), "fcg"),
-                                                      ("bj23", ("bj23", "bj23"), "fcg"),
-                                                      ("cg", ("bgs", "rbgs"), "cg")])
-def test_colour_order_histories_match_reference(case, variant, smoothers, krylov):
+VARIANTS = [("colour", ("bgs", "rbgs"), "fcg", "V"),
+            ("bj23", ("bj23", "bj23"), "fcg", "V"),
+            ("cg", ("bgs", "rbgs"), "cg", "V"),
+            ("w", ("bgs", "rbgs"), "fcg", "W"),
+            ("sbgs", ("sbgs", "sbgs"), "fcg", "V"),
+            ("abgs", ("abgs", "rabgs"), "fcg", "V")]
+
+
+@pytest.mark.parametrize("variant,smoothers,krylov,cycle", VARIANTS)
+def test_colour_order_histories_match_reference(case, variant, smoothers, krylov, cycle):
     Ac, Pc, bc = O.permute_hierarchy(case.As, case.Ps, case.b, case.bs, case.perms)
-    x, hist, it, rc = O.fcgmg_solve(Ac, Pc, bc, case.bs, pre=smoothers[0], post=smoothers[1], krylov=krylov)
+    x, hist, it, rc = O.fcgmg_solve(Ac, Pc, bc, case.bs, pre=smoothers[0], post=smoothers[1], krylov=krylov,
+                                    cycle=cycle)
     ref = case[f"hist_{variant}"]
     assert rc == 0
     if variant == "bj23":
