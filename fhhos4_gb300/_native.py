@@ -35,7 +35,7 @@ OP_COARSE_SOLVE, OP_VCYCLE = 8, 9
 # Every symbol include/fhg.h declares.
 EXPORTS = ["fhg_default_options", "fhg_create", "fhg_destroy", "fhg_last_error", "fhg_set_level",
            "fhg_set_prolongation", "fhg_setup", "fhg_solve", "fhg_solve_device", "fhg_apply",
-           "fhg_time_op", "fhg_set_vcycle_precision", "fhg_level_info", "fhg_get_permutation",
+           "fhg_time_op", "fhg_set_cycle", "fhg_set_vcycle_precision", "fhg_level_info", "fhg_get_permutation",
            "fhg_kernel_launches", "fhg_residual_norm_noalloc"]
 
 FHG_NOALLOC_MAX_PARTIALS = 131072
@@ -87,6 +87,7 @@ def load(path: str = LIB):
     lib.fhg_apply.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.fhg_time_op.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_double)]
     lib.fhg_set_vcycle_precision.argtypes = [C.c_void_p, C.c_int]
+    lib.fhg_set_cycle.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
     lib.fhg_level_info.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_longlong), P(C.c_int), P(C.c_int),
                                    P(C.c_longlong)]
     lib.fhg_get_permutation.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
@@ -170,6 +171,9 @@ class Context:
         ms = C.c_double()
         self._check(self.lib.fhg_time_op(self.h, level, op, PRECISION[precision], warmup, reps, C.byref(ms)))
         return ms.value
+
+    def set_cycle(self, pre: str = "bgs", post: str = "rbgs", npre: int = 1, npost: int = 1, w_loops: int = 1):
+        self._check(self.lib.fhg_set_cycle(self.h, SMOOTHERS[pre], SMOOTHERS[post], npre, npost, w_loops))
 
     def set_vcycle_precision(self, precision: str):
         self._check(self.lib.fhg_set_vcycle_precision(self.h, PRECISION[precision]))

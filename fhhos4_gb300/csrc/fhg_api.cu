@@ -1381,6 +1381,26 @@ int fhg_time_op(fhg_ctx* ctx, int level, int op, int precision, int warmup, int 
     return time_op_t<double>(ctx, level, op, warmup, reps, avg_ms);
 }
 
+int fhg_set_cycle(fhg_ctx* ctx, int pre_smoother, int post_smoother, int pre_iterations, int post_iterations,
+                  int w_loops)
+{
+    if (!ctx) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
+    if (pre_smoother < 0 || pre_smoother > 6 || post_smoother < 0 || post_smoother > 6)
+        return fail(ctx, FHG_ERR_INVALID_ARG, "unknown smoother code");
+    if (pre_iterations < 0 || post_iterations < 0 || w_loops < 1)
+        return fail(ctx, FHG_ERR_INVALID_ARG, "negative smoothing count or cycle loops < 1");
+    for (int g = 0; g < 2; g++)
+        if (ctx->graph[g]) { cudaGraphExecDestroy(ctx->graph[g]); ctx->graph[g] = nullptr; }
+    ctx->graphs_built = 0;
+    ctx->opts.pre_smoother = pre_smoother;
+    ctx->opts.post_smoother = post_smoother;
+    ctx->opts.pre_iterations = pre_iterations;
+    ctx->opts.post_iterations = post_iterations;
+    ctx->opts.w_loops = w_loops;
+    return FHG_OK;
+}
+
 int fhg_set_vcycle_precision(fhg_ctx* ctx, int precision)
 {
     if (!ctx) return FHG_ERR_INVALID_ARG;

@@ -138,6 +138,12 @@ int fhg_apply(fhg_ctx* ctx, int level, int op, const double* in, const double* a
  * its colour launches. */
 int fhg_time_op(fhg_ctx* ctx, int level, int op, int precision, int warmup, int reps, double* avg_ms);
 
+/* Change the cycle of a set-up context: smoothers (FHG_SMOOTHER_*), smoothing steps and WLoops,
+ * the Multigrid fields PreSmootherCode/PostSmootherCode/Pre-/PostSmoothingIterations/WLoops
+ * (src/Solver/Multigrid/Multigrid.h:19-26), without rebuilding the hierarchy. */
+int fhg_set_cycle(fhg_ctx* ctx, int pre_smoother, int post_smoother, int pre_iterations, int post_iterations,
+                  int w_loops);
+
 /* Switch the V-cycle precision of a set-up context (FP32 needs a setup with FHG_PREC_FP32,
  * which keeps both copies). The outer Krylov iteration stays FP64. */
 int fhg_set_vcycle_precision(fhg_ctx* ctx, int precision);
