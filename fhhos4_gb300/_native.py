@@ -30,13 +30,18 @@ PRECISION = {"fp64": 0, "fp32": 1}
 
 OP_SPMV, OP_RESIDUAL, OP_RESTRICT, OP_PROLONG_ADD = 0, 1, 2, 3
 OP_GS_FORWARD, OP_GS_BACKWARD, OP_JACOBI, OP_SYM_SPMV = 4, 5, 6, 7
-OP_COARSE_SOLVE, OP_VCYCLE = 8, 9
+OP_COARSE_SOLVE, OP_VCYCLE, OP_VCYCLE_LEARNED = 8, 9, 10
+LEARNED = {"off": 0, "fallback": 1, "always": 2}
+LEARNED_PARAMS = 24848
 
 # Every symbol include/fhg.h declares.
 EXPORTS = ["fhg_default_options", "fhg_create", "fhg_destroy", "fhg_last_error", "fhg_set_level",
            "fhg_set_prolongation", "fhg_setup", "fhg_solve", "fhg_solve_device", "fhg_apply",
            "fhg_time_op", "fhg_set_cycle", "fhg_set_vcycle_precision", "fhg_level_info", "fhg_get_permutation",
-           "fhg_kernel_launches", "fhg_residual_norm_noalloc"]
+           "fhg_kernel_launches", "fhg_residual_norm_noalloc", "fhg_set_face_tensors", "fhg_set_learned",
+           "fhg_learned_reference_rate", "fhg_learned_features", "fhg_apply_internal", "fhg_net_num_params",
+           "fhg_net_create", "fhg_net_destroy", "fhg_net_last_error", "fhg_net_set_params", "fhg_net_get_params",
+           "fhg_net_train_step"]
 
 FHG_NOALLOC_MAX_PARTIALS = 131072
 
@@ -52,12 +57,13 @@ class Options(C.Structure):
                 ("pre_iterations", C.c_int), ("post_iterations", C.c_int), ("omega", C.c_double),
                 ("tolerance", C.c_double), ("max_iterations", C.c_int), ("vcycle_precision", C.c_int),
                 ("colouring", C.c_int), ("use_graphs", C.c_int), ("autotune", C.c_int),
-                ("max_coarse_rows", C.c_int), ("outer_split", C.c_int), ("w_loops", C.c_int)]
+                ("max_coarse_rows", C.c_int), ("outer_split", C.c_int), ("w_loops", C.c_int),
+                ("galerkin", C.c_int)]
 
 
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", C.c_int), ("status", C.c_int), ("normalized_residual", C.c_double),
-                ("solve_ms", C.c_double)]
+                ("solve_ms", C.c_double), ("learned_iterations", C.c_int), ("true_relative_residual", C.c_double)]
 
 
 _lib = None
@@ -95,6 +101,21 @@ def load(path: str = LIB):
     lib.fhg_kernel_launches.restype = C.c_longlong
     lib.fhg_residual_norm_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                               C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.fhg_set_face_tensors.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    lib.fhg_set_learned.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+    lib.fhg_learned_reference_rate.argtypes = [C.c_void_p, P(C.c_double)]
+    lib.fhg_learned_features.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.fhg_apply_internal.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.fhg_net_num_params.argtypes = []
+    lib.fhg_net_create.argtypes = [P(C.c_void_p), C.c_int]
+    lib.fhg_net_destroy.argtypes = [C.c_void_p]
+    lib.fhg_net_destroy.restype = None
+    lib.fhg_net_last_error.argtypes = [C.c_void_p]
+    lib.fhg_net_last_error.restype = C.c_char_p
+    lib.fhg_net_set_params.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+    lib.fhg_net_get_params.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+    lib.fhg_net_train_step.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_float, C.c_float, C.c_int,
+                                       P(C.c_double), C.c_void_p]
     _lib = lib
     return lib
 
@@ -191,6 +212,79 @@ class Context:
 
     def kernel_launches(self) -> int:
         return int(self.lib.fhg_kernel_launches(self.h))
+
+    # -- learned correction ----------------------------------------------
+    def set_face_tensors(self, tensors: np.ndarray):
+        t = np.ascontiguousarray(tensors, dtype=np.float64)
+        if t.ndim != 2 or t.shape[1] != 12:
+            raise ValueError("face tensors are (n_blocks, 12)")
+        self._check(self.lib.fhg_set_face_tensors(self.h, t.shape[0], ptr(t)))
+
+    def set_learned(self, params: np.ndarray | None, mode: str = "fallback"):
+        if params is None:
+            self._check(self.lib.fhg_set_learned(self.h, None, 0, LEARNED[mode]))
+            return
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        self._check(self.lib.fhg_set_learned(self.h, ptr(p), p.size, LEARNED[mode]))
+
+    def learned_reference_rate(self) -> float:
+        r = C.c_double()
+        self._check(self.lib.fhg_learned_reference_rate(self.h, C.byref(r)))
+        return r.value
+
+    def learned_features(self, r_dev: int, features_dev: int, scale_dev: int):
+        self._check(self.lib.fhg_learned_features(self.h, C.c_void_p(r_dev), C.c_void_p(features_dev),
+                                                  C.c_void_p(scale_dev)))
+
+    def apply_internal(self, level: int, op: int, precision: str, in_dev: int, aux_dev: int | None, out_dev: int):
+        """One operator on device vectors in the context's colour numbering (see fhg_apply_internal)."""
+        self._check(self.lib.fhg_apply_internal(self.h, level, op, PRECISION[precision], C.c_void_p(in_dev),
+                                                C.c_void_p(aux_dev) if aux_dev else None, C.c_void_p(out_dev)))
+
+
+class Net:
+    """Owns one fhg_net: the network's FP32 parameters, Adam state and training buffers on a GPU."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        self.h = C.c_void_p()
+        rc = self.lib.fhg_net_create(C.byref(self.h), device)
+        self._check(rc)
+        self.n_params = int(self.lib.fhg_net_num_params())
+
+    def _check(self, rc: int):
+        if rc != FHG_OK:
+            msg = self.lib.fhg_net_last_error(self.h).decode() if self.h else "no network"
+            raise FhgError(rc, msg)
+
+    def close(self):
+        if self.h:
+            self.lib.fhg_net_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params: np.ndarray):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        self._check(self.lib.fhg_net_set_params(self.h, ptr(p), p.size))
+
+    def params(self) -> np.ndarray:
+        p = np.empty(self.n_params, dtype=np.float32)
+        self._check(self.lib.fhg_net_get_params(self.h, ptr(p), p.size))
+        return p
+
+    def train_step(self, ctx: Context, r_dev: int, energy: float, lr: float, weight_decay: float = 0.0,
+                   update: bool = True, want_grad: bool = False):
+        """One step on one field; returns (loss before the update, gradient or None)."""
+        loss = C.c_double()
+        g = np.empty(self.n_params, dtype=np.float32) if want_grad else None
+        self._check(self.lib.fhg_net_train_step(self.h, ctx.h, C.c_void_p(r_dev), float(energy), float(lr),
+                                                float(weight_decay), 1 if update else 0, C.byref(loss), ptr(g)))
+        return loss.value, g
 
 
 def default_options() -> Options:

@@ -19,6 +19,7 @@
 #include <numeric>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 using fhg::BsrView;
@@ -55,6 +56,7 @@ struct DevBsr {
 struct Level {
     int n = 0, nb = 0, bs = 0;
     HostCsr A_in, P_in;
+    bool A_is_galerkin = false;    // A_in was computed as R A P by a setup with galerkin = 1
     int ncolours = 0;
     int gs_lanes = 0;              // lanes per block row of the GS/Jacobi sweeps (0: those of A)
     int gs_unroll = 1;             // blocks per lane step of the GS sweeps
@@ -99,6 +101,39 @@ struct fhg_ctx {
     int graphs_built = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<void*> allocations;
+    // Learned correction of the FP32 V-cycle on the finest level (built at setup when the
+    // V-cycle is FP32 and bs <= 4; the network is installed with fhg_set_learned).
+    int* nbr_d = nullptr;              // nb0 x 6 neighbour blocks by decreasing |A_ij|_F, -1 padded
+    uint16_t* tfeat_d = nullptr;       // nb0 x 16 BF16 element-tensor features (colour numbering)
+    std::vector<double> tensors_host;  // nb0 x 12 element tensors, caller's numbering
+    float* lw = nullptr;               // D^-1 r scratch (n0)
+    float* lparams = nullptr;          // FP32 parameters of the installed network
+    uint16_t* lwts = nullptr;          // its BF16 weights
+    float* lbias = nullptr;            // its FP32 biases
+    int learned_mode = FHG_LEARNED_OFF;
+    bool learned_now = false;          // the cycle being launched or captured applies the step
+    double rho_plain = 0.0;            // calibrated per-iteration reduction of the plain method
+    cudaGraphExec_t graph_l[2] = {nullptr, nullptr};
+    long long graph_l_kernels[2] = {0, 0};
+    int graphs_l_built = 0;
+};
+
+// Training state of one network (fhg_net_*): FP32 master parameters, Adam moments and the
+// activations of one field.
+struct fhg_net {
+    int device = 0;
+    std::string err;
+    float *params = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
+    uint16_t* wts = nullptr;
+    float* bias = nullptr;
+    int step = 0;
+    long long rows_cap = 0;
+    uint16_t *feat = nullptr, *h1 = nullptr, *h2 = nullptr, *dy = nullptr, *d2 = nullptr, *d1 = nullptr;
+    float *a1 = nullptr, *a2 = nullptr, *y = nullptr, *dh = nullptr, *scale = nullptr, *c = nullptr, *q = nullptr;
+    float *gparts = nullptr, *cparts = nullptr;
+    double* lparts = nullptr;
+    double* lparts_host = nullptr;
+    std::vector<void*> fixed, scratch;
 };
 
 namespace {
@@ -288,6 +323,98 @@ void transpose_bsr(const HostBsr& B, HostBsr& T)
 
 // tril(A) + tril(A,-1)^T: the operator A.selfadjointView<Eigen::Lower>() applies
 // (src/Solver/Krylov/FlexibleConjugateGradient.h:124).
+// C = A B for block-sparse operators of one block size: row-parallel Gustavson (each thread owns
+// a contiguous slice of block rows and a dense block-column marker); every row is summed in the
+// same order whatever the thread count.
+void bsr_multiply(const HostBsr& A, const HostBsr& B, HostBsr& C)
+{
+    const int bs = A.bs, bb = bs * bs;
+    C.bs = bs;
+    C.nbr = A.nbr;
+    C.nbc = B.nbc;
+    C.rowptr.assign(C.nbr + 1, 0);
+    const int nt = std::max(1, std::min((int)std::thread::hardware_concurrency(), 64));
+    const int chunk = (C.nbr + nt - 1) / nt;
+    auto run = [&](auto body) {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nt; t++) {
+            const int r0 = t * chunk, r1 = std::min(C.nbr, r0 + chunk);
+            if (r0 < r1) th.emplace_back(body, r0, r1);
+        }
+        for (auto& x : th) x.join();
+    };
+    run([&](int r0, int r1) {
+        std::vector<int> mark(C.nbc, -1);
+        for (int I = r0; I < r1; I++) {
+            int cnt = 0;
+            for (int p = A.rowptr[I]; p < A.rowptr[I + 1]; p++) {
+                const int J = A.colidx[p];
+                for (int q = B.rowptr[J]; q < B.rowptr[J + 1]; q++)
+                    if (mark[B.colidx[q]] != I) { mark[B.colidx[q]] = I; cnt++; }
+            }
+            C.rowptr[I + 1] = cnt;
+        }
+    });
+    for (int I = 0; I < C.nbr; I++) C.rowptr[I + 1] += C.rowptr[I];
+    C.colidx.assign(C.rowptr[C.nbr], 0);
+    C.vals.assign((size_t)C.rowptr[C.nbr] * bb, 0.0);
+    run([&](int r0, int r1) {
+        std::vector<int> mark(C.nbc, -1), slot(C.nbc, 0);
+        std::vector<int> cols;
+        for (int I = r0; I < r1; I++) {
+            cols.clear();
+            for (int p = A.rowptr[I]; p < A.rowptr[I + 1]; p++) {
+                const int J = A.colidx[p];
+                for (int q = B.rowptr[J]; q < B.rowptr[J + 1]; q++)
+                    if (mark[B.colidx[q]] != I) { mark[B.colidx[q]] = I; cols.push_back(B.colidx[q]); }
+            }
+            std::sort(cols.begin(), cols.end());
+            const int base = C.rowptr[I];
+            for (size_t k = 0; k < cols.size(); k++) {
+                C.colidx[base + k] = cols[k];
+                slot[cols[k]] = base + (int)k;
+            }
+            for (int p = A.rowptr[I]; p < A.rowptr[I + 1]; p++) {
+                const double* a = &A.vals[(size_t)p * bb];
+                const int J = A.colidx[p];
+                for (int q = B.rowptr[J]; q < B.rowptr[J + 1]; q++) {
+                    const double* b = &B.vals[(size_t)q * bb];
+                    double* c = &C.vals[(size_t)slot[B.colidx[q]] * bb];
+                    for (int r = 0; r < bs; r++)
+                        for (int m = 0; m < bs; m++) {
+                            const double arm = a[r * bs + m];
+                            for (int k = 0; k < bs; k++) c[r * bs + k] += arm * b[m * bs + k];
+                        }
+                }
+            }
+        }
+    });
+}
+
+// Scalar CSR of a block operator: every entry of every stored block, columns ascending.
+void bsr_to_csr(const HostBsr& B, HostCsr& A)
+{
+    const int bs = B.bs, bb = bs * bs;
+    A.n_rows = B.nbr * bs;
+    A.n_cols = B.nbc * bs;
+    A.rowptr.assign(A.n_rows + 1, 0);
+    for (int I = 0; I < B.nbr; I++)
+        for (int r = 0; r < bs; r++)
+            A.rowptr[I * bs + r + 1] = A.rowptr[I * bs + r] + (B.rowptr[I + 1] - B.rowptr[I]) * bs;
+    A.colidx.resize(A.rowptr[A.n_rows]);
+    A.vals.resize(A.rowptr[A.n_rows]);
+    for (int I = 0; I < B.nbr; I++)
+        for (int r = 0; r < bs; r++) {
+            int o = A.rowptr[I * bs + r];
+            for (int p = B.rowptr[I]; p < B.rowptr[I + 1]; p++)
+                for (int c = 0; c < bs; c++) {
+                    A.colidx[o] = B.colidx[p] * bs + c;
+                    A.vals[o++] = B.vals[(size_t)p * bb + r * bs + c];
+                }
+        }
+    A.set = true;
+}
+
 void symmetrise_lower(const HostCsr& A, HostCsr& S)
 {
     const int n = A.n_rows;
@@ -499,6 +626,69 @@ int upload_bsr_split(fhg_ctx* ctx, const HostBsr& B, DevBsr<float>& D, float** l
 bool supported_bs(int bs) { return bs == 2 || bs == 3 || bs == 4 || bs == 6; }
 
 // ---------------------------------------------------------------------------
+// Learned-step setup (host)
+
+// For every block row of the (permuted) finest operator: its off-diagonal block columns by
+// decreasing |A_ij|_F^2 rounded to FP32 (so that couplings equal up to rounding order tie), ties
+// by smaller column, the first six, -1 padded.
+void learned_neighbours(const HostBsr& B, std::vector<int>& nbr)
+{
+    const int K = fhg::learned::kNeighbours;
+    const int bb = B.bs * B.bs;
+    nbr.assign((size_t)B.nbr * K, -1);
+    std::vector<std::pair<float, int>> row;
+    for (int i = 0; i < B.nbr; i++) {
+        row.clear();
+        for (int p = B.rowptr[i]; p < B.rowptr[i + 1]; p++) {
+            const int j = B.colidx[p];
+            if (j == i) continue;
+            double f = 0.0;
+            for (int e = 0; e < bb; e++) f += B.vals[(size_t)p * bb + e] * B.vals[(size_t)p * bb + e];
+            row.push_back({(float)f, j});
+        }
+        std::sort(row.begin(), row.end(), [](const std::pair<float, int>& a, const std::pair<float, int>& b) {
+            return a.first != b.first ? a.first > b.first : a.second < b.second;
+        });
+        for (int k = 0; k < K && k < (int)row.size(); k++) nbr[(size_t)i * K + k] = row[k].second;
+    }
+}
+
+// float -> bfloat16 bits, round to nearest even (finite inputs).
+uint16_t to_bf16(float f)
+{
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+// Element-tensor features of every face in colour numbering: both tensors divided by the larger
+// of their Frobenius norms; zeros when no tensors were given.
+int upload_tensor_features(fhg_ctx* ctx)
+{
+    Level& L = ctx->levels[0];
+    if (!ctx->tfeat_d) return FHG_OK;
+    const int S = fhg::learned::kTensorSlots;
+    std::vector<uint16_t> f((size_t)L.nb * S, 0);
+    if (ctx->tensors_host.size() == (size_t)L.nb * 12) {
+        for (int I = 0; I < L.nb; I++) {
+            const double* t = &ctx->tensors_host[(size_t)L.perm[I] * 12];
+            double nrm[2] = {0, 0};
+            for (int side = 0; side < 2; side++) {
+                const double* T = t + 6 * side;
+                nrm[side] = std::sqrt(T[0] * T[0] + T[1] * T[1] + T[2] * T[2] +
+                                      2 * (T[3] * T[3] + T[4] * T[4] + T[5] * T[5]));
+            }
+            const double tau = std::max(nrm[0], nrm[1]);
+            if (!(tau > 0) || !std::isfinite(tau)) continue;
+            for (int q = 0; q < 12; q++) f[(size_t)I * S + q] = to_bf16((float)(t[q] / tau));
+        }
+    }
+    CK(cudaMemcpy(ctx->tfeat_d, f.data(), f.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    return FHG_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Device operations
 
 template <class T> struct LevelVecs;
@@ -567,6 +757,18 @@ void smooth(fhg_ctx* ctx, int l, int code, int iters, const T* b, T* x, bool fro
 
 bool is_gs(int code) { return code != FHG_SMOOTHER_BJ && code != FHG_SMOOTHER_BJ23; }
 
+// Learned correction at the end of the finest level's post-smoothing: w = D^-1 (b - A x),
+// then x += s N(w-patch, tensors) face by face (fhg_learned.cu). r32 of level 0 is free here
+// (its last use is the restriction).
+void learned_step(fhg_ctx* ctx, const float* b, float* x)
+{
+    Level& L = ctx->levels[0];
+    cudaStream_t s = ctx->stream;
+    fhg::launch_spmv<float>(L.A32.v, fhg::kSpmvResidual, x, b, L.r32, s);
+    fhg::launch_block_diag(L.nb, L.bs, L.dinv32, L.nb, L.r32, ctx->lw, s);
+    fhg::launch_learned_apply(L.nb, L.bs, ctx->nbr_d, ctx->lw, ctx->tfeat_d, ctx->lwts, ctx->lbias, x, s);
+}
+
 // One multigrid cycle on level l (src/Solver/Multigrid/Multigrid.h:438-608): V for w_loops = 1,
 // W for 2 (the coarse correction repeated, except directly above the coarsest level). x is the
 // initial guess, zero when x_zero.
@@ -595,6 +797,9 @@ void mg_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
     }
     fhg::launch_spmv<T>(V::P(L), fhg::kSpmvAddTo, V::x(C), x, x, s);
     smooth<T>(ctx, l, ctx->opts.post_smoother, ctx->opts.post_iterations, b, x);
+    if constexpr (std::is_same<T, float>::value) {
+        if (l == 0 && ctx->learned_now) learned_step(ctx, b, x);
+    }
 }
 
 template <class T>
@@ -674,23 +879,36 @@ void cg_iteration(fhg_ctx* ctx)
     cudaMemcpyAsync(ctx->nr_host, ctx->scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s);
 }
 
-int build_graphs(fhg_ctx* ctx)
+// One captured Krylov iteration per ping-pong parity; `learned`: the V-cycle of the captured
+// iteration applies the learned correction (graph_l) or not (graph).
+int build_graphs(fhg_ctx* ctx, bool learned = false)
 {
     const int ngraphs = ctx->opts.krylov == FHG_KRYLOV_CG ? 1 : 2;
+    cudaGraphExec_t* exec = learned ? ctx->graph_l : ctx->graph;
+    long long* kernels = learned ? ctx->graph_l_kernels : ctx->graph_kernels;
+    ctx->learned_now = learned;
     for (int g = 0; g < ngraphs; g++) {
         cudaGraph_t graph = nullptr;
         const long long before = fhg::g_kernel_launches.load();
-        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        if (ctx->opts.krylov == FHG_KRYLOV_CG) cg_iteration(ctx);
-        else fcg_iteration(ctx, g);
-        CK(cudaStreamEndCapture(ctx->stream, &graph));
+        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            if (ctx->opts.krylov == FHG_KRYLOV_CG) cg_iteration(ctx);
+            else fcg_iteration(ctx, g);
+            e = cudaStreamEndCapture(ctx->stream, &graph);
+        }
         const long long after = fhg::g_kernel_launches.load();
         fhg::g_kernel_launches -= (after - before);  // captured, not executed
-        ctx->graph_kernels[g] = after - before;
-        CK(cudaGraphInstantiate(&ctx->graph[g], graph, 0));
-        CK(cudaGraphDestroy(graph));
+        kernels[g] = after - before;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec[g], graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            ctx->learned_now = false;
+            return fail(ctx, FHG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        }
     }
-    ctx->graphs_built = ngraphs;
+    ctx->learned_now = false;
+    if (learned) ctx->graphs_l_built = ngraphs;
+    else ctx->graphs_built = ngraphs;
     return FHG_OK;
 }
 
@@ -764,11 +982,24 @@ int tune_level(fhg_ctx* ctx, int l)
     return FHG_OK;
 }
 
+void free_graphs(fhg_ctx* ctx)
+{
+    for (int g = 0; g < 2; g++) {
+        if (ctx->graph[g]) { cudaGraphExecDestroy(ctx->graph[g]); ctx->graph[g] = nullptr; }
+        if (ctx->graph_l[g]) { cudaGraphExecDestroy(ctx->graph_l[g]); ctx->graph_l[g] = nullptr; }
+    }
+    ctx->graphs_built = 0;
+    ctx->graphs_l_built = 0;
+}
+
 void free_all(fhg_ctx* ctx)
 {
-    for (int g = 0; g < 2; g++)
-        if (ctx->graph[g]) { cudaGraphExecDestroy(ctx->graph[g]); ctx->graph[g] = nullptr; }
-    ctx->graphs_built = 0;
+    free_graphs(ctx);
+    ctx->nbr_d = nullptr; ctx->tfeat_d = nullptr; ctx->lw = nullptr;
+    ctx->lparams = nullptr; ctx->lwts = nullptr; ctx->lbias = nullptr;
+    ctx->learned_mode = FHG_LEARNED_OFF;
+    ctx->learned_now = false;
+    ctx->rho_plain = 0.0;
     for (void* p : ctx->allocations) cudaFree(p);
     ctx->allocations.clear();
     if (ctx->nr_host) { cudaFreeHost(ctx->nr_host); ctx->nr_host = nullptr; }
@@ -802,32 +1033,63 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
         fhg::launch_dot(n, ctx->kr, ctx->kz[0], part(ctx, 0), s);
         fhg::launch_sum(part(ctx, 0), ctx->scal + 3, s);
     }
+    // The learned correction runs inside FP32 V-cycles of FCG (the flexible method absorbs the
+    // variable preconditioner).
+    bool learned = ctx->learned_mode != FHG_LEARNED_OFF && ctx->lwts && ctx->opts.krylov == FHG_KRYLOV_FCG &&
+                   ctx->opts.vcycle_precision == FHG_PREC_FP32;
     if (ctx->opts.use_graphs && !ctx->graphs_built) {
-        int rc = build_graphs(ctx);
+        int rc = build_graphs(ctx, false);
+        if (rc) return rc;
+    }
+    if (learned && ctx->opts.use_graphs && !ctx->graphs_l_built) {
+        int rc = build_graphs(ctx, true);
         if (rc) return rc;
     }
     std::vector<double> hist(maxit + 1, 0.0);
     hist[0] = 1.0;
     double nr = 1.0;
-    int it = 0;
+    int it = 0, learned_its = 0;
     int status = FHG_OK;
     while (!(it > 0 && (it >= maxit || nr < ctx->opts.tolerance))) {
         const int p = it & 1;
         if (ctx->opts.use_graphs) {
             const int g = ctx->opts.krylov == FHG_KRYLOV_CG ? 0 : p;
-            CK(cudaGraphLaunch(ctx->graph[g], s));
-            fhg::g_kernel_launches += ctx->graph_kernels[g];
+            CK(cudaGraphLaunch(learned ? ctx->graph_l[g] : ctx->graph[g], s));
+            fhg::g_kernel_launches += learned ? ctx->graph_l_kernels[g] : ctx->graph_kernels[g];
         } else if (ctx->opts.krylov == FHG_KRYLOV_CG) {
             cg_iteration(ctx);
         } else {
+            ctx->learned_now = learned;
             fcg_iteration(ctx, p);
+            ctx->learned_now = false;
         }
         CK(cudaStreamSynchronize(s));
         nr = *ctx->nr_host;
         it++;
         hist[it] = nr;
+        if (learned) learned_its++;
         if (std::isinf(nr)) { status = fail(ctx, FHG_ERR_DIVERGED, "divergence of the solver"); break; }
         if (std::isnan(nr)) { status = fail(ctx, FHG_ERR_NAN, "the residual is NaN."); break; }
+        // Fallback rule: from the third iteration on, when the mean reduction of the last two
+        // iterations falls behind the plain method's calibrated per-iteration reduction by more
+        // than half of it in logarithmic terms (rho > rho_plain^(1/2): the margin absorbs how much
+        // the early iterations of one right-hand side differ from the calibration's), the
+        // remaining iterations use the plain V-cycle.
+        if (learned && ctx->learned_mode == FHG_LEARNED_FALLBACK && it >= 3 && ctx->rho_plain > 0.0) {
+            const double rho = std::sqrt(hist[it] / hist[it - 2]);
+            if (!(rho <= std::sqrt(ctx->rho_plain))) learned = false;
+        }
+    }
+    // The FP64 true residual ||b - A x|| / ||b|| judges the solve (A the full level-0 operator).
+    double true_rel = -1.0;
+    if (status == FHG_OK) {
+        fhg::launch_spmv<double>(L0.A.v, fhg::kSpmvResidual, ctx->kx, ctx->kb, ctx->kz[0], s);
+        fhg::launch_dot(n, ctx->kz[0], ctx->kz[0], part(ctx, 0), s);
+        fhg::launch_sqrt_sum(part(ctx, 0), ctx->scal + 5, s);
+        double h[6];
+        CK(cudaMemcpyAsync(h, ctx->scal, sizeof(h), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        true_rel = h[0] > 0 ? h[5] / h[0] : h[5];
     }
     if (history)
         for (int k = 0; k <= maxit; k++) history[k] = k <= it ? hist[k] : 0.0;
@@ -835,8 +1097,44 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
         info->iterations = it;
         info->status = status;
         info->normalized_residual = nr;
+        info->learned_iterations = learned_its;
+        info->true_relative_residual = true_rel;
     }
     return status;
+}
+
+// Per-iteration reduction of the plain method (FCG with the plain V-cycle of the current
+// options) on a seeded random right-hand side: the geometric mean over iterations 3..12.
+int calibrate_plain(fhg_ctx* ctx)
+{
+    Level& L0 = ctx->levels[0];
+    std::vector<double> b(L0.n);
+    uint64_t st = 0x5DEECE66DULL;
+    for (auto& v : b) {
+        st += 0x9E3779B97F4A7C15ull;
+        uint64_t z = st;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        v = (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+    }
+    CK(cudaMemcpyAsync(ctx->kb, b.data(), sizeof(double) * L0.n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const fhg_options saved = ctx->opts;
+    const int mode = ctx->learned_mode;
+    const int K = std::min(12, std::max(4, saved.max_iterations));
+    ctx->opts.tolerance = 0.0;
+    ctx->opts.max_iterations = K;
+    ctx->learned_mode = FHG_LEARNED_OFF;
+    std::vector<double> hist(K + 1);
+    fhg_solve_info info{};
+    int rc = run_solve(ctx, hist.data(), &info);
+    ctx->opts = saved;
+    ctx->learned_mode = mode;
+    if (rc) return rc;
+    const int k1 = std::min(info.iterations, K);
+    ctx->rho_plain = k1 >= 4 && hist[2] > 0 ? std::pow(hist[k1] / hist[2], 1.0 / (k1 - 2)) : 0.0;
+    return FHG_OK;
 }
 
 }  // namespace
@@ -864,6 +1162,7 @@ void fhg_default_options(fhg_options* o)
     o->max_coarse_rows = 8192;
     o->outer_split = 1;
     o->w_loops = 1;
+    o->galerkin = 0;
 }
 
 int fhg_create(fhg_ctx** out, int device)
@@ -921,6 +1220,7 @@ int fhg_set_level(fhg_ctx* ctx, int level, int block_size, int n, const int* row
     L.A_in.colidx.assign(colidx, colidx + rowptr[n]);
     L.A_in.vals.assign(vals, vals + rowptr[n]);
     L.A_in.set = true;
+    L.A_is_galerkin = false;
     ctx->ready = false;
     return FHG_OK;
 }
@@ -958,10 +1258,40 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
     if (o.pre_smoother < 0 || o.pre_smoother > 6 || o.post_smoother < 0 || o.post_smoother > 6)
         return fail(ctx, FHG_ERR_INVALID_ARG, "unknown smoother code");
     if (o.w_loops < 1) o.w_loops = 1;
+    if (o.galerkin && nlevels > 0 && nlevels <= 64 && (int)ctx->levels.size() < nlevels) ctx->levels.resize(nlevels);
     if (nlevels <= 0 || nlevels > (int)ctx->levels.size())
         return fail(ctx, FHG_ERR_INVALID_ARG, "nlevels=%d but %zu levels were given", nlevels, ctx->levels.size());
     ctx->nlevels = nlevels;
     const int bs = ctx->levels[0].bs;
+    if (o.galerkin) {
+        // Galerkin coarse operators A_{l+1} = R_l A_l P_l, R_l = P_l^T (Level::ComputeGalerkinOperator,
+        // src/Solver/Multigrid/Level.h:133-137; "-g 1"), replacing any operator given for l >= 1.
+        if (!ctx->levels[0].A_in.set) return fail(ctx, FHG_ERR_INVALID_ARG, "level 0 operator not set");
+        for (int l = 0; l + 1 < nlevels; l++) {
+            Level& L = ctx->levels[l];
+            Level& C = ctx->levels[l + 1];
+            if (!L.P_in.set) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d prolongation not set", l);
+            if (L.P_in.n_rows != L.n || L.P_in.n_cols % bs)
+                return fail(ctx, FHG_ERR_INVALID_ARG, "level %d prolongation is %dx%d for %d rows", l, L.P_in.n_rows,
+                            L.P_in.n_cols, L.n);
+            HostBsr Ab, Pb, Rb, APb, Cb;
+            csr_to_bsr(L.A_in, bs, Ab);
+            csr_to_bsr(L.P_in, bs, Pb);
+            transpose_bsr(Pb, Rb);
+            bsr_multiply(Ab, Pb, APb);
+            Ab = HostBsr();
+            bsr_multiply(Rb, APb, Cb);
+            bsr_to_csr(Cb, C.A_in);
+            C.n = L.P_in.n_cols;
+            C.bs = bs;
+            C.nb = C.n / bs;
+            C.A_is_galerkin = true;
+        }
+    } else {
+        for (int l = 1; l < nlevels; l++)
+            if (ctx->levels[l].A_is_galerkin)
+                return fail(ctx, FHG_ERR_INVALID_ARG, "level %d holds a Galerkin operator from an earlier setup: set it again", l);
+    }
     for (int l = 0; l < nlevels; l++) {
         Level& L = ctx->levels[l];
         if (!L.A_in.set) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d operator not set", l);
@@ -1052,6 +1382,15 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
                 if ((rc = upload_bsr<float>(ctx, Pp, L.P32, &L.P))) return rc;
                 if ((rc = upload_bsr<float>(ctx, Rp, L.R32, &L.R))) return rc;
             }
+        }
+        if (l == 0 && fp32 && nlevels > 1 && fhg::learned_supports(bs)) {
+            // Learned-step inputs: neighbour table, scratch and element-tensor features.
+            std::vector<int> nbr;
+            learned_neighbours(Ap, nbr);
+            if ((rc = upload(ctx, &ctx->nbr_d, nbr.data(), nbr.size()))) return rc;
+            if ((rc = dalloc(ctx, &ctx->lw, L.n))) return rc;
+            if ((rc = dalloc(ctx, &ctx->tfeat_d, (size_t)L.nb * fhg::learned::kTensorSlots))) return rc;
+            if ((rc = upload_tensor_features(ctx))) return rc;
         }
         if (l == 0) {
             HostCsr S;
@@ -1144,6 +1483,11 @@ int fhg_solve_device(fhg_ctx* ctx, const double* b_dev, double* x_dev, double* h
     if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
     CK(cudaSetDevice(ctx->device));
     Level& L0 = ctx->levels[0];
+    if (ctx->learned_mode == FHG_LEARNED_FALLBACK && ctx->rho_plain == 0.0 &&
+        ctx->opts.vcycle_precision == FHG_PREC_FP32 && ctx->opts.krylov == FHG_KRYLOV_FCG) {
+        int rc0 = calibrate_plain(ctx);
+        if (rc0) return rc0;
+    }
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     // b' = Pi_0 b
     fhg::launch_permute<double>(L0.nb, L0.bs, L0.perm_d, b_dev, ctx->kb, true, ctx->stream);
@@ -1390,9 +1734,8 @@ int fhg_set_cycle(fhg_ctx* ctx, int pre_smoother, int post_smoother, int pre_ite
         return fail(ctx, FHG_ERR_INVALID_ARG, "unknown smoother code");
     if (pre_iterations < 0 || post_iterations < 0 || w_loops < 1)
         return fail(ctx, FHG_ERR_INVALID_ARG, "negative smoothing count or cycle loops < 1");
-    for (int g = 0; g < 2; g++)
-        if (ctx->graph[g]) { cudaGraphExecDestroy(ctx->graph[g]); ctx->graph[g] = nullptr; }
-    ctx->graphs_built = 0;
+    free_graphs(ctx);
+    ctx->rho_plain = 0.0;  // the plain method's reduction is measured again for the new cycle
     ctx->opts.pre_smoother = pre_smoother;
     ctx->opts.post_smoother = post_smoother;
     ctx->opts.pre_iterations = pre_iterations;
@@ -1409,9 +1752,8 @@ int fhg_set_vcycle_precision(fhg_ctx* ctx, int precision)
     if (precision == FHG_PREC_FP32 && !ctx->levels[0].A32.vals)
         return fail(ctx, FHG_ERR_NOT_READY, "FP32 operators were not built: set up with FHG_PREC_FP32");
     if (ctx->opts.vcycle_precision != precision) {
-        for (int g = 0; g < 2; g++)
-            if (ctx->graph[g]) { cudaGraphExecDestroy(ctx->graph[g]); ctx->graph[g] = nullptr; }
-        ctx->graphs_built = 0;
+        free_graphs(ctx);
+        ctx->rho_plain = 0.0;
         ctx->opts.vcycle_precision = precision;
     }
     return FHG_OK;
@@ -1442,6 +1784,312 @@ long long fhg_kernel_launches(const fhg_ctx* ctx)
 {
     (void)ctx;
     return fhg::g_kernel_launches.load();
+}
+
+// ---------------------------------------------------------------------------
+// Learned correction step and its training (no counterpart in the reference)
+
+int fhg_set_face_tensors(fhg_ctx* ctx, int n_blocks, const double* tensors)
+{
+    if (!ctx) return FHG_ERR_INVALID_ARG;
+    if (ctx->levels.empty() || !ctx->levels[0].A_in.set)
+        return fail(ctx, FHG_ERR_NOT_READY, "the finest operator must be set before its face tensors");
+    if (n_blocks != ctx->levels[0].nb || !tensors)
+        return fail(ctx, FHG_ERR_INVALID_ARG, "%d face blocks given, level 0 has %d", n_blocks, ctx->levels[0].nb);
+    ctx->tensors_host.assign(tensors, tensors + (size_t)n_blocks * 12);
+    if (!ctx->ready) return FHG_OK;
+    CK(cudaSetDevice(ctx->device));
+    return upload_tensor_features(ctx);
+}
+
+int fhg_set_learned(fhg_ctx* ctx, const float* params, int n_params, int mode)
+{
+    using namespace fhg::learned;
+    if (!ctx) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
+    if (mode < FHG_LEARNED_OFF || mode > FHG_LEARNED_ALWAYS) return fail(ctx, FHG_ERR_INVALID_ARG, "unknown mode %d", mode);
+    CK(cudaSetDevice(ctx->device));
+    if ((params || mode != FHG_LEARNED_OFF) && !ctx->nbr_d)
+        return fail(ctx, FHG_ERR_UNSUPPORTED,
+                    "the learned step needs a setup with the FP32 V-cycle, two levels or more and block size 2..4");
+    Level& L0 = ctx->levels[0];
+    cudaStream_t s = ctx->stream;
+    int rc;
+    if (params) {
+        if (n_params != kParams) return fail(ctx, FHG_ERR_INVALID_ARG, "%d parameters given, the network has %d", n_params, kParams);
+        for (int i = 0; i < kParams; i++)
+            if (!std::isfinite(params[i])) return fail(ctx, FHG_ERR_INVALID_ARG, "parameter %d is not finite", i);
+        if (!ctx->lparams) {
+            if ((rc = dalloc(ctx, &ctx->lparams, kParams)) || (rc = dalloc(ctx, &ctx->lwts, kWeights)) ||
+                (rc = dalloc(ctx, &ctx->lbias, kBiases)))
+                return rc;
+        }
+        CK(cudaMemcpyAsync(ctx->lparams, params, sizeof(float) * kParams, cudaMemcpyHostToDevice, s));
+        fhg::launch_split_params(ctx->lparams, ctx->lwts, ctx->lbias, s);
+        // First launch outside any capture: fixes the kernel's shared-memory limit and grid. With
+        // w = 0 every scale is 0 and nothing is added to x.
+        CK(cudaMemsetAsync(ctx->lw, 0, sizeof(float) * L0.n, s));
+        if (fhg::launch_learned_apply(L0.nb, L0.bs, ctx->nbr_d, ctx->lw, ctx->tfeat_d, ctx->lwts, ctx->lbias, L0.x32, s))
+            return fail(ctx, FHG_ERR_CUDA, "the learned-step kernel cannot run on this device");
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(s));
+        for (int g = 0; g < 2; g++)
+            if (ctx->graph_l[g]) { cudaGraphExecDestroy(ctx->graph_l[g]); ctx->graph_l[g] = nullptr; }
+        ctx->graphs_l_built = 0;
+    } else if (mode != FHG_LEARNED_OFF && !ctx->lwts) {
+        return fail(ctx, FHG_ERR_NOT_READY, "no network installed");
+    }
+    ctx->learned_mode = mode;
+    ctx->rho_plain = 0.0;
+    return FHG_OK;
+}
+
+int fhg_learned_reference_rate(fhg_ctx* ctx, double* rho)
+{
+    if (!ctx || !rho) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
+    CK(cudaSetDevice(ctx->device));
+    if (ctx->rho_plain == 0.0) {
+        int rc = calibrate_plain(ctx);
+        if (rc) return rc;
+    }
+    *rho = ctx->rho_plain;
+    return FHG_OK;
+}
+
+int fhg_learned_features(fhg_ctx* ctx, const float* r, void* features, float* scale)
+{
+    if (!ctx || !r || !features || !scale) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready || !ctx->nbr_d) return fail(ctx, FHG_ERR_NOT_READY, "no learned-step data (FP32 setup, bs 2..4)");
+    CK(cudaSetDevice(ctx->device));
+    Level& L = ctx->levels[0];
+    fhg::launch_block_diag(L.nb, L.bs, L.dinv32, L.nb, r, ctx->lw, ctx->stream);
+    fhg::launch_features(L.nb, L.nb, L.bs, ctx->nbr_d, ctx->lw, ctx->tfeat_d, features, scale, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+    return FHG_OK;
+}
+
+int fhg_apply_internal(fhg_ctx* ctx, int level, int op, int precision, const void* in, const void* aux, void* out)
+{
+    if (!ctx) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
+    if (level < 0 || level >= ctx->nlevels) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d out of range", level);
+    if (!in || !out) return fail(ctx, FHG_ERR_INVALID_ARG, "null vector");
+    CK(cudaSetDevice(ctx->device));
+    int rc = FHG_OK;
+    if (precision == FHG_PREC_FP64) {
+        if (op == FHG_OP_VCYCLE_LEARNED) return fail(ctx, FHG_ERR_INVALID_ARG, "the learned step runs in the FP32 V-cycle");
+        if (op == FHG_OP_VCYCLE && ctx->opts.vcycle_precision != FHG_PREC_FP64)
+            return fail(ctx, FHG_ERR_INVALID_ARG, "FP64 V-cycle requested while the context runs FP32");
+        rc = apply_device(ctx, level, op, (double*)in, (double*)aux, (double*)out);
+    } else if (precision == FHG_PREC_FP32) {
+        if (!ctx->levels[0].A32.vals) return fail(ctx, FHG_ERR_NOT_READY, "FP32 operators were not built at setup");
+        if (op == FHG_OP_VCYCLE || op == FHG_OP_VCYCLE_LEARNED) {
+            if (level != 0) return fail(ctx, FHG_ERR_INVALID_ARG, "V-cycle starts on level 0");
+            if (op == FHG_OP_VCYCLE_LEARNED && !ctx->lwts) return fail(ctx, FHG_ERR_NOT_READY, "no network installed");
+            ctx->learned_now = op == FHG_OP_VCYCLE_LEARNED;
+            vcycle<float>(ctx, 0, (const float*)in, (float*)out);
+            ctx->learned_now = false;
+        } else if (op == FHG_OP_SYM_SPMV) {
+            return fail(ctx, FHG_ERR_INVALID_ARG, "the outer operator is FP64");
+        } else {
+            rc = apply_device_t<float>(ctx, level, op, (float*)in, (float*)aux, (float*)out);
+        }
+    } else {
+        return fail(ctx, FHG_ERR_INVALID_ARG, "unknown precision %d", precision);
+    }
+    if (rc) return rc;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+    return FHG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+int net_fail(fhg_net* net, int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (net) net->err = buf;
+    return code;
+}
+
+#define NCK(call)                                                                                  \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return net_fail(net, FHG_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));    \
+    } while (0)
+
+template <class T>
+int net_alloc(fhg_net* net, T** p, size_t count, bool scratch)
+{
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+    if (e != cudaSuccess)
+        return net_fail(net, FHG_ERR_CUDA, "cudaMalloc(%zu bytes) failed: %s", count * sizeof(T), cudaGetErrorString(e));
+    (scratch ? net->scratch : net->fixed).push_back(q);
+    *p = (T*)q;
+    return FHG_OK;
+}
+
+// Activation buffers for `rows` (a multiple of 64) faces.
+int net_reserve(fhg_net* net, long long rows)
+{
+    using namespace fhg::learned;
+    if (rows <= net->rows_cap) return FHG_OK;
+    for (void* p : net->scratch) cudaFree(p);
+    net->scratch.clear();
+    net->rows_cap = 0;
+    const size_t R = (size_t)rows;
+    int rc;
+    if ((rc = net_alloc(net, &net->feat, R * kIn, true)) || (rc = net_alloc(net, &net->h1, R * kHid, true)) ||
+        (rc = net_alloc(net, &net->h2, R * kHid, true)) || (rc = net_alloc(net, &net->dy, R * kOut, true)) ||
+        (rc = net_alloc(net, &net->d2, R * kHid, true)) || (rc = net_alloc(net, &net->d1, R * kHid, true)) ||
+        (rc = net_alloc(net, &net->a1, R * kHid, true)) || (rc = net_alloc(net, &net->a2, R * kHid, true)) ||
+        (rc = net_alloc(net, &net->y, R * kOut, true)) || (rc = net_alloc(net, &net->dh, R * kHid, true)) ||
+        (rc = net_alloc(net, &net->scale, R, true)) || (rc = net_alloc(net, &net->c, R * kMaxLearnedBs, true)) ||
+        (rc = net_alloc(net, &net->q, R * kMaxLearnedBs, true)))
+        return rc;
+    net->rows_cap = rows;
+    return FHG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fhg_net_num_params(void) { return fhg::learned::kParams; }
+
+int fhg_net_create(fhg_net** out, int device)
+{
+    using namespace fhg::learned;
+    if (!out) return FHG_ERR_INVALID_ARG;
+    fhg_net* net = new fhg_net();
+    *out = net;
+    net->device = device;
+    NCK(cudaSetDevice(device));
+    int rc;
+    if ((rc = net_alloc(net, &net->params, kParams, false)) || (rc = net_alloc(net, &net->grad, kParams, false)) ||
+        (rc = net_alloc(net, &net->m, kParams, false)) || (rc = net_alloc(net, &net->v, kParams, false)) ||
+        (rc = net_alloc(net, &net->wts, kWeights, false)) || (rc = net_alloc(net, &net->bias, kBiases, false)) ||
+        (rc = net_alloc(net, &net->gparts, (size_t)64 * kHid * kHid, false)) ||
+        (rc = net_alloc(net, &net->cparts, (size_t)kColsumChunks * kHid, false)) ||
+        (rc = net_alloc(net, &net->lparts, (size_t)fhg::kReduceCtas, false)))
+        return rc;
+    NCK(cudaMallocHost(&net->lparts_host, sizeof(double) * fhg::kReduceCtas));
+    NCK(cudaMemset(net->params, 0, sizeof(float) * kParams));
+    NCK(cudaMemset(net->m, 0, sizeof(float) * kParams));
+    NCK(cudaMemset(net->v, 0, sizeof(float) * kParams));
+    fhg::launch_split_params(net->params, net->wts, net->bias, 0);
+    NCK(cudaDeviceSynchronize());
+    return FHG_OK;
+}
+
+void fhg_net_destroy(fhg_net* net)
+{
+    if (!net) return;
+    cudaSetDevice(net->device);
+    for (void* p : net->scratch) cudaFree(p);
+    for (void* p : net->fixed) cudaFree(p);
+    if (net->lparts_host) cudaFreeHost(net->lparts_host);
+    delete net;
+}
+
+const char* fhg_net_last_error(const fhg_net* net) { return net ? net->err.c_str() : "null network"; }
+
+int fhg_net_set_params(fhg_net* net, const float* params, int n_params)
+{
+    using namespace fhg::learned;
+    if (!net || !params) return FHG_ERR_INVALID_ARG;
+    if (n_params != kParams) return net_fail(net, FHG_ERR_INVALID_ARG, "%d parameters given, the network has %d", n_params, kParams);
+    NCK(cudaSetDevice(net->device));
+    NCK(cudaMemcpy(net->params, params, sizeof(float) * kParams, cudaMemcpyHostToDevice));
+    NCK(cudaMemset(net->m, 0, sizeof(float) * kParams));
+    NCK(cudaMemset(net->v, 0, sizeof(float) * kParams));
+    net->step = 0;
+    fhg::launch_split_params(net->params, net->wts, net->bias, 0);
+    NCK(cudaDeviceSynchronize());
+    return FHG_OK;
+}
+
+int fhg_net_get_params(const fhg_net* net, float* params, int n_params)
+{
+    using namespace fhg::learned;
+    if (!net || !params || n_params != kParams) return FHG_ERR_INVALID_ARG;
+    if (cudaSetDevice(net->device) != cudaSuccess) return FHG_ERR_CUDA;
+    if (cudaMemcpy(params, net->params, sizeof(float) * kParams, cudaMemcpyDeviceToHost) != cudaSuccess) return FHG_ERR_CUDA;
+    return FHG_OK;
+}
+
+int fhg_net_train_step(fhg_net* net, fhg_ctx* ctx, const float* r, double energy, float lr, float weight_decay,
+                       int update, double* loss, float* grad)
+{
+    using namespace fhg::learned;
+    if (!net || !ctx || !r) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready || !ctx->nbr_d)
+        return net_fail(net, FHG_ERR_NOT_READY, "the context has no learned-step data (FP32 setup, bs 2..4)");
+    if (net->device != ctx->device) return net_fail(net, FHG_ERR_INVALID_ARG, "network and context on different devices");
+    if (!(energy > 0) || !std::isfinite(energy)) return net_fail(net, FHG_ERR_INVALID_ARG, "the energy e.Ae must be positive");
+    NCK(cudaSetDevice(ctx->device));
+    Level& L = ctx->levels[0];
+    const int nb = L.nb, bs = L.bs;
+    const long long R = ((long long)nb + 63) / 64 * 64;
+    int rc = net_reserve(net, R);
+    if (rc) return rc;
+    cudaStream_t s = ctx->stream;
+    const uint16_t* W1 = net->wts;
+    const uint16_t* W2 = W1 + kHid * kIn;
+    const uint16_t* W3 = W2 + kHid * kHid;
+    const float* b1 = net->bias;
+    const float* b2 = b1 + kHid;
+    const float* b3 = b2 + kHid;
+    const int M = (int)R;
+    // Forward over every face of the field, the correction, and q = A c.
+    fhg::launch_block_diag(nb, bs, L.dinv32, nb, r, ctx->lw, s);
+    fhg::launch_features(nb, M, bs, ctx->nbr_d, ctx->lw, ctx->tfeat_d, net->feat, net->scale, s);
+    fhg::launch_gemm(kGemmFwdHid, M, kIn, net->feat, kIn, W1, kIn, net->a1, nullptr, 1, 0, s);
+    fhg::launch_bias_gelu(R, net->a1, b1, net->h1, s);
+    fhg::launch_gemm(kGemmFwdHid, M, kHid, net->h1, kHid, W2, kHid, net->a2, nullptr, 1, 0, s);
+    fhg::launch_bias_gelu(R, net->a2, b2, net->h2, s);
+    fhg::launch_gemm(kGemmFwdOut, M, kHid, net->h2, kHid, W3, kHid, net->y, nullptr, 1, 0, s);
+    fhg::launch_correction(nb, bs, net->y, b3, net->scale, net->c, s);
+    fhg::launch_spmv<float>(L.A32.v, fhg::kSpmvAssign, net->c, nullptr, net->q, s);
+    fhg::launch_energy_grad(nb, M, bs, r, net->q, net->c, net->scale, 1.0 / energy, net->dy, net->lparts, s);
+    // Backward (weight gradients reduced over the faces in fixed-order K splits).
+    float* g = net->grad;
+    const int ns = (int)std::max(1LL, std::min(64LL, R / 512));
+    fhg::launch_colsum(R, kOut, net->dy, net->cparts, g + kOffB3, s);
+    fhg::launch_gemm(kGemmGradHid, kOut, M, net->dy, kOut, net->h2, kHid, g + kOffW3, net->gparts, ns, 0, s);
+    fhg::launch_gemm(kGemmBwdData, M, kOut, net->dy, kOut, W3, kHid, net->dh, nullptr, 1, 0, s);
+    fhg::launch_gelu_back(R * kHid, net->dh, net->a2, net->d2, s);
+    fhg::launch_colsum(R, kHid, net->d2, net->cparts, g + kOffB2, s);
+    fhg::launch_gemm(kGemmGradHid, kHid, M, net->d2, kHid, net->h1, kHid, g + kOffW2, net->gparts, ns, 0, s);
+    fhg::launch_gemm(kGemmBwdData, M, kHid, net->d2, kHid, W2, kHid, net->dh, nullptr, 1, 0, s);
+    fhg::launch_gelu_back(R * kHid, net->dh, net->a1, net->d1, s);
+    fhg::launch_colsum(R, kHid, net->d1, net->cparts, g + kOffB1, s);
+    fhg::launch_gemm(kGemmGradIn, kHid, M, net->d1, kHid, net->feat, kIn, g + kOffW1, net->gparts, ns, 0, s);
+    NCK(cudaMemcpyAsync(net->lparts_host, net->lparts, sizeof(double) * fhg::kReduceCtas, cudaMemcpyDeviceToHost, s));
+    if (grad) NCK(cudaMemcpyAsync(grad, g, sizeof(float) * kParams, cudaMemcpyDeviceToHost, s));
+    if (update) {
+        net->step++;
+        fhg::launch_adam(kParams, net->params, g, net->m, net->v, lr, 0.9f, 0.999f, 1e-8f, net->step, weight_decay, s);
+        fhg::launch_split_params(net->params, net->wts, net->bias, s);
+    }
+    NCK(cudaGetLastError());
+    NCK(cudaStreamSynchronize(s));
+    if (loss) {
+        double t = 0.0;
+        for (int i = 0; i < fhg::kReduceCtas; i++) t += net->lparts_host[i];
+        *loss = 1.0 + t / energy;
+    }
+    return FHG_OK;
 }
 
 }  // extern "C"

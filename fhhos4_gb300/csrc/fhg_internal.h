@@ -96,4 +96,52 @@ void launch_convert(long long n, const Tin* in, Tout* out, cudaStream_t s);
 template <class T>
 void launch_permute(int nb, int bs, const int* perm, const T* in, T* out, bool gather, cudaStream_t s);
 
+// ---------------------------------------------------------------------------
+// Learned correction step (fhg_learned.cu)
+
+namespace learned {
+constexpr int kIn = 48;            // network input per face
+constexpr int kHid = 128;          // two hidden layers
+constexpr int kOut = 16;           // output rows (the first bs are the correction)
+constexpr int kResidualSlots = 32; // input [0, 32): scaled residual of the face and 6 neighbours (7 bs used)
+constexpr int kTensorSlots = 16;   // input [32, 48): two element tensors (2 x 6) and 4 zeros
+constexpr int kNeighbours = 6;
+constexpr int kMaxLearnedBs = 4;
+// FP32 master parameter layout: W1 [128][48], b1, W2 [128][128], b2, W3 [16][128], b3.
+constexpr int kOffW1 = 0;
+constexpr int kOffB1 = kOffW1 + kHid * kIn;
+constexpr int kOffW2 = kOffB1 + kHid;
+constexpr int kOffB2 = kOffW2 + kHid * kHid;
+constexpr int kOffW3 = kOffB2 + kHid;
+constexpr int kOffB3 = kOffW3 + kOut * kHid;
+constexpr int kParams = kOffB3 + kOut;
+constexpr int kWeights = kHid * kIn + kHid * kHid + kOut * kHid;  // BF16 copy: W1, W2, W3
+constexpr int kBiases = 2 * kHid + kOut;                           // FP32: b1, b2, b3
+constexpr int kColsumChunks = 256;
+enum GemmKind { kGemmFwdHid = 0, kGemmFwdOut = 1, kGemmBwdData = 2, kGemmGradHid = 3, kGemmGradIn = 4 };
+}  // namespace learned
+
+bool learned_supports(int bs);
+// w = D^-1 r on the level's blocks (FP32).
+void launch_block_diag(int nb, int bs, const float* dinv, long long dld, const float* r, float* w, cudaStream_t s);
+// Training features: feat (rows x 48 BF16, rows >= nb zero), scale (rows).
+void launch_features(int nb, int rows, int bs, const int* nbr, const float* w, const void* tfeat, void* feat,
+                     float* scale, cudaStream_t s);
+// x += s y for every face (fused gather + 3-layer MLP). Returns non-zero if the kernel cannot run.
+int launch_learned_apply(int nb, int bs, const int* nbr, const float* w, const void* tfeat, const void* wts,
+                         const float* bias, float* x, cudaStream_t s);
+void launch_gemm(int kind, int M, int K, const void* A, int lda, const void* B, int ldb, float* C, float* parts,
+                 int nsplit, int accumulate, cudaStream_t s);
+void launch_bias_gelu(long long rows, float* a, const float* bias, void* h, cudaStream_t s);
+void launch_gelu_back(long long count, const float* dh, const float* a, void* delta, cudaStream_t s);
+void launch_correction(int nb, int bs, const float* y, const float* b3, const float* scale, float* c, cudaStream_t s);
+// dy (rows x 16 BF16) = dL/dy of the energy loss; partials[kReduceCtas] of (c.q - 2 c.r).
+void launch_energy_grad(int nb, int rows, int bs, const float* r, const float* q, const float* c, const float* scale,
+                        double inv_energy, void* dy, double* partials, cudaStream_t s);
+// out[ncol] = column sums of a BF16 rows x ncol matrix (parts: kColsumChunks * ncol floats).
+void launch_colsum(long long rows, int ncol, const void* m, float* parts, float* out, cudaStream_t s);
+void launch_adam(int n, float* p, const float* grad, float* m, float* v, float lr, float beta1, float beta2, float eps,
+                 int step, float weight_decay, cudaStream_t s);
+void launch_split_params(const float* p, void* wts, float* bias, cudaStream_t s);
+
 }  // namespace fhg

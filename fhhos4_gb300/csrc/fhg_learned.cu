@@ -1,0 +1,671 @@
+// Learned correction step of the FP32 V-cycle: a per-face-patch MLP, its BF16 tensor-core
+// inference and training kernels (FP32 accumulation), and the energy-norm loss.
+//
+// The network sees, for every face block i of the finest level, the block-Jacobi-scaled
+// residual w = D^-1 (b - A x) on the face and on its (up to) six neighbours in the operator,
+// ordered by decreasing coupling strength |A_ij|_F, plus the diffusion tensors of the face's
+// two elements:
+//
+//   input  u_i (48)  = [ w_i / s_i, w_j1 / s_i, ..., w_j6 / s_i  (7 bs, zero padded to 32),
+//                        T_1 / tau_i, T_2 / tau_i  (2 x 6: xx yy zz xy xz yz), 0 0 0 0 ]
+//   s_i             = sqrt(mean of the squares of the 7 bs residual slots)
+//   h1 = gelu(W1 u + b1)    (128)
+//   h2 = gelu(W2 h1 + b2)   (128)
+//   y  = W3 h2 + b3         (16, entries >= bs unused)
+//   x_i += s_i y_i[0..bs)
+//
+// so the correction is positively homogeneous in the residual (a residual scaled by a > 0
+// gets a correction scaled by a), which keeps it meaningful across the twelve orders of
+// magnitude of a solve. gelu is the tanh form of Hendrycks & Gimpel (2016),
+// 0.5 a (1 + tanh(sqrt(2/pi) (a + 0.044715 a^3))), with the hardware tanh approximation.
+//
+// Tensor cores: mma.sync.m16n8k16 BF16 x BF16 -> FP32 with ldmatrix fragment loads. The
+// inference kernel keeps a 16-face tile in registers through all three layers (the FP32
+// accumulator fragment of one layer is exactly the BF16 A fragment of the next), with the
+// weights staged once per CTA in shared memory; the training kernels are tiled GEMMs.
+#include "fhg_internal.h"
+
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstdint>
+
+namespace fhg {
+namespace {
+
+using bf16 = __nv_bfloat16;
+using namespace learned;
+
+// ---------------------------------------------------------------------------
+// Fragment helpers (m16n8k16, row.col, BF16 in, FP32 accumulate)
+
+__device__ __forceinline__ unsigned smem_u32(const void* p)
+{
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const bf16* p)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_u32(p)));
+}
+
+__device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const bf16* p)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_u32(p)));
+}
+
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+{
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};\n"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
+{
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+
+__device__ __forceinline__ float tanh_fast(float x)
+{
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+constexpr float kGeluC0 = 0.7978845608028654f;  // sqrt(2/pi)
+constexpr float kGeluC1 = 0.044715f;
+
+__device__ __forceinline__ float gelu(float a)
+{
+    const float u = kGeluC0 * fmaf(kGeluC1 * a, a * a, a);
+    return 0.5f * a * (1.0f + tanh_fast(u));
+}
+
+__device__ __forceinline__ float gelu_grad(float a)
+{
+    const float a2 = a * a;
+    const float t = tanh_fast(kGeluC0 * fmaf(kGeluC1 * a, a2, a));
+    return 0.5f * (1.0f + t) + 0.5f * a * (1.0f - t * t) * kGeluC0 * fmaf(3.0f * kGeluC1, a2, 1.0f);
+}
+
+// ---------------------------------------------------------------------------
+// Input features of one face (shared by inference and training so that both see the same
+// bits). Writes the 32 residual slots of the input row as BF16 and returns s_i.
+
+template <int BS>
+__device__ __forceinline__ float face_inputs(int f, const int* __restrict__ nbr, const float* __restrict__ w,
+                                             bf16* row)
+{
+    static_assert(7 * BS <= kResidualSlots, "7 bs residual slots must fit");
+    float v[7 * BS];
+#pragma unroll
+    for (int c = 0; c < BS; c++) v[c] = w[(long long)f * BS + c];
+#pragma unroll
+    for (int j = 0; j < kNeighbours; j++) {
+        const int g = nbr[(long long)f * kNeighbours + j];
+#pragma unroll
+        for (int c = 0; c < BS; c++) v[(j + 1) * BS + c] = g >= 0 ? w[(long long)g * BS + c] : 0.0f;
+    }
+    float ss = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 7 * BS; q++) ss = fmaf(v[q], v[q], ss);
+    const float s = sqrtf(ss * (1.0f / (7 * BS)));
+    const float inv = s > 0.0f ? 1.0f / s : 0.0f;
+    uint32_t packed[kResidualSlots / 2];
+#pragma unroll
+    for (int q = 0; q < kResidualSlots / 2; q++) {
+        const float lo = 2 * q < 7 * BS ? v[2 * q] * inv : 0.0f;
+        const float hi = 2 * q + 1 < 7 * BS ? v[2 * q + 1] * inv : 0.0f;
+        packed[q] = pack_bf16(lo, hi);
+    }
+    uint4* dst = reinterpret_cast<uint4*>(row);
+#pragma unroll
+    for (int q = 0; q < kResidualSlots / 8; q++)
+        dst[q] = make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
+    return s;
+}
+
+// Features of every face (training path): feat[f] = input row (48 BF16), scale[f] = s_f.
+// Rows in [nb, rows) are zero (padding of the GEMM tiles).
+template <int BS>
+__global__ void __launch_bounds__(256) k_features(int nb, int rows, const int* __restrict__ nbr,
+                                                  const float* __restrict__ w, const bf16* __restrict__ tfeat,
+                                                  bf16* __restrict__ feat, float* __restrict__ scale)
+{
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= rows) return;
+    bf16* row = feat + (long long)f * kIn;
+    uint4* dst = reinterpret_cast<uint4*>(row);
+    if (f >= nb) {
+#pragma unroll
+        for (int q = 0; q < kIn / 8; q++) dst[q] = make_uint4(0, 0, 0, 0);
+        scale[f] = 0.0f;
+        return;
+    }
+    scale[f] = face_inputs<BS>(f, nbr, w, row);
+    const uint4* src = reinterpret_cast<const uint4*>(tfeat + (long long)f * kTensorSlots);
+    dst[kResidualSlots / 8] = src[0];
+    dst[kResidualSlots / 8 + 1] = src[1];
+}
+
+// ---------------------------------------------------------------------------
+// Fused inference: x_i += s_i y_i for every face, one warp per 16-face tile.
+
+constexpr int kApplyWarps = 8;
+constexpr int kLd1 = kIn + 8;    // padded shared-memory row of W1 and of the input tile (BF16)
+constexpr int kLd2 = kHid + 8;   // padded row of W2 and W3
+constexpr size_t kApplySmem =
+    sizeof(bf16) * ((size_t)kHid * kLd1 + (size_t)kHid * kLd2 + (size_t)kOut * kLd2 + (size_t)kApplyWarps * 16 * kLd1) +
+    sizeof(float) * (kHid + kHid + kOut);
+
+template <int BS>
+__global__ void __launch_bounds__(kApplyWarps * 32, 1)
+    k_learned_apply(int nb, const int* __restrict__ nbr, const float* __restrict__ w, const bf16* __restrict__ tfeat,
+                    const bf16* __restrict__ wts, const float* __restrict__ bias, float* __restrict__ x)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    bf16* sW1 = reinterpret_cast<bf16*>(smem_raw);
+    bf16* sW2 = sW1 + kHid * kLd1;
+    bf16* sW3 = sW2 + kHid * kLd2;
+    bf16* sX = sW3 + kOut * kLd2;
+    float* sB = reinterpret_cast<float*>(sX + kApplyWarps * 16 * kLd1);
+    // Stage the weights (global layout: W1 [128][48], W2 [128][128], W3 [16][128], row-major).
+    const bf16* gW1 = wts;
+    const bf16* gW2 = gW1 + kHid * kIn;
+    const bf16* gW3 = gW2 + kHid * kHid;
+    for (int v = threadIdx.x; v < kHid * kIn / 8; v += blockDim.x) {
+        const int r = v / (kIn / 8), c = (v % (kIn / 8)) * 8;
+        *reinterpret_cast<uint4*>(sW1 + r * kLd1 + c) = *reinterpret_cast<const uint4*>(gW1 + r * kIn + c);
+    }
+    for (int v = threadIdx.x; v < kHid * kHid / 8; v += blockDim.x) {
+        const int r = v / (kHid / 8), c = (v % (kHid / 8)) * 8;
+        *reinterpret_cast<uint4*>(sW2 + r * kLd2 + c) = *reinterpret_cast<const uint4*>(gW2 + r * kHid + c);
+    }
+    for (int v = threadIdx.x; v < kOut * kHid / 8; v += blockDim.x) {
+        const int r = v / (kHid / 8), c = (v % (kHid / 8)) * 8;
+        *reinterpret_cast<uint4*>(sW3 + r * kLd2 + c) = *reinterpret_cast<const uint4*>(gW3 + r * kHid + c);
+    }
+    for (int v = threadIdx.x; v < 2 * kHid + kOut; v += blockDim.x) sB[v] = bias[v];
+    __syncthreads();
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = lane >> 2, t = lane & 3, q = lane >> 3, r8 = lane & 7;
+    bf16* tile = sX + warp * 16 * kLd1;
+    const int ntiles = (nb + 15) / 16;
+    for (int tI = blockIdx.x * kApplyWarps + warp; tI < ntiles; tI += gridDim.x * kApplyWarps) {
+        const int f0 = tI * 16;
+        // Gather: lanes 0-15 build the residual slots of face f0+lane, lanes 16-31 copy its tensors.
+        float s = 0.0f;
+        {
+            const int row = lane & 15;
+            const int f = f0 + row;
+            bf16* dst = tile + row * kLd1;
+            if (lane < 16) {
+                if (f < nb) {
+                    s = face_inputs<BS>(f, nbr, w, dst);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < kResidualSlots / 8; c++) reinterpret_cast<uint4*>(dst)[c] = make_uint4(0, 0, 0, 0);
+                }
+            } else {
+                uint4 a = make_uint4(0, 0, 0, 0), b = a;
+                if (f < nb) {
+                    const uint4* src = reinterpret_cast<const uint4*>(tfeat + (long long)f * kTensorSlots);
+                    a = src[0];
+                    b = src[1];
+                }
+                reinterpret_cast<uint4*>(dst + kResidualSlots)[0] = a;
+                reinterpret_cast<uint4*>(dst + kResidualSlots)[1] = b;
+            }
+        }
+        __syncwarp();
+        const float s_lo = __shfl_sync(0xffffffffu, s, g);
+        const float s_hi = __shfl_sync(0xffffffffu, s, g + 8);
+
+        float acc[kHid / 8][4];
+#pragma unroll
+        for (int j = 0; j < kHid / 8; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+        // Layer 1: [16 x 48] x W1^T
+#pragma unroll
+        for (int ks = 0; ks < kIn / 16; ks++) {
+            uint32_t a[4];
+            ldsm_x4(a, tile + (r8 + (q & 1) * 8) * kLd1 + ks * 16 + (q >> 1) * 8);
+#pragma unroll
+            for (int j = 0; j < kHid / 8; j += 2) {
+                uint32_t b[4];
+                ldsm_x4(b, sW1 + (8 * j + r8 + (q >> 1) * 8) * kLd1 + ks * 16 + (q & 1) * 8);
+                mma16816(acc[j], a, b[0], b[1]);
+                mma16816(acc[j + 1], a, b[2], b[3]);
+            }
+        }
+        uint32_t h[kHid / 16][4];
+#pragma unroll
+        for (int kk = 0; kk < kHid / 16; kk++) {
+#pragma unroll
+            for (int half = 0; half < 2; half++) {
+                const int j = 2 * kk + half;
+                const float b0 = sB[8 * j + 2 * t], b1 = sB[8 * j + 2 * t + 1];
+                h[kk][2 * half] = pack_bf16(gelu(acc[j][0] + b0), gelu(acc[j][1] + b1));
+                h[kk][2 * half + 1] = pack_bf16(gelu(acc[j][2] + b0), gelu(acc[j][3] + b1));
+            }
+        }
+        // Layer 2: [16 x 128] x W2^T
+#pragma unroll
+        for (int j = 0; j < kHid / 8; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+#pragma unroll
+        for (int kk = 0; kk < kHid / 16; kk++) {
+#pragma unroll
+            for (int j = 0; j < kHid / 8; j += 2) {
+                uint32_t b[4];
+                ldsm_x4(b, sW2 + (8 * j + r8 + (q >> 1) * 8) * kLd2 + kk * 16 + (q & 1) * 8);
+                mma16816(acc[j], h[kk], b[0], b[1]);
+                mma16816(acc[j + 1], h[kk], b[2], b[3]);
+            }
+        }
+#pragma unroll
+        for (int kk = 0; kk < kHid / 16; kk++) {
+#pragma unroll
+            for (int half = 0; half < 2; half++) {
+                const int j = 2 * kk + half;
+                const float b0 = sB[kHid + 8 * j + 2 * t], b1 = sB[kHid + 8 * j + 2 * t + 1];
+                h[kk][2 * half] = pack_bf16(gelu(acc[j][0] + b0), gelu(acc[j][1] + b1));
+                h[kk][2 * half + 1] = pack_bf16(gelu(acc[j][2] + b0), gelu(acc[j][3] + b1));
+            }
+        }
+        // Layer 3: [16 x 128] x W3^T -> 16 outputs
+        float y[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+        for (int kk = 0; kk < kHid / 16; kk++) {
+            uint32_t b[4];
+            ldsm_x4(b, sW3 + (r8 + (q >> 1) * 8) * kLd2 + kk * 16 + (q & 1) * 8);
+            mma16816(y[0], h[kk], b[0], b[1]);
+            mma16816(y[1], h[kk], b[2], b[3]);
+        }
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+#pragma unroll
+            for (int e = 0; e < 2; e++) {
+                const int col = 8 * j + 2 * t + e;
+                if (col < BS) {
+                    const float bo = sB[2 * kHid + col];
+                    const int fa = f0 + g, fb = f0 + g + 8;
+                    const float ca = s_lo * (y[j][e] + bo), cb = s_hi * (y[j][2 + e] + bo);
+                    // A non-finite network output adds nothing (the step is then the plain cycle's).
+                    if (fa < nb && isfinite(ca)) x[(long long)fa * BS + col] += ca;
+                    if (fb < nb && isfinite(cb)) x[(long long)fb * BS + col] += cb;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Training GEMM: C (+split) = sum_{k in chunk} A(m, k) B(k, n), 64 x BN tile per CTA (4 warps of
+// 16 rows), K staged 32 at a time. A(m, k) = A[m*lda + k] (AM = false) or A[k*lda + m]
+// (AM = true); B(k, n) = B[n*ldb + k] (BNM = false) or B[k*ldb + n] (BNM = true). N == BN.
+// M, lda, ldb and the chunk bounds are multiples of 8. Split y writes C + y * M * BN.
+
+template <int BN, bool AM, bool BNM>
+__global__ void __launch_bounds__(128) k_gemm(int M, int K, int k_chunk, const bf16* __restrict__ A, int lda,
+                                              const bf16* __restrict__ B, int ldb, float* __restrict__ C)
+{
+    constexpr int BK = 32;
+    constexpr int LA = AM ? 64 + 8 : BK + 8;
+    constexpr int LB = BNM ? BN + 8 : BK + 8;
+    __shared__ __align__(16) bf16 sA[AM ? BK * LA : 64 * LA];
+    __shared__ __align__(16) bf16 sB[BNM ? BK * LB : BN * LB];
+    const int m0 = blockIdx.x * 64;
+    const int kb = blockIdx.y * k_chunk;
+    const int ke = min(K, kb + k_chunk);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int q = lane >> 3, r8 = lane & 7;
+    float acc[BN / 8][4];
+#pragma unroll
+    for (int j = 0; j < BN / 8; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+    const uint4 zero = make_uint4(0, 0, 0, 0);
+    for (int k0 = kb; k0 < ke; k0 += BK) {
+        if (!AM) {
+            for (int v = threadIdx.x; v < 64 * (BK / 8); v += blockDim.x) {
+                const int r = v / (BK / 8), c = (v % (BK / 8)) * 8;
+                const int m = m0 + r, k = k0 + c;
+                *reinterpret_cast<uint4*>(sA + r * LA + c) =
+                    (m < M && k < ke) ? *reinterpret_cast<const uint4*>(A + (long long)m * lda + k) : zero;
+            }
+        } else {
+            for (int v = threadIdx.x; v < BK * 8; v += blockDim.x) {
+                const int r = v / 8, c = (v % 8) * 8;
+                const int k = k0 + r, m = m0 + c;
+                *reinterpret_cast<uint4*>(sA + r * LA + c) =
+                    (k < ke && m < M) ? *reinterpret_cast<const uint4*>(A + (long long)k * lda + m) : zero;
+            }
+        }
+        if (!BNM) {
+            for (int v = threadIdx.x; v < BN * (BK / 8); v += blockDim.x) {
+                const int r = v / (BK / 8), c = (v % (BK / 8)) * 8;
+                const int k = k0 + c;
+                *reinterpret_cast<uint4*>(sB + r * LB + c) =
+                    k < ke ? *reinterpret_cast<const uint4*>(B + (long long)r * ldb + k) : zero;
+            }
+        } else {
+            for (int v = threadIdx.x; v < BK * (BN / 8); v += blockDim.x) {
+                const int r = v / (BN / 8), c = (v % (BN / 8)) * 8;
+                const int k = k0 + r;
+                *reinterpret_cast<uint4*>(sB + r * LB + c) =
+                    k < ke ? *reinterpret_cast<const uint4*>(B + (long long)k * ldb + c) : zero;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int ks = 0; ks < BK; ks += 16) {
+            uint32_t a[4];
+            if (!AM) ldsm_x4(a, sA + (16 * warp + r8 + (q & 1) * 8) * LA + ks + (q >> 1) * 8);
+            else ldsm_x4_t(a, sA + (ks + r8 + (q >> 1) * 8) * LA + 16 * warp + (q & 1) * 8);
+#pragma unroll
+            for (int j = 0; j < BN / 8; j += 2) {
+                uint32_t b[4];
+                if (!BNM) ldsm_x4(b, sB + (8 * j + r8 + (q >> 1) * 8) * LB + ks + (q & 1) * 8);
+                else ldsm_x4_t(b, sB + (ks + r8 + (q & 1) * 8) * LB + 8 * j + (q >> 1) * 8);
+                mma16816(acc[j], a, b[0], b[1]);
+                mma16816(acc[j + 1], a, b[2], b[3]);
+            }
+        }
+        __syncthreads();
+    }
+    float* Cp = C + (long long)blockIdx.y * M * BN;
+    const int g = lane >> 2, t = lane & 3;
+    const int ma = m0 + 16 * warp + g, mb = ma + 8;
+#pragma unroll
+    for (int j = 0; j < BN / 8; j++) {
+        const int n = 8 * j + 2 * t;
+        if (ma < M) { Cp[(long long)ma * BN + n] = acc[j][0]; Cp[(long long)ma * BN + n + 1] = acc[j][1]; }
+        if (mb < M) { Cp[(long long)mb * BN + n] = acc[j][2]; Cp[(long long)mb * BN + n + 1] = acc[j][3]; }
+    }
+}
+
+// out[i] (+)= sum_s parts[s * count + i], fixed order.
+__global__ void k_sum_splits(int nsplit, long long count, const float* __restrict__ parts, float* __restrict__ out,
+                             int accumulate)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    float v = 0.0f;
+    for (int s = 0; s < nsplit; s++) v += parts[(long long)s * count + i];
+    out[i] = accumulate ? out[i] + v : v;
+}
+
+// a += bias (per column, 128 columns); h = bf16(gelu(a)). a keeps the pre-activation.
+__global__ void k_bias_gelu(long long rows, float* __restrict__ a, const float* __restrict__ bias, bf16* __restrict__ h)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows * kHid) return;
+    const float v = a[i] + bias[i % kHid];
+    a[i] = v;
+    h[i] = __float2bfloat16_rn(gelu(v));
+}
+
+// delta = bf16(dh * gelu'(a)).
+__global__ void k_gelu_back(long long count, const float* __restrict__ dh, const float* __restrict__ a,
+                            bf16* __restrict__ delta)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    delta[i] = __float2bfloat16_rn(dh[i] * gelu_grad(a[i]));
+}
+
+// Correction c_f = s_f (y_f + b3)[0..bs) into the level-0 vector layout.
+template <int BS>
+__global__ void k_correction(int nb, const float* __restrict__ y, const float* __restrict__ b3,
+                             const float* __restrict__ scale, float* __restrict__ c)
+{
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nb) return;
+#pragma unroll
+    for (int k = 0; k < BS; k++) c[(long long)f * BS + k] = scale[f] * (y[(long long)f * kOut + k] + b3[k]);
+}
+
+// Energy loss L = |e - c|_A^2 / E with E = e^T A e = e^T r, r = A e, q = A c:
+//   L = 1 + (c.q - 2 c.r) / E,   dL/dc = -2 (r - q) / E,   dL/dy_f = s_f dL/dc_f.
+// dy rows >= nb (GEMM padding) are zero. partials[cta] = sum (c.q - 2 c.r) of the CTA.
+template <int BS>
+__global__ void __launch_bounds__(256) k_energy_grad(int nb, int rows, const float* __restrict__ r,
+                                                     const float* __restrict__ q, const float* __restrict__ c,
+                                                     const float* __restrict__ scale, double inv_energy,
+                                                     bf16* __restrict__ dy, double* __restrict__ partials)
+{
+    __shared__ double sh[256 / 32];
+    double acc = 0.0;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < rows; f += gridDim.x * blockDim.x) {
+        uint32_t packed[kOut / 2];
+        float gv[kOut];
+#pragma unroll
+        for (int k = 0; k < kOut; k++) gv[k] = 0.0f;
+        if (f < nb) {
+#pragma unroll
+            for (int k = 0; k < BS; k++) {
+                const long long i = (long long)f * BS + k;
+                const float ri = r[i], qi = q[i], ci = c[i];
+                acc += (double)ci * qi - 2.0 * (double)ci * ri;
+                gv[k] = (float)(scale[f] * (-2.0 * ((double)ri - qi) * inv_energy));
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kOut / 2; k++) packed[k] = pack_bf16(gv[2 * k], gv[2 * k + 1]);
+        uint4* dst = reinterpret_cast<uint4*>(dy + (long long)f * kOut);
+        dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+        dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int wI = 0; wI < 256 / 32; wI++) t += sh[wI];
+        partials[blockIdx.x] = t;
+    }
+}
+
+// Column sums of a BF16 [rows x ncol] matrix into parts[chunk][ncol] (fixed row chunks).
+__global__ void k_colsum(long long rows, int ncol, long long chunk, const bf16* __restrict__ m,
+                         float* __restrict__ parts)
+{
+    const int col = threadIdx.x;
+    if (col >= ncol) return;
+    const long long r0 = (long long)blockIdx.x * chunk, r1 = min(rows, r0 + chunk);
+    float v = 0.0f;
+    for (long long r = r0; r < r1; r++) v += __bfloat162float(m[r * ncol + col]);
+    parts[(long long)blockIdx.x * ncol + col] = v;
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master parameters, then the BF16 weight copy.
+__global__ void k_adam(int n, float* __restrict__ p, const float* __restrict__ grad, float* __restrict__ m,
+                       float* __restrict__ v, float lr, float beta1, float beta2, float eps, float c1, float c2,
+                       float weight_decay)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gI = grad[i];
+    const float mi = beta1 * m[i] + (1.0f - beta1) * gI;
+    const float vi = beta2 * v[i] + (1.0f - beta2) * gI * gI;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * ((mi / c1) / (sqrtf(vi / c2) + eps) + weight_decay * p[i]);
+}
+
+// Master parameters -> BF16 weights (W1, W2, W3 contiguous) and FP32 biases (b1, b2, b3).
+__global__ void k_split_params(const float* __restrict__ p, bf16* __restrict__ wts, float* __restrict__ bias)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < kHid * kIn) wts[i] = __float2bfloat16_rn(p[kOffW1 + i]);
+    if (i < kHid * kHid) wts[kHid * kIn + i] = __float2bfloat16_rn(p[kOffW2 + i]);
+    if (i < kOut * kHid) wts[kHid * kIn + kHid * kHid + i] = __float2bfloat16_rn(p[kOffW3 + i]);
+    if (i < kHid) { bias[i] = p[kOffB1 + i]; bias[kHid + i] = p[kOffB2 + i]; }
+    if (i < kOut) bias[2 * kHid + i] = p[kOffB3 + i];
+}
+
+// w = D^-1 r (block diagonal, D^-1 entry-major: entry (r, c) of block i at dinv[(r*BS + c)*dld + i]).
+template <int BS>
+__global__ void k_block_diag(int nb, const float* __restrict__ dinv, long long dld, const float* __restrict__ r,
+                             float* __restrict__ w)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    float t[BS];
+#pragma unroll
+    for (int c = 0; c < BS; c++) t[c] = r[(long long)i * BS + c];
+#pragma unroll
+    for (int rr = 0; rr < BS; rr++) {
+        float v = 0.0f;
+#pragma unroll
+        for (int c = 0; c < BS; c++) v = fmaf(dinv[(long long)(rr * BS + c) * dld + i], t[c], v);
+        w[(long long)i * BS + rr] = v;
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Launchers
+
+#define FHG_LEARNED_BS(BSV, ...)                                                                   \
+    switch (BSV) {                                                                                 \
+    case 2: { constexpr int BS = 2; __VA_ARGS__; } break;                                          \
+    case 3: { constexpr int BS = 3; __VA_ARGS__; } break;                                          \
+    case 4: { constexpr int BS = 4; __VA_ARGS__; } break;                                          \
+    default: break;                                                                                \
+    }
+
+bool learned_supports(int bs) { return bs >= 2 && bs <= kMaxLearnedBs; }
+
+void launch_block_diag(int nb, int bs, const float* dinv, long long dld, const float* r, float* w, cudaStream_t s)
+{
+    const int grid = (nb + 255) / 256;
+    FHG_LEARNED_BS(bs, k_block_diag<BS><<<grid, 256, 0, s>>>(nb, dinv, dld, r, w));
+    g_kernel_launches++;
+}
+
+void launch_features(int nb, int rows, int bs, const int* nbr, const float* w, const void* tfeat, void* feat,
+                     float* scale, cudaStream_t s)
+{
+    const int grid = (rows + 255) / 256;
+    FHG_LEARNED_BS(bs, k_features<BS><<<grid, 256, 0, s>>>(nb, rows, nbr, w, (const bf16*)tfeat, (bf16*)feat, scale));
+    g_kernel_launches++;
+}
+
+int launch_learned_apply(int nb, int bs, const int* nbr, const float* w, const void* tfeat, const void* wts,
+                         const float* bias, float* x, cudaStream_t s)
+{
+    // Persistent grid: as many CTAs as fit on the device at once (computed once per block size
+    // and device; the shared-memory attribute is set with it).
+    static int grid_of[kMaxLearnedBs + 1][16] = {};
+    int dev = 0;
+    if (!learned_supports(bs) || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) return -1;
+    if (grid_of[bs][dev] == 0) {
+        cudaError_t e = cudaErrorInvalidValue;
+        int per_sm = 0, sms = 0;
+        FHG_LEARNED_BS(bs, {
+            e = cudaFuncSetAttribute(k_learned_apply<BS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kApplySmem);
+            if (e == cudaSuccess)
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_learned_apply<BS>, kApplyWarps * 32, kApplySmem);
+        });
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess || per_sm < 1) return -1;
+        grid_of[bs][dev] = per_sm * sms;
+    }
+    const int tiles = (nb + 15) / 16;
+    const int grid = std::min(grid_of[bs][dev], (tiles + kApplyWarps - 1) / kApplyWarps);
+    if (grid < 1) return 0;
+    FHG_LEARNED_BS(bs, k_learned_apply<BS><<<grid, kApplyWarps * 32, kApplySmem, s>>>(
+                           nb, nbr, w, (const bf16*)tfeat, (const bf16*)wts, bias, x));
+    g_kernel_launches++;
+    return 0;
+}
+
+// C = A B over K (see k_gemm); nsplit > 1 splits K into chunks written to `parts`
+// (nsplit * M * N floats) and summed into C in a fixed order.
+void launch_gemm(int kind, int M, int K, const void* A, int lda, const void* B, int ldb, float* C, float* parts,
+                 int nsplit, int accumulate, cudaStream_t s)
+{
+    const bf16* a = (const bf16*)A;
+    const bf16* b = (const bf16*)B;
+    int chunk = K;
+    if (nsplit > 1) chunk = ((K + nsplit - 1) / nsplit + 31) / 32 * 32;
+    if (chunk < 32) chunk = 32;
+    const int splits = (K + chunk - 1) / chunk;
+    float* out = splits > 1 || accumulate ? parts : C;
+    dim3 grid((M + 63) / 64, splits);
+    int N = 0;
+    switch (kind) {
+    case kGemmFwdHid: k_gemm<kHid, false, false><<<grid, 128, 0, s>>>(M, K, chunk, a, lda, b, ldb, out); N = kHid; break;
+    case kGemmFwdOut: k_gemm<kOut, false, false><<<grid, 128, 0, s>>>(M, K, chunk, a, lda, b, ldb, out); N = kOut; break;
+    case kGemmBwdData: k_gemm<kHid, false, true><<<grid, 128, 0, s>>>(M, K, chunk, a, lda, b, ldb, out); N = kHid; break;
+    case kGemmGradHid: k_gemm<kHid, true, true><<<grid, 128, 0, s>>>(M, K, chunk, a, lda, b, ldb, out); N = kHid; break;
+    case kGemmGradIn: k_gemm<kIn, true, true><<<grid, 128, 0, s>>>(M, K, chunk, a, lda, b, ldb, out); N = kIn; break;
+    default: return;
+    }
+    g_kernel_launches++;
+    if (out == parts) {
+        const long long count = (long long)M * N;
+        k_sum_splits<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(splits, count, parts, C, accumulate);
+        g_kernel_launches++;
+    }
+}
+
+void launch_bias_gelu(long long rows, float* a, const float* bias, void* h, cudaStream_t s)
+{
+    const long long n = rows * kHid;
+    k_bias_gelu<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(rows, a, bias, (bf16*)h);
+    g_kernel_launches++;
+}
+
+void launch_gelu_back(long long count, const float* dh, const float* a, void* delta, cudaStream_t s)
+{
+    k_gelu_back<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(count, dh, a, (bf16*)delta);
+    g_kernel_launches++;
+}
+
+void launch_correction(int nb, int bs, const float* y, const float* b3, const float* scale, float* c, cudaStream_t s)
+{
+    FHG_LEARNED_BS(bs, k_correction<BS><<<(nb + 255) / 256, 256, 0, s>>>(nb, y, b3, scale, c));
+    g_kernel_launches++;
+}
+
+void launch_energy_grad(int nb, int rows, int bs, const float* r, const float* q, const float* c, const float* scale,
+                        double inv_energy, void* dy, double* partials, cudaStream_t s)
+{
+    FHG_LEARNED_BS(bs, k_energy_grad<BS><<<kReduceCtas, 256, 0, s>>>(nb, rows, r, q, c, scale, inv_energy, (bf16*)dy,
+                                                                     partials));
+    g_kernel_launches++;
+}
+
+void launch_colsum(long long rows, int ncol, const void* m, float* parts, float* out, cudaStream_t s)
+{
+    const long long chunk = (rows + kColsumChunks - 1) / kColsumChunks;
+    k_colsum<<<kColsumChunks, 128, 0, s>>>(rows, ncol, chunk > 0 ? chunk : 1, (const bf16*)m, parts);
+    k_sum_splits<<<(ncol + 255) / 256, 256, 0, s>>>(kColsumChunks, ncol, parts, out, 0);
+    g_kernel_launches += 2;
+}
+
+void launch_adam(int n, float* p, const float* grad, float* m, float* v, float lr, float beta1, float beta2, float eps,
+                 int step, float weight_decay, cudaStream_t s)
+{
+    const float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
+    k_adam<<<(n + 255) / 256, 256, 0, s>>>(n, p, grad, m, v, lr, beta1, beta2, eps, c1, c2, weight_decay);
+    g_kernel_launches++;
+}
+
+void launch_split_params(const float* p, void* wts, float* bias, cudaStream_t s)
+{
+    k_split_params<<<(kHid * kHid + 255) / 256, 256, 0, s>>>(p, (bf16*)wts, bias);
+    g_kernel_launches++;
+}
+
+}  // namespace fhg

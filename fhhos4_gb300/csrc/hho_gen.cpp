@@ -1370,4 +1370,26 @@ int fhg_hho_rhs(const fhg_hho* h, const double** b)
     return 0;
 }
 
+int fhg_hho_face_tensors(const fhg_hho* h, int l, double* out)
+{
+    if (!h || !out || l < 0 || l >= (int)h->levels.size()) return -1;
+    const Mesh& M = h->levels[l].mesh;
+    const int dim = M.dim;
+    for (size_t f = 0; f < M.fv.size(); f++) {
+        const int u = M.number[f];
+        if (u < 0) continue;
+        const int els[2] = {M.fe1[f], M.fe2[f]};
+        for (int side = 0; side < 2; side++) {
+            double* t = out + (size_t)u * 12 + side * 6;
+            const auto& K = M.K[els[side]];
+            if (dim == 3) {
+                t[0] = K[0]; t[1] = K[4]; t[2] = K[8]; t[3] = K[1]; t[4] = K[2]; t[5] = K[5];
+            } else {
+                t[0] = K[0]; t[1] = K[3]; t[2] = K[1]; t[3] = 0; t[4] = 0; t[5] = 0;
+            }
+        }
+    }
+    return 0;
+}
+
 }  // extern "C"

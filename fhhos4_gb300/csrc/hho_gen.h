@@ -47,6 +47,11 @@ int fhg_hho_rhs(const fhg_hho* h, const double** b);
 /* Relative L2 error of the reconstruction of face solution x (level-0 numbering) against the
  * exact solution of the sine source; -2 for sources without a closed form. */
 int fhg_hho_l2_error(const fhg_hho* h, const double* x, double* rel_error);
+/* Diffusion tensors of the two elements of every unknown face of level `level` (both exist: the
+ * unknowns are the interior faces): out[12*u .. 12*u+11] for face block u, element 1 then
+ * element 2 (the face's own element order), each as (xx, yy, zz, xy, xz, yz) in 3D and
+ * (xx, yy, xy, 0, 0, 0) in 2D. */
+int fhg_hho_face_tensors(const fhg_hho* h, int level, double* out);
 
 #ifdef __cplusplus
 }

@@ -48,6 +48,7 @@ def lib():
                                            P(P(C.c_int)), P(P(C.c_int)), P(P(C.c_double))]
         L.fhg_hho_rhs.argtypes = [C.c_void_p, P(P(C.c_double))]
         L.fhg_hho_l2_error.argtypes = [C.c_void_p, C.c_void_p, P(C.c_double)]
+        L.fhg_hho_face_tensors.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         _lib = L
     return _lib
 
@@ -114,6 +115,15 @@ class Hierarchy:
         if rc != 0:
             raise RuntimeError("no exact solution for this source" if rc == -2 else "l2_error failed")
         return out.value
+
+    def face_tensors(self, l: int = 0) -> np.ndarray:
+        """(n_blocks, 12): diffusion tensors of the two elements of every unknown face of level l,
+        (xx, yy, zz, xy, xz, yz) each in 3D, (xx, yy, xy, 0, 0, 0) in 2D."""
+        nb = self.A_rows(l) // self.block_size
+        out = np.zeros((nb, 12), dtype=np.float64)
+        if lib().fhg_hho_face_tensors(self.h, l, C.c_void_p(out.ctypes.data)) != 0:
+            raise RuntimeError("face_tensors failed")
+        return out
 
     def A_rows(self, l: int) -> int:
         n = C.c_int()

@@ -79,6 +79,7 @@ class Multigrid(IterativeSolver):
         self.RelaxationParameter = 1.0
         self.BlockSizeForBlockSmoothers = -1
         self.MatrixMaxSizeForCoarsestLevel = 1000
+        self.UseGalerkinOperator = False   # coarse operators P^T A P (Level.h:133-137, "-g 1")
         # GB300 knobs
         self.VCyclePrecision = "fp64"
         self.Colouring = True
@@ -150,6 +151,7 @@ class _KrylovOnGpu(IterativeSolver):
         o.max_coarse_rows = mg.MaxCoarseRows
         o.outer_split = 1 if self.OuterSplit else 0
         o.w_loops = mg.WLoops if mg.Cycle == "W" else 1
+        o.galerkin = 1 if mg.UseGalerkinOperator else 0
         return o
 
     def Setup(self, A):
@@ -223,7 +225,7 @@ class ConjugateGradient(_KrylovOnGpu):
 
 def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: str = "bgs", post: str = "rbgs",
            precision: str = "fp64", krylov: str = "fcg", device: int = 0, autotune: bool = False,
-           use_graphs: bool = True, outer_split: bool = True, cycle: str = "V"):
+           use_graphs: bool = True, outer_split: bool = True, cycle: str = "V", galerkin: bool = False):
     """SolverFactory-style construction of "-s fcgmg -cycle V,1,1" (src/Solver/SolverFactory.h:156-200)."""
     mg = Multigrid(len(As))
     mg.SetHierarchy(As, Ps)
@@ -233,6 +235,7 @@ def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: st
     mg.Autotune = autotune
     mg.Cycle = cycle
     mg.WLoops = 2 if cycle == "W" else 1
+    mg.UseGalerkinOperator = galerkin
     solver = FlexibleConjugateGradient(1) if krylov == "fcg" else ConjugateGradient()
     solver.Precond = SolverPreconditioner(mg)
     solver.Tolerance = tol

@@ -54,6 +54,13 @@ extern "C" {
 #define FHG_PREC_FP64 0
 #define FHG_PREC_FP32 1
 
+/* Learned correction step of the FP32 V-cycle (no counterpart in the reference): off, on with
+ * the fallback rule of fhg_set_learned, or on for every iteration. */
+#define FHG_LEARNED_OFF 0
+#define FHG_LEARNED_FALLBACK 1
+#define FHG_LEARNED_ALWAYS 2
+#define FHG_LEARNED_PARAMS 24848  /* FP32 parameters: W1 128x48, b1 128, W2 128x128, b2 128, W3 16x128, b3 16 */
+
 typedef struct fhg_ctx fhg_ctx;
 
 typedef struct {
@@ -75,6 +82,9 @@ typedef struct {
                                    arithmetic (FP32 pairs, ~2^-47 relative per term, on the FP32 pipe);
                                    0 = native FP64. GB300's FP64 pipe is 56x slower than FP32. */
     int w_loops;                /* Multigrid::WLoops: 1 = V-cycle, 2 = W-cycle ("-cycle W,..", main.cpp:1179-1215) */
+    int galerkin;               /* Multigrid::UseGalerkinOperator ("-g 1", main.cpp:1307): coarse operators
+                                   A_{l+1} = P_l^T A_l P_l formed at setup (Level.h:133-137); operators given
+                                   for levels >= 1 are then not needed and are replaced */
 } fhg_options;
 
 typedef struct {
@@ -82,6 +92,8 @@ typedef struct {
     int status;                 /* FHG_OK or FHG_ERR_* */
     double normalized_residual; /* last ||r||/||b|| (recursive residual, IterationResult.h:121-139) */
     double solve_ms;            /* device time of the solve (CUDA events on the context stream) */
+    int learned_iterations;     /* iterations whose V-cycle applied the learned correction */
+    double true_relative_residual; /* FP64 ||b - A x|| / ||b|| of the returned x (-1 if the solve failed) */
 } fhg_solve_info;
 
 /* Fill *opts with the reference defaults of "-s fcgmg -cycle V,1,1": FCG(1), bgs/rbgs, 1+1
@@ -130,6 +142,7 @@ int fhg_solve_device(fhg_ctx* ctx, const double* b_dev, double* x_dev, double* h
 #define FHG_OP_SYM_SPMV 7     /* out = A.selfadjointView<Lower>() in (FlexibleConjugateGradient.h:124), level 0 */
 #define FHG_OP_COARSE_SOLVE 8 /* out = A_coarsest^{-1} in          (Multigrid.h:445-452)            */
 #define FHG_OP_VCYCLE 9       /* out = one V-cycle from zero on rhs in (Preconditioner.h:162-167), level 0 */
+#define FHG_OP_VCYCLE_LEARNED 10 /* same with the learned correction (FP32, fhg_apply_internal only) */
 int fhg_apply(fhg_ctx* ctx, int level, int op, const double* in, const double* aux, double* out);
 
 /* Device timing of one operator (same ops; vectors left in device memory) in FHG_PREC_FP64 or
@@ -178,6 +191,57 @@ long long fhg_kernel_launches(const fhg_ctx* ctx);
 int fhg_residual_norm_noalloc(int device, int n_block_rows, int block_size, int lanes,
                               const int* rowptr, const int* colidx, const double* vals, long long ld,
                               const double* x, const double* b, double* norm_out, void* stream);
+
+/* ---- Learned correction step (no counterpart in the reference) --------------------------------
+ * A per-face-patch network adds a correction at the end of the finest level's post-smoothing in
+ * the FP32 V-cycle: x_i += s_i N(u_i), where u_i holds the block-Jacobi-scaled residual
+ * D^-1 (b - A x) of face i and of its six most strongly coupled neighbours (divided by their RMS
+ * s_i) and the diffusion tensors of the face's two elements; N is a 48-128-128-16 GELU MLP run
+ * on BF16 tensor cores with FP32 accumulation. The Krylov method must be FCG (it absorbs the
+ * variable preconditioner). */
+
+/* Diffusion tensors of the two elements of every face block of level 0, in the caller's
+ * numbering: tensors[12 u .. 12 u + 11] = element 1 then element 2, each (xx, yy, zz, xy, xz, yz)
+ * ((xx, yy, xy, 0, 0, 0) in 2D). Call after fhg_set_level(0, ...), before or after setup. Faces
+ * without tensors get zero features. */
+int fhg_set_face_tensors(fhg_ctx* ctx, int n_blocks, const double* tensors);
+
+/* Install a network (params: FHG_LEARNED_PARAMS floats, host; NULL keeps the installed one) and
+ * select the mode. Needs a setup with FHG_PREC_FP32, two levels or more and block size 2..4;
+ * call after every fhg_setup. FHG_LEARNED_FALLBACK: from the third iteration of a solve on,
+ * when the geometric mean rho of the last two residual reductions falls behind the plain
+ * method's per-iteration reduction rho_p by more than half of it in log terms (rho > sqrt(rho_p);
+ * rho_p measured once per cycle configuration on a seeded random right-hand side, before the
+ * first solve's timed region), the remaining iterations use the plain V-cycle. */
+int fhg_set_learned(fhg_ctx* ctx, const float* params, int n_params, int mode);
+
+/* The plain method's calibrated per-iteration reduction used by the fallback rule. */
+int fhg_learned_reference_rate(fhg_ctx* ctx, double* rho);
+
+/* Network inputs for a level-0 residual r (FP32, DEVICE, the context's colour numbering):
+ * features = n_block_rows x 48 BF16 values (uint16 bits), scale = n_block_rows FP32 (s_i). */
+int fhg_learned_features(fhg_ctx* ctx, const float* r, void* features, float* scale);
+
+/* fhg_apply on DEVICE vectors in the context's colour numbering (fhg_get_permutation), in
+ * FHG_PREC_FP64 (double) or FHG_PREC_FP32 (float, the V-cycle copies; FHG_OP_VCYCLE_LEARNED
+ * applies the installed network). Returns after the stream has finished. */
+int fhg_apply_internal(fhg_ctx* ctx, int level, int op, int precision, const void* in, const void* aux, void* out);
+
+/* Training of the network on the GPU (FP32 master weights, BF16 tensor-core forward and backward,
+ * Adam). One step on one field: r = A e (FP32, DEVICE, colour numbering of `ctx`, which must
+ * satisfy fhg_set_learned's conditions) for an error e with energy = e.A e > 0. The loss is the
+ * relative energy error after the correction, |e - c|_A^2 / |e|_A^2, c the network's correction of
+ * every face; *loss receives it before the update, grad (host, nullable) its gradient. update = 0
+ * leaves the parameters unchanged. */
+typedef struct fhg_net fhg_net;
+int fhg_net_num_params(void);
+int fhg_net_create(fhg_net** net, int device);
+void fhg_net_destroy(fhg_net* net);
+const char* fhg_net_last_error(const fhg_net* net);
+int fhg_net_set_params(fhg_net* net, const float* params, int n_params);  /* also resets Adam */
+int fhg_net_get_params(const fhg_net* net, float* params, int n_params);
+int fhg_net_train_step(fhg_net* net, fhg_ctx* ctx, const float* r, double energy, float lr, float weight_decay,
+                       int update, double* loss, float* grad);
 
 #ifdef __cplusplus
 }
