@@ -30,8 +30,9 @@ PRECISION = {"fp64": 0, "fp32": 1}
 
 OP_SPMV, OP_RESIDUAL, OP_RESTRICT, OP_PROLONG_ADD = 0, 1, 2, 3
 OP_GS_FORWARD, OP_GS_BACKWARD, OP_JACOBI, OP_SYM_SPMV = 4, 5, 6, 7
-OP_COARSE_SOLVE, OP_VCYCLE, OP_VCYCLE_LEARNED = 8, 9, 10
+OP_COARSE_SOLVE, OP_VCYCLE, OP_VCYCLE_LEARNED, OP_LEARNED_STEP = 8, 9, 10, 11
 LEARNED = {"off": 0, "fallback": 1, "always": 2}
+LEARNED_MMA_SYNC = 16
 LEARNED_PARAMS = 24848
 
 # Every symbol include/fhg.h declares.
@@ -220,12 +221,15 @@ class Context:
             raise ValueError("face tensors are (n_blocks, 12)")
         self._check(self.lib.fhg_set_face_tensors(self.h, t.shape[0], ptr(t)))
 
-    def set_learned(self, params: np.ndarray | None, mode: str = "fallback"):
+    def set_learned(self, params: np.ndarray | None, mode: str = "fallback", kernel: str = "tcgen05"):
+        """Install a network (None keeps the installed one) and select the mode; kernel "tcgen05"
+        (tensor-memory accumulators) or "mma_sync"."""
+        m = LEARNED[mode] | (LEARNED_MMA_SYNC if kernel == "mma_sync" else 0)
         if params is None:
-            self._check(self.lib.fhg_set_learned(self.h, None, 0, LEARNED[mode]))
+            self._check(self.lib.fhg_set_learned(self.h, None, 0, m))
             return
         p = np.ascontiguousarray(params, dtype=np.float32)
-        self._check(self.lib.fhg_set_learned(self.h, ptr(p), p.size, LEARNED[mode]))
+        self._check(self.lib.fhg_set_learned(self.h, ptr(p), p.size, m))
 
     def learned_reference_rate(self) -> float:
         r = C.c_double()

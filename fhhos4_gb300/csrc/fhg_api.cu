@@ -89,6 +89,7 @@ struct fhg_ctx {
     bool ready = false;
     // Krylov state (level-0 numbering after permutation)
     double *kx = nullptr, *kr = nullptr, *kb = nullptr, *kz[2] = {nullptr, nullptr}, *kAd[2] = {nullptr, nullptr};
+    double* kt = nullptr;        // b - A x of the returned x (the true residual)
     double* partials = nullptr;  // 8 * kReduceCtas
     double* scal = nullptr;      // [0]=bnorm [1]=dAdp [2]=nr [3]=rz [4]=beta
     double* hist_d = nullptr;
@@ -110,6 +111,8 @@ struct fhg_ctx {
     float* lparams = nullptr;          // FP32 parameters of the installed network
     uint16_t* lwts = nullptr;          // its BF16 weights
     float* lbias = nullptr;            // its FP32 biases
+    int* lstatus = nullptr;            // set to 1 by a learned-step kernel whose bounded wait expired
+    int learned_kernel = 0;            // fhg::kLearnedKernelTcgen05 or kLearnedKernelMmaSync
     int learned_mode = FHG_LEARNED_OFF;
     bool learned_now = false;          // the cycle being launched or captured applies the step
     double rho_plain = 0.0;            // calibrated per-iteration reduction of the plain method
@@ -766,7 +769,8 @@ void learned_step(fhg_ctx* ctx, const float* b, float* x)
     cudaStream_t s = ctx->stream;
     fhg::launch_spmv<float>(L.A32.v, fhg::kSpmvResidual, x, b, L.r32, s);
     fhg::launch_block_diag(L.nb, L.bs, L.dinv32, L.nb, L.r32, ctx->lw, s);
-    fhg::launch_learned_apply(L.nb, L.bs, ctx->nbr_d, ctx->lw, ctx->tfeat_d, ctx->lwts, ctx->lbias, x, s);
+    fhg::launch_learned_apply(L.nb, L.bs, ctx->nbr_d, ctx->lw, ctx->tfeat_d, ctx->lwts, ctx->lbias, x, ctx->lstatus,
+                              ctx->learned_kernel, s);
 }
 
 // One multigrid cycle on level l (src/Solver/Multigrid/Multigrid.h:438-608): V for w_loops = 1,
@@ -995,7 +999,7 @@ void free_graphs(fhg_ctx* ctx)
 void free_all(fhg_ctx* ctx)
 {
     free_graphs(ctx);
-    ctx->nbr_d = nullptr; ctx->tfeat_d = nullptr; ctx->lw = nullptr;
+    ctx->nbr_d = nullptr; ctx->tfeat_d = nullptr; ctx->lw = nullptr; ctx->lstatus = nullptr;
     ctx->lparams = nullptr; ctx->lwts = nullptr; ctx->lbias = nullptr;
     ctx->learned_mode = FHG_LEARNED_OFF;
     ctx->learned_now = false;
@@ -1004,6 +1008,18 @@ void free_all(fhg_ctx* ctx)
     ctx->allocations.clear();
     if (ctx->nr_host) { cudaFreeHost(ctx->nr_host); ctx->nr_host = nullptr; }
     ctx->ready = false;
+}
+
+// A learned-step kernel whose bounded wait on the tensor cores expired leaves 1 in lstatus.
+int check_learned_status(fhg_ctx* ctx)
+{
+    if (!ctx->lstatus) return FHG_OK;
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, ctx->lstatus, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (st == 0) return FHG_OK;
+    CK(cudaMemsetAsync(ctx->lstatus, 0, sizeof(int), ctx->stream));
+    return fail(ctx, FHG_ERR_CUDA, "learned step: a wait on the tensor-core pipeline expired");
 }
 
 int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
@@ -1048,48 +1064,67 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
     std::vector<double> hist(maxit + 1, 0.0);
     hist[0] = 1.0;
     double nr = 1.0;
-    int it = 0, learned_its = 0;
+    int it = 0, learned_its = 0, replacements = 0;
     int status = FHG_OK;
-    while (!(it > 0 && (it >= maxit || nr < ctx->opts.tolerance))) {
-        const int p = it & 1;
-        if (ctx->opts.use_graphs) {
-            const int g = ctx->opts.krylov == FHG_KRYLOV_CG ? 0 : p;
-            CK(cudaGraphLaunch(learned ? ctx->graph_l[g] : ctx->graph[g], s));
-            fhg::g_kernel_launches += learned ? ctx->graph_l_kernels[g] : ctx->graph_kernels[g];
-        } else if (ctx->opts.krylov == FHG_KRYLOV_CG) {
-            cg_iteration(ctx);
-        } else {
-            ctx->learned_now = learned;
-            fcg_iteration(ctx, p);
-            ctx->learned_now = false;
-        }
-        CK(cudaStreamSynchronize(s));
-        nr = *ctx->nr_host;
-        it++;
-        hist[it] = nr;
-        if (learned) learned_its++;
-        if (std::isinf(nr)) { status = fail(ctx, FHG_ERR_DIVERGED, "divergence of the solver"); break; }
-        if (std::isnan(nr)) { status = fail(ctx, FHG_ERR_NAN, "the residual is NaN."); break; }
-        // Fallback rule: from the third iteration on, when the mean reduction of the last two
-        // iterations falls behind the plain method's calibrated per-iteration reduction by more
-        // than half of it in logarithmic terms (rho > rho_plain^(1/2): the margin absorbs how much
-        // the early iterations of one right-hand side differ from the calibration's), the
-        // remaining iterations use the plain V-cycle.
-        if (learned && ctx->learned_mode == FHG_LEARNED_FALLBACK && it >= 3 && ctx->rho_plain > 0.0) {
-            const double rho = std::sqrt(hist[it] / hist[it - 2]);
-            if (!(rho <= std::sqrt(ctx->rho_plain))) learned = false;
-        }
-    }
-    // The FP64 true residual ||b - A x|| / ||b|| judges the solve (A the full level-0 operator).
     double true_rel = -1.0;
-    if (status == FHG_OK) {
-        fhg::launch_spmv<double>(L0.A.v, fhg::kSpmvResidual, ctx->kx, ctx->kb, ctx->kz[0], s);
-        fhg::launch_dot(n, ctx->kz[0], ctx->kz[0], part(ctx, 0), s);
+    const bool fp32 = ctx->opts.vcycle_precision == FHG_PREC_FP32;
+    while (true) {
+        while (!(it > 0 && (it >= maxit || nr < ctx->opts.tolerance))) {
+            const int p = it & 1;
+            if (ctx->opts.use_graphs) {
+                const int g = ctx->opts.krylov == FHG_KRYLOV_CG ? 0 : p;
+                CK(cudaGraphLaunch(learned ? ctx->graph_l[g] : ctx->graph[g], s));
+                fhg::g_kernel_launches += learned ? ctx->graph_l_kernels[g] : ctx->graph_kernels[g];
+            } else if (ctx->opts.krylov == FHG_KRYLOV_CG) {
+                cg_iteration(ctx);
+            } else {
+                ctx->learned_now = learned;
+                fcg_iteration(ctx, p);
+                ctx->learned_now = false;
+            }
+            CK(cudaStreamSynchronize(s));
+            nr = *ctx->nr_host;
+            it++;
+            hist[it] = nr;
+            if (learned) learned_its++;
+            if (std::isinf(nr)) { status = fail(ctx, FHG_ERR_DIVERGED, "divergence of the solver"); break; }
+            if (std::isnan(nr)) { status = fail(ctx, FHG_ERR_NAN, "the residual is NaN."); break; }
+            // Fallback rule: from the third iteration on, when the mean reduction of the last two
+            // iterations falls behind the plain method's calibrated per-iteration reduction by more
+            // than half of it in logarithmic terms (rho > rho_plain^(1/2): the margin absorbs how
+            // much the early iterations of one right-hand side differ from the calibration's), the
+            // remaining iterations use the plain V-cycle.
+            if (learned && ctx->learned_mode == FHG_LEARNED_FALLBACK && it >= 3 && ctx->rho_plain > 0.0) {
+                const double rho = std::sqrt(hist[it] / hist[it - 2]);
+                if (!(rho <= std::sqrt(ctx->rho_plain))) learned = false;
+            }
+        }
+        if (learned_its > 0 && status == FHG_OK) status = check_learned_status(ctx);
+        if (status != FHG_OK) break;
+        // The FP64 true residual ||b - A x|| / ||b|| judges the solve (A the full level-0 operator).
+        fhg::launch_spmv<double>(L0.A.v, fhg::kSpmvResidual, ctx->kx, ctx->kb, ctx->kt, s);
+        fhg::launch_dot(n, ctx->kt, ctx->kt, part(ctx, 0), s);
         fhg::launch_sqrt_sum(part(ctx, 0), ctx->scal + 5, s);
         double h[6];
         CK(cudaMemcpyAsync(h, ctx->scal, sizeof(h), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         true_rel = h[0] > 0 ? h[5] / h[0] : h[5];
+        // FP32 V-cycle: the recursive residual of the outer iteration can drift from the true one
+        // (the double-FP32 outer product loses digits to cancellation at high coefficient
+        // contrast). Residual replacement: r = b - A x in FP64 and the iteration continues (the
+        // direction recurrence is kept) until the true residual meets the tolerance. The FP64
+        // mode keeps the reference's loop unchanged.
+        if (fp32 && ctx->opts.krylov == FHG_KRYLOV_FCG && it < maxit && !(true_rel < ctx->opts.tolerance) &&
+            replacements < 8) {
+            replacements++;
+            CK(cudaMemcpyAsync(ctx->kr, ctx->kt, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+            CK(cudaMemcpyAsync(ctx->scal + 2, &true_rel, sizeof(double), cudaMemcpyHostToDevice, s));
+            fhg::launch_convert<double, float>(n, ctx->kr, L0.b32, s);
+            CK(cudaStreamSynchronize(s));
+            nr = true_rel;
+            continue;
+        }
+        break;
     }
     if (history)
         for (int k = 0; k <= maxit; k++) history[k] = k <= it ? hist[k] : 0.0;
@@ -1389,6 +1424,8 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
             learned_neighbours(Ap, nbr);
             if ((rc = upload(ctx, &ctx->nbr_d, nbr.data(), nbr.size()))) return rc;
             if ((rc = dalloc(ctx, &ctx->lw, L.n))) return rc;
+            if ((rc = dalloc(ctx, &ctx->lstatus, 1))) return rc;
+            CK(cudaMemset(ctx->lstatus, 0, sizeof(int)));
             if ((rc = dalloc(ctx, &ctx->tfeat_d, (size_t)L.nb * fhg::learned::kTensorSlots))) return rc;
             if ((rc = upload_tensor_features(ctx))) return rc;
         }
@@ -1423,7 +1460,7 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
     }
     const long long n0 = ctx->levels[0].n;
     if ((rc = dalloc(ctx, &ctx->kx, n0)) || (rc = dalloc(ctx, &ctx->kr, n0)) || (rc = dalloc(ctx, &ctx->kb, n0)) ||
-        (rc = dalloc(ctx, &ctx->kz[0], n0)) || (rc = dalloc(ctx, &ctx->kz[1], n0)) ||
+        (rc = dalloc(ctx, &ctx->kz[0], n0)) || (rc = dalloc(ctx, &ctx->kz[1], n0)) || (rc = dalloc(ctx, &ctx->kt, n0)) ||
         (rc = dalloc(ctx, &ctx->kAd[0], n0)) || (rc = dalloc(ctx, &ctx->kAd[1], n0)) ||
         (rc = dalloc(ctx, &ctx->partials, (size_t)8 * fhg::kReduceCtas)) || (rc = dalloc(ctx, &ctx->scal, 8)) ||
         (rc = dalloc(ctx, &ctx->hist_d, (size_t)o.max_iterations + 2)) || (rc = dalloc(ctx, &ctx->counter_d, 1)) ||
@@ -1642,6 +1679,7 @@ static int time_op_t(fhg_ctx* ctx, int level, int op, int warmup, int reps, doub
     if (rc) return rc;
     T *in = t, *aux = t + mx, *out = t + 2 * mx;
     cudaStream_t s = ctx->stream;
+    CK(cudaMemsetAsync(out, 0, sizeof(T) * mx, s));
     // Inputs: the level's last V-cycle vectors (finite, representative values), converted.
     const int la = op == FHG_OP_PROLONG_ADD ? lo : li;
     if (sizeof(T) == sizeof(double)) {
@@ -1656,6 +1694,18 @@ static int time_op_t(fhg_ctx* ctx, int level, int op, int warmup, int reps, doub
             if (level == ctx->nlevels - 1) return fail(ctx, FHG_ERR_INVALID_ARG, "no smoother on the coarsest level");
             smooth<T>(ctx, level, op == FHG_OP_GS_FORWARD ? FHG_SMOOTHER_BGS : FHG_SMOOTHER_RBGS, 1, aux, in);
             return FHG_OK;
+        }
+        if constexpr (std::is_same<T, float>::value) {
+            if (op == FHG_OP_VCYCLE || op == FHG_OP_VCYCLE_LEARNED) {
+                ctx->learned_now = op == FHG_OP_VCYCLE_LEARNED;
+                vcycle<float>(ctx, 0, aux, out);
+                ctx->learned_now = false;
+                return FHG_OK;
+            }
+            if (op == FHG_OP_LEARNED_STEP) {
+                learned_step(ctx, aux, out);
+                return FHG_OK;
+            }
         }
         return apply_device_t<T>(ctx, level, op, in, aux, out);
     };
@@ -1683,6 +1733,14 @@ int fhg_time_op(fhg_ctx* ctx, int level, int op, int precision, int warmup, int 
     if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
     if (level < 0 || level >= ctx->nlevels) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d out of range", level);
     CK(cudaSetDevice(ctx->device));
+    if (op == FHG_OP_VCYCLE_LEARNED || op == FHG_OP_LEARNED_STEP || (op == FHG_OP_VCYCLE && precision == FHG_PREC_FP32)) {
+        if (level != 0 || precision != FHG_PREC_FP32 || !ctx->levels[0].A32.vals)
+            return fail(ctx, FHG_ERR_INVALID_ARG, "op %d is timed on level 0 in FP32 (FP32 setup)", op);
+        if (op != FHG_OP_VCYCLE && !ctx->lwts) return fail(ctx, FHG_ERR_NOT_READY, "no network installed");
+        int rc = time_op_t<float>(ctx, 0, op, warmup, reps, avg_ms);
+        if (rc == FHG_OK && op != FHG_OP_VCYCLE) rc = check_learned_status(ctx);
+        return rc;
+    }
     if (op == FHG_OP_SYM_SPMV || op == FHG_OP_VCYCLE) {
         Level& L0 = ctx->levels[0];
         const bool split = op == FHG_OP_SYM_SPMV && precision == FHG_PREC_FP32;
@@ -1807,6 +1865,8 @@ int fhg_set_learned(fhg_ctx* ctx, const float* params, int n_params, int mode)
     using namespace fhg::learned;
     if (!ctx) return FHG_ERR_INVALID_ARG;
     if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
+    const int kernel = (mode & FHG_LEARNED_MMA_SYNC) ? fhg::kLearnedKernelMmaSync : fhg::kLearnedKernelTcgen05;
+    mode &= ~FHG_LEARNED_MMA_SYNC;
     if (mode < FHG_LEARNED_OFF || mode > FHG_LEARNED_ALWAYS) return fail(ctx, FHG_ERR_INVALID_ARG, "unknown mode %d", mode);
     CK(cudaSetDevice(ctx->device));
     if ((params || mode != FHG_LEARNED_OFF) && !ctx->nbr_d)
@@ -1815,6 +1875,12 @@ int fhg_set_learned(fhg_ctx* ctx, const float* params, int n_params, int mode)
     Level& L0 = ctx->levels[0];
     cudaStream_t s = ctx->stream;
     int rc;
+    if (kernel != ctx->learned_kernel) {
+        ctx->learned_kernel = kernel;
+        for (int g = 0; g < 2; g++)
+            if (ctx->graph_l[g]) { cudaGraphExecDestroy(ctx->graph_l[g]); ctx->graph_l[g] = nullptr; }
+        ctx->graphs_l_built = 0;
+    }
     if (params) {
         if (n_params != kParams) return fail(ctx, FHG_ERR_INVALID_ARG, "%d parameters given, the network has %d", n_params, kParams);
         for (int i = 0; i < kParams; i++)
@@ -1829,10 +1895,12 @@ int fhg_set_learned(fhg_ctx* ctx, const float* params, int n_params, int mode)
         // First launch outside any capture: fixes the kernel's shared-memory limit and grid. With
         // w = 0 every scale is 0 and nothing is added to x.
         CK(cudaMemsetAsync(ctx->lw, 0, sizeof(float) * L0.n, s));
-        if (fhg::launch_learned_apply(L0.nb, L0.bs, ctx->nbr_d, ctx->lw, ctx->tfeat_d, ctx->lwts, ctx->lbias, L0.x32, s))
+        if (fhg::launch_learned_apply(L0.nb, L0.bs, ctx->nbr_d, ctx->lw, ctx->tfeat_d, ctx->lwts, ctx->lbias, L0.x32,
+                                      ctx->lstatus, ctx->learned_kernel, s))
             return fail(ctx, FHG_ERR_CUDA, "the learned-step kernel cannot run on this device");
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(s));
+        if ((rc = check_learned_status(ctx))) return rc;
         for (int g = 0; g < 2; g++)
             if (ctx->graph_l[g]) { cudaGraphExecDestroy(ctx->graph_l[g]); ctx->graph_l[g] = nullptr; }
         ctx->graphs_l_built = 0;
@@ -1891,6 +1959,12 @@ int fhg_apply_internal(fhg_ctx* ctx, int level, int op, int precision, const voi
             ctx->learned_now = op == FHG_OP_VCYCLE_LEARNED;
             vcycle<float>(ctx, 0, (const float*)in, (float*)out);
             ctx->learned_now = false;
+            if (op == FHG_OP_VCYCLE_LEARNED && (rc = check_learned_status(ctx))) return rc;
+        } else if (op == FHG_OP_LEARNED_STEP) {
+            if (level != 0 || !ctx->lwts || !aux) return fail(ctx, FHG_ERR_INVALID_ARG, "learned step: level 0, installed network, aux = b");
+            if (out != in) CK(cudaMemcpyAsync(out, in, sizeof(float) * ctx->levels[0].n, cudaMemcpyDeviceToDevice, ctx->stream));
+            learned_step(ctx, (const float*)aux, (float*)out);
+            if ((rc = check_learned_status(ctx))) return rc;
         } else if (op == FHG_OP_SYM_SPMV) {
             return fail(ctx, FHG_ERR_INVALID_ARG, "the outer operator is FP64");
         } else {

@@ -127,9 +127,13 @@ void launch_block_diag(int nb, int bs, const float* dinv, long long dld, const f
 // Training features: feat (rows x 48 BF16, rows >= nb zero), scale (rows).
 void launch_features(int nb, int rows, int bs, const int* nbr, const float* w, const void* tfeat, void* feat,
                      float* scale, cudaStream_t s);
-// x += s y for every face (fused gather + 3-layer MLP). Returns non-zero if the kernel cannot run.
+// x += s y for every face (fused gather + 3-layer MLP). kernel: kLearnedKernelTcgen05 (tensor
+// memory accumulators; a bounded wait that expires sets *status = 1) or kLearnedKernelMmaSync.
+// Returns non-zero if the kernel cannot run.
+constexpr int kLearnedKernelTcgen05 = 0;
+constexpr int kLearnedKernelMmaSync = 1;
 int launch_learned_apply(int nb, int bs, const int* nbr, const float* w, const void* tfeat, const void* wts,
-                         const float* bias, float* x, cudaStream_t s);
+                         const float* bias, float* x, int* status, int kernel, cudaStream_t s);
 void launch_gemm(int kind, int M, int K, const void* A, int lda, const void* B, int ldb, float* C, float* parts,
                  int nsplit, int accumulate, cudaStream_t s);
 void launch_bias_gelu(long long rows, float* a, const float* bias, void* h, cudaStream_t s);

@@ -17,7 +17,9 @@
 // so the correction is positively homogeneous in the residual (a residual scaled by a > 0
 // gets a correction scaled by a), which keeps it meaningful across the twelve orders of
 // magnitude of a solve. gelu is the tanh form of Hendrycks & Gimpel (2016),
-// 0.5 a (1 + tanh(sqrt(2/pi) (a + 0.044715 a^3))), with the hardware tanh approximation.
+// 0.5 a (1 + tanh(sqrt(2/pi) (a + 0.044715 a^3))), evaluated in packed BF16 arithmetic with the
+// hardware bf16x2 tanh (its result is the BF16 operand of the next layer); the backward pass uses
+// the FP32 derivative of the same formula.
 //
 // Tensor cores: mma.sync.m16n8k16 BF16 x BF16 -> FP32 with ldmatrix fragment loads. The
 // inference kernel keeps a 16-face tile in registers through all three layers (the FP32
@@ -82,10 +84,25 @@ __device__ __forceinline__ float tanh_fast(float x)
 constexpr float kGeluC0 = 0.7978845608028654f;  // sqrt(2/pi)
 constexpr float kGeluC1 = 0.044715f;
 
-__device__ __forceinline__ float gelu(float a)
+// gelu of two values in packed BF16 arithmetic, the activation the network uses: the inputs
+// are rounded to BF16, then 0.5 x (1 + tanh(c0 x (1 + c1 x^2))) with bf16x2 multiplies/FMAs and
+// the bf16x2 hardware tanh (one multi-function op per two values). Returns the packed result (the
+// next layer's BF16 operand).
+__device__ __forceinline__ uint32_t gelu_bf16x2(float a0, float a1)
 {
-    const float u = kGeluC0 * fmaf(kGeluC1 * a, a * a, a);
-    return 0.5f * a * (1.0f + tanh_fast(u));
+    const __nv_bfloat162 x = __floats2bfloat162_rn(a0, a1);
+    const __nv_bfloat162 c0 = __float2bfloat162_rn(kGeluC0);
+    const __nv_bfloat162 c1 = __float2bfloat162_rn(kGeluC1);
+    const __nv_bfloat162 one = __float2bfloat162_rn(1.0f);
+    const __nv_bfloat162 half = __float2bfloat162_rn(0.5f);
+    const __nv_bfloat162 p = __hfma2(__hmul2(x, x), c1, one);
+    const __nv_bfloat162 u = __hmul2(__hmul2(x, c0), p);
+    uint32_t ui = *reinterpret_cast<const uint32_t*>(&u), ti;
+    asm("tanh.approx.bf16x2 %0, %1;" : "=r"(ti) : "r"(ui));
+    const __nv_bfloat162 t = *reinterpret_cast<const __nv_bfloat162*>(&ti);
+    const __nv_bfloat162 h = __hmul2(x, half);
+    const __nv_bfloat162 g = __hfma2(h, t, h);
+    return *reinterpret_cast<const uint32_t*>(&g);
 }
 
 __device__ __forceinline__ float gelu_grad(float a)
@@ -166,7 +183,7 @@ constexpr size_t kApplySmem =
     sizeof(float) * (kHid + kHid + kOut);
 
 template <int BS>
-__global__ void __launch_bounds__(kApplyWarps * 32, 1)
+__global__ void __launch_bounds__(kApplyWarps * 32, 2)
     k_learned_apply(int nb, const int* __restrict__ nbr, const float* __restrict__ w, const bf16* __restrict__ tfeat,
                     const bf16* __restrict__ wts, const float* __restrict__ bias, float* __restrict__ x)
 {
@@ -252,8 +269,8 @@ __global__ void __launch_bounds__(kApplyWarps * 32, 1)
             for (int half = 0; half < 2; half++) {
                 const int j = 2 * kk + half;
                 const float b0 = sB[8 * j + 2 * t], b1 = sB[8 * j + 2 * t + 1];
-                h[kk][2 * half] = pack_bf16(gelu(acc[j][0] + b0), gelu(acc[j][1] + b1));
-                h[kk][2 * half + 1] = pack_bf16(gelu(acc[j][2] + b0), gelu(acc[j][3] + b1));
+                h[kk][2 * half] = gelu_bf16x2(acc[j][0] + b0, acc[j][1] + b1);
+                h[kk][2 * half + 1] = gelu_bf16x2(acc[j][2] + b0, acc[j][3] + b1);
             }
         }
         // Layer 2: [16 x 128] x W2^T
@@ -275,8 +292,8 @@ __global__ void __launch_bounds__(kApplyWarps * 32, 1)
             for (int half = 0; half < 2; half++) {
                 const int j = 2 * kk + half;
                 const float b0 = sB[kHid + 8 * j + 2 * t], b1 = sB[kHid + 8 * j + 2 * t + 1];
-                h[kk][2 * half] = pack_bf16(gelu(acc[j][0] + b0), gelu(acc[j][1] + b1));
-                h[kk][2 * half + 1] = pack_bf16(gelu(acc[j][2] + b0), gelu(acc[j][3] + b1));
+                h[kk][2 * half] = gelu_bf16x2(acc[j][0] + b0, acc[j][1] + b1);
+                h[kk][2 * half + 1] = gelu_bf16x2(acc[j][2] + b0, acc[j][3] + b1);
             }
         }
         // Layer 3: [16 x 128] x W3^T -> 16 outputs
@@ -305,6 +322,338 @@ __global__ void __launch_bounds__(kApplyWarps * 32, 1)
         }
         __syncwarp();
     }
+}
+
+// ---------------------------------------------------------------------------
+// Fused inference on the 5th-generation tensor cores: one CTA of 256 threads per tile of 128
+// faces (persistent over tiles, two CTAs per SM). Threads 0-127 gather the residual patch of face
+// t of the tile (the next tile's patch is loaded while the current tile's layers run), threads
+// 128-255 copy its tensor features; one thread issues tcgen05.mma (BF16 x BF16 -> FP32, M = 128
+// faces, N = 128 or 16, K = 16 per instruction) with the accumulator in tensor memory (TMEM lane
+// t = face t); both warpgroups read it back with tcgen05.ld (warpgroup h: columns 64h..64h+63),
+// add the bias, apply gelu and write the BF16 A operand of the next layer. Operands live in
+// shared memory in the canonical K-major layout without swizzle: 8-row x 16-byte core matrices,
+// element (row r, k) at byte
+//   (r / 8) * SBO + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2,
+// i.e. LBO = 128 bytes between core matrices along K and SBO = (K / 8) * 128 bytes between
+// 8-row groups. Every wait on the MMA-completion mbarrier is bounded (about a second of SM
+// clocks): on expiry the kernel records the failure, frees its TMEM and returns.
+
+constexpr int kTcThreads = 256;
+constexpr int kTcRows = 128;                  // faces per tile (TMEM lanes)
+constexpr uint32_t kTmemCols = 256;           // layer accumulator (128 columns) + output (16)
+constexpr int kTcSW1 = 0;                     // W1: 128 x 48
+constexpr int kTcSW2 = kTcSW1 + kHid * kIn * 2;   // W2: 128 x 128
+constexpr int kTcSW3 = kTcSW2 + kHid * kHid * 2;  // W3: 16 x 128
+constexpr int kTcSA = kTcSW3 + kOut * kHid * 2;   // inputs: 128 x 48
+constexpr int kTcSH = kTcSA + kTcRows * kIn * 2;  // hidden activations: 128 x 128
+constexpr int kTcSBias = kTcSH + kTcRows * kHid * 2;  // b1, b2, b3 (FP32)
+constexpr int kTcSScale = kTcSBias + (2 * kHid + kOut) * 4;  // s of the tile's faces
+constexpr int kTcSMisc = kTcSScale + kTcRows * 4;  // mbarrier (8), TMEM base (4)
+constexpr size_t kTcSmem = kTcSMisc + 64 + 1024;  // + alignment slack for a 1024-byte base
+constexpr long long kTcWaitCycles = 2000000000LL;
+
+__device__ __forceinline__ uint32_t core_off(int row, int kchunk, int sbo)
+{
+    return (uint32_t)((row >> 3) * sbo + kchunk * 128 + (row & 7) * 16);
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M x N.
+__host__ __device__ constexpr uint32_t mma_idesc(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+                 :: "r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" :: "r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+// Bounded wait for the mbarrier phase with parity `parity`; false on expiry.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
+{
+    const long long t0 = clock64();
+    while (true) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}\n"
+                     : "=r"(done) : "r"(mbar), "r"(parity) : "memory");
+        if (done) return true;
+        if (clock64() - t0 > kTcWaitCycles) return false;
+    }
+}
+
+// 32 consecutive FP32 accumulator columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                   "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                   "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                 "[%16];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// Bias + gelu of 64 accumulator columns [c0, c0 + 64) of this thread's lane into its row of the
+// hidden tile.
+__device__ __forceinline__ void tc_hidden_epilogue(uint32_t taddr, int c0, const float* bias, unsigned char* sH,
+                                                   int row)
+{
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        float v[32];
+        tmem_ld32(taddr + c0 + q * 32, v);
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            uint32_t w[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int j = c0 + q * 32 + c * 8 + 2 * e;
+                w[e] = gelu_bf16x2(v[c * 8 + 2 * e] + bias[j], v[c * 8 + 2 * e + 1] + bias[j + 1]);
+            }
+            *reinterpret_cast<uint4*>(sH + core_off(row, (c0 + q * 32) / 8 + c, kHid * 16)) =
+                make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    }
+}
+
+// Neighbour blocks of face f (-1 where none; all -1 past the last face).
+__device__ __forceinline__ void load_neighbours(int f, int nb, const int* __restrict__ nbr, int (&g)[kNeighbours])
+{
+#pragma unroll
+    for (int j = 0; j < kNeighbours; j++) g[j] = f < nb ? nbr[(long long)f * kNeighbours + j] : -1;
+}
+
+// Residual patch of face f from its neighbour list: own block then the six neighbours (zero where
+// none or past the last face).
+template <int BS>
+__device__ __forceinline__ void load_patch(int f, int nb, const int (&g)[kNeighbours], const float* __restrict__ w,
+                                           float (&v)[7 * BS])
+{
+#pragma unroll
+    for (int c = 0; c < BS; c++) v[c] = f < nb ? w[(long long)f * BS + c] : 0.0f;
+#pragma unroll
+    for (int j = 0; j < kNeighbours; j++)
+#pragma unroll
+        for (int c = 0; c < BS; c++) v[(j + 1) * BS + c] = g[j] >= 0 ? w[(long long)g[j] * BS + c] : 0.0f;
+}
+
+// Scaled BF16 residual slots of a patch into a row of the canonical input tile; returns s.
+template <int BS>
+__device__ __forceinline__ float store_patch(const float (&v)[7 * BS], unsigned char* sA, int row)
+{
+    float ss = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 7 * BS; q++) ss = fmaf(v[q], v[q], ss);
+    const float s = sqrtf(ss * (1.0f / (7 * BS)));
+    const float inv = s > 0.0f ? 1.0f / s : 0.0f;
+#pragma unroll
+    for (int c = 0; c < kResidualSlots / 8; c++) {
+        uint32_t p4[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int q = c * 8 + 2 * e;
+            p4[e] = pack_bf16(q < 7 * BS ? v[q] * inv : 0.0f, q + 1 < 7 * BS ? v[q + 1] * inv : 0.0f);
+        }
+        *reinterpret_cast<uint4*>(sA + core_off(row, c, kIn * 16)) = make_uint4(p4[0], p4[1], p4[2], p4[3]);
+    }
+    return s;
+}
+
+template <int BS>
+__global__ void __launch_bounds__(kTcThreads, 2)
+    k_learned_apply_tc(int nb, const int* __restrict__ nbr, const float* __restrict__ w, const bf16* __restrict__ tfeat,
+                       const bf16* __restrict__ wts, const float* __restrict__ bias, float* __restrict__ x,
+                       int* __restrict__ status)
+{
+    extern __shared__ unsigned char smem_dyn[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smem_dyn + 1023) & ~(uintptr_t)1023);
+    float* sBias = reinterpret_cast<float*>(sm + kTcSBias);
+    float* sScale = reinterpret_cast<float*>(sm + kTcSScale);
+    uint64_t* mbar_p = reinterpret_cast<uint64_t*>(sm + kTcSMisc);
+    uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(sm + kTcSMisc + 8);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int row = tid & (kTcRows - 1);      // face of the tile / TMEM lane
+    const int half = tid >> 7;                // warpgroup: column half of the hidden epilogues
+    const uint32_t s_base = smem_u32(sm);
+    const uint32_t mbar = smem_u32(mbar_p);
+
+    // Weights into the canonical layout, biases, barrier, TMEM.
+    const bf16* gW1 = wts;
+    const bf16* gW2 = gW1 + kHid * kIn;
+    const bf16* gW3 = gW2 + kHid * kHid;
+    for (int v = tid; v < kHid * kIn / 8; v += kTcThreads) {
+        const int r = v / (kIn / 8), c = v % (kIn / 8);
+        *reinterpret_cast<uint4*>(sm + kTcSW1 + core_off(r, c, kIn * 16)) = *reinterpret_cast<const uint4*>(gW1 + r * kIn + 8 * c);
+    }
+    for (int v = tid; v < kHid * kHid / 8; v += kTcThreads) {
+        const int r = v / (kHid / 8), c = v % (kHid / 8);
+        *reinterpret_cast<uint4*>(sm + kTcSW2 + core_off(r, c, kHid * 16)) = *reinterpret_cast<const uint4*>(gW2 + r * kHid + 8 * c);
+    }
+    for (int v = tid; v < kOut * kHid / 8; v += kTcThreads) {
+        const int r = v / (kHid / 8), c = v % (kHid / 8);
+        *reinterpret_cast<uint4*>(sm + kTcSW3 + core_off(r, c, kHid * 16)) = *reinterpret_cast<const uint4*>(gW3 + r * kHid + 8 * c);
+    }
+    for (int v = tid; v < 2 * kHid + kOut; v += kTcThreads) sBias[v] = bias[v];
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n"
+                     :: "r"(smem_u32(tmem_holder)), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_holder;
+    const uint32_t t_lane = tmem + ((uint32_t)((warp & 3) * 32) << 16);   // this warp's 32 lanes, column 0
+
+    const uint32_t idesc_h = mma_idesc(kTcRows, kHid);
+    const uint32_t idesc_o = mma_idesc(kTcRows, kOut);
+    uint32_t phase = 0;
+    bool ok = true;
+    const int ntiles = (nb + kTcRows - 1) / kTcRows;
+    // Two-stage prefetch: neighbour lists two tiles ahead, patch values one tile ahead, so that
+    // no dependent load waits inside a tile.
+    float v[7 * BS];
+    int g[kNeighbours];
+    if (half == 0) {
+        load_neighbours(blockIdx.x * kTcRows + row, nb, nbr, g);
+        load_patch<BS>(blockIdx.x * kTcRows + row, nb, g, w, v);
+        load_neighbours((blockIdx.x + gridDim.x) * kTcRows + row, nb, nbr, g);
+    }
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int f = tile * kTcRows + row;
+        // 1. inputs of face f (row `row` of the tile): residual slots by warpgroup 0, tensors by 1
+        if (half == 0) {
+            sScale[row] = f < nb ? store_patch<BS>(v, sm + kTcSA, row) : 0.0f;
+        } else {
+            uint4 a = make_uint4(0, 0, 0, 0), b = a;
+            if (f < nb) {
+                const uint4* src = reinterpret_cast<const uint4*>(tfeat + (long long)f * kTensorSlots);
+                a = src[0];
+                b = src[1];
+            }
+            *reinterpret_cast<uint4*>(sm + kTcSA + core_off(row, kResidualSlots / 8, kIn * 16)) = a;
+            *reinterpret_cast<uint4*>(sm + kTcSA + core_off(row, kResidualSlots / 8 + 1, kIn * 16)) = b;
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        // 2. layer 1; meanwhile the next tile's patch is loaded
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int k = 0; k < kIn / 16; k++)
+                tc_mma(tmem, smem_desc(s_base + kTcSA + k * 256, 128, kIn * 16),
+                       smem_desc(s_base + kTcSW1 + k * 256, 128, kIn * 16), idesc_h, k > 0);
+            tc_commit(mbar);
+        }
+        if (half == 0) {
+            load_patch<BS>((tile + gridDim.x) * kTcRows + row, nb, g, w, v);
+            load_neighbours((tile + 2 * gridDim.x) * kTcRows + row, nb, nbr, g);
+        }
+        // every thread leaves together if any wait expired
+        ok = __syncthreads_and(mbar_wait(mbar, phase) ? 1 : 0) != 0;
+        phase ^= 1;
+        if (!ok) break;
+        tc_fence_after();
+        tc_hidden_epilogue(t_lane, 64 * half, sBias, sm + kTcSH, row);
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        // 3. layer 2
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int k = 0; k < kHid / 16; k++)
+                tc_mma(tmem, smem_desc(s_base + kTcSH + k * 256, 128, kHid * 16),
+                       smem_desc(s_base + kTcSW2 + k * 256, 128, kHid * 16), idesc_h, k > 0);
+            tc_commit(mbar);
+        }
+        ok = __syncthreads_and(mbar_wait(mbar, phase) ? 1 : 0) != 0;
+        phase ^= 1;
+        if (!ok) break;
+        tc_fence_after();
+        tc_hidden_epilogue(t_lane, 64 * half, sBias + kHid, sm + kTcSH, row);
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        // 4. layer 3 into columns [128, 144)
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int k = 0; k < kHid / 16; k++)
+                tc_mma(tmem + kHid, smem_desc(s_base + kTcSH + k * 256, 128, kHid * 16),
+                       smem_desc(s_base + kTcSW3 + k * 256, 128, kHid * 16), idesc_o, k > 0);
+            tc_commit(mbar);
+        }
+        ok = __syncthreads_and(mbar_wait(mbar, phase) ? 1 : 0) != 0;
+        phase ^= 1;
+        if (!ok) break;
+        tc_fence_after();
+        if (half == 0) {
+            float y[16];
+            tmem_ld16(t_lane + kHid, y);
+            if (f < nb) {
+                const float s = sScale[row];
+#pragma unroll
+                for (int c = 0; c < BS; c++) {
+                    const float cv = s * (y[c] + sBias[2 * kHid + c]);
+                    if (isfinite(cv)) x[(long long)f * BS + c] += cv;
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+    }
+    if (!ok && tid == 0 && status) atomicExch(status, 1);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" :: "r"(tmem), "r"(kTmemCols) : "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -401,14 +750,16 @@ __global__ void k_sum_splits(int nsplit, long long count, const float* __restric
     out[i] = accumulate ? out[i] + v : v;
 }
 
-// a += bias (per column, 128 columns); h = bf16(gelu(a)). a keeps the pre-activation.
+// a += bias (per column, 128 columns); h = gelu(a) as the inference kernels compute it (pairs
+// of columns in bf16x2). a keeps the pre-activation.
 __global__ void k_bias_gelu(long long rows, float* __restrict__ a, const float* __restrict__ bias, bf16* __restrict__ h)
 {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long i = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
     if (i >= rows * kHid) return;
-    const float v = a[i] + bias[i % kHid];
-    a[i] = v;
-    h[i] = __float2bfloat16_rn(gelu(v));
+    const float v0 = a[i] + bias[i % kHid], v1 = a[i + 1] + bias[(i + 1) % kHid];
+    a[i] = v0;
+    a[i + 1] = v1;
+    *reinterpret_cast<uint32_t*>(h + i) = gelu_bf16x2(v0, v1);
 }
 
 // delta = bf16(dh * gelu'(a)).
@@ -561,30 +912,53 @@ void launch_features(int nb, int rows, int bs, const int* nbr, const float* w, c
 }
 
 int launch_learned_apply(int nb, int bs, const int* nbr, const float* w, const void* tfeat, const void* wts,
-                         const float* bias, float* x, cudaStream_t s)
+                         const float* bias, float* x, int* status, int kernel, cudaStream_t s)
 {
-    // Persistent grid: as many CTAs as fit on the device at once (computed once per block size
-    // and device; the shared-memory attribute is set with it).
-    static int grid_of[kMaxLearnedBs + 1][16] = {};
+    // Persistent grids: as many CTAs as fit on the device at once, computed once per kernel, block
+    // size and device (the shared-memory attribute is set with it).
+    static int grid_of[2][kMaxLearnedBs + 1][16] = {};
     int dev = 0;
     if (!learned_supports(bs) || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) return -1;
-    if (grid_of[bs][dev] == 0) {
+    const int kk = kernel == kLearnedKernelMmaSync ? 1 : 0;
+    if (grid_of[kk][bs][dev] == 0) {
+        // Two CTAs per SM for both kernels: tcgen05 by its TMEM columns (2 x 256 of 512), shared
+        // memory (2 x 97 KB) and registers (<= 128 per thread); mma.sync by its registers
+        // (<= 128 per thread) and shared memory (2 x 70 KB). The shared-memory limit and carveout
+        // are set once here.
         cudaError_t e = cudaErrorInvalidValue;
-        int per_sm = 0, sms = 0;
-        FHG_LEARNED_BS(bs, {
-            e = cudaFuncSetAttribute(k_learned_apply<BS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kApplySmem);
-            if (e == cudaSuccess)
-                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_learned_apply<BS>, kApplyWarps * 32, kApplySmem);
-        });
+        int sms = 0;
+        if (kk == 1) {
+            FHG_LEARNED_BS(bs, {
+                e = cudaFuncSetAttribute(k_learned_apply<BS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kApplySmem);
+                if (e == cudaSuccess)
+                    e = cudaFuncSetAttribute(k_learned_apply<BS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             (int)cudaSharedmemCarveoutMaxShared);
+            });
+        } else {
+            FHG_LEARNED_BS(bs, {
+                e = cudaFuncSetAttribute(k_learned_apply_tc<BS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+                if (e == cudaSuccess)
+                    e = cudaFuncSetAttribute(k_learned_apply_tc<BS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             (int)cudaSharedmemCarveoutMaxShared);
+            });
+        }
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess || per_sm < 1) return -1;
-        grid_of[bs][dev] = per_sm * sms;
+        if (e != cudaSuccess || sms < 1) return -1;
+        grid_of[kk][bs][dev] = 2 * sms;
     }
-    const int tiles = (nb + 15) / 16;
-    const int grid = std::min(grid_of[bs][dev], (tiles + kApplyWarps - 1) / kApplyWarps);
-    if (grid < 1) return 0;
-    FHG_LEARNED_BS(bs, k_learned_apply<BS><<<grid, kApplyWarps * 32, kApplySmem, s>>>(
-                           nb, nbr, w, (const bf16*)tfeat, (const bf16*)wts, bias, x));
+    if (kk == 1) {
+        const int tiles = (nb + 15) / 16;
+        const int grid = std::min(grid_of[kk][bs][dev], (tiles + kApplyWarps - 1) / kApplyWarps);
+        if (grid < 1) return 0;
+        FHG_LEARNED_BS(bs, k_learned_apply<BS><<<grid, kApplyWarps * 32, kApplySmem, s>>>(
+                               nb, nbr, w, (const bf16*)tfeat, (const bf16*)wts, bias, x));
+    } else {
+        const int tiles = (nb + kTcRows - 1) / kTcRows;
+        const int grid = std::min(grid_of[kk][bs][dev], tiles);
+        if (grid < 1) return 0;
+        FHG_LEARNED_BS(bs, k_learned_apply_tc<BS><<<grid, kTcThreads, kTcSmem, s>>>(
+                               nb, nbr, w, (const bf16*)tfeat, (const bf16*)wts, bias, x, status));
+    }
     g_kernel_launches++;
     return 0;
 }
@@ -621,7 +995,7 @@ void launch_gemm(int kind, int M, int K, const void* A, int lda, const void* B, 
 
 void launch_bias_gelu(long long rows, float* a, const float* bias, void* h, cudaStream_t s)
 {
-    const long long n = rows * kHid;
+    const long long n = rows * kHid / 2;
     k_bias_gelu<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(rows, a, bias, (bf16*)h);
     g_kernel_launches++;
 }

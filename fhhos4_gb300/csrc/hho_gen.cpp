@@ -637,12 +637,23 @@ struct ElementOps {
 
 struct Params {
     int dim, k;
-    int source;  // 0: d pi^2 prod sin(pi x_i); 1: 1
+    int source;  // 0: d pi^2 prod sin(pi x_i); 1: 1; 2: four random sine modes
+    double amp[4] = {0, 0, 0, 0};   // source 2: f = sum_i amp_i prod_d sin(pi m_id x_d)
+    int mode[4][3] = {};
 };
 
 double source_value(const Params& p, const std::array<double, 3>& x)
 {
     if (p.source == 1) return 1.0;
+    if (p.source == 2) {
+        double f = 0.0;
+        for (int i = 0; i < 4; i++) {
+            double t = p.amp[i];
+            for (int d = 0; d < p.dim; d++) t *= std::sin(kPi * p.mode[i][d] * x[d]);
+            f += t;
+        }
+        return f;
+    }
     if (p.dim == 2) return 2 * kPi * kPi * std::sin(kPi * x[0]) * std::sin(kPi * x[1]);
     return 3 * kPi * kPi * std::sin(kPi * x[0]) * std::sin(kPi * x[1]) * std::sin(kPi * x[2]);
 }
@@ -1211,7 +1222,16 @@ int fhg_hho_create(fhg_hho** out, const fhg_hho_params* p)
         return -1;
     }
     const int threads = p->threads > 0 ? p->threads : (int)std::max(1u, std::thread::hardware_concurrency());
-    Params prm{p->dim, p->k, p->source == FHG_HHO_SOURCE_ONE ? 1 : 0};
+    Params prm{p->dim, p->k, p->source == FHG_HHO_SOURCE_ONE ? 1 : p->source == FHG_HHO_SOURCE_RANDOM_MODES ? 2 : 0};
+    if (prm.source == 2) {
+        // Modes m_id uniform in {1..4}, amplitudes N(0, 1) (Box-Muller), from the seed.
+        uint64_t st = p->seed * 0x9E3779B97F4A7C15ull + 0x5EED;
+        for (int i = 0; i < 4; i++) {
+            for (int d = 0; d < 3; d++) prm.mode[i][d] = 1 + (int)(splitmix64(st) % 4);
+            const double u1 = std::max(uniform01(st), 1e-300), u2 = uniform01(st);
+            prm.amp[i] = std::sqrt(-2.0 * std::log(u1)) * std::cos(2 * kPi * u2);
+        }
+    }
     Rules rules;
     H->prm = prm;
     H->threads = threads;

@@ -9,6 +9,8 @@ extern "C" {
 
 #define FHG_HHO_SOURCE_SINE 0      /* f = d pi^2 prod sin(pi x_i), u = prod sin(pi x_i) */
 #define FHG_HHO_SOURCE_ONE 1       /* f = 1 */
+#define FHG_HHO_SOURCE_RANDOM_MODES 2 /* f = sum of 4 modes a_i prod_d sin(pi m_id x_d), m_id uniform in
+                                        {1..4}, a_i ~ N(0, 1), from the seed */
 #define FHG_HHO_IDENTITY 0         /* K = I */
 #define FHG_HHO_CHECKERBOARD 1     /* isotropic, m^d checkerboard alternating 1 and `contrast` */
 #define FHG_HHO_ANISOTROPIC 2      /* per m^d block: R diag(1,..,1,eps) R^T, eps log-uniform in

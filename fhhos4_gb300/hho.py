@@ -14,7 +14,7 @@ import scipy.sparse as sp
 
 from .build import HHO_LIB
 
-SOURCE = {"sine": 0, "one": 1}
+SOURCE = {"sine": 0, "one": 1, "modes": 2}
 COEFFICIENT = {"identity": 0, "checkerboard": 1, "anisotropic": 2, "lognormal_patches": 3}
 
 

@@ -59,6 +59,9 @@ extern "C" {
 #define FHG_LEARNED_OFF 0
 #define FHG_LEARNED_FALLBACK 1
 #define FHG_LEARNED_ALWAYS 2
+#define FHG_LEARNED_MMA_SYNC 16  /* or-ed into the mode: run the step with mma.sync tiles instead of
+                                    tcgen05 tensor-memory accumulators (the two give the same result
+                                    up to FP32 summation order) */
 #define FHG_LEARNED_PARAMS 24848  /* FP32 parameters: W1 128x48, b1 128, W2 128x128, b2 128, W3 16x128, b3 16 */
 
 typedef struct fhg_ctx fhg_ctx;
@@ -142,7 +145,9 @@ int fhg_solve_device(fhg_ctx* ctx, const double* b_dev, double* x_dev, double* h
 #define FHG_OP_SYM_SPMV 7     /* out = A.selfadjointView<Lower>() in (FlexibleConjugateGradient.h:124), level 0 */
 #define FHG_OP_COARSE_SOLVE 8 /* out = A_coarsest^{-1} in          (Multigrid.h:445-452)            */
 #define FHG_OP_VCYCLE 9       /* out = one V-cycle from zero on rhs in (Preconditioner.h:162-167), level 0 */
-#define FHG_OP_VCYCLE_LEARNED 10 /* same with the learned correction (FP32, fhg_apply_internal only) */
+#define FHG_OP_VCYCLE_LEARNED 10 /* same with the learned correction (FP32; fhg_apply_internal, fhg_time_op) */
+#define FHG_OP_LEARNED_STEP 11 /* out = in + learned correction of the residual aux - A in (FP32, level 0;
+                                  fhg_apply_internal, fhg_time_op) */
 int fhg_apply(fhg_ctx* ctx, int level, int op, const double* in, const double* aux, double* out);
 
 /* Device timing of one operator (same ops; vectors left in device memory) in FHG_PREC_FP64 or

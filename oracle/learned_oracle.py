@@ -7,7 +7,9 @@ gradients can be checked. It is imported by tests only; the product path never c
 Parity is therefore unpinned against the reference; the pins are
   * central finite differences of the exact FP64 loss (``exact=True``), and
   * the GPU's own rounding points mirrored here (``exact=False``): BF16 inputs, weights,
-    activations and backpropagated signals, FP64 accumulation in place of FP32.
+    activations (gelu in bf16 arithmetic, ``gelu_bf16``) and backpropagated signals, FP64
+    accumulation in place of FP32; the backward pass uses the derivative of the exact gelu, as
+    the GPU does.
 
 Network (per face i; s_i, tensors and neighbour order as the GPU builds them):
     u = [w_i, w_j1..w_j6 (7 bs, zero padded to 32) / s_i, T1/tau, T2/tau, 0 0 0 0]   (48)
@@ -47,6 +49,20 @@ def bf16_bits_to_float(bits) -> np.ndarray:
 
 def gelu(a):
     return 0.5 * a * (1.0 + np.tanh(GELU_C0 * (a + GELU_C1 * a ** 3)))
+
+
+def gelu_bf16(a):
+    """The activation as the GPU evaluates it: bf16 inputs, bf16x2 arithmetic (one rounding per
+    multiply or FMA), tanh rounded to bf16 (the GPU's bf16x2 hardware tanh can differ in the last
+    bit), result bf16: 0.5 x (1 + tanh(c0 x (1 + c1 x^2)))."""
+    x = bf16(a)
+    c0, c1 = bf16(GELU_C0), bf16(GELU_C1)
+    p = bf16(x * x)
+    p = bf16(p * c1 + 1.0)
+    u = bf16(bf16(x * c0) * p)
+    t = bf16(np.tanh(u))
+    h = bf16(0.5 * x)
+    return bf16(h * t + h)
 
 
 def gelu_grad(a):
@@ -122,10 +138,11 @@ def forward(p, u, exact: bool = False):
     """Activations of every row of u: a1, h1, a2, h2, y (FP64; BF16 rounding points unless exact)."""
     W1, b1, W2, b2, W3, b3 = unpack(p)
     rnd = (lambda x: x) if exact else bf16
+    act = gelu if exact else gelu_bf16
     a1 = u @ rnd(W1).T + b1
-    h1 = rnd(gelu(a1))
+    h1 = act(a1)
     a2 = h1 @ rnd(W2).T + b2
-    h2 = rnd(gelu(a2))
+    h2 = act(a2)
     y = h2 @ rnd(W3).T + b3
     return a1, h1, a2, h2, y
 

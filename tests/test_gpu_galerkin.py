@@ -111,6 +111,11 @@ def test_high_contrast_checkerboard_converges_with_galerkin(precision):
     fcg = S.fcg_mg(As, Ps, bs, galerkin=True, precision=precision, maxit=300)
     x = fcg.Solve(b)
     assert fcg.History[-1] < 1e-8
-    assert abs(fcg.IterationCount - its_o) <= (0 if precision == "fp64" else 4)
     r = np.linalg.norm(b - As[0] @ x) / np.linalg.norm(b)
-    assert r < 1.5e-8
+    if precision == "fp64":
+        assert fcg.IterationCount == its_o
+        assert r < 1.5e-8
+    else:
+        # FP32 V-cycle: residual replacement makes the FP64 true residual meet the tolerance
+        assert fcg.IterationCount <= its_o + 40
+        assert r < 1e-8 * (1 + 1e-6)

@@ -106,13 +106,15 @@ def test_gradient_matches_oracle():
         u, s = _gpu_features(f, r)
         _, A32, _ = _permuted_operator(f)
         loss_o, grad_o = LO.loss_and_grad(p, u, s, A32, r.cpu().numpy(), E, f.bs, exact=False)
-        assert abs(loss_g - loss_o) <= 1e-3 * abs(loss_o) + 1e-6
+        # tolerances: FP32 vs FP64 accumulation, and the hardware bf16x2 tanh of the activation,
+        # which is an approximation (the oracle rounds the exact tanh to bf16)
+        assert abs(loss_g - loss_o) <= 5e-3 * abs(loss_o) + 1e-6
         blocks = {"W1": (LN.OFF_W1, LN.OFF_B1), "b1": (LN.OFF_B1, LN.OFF_W2), "W2": (LN.OFF_W2, LN.OFF_B2),
                   "b2": (LN.OFF_B2, LN.OFF_W3), "W3": (LN.OFF_W3, LN.OFF_B3), "b3": (LN.OFF_B3, LN.N_PARAMS)}
         for name, (a, b) in blocks.items():
             go, gg = grad_o[a:b], grad_g[a:b].astype(np.float64)
             rel = np.linalg.norm(gg - go) / max(np.linalg.norm(go), 1e-30)
-            assert rel < 2e-2, (name, rel)
+            assert rel < 3e-2, (name, rel)
         # the unused output rows (>= bs) get no gradient
         W3g = grad_g[LN.OFF_W3:LN.OFF_B3].reshape(16, 128)
         assert np.all(W3g[f.bs:] == 0)
@@ -123,14 +125,16 @@ def test_gradient_matches_oracle():
         f.close()
 
 
-def test_fused_inference_matches_oracle():
+@pytest.mark.parametrize("kernel", ["tcgen05", "mma_sync"])
+def test_fused_inference_matches_oracle(kernel):
     """The V-cycle with the learned step minus the plain V-cycle is exactly the correction of the
-    fused kernel; compare it with the oracle's forward pass on the same inputs."""
+    fused kernel (tensor-memory tcgen05 tiles or mma.sync tiles); compare it with the oracle's
+    forward pass on the same inputs."""
     _need_gpu()
     f = _field(n=8, coefficient="anisotropic")
     try:
         p = _params_all_active(7)
-        f.ctx.set_learned(p, "always")
+        f.ctx.set_learned(p, "always", kernel=kernel)
         (r, E, e), = LN.make_samples(f, 1, cycles=(1,), seed=13)
         z0 = torch.empty_like(r)
         z1 = torch.empty_like(r)
@@ -143,7 +147,28 @@ def test_fused_inference_matches_oracle():
         u, s = _gpu_features(f, r1)
         c_or = LO.correction(p, u, s, f.bs)
         rel = np.linalg.norm(c_gpu - c_or) / np.linalg.norm(c_or)
-        assert rel < 2e-3, rel
+        assert rel < 1.5e-2, rel   # the hardware bf16x2 tanh vs the oracle's rounded exact tanh
+    finally:
+        f.close()
+
+
+def test_tcgen05_and_mma_sync_kernels_agree_at_scale():
+    """Both inference kernels on a 32^3 field (387,072 faces, every tile of both grids used)."""
+    _need_gpu()
+    f = _field(n=32, seed=21, coefficient="anisotropic")
+    try:
+        p = _params_all_active(9)
+        (r, E, e), = LN.make_samples(f, 1, cycles=(1,), seed=14)
+        z0 = torch.empty_like(r)
+        f.vcycle(r, z0, learned=False)
+        out = {}
+        for kernel in ("tcgen05", "mma_sync"):
+            f.ctx.set_learned(p, "always", kernel=kernel)
+            z = torch.empty_like(r)
+            f.vcycle(r, z, learned=True)
+            out[kernel] = (z - z0).double()
+        a, b = out["tcgen05"], out["mma_sync"]
+        assert float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b)) < 2e-3
     finally:
         f.close()
 
@@ -200,7 +225,7 @@ def test_learned_solve_reaches_fp64_tolerance():
             # the FP64 true residual judges the solve
             r_true = np.linalg.norm(f.b - f.As[0] @ x) / np.linalg.norm(f.b)
             assert info.true_relative_residual == pytest.approx(r_true, rel=1e-6)
-            assert r_true < 1.5e-8
+            assert r_true < 1e-8 * (1 + 1e-6)
             assert 0 < info.learned_iterations <= info.iterations
             if mode == "always":
                 assert info.learned_iterations == info.iterations
