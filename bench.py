@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--max-coarse-rows", type=int, default=1000)
     ap.add_argument("--fast-smoothers", default="bgs,rbgs", help="pre,post smoothers of the fast (FP32) method")
     ap.add_argument("--fast-nu", default="2,2", help="pre,post smoothing steps of the fast (FP32) method")
+    ap.add_argument("--weights", default="", help="learned-step network (default: the committed one)")
+    ap.add_argument("--no-learned", action="store_true", help="report the FP32 method as the headline")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="also run the batched workload: this many 2D problems in one graph launch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-iterations", type=int, default=2)
     return ap.parse_args()
@@ -251,6 +255,7 @@ def run_ours(args, dist: Dist):
         ctx.set_level(l, bs, A)
     for l, P in enumerate(Ps):
         ctx.set_prolongation(l, P)
+    ctx.set_face_tensors(H.face_tensors(0))
     o = N.default_options()
     o.vcycle_precision = N.PRECISION["fp32"]   # keeps FP64 and FP32 copies
     o.autotune = 1
@@ -274,19 +279,30 @@ def run_ours(args, dist: Dist):
         r = ctx.apply(0, N.OP_RESIDUAL, x, b, n0)
         return float(np.linalg.norm(r) / np.linalg.norm(b))
 
-    # Three methods on the same hierarchy and context:
+    # Four methods on the same hierarchy and context:
     #   plain     FP64 V-cycle, V(1,1) bgs/rbgs: the reference's method (its iteration count);
     #   fp64_fast FP64 V-cycle with the fast method's cycle (isolates the precision gain);
-    #   fast      FP32 V-cycle inside FP64 FCG with the fast cycle: the headline `value`.
-    methods = {"plain": ("fp64", "bgs", "rbgs", 1, 1), "fp64_fast": ("fp64", fast_pre, fast_post, fast_npre, fast_npost),
-               "fast": ("fp32", fast_pre, fast_post, fast_npre, fast_npost)}
+    #   fast      FP32 V-cycle inside FP64 FCG with the fast cycle;
+    #   learned   the same with the learned correction in the V-cycle (fallback rule on): the
+    #             headline `value` (the metric's "learned+FP32 MG-FCG").
+    from fhhos4_gb300 import learned as LN
+    params, wmeta = LN.load_params(args.weights or LN.DEFAULT_WEIGHTS)
+    methods = {"plain": ("fp64", "bgs", "rbgs", 1, 1, False),
+               "fp64_fast": ("fp64", fast_pre, fast_post, fast_npre, fast_npost, False),
+               "fast": ("fp32", fast_pre, fast_post, fast_npre, fast_npost, False),
+               "learned": ("fp32", fast_pre, fast_post, fast_npre, fast_npost, True)}
     results = {}
     launches = {}
     clocks = {}
     solutions = {}
-    for name, (prec, pre, post, npre, npost) in methods.items():
+    learned_its = {}
+    for name, (prec, pre, post, npre, npost, use_learned) in methods.items():
         ctx.set_cycle(pre, post, npre, npost, 1)
         ctx.set_vcycle_precision(prec)
+        if use_learned:
+            ctx.set_learned(params, "fallback")
+        else:
+            ctx.set_learned(None, "off")
         for _ in range(args.warmup):
             solve_device()
         dist.barrier()
@@ -307,6 +323,10 @@ def run_ours(args, dist: Dist):
         solutions[name] = x_dev.cpu().numpy()
         results[name] = dict(s=t_step, iterations=iters[-1], true_rel_residual=true_residual(), final=float(hist[-1]),
                              cycle=f"V({npre},{npost}) {pre}/{post}", vcycle_precision=prec)
+        if use_learned:
+            results[name]["learned_iterations"] = info.learned_iterations
+            results[name]["fallback_reference_rate"] = ctx.learned_reference_rate()
+            results[name]["network"] = wmeta
     x64 = solutions["plain"]
     for name in methods:
         results[name]["rel_diff_vs_plain_fp64"] = float(np.linalg.norm(solutions[name] - x64) / np.linalg.norm(x64))
@@ -315,9 +335,14 @@ def run_ours(args, dist: Dist):
     if H is not None:
         H.close()
 
-    # End to end through the public C ABI with pinned host buffers (H2D b, solve, D2H x).
+    head = "fast" if args.no_learned else "learned"
+    # End to end through the public C ABI with pinned host buffers (H2D b, solve, D2H x), headline method.
     ctx.set_cycle(fast_pre, fast_post, fast_npre, fast_npost, 1)
     ctx.set_vcycle_precision("fp32")
+    if head == "learned":
+        ctx.set_learned(params, "fallback")
+    else:
+        ctx.set_learned(None, "off")
     b_host = torch.from_numpy(b).pin_memory()
     x_host = torch.empty_like(b_host).pin_memory()
     lib = N.load()
@@ -364,7 +389,16 @@ def run_ours(args, dist: Dist):
             add_kernel(f"bsr_restrict_{prec}", N.OP_RESTRICT, prec, bytes_spmv(pb, n1 // bs, n0, n1, bs, p))
             add_kernel(f"bsr_prolong_add_{prec}", N.OP_PROLONG_ADD, prec,
                        bytes_spmv(pb, nb0, n1, n0, bs, p, add=True))
-    # Dominant kernel of the headline (FP32 V-cycle) solve: two GS sweeps per iteration on level 0.
+    # The learned step (FP32 residual, block-diagonal scaling, 48-128-128-16 MLP on the tensor
+    # cores) and its MLP work: 2 (48 x 128 + 128 x 128 + 128 x 16) FLOP per face.
+    ctx.set_learned(params, "always")
+    for kname in ("tcgen05", "mma_sync"):
+        ctx.set_learned(params, "always", kernel=kname)
+        ms = ctx.time_op(0, N.OP_LEARNED_STEP, "fp32", warmup=3, reps=20)
+        flops = 2.0 * (48 * 128 + 128 * 128 + 128 * 16) * nb0
+        kernels[f"learned_step_{kname}"] = {"ms": ms, "bytes": 0, "gbs": 0.0, "tflops_mlp": flops / (ms * 1e-3) / 1e12}
+    ctx.set_learned(params, "fallback")
+    # Dominant kernel of the headline (FP32 V-cycle) solve: GS sweeps on level 0.
     ncol = info0["colours"]
     dom = "bsr_gs_sweep_fp32"
     hbm, hbm_kind = measured_hbm_peak()
@@ -389,8 +423,8 @@ def run_ours(args, dist: Dist):
                           f"(natural block-GS order, OpenMP row-parallel products), {per_it:.3f} s/iteration "
                           f"x {its} reference iterations; setup {cpu_setup:.1f} s excluded")}
 
-    clk = clocks["fast"]
-    value = results["fast"]["s"]
+    clk = clocks[head]
+    value = results[head]["s"]
     line = {
         "metric": METRIC,
         "value": round(value, 6),
@@ -406,28 +440,75 @@ def run_ours(args, dist: Dist):
         "data": (f"synthetic: the reference's own {args.n}^{args.dim} HHO system ({args.coefficient} coefficient), "
                  "generated on the host"),
         "config": dict(workload_config(args), parallelism=f"replicas x{dist.world}",
-                       method=f"FP32 V-cycle {results['fast']['cycle']} inside FP64 FCG(1), double-FP32 outer product",
+                       method=(("learned correction + " if head == "learned" else "") +
+                               f"FP32 V-cycle {results[head]['cycle']} inside FP64 FCG(1), double-FP32 outer product"),
                        unknowns=n0, levels=len(As), colours_level0=ncol),
         "plain_fp64": dict(results["plain"], reference_iterations_colour_order=ref_col,
                            reference_iterations_natural_order=ref_nat),
         "fp64_fast_cycle": results["fp64_fast"],
         "fast": results["fast"],
+        "learned": results["learned"],
+        "headline_method": head,
         "speedup_vs_plain_fp64": round(results["plain"]["s"] / value, 3),
         "speedup_vs_fp64_same_cycle": round(results["fp64_fast"]["s"] / value, 3),
+        "learned_vs_fast": round(results["fast"]["s"] / results["learned"]["s"], 3),
         "dofs_per_s": round(n0 * dist.world / value, 1),
         "e2e": {"value": round(e2e_s, 6), "unit": "s", "h2d_bytes_per_step": int(n0 * 8),
                 "d2h_bytes_per_step": int(n0 * 8)},
         "roofline": roofline,
-        "kernels": {k: {"ms": round(v["ms"], 4), "gbs": round(v["gbs"], 1), "frac": round(v["gbs"] / hbm, 4)}
+        "kernels": {k: ({"ms": round(v["ms"], 4), "gbs": round(v["gbs"], 1), "frac": round(v["gbs"] / hbm, 4)}
+                        if "tflops_mlp" not in v else {"ms": round(v["ms"], 4), "tflops_mlp": round(v["tflops_mlp"], 1)})
                     for k, v in kernels.items()},
-        "gpu_launches": int(launches["fast"]),
+        "gpu_launches": int(launches[head]),
         "clocks": clk,
         "setup_s": {"hierarchy_generation": round(gen_s, 2), "gpu_setup": round(setup_s, 2)},
         "cpu_baseline": cpu,
     }
+    ctx.close()
+    if args.batch > 0:
+        line["batched"] = run_batched(args, dist)
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
+
+
+def run_batched(args, dist: Dist):
+    """Many 2D problems of uneven size in one graph launch against the same problems solved one
+    after another (fhg_solve_device each)."""
+    import torch
+    from fhhos4_gb300 import batch as BT
+    specs = BT.batched_specs(args.batch)
+    t0 = time.perf_counter()
+    probs, batch, build_s = BT.build(specs, device=dist.local_rank, precision="fp32", autotune=True)
+    for _ in range(2):
+        rc, infos, ms = batch.solve()
+    times = []
+    for _ in range(max(3, args.steps // 2)):
+        rc, infos, ms = batch.solve()
+        times.append(ms)
+    batched_ms = dist.max(float(np.median(times)))
+    seq_ms = 0.0
+    for p in probs:
+        bd = torch.from_numpy(p.b).cuda()
+        xd = torch.empty_like(bd)
+        torch.cuda.synchronize()
+        p.ctx.solve_device(bd.data_ptr(), xd.data_ptr(), 200)
+        rc1, h, info = p.ctx.solve_device(bd.data_ptr(), xd.data_ptr(), 200)
+        seq_ms += info.solve_ms
+    dofs = sum(p.n for p in probs)
+    its = [i.iterations for i in infos]
+    worst_true = max(i.true_relative_residual for i in infos)
+    out = {"problems": len(probs), "unknowns": int(dofs), "n_range": [min(s.n for s in specs), max(s.n for s in specs)],
+           "k_counts": {k: sum(1 for s in specs if s.k == k) for k in (1, 2, 3)},
+           "batched_ms": round(batched_ms, 2), "sequential_ms": round(seq_ms, 2),
+           "speedup_batched_vs_sequential": round(seq_ms / batched_ms, 2),
+           "dofs_per_s": round(dofs / (batched_ms * 1e-3), 1), "iterations_min_max": [min(its), max(its)],
+           "worst_true_rel_residual": worst_true, "status": rc,
+           "method": "FP32 V(1,1) bgs/rbgs inside FP64 FCG(1), Galerkin coarse operators, autotuned launch shapes",
+           "setup_s": round(time.perf_counter() - t0, 1)}
+    batch.close()
+    for p in probs:
+        p.close()
+    return out
 
 
 def run_reference(args, dist: Dist):

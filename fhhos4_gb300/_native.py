@@ -42,7 +42,8 @@ EXPORTS = ["fhg_default_options", "fhg_create", "fhg_destroy", "fhg_last_error",
            "fhg_kernel_launches", "fhg_residual_norm_noalloc", "fhg_set_face_tensors", "fhg_set_learned",
            "fhg_learned_reference_rate", "fhg_learned_features", "fhg_apply_internal", "fhg_net_num_params",
            "fhg_net_create", "fhg_net_destroy", "fhg_net_last_error", "fhg_net_set_params", "fhg_net_get_params",
-           "fhg_net_train_step"]
+           "fhg_net_train_step", "fhg_io_buffers", "fhg_io_upload", "fhg_io_download", "fhg_batch_create", "fhg_batch_destroy", "fhg_batch_last_error",
+           "fhg_batch_add", "fhg_batch_solve"]
 
 FHG_NOALLOC_MAX_PARTIALS = 131072
 
@@ -117,6 +118,16 @@ def load(path: str = LIB):
     lib.fhg_net_get_params.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
     lib.fhg_net_train_step.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_float, C.c_float, C.c_int,
                                        P(C.c_double), C.c_void_p]
+    lib.fhg_io_buffers.argtypes = [C.c_void_p, P(C.c_void_p), P(C.c_void_p)]
+    lib.fhg_io_upload.argtypes = [C.c_void_p, C.c_void_p]
+    lib.fhg_io_download.argtypes = [C.c_void_p, C.c_void_p]
+    lib.fhg_batch_create.argtypes = [P(C.c_void_p), C.c_int]
+    lib.fhg_batch_destroy.argtypes = [C.c_void_p]
+    lib.fhg_batch_destroy.restype = None
+    lib.fhg_batch_last_error.argtypes = [C.c_void_p]
+    lib.fhg_batch_last_error.restype = C.c_char_p
+    lib.fhg_batch_add.argtypes = [C.c_void_p, C.c_void_p]
+    lib.fhg_batch_solve.argtypes = [C.c_void_p, C.c_void_p, P(C.c_double)]
     _lib = lib
     return lib
 
@@ -244,6 +255,59 @@ class Context:
         """One operator on device vectors in the context's colour numbering (see fhg_apply_internal)."""
         self._check(self.lib.fhg_apply_internal(self.h, level, op, PRECISION[precision], C.c_void_p(in_dev),
                                                 C.c_void_p(aux_dev) if aux_dev else None, C.c_void_p(out_dev)))
+
+
+    def io_buffers(self):
+        """(b_dev, x_dev): the context's device vectors read and written by a batched solve."""
+        b, x = C.c_void_p(), C.c_void_p()
+        self._check(self.lib.fhg_io_buffers(self.h, C.byref(b), C.byref(x)))
+        return b.value, x.value
+
+    def io_upload(self, b: np.ndarray):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        self._check(self.lib.fhg_io_upload(self.h, ptr(b)))
+
+    def io_download(self, n: int) -> np.ndarray:
+        x = np.empty(n)
+        self._check(self.lib.fhg_io_download(self.h, ptr(x)))
+        return x
+
+
+class Batch:
+    """Owns one fhg_batch: set-up contexts solved together by one graph launch."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        self.h = C.c_void_p()
+        self._ctxs = []
+        self._check(self.lib.fhg_batch_create(C.byref(self.h), device))
+
+    def _check(self, rc: int):
+        if rc != FHG_OK:
+            msg = self.lib.fhg_batch_last_error(self.h).decode() if self.h else "no batch"
+            raise FhgError(rc, msg)
+
+    def add(self, ctx: "Context"):
+        self._check(self.lib.fhg_batch_add(self.h, ctx.h))
+        self._ctxs.append(ctx)
+
+    def solve(self):
+        """Returns (status, [SolveInfo per context], elapsed ms of the launch)."""
+        infos = (SolveInfo * len(self._ctxs))()
+        ms = C.c_double()
+        rc = self.lib.fhg_batch_solve(self.h, infos, C.byref(ms))
+        return rc, list(infos), ms.value
+
+    def close(self):
+        if self.h:
+            self.lib.fhg_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Net:

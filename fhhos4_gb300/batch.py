@@ -1,0 +1,92 @@
+"""Batched solve of many independent problems of uneven size (one graph launch, fhg_batch_*).
+
+The workload generator follows the batched configuration: 2D unit squares, n x n cells split into
+two triangles each, HHO degree k in {1, 2, 3} (face blocks of 2, 3, 4 unknowns), an isotropic
+coefficient constant on each of 8 x 8 patches and log-uniform in [1e-3, 1e3], and a smooth source
+made of four random sine modes with N(0, 1) amplitudes, all drawn from one seed.
+
+n is drawn from the multiples of 16 in [32, 256]: the reference's geometric coarsening halves n
+while it is even, so an n with a large odd factor leaves a coarsest level far above what a dense
+direct solve takes (an odd n is a single level, i.e. a direct solve of the whole system). The
+coarse operators are Galerkin products (Multigrid::UseGalerkinOperator, "-g 1"): with
+rediscretised coarse operators the V-cycle is not a contraction when coarse cells straddle the
+coefficient patches (n = 48, 80, 112, ...), and FCG does not converge.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass
+from typing import List
+
+import numpy as np
+
+from . import _native as N
+from . import hho
+
+
+@dataclass
+class ProblemSpec:
+    n: int
+    k: int
+    seed: int
+
+
+def batched_specs(count: int, seed: int = 20261203, n_min: int = 32, n_max: int = 256, step: int = 16,
+                  ks=(1, 2, 3)) -> List[ProblemSpec]:
+    rng = np.random.default_rng(seed)
+    ns = np.arange(n_min, n_max + 1, step)
+    return [ProblemSpec(int(rng.choice(ns)), int(rng.choice(ks)), int(rng.integers(1, 2 ** 62))) for _ in range(count)]
+
+
+class Problem:
+    """One problem: its hierarchy on a set-up context; b uploaded to the context's device buffer."""
+
+    def __init__(self, spec: ProblemSpec, device: int = 0, precision: str = "fp64", autotune: bool = True,
+                 tol: float = 1e-8, maxit: int = 200, keep_operator: bool = False):
+        H = hho.Hierarchy(2, spec.n, spec.k, source="modes", coefficient="lognormal_patches", contrast=1e3,
+                          checker_blocks=8, seed=spec.seed, max_coarse_rows=1000)
+        self.spec = spec
+        self.bs = H.block_size
+        A0 = H.A(0)
+        Ps = [H.P(l) for l in range(H.levels - 1)]
+        self.b = H.b()
+        self.n = A0.shape[0]
+        self.levels = H.levels
+        H.close()
+        ctx = N.Context(device)
+        ctx.set_level(0, self.bs, A0)
+        for l, P in enumerate(Ps):
+            ctx.set_prolongation(l, P)
+        o = N.default_options()
+        o.galerkin = 1
+        o.vcycle_precision = N.PRECISION[precision]
+        o.autotune = 1 if autotune else 0
+        o.tolerance = tol
+        o.max_iterations = maxit
+        ctx.setup(self.levels, o)
+        self.ctx = ctx
+        self.A0 = A0 if keep_operator else None
+
+    def upload_b(self):
+        self.ctx.io_upload(self.b)
+
+    def x(self) -> np.ndarray:
+        return self.ctx.io_download(self.n)
+
+    def close(self):
+        if self.ctx is not None:
+            self.ctx.close()
+            self.ctx = None
+
+
+def build(specs: List[ProblemSpec], device: int = 0, precision: str = "fp64", autotune: bool = True,
+          keep_operator: bool = False):
+    """Problems with b uploaded, and a Batch holding all of them. Returns (problems, batch, seconds)."""
+    t0 = time.time()
+    probs = [Problem(s, device, precision, autotune, keep_operator=keep_operator) for s in specs]
+    for p in probs:
+        p.upload_b()
+    batch = N.Batch(device)
+    for p in probs:
+        batch.add(p.ctx)
+    return probs, batch, time.time() - t0

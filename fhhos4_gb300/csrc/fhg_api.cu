@@ -119,6 +119,23 @@ struct fhg_ctx {
     cudaGraphExec_t graph_l[2] = {nullptr, nullptr};
     long long graph_l_kernels[2] = {0, 0};
     int graphs_l_built = 0;
+    bool device_loop = false;          // capturing for the device-side loop: no host read-back
+    long long epoch = 0;               // incremented by every setup (batched graphs hold its buffers)
+};
+
+// Many independent solves in one graph launch (fhg_batch_*): per problem a captured prelude, a
+// WHILE conditional node whose body is one FCG iteration and the device-side stopping test, and a
+// captured epilogue (FP64 true residual, x out).
+struct fhg_batch {
+    int device = 0;
+    std::string err;
+    std::vector<fhg_ctx*> probs;
+    std::vector<long long> epochs;     // setup epoch of every context when the graph was built
+    std::vector<long long> body_kernels;
+    long long fixed_kernels = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaGraphExec_t exec = nullptr;
 };
 
 // Training state of one network (fhg_net_*): FP32 master parameters, Adam moments and the
@@ -861,7 +878,7 @@ void fcg_iteration(fhg_ctx* ctx, int p)
                             fp32 ? L0.b32 : nullptr);
     fhg::launch_finalize_norm(part(ctx, 3), ctx->scal + 0, ctx->scal + 2, ctx->hist_d, ctx->counter_d,
                               ctx->opts.max_iterations + 1, s);
-    cudaMemcpyAsync(ctx->nr_host, ctx->scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (!ctx->device_loop) cudaMemcpyAsync(ctx->nr_host, ctx->scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s);
 }
 
 // One PCG iteration (src/Solver/Krylov/ConjugateGradient.h:58-96); z, d, Ad = kz[0], kz[1], kAd[0].
@@ -1285,6 +1302,7 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
     if (!ctx) return FHG_ERR_INVALID_ARG;
     CK(cudaSetDevice(ctx->device));
     free_all(ctx);
+    ctx->epoch++;
     if (opts) ctx->opts = *opts;
     fhg_options& o = ctx->opts;
     if (o.max_coarse_rows <= 0) o.max_coarse_rows = 8192;
@@ -2164,6 +2182,269 @@ int fhg_net_train_step(fhg_net* net, fhg_ctx* ctx, const float* r, double energy
         *loss = 1.0 + t / energy;
     }
     return FHG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched solve (no counterpart in the reference)
+
+int fhg_io_buffers(fhg_ctx* ctx, double** b_dev, double** x_dev)
+{
+    if (!ctx || !b_dev || !x_dev) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
+    *b_dev = ctx->io;
+    *x_dev = ctx->io + ctx->levels[0].n;
+    return FHG_OK;
+}
+
+int fhg_io_upload(fhg_ctx* ctx, const double* b)
+{
+    if (!ctx || !b) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(ctx->io, b, sizeof(double) * ctx->levels[0].n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return FHG_OK;
+}
+
+int fhg_io_download(fhg_ctx* ctx, double* x)
+{
+    if (!ctx || !x) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
+    CK(cudaSetDevice(ctx->device));
+    const long long n = ctx->levels[0].n;
+    CK(cudaMemcpyAsync(x, ctx->io + n, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return FHG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+int batch_fail(fhg_batch* b, int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (b) b->err = buf;
+    return code;
+}
+
+#define BCK(call)                                                                                  \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return batch_fail(batch, FHG_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+// Start of a solve on the device (run_solve's prelude): b' = Pi b, x = 0, r = b, direction
+// placeholders, ||b||, scalars and counter.
+void batch_prelude(fhg_ctx* ctx)
+{
+    Level& L0 = ctx->levels[0];
+    const long long n = L0.n;
+    cudaStream_t s = ctx->stream;
+    fhg::launch_permute<double>(L0.nb, L0.bs, L0.perm_d, ctx->io, ctx->kb, true, s);
+    cudaMemsetAsync(ctx->kx, 0, sizeof(double) * n, s);
+    cudaMemcpyAsync(ctx->kr, ctx->kb, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    for (int q = 0; q < 2; q++) {
+        cudaMemsetAsync(ctx->kz[q], 0, sizeof(double) * n, s);
+        cudaMemsetAsync(ctx->kAd[q], 0, sizeof(double) * n, s);
+    }
+    fhg::launch_dot(n, ctx->kb, ctx->kb, part(ctx, 0), s);
+    fhg::launch_sqrt_sum(part(ctx, 0), ctx->scal + 0, s);
+    fhg::launch_init_solve(ctx->scal, ctx->counter_d, s);
+    if (ctx->opts.vcycle_precision == FHG_PREC_FP32) fhg::launch_convert<double, float>(n, ctx->kr, L0.b32, s);
+}
+
+// End of a solve: FP64 true residual into scal[5] (||b - A x||), x = Pi^T x'.
+void batch_epilogue(fhg_ctx* ctx)
+{
+    Level& L0 = ctx->levels[0];
+    const long long n = L0.n;
+    cudaStream_t s = ctx->stream;
+    fhg::launch_spmv<double>(L0.A.v, fhg::kSpmvResidual, ctx->kx, ctx->kb, ctx->kt, s);
+    fhg::launch_dot(n, ctx->kt, ctx->kt, part(ctx, 0), s);
+    fhg::launch_sqrt_sum(part(ctx, 0), ctx->scal + 5, s);
+    fhg::launch_permute<double>(L0.nb, L0.bs, L0.perm_d, ctx->kx, ctx->io + n, false, s);
+}
+
+// Capture `fn(ctx)` on the context's stream into `g` (a new graph when g is null, else the given
+// body graph).
+template <class F>
+cudaError_t capture(fhg_ctx* ctx, cudaGraph_t* g, bool into, F fn)
+{
+    cudaError_t e = into ? cudaStreamBeginCaptureToGraph(ctx->stream, *g, nullptr, nullptr, 0,
+                                                         cudaStreamCaptureModeThreadLocal)
+                         : cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    fn(ctx);
+    cudaGraph_t out = nullptr;
+    e = cudaStreamEndCapture(ctx->stream, &out);
+    if (e == cudaSuccess && !into) *g = out;
+    return e;
+}
+
+int batch_build(fhg_batch* batch)
+{
+    cudaGraph_t top = nullptr;
+    BCK(cudaGraphCreate(&top, 0));
+    batch->body_kernels.assign(batch->probs.size(), 0);
+    batch->fixed_kernels = 0;
+    int rc = FHG_OK;
+    for (size_t i = 0; i < batch->probs.size() && rc == FHG_OK; i++) {
+        fhg_ctx* ctx = batch->probs[i];
+        cudaError_t e = cudaSuccess;
+        const long long k0 = fhg::g_kernel_launches.load();
+        cudaGraph_t pre = nullptr, post = nullptr;
+        cudaGraphNode_t npre = nullptr, nwhile = nullptr, npost = nullptr;
+        e = capture(ctx, &pre, false, batch_prelude);
+        if (e == cudaSuccess) e = cudaGraphAddChildGraphNode(&npre, top, nullptr, 0, pre);
+        const long long k1 = fhg::g_kernel_launches.load();
+        cudaGraphConditionalHandle h = 0;
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, top, 1, cudaGraphCondAssignDefault);
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&nwhile, top, &npre, nullptr, 1, &cp);
+        if (e == cudaSuccess) {
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            ctx->device_loop = true;
+            const double tol = ctx->opts.tolerance;
+            const int maxit = ctx->opts.max_iterations;
+            e = capture(ctx, &body, true, [&](fhg_ctx* c) {
+                fcg_iteration(c, 0);
+                const long long n = c->levels[0].n;
+                fhg::launch_copy2(n, c->kz[0], c->kz[1], c->kAd[0], c->kAd[1], c->stream);
+                fhg::launch_loop_control(c->scal + 2, c->counter_d, tol, maxit, h, c->stream);
+            });
+            ctx->device_loop = false;
+        }
+        const long long k2 = fhg::g_kernel_launches.load();
+        if (e == cudaSuccess) e = capture(ctx, &post, false, batch_epilogue);
+        if (e == cudaSuccess) e = cudaGraphAddChildGraphNode(&npost, top, &nwhile, 1, post);
+        const long long k3 = fhg::g_kernel_launches.load();
+        fhg::g_kernel_launches -= (k3 - k0);  // captured, not executed
+        batch->fixed_kernels += (k1 - k0) + (k3 - k2);
+        batch->body_kernels[i] = k2 - k1;
+        if (pre) cudaGraphDestroy(pre);
+        if (post) cudaGraphDestroy(post);
+        if (e != cudaSuccess) rc = batch_fail(batch, FHG_ERR_CUDA, "problem %zu: graph construction: %s", i, cudaGetErrorString(e));
+    }
+    if (rc == FHG_OK) {
+        cudaError_t e = cudaGraphInstantiate(&batch->exec, top, 0);
+        if (e != cudaSuccess) rc = batch_fail(batch, FHG_ERR_CUDA, "graph instantiation: %s", cudaGetErrorString(e));
+    }
+    cudaGraphDestroy(top);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fhg_batch_create(fhg_batch** out, int device)
+{
+    if (!out) return FHG_ERR_INVALID_ARG;
+    fhg_batch* batch = new fhg_batch();
+    *out = batch;
+    batch->device = device;
+    BCK(cudaSetDevice(device));
+    BCK(cudaStreamCreateWithFlags(&batch->stream, cudaStreamNonBlocking));
+    BCK(cudaEventCreate(&batch->ev0));
+    BCK(cudaEventCreate(&batch->ev1));
+    return FHG_OK;
+}
+
+void fhg_batch_destroy(fhg_batch* batch)
+{
+    if (!batch) return;
+    cudaSetDevice(batch->device);
+    if (batch->exec) cudaGraphExecDestroy(batch->exec);
+    if (batch->ev0) cudaEventDestroy(batch->ev0);
+    if (batch->ev1) cudaEventDestroy(batch->ev1);
+    if (batch->stream) cudaStreamDestroy(batch->stream);
+    delete batch;
+}
+
+const char* fhg_batch_last_error(const fhg_batch* batch) { return batch ? batch->err.c_str() : "null batch"; }
+
+int fhg_batch_add(fhg_batch* batch, fhg_ctx* ctx)
+{
+    if (!batch || !ctx) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready) return batch_fail(batch, FHG_ERR_NOT_READY, "the context has not been set up");
+    if (ctx->device != batch->device) return batch_fail(batch, FHG_ERR_INVALID_ARG, "context on device %d, batch on %d", ctx->device, batch->device);
+    if (ctx->opts.krylov != FHG_KRYLOV_FCG) return batch_fail(batch, FHG_ERR_UNSUPPORTED, "the batched solve runs FCG");
+    if (ctx->learned_mode != FHG_LEARNED_OFF) return batch_fail(batch, FHG_ERR_UNSUPPORTED, "the batched solve runs the plain V-cycle");
+    for (fhg_ctx* c : batch->probs)
+        if (c == ctx) return batch_fail(batch, FHG_ERR_INVALID_ARG, "context added twice");
+    if (batch->exec) {
+        cudaGraphExecDestroy(batch->exec);
+        batch->exec = nullptr;
+    }
+    batch->probs.push_back(ctx);
+    return FHG_OK;
+}
+
+int fhg_batch_solve(fhg_batch* batch, fhg_solve_info* infos, double* elapsed_ms)
+{
+    if (!batch) return FHG_ERR_INVALID_ARG;
+    if (batch->probs.empty()) return batch_fail(batch, FHG_ERR_INVALID_ARG, "empty batch");
+    BCK(cudaSetDevice(batch->device));
+    bool stale = !batch->exec || batch->epochs.size() != batch->probs.size();
+    for (size_t i = 0; i < batch->probs.size(); i++) {
+        fhg_ctx* c = batch->probs[i];
+        if (!c->ready) return batch_fail(batch, FHG_ERR_NOT_READY, "a context of the batch is not set up");
+        if (!stale && batch->epochs[i] != c->epoch) stale = true;  // set up again since the graph was built
+        BCK(cudaStreamSynchronize(c->stream));
+    }
+    if (stale) {
+        if (batch->exec) {
+            cudaGraphExecDestroy(batch->exec);
+            batch->exec = nullptr;
+        }
+        int rc = batch_build(batch);
+        if (rc) return rc;
+        batch->epochs.clear();
+        for (fhg_ctx* c : batch->probs) batch->epochs.push_back(c->epoch);
+    }
+    BCK(cudaEventRecord(batch->ev0, batch->stream));
+    BCK(cudaGraphLaunch(batch->exec, batch->stream));
+    BCK(cudaEventRecord(batch->ev1, batch->stream));
+    BCK(cudaEventSynchronize(batch->ev1));
+    float ms = 0;
+    BCK(cudaEventElapsedTime(&ms, batch->ev0, batch->ev1));
+    if (elapsed_ms) *elapsed_ms = ms;
+    int status = FHG_OK;
+    long long kernels = batch->fixed_kernels;
+    for (size_t i = 0; i < batch->probs.size(); i++) {
+        fhg_ctx* c = batch->probs[i];
+        double sc[6];
+        int counter = 0;
+        BCK(cudaMemcpy(sc, c->scal, sizeof(sc), cudaMemcpyDeviceToHost));
+        BCK(cudaMemcpy(&counter, c->counter_d, sizeof(int), cudaMemcpyDeviceToHost));
+        const int its = counter - 1;
+        kernels += (long long)its * batch->body_kernels[i];
+        int st = FHG_OK;
+        if (std::isinf(sc[2])) st = FHG_ERR_DIVERGED;
+        else if (std::isnan(sc[2])) st = FHG_ERR_NAN;
+        if (st != FHG_OK && status == FHG_OK) status = st;
+        if (infos) {
+            infos[i].iterations = its;
+            infos[i].status = st;
+            infos[i].normalized_residual = sc[2];
+            infos[i].solve_ms = ms;
+            infos[i].learned_iterations = 0;
+            infos[i].true_relative_residual = st == FHG_OK ? (sc[0] > 0 ? sc[5] / sc[0] : sc[5]) : -1.0;
+        }
+    }
+    fhg::g_kernel_launches += kernels;
+    if (status != FHG_OK) batch_fail(batch, status, "a problem of the batch diverged or produced NaN");
+    return status;
 }
 
 }  // extern "C"

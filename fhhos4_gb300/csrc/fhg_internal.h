@@ -92,6 +92,12 @@ void launch_cg_step(long long n, double* x, double* r, const double* d, const do
 
 template <class Tin, class Tout>
 void launch_convert(long long n, const Tin* in, Tout* out, cudaStream_t s);
+// Device-side solve loop: b0 = a0 and b1 = a1; solve scalars and iteration counter at their start
+// values; the WHILE-node condition from ||r||/||b|| (nr), the counter, tol and maxit.
+void launch_copy2(long long n, const double* a0, double* b0, const double* a1, double* b1, cudaStream_t s);
+void launch_init_solve(double* scal, int* counter, cudaStream_t s);
+void launch_loop_control(const double* nr, const int* counter, double tol, int maxit, cudaGraphConditionalHandle h,
+                         cudaStream_t s);
 // gather: out[b*bs+c] = in[perm[b]*bs+c]; scatter: out[perm[b]*bs+c] = in[b*bs+c].
 template <class T>
 void launch_permute(int nb, int bs, const int* perm, const T* in, T* out, bool gather, cudaStream_t s);

@@ -13,6 +13,7 @@
 //     so one whole iteration can be replayed as a CUDA graph.
 #include "fhg_internal.h"
 
+#include <algorithm>
 #include <cmath>
 
 namespace fhg {
@@ -817,5 +818,67 @@ template void launch_convert<double, float>(long long, const double*, float*, cu
 template void launch_convert<float, double>(long long, const float*, double*, cudaStream_t);
 template void launch_permute<double>(int, int, const int*, const double*, double*, bool, cudaStream_t);
 template void launch_permute<float>(int, int, const int*, const float*, float*, bool, cudaStream_t);
+
+
+// ---------------------------------------------------------------------------
+// Device-side solve loop (batched solve): the stopping test runs on the device and drives the
+// WHILE node of the graph.
+
+namespace {
+
+__global__ void k_copy2(long long n, const double* __restrict__ a0, double* __restrict__ b0,
+                        const double* __restrict__ a1, double* __restrict__ b1)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        b0[i] = a0[i];
+        b1[i] = a1[i];
+    }
+}
+
+__global__ void k_init_solve(double* scal, int* counter)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        scal[1] = 1.0;  // d.Ad of the (absent) previous direction
+        scal[2] = 1.0;  // ||r|| / ||b||
+        scal[3] = 0.0;
+        scal[4] = 0.0;
+        *counter = 1;
+    }
+}
+
+// Continue while iterations < maxit, ||r||/||b|| >= tol and finite (IterativeSolver's stopping
+// test, src/Solver/IterativeSolver.h:224-247). `counter` = iterations done + 1.
+__global__ void k_loop_control(const double* nr, const int* counter, double tol, int maxit,
+                               cudaGraphConditionalHandle handle)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const double v = *nr;
+        const int it = *counter - 1;
+        const bool go = it < maxit && v >= tol && isfinite(v);
+        cudaGraphSetConditional(handle, go ? 1u : 0u);
+    }
+}
+
+}  // namespace
+
+void launch_copy2(long long n, const double* a0, double* b0, const double* a1, double* b1, cudaStream_t s)
+{
+    const long long blocks = std::min<long long>((n + 255) / 256, 4 * 152);
+    k_copy2<<<(unsigned)std::max<long long>(blocks, 1), 256, 0, s>>>(n, a0, b0, a1, b1);
+    g_kernel_launches++;
+}
+
+void launch_init_solve(double* scal, int* counter, cudaStream_t s)
+{
+    k_init_solve<<<1, 32, 0, s>>>(scal, counter);
+    g_kernel_launches++;
+}
+
+void launch_loop_control(const double* nr, const int* counter, double tol, int maxit, cudaGraphConditionalHandle h,
+                         cudaStream_t s)
+{
+    k_loop_control<<<1, 32, 0, s>>>(nr, counter, tol, maxit, h);
+    g_kernel_launches++;
+}
 
 }  // namespace fhg

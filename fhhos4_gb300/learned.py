@@ -176,14 +176,19 @@ class TrainLog:
 
 def train(net: N.Net, fields: int = 64, n: int = 16, samples_per_field: int = 4, steps_per_sample: int = 1,
           lr: float = 2e-3, lr_min: float = 1e-4, weight_decay: float = 0.0, seed0: int = 1000, device: int = 0,
-          spec_kw: Optional[dict] = None, log_every: int = 0, smoothers=("bgs", "rbgs"), nu=(1, 1)) -> TrainLog:
-    """Stream `fields` seeded fields (seeds seed0, seed0+1, ...) and take Adam steps on their samples."""
+          spec_kw: Optional[dict] = None, log_every: int = 0, smoothers=("bgs", "rbgs"), nu=(1, 1),
+          identity_every: int = 0) -> TrainLog:
+    """Stream `fields` seeded fields (seeds seed0, seed0+1, ...) and take Adam steps on their samples;
+    identity_every = m > 0 makes every m-th field the identity coefficient instead."""
     log = TrainLog()
     total = max(1, fields * samples_per_field * steps_per_sample)
     t0 = time.time()
     step = 0
     for fi in range(fields):
-        spec = FieldSpec(n=n, seed=seed0 + fi, **(spec_kw or {}))
+        kw = dict(spec_kw or {})
+        if identity_every and fi % identity_every == identity_every - 1:
+            kw["coefficient"] = "identity"
+        spec = FieldSpec(n=n, seed=seed0 + fi, **kw)
         f = Field(spec, device=device, smoothers=smoothers, nu=nu)
         try:
             samples = make_samples(f, samples_per_field, seed=seed0 * 7919 + fi)
@@ -217,15 +222,20 @@ def _cli():
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
     ap.add_argument("--init", default="")
     ap.add_argument("--log-every", type=int, default=20)
+    ap.add_argument("--nu", default="2,2", help="pre,post smoothing steps of the cycle the step corrects")
+    ap.add_argument("--identity-every", type=int, default=4, help="every m-th field has K = I (0: none)")
     a = ap.parse_args()
+    nu = tuple(int(v) for v in a.nu.split(","))
     net = N.Net(0)
     p0 = load_params(a.init)[0] if a.init else init_params(a.seed)
     net.set_params(p0)
     log = train(net, fields=a.fields, n=a.n, samples_per_field=a.samples, steps_per_sample=a.repeat, lr=a.lr,
-                seed0=a.seed, log_every=a.log_every)
+                seed0=a.seed, log_every=a.log_every, nu=nu, identity_every=a.identity_every)
     meta = {"fields": a.fields, "n": a.n, "k": 1, "coefficient": "anisotropic diag(1,1,eps), eps log-U[1e-3,1], "
-            "random rotation per 4^3 block", "samples_per_field": a.samples, "repeat": a.repeat, "lr": a.lr,
+            "random rotation per 4^3 block" + (f"; every {a.identity_every}th field K = I" if a.identity_every else ""),
+            "cycle": f"V({nu[0]},{nu[1]}) bgs/rbgs", "samples_per_field": a.samples, "repeat": a.repeat, "lr": a.lr,
             "seed0": a.seed, "steps": log.steps, "seconds": round(log.seconds, 1),
+            "first_mean_loss": float(np.mean(log.losses[:200])) if log.losses else None,
             "final_mean_loss": float(np.mean(log.losses[-200:])) if log.losses else None}
     save_params(a.out, net.params(), meta)
     print(json.dumps(meta), flush=True)

@@ -248,6 +248,26 @@ int fhg_net_get_params(const fhg_net* net, float* params, int n_params);
 int fhg_net_train_step(fhg_net* net, fhg_ctx* ctx, const float* r, double energy, float lr, float weight_decay,
                        int update, double* loss, float* grad);
 
+/* ---- Batched solve (no counterpart in the reference) --------------------------------------------
+ * Many independent systems, each a set-up FCG context (plain V-cycle, FP64 or FP32), solved by ONE
+ * graph launch: per context a prelude, a WHILE conditional node whose body is one FCG iteration
+ * followed by the stopping test evaluated on the device (||r||/||b|| < tolerance, NaN/inf or
+ * max_iterations), and an epilogue (FP64 true residual, x out). Each context reads b from and writes
+ * x to its own device buffers (fhg_io_buffers, the caller's numbering). The contexts are borrowed;
+ * setting one up again makes the next solve rebuild the graph. The launch sequence of every system
+ * is that of fhg_solve_device, so iteration counts and results are the same. */
+typedef struct fhg_batch fhg_batch;
+int fhg_io_buffers(fhg_ctx* ctx, double** b_dev, double** x_dev);
+int fhg_io_upload(fhg_ctx* ctx, const double* b);   /* host b -> the context's device b */
+int fhg_io_download(fhg_ctx* ctx, double* x);       /* the context's device x -> host x */
+int fhg_batch_create(fhg_batch** batch, int device);
+void fhg_batch_destroy(fhg_batch* batch);
+const char* fhg_batch_last_error(const fhg_batch* batch);
+int fhg_batch_add(fhg_batch* batch, fhg_ctx* ctx);
+/* infos: one per added context, in order (solve_ms = the whole batch); elapsed_ms: device time of
+ * the launch (CUDA events on the batch's stream). */
+int fhg_batch_solve(fhg_batch* batch, fhg_solve_info* infos, double* elapsed_ms);
+
 #ifdef __cplusplus
 }
 #endif
