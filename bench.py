@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--contrast", type=float, default=1e6)
     ap.add_argument("--source", default="sine", choices=["sine", "one"])
     ap.add_argument("--max-coarse-rows", type=int, default=1000)
+    ap.add_argument("--galerkin", action="store_true", help="Galerkin coarse operators (the reference's -g 1)")
     ap.add_argument("--fast-smoothers", default="bgs,rbgs", help="pre,post smoothers of the fast (FP32) method")
     ap.add_argument("--fast-nu", default="2,2", help="pre,post smoothing steps of the fast (FP32) method")
     ap.add_argument("--weights", default="", help="learned-step network (default: the committed one)")
@@ -189,6 +190,7 @@ def workload_config(args):
     return {"workload": name, "dim": args.dim, "n": args.n, "k": args.k, "mesh": "stetra" if args.dim == 3 else "stri",
             "krylov": "FCG(1)", "cycle": "V(1,1)", "smoothers": "bgs/rbgs (multicolour order)",
             "coarse": "FP64 dense inverse of the coarsest operator",
+            "coarse_operators": "Galerkin P^T A P (-g 1)" if args.galerkin else "rediscretised (the reference default)",
             "l2": "inputs larger than L2 (fine operator alone is > 1 GB)"}
 
 
@@ -258,6 +260,7 @@ def run_ours(args, dist: Dist):
     ctx.set_face_tensors(H.face_tensors(0))
     o = N.default_options()
     o.vcycle_precision = N.PRECISION["fp32"]   # keeps FP64 and FP32 copies
+    o.galerkin = 1 if args.galerkin else 0
     o.autotune = 1
     o.max_iterations = 200
     ctx.setup(len(As), o)
@@ -287,10 +290,13 @@ def run_ours(args, dist: Dist):
     #             headline `value` (the metric's "learned+FP32 MG-FCG").
     from fhhos4_gb300 import learned as LN
     params, wmeta = LN.load_params(args.weights or LN.DEFAULT_WEIGHTS)
+    # the learned step exists for face blocks of 2..4 unknowns (k = 1 in 3D)
+    have_learned = bs <= 4 and not args.no_learned
     methods = {"plain": ("fp64", "bgs", "rbgs", 1, 1, False),
                "fp64_fast": ("fp64", fast_pre, fast_post, fast_npre, fast_npost, False),
-               "fast": ("fp32", fast_pre, fast_post, fast_npre, fast_npost, False),
-               "learned": ("fp32", fast_pre, fast_post, fast_npre, fast_npost, True)}
+               "fast": ("fp32", fast_pre, fast_post, fast_npre, fast_npost, False)}
+    if have_learned:
+        methods["learned"] = ("fp32", fast_pre, fast_post, fast_npre, fast_npost, True)
     results = {}
     launches = {}
     clocks = {}
@@ -301,7 +307,7 @@ def run_ours(args, dist: Dist):
         ctx.set_vcycle_precision(prec)
         if use_learned:
             ctx.set_learned(params, "fallback")
-        else:
+        elif bs <= 4:
             ctx.set_learned(None, "off")
         for _ in range(args.warmup):
             solve_device()
@@ -335,13 +341,13 @@ def run_ours(args, dist: Dist):
     if H is not None:
         H.close()
 
-    head = "fast" if args.no_learned else "learned"
+    head = "learned" if have_learned else "fast"
     # End to end through the public C ABI with pinned host buffers (H2D b, solve, D2H x), headline method.
     ctx.set_cycle(fast_pre, fast_post, fast_npre, fast_npost, 1)
     ctx.set_vcycle_precision("fp32")
     if head == "learned":
         ctx.set_learned(params, "fallback")
-    else:
+    elif bs <= 4:
         ctx.set_learned(None, "off")
     b_host = torch.from_numpy(b).pin_memory()
     x_host = torch.empty_like(b_host).pin_memory()
@@ -391,13 +397,14 @@ def run_ours(args, dist: Dist):
                        bytes_spmv(pb, nb0, n1, n0, bs, p, add=True))
     # The learned step (FP32 residual, block-diagonal scaling, 48-128-128-16 MLP on the tensor
     # cores) and its MLP work: 2 (48 x 128 + 128 x 128 + 128 x 16) FLOP per face.
-    ctx.set_learned(params, "always")
-    for kname in ("tcgen05", "mma_sync"):
-        ctx.set_learned(params, "always", kernel=kname)
-        ms = ctx.time_op(0, N.OP_LEARNED_STEP, "fp32", warmup=3, reps=20)
-        flops = 2.0 * (48 * 128 + 128 * 128 + 128 * 16) * nb0
-        kernels[f"learned_step_{kname}"] = {"ms": ms, "bytes": 0, "gbs": 0.0, "tflops_mlp": flops / (ms * 1e-3) / 1e12}
-    ctx.set_learned(params, "fallback")
+    if have_learned:
+        for kname in ("tcgen05", "mma_sync"):
+            ctx.set_learned(params, "always", kernel=kname)
+            ms = ctx.time_op(0, N.OP_LEARNED_STEP, "fp32", warmup=3, reps=20)
+            flops = 2.0 * (48 * 128 + 128 * 128 + 128 * 16) * nb0
+            kernels[f"learned_step_{kname}"] = {"ms": ms, "bytes": 0, "gbs": 0.0,
+                                                "tflops_mlp": flops / (ms * 1e-3) / 1e12}
+        ctx.set_learned(params, "fallback")
     # Dominant kernel of the headline (FP32 V-cycle) solve: GS sweeps on level 0.
     ncol = info0["colours"]
     dom = "bsr_gs_sweep_fp32"
@@ -447,11 +454,11 @@ def run_ours(args, dist: Dist):
                            reference_iterations_natural_order=ref_nat),
         "fp64_fast_cycle": results["fp64_fast"],
         "fast": results["fast"],
-        "learned": results["learned"],
+        "learned": results.get("learned"),
         "headline_method": head,
         "speedup_vs_plain_fp64": round(results["plain"]["s"] / value, 3),
         "speedup_vs_fp64_same_cycle": round(results["fp64_fast"]["s"] / value, 3),
-        "learned_vs_fast": round(results["fast"]["s"] / results["learned"]["s"], 3),
+        "learned_vs_fast": round(results["fast"]["s"] / results["learned"]["s"], 3) if have_learned else None,
         "dofs_per_s": round(n0 * dist.world / value, 1),
         "e2e": {"value": round(e2e_s, 6), "unit": "s", "h2d_bytes_per_step": int(n0 * 8),
                 "d2h_bytes_per_step": int(n0 * 8)},

@@ -777,15 +777,13 @@ void smooth(fhg_ctx* ctx, int l, int code, int iters, const T* b, T* x, bool fro
 
 bool is_gs(int code) { return code != FHG_SMOOTHER_BJ && code != FHG_SMOOTHER_BJ23; }
 
-// Learned correction at the end of the finest level's post-smoothing: w = D^-1 (b - A x),
-// then x += s N(w-patch, tensors) face by face (fhg_learned.cu). r32 of level 0 is free here
-// (its last use is the restriction).
+// Learned correction at the end of the finest level's post-smoothing: w = D^-1 (b - A x) in one
+// pass, then x += s N(w-patch, tensors) face by face (fhg_learned.cu).
 void learned_step(fhg_ctx* ctx, const float* b, float* x)
 {
     Level& L = ctx->levels[0];
     cudaStream_t s = ctx->stream;
-    fhg::launch_spmv<float>(L.A32.v, fhg::kSpmvResidual, x, b, L.r32, s);
-    fhg::launch_block_diag(L.nb, L.bs, L.dinv32, L.nb, L.r32, ctx->lw, s);
+    fhg::launch_residual_dinv(L.A32.v, L.dinv32, L.nb, x, b, ctx->lw, s);
     fhg::launch_learned_apply(L.nb, L.bs, ctx->nbr_d, ctx->lw, ctx->tfeat_d, ctx->lwts, ctx->lbias, x, ctx->lstatus,
                               ctx->learned_kernel, s);
 }

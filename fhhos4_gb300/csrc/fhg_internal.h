@@ -128,6 +128,9 @@ enum GemmKind { kGemmFwdHid = 0, kGemmFwdOut = 1, kGemmBwdData = 2, kGemmGradHid
 }  // namespace learned
 
 bool learned_supports(int bs);
+// w = D^-1 (b - A x) in one pass (FP32; lanes >= bs, i.e. the learned step's block sizes).
+void launch_residual_dinv(const BsrView<float>& A, const float* dinv, long long dld, const float* x, const float* b,
+                          float* w, cudaStream_t s);
 // w = D^-1 r on the level's blocks (FP32).
 void launch_block_diag(int nb, int bs, const float* dinv, long long dld, const float* r, float* w, cudaStream_t s);
 // Training features: feat (rows x 48 BF16, rows >= nb zero), scale (rows).

@@ -167,6 +167,40 @@ __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int nbr, const int* __res
     }
 }
 
+// w = D^-1 (b - A x) (block-Jacobi-scaled residual, the learned step's input): the residual of a
+// row is reduced over the row's lanes, then lane r < BS applies row r of the row's D^-1.
+template <class T, int BS, int G, int U>
+__global__ void __launch_bounds__(kThreads) k_bsr_residual_dinv(int nbr, const int* __restrict__ rowptr,
+                                                                const int* __restrict__ colidx,
+                                                                const T* __restrict__ vals, long long ld,
+                                                                const T* __restrict__ dinv, long long dld,
+                                                                const T* __restrict__ x, const T* __restrict__ b,
+                                                                T* __restrict__ w)
+{
+    const int lane = threadIdx.x & (G - 1);
+    const int row = (int)(((long long)blockIdx.x * kThreads + threadIdx.x) / G);
+    T acc[BS];
+#pragma unroll
+    for (int r = 0; r < BS; r++) acc[r] = T(0);
+    T bv[BS], dv[BS];
+    if (row < nbr) {
+#pragma unroll
+        for (int c = 0; c < BS; c++) bv[c] = b[(long long)row * BS + c];
+        if (lane < BS)
+#pragma unroll
+            for (int c = 0; c < BS; c++) dv[c] = dinv[(long long)(lane * BS + c) * dld + row];
+        accumulate_row<T, BS, G, U>(rowptr[row], rowptr[row + 1], lane, colidx, vals, ld, x, acc, UseAll());
+    }
+#pragma unroll
+    for (int r = 0; r < BS; r++) acc[r] = group_sum<G>(acc[r]);
+    if (row < nbr && lane < BS) {
+        T v = T(0);
+#pragma unroll
+        for (int c = 0; c < BS; c++) v += dv[c] * (bv[c] - acc[c]);
+        w[(long long)row * BS + lane] = v;
+    }
+}
+
 // One colour of block Gauss-Seidel: rows [row0, row1) are mutually uncoupled.
 // x_i <- D_i^{-1} (b_i - sum_{j != i} A_ij x_j)
 // Columns outside [col_lo, col_hi) are skipped: in a sweep that starts from x = 0 they hold
@@ -650,6 +684,24 @@ void launch_spmv(const BsrView<T>& A, int mode, const T* x, const T* aux, T* y, 
     FHG_DISPATCH_BS_G(A.bs, A.lanes, {
         if (A.unroll == 2) spmv_u<T, BS, G, 2>(A, grid, mode, x, aux, y, s);
         else spmv_u<T, BS, G, 1>(A, grid, mode, x, aux, y, s);
+    });
+    g_kernel_launches++;
+}
+
+void launch_residual_dinv(const BsrView<float>& A, const float* dinv, long long dld, const float* x, const float* b,
+                          float* w, cudaStream_t s)
+{
+    if (A.nbr == 0) return;
+    const unsigned grid = grid_for((long long)A.nbr * A.lanes, kThreads);
+    FHG_DISPATCH_BS_G(A.bs, A.lanes, {
+        if constexpr (G >= BS) {
+            if (A.unroll == 2)
+                k_bsr_residual_dinv<float, BS, G, 2><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld,
+                                                                                dinv, dld, x, b, w);
+            else
+                k_bsr_residual_dinv<float, BS, G, 1><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld,
+                                                                                dinv, dld, x, b, w);
+        }
     });
     g_kernel_launches++;
 }

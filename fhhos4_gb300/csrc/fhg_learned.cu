@@ -325,33 +325,39 @@ __global__ void __launch_bounds__(kApplyWarps * 32, 2)
 }
 
 // ---------------------------------------------------------------------------
-// Fused inference on the 5th-generation tensor cores: one CTA of 256 threads per tile of 128
-// faces (persistent over tiles, two CTAs per SM). Threads 0-127 gather the residual patch of face
-// t of the tile (the next tile's patch is loaded while the current tile's layers run), threads
-// 128-255 copy its tensor features; one thread issues tcgen05.mma (BF16 x BF16 -> FP32, M = 128
-// faces, N = 128 or 16, K = 16 per instruction) with the accumulator in tensor memory (TMEM lane
-// t = face t); both warpgroups read it back with tcgen05.ld (warpgroup h: columns 64h..64h+63),
-// add the bias, apply gelu and write the BF16 A operand of the next layer. Operands live in
-// shared memory in the canonical K-major layout without swizzle: 8-row x 16-byte core matrices,
-// element (row r, k) at byte
+// Fused inference on the 5th-generation tensor cores: one persistent CTA per SM with four
+// independent tile pipelines, one per warpgroup (slot), each on its own tiles of 128 faces. In a
+// slot, thread t gathers the residual patch and the tensor features of face t (the next tile's are
+// loaded while the current tile's layers run), one thread issues tcgen05.mma (BF16 x BF16 -> FP32,
+// M = 128 faces, N = 128 or 16, K = 16 per instruction) with the accumulator in the slot's 128 TMEM
+// columns (TMEM lane t = face t), and the warpgroup reads it back with tcgen05.ld, adds the bias,
+// applies gelu and writes the BF16 A operand of the next layer. The slots share the weights in
+// shared memory and synchronise only within the warpgroup (named barriers, one mbarrier each), so
+// the MMA waits, gathers and epilogues of four tiles overlap on every SM. Operands live in shared
+// memory in the canonical K-major layout without swizzle: 8-row x 16-byte core matrices, element
+// (row r, k) at byte
 //   (r / 8) * SBO + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2,
-// i.e. LBO = 128 bytes between core matrices along K and SBO = (K / 8) * 128 bytes between
-// 8-row groups. Every wait on the MMA-completion mbarrier is bounded (about a second of SM
-// clocks): on expiry the kernel records the failure, frees its TMEM and returns.
+// i.e. LBO = 128 bytes between core matrices along K and SBO = (K / 8) * 128 bytes between 8-row
+// groups; a slot's input tile (K = 48) occupies the first bytes of its hidden tile (K = 128), which
+// is written only after the layer-1 MMA has read the inputs. Every wait on an MMA-completion
+// mbarrier is bounded (about a second of SM clocks): on expiry the slot records the failure and
+// stops, and the CTA frees its TMEM and returns.
 
-constexpr int kTcThreads = 256;
-constexpr int kTcRows = 128;                  // faces per tile (TMEM lanes)
-constexpr uint32_t kTmemCols = 256;           // layer accumulator (128 columns) + output (16)
-constexpr int kTcSW1 = 0;                     // W1: 128 x 48
-constexpr int kTcSW2 = kTcSW1 + kHid * kIn * 2;   // W2: 128 x 128
-constexpr int kTcSW3 = kTcSW2 + kHid * kHid * 2;  // W3: 16 x 128
-constexpr int kTcSA = kTcSW3 + kOut * kHid * 2;   // inputs: 128 x 48
-constexpr int kTcSH = kTcSA + kTcRows * kIn * 2;  // hidden activations: 128 x 128
-constexpr int kTcSBias = kTcSH + kTcRows * kHid * 2;  // b1, b2, b3 (FP32)
-constexpr int kTcSScale = kTcSBias + (2 * kHid + kOut) * 4;  // s of the tile's faces
-constexpr int kTcSMisc = kTcSScale + kTcRows * 4;  // mbarrier (8), TMEM base (4)
-constexpr size_t kTcSmem = kTcSMisc + 64 + 1024;  // + alignment slack for a 1024-byte base
+constexpr int kTcSlots = 4;
+constexpr int kTcRows = 128;                       // faces per tile (TMEM lanes)
+constexpr int kTcThreads = kTcRows * kTcSlots;     // one warpgroup per slot
+constexpr uint32_t kTmemCols = 128 * kTcSlots;     // per slot: layer accumulators (the output reuses 16)
+constexpr int kTcSW1 = 0;                          // W1: 128 x 48
+constexpr int kTcSW2 = kTcSW1 + kHid * kIn * 2;    // W2: 128 x 128
+constexpr int kTcSW3 = kTcSW2 + kHid * kHid * 2;   // W3: 16 x 128
+constexpr int kTcSBias = kTcSW3 + kOut * kHid * 2; // b1, b2, b3 (FP32)
+constexpr int kTcSlot0 = ((kTcSBias + (2 * kHid + kOut) * 4 + 1023) / 1024) * 1024;
+constexpr int kTcSlotBytes = kTcRows * kHid * 2;   // hidden tile (the input tile aliases its start)
+constexpr int kTcSScale = kTcSlot0 + kTcSlots * kTcSlotBytes;  // s of every slot's faces
+constexpr int kTcSMisc = kTcSScale + kTcSlots * kTcRows * 4;   // mbarriers (8 each), TMEM base (4)
+constexpr size_t kTcSmem = kTcSMisc + 8 * kTcSlots + 16 + 1024;  // + alignment slack for a 1024-byte base
 constexpr long long kTcWaitCycles = 2000000000LL;
+static_assert(kTcSmem <= 232448, "one CTA per SM must fit in shared memory");
 
 __device__ __forceinline__ uint32_t core_off(int row, int kchunk, int sbo)
 {
@@ -432,27 +438,40 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// Bias + gelu of 64 accumulator columns [c0, c0 + 64) of this thread's lane into its row of the
-// hidden tile.
-__device__ __forceinline__ void tc_hidden_epilogue(uint32_t taddr, int c0, const float* bias, unsigned char* sH,
-                                                   int row)
+// Bias + gelu of the 128 accumulator columns of this thread's lane into its row of the hidden tile.
+__device__ __forceinline__ void tc_hidden_epilogue(uint32_t taddr, const float* bias, unsigned char* sH, int row)
 {
-#pragma unroll
-    for (int q = 0; q < 2; q++) {
+#pragma unroll 1
+    for (int q = 0; q < kHid / 32; q++) {
         float v[32];
-        tmem_ld32(taddr + c0 + q * 32, v);
+        tmem_ld32(taddr + q * 32, v);
 #pragma unroll
         for (int c = 0; c < 4; c++) {
             uint32_t w[4];
 #pragma unroll
             for (int e = 0; e < 4; e++) {
-                const int j = c0 + q * 32 + c * 8 + 2 * e;
+                const int j = q * 32 + c * 8 + 2 * e;
                 w[e] = gelu_bf16x2(v[c * 8 + 2 * e] + bias[j], v[c * 8 + 2 * e + 1] + bias[j + 1]);
             }
-            *reinterpret_cast<uint4*>(sH + core_off(row, (c0 + q * 32) / 8 + c, kHid * 16)) =
-                make_uint4(w[0], w[1], w[2], w[3]);
+            *reinterpret_cast<uint4*>(sH + core_off(row, q * 4 + c, kHid * 16)) = make_uint4(w[0], w[1], w[2], w[3]);
         }
     }
+}
+
+// Named barrier of one slot's 128 threads.
+__device__ __forceinline__ void slot_sync(int slot)
+{
+    asm volatile("bar.sync %0, %1;\n" :: "r"(1 + slot), "r"(kTcRows) : "memory");
+}
+
+// Named barrier returning the AND of `pred` over the slot's threads.
+__device__ __forceinline__ bool slot_and(int slot, bool pred)
+{
+    uint32_t r;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\t"
+                 "bar.red.and.pred q, %2, %3, p;\n\tselp.u32 %0, 1, 0, q;\n\t}\n"
+                 : "=r"(r) : "r"(pred ? 1u : 0u), "r"(1 + slot), "r"(kTcRows) : "memory");
+    return r != 0;
 }
 
 // Neighbour blocks of face f (-1 where none; all -1 past the last face).
@@ -499,7 +518,7 @@ __device__ __forceinline__ float store_patch(const float (&v)[7 * BS], unsigned 
 }
 
 template <int BS>
-__global__ void __launch_bounds__(kTcThreads, 2)
+__global__ void __launch_bounds__(kTcThreads, 1)
     k_learned_apply_tc(int nb, const int* __restrict__ nbr, const float* __restrict__ w, const bf16* __restrict__ tfeat,
                        const bf16* __restrict__ wts, const float* __restrict__ bias, float* __restrict__ x,
                        int* __restrict__ status)
@@ -507,16 +526,17 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     extern __shared__ unsigned char smem_dyn[];
     unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)smem_dyn + 1023) & ~(uintptr_t)1023);
     float* sBias = reinterpret_cast<float*>(sm + kTcSBias);
-    float* sScale = reinterpret_cast<float*>(sm + kTcSScale);
-    uint64_t* mbar_p = reinterpret_cast<uint64_t*>(sm + kTcSMisc);
-    uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(sm + kTcSMisc + 8);
+    uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(sm + kTcSMisc + 8 * kTcSlots);
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int row = tid & (kTcRows - 1);      // face of the tile / TMEM lane
-    const int half = tid >> 7;                // warpgroup: column half of the hidden epilogues
+    const int slot = tid / kTcRows;           // warpgroup = tile pipeline
+    const int row = tid % kTcRows;            // face of the tile / TMEM lane
     const uint32_t s_base = smem_u32(sm);
-    const uint32_t mbar = smem_u32(mbar_p);
+    const uint32_t mbar = smem_u32(sm + kTcSMisc + 8 * slot);
+    unsigned char* sSlot = sm + kTcSlot0 + slot * kTcSlotBytes;
+    const uint32_t sSlot_a = s_base + kTcSlot0 + slot * kTcSlotBytes;
+    float* sScale = reinterpret_cast<float*>(sm + kTcSScale) + slot * kTcRows;
 
-    // Weights into the canonical layout, biases, barrier, TMEM.
+    // Weights into the canonical layout, biases, barriers, TMEM (whole CTA).
     const bf16* gW1 = wts;
     const bf16* gW2 = gW1 + kHid * kIn;
     const bf16* gW3 = gW2 + kHid * kHid;
@@ -533,7 +553,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         *reinterpret_cast<uint4*>(sm + kTcSW3 + core_off(r, c, kHid * 16)) = *reinterpret_cast<const uint4*>(gW3 + r * kHid + 8 * c);
     }
     for (int v = tid; v < 2 * kHid + kOut; v += kTcThreads) sBias[v] = bias[v];
-    if (tid == 0) {
+    if (row == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(mbar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
@@ -546,114 +566,113 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *tmem_holder;
-    const uint32_t t_lane = tmem + ((uint32_t)((warp & 3) * 32) << 16);   // this warp's 32 lanes, column 0
+    const uint32_t tmem = *tmem_holder + (uint32_t)(slot * 128);           // the slot's columns
+    const uint32_t t_lane = tmem + ((uint32_t)((warp & 3) * 32) << 16);    // this warp's 32 lanes
 
     const uint32_t idesc_h = mma_idesc(kTcRows, kHid);
     const uint32_t idesc_o = mma_idesc(kTcRows, kOut);
+    const int ntiles = (nb + kTcRows - 1) / kTcRows;
+    const int stride = gridDim.x * kTcSlots;
     uint32_t phase = 0;
     bool ok = true;
-    const int ntiles = (nb + kTcRows - 1) / kTcRows;
-    // Two-stage prefetch: neighbour lists two tiles ahead, patch values one tile ahead, so that
-    // no dependent load waits inside a tile.
+    // Two-stage prefetch: neighbour lists two tiles ahead, patch values and tensor features one
+    // tile ahead, so that no dependent load waits inside a tile.
     float v[7 * BS];
     int g[kNeighbours];
-    if (half == 0) {
-        load_neighbours(blockIdx.x * kTcRows + row, nb, nbr, g);
-        load_patch<BS>(blockIdx.x * kTcRows + row, nb, g, w, v);
-        load_neighbours((blockIdx.x + gridDim.x) * kTcRows + row, nb, nbr, g);
-    }
-    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int f = tile * kTcRows + row;
-        // 1. inputs of face f (row `row` of the tile): residual slots by warpgroup 0, tensors by 1
-        if (half == 0) {
-            sScale[row] = f < nb ? store_patch<BS>(v, sm + kTcSA, row) : 0.0f;
-        } else {
-            uint4 a = make_uint4(0, 0, 0, 0), b = a;
-            if (f < nb) {
-                const uint4* src = reinterpret_cast<const uint4*>(tfeat + (long long)f * kTensorSlots);
-                a = src[0];
-                b = src[1];
-            }
-            *reinterpret_cast<uint4*>(sm + kTcSA + core_off(row, kResidualSlots / 8, kIn * 16)) = a;
-            *reinterpret_cast<uint4*>(sm + kTcSA + core_off(row, kResidualSlots / 8 + 1, kIn * 16)) = b;
+    uint4 ta, tb;
+    auto load_tensors = [&](int f) {
+        ta = make_uint4(0, 0, 0, 0);
+        tb = ta;
+        if (f < nb) {
+            const uint4* src = reinterpret_cast<const uint4*>(tfeat + (long long)f * kTensorSlots);
+            ta = src[0];
+            tb = src[1];
         }
+    };
+    int tile = blockIdx.x * kTcSlots + slot;
+    load_neighbours(tile * kTcRows + row, nb, nbr, g);
+    load_patch<BS>(tile * kTcRows + row, nb, g, w, v);
+    load_tensors(tile * kTcRows + row);
+    load_neighbours((tile + stride) * kTcRows + row, nb, nbr, g);
+    for (; tile < ntiles && ok; tile += stride) {
+        const int f = tile * kTcRows + row;
+        // 1. inputs of face f into row `row` of the slot's input tile
+        sScale[row] = f < nb ? store_patch<BS>(v, sSlot, row) : 0.0f;
+        *reinterpret_cast<uint4*>(sSlot + core_off(row, kResidualSlots / 8, kIn * 16)) = ta;
+        *reinterpret_cast<uint4*>(sSlot + core_off(row, kResidualSlots / 8 + 1, kIn * 16)) = tb;
         fence_async_smem();
         tc_fence_before();
-        __syncthreads();
-        // 2. layer 1; meanwhile the next tile's patch is loaded
-        if (tid == 0) {
+        slot_sync(slot);
+        // 2. layer 1; meanwhile the next tile's inputs are loaded
+        if (row == 0) {
             tc_fence_after();
 #pragma unroll
             for (int k = 0; k < kIn / 16; k++)
-                tc_mma(tmem, smem_desc(s_base + kTcSA + k * 256, 128, kIn * 16),
-                       smem_desc(s_base + kTcSW1 + k * 256, 128, kIn * 16), idesc_h, k > 0);
+                tc_mma(tmem, smem_desc(sSlot_a + k * 256, 128, kIn * 16), smem_desc(s_base + kTcSW1 + k * 256, 128, kIn * 16),
+                       idesc_h, k > 0);
             tc_commit(mbar);
         }
-        if (half == 0) {
-            load_patch<BS>((tile + gridDim.x) * kTcRows + row, nb, g, w, v);
-            load_neighbours((tile + 2 * gridDim.x) * kTcRows + row, nb, nbr, g);
-        }
-        // every thread leaves together if any wait expired
-        ok = __syncthreads_and(mbar_wait(mbar, phase) ? 1 : 0) != 0;
+        load_patch<BS>((tile + stride) * kTcRows + row, nb, g, w, v);
+        load_tensors((tile + stride) * kTcRows + row);
+        load_neighbours((tile + 2 * stride) * kTcRows + row, nb, nbr, g);
+        ok = slot_and(slot, mbar_wait(mbar, phase));   // the slot leaves together if a wait expired
         phase ^= 1;
         if (!ok) break;
         tc_fence_after();
-        tc_hidden_epilogue(t_lane, 64 * half, sBias, sm + kTcSH, row);
+        tc_hidden_epilogue(t_lane, sBias, sSlot, row);
         fence_async_smem();
         tc_fence_before();
-        __syncthreads();
+        slot_sync(slot);
         // 3. layer 2
-        if (tid == 0) {
+        if (row == 0) {
             tc_fence_after();
 #pragma unroll
             for (int k = 0; k < kHid / 16; k++)
-                tc_mma(tmem, smem_desc(s_base + kTcSH + k * 256, 128, kHid * 16),
-                       smem_desc(s_base + kTcSW2 + k * 256, 128, kHid * 16), idesc_h, k > 0);
+                tc_mma(tmem, smem_desc(sSlot_a + k * 256, 128, kHid * 16), smem_desc(s_base + kTcSW2 + k * 256, 128, kHid * 16),
+                       idesc_h, k > 0);
             tc_commit(mbar);
         }
-        ok = __syncthreads_and(mbar_wait(mbar, phase) ? 1 : 0) != 0;
+        ok = slot_and(slot, mbar_wait(mbar, phase));
         phase ^= 1;
         if (!ok) break;
         tc_fence_after();
-        tc_hidden_epilogue(t_lane, 64 * half, sBias + kHid, sm + kTcSH, row);
+        tc_hidden_epilogue(t_lane, sBias + kHid, sSlot, row);
         fence_async_smem();
         tc_fence_before();
-        __syncthreads();
-        // 4. layer 3 into columns [128, 144)
-        if (tid == 0) {
+        slot_sync(slot);
+        // 4. layer 3 into the slot's first 16 columns
+        if (row == 0) {
             tc_fence_after();
 #pragma unroll
             for (int k = 0; k < kHid / 16; k++)
-                tc_mma(tmem + kHid, smem_desc(s_base + kTcSH + k * 256, 128, kHid * 16),
-                       smem_desc(s_base + kTcSW3 + k * 256, 128, kHid * 16), idesc_o, k > 0);
+                tc_mma(tmem, smem_desc(sSlot_a + k * 256, 128, kHid * 16), smem_desc(s_base + kTcSW3 + k * 256, 128, kHid * 16),
+                       idesc_o, k > 0);
             tc_commit(mbar);
         }
-        ok = __syncthreads_and(mbar_wait(mbar, phase) ? 1 : 0) != 0;
+        ok = slot_and(slot, mbar_wait(mbar, phase));
         phase ^= 1;
         if (!ok) break;
         tc_fence_after();
-        if (half == 0) {
-            float y[16];
-            tmem_ld16(t_lane + kHid, y);
-            if (f < nb) {
-                const float s = sScale[row];
+        float y[16];
+        tmem_ld16(t_lane, y);
+        if (f < nb) {
+            const float sc = sScale[row];
 #pragma unroll
-                for (int c = 0; c < BS; c++) {
-                    const float cv = s * (y[c] + sBias[2 * kHid + c]);
-                    if (isfinite(cv)) x[(long long)f * BS + c] += cv;
-                }
+            for (int c = 0; c < BS; c++) {
+                const float cv = sc * (y[c] + sBias[2 * kHid + c]);
+                if (isfinite(cv)) x[(long long)f * BS + c] += cv;
             }
         }
         tc_fence_before();
-        __syncthreads();
+        slot_sync(slot);
     }
-    if (!ok && tid == 0 && status) atomicExch(status, 1);
+    if (!ok && row == 0 && status) atomicExch(status, 1);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" :: "r"(tmem), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" :: "r"(*tmem_holder), "r"(kTmemCols)
+                     : "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -921,10 +940,9 @@ int launch_learned_apply(int nb, int bs, const int* nbr, const float* w, const v
     if (!learned_supports(bs) || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) return -1;
     const int kk = kernel == kLearnedKernelMmaSync ? 1 : 0;
     if (grid_of[kk][bs][dev] == 0) {
-        // Two CTAs per SM for both kernels: tcgen05 by its TMEM columns (2 x 256 of 512), shared
-        // memory (2 x 97 KB) and registers (<= 128 per thread); mma.sync by its registers
-        // (<= 128 per thread) and shared memory (2 x 70 KB). The shared-memory limit and carveout
-        // are set once here.
+        // tcgen05: one CTA per SM (all 512 TMEM columns, four tile pipelines, 181 KB of shared
+        // memory); mma.sync: two CTAs per SM (registers <= 128 per thread, 2 x 70 KB of shared
+        // memory). The shared-memory limit and carveout are set once here.
         cudaError_t e = cudaErrorInvalidValue;
         int sms = 0;
         if (kk == 1) {
@@ -944,7 +962,7 @@ int launch_learned_apply(int nb, int bs, const int* nbr, const float* w, const v
         }
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess || sms < 1) return -1;
-        grid_of[kk][bs][dev] = 2 * sms;
+        grid_of[kk][bs][dev] = (kk == 1 ? 2 : 1) * sms;
     }
     if (kk == 1) {
         const int tiles = (nb + 15) / 16;
@@ -954,7 +972,7 @@ int launch_learned_apply(int nb, int bs, const int* nbr, const float* w, const v
                                nb, nbr, w, (const bf16*)tfeat, (const bf16*)wts, bias, x));
     } else {
         const int tiles = (nb + kTcRows - 1) / kTcRows;
-        const int grid = std::min(grid_of[kk][bs][dev], tiles);
+        const int grid = std::min(grid_of[kk][bs][dev], (tiles + kTcSlots - 1) / kTcSlots);
         if (grid < 1) return 0;
         FHG_LEARNED_BS(bs, k_learned_apply_tc<BS><<<grid, kTcThreads, kTcSmem, s>>>(
                                nb, nbr, w, (const bf16*)tfeat, (const bf16*)wts, bias, x, status));

@@ -33,7 +33,9 @@ def test_batch_matches_individual_solves(precision):
             assert info.status == 0
             x = p.x()
             r_true = np.linalg.norm(p.b - p.A0 @ x) / np.linalg.norm(p.b)
-            assert info.true_relative_residual == pytest.approx(r_true, rel=1e-6)
+            # ||b - A x|| in FP64 has few significant digits at 1e-8 with a 1e6 coefficient contrast
+            # (cancellation against |A||x|): compare to 1e-11 of ||b||
+            assert info.true_relative_residual == pytest.approx(r_true, rel=1e-3, abs=1e-11)
             assert info.normalized_residual < 1e-8
             if precision == "fp32" and info_ref.iterations > info.iterations:
                 # the individual FP32 solve went on with residual replacement (the device loop
