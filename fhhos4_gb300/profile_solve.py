@@ -1,0 +1,86 @@
+"""Solve one HHO problem a few times inside an NVTX range, for profilers.
+
+    python -m fhhos4_gb300.profile_solve --n 64 --solves 1 [--method learned|fast|plain]
+
+Setup (hierarchy generation, upload, autotuning) and warm-up solves run outside the range
+"solve"; `ncu --nvtx --nvtx-include "solve/" ...` then captures the launches of the timed solves
+only. `--step` instead applies one operator (the learned step, a forward GS sweep, the
+double-FP32 outer product) inside the range.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--dim", type=int, default=3)
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--k", type=int, default=1)
+    ap.add_argument("--method", choices=["learned", "fast", "plain"], default="learned")
+    ap.add_argument("--nu", default="2,2")
+    ap.add_argument("--solves", type=int, default=1)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--step", choices=["", "learned_tcgen05", "learned_mma_sync", "gs_fp32", "outer_df"], default="")
+    a = ap.parse_args()
+
+    import torch
+    from . import _native as N
+    from . import hho
+    from . import learned as LN
+
+    H = hho.Hierarchy(a.dim, a.n, a.k)
+    As = [H.A(l) for l in range(H.levels)]
+    Ps = [H.P(l) for l in range(H.levels - 1)]
+    b, bs = H.b(), H.block_size
+    ctx = N.Context(0)
+    for l, A in enumerate(As):
+        ctx.set_level(l, bs, A)
+    for l, P in enumerate(Ps):
+        ctx.set_prolongation(l, P)
+    ctx.set_face_tensors(H.face_tensors(0))
+    H.close()
+    o = N.default_options()
+    o.vcycle_precision = N.PRECISION["fp32"]
+    o.autotune = 1
+    ctx.setup(len(As), o)
+    npre, npost = (int(v) for v in a.nu.split(","))
+    params = LN.load_params()[0]
+    if a.method == "plain":
+        ctx.set_cycle("bgs", "rbgs", 1, 1, 1)
+        ctx.set_vcycle_precision("fp64")
+    else:
+        ctx.set_cycle("bgs", "rbgs", npre, npost, 1)
+        if a.method == "learned" and bs <= 4:
+            ctx.set_learned(params, "fallback")
+    bd = torch.from_numpy(b).cuda()
+    xd = torch.empty_like(bd)
+    torch.cuda.synchronize()
+    out = {}
+    if a.step:
+        op, prec = {"learned_tcgen05": (N.OP_LEARNED_STEP, "fp32"), "learned_mma_sync": (N.OP_LEARNED_STEP, "fp32"),
+                    "gs_fp32": (N.OP_GS_FORWARD, "fp32"), "outer_df": (N.OP_SYM_SPMV, "fp32")}[a.step]
+        if a.step.startswith("learned"):
+            ctx.set_learned(params, "always", kernel=a.step.split("_", 1)[1])
+        ctx.time_op(0, op, prec, warmup=a.warmup, reps=1)
+        torch.cuda.nvtx.range_push("solve")
+        out["ms"] = ctx.time_op(0, op, prec, warmup=0, reps=a.solves)
+        torch.cuda.nvtx.range_pop()
+    else:
+        for _ in range(a.warmup):
+            ctx.solve_device(bd.data_ptr(), xd.data_ptr(), 200)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("solve")
+        for _ in range(a.solves):
+            rc, hist, info = ctx.solve_device(bd.data_ptr(), xd.data_ptr(), 200)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        out = {"rc": rc, "iterations": info.iterations, "ms": info.solve_ms,
+               "learned_iterations": info.learned_iterations}
+    print(json.dumps(out), flush=True)
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()
