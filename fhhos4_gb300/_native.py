@@ -31,6 +31,7 @@ PRECISION = {"fp64": 0, "fp32": 1}
 OP_SPMV, OP_RESIDUAL, OP_RESTRICT, OP_PROLONG_ADD = 0, 1, 2, 3
 OP_GS_FORWARD, OP_GS_BACKWARD, OP_JACOBI, OP_SYM_SPMV = 4, 5, 6, 7
 OP_COARSE_SOLVE, OP_VCYCLE, OP_VCYCLE_LEARNED, OP_LEARNED_STEP = 8, 9, 10, 11
+CYCLE_K = -1   # fhg_options.w_loops / set_cycle: the K-cycle
 LEARNED = {"off": 0, "fallback": 1, "always": 2}
 LEARNED_MMA_SYNC = 16
 LEARNED_PARAMS = 24848

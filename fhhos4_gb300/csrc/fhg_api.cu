@@ -73,6 +73,8 @@ struct Level {
     int* perm_d = nullptr;
     double *x = nullptr, *b = nullptr, *r = nullptr;
     float *x32 = nullptr, *b32 = nullptr, *r32 = nullptr;
+    double* kv64[4] = {nullptr, nullptr, nullptr, nullptr};  // K-cycle c, A c, d, A d (levels 1..L-2)
+    float* kv32[4] = {nullptr, nullptr, nullptr, nullptr};
     double* cinv = nullptr;  // coarsest only, n x n row-major
     long long p_blocks = 0;
 };
@@ -720,6 +722,7 @@ template <> struct LevelVecs<double> {
     static const BsrView<double>& P(Level& L) { return L.P.v; }
     static const BsrView<double>& R(Level& L) { return L.R.v; }
     static const double* dinv(Level& L) { return L.dinv; }
+    static double* k(Level& L, int i) { return L.kv64[i]; }
 };
 template <> struct LevelVecs<float> {
     static float* x(Level& L) { return L.x32; }
@@ -729,6 +732,7 @@ template <> struct LevelVecs<float> {
     static const BsrView<float>& P(Level& L) { return L.P32.v; }
     static const BsrView<float>& R(Level& L) { return L.R32.v; }
     static const float* dinv(Level& L) { return L.dinv32; }
+    static float* k(Level& L, int i) { return L.kv32[i]; }
 };
 
 // `from_zero`: x holds zeros on entry (the pre-smoothing of a V-cycle), so the first GS sweep
@@ -788,9 +792,62 @@ void learned_step(fhg_ctx* ctx, const float* b, float* x)
                               ctx->learned_kernel, s);
 }
 
+template <class T>
+void mg_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero);
+
+// Dot products a_q . b_q (q < nq) on the device, summed on the host in a fixed order (one
+// read-back: the K-cycle's branch is decided on the host).
+template <class T>
+void host_dots(fhg_ctx* ctx, long long n, int nq, const T* a0, const T* b0, const T* a1, const T* b1, const T* a2,
+               const T* b2, double* out)
+{
+    double* p = ctx->partials + (size_t)5 * fhg::kReduceCtas;  // parts 5-7: free inside a cycle
+    fhg::launch_dots3<T>(n, nq, a0, b0, a1, b1, a2, b2, p, ctx->stream);
+    std::vector<double> h((size_t)3 * fhg::kReduceCtas);
+    cudaMemcpyAsync(h.data(), p, sizeof(double) * nq * fhg::kReduceCtas, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    for (int q = 0; q < nq; q++) {
+        double t = 0.0;
+        for (int i = 0; i < fhg::kReduceCtas; i++) t += h[(size_t)q * fhg::kReduceCtas + i];
+        out[q] = t;
+    }
+}
+
+// Multigrid::FCGForKCycle (src/Solver/Multigrid/Multigrid.h:611-656): x = the coarse correction
+// on level m from two FCG steps preconditioned by the cycle on level m, the second only when the
+// first reduced ||r|| by less than t = 0.25. r is overwritten (r -= (alpha1 / rho1) A c).
+template <class T>
+void kcycle_fcg(fhg_ctx* ctx, int m, T* r, T* x)
+{
+    Level& L = ctx->levels[m];
+    using V = LevelVecs<T>;
+    cudaStream_t s = ctx->stream;
+    const long long n = L.n;
+    T *c = V::k(L, 0), *v = V::k(L, 1), *d = V::k(L, 2), *w = V::k(L, 3);
+    mg_cycle<T>(ctx, m, r, c, true);
+    fhg::launch_spmv<T>(V::A(L), fhg::kSpmvAssign, c, nullptr, v, s);
+    double q[3];
+    host_dots<T>(ctx, n, 3, c, v, c, r, r, r, q);
+    const double rho1 = q[0], alpha1 = q[1], norm_old = std::sqrt(q[2]);
+    fhg::launch_axpy<T>(n, -(alpha1 / rho1), v, r, s);
+    host_dots<T>(ctx, n, 1, r, r, (const T*)nullptr, (const T*)nullptr, (const T*)nullptr, (const T*)nullptr, q);
+    const double norm_new = std::sqrt(q[0]);
+    if (norm_new <= 0.25 * norm_old) {
+        fhg::launch_lincomb<T>(n, alpha1 / rho1, c, 0.0, c, x, s);
+        return;
+    }
+    mg_cycle<T>(ctx, m, r, d, true);
+    fhg::launch_spmv<T>(V::A(L), fhg::kSpmvAssign, d, nullptr, w, s);
+    host_dots<T>(ctx, n, 3, d, v, d, w, d, r, q);
+    const double gamma = q[0], beta = q[1], alpha2 = q[2];
+    const double rho2 = beta - gamma * gamma / rho1;
+    fhg::launch_lincomb<T>(n, alpha1 / rho1 - gamma * alpha2 / (rho1 * rho2), c, alpha2 / rho2, d, x, s);
+}
+
 // One multigrid cycle on level l (src/Solver/Multigrid/Multigrid.h:438-608): V for w_loops = 1,
-// W for 2 (the coarse correction repeated, except directly above the coarsest level). x is the
-// initial guess, zero when x_zero.
+// W for 2 (the coarse correction repeated, except directly above the coarsest level), K for
+// FHG_CYCLE_K (kcycle_fcg on the coarser level unless that is the coarsest). x is the initial
+// guess, zero when x_zero.
 template <class T>
 void mg_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
 {
@@ -809,10 +866,14 @@ void mg_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
     smooth<T>(ctx, l, pre, ctx->opts.pre_iterations, b, x, gs_zero);
     fhg::launch_spmv<T>(V::A(L), fhg::kSpmvResidual, x, b, V::r(L), s);
     fhg::launch_spmv<T>(V::R(L), fhg::kSpmvAssign, V::r(L), nullptr, V::b(C), s);
-    const int loops = ctx->opts.w_loops > 1 ? ctx->opts.w_loops : 1;
-    for (int w = 0; w < loops; w++) {
-        mg_cycle<T>(ctx, l + 1, V::b(C), V::x(C), w == 0);
-        if (l + 1 == ctx->nlevels - 1) break;
+    if (ctx->opts.w_loops == FHG_CYCLE_K && l + 1 < ctx->nlevels - 1) {
+        kcycle_fcg<T>(ctx, l + 1, V::b(C), V::x(C));
+    } else {
+        const int loops = ctx->opts.w_loops > 1 ? ctx->opts.w_loops : 1;
+        for (int w = 0; w < loops; w++) {
+            mg_cycle<T>(ctx, l + 1, V::b(C), V::x(C), w == 0);
+            if (l + 1 == ctx->nlevels - 1) break;
+        }
     }
     fhg::launch_spmv<T>(V::P(L), fhg::kSpmvAddTo, V::x(C), x, x, s);
     smooth<T>(ctx, l, ctx->opts.post_smoother, ctx->opts.post_iterations, b, x);
@@ -1068,11 +1129,13 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
     // variable preconditioner).
     bool learned = ctx->learned_mode != FHG_LEARNED_OFF && ctx->lwts && ctx->opts.krylov == FHG_KRYLOV_FCG &&
                    ctx->opts.vcycle_precision == FHG_PREC_FP32;
-    if (ctx->opts.use_graphs && !ctx->graphs_built) {
+    // The K-cycle decides its second coarse FCG step on the host: no graph replay then.
+    const bool graphs = ctx->opts.use_graphs && ctx->opts.w_loops != FHG_CYCLE_K;
+    if (graphs && !ctx->graphs_built) {
         int rc = build_graphs(ctx, false);
         if (rc) return rc;
     }
-    if (learned && ctx->opts.use_graphs && !ctx->graphs_l_built) {
+    if (learned && graphs && !ctx->graphs_l_built) {
         int rc = build_graphs(ctx, true);
         if (rc) return rc;
     }
@@ -1086,7 +1149,7 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
     while (true) {
         while (!(it > 0 && (it >= maxit || nr < ctx->opts.tolerance))) {
             const int p = it & 1;
-            if (ctx->opts.use_graphs) {
+            if (graphs) {
                 const int g = ctx->opts.krylov == FHG_KRYLOV_CG ? 0 : p;
                 CK(cudaGraphLaunch(learned ? ctx->graph_l[g] : ctx->graph[g], s));
                 fhg::g_kernel_launches += learned ? ctx->graph_l_kernels[g] : ctx->graph_kernels[g];
@@ -1308,7 +1371,7 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         return fail(ctx, FHG_ERR_INVALID_ARG, "negative iteration count");
     if (o.pre_smoother < 0 || o.pre_smoother > 6 || o.post_smoother < 0 || o.post_smoother > 6)
         return fail(ctx, FHG_ERR_INVALID_ARG, "unknown smoother code");
-    if (o.w_loops < 1) o.w_loops = 1;
+    if (o.w_loops < 1 && o.w_loops != FHG_CYCLE_K) o.w_loops = 1;
     if (o.galerkin && nlevels > 0 && nlevels <= 64 && (int)ctx->levels.size() < nlevels) ctx->levels.resize(nlevels);
     if (nlevels <= 0 || nlevels > (int)ctx->levels.size())
         return fail(ctx, FHG_ERR_INVALID_ARG, "nlevels=%d but %zu levels were given", nlevels, ctx->levels.size());
@@ -1473,6 +1536,11 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         if ((rc = dalloc(ctx, &L.x, L.n)) || (rc = dalloc(ctx, &L.b, L.n)) || (rc = dalloc(ctx, &L.r, L.n))) return rc;
         if (fp32 && ((rc = dalloc(ctx, &L.x32, L.n)) || (rc = dalloc(ctx, &L.b32, L.n)) || (rc = dalloc(ctx, &L.r32, L.n))))
             return rc;
+        if (l > 0 && l < nlevels - 1)  // K-cycle vectors (the K-cycle runs FCG on levels 1..L-2)
+            for (int i = 0; i < 4; i++) {
+                if ((rc = dalloc(ctx, &L.kv64[i], L.n))) return rc;
+                if (fp32 && (rc = dalloc(ctx, &L.kv32[i], L.n))) return rc;
+            }
     }
     const long long n0 = ctx->levels[0].n;
     if ((rc = dalloc(ctx, &ctx->kx, n0)) || (rc = dalloc(ctx, &ctx->kr, n0)) || (rc = dalloc(ctx, &ctx->kb, n0)) ||
@@ -1806,7 +1874,7 @@ int fhg_set_cycle(fhg_ctx* ctx, int pre_smoother, int post_smoother, int pre_ite
     if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
     if (pre_smoother < 0 || pre_smoother > 6 || post_smoother < 0 || post_smoother > 6)
         return fail(ctx, FHG_ERR_INVALID_ARG, "unknown smoother code");
-    if (pre_iterations < 0 || post_iterations < 0 || w_loops < 1)
+    if (pre_iterations < 0 || post_iterations < 0 || (w_loops < 1 && w_loops != FHG_CYCLE_K))
         return fail(ctx, FHG_ERR_INVALID_ARG, "negative smoothing count or cycle loops < 1");
     free_graphs(ctx);
     ctx->rho_plain = 0.0;  // the plain method's reduction is measured again for the new cycle
@@ -2377,6 +2445,8 @@ int fhg_batch_add(fhg_batch* batch, fhg_ctx* ctx)
     if (!ctx->ready) return batch_fail(batch, FHG_ERR_NOT_READY, "the context has not been set up");
     if (ctx->device != batch->device) return batch_fail(batch, FHG_ERR_INVALID_ARG, "context on device %d, batch on %d", ctx->device, batch->device);
     if (ctx->opts.krylov != FHG_KRYLOV_FCG) return batch_fail(batch, FHG_ERR_UNSUPPORTED, "the batched solve runs FCG");
+    if (ctx->opts.w_loops == FHG_CYCLE_K)
+        return batch_fail(batch, FHG_ERR_UNSUPPORTED, "the K-cycle decides on the host: not in a batched solve");
     if (ctx->learned_mode != FHG_LEARNED_OFF) return batch_fail(batch, FHG_ERR_UNSUPPORTED, "the batched solve runs the plain V-cycle");
     for (fhg_ctx* c : batch->probs)
         if (c == ctx) return batch_fail(batch, FHG_ERR_INVALID_ARG, "context added twice");

@@ -92,6 +92,15 @@ void launch_cg_step(long long n, double* x, double* r, const double* d, const do
 
 template <class Tin, class Tout>
 void launch_convert(long long n, const Tin* in, Tout* out, cudaStream_t s);
+// K-cycle: partials[q * kReduceCtas ..] of a_q . b_q for q < nq (FP64 accumulation); y += alpha x;
+// out = a c + b d.
+template <class T>
+void launch_dots3(long long n, int nq, const T* a0, const T* b0, const T* a1, const T* b1, const T* a2, const T* b2,
+                  double* partials, cudaStream_t s);
+template <class T>
+void launch_axpy(long long n, double alpha, const T* x, T* y, cudaStream_t s);
+template <class T>
+void launch_lincomb(long long n, double a, const T* c, double b, const T* d, T* out, cudaStream_t s);
 // Device-side solve loop: b0 = a0 and b1 = a1; solve scalars and iteration counter at their start
 // values; the WHILE-node condition from ||r||/||b|| (nr), the counter, tol and maxit.
 void launch_copy2(long long n, const double* a0, double* b0, const double* a1, double* b1, cudaStream_t s);

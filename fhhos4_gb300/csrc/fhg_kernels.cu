@@ -491,6 +491,49 @@ __global__ void __launch_bounds__(kReduceThreads) k_dot(long long n, const doubl
     if (threadIdx.x == 0) partials[blockIdx.x] = v;
 }
 
+// Up to three dot products in one pass (K-cycle): partials[q * kReduceCtas + cta] of a_q . b_q,
+// FP64 accumulation whatever T.
+template <class T>
+__global__ void __launch_bounds__(kReduceThreads) k_dots3(long long n, int nq, const T* __restrict__ a0,
+                                                          const T* __restrict__ b0, const T* __restrict__ a1,
+                                                          const T* __restrict__ b1, const T* __restrict__ a2,
+                                                          const T* __restrict__ b2, double* __restrict__ partials)
+{
+    __shared__ double sh[33];
+    double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads) {
+        v0 = fma((double)a0[i], (double)b0[i], v0);
+        if (nq > 1) v1 = fma((double)a1[i], (double)b1[i], v1);
+        if (nq > 2) v2 = fma((double)a2[i], (double)b2[i], v2);
+    }
+    v0 = block_sum(v0, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v0;
+    if (nq > 1) {
+        v1 = block_sum(v1, sh);
+        if (threadIdx.x == 0) partials[kReduceCtas + blockIdx.x] = v1;
+    }
+    if (nq > 2) {
+        v2 = block_sum(v2, sh);
+        if (threadIdx.x == 0) partials[2 * kReduceCtas + blockIdx.x] = v2;
+    }
+}
+
+// y += alpha x; out = a c + b d (K-cycle updates, coefficients from the host).
+template <class T>
+__global__ void k_axpy(long long n, double alpha, const T* __restrict__ x, T* __restrict__ y)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        y[i] = y[i] + (T)alpha * x[i];
+}
+
+template <class T>
+__global__ void k_lincomb(long long n, double a, const T* __restrict__ c, double b, const T* __restrict__ d,
+                          T* __restrict__ out)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (T)a * c[i] + (T)b * d[i];
+}
+
 __global__ void __launch_bounds__(kReduceThreads) k_dot_mixed(long long n, const float* __restrict__ a,
                                                               const double* __restrict__ b, double* __restrict__ partials)
 {
@@ -758,6 +801,40 @@ void launch_dot(long long n, const double* a, const double* b, double* partials,
     k_dot<<<kReduceCtas, kReduceThreads, 0, s>>>(n, a, b, partials);
     g_kernel_launches++;
 }
+
+template <class T>
+void launch_dots3(long long n, int nq, const T* a0, const T* b0, const T* a1, const T* b1, const T* a2, const T* b2,
+                  double* partials, cudaStream_t s)
+{
+    k_dots3<T><<<kReduceCtas, kReduceThreads, 0, s>>>(n, nq, a0, b0, a1 ? a1 : a0, b1 ? b1 : b0, a2 ? a2 : a0,
+                                                      b2 ? b2 : b0, partials);
+    g_kernel_launches++;
+}
+
+template <class T>
+void launch_axpy(long long n, double alpha, const T* x, T* y, cudaStream_t s)
+{
+    const long long blocks = std::min<long long>((n + 255) / 256, 4 * 152);
+    k_axpy<T><<<(unsigned)std::max<long long>(blocks, 1), 256, 0, s>>>(n, alpha, x, y);
+    g_kernel_launches++;
+}
+
+template <class T>
+void launch_lincomb(long long n, double a, const T* c, double b, const T* d, T* out, cudaStream_t s)
+{
+    const long long blocks = std::min<long long>((n + 255) / 256, 4 * 152);
+    k_lincomb<T><<<(unsigned)std::max<long long>(blocks, 1), 256, 0, s>>>(n, a, c, b, d, out);
+    g_kernel_launches++;
+}
+
+template void launch_dots3<double>(long long, int, const double*, const double*, const double*, const double*,
+                                   const double*, const double*, double*, cudaStream_t);
+template void launch_dots3<float>(long long, int, const float*, const float*, const float*, const float*, const float*,
+                                  const float*, double*, cudaStream_t);
+template void launch_axpy<double>(long long, double, const double*, double*, cudaStream_t);
+template void launch_axpy<float>(long long, double, const float*, float*, cudaStream_t);
+template void launch_lincomb<double>(long long, double, const double*, double, const double*, double*, cudaStream_t);
+template void launch_lincomb<float>(long long, double, const float*, double, const float*, float*, cudaStream_t);
 
 void launch_fcg_direction(long long n, const double* z, const double* dp, const double* partials_zadp,
                           const double* dadp, double* d, cudaStream_t s)

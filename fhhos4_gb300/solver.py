@@ -101,8 +101,8 @@ class Multigrid(IterativeSolver):
         return self._nLevels
 
     def _check_supported(self):
-        if self.Cycle not in ("V", "W"):
-            raise NotImplementedError("V- and W-cycles run on the GPU (Cycle='V' or 'W')")
+        if self.Cycle not in ("V", "W", "K"):
+            raise NotImplementedError("V-, W- and K-cycles run on the GPU (Cycle='V', 'W' or 'K')")
         if self.Cycle == "W" and self.WLoops < 2:
             self.WLoops = 2
         for code in (self.PreSmootherCode, self.PostSmootherCode):
@@ -150,7 +150,7 @@ class _KrylovOnGpu(IterativeSolver):
         o.autotune = 1 if mg.Autotune else 0
         o.max_coarse_rows = mg.MaxCoarseRows
         o.outer_split = 1 if self.OuterSplit else 0
-        o.w_loops = mg.WLoops if mg.Cycle == "W" else 1
+        o.w_loops = N.CYCLE_K if mg.Cycle == "K" else (mg.WLoops if mg.Cycle == "W" else 1)
         o.galerkin = 1 if mg.UseGalerkinOperator else 0
         return o
 

@@ -51,6 +51,8 @@ extern "C" {
 
 /* V-cycle precision: FP64 everywhere, or FP32 smoothers/transfers/operators inside the
  * FP64 Krylov iteration with an FP64 coarsest solve. */
+#define FHG_CYCLE_K (-1)   /* fhg_options.w_loops / fhg_set_cycle: the K-cycle */
+
 #define FHG_PREC_FP64 0
 #define FHG_PREC_FP32 1
 
@@ -84,7 +86,11 @@ typedef struct {
     int outer_split;            /* FP32 V-cycle only: 1 = the outer FCG operator product in double-FP32
                                    arithmetic (FP32 pairs, ~2^-47 relative per term, on the FP32 pipe);
                                    0 = native FP64. GB300's FP64 pipe is 56x slower than FP32. */
-    int w_loops;                /* Multigrid::WLoops: 1 = V-cycle, 2 = W-cycle ("-cycle W,..", main.cpp:1179-1215) */
+    int w_loops;                /* Multigrid::WLoops: 1 = V-cycle, 2 = W-cycle ("-cycle W,..", main.cpp:1179-1215);
+                                   FHG_CYCLE_K = K-cycle ("-cycle K,..", Multigrid.h:523-537,611-656: two FCG steps
+                                   on every coarse level but the coarsest, the second only when the first reduced
+                                   the residual by less than 0.25; decided on the host, so solves do not replay
+                                   CUDA graphs) */
     int galerkin;               /* Multigrid::UseGalerkinOperator ("-g 1", main.cpp:1307): coarse operators
                                    A_{l+1} = P_l^T A_l P_l formed at setup (Level.h:133-137); operators given
                                    for levels >= 1 are then not needed and are replaced */

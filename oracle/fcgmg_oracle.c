@@ -379,6 +379,10 @@ typedef struct {
     double** rc;
     double** ec;
     double** tmp;
+    double** kc;  /* K-cycle: per-level c, A c, d, A d */
+    double** kv;
+    double** kd;
+    double** kw;
 } orc_mg;
 
 /* One smoother application of `iters` iterations: BlockGaussSeidel::ExecuteOneIteration's
@@ -401,9 +405,44 @@ static void smooth(orc_mg* mg, int l, int code, int iters, const double* b, doub
     }
 }
 
-/* Multigrid::MultigridCycle (Multigrid.h:438-608) for V (WLoops 1) and W (WLoops 2): x is the
+static void cycle(orc_mg* mg, int l, const double* b, double* x, int x_zero);
+
+static double dot(const double* a, const double* b, int n)
+{
+    double s = 0.0;
+    for (int i = 0; i < n; i++) s += a[i] * b[i];
+    return s;
+}
+
+/* Multigrid::FCGForKCycle (Multigrid.h:611-656): x = the coarse correction on level m from two
+ * FCG steps preconditioned by the cycle on level m, the second only when the first reduced ||r||
+ * by less than t = 0.25. r is overwritten (r -= (alpha1 / rho1) A c). */
+static void kcycle_fcg(orc_mg* mg, int m, double* r, double* x)
+{
+    const int n = mg->A[m].n_rows;
+    double *c = mg->kc[m], *v = mg->kv[m], *d = mg->kd[m], *w = mg->kw[m];
+    cycle(mg, m, r, c, 1);
+    orc_spmv(&mg->A[m], c, v);
+    const double rho1 = dot(c, v, n), alpha1 = dot(c, r, n);
+    const double norm_old = sqrt(dot(r, r, n));
+    for (int i = 0; i < n; i++) r[i] -= (alpha1 / rho1) * v[i];
+    const double norm_new = sqrt(dot(r, r, n));
+    if (norm_new <= 0.25 * norm_old) {
+        for (int i = 0; i < n; i++) x[i] = (alpha1 / rho1) * c[i];
+        return;
+    }
+    cycle(mg, m, r, d, 1);
+    orc_spmv(&mg->A[m], d, w);
+    const double gamma = dot(d, v, n), beta = dot(d, w, n), alpha2 = dot(d, r, n);
+    const double rho2 = beta - gamma * gamma / rho1;
+    const double a = alpha1 / rho1 - gamma * alpha2 / (rho1 * rho2), bb = alpha2 / rho2;
+    for (int i = 0; i < n; i++) x[i] = a * c[i] + bb * d[i];
+}
+
+/* Multigrid::MultigridCycle (Multigrid.h:438-608) for V (WLoops 1), W (WLoops 2) and K: x is the
  * initial guess (zero when x_zero); the coarse correction loops WLoops times except directly
- * above the coarsest level. */
+ * above the coarsest level, or (K) is kcycle_fcg on the coarser level unless that is the
+ * coarsest. */
 static void cycle(orc_mg* mg, int l, const double* b, double* x, int x_zero)
 {
     int n = mg->A[l].n_rows;
@@ -417,10 +456,14 @@ static void cycle(orc_mg* mg, int l, const double* b, double* x, int x_zero)
     orc_spmv(&mg->R[l], mg->r[l], mg->rc[l]);
     int nc = mg->A[l + 1].n_rows;
     memset(mg->ec[l], 0, sizeof(double) * (size_t)nc);
-    const int loops = mg->opt->w_loops > 1 ? mg->opt->w_loops : 1;
-    for (int w = 0; w < loops; w++) {
-        cycle(mg, l + 1, mg->rc[l], mg->ec[l], w == 0);
-        if (l + 1 == mg->nlevels - 1) break;
+    if (mg->opt->w_loops == ORC_CYCLE_K && l + 1 < mg->nlevels - 1) {
+        kcycle_fcg(mg, l + 1, mg->rc[l], mg->ec[l]);
+    } else {
+        const int loops = mg->opt->w_loops > 1 ? mg->opt->w_loops : 1;
+        for (int w = 0; w < loops; w++) {
+            cycle(mg, l + 1, mg->rc[l], mg->ec[l], w == 0);
+            if (l + 1 == mg->nlevels - 1) break;
+        }
     }
     orc_spmv(&mg->P[l], mg->ec[l], mg->r[l]);
     for (int i = 0; i < n; i++) x[i] += mg->r[l][i];
@@ -428,13 +471,6 @@ static void cycle(orc_mg* mg, int l, const double* b, double* x, int x_zero)
 }
 
 static void vcycle(orc_mg* mg, int l, const double* b, double* x) { cycle(mg, l, b, x, 1); }
-
-static double dot(const double* a, const double* b, int n)
-{
-    double s = 0.0;
-    for (int i = 0; i < n; i++) s += a[i] * b[i];
-    return s;
-}
 
 static double g_setup_s = 0.0, g_iter_s = 0.0;
 
@@ -459,6 +495,17 @@ int orc_fcgmg_solve(int nlevels, int bs, const orc_csr* A, const orc_csr* P,
     mg.rc = (double**)calloc((size_t)nlevels, sizeof(double*));
     mg.ec = (double**)calloc((size_t)nlevels, sizeof(double*));
     mg.tmp = (double**)calloc((size_t)nlevels, sizeof(double*));
+    mg.kc = (double**)calloc((size_t)nlevels, sizeof(double*));
+    mg.kv = (double**)calloc((size_t)nlevels, sizeof(double*));
+    mg.kd = (double**)calloc((size_t)nlevels, sizeof(double*));
+    mg.kw = (double**)calloc((size_t)nlevels, sizeof(double*));
+    for (int l = 0; l < nlevels; l++) {
+        const size_t nl = (size_t)A[l].n_rows;
+        mg.kc[l] = (double*)malloc(sizeof(double) * nl);
+        mg.kv[l] = (double*)malloc(sizeof(double) * nl);
+        mg.kd[l] = (double*)malloc(sizeof(double) * nl);
+        mg.kw[l] = (double*)malloc(sizeof(double) * nl);
+    }
     for (int l = 0; l + 1 < nlevels; l++) {
         int nnz = P[l].rowptr[P[l].n_rows];
         int* rp = (int*)malloc(sizeof(int) * (size_t)(P[l].n_cols + 1));
@@ -549,6 +596,8 @@ int orc_fcgmg_solve(int nlevels, int bs, const orc_csr* A, const orc_csr* P,
         free(mg.r[l]); free(mg.tmp[l]); free(mg.rc[l]); free(mg.ec[l]);
     }
     free(mg.coarse.L); free(mg.coarse.d);
+    for (int l = 0; l < nlevels; l++) { free(mg.kc[l]); free(mg.kv[l]); free(mg.kd[l]); free(mg.kw[l]); }
+    free(mg.kc); free(mg.kv); free(mg.kd); free(mg.kw);
     free(mg.R); free(mg.D); free(mg.r); free(mg.rc); free(mg.ec); free(mg.tmp);
     return rc;
 }

@@ -32,8 +32,9 @@ typedef struct {
     int krylov;                        /* ORC_KRYLOV_FCG (FCG(1)) or ORC_KRYLOV_CG */
     double tolerance;
     int max_iterations;
-    int w_loops;                       /* Multigrid::WLoops: 1 V-cycle, 2 W-cycle */
+    int w_loops;                       /* Multigrid::WLoops: 1 V-cycle, 2 W-cycle; ORC_CYCLE_K: K-cycle */
 } orc_options;
+#define ORC_CYCLE_K (-1)
 
 /* y = A x, one sequential sum per row in column order (Eigen SparseDenseProduct.h:34-70). */
 void orc_spmv(const orc_csr* A, const double* x, double* y);

@@ -160,7 +160,8 @@ def fcgmg_solve(As, Ps, b, bs, pre="bgs", post="rbgs", krylov="fcg", tol=1e-8, m
     pc, om = SMOOTHER_CODES[pre]
     qc, om2 = SMOOTHER_CODES[post]
     opts = _Opts(pc, qc, om if pc == BJ else om2, pre_iterations, post_iterations,
-                 KRYLOV_CG if krylov == "cg" else KRYLOV_FCG, tol, maxit, 2 if cycle == "W" else 1)
+                 KRYLOV_CG if krylov == "cg" else KRYLOV_FCG, tol, maxit,
+                 2 if cycle == "W" else (-1 if cycle == "K" else 1))
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.zeros(As[0].shape[0])
     hist = np.zeros(maxit + 1)

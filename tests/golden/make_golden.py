@@ -10,11 +10,12 @@ checkout by ``make -C oracle ref``) and stores, per case, in a compressed .npz:
   colouring, and the reference's own classes re-run on the colour-permuted
   hierarchy (``hist_colour``, ``x_colour`` in the permuted numbering), for
   block GS (bgs/rbgs), block Jacobi (bj23), PCG (``cg``), the W-cycle (``w``), symmetric block
-  GS (``sbgs``) and alternating block GS (``abgs``/``rabgs``).
+  GS (``sbgs``) and alternating block GS (``abgs``/``rabgs``); ``--add-k-cycle`` adds the K-cycle
+  (``hist_k``, ``x_k``) to existing full cases.
 
 Only ``hist_*`` summaries are kept for the large cases (``--histories-only``).
 
-Usage:  python tests/golden/make_golden.py [case ...] [--histories-only]
+Usage:  python tests/golden/make_golden.py [case ...] [--histories-only | --add-k-cycle]
 """
 from __future__ import annotations
 
@@ -133,8 +134,34 @@ def make_case(name, dim, n, k, histories_only=False):
               f"size={os.path.getsize(path)/1e6:.2f} MB", flush=True)
 
 
+def add_k_cycle(name):
+    """Add the reference's K-cycle (FCG(1) + K,1,1, bgs/rbgs; Multigrid.h:523-537,611-656) on the
+    stored colour-permuted hierarchy of a full case: hist_k, x_k."""
+    path = os.path.join(GOLDEN, name + ".npz")
+    with np.load(path) as z:
+        data = {k: z[k] for k in z.files}
+    nl = int(data["levels"])
+    bs = int(data["block_size"])
+    As = [sp.csr_matrix((data[f"A{l}_data"], data[f"A{l}_indices"], data[f"A{l}_indptr"])) for l in range(nl)]
+    Ps = [sp.csr_matrix((data[f"P{l}_data"], data[f"P{l}_indices"], data[f"P{l}_indptr"]),
+                        shape=tuple(data[f"P{l}_shape"])) for l in range(nl - 1)]
+    perms = [data[f"perm{l}"] for l in range(nl)]
+    Ac, Pc, bc = O.permute_hierarchy(As, Ps, data["b"], bs, perms)
+    with tempfile.TemporaryDirectory() as tmp:
+        hist_k, x_k = ref_solve(Ac, Pc, bc, bs, os.path.join(tmp, "k"), cycle="K")
+    data.update(hist_k=hist_k, x_k=x_k)
+    np.savez_compressed(path, **data)
+    print(f"{name}: K-cycle iterations {len(hist_k) - 1}", flush=True)
+
+
 def main(argv):
     histories_only = "--histories-only" in argv
+    if "--add-k-cycle" in argv:
+        if not os.path.exists(O.REF_DRIVER):
+            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+        for name in [a for a in argv if not a.startswith("--")] or list(CASES):
+            add_k_cycle(name)
+        return
     names = [a for a in argv if not a.startswith("--")]
     table = dict(CASES, **LARGE)
     if not names:

@@ -94,7 +94,7 @@ def test_pcg_mg_matches_reference(case):
 
 
 @pytest.mark.parametrize("variant,pre,post,cycle", [("w", "bgs", "rbgs", "W"), ("sbgs", "sbgs", "sbgs", "V"),
-                                                   ("abgs", "abgs", "rabgs", "V")])
+                                                   ("abgs", "abgs", "rabgs", "V"), ("k", "bgs", "rbgs", "K")])
 def test_cycles_and_smoothers_match_reference(case, variant, pre, post, cycle):
     solver = S().fcg_mg(case.As, case.Ps, case.bs, pre=pre, post=post, cycle=cycle)
     x = solver.Solve(case.b)
@@ -104,6 +104,16 @@ def test_cycles_and_smoothers_match_reference(case, variant, pre, post, cycle):
     sp_ = scalar_perm(case.perms[0], case.bs)
     xr = case[f"x_{variant}"]
     assert np.linalg.norm(x[sp_] - xr) / np.linalg.norm(xr) < X_RTOL
+
+
+def test_kcycle_with_fp32_vcycle_reaches_fp64_tolerance(case):
+    """K-cycle with FP32 cycles inside the FP64 FCG: the FP64 true residual meets 1e-8 within a few
+    iterations of the reference's FP64 K-cycle."""
+    solver = S().fcg_mg(case.As, case.Ps, case.bs, cycle="K", precision="fp32")
+    x = solver.Solve(case.b)
+    ref = case["hist_k"]
+    assert abs(solver.IterationCount - (len(ref) - 1)) <= 3
+    assert true_rel_residual(case.As[0], case.b, x) < 1e-8 * (1 + 1e-6)
 
 
 def test_block_jacobi_smoother_matches_reference(case):

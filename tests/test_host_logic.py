@@ -30,6 +30,8 @@ def test_unsupported_configurations_fail_loudly():
         S.FlexibleConjugateGradient(truncation=2)
     mg = S.Multigrid()
     mg.Cycle = "K"
+    mg._check_supported()           # V, W and K run on the GPU
+    mg.Cycle = "F"                  # no such cycle in the reference
     with pytest.raises(NotImplementedError):
         mg._check_supported()
     mg.Cycle = "V"

@@ -45,7 +45,8 @@ VARIANTS = [("colour", ("bgs", "rbgs"), "fcg", "V"),
             ("cg", ("bgs", "rbgs"), "cg", "V"),
             ("w", ("bgs", "rbgs"), "fcg", "W"),
             ("sbgs", ("sbgs", "sbgs"), "fcg", "V"),
-            ("abgs", ("abgs", "rabgs"), "fcg", "V")]
+            ("abgs", ("abgs", "rabgs"), "fcg", "V"),
+            ("k", ("bgs", "rbgs"), "fcg", "K")]
 
 
 @pytest.mark.parametrize("variant,smoothers,krylov,cycle", VARIANTS)
