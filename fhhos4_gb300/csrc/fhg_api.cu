@@ -1877,6 +1877,7 @@ int fhg_set_cycle(fhg_ctx* ctx, int pre_smoother, int post_smoother, int pre_ite
     if (pre_iterations < 0 || post_iterations < 0 || (w_loops < 1 && w_loops != FHG_CYCLE_K))
         return fail(ctx, FHG_ERR_INVALID_ARG, "negative smoothing count or cycle loops < 1");
     free_graphs(ctx);
+    ctx->epoch++;          // batched graphs that captured the old cycle are rebuilt
     ctx->rho_plain = 0.0;  // the plain method's reduction is measured again for the new cycle
     ctx->opts.pre_smoother = pre_smoother;
     ctx->opts.post_smoother = post_smoother;
@@ -1895,6 +1896,7 @@ int fhg_set_vcycle_precision(fhg_ctx* ctx, int precision)
         return fail(ctx, FHG_ERR_NOT_READY, "FP32 operators were not built: set up with FHG_PREC_FP32");
     if (ctx->opts.vcycle_precision != precision) {
         free_graphs(ctx);
+        ctx->epoch++;
         ctx->rho_plain = 0.0;
         ctx->opts.vcycle_precision = precision;
     }
@@ -1993,6 +1995,7 @@ int fhg_set_learned(fhg_ctx* ctx, const float* params, int n_params, int mode)
     }
     ctx->learned_mode = mode;
     ctx->rho_plain = 0.0;
+    ctx->epoch++;
     return FHG_OK;
 }
 

@@ -88,6 +88,30 @@ def test_batch_rebuilds_after_setup_and_stops_at_max_iterations():
             p.close()
 
 
+def test_batch_follows_cycle_and_precision_changes():
+    """Changing the cycle or the V-cycle precision of a context in a batch makes the next batched
+    solve capture the new launch sequence (the same iterations as the individual solve)."""
+    from fhhos4_gb300 import batch as B
+    probs, batch, _ = B.build(_specs()[:2], precision="fp32", autotune=False)
+    try:
+        rc, infos, _ = batch.solve()
+        assert rc == 0
+        for prec, nu in (("fp64", (1, 1)), ("fp32", (2, 2))):
+            for p in probs:
+                p.ctx.set_vcycle_precision(prec)
+                p.ctx.set_cycle("bgs", "rbgs", nu[0], nu[1], 1)
+            ref = [p.ctx.solve(p.b, 200)[3].iterations for p in probs]
+            for p in probs:
+                p.upload_b()
+            rc, infos, _ = batch.solve()
+            assert rc == 0
+            assert [i.iterations for i in infos] == ref
+    finally:
+        batch.close()
+        for p in probs:
+            p.close()
+
+
 def test_batch_rejects_unsupported_contexts():
     from fhhos4_gb300 import _native as N
     from fhhos4_gb300 import hho
