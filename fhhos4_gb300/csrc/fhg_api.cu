@@ -98,7 +98,10 @@ struct fhg_ctx {
     int* counter_d = nullptr;
     double* nr_host = nullptr;   // pinned
     double* io = nullptr;        // user-numbered I/O scratch (2 * n0)
-    float *dhi = nullptr, *dlo = nullptr;  // FP32 pair of the search direction (double-FP32 outer product)
+    // Double-FP32 outer iteration (FP32 V-cycle with the split outer operator): x as an FP32 pair
+    // (hi: n floats, then lo: n) and the low part of r, whose high part is the V-cycle input b32;
+    // d and Ad live as pairs in kz[p] and kAd[p] (hi: n floats, then lo).
+    float *xdf = nullptr, *rlo = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     long long graph_kernels[2] = {0, 0};
     int graphs_built = 0;
@@ -900,6 +903,25 @@ void precondition(fhg_ctx* ctx, const double* r, double* z)
 
 double* part(fhg_ctx* ctx, int i) { return ctx->partials + (size_t)i * fhg::kReduceCtas; }
 
+// The outer iteration runs on FP32 pairs (double-FP32 outer product built at setup).
+bool outer_df(const fhg_ctx* ctx)
+{
+    return ctx->opts.vcycle_precision == FHG_PREC_FP32 && ctx->opts.krylov == FHG_KRYLOV_FCG &&
+           ctx->levels[0].ahat_lo && ctx->xdf;
+}
+
+// FP32 pair views of an n-long FP64 buffer (hi: first n floats, lo: next n).
+float* pair_hi(double* v) { return reinterpret_cast<float*>(v); }
+float* pair_lo(double* v, long long n) { return reinterpret_cast<float*>(v) + n; }
+
+// Start of a double-FP32 outer iteration: x = 0 and (b32, rlo) = r.
+void outer_df_start(fhg_ctx* ctx, const double* r)
+{
+    const long long n = ctx->levels[0].n;
+    cudaMemsetAsync(ctx->xdf, 0, sizeof(float) * 2 * n, ctx->stream);
+    fhg::launch_split_df(n, r, ctx->levels[0].b32, ctx->rlo, ctx->stream);
+}
+
 // One FCG(1) iteration (src/Solver/Krylov/FlexibleConjugateGradient.h:80-162), parity p
 // selects the ping-pong buffers (z/d, Ad) of this iteration.
 void fcg_iteration(fhg_ctx* ctx, int p)
@@ -912,22 +934,33 @@ void fcg_iteration(fhg_ctx* ctx, int p)
     double* Adp = ctx->kAd[1 - p];
     Level& L0 = ctx->levels[0];
     const bool fp32 = ctx->opts.vcycle_precision == FHG_PREC_FP32;
-    const bool split = fp32 && L0.ahat_lo && ctx->dhi;
+    if (outer_df(ctx)) {
+        // FP32 pairs throughout: z = M r_hi (FP32 V-cycle), d = z - s dp, Ad = Â d, x += alpha d,
+        // r -= alpha Ad, with no FP64 instruction per element.
+        vcycle<float>(ctx, 0, L0.b32, L0.x32);
+        float *dh = pair_hi(z), *dl = pair_lo(z, n), *Adh = pair_hi(Ad), *Adl = pair_lo(Ad, n);
+        fhg::launch_dot_df(n, L0.x32, pair_hi(Adp), pair_lo(Adp, n), part(ctx, 0), s);
+        fhg::launch_fcg_direction_df(n, L0.x32, pair_hi(dp), pair_lo(dp, n), part(ctx, 0), ctx->scal + 1, dh, dl, s);
+        fhg::launch_spmv_dots_df(L0.Ahat_hi.v, L0.ahat_lo, dh, dl, L0.b32, ctx->rlo, Adh, Adl, part(ctx, 1), s);
+        fhg::launch_krylov_step_df(n, ctx->xdf, ctx->xdf + n, L0.b32, ctx->rlo, dh, dl, Adh, Adl, part(ctx, 2),
+                                   part(ctx, 1), ctx->scal + 1, part(ctx, 3), s);
+        fhg::launch_finalize_norm(part(ctx, 3), ctx->scal + 0, ctx->scal + 2, ctx->hist_d, ctx->counter_d,
+                                  ctx->opts.max_iterations + 1, s);
+        if (!ctx->device_loop) cudaMemcpyAsync(ctx->nr_host, ctx->scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s);
+        return;
+    }
     if (fp32) {
         // V-cycle on the FP32 copy of r written by the previous step; z stays FP32 and is
         // widened inside the direction update.
         vcycle<float>(ctx, 0, L0.b32, L0.x32);
         fhg::launch_dot_mixed(n, L0.x32, Adp, part(ctx, 0), s);
-        fhg::launch_fcg_direction_mixed(n, L0.x32, dp, part(ctx, 0), ctx->scal + 1, z, s, split ? ctx->dhi : nullptr,
-                                        split ? ctx->dlo : nullptr);
+        fhg::launch_fcg_direction_mixed(n, L0.x32, dp, part(ctx, 0), ctx->scal + 1, z, s);
     } else {
         precondition(ctx, ctx->kr, z);
         fhg::launch_dot(n, z, Adp, part(ctx, 0), s);
         fhg::launch_fcg_direction(n, z, dp, part(ctx, 0), ctx->scal + 1, z, s);
     }
-    if (split) {
-        fhg::launch_spmv_dots_df(L0.Ahat_hi.v, L0.ahat_lo, ctx->dhi, ctx->dlo, z, ctx->kr, Ad, part(ctx, 1), s);
-    } else {
+    {
         BsrView<double> Ah = L0.ahat_is_a ? L0.A.v : L0.Ahat.v;
         if (L0.outer_lanes) Ah.lanes = L0.outer_lanes;
         fhg::launch_spmv_dots(Ah, z, ctx->kr, Ad, part(ctx, 1), s);
@@ -1076,6 +1109,7 @@ void free_all(fhg_ctx* ctx)
 {
     free_graphs(ctx);
     ctx->nbr_d = nullptr; ctx->tfeat_d = nullptr; ctx->lw = nullptr; ctx->lstatus = nullptr;
+    ctx->xdf = nullptr; ctx->rlo = nullptr;
     ctx->lparams = nullptr; ctx->lwts = nullptr; ctx->lbias = nullptr;
     ctx->learned_mode = FHG_LEARNED_OFF;
     ctx->learned_now = false;
@@ -1117,7 +1151,9 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
     CK(cudaMemcpyAsync(ctx->scal + 1, init, sizeof(init), cudaMemcpyHostToDevice, s));
     const int one = 1;
     CK(cudaMemcpyAsync(ctx->counter_d, &one, sizeof(int), cudaMemcpyHostToDevice, s));
-    if (ctx->opts.krylov == FHG_KRYLOV_FCG && ctx->opts.vcycle_precision == FHG_PREC_FP32)
+    if (outer_df(ctx))
+        outer_df_start(ctx, ctx->kr);  // x = 0 and r = b as FP32 pairs
+    else if (ctx->opts.krylov == FHG_KRYLOV_FCG && ctx->opts.vcycle_precision == FHG_PREC_FP32)
         fhg::launch_convert<double, float>(n, ctx->kr, L0.b32, s);  // FP32 copy of r = b
     if (ctx->opts.krylov == FHG_KRYLOV_CG) {
         // z = M r; d = 0 so that the first direction is z; rz = r.z
@@ -1179,6 +1215,7 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
         }
         if (learned_its > 0 && status == FHG_OK) status = check_learned_status(ctx);
         if (status != FHG_OK) break;
+        if (outer_df(ctx)) fhg::launch_join_df(n, ctx->xdf, ctx->xdf + n, ctx->kx, s);
         // The FP64 true residual ||b - A x|| / ||b|| judges the solve (A the full level-0 operator).
         fhg::launch_spmv<double>(L0.A.v, fhg::kSpmvResidual, ctx->kx, ctx->kb, ctx->kt, s);
         fhg::launch_dot(n, ctx->kt, ctx->kt, part(ctx, 0), s);
@@ -1197,7 +1234,8 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
             replacements++;
             CK(cudaMemcpyAsync(ctx->kr, ctx->kt, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
             CK(cudaMemcpyAsync(ctx->scal + 2, &true_rel, sizeof(double), cudaMemcpyHostToDevice, s));
-            fhg::launch_convert<double, float>(n, ctx->kr, L0.b32, s);
+            if (outer_df(ctx)) fhg::launch_split_df(n, ctx->kr, L0.b32, ctx->rlo, s);
+            else fhg::launch_convert<double, float>(n, ctx->kr, L0.b32, s);
             CK(cudaStreamSynchronize(s));
             nr = true_rel;
             continue;
@@ -1550,7 +1588,9 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         (rc = dalloc(ctx, &ctx->hist_d, (size_t)o.max_iterations + 2)) || (rc = dalloc(ctx, &ctx->counter_d, 1)) ||
         (rc = dalloc(ctx, &ctx->io, (size_t)2 * n0)))
         return rc;
-    if (fp32 && o.outer_split && ((rc = dalloc(ctx, &ctx->dhi, n0)) || (rc = dalloc(ctx, &ctx->dlo, n0)))) return rc;
+    ctx->xdf = nullptr;
+    ctx->rlo = nullptr;
+    if (fp32 && o.outer_split && ((rc = dalloc(ctx, &ctx->xdf, 2 * n0)) || (rc = dalloc(ctx, &ctx->rlo, n0)))) return rc;
     CK(cudaMallocHost(&ctx->nr_host, sizeof(double)));
 
     if (o.autotune) {
@@ -1582,12 +1622,12 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         L0.outer_lanes = g;
         if (L0.ahat_lo) {
             int gd = g, gdu = 1;
-            CK(cudaMemsetAsync(ctx->dhi, 0, sizeof(float) * L0.n, ctx->stream));
-            CK(cudaMemsetAsync(ctx->dlo, 0, sizeof(float) * L0.n, ctx->stream));
+            const long long n = L0.n;
             if ((rc = tune(ctx, 9, gd, gdu, [&](int G, int) {
                      BsrView<float> v = L0.Ahat_hi.v; v.lanes = G;
-                     fhg::launch_spmv_dots_df(v, L0.ahat_lo, ctx->dhi, ctx->dlo, ctx->kz[0], ctx->kz[0], ctx->kAd[0],
-                                              part(ctx, 5), ctx->stream);
+                     fhg::launch_spmv_dots_df(v, L0.ahat_lo, pair_hi(ctx->kz[0]), pair_lo(ctx->kz[0], n),
+                                              pair_hi(ctx->kz[0]), pair_lo(ctx->kz[0], n), pair_hi(ctx->kAd[0]),
+                                              pair_lo(ctx->kAd[0], n), part(ctx, 5), ctx->stream);
                  })))
                 return rc;
             L0.Ahat_hi.v.lanes = gd;
@@ -1829,21 +1869,21 @@ int fhg_time_op(fhg_ctx* ctx, int level, int op, int precision, int warmup, int 
         Level& L0 = ctx->levels[0];
         const bool split = op == FHG_OP_SYM_SPMV && precision == FHG_PREC_FP32;
         if (precision != FHG_PREC_FP64 && !split) return fail(ctx, FHG_ERR_INVALID_ARG, "op %d is timed in FP64 only", op);
-        if (split && (!L0.ahat_lo || !ctx->dhi))
+        if (split && (!L0.ahat_lo || !ctx->xdf))
             return fail(ctx, FHG_ERR_NOT_READY, "the double-FP32 outer operator was not built at setup");
         const size_t n0 = L0.n;
         double* t = nullptr;
         int rc = dalloc(ctx, &t, 2 * n0);
         if (rc) return rc;
         CK(cudaMemcpyAsync(t, ctx->kr, sizeof(double) * n0, cudaMemcpyDeviceToDevice, ctx->stream));
-        if (split) {
-            fhg::launch_convert<double, float>(n0, t, ctx->dhi, ctx->stream);
-            CK(cudaMemsetAsync(ctx->dlo, 0, sizeof(float) * n0, ctx->stream));
-        }
+        // double-FP32: d = r (FP32 pair in the first n0 doubles), Ad pair in the second
+        float* dh = pair_hi(t);
+        float* dl = pair_lo(t, (long long)n0);
+        if (split) fhg::launch_split_df((long long)n0, ctx->kr, dh, dl, ctx->stream);
         auto one = [&]() -> int {
             if (split) {
-                fhg::launch_spmv_dots_df(L0.Ahat_hi.v, L0.ahat_lo, ctx->dhi, ctx->dlo, t, t, t + n0, part(ctx, 4),
-                                         ctx->stream);
+                fhg::launch_spmv_dots_df(L0.Ahat_hi.v, L0.ahat_lo, dh, dl, dh, dl, pair_hi(t + n0),
+                                         pair_lo(t + n0, (long long)n0), part(ctx, 4), ctx->stream);
                 return FHG_OK;
             }
             return apply_device(ctx, level, op, t, nullptr, t + n0);
@@ -2325,7 +2365,8 @@ void batch_prelude(fhg_ctx* ctx)
     fhg::launch_dot(n, ctx->kb, ctx->kb, part(ctx, 0), s);
     fhg::launch_sqrt_sum(part(ctx, 0), ctx->scal + 0, s);
     fhg::launch_init_solve(ctx->scal, ctx->counter_d, s);
-    if (ctx->opts.vcycle_precision == FHG_PREC_FP32) fhg::launch_convert<double, float>(n, ctx->kr, L0.b32, s);
+    if (outer_df(ctx)) outer_df_start(ctx, ctx->kr);
+    else if (ctx->opts.vcycle_precision == FHG_PREC_FP32) fhg::launch_convert<double, float>(n, ctx->kr, L0.b32, s);
 }
 
 // End of a solve: FP64 true residual into scal[5] (||b - A x||), x = Pi^T x'.
@@ -2334,6 +2375,7 @@ void batch_epilogue(fhg_ctx* ctx)
     Level& L0 = ctx->levels[0];
     const long long n = L0.n;
     cudaStream_t s = ctx->stream;
+    if (outer_df(ctx)) fhg::launch_join_df(n, ctx->xdf, ctx->xdf + n, ctx->kx, s);
     fhg::launch_spmv<double>(L0.A.v, fhg::kSpmvResidual, ctx->kx, ctx->kb, ctx->kt, s);
     fhg::launch_dot(n, ctx->kt, ctx->kt, part(ctx, 0), s);
     fhg::launch_sqrt_sum(part(ctx, 0), ctx->scal + 5, s);

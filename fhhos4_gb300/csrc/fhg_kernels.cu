@@ -64,6 +64,40 @@ __device__ __forceinline__ double reduce_partials(const double* __restrict__ p, 
     return block_sum(v, sh);
 }
 
+// Element loop of the fixed-grid vector kernels: thread t of CTA c visits
+// i = c * kReduceThreads + t, then i + S, i + 2 S, ... (S = kReduceCtas * kReduceThreads) in that
+// order, so every per-thread sum is taken in one fixed order. Four elements go per step with all
+// their loads issued before the first use: one element per thread per step leaves too few bytes
+// in flight for HBM (a quarter of what the copy rate needs at 152 x 4 CTAs of 256 threads).
+// `load(i)` returns the element's inputs, `use(i, v)` computes and stores.
+constexpr long long kRedStride = (long long)kReduceCtas * kReduceThreads;
+constexpr int kRedUnroll = 4;
+
+template <class Load, class Use>
+__device__ __forceinline__ void for_each_element(long long n, Load load, Use use)
+{
+    long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x;
+    for (; i + (kRedUnroll - 1) * kRedStride < n; i += kRedUnroll * kRedStride) {
+        decltype(load(i)) v[kRedUnroll];
+#pragma unroll
+        for (int u = 0; u < kRedUnroll; u++) v[u] = load(i + u * kRedStride);
+#pragma unroll
+        for (int u = 0; u < kRedUnroll; u++) use(i + u * kRedStride, v[u]);
+    }
+    for (; i < n; i += kRedStride) use(i, load(i));
+}
+
+template <class A, class B>
+struct Pair2 {
+    A a;
+    B b;
+};
+
+template <class T>
+struct Quad4 {
+    T a, b, c, d;
+};
+
 // ---------------------------------------------------------------------------
 // Row accumulation: acc[r] += sum over this lane's blocks of (A_block x_col)[r].
 // `sel(col)` returns 0 (skip the block), 1 (use it) or 2 (stop: columns are sorted, nothing
@@ -367,12 +401,13 @@ __global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots(int nbr, const
 
 // ---------------------------------------------------------------------------
 // Ad = Â d in double-FP32 ("double-single") arithmetic on the FP32 pipe, with per-CTA partials
-// of d.Ad and r.d in FP64. Â = a_hi + a_lo and d = d_hi + d_lo are FP32 pairs (a_lo, d_lo the
-// FP32-rounded remainders); every product a_hi*d_hi is split exactly with an FMA, the cross
-// terms a_hi*d_lo + a_lo*d_hi are added in FP32, a_lo*d_lo (2^-48 relative) is dropped, and the
-// running sum is a (hi, lo) FP32 pair kept exact with TwoSum. Relative accuracy of every term
-// ~2^-47: the result carries FP64-class accuracy (a few units in 1e-14) while the FP64 pipe,
-// 56x slower than FP32 on GB300, only adds the final pair and the two dot products.
+// of d.Ad and r.d. Â = a_hi + a_lo, d = d_hi + d_lo, r = r_hi + r_lo and the result Ad are FP32
+// pairs (the lo parts the FP32-rounded remainders); every product a_hi*d_hi is split exactly with
+// an FMA, the cross terms a_hi*d_lo + a_lo*d_hi are added in FP32, a_lo*d_lo (2^-48 relative) is
+// dropped, and the running sum is a (hi, lo) FP32 pair kept exact with TwoSum. Relative accuracy
+// of every term ~2^-47: the result carries FP64-class accuracy (a few units in 1e-14) with no
+// FP64 instruction per element (GB300's FP64 pipe is 56x slower than FP32); the dot products are
+// summed per thread as pairs too and only the per-thread sums are widened to FP64.
 __device__ __forceinline__ void df_add(float& sh, float& sl, float ph, float pl)
 {
     const float s = sh + ph;
@@ -382,6 +417,35 @@ __device__ __forceinline__ void df_add(float& sh, float& sl, float ph, float pl)
     sh = s;
 }
 
+// Product of two pairs (a_lo * b_lo, 2^-48 relative, dropped): ph + pl, ph = fl(a_hi b_hi) and its
+// FMA-exact error carrying the cross terms.
+__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& ph, float& pl)
+{
+    ph = ah * bh;
+    pl = fmaf(ah, bh, -ph) + fmaf(ah, bl, al * bh);
+}
+
+// The normalized pair of s + e: hi = fl(s + e) (the FP32 value nearest the pair), lo the rest.
+__device__ __forceinline__ void df_norm(float s, float e, float& h, float& l)
+{
+    h = s + e;
+    l = e - (h - s);
+}
+
+// (xh, xl) + (ph, pl), normalized.
+__device__ __forceinline__ void df_sum(float xh, float xl, float ph, float pl, float& h, float& l)
+{
+    df_add(xh, xl, ph, pl);
+    df_norm(xh, xl, h, l);
+}
+
+// An FP64 value as an FP32 pair (exact to 2^-48 relative); per thread, not per element.
+__device__ __forceinline__ void df_split(double v, float& h, float& l)
+{
+    h = (float)v;
+    l = (float)(v - (double)h);
+}
+
 template <int BS, int G>
 __global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots_df(int nbr, const int* __restrict__ rowptr,
                                                                      const int* __restrict__ colidx,
@@ -389,9 +453,9 @@ __global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots_df(int nbr, co
                                                                      const float* __restrict__ vlo, long long ld,
                                                                      const float* __restrict__ dhi,
                                                                      const float* __restrict__ dlo,
-                                                                     const double* __restrict__ d,
-                                                                     const double* __restrict__ rvec,
-                                                                     double* __restrict__ Ad,
+                                                                     const float* __restrict__ rhi,
+                                                                     const float* __restrict__ rlo,
+                                                                     float* __restrict__ Adhi, float* __restrict__ Adlo,
                                                                      double* __restrict__ partials)
 {
     __shared__ double sh_red[33];
@@ -400,17 +464,20 @@ __global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots_df(int nbr, co
     const long long warp_id = ((long long)blockIdx.x * kReduceThreads + threadIdx.x) >> 5;
     const long long warp_stride = (long long)kReduceCtas * kReduceThreads / 32 * kGroupsPerWarp;
     const int group_in_warp = (threadIdx.x & 31) / G;
-    double dad = 0.0, rd = 0.0;
+    float dad_h = 0.f, dad_l = 0.f, rd_h = 0.f, rd_l = 0.f;
     for (long long row0 = warp_id * kGroupsPerWarp; row0 < nbr; row0 += warp_stride) {
         const int row = (int)(row0 + group_in_warp);
         float hi[BS], lo[BS];
 #pragma unroll
         for (int r = 0; r < BS; r++) { hi[r] = 0.f; lo[r] = 0.f; }
-        double dv = 0.0, rv = 0.0;
+        float dvh = 0.f, dvl = 0.f, rvh = 0.f, rvl = 0.f;
         if (row < nbr) {
             if (lane < BS) {
-                dv = d[(long long)row * BS + lane];
-                rv = rvec[(long long)row * BS + lane];
+                const long long i = (long long)row * BS + lane;
+                dvh = dhi[i];
+                dvl = dlo[i];
+                rvh = rhi[i];
+                rvl = rlo[i];
             }
             const int p1 = rowptr[row + 1];
             for (int p = rowptr[row] + lane; p < p1; p += G) {
@@ -427,11 +494,9 @@ __global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots_df(int nbr, co
                 for (int r = 0; r < BS; r++)
 #pragma unroll
                     for (int c = 0; c < BS; c++) {
-                        const float ah = ahv[r * BS + c], al = alv[r * BS + c];
-                        const float ph = ah * xh[c];
-                        const float pe = fmaf(ah, xh[c], -ph);
-                        const float cross = fmaf(ah, xl[c], al * xh[c]);
-                        df_add(hi[r], lo[r], ph, pe + cross);
+                        float ph, pl;
+                        df_mul(ahv[r * BS + c], alv[r * BS + c], xh[c], xl[c], ph, pl);
+                        df_add(hi[r], lo[r], ph, pl);
                     }
             }
         }
@@ -449,16 +514,20 @@ __global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots_df(int nbr, co
             for (int r = 0; r < BS; r++) {
                 if (lane == r) {   // G >= BS: launch_spmv_dots_df rejects smaller G
                     const long long i = (long long)row * BS + r;
-                    const double v = (double)hi[r] + (double)lo[r];
-                    Ad[i] = v;
-                    dad = fma(dv, v, dad);
-                    rd = fma(rv, dv, rd);
+                    float ah, al, ph, pl;
+                    df_norm(hi[r], lo[r], ah, al);
+                    Adhi[i] = ah;
+                    Adlo[i] = al;
+                    df_mul(dvh, dvl, ah, al, ph, pl);
+                    df_add(dad_h, dad_l, ph, pl);
+                    df_mul(rvh, rvl, dvh, dvl, ph, pl);
+                    df_add(rd_h, rd_l, ph, pl);
                 }
             }
         }
     }
-    const double s1 = block_sum(dad, sh_red);
-    const double s2 = block_sum(rd, sh_red);
+    const double s1 = block_sum((double)dad_h + (double)dad_l, sh_red);
+    const double s2 = block_sum((double)rd_h + (double)rd_l, sh_red);
     if (threadIdx.x == 0) {
         partials[blockIdx.x] = s1;
         partials[kReduceCtas + blockIdx.x] = s2;
@@ -485,8 +554,8 @@ __global__ void __launch_bounds__(kReduceThreads) k_dot(long long n, const doubl
 {
     __shared__ double sh[33];
     double v = 0.0;
-    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads)
-        v = fma(a[i], b[i], v);
+    for_each_element(n, [&](long long i) { return Pair2<double, double>{a[i], b[i]}; },
+                     [&](long long, const Pair2<double, double>& e) { v = fma(e.a, e.b, v); });
     v = block_sum(v, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = v;
 }
@@ -501,11 +570,22 @@ __global__ void __launch_bounds__(kReduceThreads) k_dots3(long long n, int nq, c
 {
     __shared__ double sh[33];
     double v0 = 0.0, v1 = 0.0, v2 = 0.0;
-    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads) {
-        v0 = fma((double)a0[i], (double)b0[i], v0);
-        if (nq > 1) v1 = fma((double)a1[i], (double)b1[i], v1);
-        if (nq > 2) v2 = fma((double)a2[i], (double)b2[i], v2);
-    }
+    struct E {
+        T a0, b0, a1, b1, a2, b2;
+    };
+    for_each_element(
+        n,
+        [&](long long i) {
+            E e{a0[i], b0[i], T(0), T(0), T(0), T(0)};
+            if (nq > 1) { e.a1 = a1[i]; e.b1 = b1[i]; }
+            if (nq > 2) { e.a2 = a2[i]; e.b2 = b2[i]; }
+            return e;
+        },
+        [&](long long, const E& e) {
+            v0 = fma((double)e.a0, (double)e.b0, v0);
+            if (nq > 1) v1 = fma((double)e.a1, (double)e.b1, v1);
+            if (nq > 2) v2 = fma((double)e.a2, (double)e.b2, v2);
+        });
     v0 = block_sum(v0, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = v0;
     if (nq > 1) {
@@ -539,8 +619,8 @@ __global__ void __launch_bounds__(kReduceThreads) k_dot_mixed(long long n, const
 {
     __shared__ double sh[33];
     double v = 0.0;
-    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads)
-        v = fma((double)a[i], b[i], v);
+    for_each_element(n, [&](long long i) { return Pair2<float, double>{a[i], b[i]}; },
+                     [&](long long, const Pair2<float, double>& e) { v = fma((double)e.a, e.b, v); });
     v = block_sum(v, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = v;
 }
@@ -553,15 +633,16 @@ __global__ void __launch_bounds__(kReduceThreads) k_fcg_direction_mixed(long lon
 {
     __shared__ double sh[33];
     const double s = reduce_partials(partials, sh) / *dadp;
-    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads) {
-        const double v = (double)z[i] - s * dp[i];
-        d[i] = v;
-        if (dhi) {
-            const float h = (float)v;
-            dhi[i] = h;
-            dlo[i] = (float)(v - (double)h);
-        }
-    }
+    for_each_element(n, [&](long long i) { return Pair2<float, double>{z[i], dp[i]}; },
+                     [&](long long i, const Pair2<float, double>& e) {
+                         const double v = (double)e.a - s * e.b;
+                         d[i] = v;
+                         if (dhi) {
+                             const float h = (float)v;
+                             dhi[i] = h;
+                             dlo[i] = (float)(v - (double)h);
+                         }
+                     });
 }
 
 __global__ void __launch_bounds__(kReduceThreads) k_fcg_direction(long long n, const double* z, const double* __restrict__ dp,
@@ -570,8 +651,8 @@ __global__ void __launch_bounds__(kReduceThreads) k_fcg_direction(long long n, c
 {
     __shared__ double sh[33];
     const double s = reduce_partials(partials, sh) / *dadp;
-    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads)
-        d[i] = z[i] - s * dp[i];
+    for_each_element(n, [&](long long i) { return Pair2<double, double>{z[i], dp[i]}; },
+                     [&](long long i, const Pair2<double, double>& e) { d[i] = e.a - s * e.b; });
 }
 
 __global__ void __launch_bounds__(kReduceThreads) k_krylov_step(long long n, double* __restrict__ x, double* __restrict__ r,
@@ -586,15 +667,117 @@ __global__ void __launch_bounds__(kReduceThreads) k_krylov_step(long long n, dou
     const double alpha = num / den;
     if (blockIdx.x == 0 && threadIdx.x == 0 && den_out) *den_out = den;
     double rr = 0.0;
-    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads) {
-        x[i] = x[i] + alpha * d[i];
-        const double ri = r[i] - alpha * Ad[i];
-        r[i] = ri;
-        if (r32) r32[i] = (float)ri;
-        rr = fma(ri, ri, rr);
-    }
+    for_each_element(n, [&](long long i) { return Quad4<double>{x[i], d[i], r[i], Ad[i]}; },
+                     [&](long long i, const Quad4<double>& e) {
+                         x[i] = e.a + alpha * e.b;
+                         const double ri = e.c - alpha * e.d;
+                         r[i] = ri;
+                         if (r32) r32[i] = (float)ri;
+                         rr = fma(ri, ri, rr);
+                     });
     rr = block_sum(rr, sh);
     if (threadIdx.x == 0) prr[blockIdx.x] = rr;
+}
+
+// Double-FP32 outer iteration: x, r, d and Ad are FP32 pairs (hi, lo), so that no FP64 instruction
+// runs per element; the Krylov scalars stay FP64 and are split into pairs once per thread.
+// partials of z.Adp with z the FP32 V-cycle output.
+__global__ void __launch_bounds__(kReduceThreads) k_dot_df(long long n, const float* __restrict__ z,
+                                                           const float* __restrict__ ah, const float* __restrict__ al,
+                                                           double* __restrict__ partials)
+{
+    __shared__ double sh[33];
+    float vh = 0.f, vl = 0.f;
+    struct E {
+        float z, h, l;
+    };
+    for_each_element(n, [&](long long i) { return E{z[i], ah[i], al[i]}; },
+                     [&](long long, const E& e) {
+                         float ph, pl;
+                         df_mul(e.z, 0.f, e.h, e.l, ph, pl);
+                         df_add(vh, vl, ph, pl);
+                     });
+    const double v = block_sum((double)vh + (double)vl, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v;
+}
+
+// d = z - s dp, s = sum(partials_zadp) / *dadp.
+__global__ void __launch_bounds__(kReduceThreads) k_fcg_direction_df(long long n, const float* __restrict__ z,
+                                                                     const float* __restrict__ dph,
+                                                                     const float* __restrict__ dpl,
+                                                                     const double* __restrict__ partials,
+                                                                     const double* __restrict__ dadp,
+                                                                     float* __restrict__ dh, float* __restrict__ dl)
+{
+    __shared__ double sh[33];
+    float sh_, sl_;
+    df_split(reduce_partials(partials, sh) / *dadp, sh_, sl_);
+    struct E {
+        float z, h, l;
+    };
+    for_each_element(n, [&](long long i) { return E{z[i], dph[i], dpl[i]}; },
+                     [&](long long i, const E& e) {
+                         float ph, pl, h, l;
+                         df_mul(sh_, sl_, e.h, e.l, ph, pl);
+                         df_sum(e.z, 0.f, -ph, -pl, h, l);
+                         dh[i] = h;
+                         dl[i] = l;
+                     });
+}
+
+// alpha = num / den; x += alpha d; r -= alpha Ad (rh is the next V-cycle's FP32 right-hand side);
+// partials_rr of r.r; *den_out = den.
+__global__ void __launch_bounds__(kReduceThreads) k_krylov_step_df(long long n, float* __restrict__ xh,
+                                                                   float* __restrict__ xl, float* __restrict__ rh,
+                                                                   float* __restrict__ rl, const float* __restrict__ dh,
+                                                                   const float* __restrict__ dl,
+                                                                   const float* __restrict__ Adh,
+                                                                   const float* __restrict__ Adl,
+                                                                   const double* __restrict__ pnum,
+                                                                   const double* __restrict__ pden,
+                                                                   double* __restrict__ den_out, double* __restrict__ prr)
+{
+    __shared__ double sh[33];
+    const double num = reduce_partials(pnum, sh);
+    const double den = reduce_partials(pden, sh);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && den_out) *den_out = den;
+    float ah, al;
+    df_split(num / den, ah, al);
+    float rrh = 0.f, rrl = 0.f;
+    struct E {
+        float xh, xl, rh, rl, dh, dl, ah, al;
+    };
+    for_each_element(n, [&](long long i) { return E{xh[i], xl[i], rh[i], rl[i], dh[i], dl[i], Adh[i], Adl[i]}; },
+                     [&](long long i, const E& e) {
+                         float ph, pl, h, l;
+                         df_mul(ah, al, e.dh, e.dl, ph, pl);
+                         df_sum(e.xh, e.xl, ph, pl, h, l);
+                         xh[i] = h;
+                         xl[i] = l;
+                         df_mul(ah, al, e.ah, e.al, ph, pl);
+                         df_sum(e.rh, e.rl, -ph, -pl, h, l);
+                         rh[i] = h;
+                         rl[i] = l;
+                         df_mul(h, l, h, l, ph, pl);
+                         df_add(rrh, rrl, ph, pl);
+                     });
+    const double rr = block_sum((double)rrh + (double)rrl, sh);
+    if (threadIdx.x == 0) prr[blockIdx.x] = rr;
+}
+
+// FP64 <-> FP32 pair (the boundaries of the double-FP32 iteration).
+__global__ void __launch_bounds__(kThreads) k_split_df(long long n, const double* __restrict__ v, float* __restrict__ h,
+                                                      float* __restrict__ l)
+{
+    const long long i = (long long)blockIdx.x * kThreads + threadIdx.x;
+    if (i < n) df_split(v[i], h[i], l[i]);
+}
+
+__global__ void __launch_bounds__(kThreads) k_join_df(long long n, const float* __restrict__ h,
+                                                     const float* __restrict__ l, double* __restrict__ v)
+{
+    const long long i = (long long)blockIdx.x * kThreads + threadIdx.x;
+    if (i < n) v[i] = (double)h[i] + (double)l[i];
 }
 
 __global__ void __launch_bounds__(kReduceThreads) k_cg_step(long long n, double* __restrict__ x, double* __restrict__ r,
@@ -606,12 +789,13 @@ __global__ void __launch_bounds__(kReduceThreads) k_cg_step(long long n, double*
     const double den = reduce_partials(pden, sh);
     const double alpha = *num / den;
     double rr = 0.0;
-    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads) {
-        x[i] = x[i] + alpha * d[i];
-        const double ri = r[i] - alpha * Ad[i];
-        r[i] = ri;
-        rr = fma(ri, ri, rr);
-    }
+    for_each_element(n, [&](long long i) { return Quad4<double>{x[i], d[i], r[i], Ad[i]}; },
+                     [&](long long i, const Quad4<double>& e) {
+                         x[i] = e.a + alpha * e.b;
+                         const double ri = e.c - alpha * e.d;
+                         r[i] = ri;
+                         rr = fma(ri, ri, rr);
+                     });
     rr = block_sum(rr, sh);
     if (threadIdx.x == 0) prr[blockIdx.x] = rr;
 }
@@ -620,8 +804,8 @@ __global__ void __launch_bounds__(kReduceThreads) k_cg_direction(long long n, co
                                                                  const double* __restrict__ beta, double* __restrict__ d)
 {
     const double bt = *beta;
-    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += (long long)kReduceCtas * kReduceThreads)
-        d[i] = z[i] + bt * d[i];
+    for_each_element(n, [&](long long i) { return Pair2<double, double>{z[i], d[i]}; },
+                     [&](long long i, const Pair2<double, double>& e) { d[i] = e.a + bt * e.b; });
 }
 
 __global__ void __launch_bounds__(kReduceThreads) k_finalize_norm(const double* __restrict__ prr, const double* __restrict__ bnorm,
@@ -866,14 +1050,50 @@ void launch_fcg_direction_mixed(long long n, const float* z, const double* dp, c
 }
 
 void launch_spmv_dots_df(const BsrView<float>& Ahi, const float* vlo, const float* dhi, const float* dlo,
-                         const double* d, const double* r, double* Ad, double* partials, cudaStream_t s)
+                         const float* rhi, const float* rlo, float* Adhi, float* Adlo, double* partials,
+                         cudaStream_t s)
 {
     // lane r writes output r: needs G >= bs (always true for G >= 4 and bs <= 4; bs = 6 uses 8)
     const int lanes = Ahi.lanes < Ahi.bs ? 8 : Ahi.lanes;
     FHG_DISPATCH_BS_G(Ahi.bs, lanes, {
         k_bsr_spmv_dots_df<BS, G><<<kReduceCtas, kReduceThreads, 0, s>>>(Ahi.nbr, Ahi.rowptr, Ahi.colidx, Ahi.vals, vlo,
-                                                                         Ahi.ld, dhi, dlo, d, r, Ad, partials);
+                                                                         Ahi.ld, dhi, dlo, rhi, rlo, Adhi, Adlo,
+                                                                         partials);
     });
+    g_kernel_launches++;
+}
+
+void launch_dot_df(long long n, const float* z, const float* ah, const float* al, double* partials, cudaStream_t s)
+{
+    k_dot_df<<<kReduceCtas, kReduceThreads, 0, s>>>(n, z, ah, al, partials);
+    g_kernel_launches++;
+}
+
+void launch_fcg_direction_df(long long n, const float* z, const float* dph, const float* dpl,
+                             const double* partials_zadp, const double* dadp, float* dh, float* dl, cudaStream_t s)
+{
+    k_fcg_direction_df<<<kReduceCtas, kReduceThreads, 0, s>>>(n, z, dph, dpl, partials_zadp, dadp, dh, dl);
+    g_kernel_launches++;
+}
+
+void launch_krylov_step_df(long long n, float* xh, float* xl, float* rh, float* rl, const float* dh, const float* dl,
+                           const float* Adh, const float* Adl, const double* partials_num,
+                           const double* partials_den, double* den_out, double* partials_rr, cudaStream_t s)
+{
+    k_krylov_step_df<<<kReduceCtas, kReduceThreads, 0, s>>>(n, xh, xl, rh, rl, dh, dl, Adh, Adl, partials_num,
+                                                            partials_den, den_out, partials_rr);
+    g_kernel_launches++;
+}
+
+void launch_split_df(long long n, const double* v, float* h, float* l, cudaStream_t s)
+{
+    k_split_df<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, v, h, l);
+    g_kernel_launches++;
+}
+
+void launch_join_df(long long n, const float* h, const float* l, double* v, cudaStream_t s)
+{
+    k_join_df<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, h, l, v);
     g_kernel_launches++;
 }
 

@@ -84,24 +84,39 @@ __device__ __forceinline__ float tanh_fast(float x)
 constexpr float kGeluC0 = 0.7978845608028654f;  // sqrt(2/pi)
 constexpr float kGeluC1 = 0.044715f;
 
-// gelu of two values in packed BF16 arithmetic, the activation the network uses: the inputs
-// are rounded to BF16, then 0.5 x (1 + tanh(c0 x (1 + c1 x^2))) with bf16x2 multiplies/FMAs and
-// the bf16x2 hardware tanh (one multi-function op per two values). Returns the packed result (the
-// next layer's BF16 operand).
+// tanh(x (c0 + c0 c1 x^2)) of two BF16 values in packed BF16 arithmetic: x^2, one FMA with the
+// BF16-rounded constants c0 c1 and c0, one multiply, then the bf16x2 hardware tanh (one
+// multi-function op per two values).
+__device__ __forceinline__ __nv_bfloat162 gelu_tanh_bf16x2(__nv_bfloat162 x)
+{
+    const __nv_bfloat162 c0 = __float2bfloat162_rn(kGeluC0);
+    const __nv_bfloat162 c01 = __float2bfloat162_rn(kGeluC0 * kGeluC1);
+    const __nv_bfloat162 q = __hfma2(__hmul2(x, x), c01, c0);
+    const __nv_bfloat162 u = __hmul2(x, q);
+    uint32_t ui = *reinterpret_cast<const uint32_t*>(&u), ti;
+    asm("tanh.approx.bf16x2 %0, %1;" : "=r"(ti) : "r"(ui));
+    return *reinterpret_cast<const __nv_bfloat162*>(&ti);
+}
+
+// gelu of two values in packed BF16 arithmetic, the activation the network uses: the inputs are
+// rounded to BF16, t = gelu_tanh_bf16x2(x), h = x / 2 (exact), gelu = h t + h in one bf16x2 FMA.
+// Returns the packed result (the next layer's BF16 operand).
 __device__ __forceinline__ uint32_t gelu_bf16x2(float a0, float a1)
 {
     const __nv_bfloat162 x = __floats2bfloat162_rn(a0, a1);
-    const __nv_bfloat162 c0 = __float2bfloat162_rn(kGeluC0);
-    const __nv_bfloat162 c1 = __float2bfloat162_rn(kGeluC1);
-    const __nv_bfloat162 one = __float2bfloat162_rn(1.0f);
-    const __nv_bfloat162 half = __float2bfloat162_rn(0.5f);
-    const __nv_bfloat162 p = __hfma2(__hmul2(x, x), c1, one);
-    const __nv_bfloat162 u = __hmul2(__hmul2(x, c0), p);
-    uint32_t ui = *reinterpret_cast<const uint32_t*>(&u), ti;
-    asm("tanh.approx.bf16x2 %0, %1;" : "=r"(ti) : "r"(ui));
-    const __nv_bfloat162 t = *reinterpret_cast<const __nv_bfloat162*>(&ti);
-    const __nv_bfloat162 h = __hmul2(x, half);
+    const __nv_bfloat162 t = gelu_tanh_bf16x2(x);
+    const __nv_bfloat162 h = __hmul2(x, __float2bfloat162_rn(0.5f));
     const __nv_bfloat162 g = __hfma2(h, t, h);
+    return *reinterpret_cast<const uint32_t*>(&g);
+}
+
+// 2 gelu of two values, x t + x in one bf16x2 FMA: bit for bit twice gelu_bf16x2 (scaling by 2
+// commutes with round-to-nearest away from the subnormal range), one multiply fewer. A layer fed
+// with it uses weights scaled by 1/2, again exactly, so its accumulators are unchanged.
+__device__ __forceinline__ uint32_t gelu2_bf16x2(float a0, float a1)
+{
+    const __nv_bfloat162 x = __floats2bfloat162_rn(a0, a1);
+    const __nv_bfloat162 g = __hfma2(x, gelu_tanh_bf16x2(x), x);
     return *reinterpret_cast<const uint32_t*>(&g);
 }
 
@@ -330,8 +345,13 @@ __global__ void __launch_bounds__(kApplyWarps * 32, 2)
 // slot, thread t gathers the residual patch and the tensor features of face t (the next tile's are
 // loaded while the current tile's layers run), one thread issues tcgen05.mma (BF16 x BF16 -> FP32,
 // M = 128 faces, N = 128 or 16, K = 16 per instruction) with the accumulator in the slot's 128 TMEM
-// columns (TMEM lane t = face t), and the warpgroup reads it back with tcgen05.ld, adds the bias,
-// applies gelu and writes the BF16 A operand of the next layer. The slots share the weights in
+// columns (TMEM lane t = face t), and the warpgroup reads it back with tcgen05.ld, applies gelu
+// and writes the BF16 A operand of the next layer. The biases of the hidden layers ride in the
+// MMAs: b1 as three BF16 parts (hi + mid + lo = the FP32 bias) in the input columns 44..46 of W1,
+// which face constant-1 inputs (those tensor-feature slots are zero in the network's input), and
+// b2 the same way in an extra K = 16 chunk of layer 2 against a constant tile of ones. The
+// epilogue writes 2 gelu (gelu2_bf16x2) and W2, W3 are staged halved, both exact, so the
+// epilogue is one conversion, four bf16x2 ops and a tanh per two values. The slots share the weights in
 // shared memory and synchronise only within the warpgroup (named barriers, one mbarrier each), so
 // the MMA waits, gathers and epilogues of four tiles overlap on every SM. Operands live in shared
 // memory in the canonical K-major layout without swizzle: 8-row x 16-byte core matrices, element
@@ -350,8 +370,10 @@ constexpr uint32_t kTmemCols = 128 * kTcSlots;     // per slot: layer accumulato
 constexpr int kTcSW1 = 0;                          // W1: 128 x 48
 constexpr int kTcSW2 = kTcSW1 + kHid * kIn * 2;    // W2: 128 x 128
 constexpr int kTcSW3 = kTcSW2 + kHid * kHid * 2;   // W3: 16 x 128
-constexpr int kTcSBias = kTcSW3 + kOut * kHid * 2; // b1, b2, b3 (FP32)
-constexpr int kTcSlot0 = ((kTcSBias + (2 * kHid + kOut) * 4 + 1023) / 1024) * 1024;
+constexpr int kTcSBias = kTcSW3 + kOut * kHid * 2; // b1, b2, b3 (FP32; the output layer reads b3)
+constexpr int kTcSOnes = ((kTcSBias + (2 * kHid + kOut) * 4 + 1023) / 1024) * 1024;  // 128 x 16: ones in K 0..2
+constexpr int kTcSB2 = kTcSOnes + kTcRows * 16 * 2;  // 128 x 16: b2 as hi, mid, lo BF16 in K 0..2
+constexpr int kTcSlot0 = kTcSB2 + kHid * 16 * 2;
 constexpr int kTcSlotBytes = kTcRows * kHid * 2;   // hidden tile (the input tile aliases its start)
 constexpr int kTcSScale = kTcSlot0 + kTcSlots * kTcSlotBytes;  // s of every slot's faces
 constexpr int kTcSMisc = kTcSScale + kTcSlots * kTcRows * 4;   // mbarriers (8 each), TMEM base (4)
@@ -438,8 +460,9 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// Bias + gelu of the 128 accumulator columns of this thread's lane into its row of the hidden tile.
-__device__ __forceinline__ void tc_hidden_epilogue(uint32_t taddr, const float* bias, unsigned char* sH, int row)
+// 2 gelu of the 128 accumulator columns (bias included) of this thread's lane into its row of the
+// hidden tile.
+__device__ __forceinline__ void tc_hidden_epilogue(uint32_t taddr, unsigned char* sH, int row)
 {
 #pragma unroll 1
     for (int q = 0; q < kHid / 32; q++) {
@@ -449,13 +472,35 @@ __device__ __forceinline__ void tc_hidden_epilogue(uint32_t taddr, const float* 
         for (int c = 0; c < 4; c++) {
             uint32_t w[4];
 #pragma unroll
-            for (int e = 0; e < 4; e++) {
-                const int j = q * 32 + c * 8 + 2 * e;
-                w[e] = gelu_bf16x2(v[c * 8 + 2 * e] + bias[j], v[c * 8 + 2 * e + 1] + bias[j + 1]);
-            }
+            for (int e = 0; e < 4; e++) w[e] = gelu2_bf16x2(v[c * 8 + 2 * e], v[c * 8 + 2 * e + 1]);
             *reinterpret_cast<uint4*>(sH + core_off(row, q * 4 + c, kHid * 16)) = make_uint4(w[0], w[1], w[2], w[3]);
         }
     }
+}
+
+// Eight BF16 weights scaled by 1/2 (exact).
+__device__ __forceinline__ uint4 halve_bf16x8(uint4 v)
+{
+    const __nv_bfloat162 h = __float2bfloat162_rn(0.5f);
+    uint32_t* w = reinterpret_cast<uint32_t*>(&v);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        __nv_bfloat162 x = *reinterpret_cast<__nv_bfloat162*>(&w[i]);
+        x = __hmul2(x, h);
+        w[i] = *reinterpret_cast<uint32_t*>(&x);
+    }
+    return v;
+}
+
+// An FP32 bias as three BF16 parts hi + mid + lo (each remainder is exact in FP32), packed as
+// {hi, mid} and {lo, 0}.
+__device__ __forceinline__ uint2 bias_parts(float b)
+{
+    const float hi = __bfloat162float(__float2bfloat16_rn(b));
+    const float r1 = b - hi;
+    const float mid = __bfloat162float(__float2bfloat16_rn(r1));
+    const float lo = r1 - mid;
+    return make_uint2(pack_bf16(hi, mid), pack_bf16(lo, 0.0f));
 }
 
 // Named barrier of one slot's 128 threads.
@@ -540,19 +585,36 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const bf16* gW1 = wts;
     const bf16* gW2 = gW1 + kHid * kIn;
     const bf16* gW3 = gW2 + kHid * kHid;
+    static_assert(kIn == 48 && kResidualSlots + kTensorSlots == kIn, "bias columns 44..46 of W1");
     for (int v = tid; v < kHid * kIn / 8; v += kTcThreads) {
         const int r = v / (kIn / 8), c = v % (kIn / 8);
-        *reinterpret_cast<uint4*>(sm + kTcSW1 + core_off(r, c, kIn * 16)) = *reinterpret_cast<const uint4*>(gW1 + r * kIn + 8 * c);
+        uint4 w8 = *reinterpret_cast<const uint4*>(gW1 + r * kIn + 8 * c);
+        if (c == kIn / 8 - 1) {   // columns 40..47: 44..46 carry b1 (their inputs are 1), 47 is 0
+            const uint2 bp = bias_parts(bias[r]);
+            w8.z = bp.x;
+            w8.w = bp.y;
+        }
+        *reinterpret_cast<uint4*>(sm + kTcSW1 + core_off(r, c, kIn * 16)) = w8;
     }
     for (int v = tid; v < kHid * kHid / 8; v += kTcThreads) {
         const int r = v / (kHid / 8), c = v % (kHid / 8);
-        *reinterpret_cast<uint4*>(sm + kTcSW2 + core_off(r, c, kHid * 16)) = *reinterpret_cast<const uint4*>(gW2 + r * kHid + 8 * c);
+        *reinterpret_cast<uint4*>(sm + kTcSW2 + core_off(r, c, kHid * 16)) =
+            halve_bf16x8(*reinterpret_cast<const uint4*>(gW2 + r * kHid + 8 * c));
     }
     for (int v = tid; v < kOut * kHid / 8; v += kTcThreads) {
         const int r = v / (kHid / 8), c = v % (kHid / 8);
-        *reinterpret_cast<uint4*>(sm + kTcSW3 + core_off(r, c, kHid * 16)) = *reinterpret_cast<const uint4*>(gW3 + r * kHid + 8 * c);
+        *reinterpret_cast<uint4*>(sm + kTcSW3 + core_off(r, c, kHid * 16)) =
+            halve_bf16x8(*reinterpret_cast<const uint4*>(gW3 + r * kHid + 8 * c));
     }
     for (int v = tid; v < 2 * kHid + kOut; v += kTcThreads) sBias[v] = bias[v];
+    // Layer 2's bias chunk (K = 16): A = ones in K 0..2 for every face, B = b2 parts per unit.
+    for (int v = tid; v < 2 * kTcRows; v += kTcThreads) {
+        const int r = v >> 1, c = v & 1;
+        const uint2 bp = c == 0 ? bias_parts(bias[kHid + r]) : make_uint2(0, 0);
+        *reinterpret_cast<uint4*>(sm + kTcSOnes + core_off(r, c, 16 * 16)) =
+            c == 0 ? make_uint4(0x3F803F80u, 0x00003F80u, 0, 0) : make_uint4(0, 0, 0, 0);
+        *reinterpret_cast<uint4*>(sm + kTcSB2 + core_off(r, c, 16 * 16)) = make_uint4(bp.x, bp.y, 0, 0);
+    }
     if (row == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(mbar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -596,8 +658,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     load_neighbours((tile + stride) * kTcRows + row, nb, nbr, g);
     for (; tile < ntiles && ok; tile += stride) {
         const int f = tile * kTcRows + row;
-        // 1. inputs of face f into row `row` of the slot's input tile
+        // x entries this tile updates, loaded now so that the update at the end does not wait
+        float xo[BS];
+#pragma unroll
+        for (int c = 0; c < BS; c++) xo[c] = f < nb ? x[(long long)f * BS + c] : 0.0f;
+        // 1. inputs of face f into row `row` of the slot's input tile; input slots 44..46 (tensor
+        // slots 12..14, zero in every feature row) are set to 1 for the bias columns of W1
         sScale[row] = f < nb ? store_patch<BS>(v, sSlot, row) : 0.0f;
+        tb.z = 0x3F803F80u;
+        tb.w = 0x00003F80u;
         *reinterpret_cast<uint4*>(sSlot + core_off(row, kResidualSlots / 8, kIn * 16)) = ta;
         *reinterpret_cast<uint4*>(sSlot + core_off(row, kResidualSlots / 8 + 1, kIn * 16)) = tb;
         fence_async_smem();
@@ -619,7 +688,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         phase ^= 1;
         if (!ok) break;
         tc_fence_after();
-        tc_hidden_epilogue(t_lane, sBias, sSlot, row);
+        tc_hidden_epilogue(t_lane, sSlot, row);
         fence_async_smem();
         tc_fence_before();
         slot_sync(slot);
@@ -630,13 +699,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             for (int k = 0; k < kHid / 16; k++)
                 tc_mma(tmem, smem_desc(sSlot_a + k * 256, 128, kHid * 16), smem_desc(s_base + kTcSW2 + k * 256, 128, kHid * 16),
                        idesc_h, k > 0);
+            tc_mma(tmem, smem_desc(s_base + kTcSOnes, 128, 16 * 16), smem_desc(s_base + kTcSB2, 128, 16 * 16), idesc_h, 1);
             tc_commit(mbar);
         }
         ok = slot_and(slot, mbar_wait(mbar, phase));
         phase ^= 1;
         if (!ok) break;
         tc_fence_after();
-        tc_hidden_epilogue(t_lane, sBias + kHid, sSlot, row);
+        tc_hidden_epilogue(t_lane, sSlot, row);
         fence_async_smem();
         tc_fence_before();
         slot_sync(slot);
@@ -660,7 +730,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
             for (int c = 0; c < BS; c++) {
                 const float cv = sc * (y[c] + sBias[2 * kHid + c]);
-                if (isfinite(cv)) x[(long long)f * BS + c] += cv;
+                if (isfinite(cv)) x[(long long)f * BS + c] = xo[c] + cv;
             }
         }
         tc_fence_before();

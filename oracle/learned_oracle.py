@@ -52,14 +52,15 @@ def gelu(a):
 
 
 def gelu_bf16(a):
-    """The activation as the GPU evaluates it: bf16 inputs, bf16x2 arithmetic (one rounding per
-    multiply or FMA), tanh rounded to bf16 (the GPU's bf16x2 hardware tanh can differ in the last
-    bit), result bf16: 0.5 x (1 + tanh(c0 x (1 + c1 x^2)))."""
+    """The activation as the GPU evaluates it (fhg_learned.cu: gelu_tanh_bf16x2, gelu_bf16x2):
+    bf16 inputs, bf16x2 arithmetic (one rounding per multiply or FMA), tanh rounded to bf16 (the
+    GPU's bf16x2 hardware tanh can differ in the last bit), result bf16:
+    h + h tanh(x (c0 + c0 c1 x^2)), h = x / 2, with c0 and c0 c1 (an FP32 product) rounded to bf16."""
     x = bf16(a)
-    c0, c1 = bf16(GELU_C0), bf16(GELU_C1)
-    p = bf16(x * x)
-    p = bf16(p * c1 + 1.0)
-    u = bf16(bf16(x * c0) * p)
+    c0 = bf16(np.float32(GELU_C0))
+    c01 = bf16(np.float32(GELU_C0) * np.float32(GELU_C1))
+    q = bf16(bf16(x * x) * c01 + c0)
+    u = bf16(x * q)
     t = bf16(np.tanh(u))
     h = bf16(0.5 * x)
     return bf16(h * t + h)
