@@ -98,10 +98,10 @@ struct fhg_ctx {
     int* counter_d = nullptr;
     double* nr_host = nullptr;   // pinned
     double* io = nullptr;        // user-numbered I/O scratch (2 * n0)
-    // Double-FP32 outer iteration (FP32 V-cycle with the split outer operator): x as an FP32 pair
-    // (hi: n floats, then lo: n) and the low part of r, whose high part is the V-cycle input b32;
-    // d and Ad live as pairs in kz[p] and kAd[p] (hi: n floats, then lo).
-    float *xdf = nullptr, *rlo = nullptr;
+    // Double-FP32 outer iteration (FP32 V-cycle with the split outer operator): the low part of r,
+    // whose high part is the V-cycle input b32; d and Ad live as FP32 pairs in kz[p] and kAd[p]
+    // (hi: n floats, then lo); x stays FP64 in kx.
+    float* rlo = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     long long graph_kernels[2] = {0, 0};
     int graphs_built = 0;
@@ -907,19 +907,17 @@ double* part(fhg_ctx* ctx, int i) { return ctx->partials + (size_t)i * fhg::kRed
 bool outer_df(const fhg_ctx* ctx)
 {
     return ctx->opts.vcycle_precision == FHG_PREC_FP32 && ctx->opts.krylov == FHG_KRYLOV_FCG &&
-           ctx->levels[0].ahat_lo && ctx->xdf;
+           ctx->levels[0].ahat_lo && ctx->rlo;
 }
 
 // FP32 pair views of an n-long FP64 buffer (hi: first n floats, lo: next n).
 float* pair_hi(double* v) { return reinterpret_cast<float*>(v); }
 float* pair_lo(double* v, long long n) { return reinterpret_cast<float*>(v) + n; }
 
-// Start of a double-FP32 outer iteration: x = 0 and (b32, rlo) = r.
+// Start of a double-FP32 outer iteration: (b32, rlo) = r.
 void outer_df_start(fhg_ctx* ctx, const double* r)
 {
-    const long long n = ctx->levels[0].n;
-    cudaMemsetAsync(ctx->xdf, 0, sizeof(float) * 2 * n, ctx->stream);
-    fhg::launch_split_df(n, r, ctx->levels[0].b32, ctx->rlo, ctx->stream);
+    fhg::launch_split_df(ctx->levels[0].n, r, ctx->levels[0].b32, ctx->rlo, ctx->stream);
 }
 
 // One FCG(1) iteration (src/Solver/Krylov/FlexibleConjugateGradient.h:80-162), parity p
@@ -935,14 +933,14 @@ void fcg_iteration(fhg_ctx* ctx, int p)
     Level& L0 = ctx->levels[0];
     const bool fp32 = ctx->opts.vcycle_precision == FHG_PREC_FP32;
     if (outer_df(ctx)) {
-        // FP32 pairs throughout: z = M r_hi (FP32 V-cycle), d = z - s dp, Ad = Â d, x += alpha d,
-        // r -= alpha Ad, with no FP64 instruction per element.
+        // FP32 pairs for r, d, Ad: z = M r_hi (FP32 V-cycle), d = z - s dp, Ad = Â d, r -= alpha Ad
+        // with no FP64 instruction per element; x += alpha d in FP64.
         vcycle<float>(ctx, 0, L0.b32, L0.x32);
         float *dh = pair_hi(z), *dl = pair_lo(z, n), *Adh = pair_hi(Ad), *Adl = pair_lo(Ad, n);
         fhg::launch_dot_df(n, L0.x32, pair_hi(Adp), pair_lo(Adp, n), part(ctx, 0), s);
         fhg::launch_fcg_direction_df(n, L0.x32, pair_hi(dp), pair_lo(dp, n), part(ctx, 0), ctx->scal + 1, dh, dl, s);
         fhg::launch_spmv_dots_df(L0.Ahat_hi.v, L0.ahat_lo, dh, dl, L0.b32, ctx->rlo, Adh, Adl, part(ctx, 1), s);
-        fhg::launch_krylov_step_df(n, ctx->xdf, ctx->xdf + n, L0.b32, ctx->rlo, dh, dl, Adh, Adl, part(ctx, 2),
+        fhg::launch_krylov_step_df(n, ctx->kx, L0.b32, ctx->rlo, dh, dl, Adh, Adl, part(ctx, 2),
                                    part(ctx, 1), ctx->scal + 1, part(ctx, 3), s);
         fhg::launch_finalize_norm(part(ctx, 3), ctx->scal + 0, ctx->scal + 2, ctx->hist_d, ctx->counter_d,
                                   ctx->opts.max_iterations + 1, s);
@@ -1109,7 +1107,7 @@ void free_all(fhg_ctx* ctx)
 {
     free_graphs(ctx);
     ctx->nbr_d = nullptr; ctx->tfeat_d = nullptr; ctx->lw = nullptr; ctx->lstatus = nullptr;
-    ctx->xdf = nullptr; ctx->rlo = nullptr;
+    ctx->rlo = nullptr;
     ctx->lparams = nullptr; ctx->lwts = nullptr; ctx->lbias = nullptr;
     ctx->learned_mode = FHG_LEARNED_OFF;
     ctx->learned_now = false;
@@ -1152,7 +1150,7 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
     const int one = 1;
     CK(cudaMemcpyAsync(ctx->counter_d, &one, sizeof(int), cudaMemcpyHostToDevice, s));
     if (outer_df(ctx))
-        outer_df_start(ctx, ctx->kr);  // x = 0 and r = b as FP32 pairs
+        outer_df_start(ctx, ctx->kr);  // r = b as an FP32 pair
     else if (ctx->opts.krylov == FHG_KRYLOV_FCG && ctx->opts.vcycle_precision == FHG_PREC_FP32)
         fhg::launch_convert<double, float>(n, ctx->kr, L0.b32, s);  // FP32 copy of r = b
     if (ctx->opts.krylov == FHG_KRYLOV_CG) {
@@ -1215,7 +1213,6 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
         }
         if (learned_its > 0 && status == FHG_OK) status = check_learned_status(ctx);
         if (status != FHG_OK) break;
-        if (outer_df(ctx)) fhg::launch_join_df(n, ctx->xdf, ctx->xdf + n, ctx->kx, s);
         // The FP64 true residual ||b - A x|| / ||b|| judges the solve (A the full level-0 operator).
         fhg::launch_spmv<double>(L0.A.v, fhg::kSpmvResidual, ctx->kx, ctx->kb, ctx->kt, s);
         fhg::launch_dot(n, ctx->kt, ctx->kt, part(ctx, 0), s);
@@ -1588,9 +1585,8 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         (rc = dalloc(ctx, &ctx->hist_d, (size_t)o.max_iterations + 2)) || (rc = dalloc(ctx, &ctx->counter_d, 1)) ||
         (rc = dalloc(ctx, &ctx->io, (size_t)2 * n0)))
         return rc;
-    ctx->xdf = nullptr;
     ctx->rlo = nullptr;
-    if (fp32 && o.outer_split && ((rc = dalloc(ctx, &ctx->xdf, 2 * n0)) || (rc = dalloc(ctx, &ctx->rlo, n0)))) return rc;
+    if (fp32 && o.outer_split && (rc = dalloc(ctx, &ctx->rlo, n0))) return rc;
     CK(cudaMallocHost(&ctx->nr_host, sizeof(double)));
 
     if (o.autotune) {
@@ -1869,7 +1865,7 @@ int fhg_time_op(fhg_ctx* ctx, int level, int op, int precision, int warmup, int 
         Level& L0 = ctx->levels[0];
         const bool split = op == FHG_OP_SYM_SPMV && precision == FHG_PREC_FP32;
         if (precision != FHG_PREC_FP64 && !split) return fail(ctx, FHG_ERR_INVALID_ARG, "op %d is timed in FP64 only", op);
-        if (split && (!L0.ahat_lo || !ctx->xdf))
+        if (split && (!L0.ahat_lo || !ctx->rlo))
             return fail(ctx, FHG_ERR_NOT_READY, "the double-FP32 outer operator was not built at setup");
         const size_t n0 = L0.n;
         double* t = nullptr;
@@ -2375,7 +2371,6 @@ void batch_epilogue(fhg_ctx* ctx)
     Level& L0 = ctx->levels[0];
     const long long n = L0.n;
     cudaStream_t s = ctx->stream;
-    if (outer_df(ctx)) fhg::launch_join_df(n, ctx->xdf, ctx->xdf + n, ctx->kx, s);
     fhg::launch_spmv<double>(L0.A.v, fhg::kSpmvResidual, ctx->kx, ctx->kb, ctx->kt, s);
     fhg::launch_dot(n, ctx->kt, ctx->kt, part(ctx, 0), s);
     fhg::launch_sqrt_sum(part(ctx, 0), ctx->scal + 5, s);

@@ -71,7 +71,7 @@ void launch_dot_mixed(long long n, const float* a, const double* b, double* part
 void launch_fcg_direction_mixed(long long n, const float* z, const double* dp, const double* partials_zadp,
                                 const double* dadp, double* d, cudaStream_t s, float* dhi = nullptr,
                                 float* dlo = nullptr);
-// Double-FP32 outer iteration (FP32 pairs hi + lo for x, r, d, Ad; FP64 Krylov scalars).
+// Double-FP32 outer iteration (FP32 pairs hi + lo for r, d, Ad; FP64 x and Krylov scalars).
 // Ad = Â d (Â = hi + lo), partials as launch_spmv_dots (d.Ad, then r.d).
 void launch_spmv_dots_df(const BsrView<float>& Ahi, const float* vlo, const float* dhi, const float* dlo,
                          const float* rhi, const float* rlo, float* Adhi, float* Adlo, double* partials,
@@ -81,13 +81,12 @@ void launch_dot_df(long long n, const float* z, const float* ah, const float* al
 // d = z - s dp, s = sum(partials_zadp) / *dadp.
 void launch_fcg_direction_df(long long n, const float* z, const float* dph, const float* dpl,
                              const double* partials_zadp, const double* dadp, float* dh, float* dl, cudaStream_t s);
-// As launch_krylov_step on pairs; rh doubles as the next V-cycle's FP32 right-hand side.
-void launch_krylov_step_df(long long n, float* xh, float* xl, float* rh, float* rl, const float* dh, const float* dl,
+// As launch_krylov_step with r, d, Ad as pairs; rh doubles as the next V-cycle's FP32 right-hand side.
+void launch_krylov_step_df(long long n, double* x, float* rh, float* rl, const float* dh, const float* dl,
                            const float* Adh, const float* Adl, const double* partials_num,
                            const double* partials_den, double* den_out, double* partials_rr, cudaStream_t s);
-// v -> (h, l) and back.
+// v -> (h, l).
 void launch_split_df(long long n, const double* v, float* h, float* l, cudaStream_t s);
-void launch_join_df(long long n, const float* h, const float* l, double* v, cudaStream_t s);
 // ||r|| / ||b||: reduces partials_rr, divides by *bnorm, writes *nr_out and hist[*counter],
 // then ++*counter.
 void launch_finalize_norm(const double* partials_rr, const double* bnorm, double* nr_out,

@@ -679,8 +679,10 @@ __global__ void __launch_bounds__(kReduceThreads) k_krylov_step(long long n, dou
     if (threadIdx.x == 0) prr[blockIdx.x] = rr;
 }
 
-// Double-FP32 outer iteration: x, r, d and Ad are FP32 pairs (hi, lo), so that no FP64 instruction
-// runs per element; the Krylov scalars stay FP64 and are split into pairs once per thread.
+// Double-FP32 outer iteration: r, d and Ad are FP32 pairs (hi, lo), so that the direction update
+// and the dot products run no FP64 instruction per element; the Krylov scalars stay FP64 and are
+// split into pairs once per thread. x stays FP64: its rounding sets the floor of the true residual
+// ||b - A x|| (about kappa times the unit roundoff of x), which a pair (2^-48) would raise 32-fold.
 // partials of z.Adp with z the FP32 V-cycle output.
 __global__ void __launch_bounds__(kReduceThreads) k_dot_df(long long n, const float* __restrict__ z,
                                                            const float* __restrict__ ah, const float* __restrict__ al,
@@ -725,10 +727,10 @@ __global__ void __launch_bounds__(kReduceThreads) k_fcg_direction_df(long long n
                      });
 }
 
-// alpha = num / den; x += alpha d; r -= alpha Ad (rh is the next V-cycle's FP32 right-hand side);
-// partials_rr of r.r; *den_out = den.
-__global__ void __launch_bounds__(kReduceThreads) k_krylov_step_df(long long n, float* __restrict__ xh,
-                                                                   float* __restrict__ xl, float* __restrict__ rh,
+// alpha = num / den; x += alpha d (FP64); r -= alpha Ad (rh is the next V-cycle's FP32 right-hand
+// side); partials_rr of r.r; *den_out = den.
+__global__ void __launch_bounds__(kReduceThreads) k_krylov_step_df(long long n, double* __restrict__ x,
+                                                                   float* __restrict__ rh,
                                                                    float* __restrict__ rl, const float* __restrict__ dh,
                                                                    const float* __restrict__ dl,
                                                                    const float* __restrict__ Adh,
@@ -741,19 +743,18 @@ __global__ void __launch_bounds__(kReduceThreads) k_krylov_step_df(long long n, 
     const double num = reduce_partials(pnum, sh);
     const double den = reduce_partials(pden, sh);
     if (blockIdx.x == 0 && threadIdx.x == 0 && den_out) *den_out = den;
+    const double alpha = num / den;
     float ah, al;
-    df_split(num / den, ah, al);
+    df_split(alpha, ah, al);
     float rrh = 0.f, rrl = 0.f;
     struct E {
-        float xh, xl, rh, rl, dh, dl, ah, al;
+        double x;
+        float rh, rl, dh, dl, ah, al;
     };
-    for_each_element(n, [&](long long i) { return E{xh[i], xl[i], rh[i], rl[i], dh[i], dl[i], Adh[i], Adl[i]}; },
+    for_each_element(n, [&](long long i) { return E{x[i], rh[i], rl[i], dh[i], dl[i], Adh[i], Adl[i]}; },
                      [&](long long i, const E& e) {
                          float ph, pl, h, l;
-                         df_mul(ah, al, e.dh, e.dl, ph, pl);
-                         df_sum(e.xh, e.xl, ph, pl, h, l);
-                         xh[i] = h;
-                         xl[i] = l;
+                         x[i] = fma(alpha, (double)e.dh + (double)e.dl, e.x);
                          df_mul(ah, al, e.ah, e.al, ph, pl);
                          df_sum(e.rh, e.rl, -ph, -pl, h, l);
                          rh[i] = h;
@@ -765,7 +766,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_krylov_step_df(long long n, 
     if (threadIdx.x == 0) prr[blockIdx.x] = rr;
 }
 
-// FP64 <-> FP32 pair (the boundaries of the double-FP32 iteration).
+// FP64 -> FP32 pair (the start of the double-FP32 iteration and residual replacement).
 __global__ void __launch_bounds__(kThreads) k_split_df(long long n, const double* __restrict__ v, float* __restrict__ h,
                                                       float* __restrict__ l)
 {
@@ -773,12 +774,6 @@ __global__ void __launch_bounds__(kThreads) k_split_df(long long n, const double
     if (i < n) df_split(v[i], h[i], l[i]);
 }
 
-__global__ void __launch_bounds__(kThreads) k_join_df(long long n, const float* __restrict__ h,
-                                                     const float* __restrict__ l, double* __restrict__ v)
-{
-    const long long i = (long long)blockIdx.x * kThreads + threadIdx.x;
-    if (i < n) v[i] = (double)h[i] + (double)l[i];
-}
 
 __global__ void __launch_bounds__(kReduceThreads) k_cg_step(long long n, double* __restrict__ x, double* __restrict__ r,
                                                             const double* __restrict__ d, const double* __restrict__ Ad,
@@ -1076,11 +1071,11 @@ void launch_fcg_direction_df(long long n, const float* z, const float* dph, cons
     g_kernel_launches++;
 }
 
-void launch_krylov_step_df(long long n, float* xh, float* xl, float* rh, float* rl, const float* dh, const float* dl,
+void launch_krylov_step_df(long long n, double* x, float* rh, float* rl, const float* dh, const float* dl,
                            const float* Adh, const float* Adl, const double* partials_num,
                            const double* partials_den, double* den_out, double* partials_rr, cudaStream_t s)
 {
-    k_krylov_step_df<<<kReduceCtas, kReduceThreads, 0, s>>>(n, xh, xl, rh, rl, dh, dl, Adh, Adl, partials_num,
+    k_krylov_step_df<<<kReduceCtas, kReduceThreads, 0, s>>>(n, x, rh, rl, dh, dl, Adh, Adl, partials_num,
                                                             partials_den, den_out, partials_rr);
     g_kernel_launches++;
 }
@@ -1091,11 +1086,6 @@ void launch_split_df(long long n, const double* v, float* h, float* l, cudaStrea
     g_kernel_launches++;
 }
 
-void launch_join_df(long long n, const float* h, const float* l, double* v, cudaStream_t s)
-{
-    k_join_df<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, h, l, v);
-    g_kernel_launches++;
-}
 
 void launch_cg_step(long long n, double* x, double* r, const double* d, const double* Ad, const double* num,
                     const double* partials_den, double* partials_rr, cudaStream_t s)
