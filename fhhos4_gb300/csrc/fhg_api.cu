@@ -1029,22 +1029,35 @@ int build_graphs(fhg_ctx* ctx, bool learned = false)
 template <class F>
 int tune(fhg_ctx* ctx, int bs, int& lanes, int& unroll, F run)
 {
-    float best = 1e30f;
-    int bestG = lanes, bestU = unroll;
-    for (int U : {1, 2}) {
-        if (U == 2 && bs > 3) continue;
-        for (int G : {4, 8, 16, 32}) {
-            for (int w = 0; w < 2; w++) run(G, U);
-            CK(cudaEventRecord(ctx->ev0, ctx->stream));
-            const int reps = 8;
-            for (int r = 0; r < reps; r++) run(G, U);
-            CK(cudaEventRecord(ctx->ev1, ctx->stream));
-            CK(cudaEventSynchronize(ctx->ev1));
-            float ms = 0;
-            CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-            if (ms < best) { best = ms; bestG = G; bestU = U; }
+    // Three rounds over all candidates, each candidate's time the minimum over the rounds: a
+    // single timing per candidate let one slow measurement decide, and the chosen shapes then
+    // changed from run to run.
+    constexpr int kRounds = 3;
+    float t[2][4];
+    for (auto& row : t)
+        for (float& v : row) v = 1e30f;
+    for (int round = 0; round < kRounds; round++) {
+        for (int U : {1, 2}) {
+            if (U == 2 && bs > 3) continue;
+            for (int gi = 0; gi < 4; gi++) {
+                const int G = 4 << gi;
+                for (int w = 0; w < 2; w++) run(G, U);
+                CK(cudaEventRecord(ctx->ev0, ctx->stream));
+                const int reps = 8;
+                for (int r = 0; r < reps; r++) run(G, U);
+                CK(cudaEventRecord(ctx->ev1, ctx->stream));
+                CK(cudaEventSynchronize(ctx->ev1));
+                float ms = 0;
+                CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+                t[U - 1][gi] = std::min(t[U - 1][gi], ms);
+            }
         }
     }
+    float best = 1e30f;
+    int bestG = lanes, bestU = unroll;
+    for (int U : {1, 2})
+        for (int gi = 0; gi < 4; gi++)
+            if (t[U - 1][gi] < best) { best = t[U - 1][gi]; bestG = 4 << gi; bestU = U; }
     lanes = bestG;
     unroll = bestU;
     return FHG_OK;

@@ -15,6 +15,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <utility>
 
 namespace fhg {
 
@@ -23,6 +25,40 @@ std::atomic<long long> g_kernel_launches{0};
 namespace {
 
 constexpr int kThreads = 256;
+
+// Programmatic dependent launch: every kernel of this file is launched with programmatic stream
+// serialization, so the next kernel's CTAs are scheduled while its predecessor drains instead of
+// after it, and begins with pdl_wait() (griddepcontrol.wait), which returns once the predecessor
+// grid has completed and its memory writes are visible. No global access precedes the wait, so
+// the order of every read and write is that of plain stream order; only launch latency overlaps.
+// Kernels launched without the attribute pass the wait at once. FHG_PDL=0 in the environment
+// launches without it.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+
+bool pdl_enabled()
+{
+    static const bool on = [] {
+        const char* e = std::getenv("FHG_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+template <class... KArgs, class... Args>
+void pdl_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 template <int G, class T>
 __device__ __forceinline__ T group_sum(T v)
@@ -174,6 +210,7 @@ __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int nbr, const int* __res
                                                        const T* __restrict__ vals, long long ld,
                                                        const T* __restrict__ x, const T* aux, T* y)
 {
+    pdl_wait();
     const int lane = threadIdx.x & (G - 1);
     const int row = (int)(((long long)blockIdx.x * kThreads + threadIdx.x) / G);
     T acc[BS];
@@ -211,6 +248,7 @@ __global__ void __launch_bounds__(kThreads) k_bsr_residual_dinv(int nbr, const i
                                                                 const T* __restrict__ x, const T* __restrict__ b,
                                                                 T* __restrict__ w)
 {
+    pdl_wait();
     const int lane = threadIdx.x & (G - 1);
     const int row = (int)(((long long)blockIdx.x * kThreads + threadIdx.x) / G);
     T acc[BS];
@@ -248,6 +286,7 @@ __global__ void __launch_bounds__(kThreads) k_bsr_gs(int row0, int row1, const i
                                                      const T* __restrict__ dinv, long long dld,
                                                      const T* __restrict__ b, T* x, int col_lo, int col_hi)
 {
+    pdl_wait();
     const int lane = threadIdx.x & (G - 1);
     const int row = row0 + (int)(((long long)blockIdx.x * kThreads + threadIdx.x) / G);
     T acc[BS];
@@ -306,6 +345,7 @@ __global__ void __launch_bounds__(kThreads) k_bsr_jacobi(int nbr, const int* __r
                                                          const T* __restrict__ b, const T* __restrict__ xold,
                                                          T* __restrict__ xnew)
 {
+    pdl_wait();
     const int lane = threadIdx.x & (G - 1);
     const int row = (int)(((long long)blockIdx.x * kThreads + threadIdx.x) / G);
     T off[BS], dia[BS];
@@ -360,6 +400,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots(int nbr, const
                                                                   double* __restrict__ Ad,
                                                                   double* __restrict__ partials)
 {
+    pdl_wait();
     __shared__ double sh[33];
     const int lane = threadIdx.x & (G - 1);
     // Loop bounds are uniform per warp (every lane runs the same shuffle rounds).
@@ -458,6 +499,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots_df(int nbr, co
                                                                      float* __restrict__ Adhi, float* __restrict__ Adlo,
                                                                      double* __restrict__ partials)
 {
+    pdl_wait();
     __shared__ double sh_red[33];
     const int lane = threadIdx.x & (G - 1);
     constexpr int kGroupsPerWarp = 32 / G;
@@ -539,6 +581,7 @@ template <class T>
 __global__ void __launch_bounds__(kThreads) k_coarse(int n, const double* __restrict__ cinv,
                                                      const T* __restrict__ b, T* __restrict__ x)
 {
+    pdl_wait();
     const int lane = threadIdx.x & 31;
     const int row = (blockIdx.x * kThreads + threadIdx.x) >> 5;
     if (row >= n) return;  // whole warps exit together
@@ -552,6 +595,7 @@ __global__ void __launch_bounds__(kThreads) k_coarse(int n, const double* __rest
 __global__ void __launch_bounds__(kReduceThreads) k_dot(long long n, const double* __restrict__ a,
                                                         const double* __restrict__ b, double* __restrict__ partials)
 {
+    pdl_wait();
     __shared__ double sh[33];
     double v = 0.0;
     for_each_element(n, [&](long long i) { return Pair2<double, double>{a[i], b[i]}; },
@@ -568,6 +612,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_dots3(long long n, int nq, c
                                                           const T* __restrict__ b1, const T* __restrict__ a2,
                                                           const T* __restrict__ b2, double* __restrict__ partials)
 {
+    pdl_wait();
     __shared__ double sh[33];
     double v0 = 0.0, v1 = 0.0, v2 = 0.0;
     struct E {
@@ -602,6 +647,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_dots3(long long n, int nq, c
 template <class T>
 __global__ void k_axpy(long long n, double alpha, const T* __restrict__ x, T* __restrict__ y)
 {
+    pdl_wait();
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         y[i] = y[i] + (T)alpha * x[i];
 }
@@ -610,6 +656,7 @@ template <class T>
 __global__ void k_lincomb(long long n, double a, const T* __restrict__ c, double b, const T* __restrict__ d,
                           T* __restrict__ out)
 {
+    pdl_wait();
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         out[i] = (T)a * c[i] + (T)b * d[i];
 }
@@ -617,6 +664,7 @@ __global__ void k_lincomb(long long n, double a, const T* __restrict__ c, double
 __global__ void __launch_bounds__(kReduceThreads) k_dot_mixed(long long n, const float* __restrict__ a,
                                                               const double* __restrict__ b, double* __restrict__ partials)
 {
+    pdl_wait();
     __shared__ double sh[33];
     double v = 0.0;
     for_each_element(n, [&](long long i) { return Pair2<float, double>{a[i], b[i]}; },
@@ -631,6 +679,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_fcg_direction_mixed(long lon
                                                                         const double* __restrict__ dadp, double* __restrict__ d,
                                                                         float* __restrict__ dhi, float* __restrict__ dlo)
 {
+    pdl_wait();
     __shared__ double sh[33];
     const double s = reduce_partials(partials, sh) / *dadp;
     for_each_element(n, [&](long long i) { return Pair2<float, double>{z[i], dp[i]}; },
@@ -649,6 +698,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_fcg_direction(long long n, c
                                                                   const double* __restrict__ partials,
                                                                   const double* __restrict__ dadp, double* d)
 {
+    pdl_wait();
     __shared__ double sh[33];
     const double s = reduce_partials(partials, sh) / *dadp;
     for_each_element(n, [&](long long i) { return Pair2<double, double>{z[i], dp[i]}; },
@@ -661,6 +711,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_krylov_step(long long n, dou
                                                                 double* __restrict__ den_out, double* __restrict__ prr,
                                                                 float* __restrict__ r32)
 {
+    pdl_wait();
     __shared__ double sh[33];
     const double num = reduce_partials(pnum, sh);
     const double den = reduce_partials(pden, sh);
@@ -688,6 +739,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_dot_df(long long n, const fl
                                                            const float* __restrict__ ah, const float* __restrict__ al,
                                                            double* __restrict__ partials)
 {
+    pdl_wait();
     __shared__ double sh[33];
     float vh = 0.f, vl = 0.f;
     struct E {
@@ -711,6 +763,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_fcg_direction_df(long long n
                                                                      const double* __restrict__ dadp,
                                                                      float* __restrict__ dh, float* __restrict__ dl)
 {
+    pdl_wait();
     __shared__ double sh[33];
     float sh_, sl_;
     df_split(reduce_partials(partials, sh) / *dadp, sh_, sl_);
@@ -739,6 +792,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_krylov_step_df(long long n, 
                                                                    const double* __restrict__ pden,
                                                                    double* __restrict__ den_out, double* __restrict__ prr)
 {
+    pdl_wait();
     __shared__ double sh[33];
     const double num = reduce_partials(pnum, sh);
     const double den = reduce_partials(pden, sh);
@@ -770,6 +824,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_krylov_step_df(long long n, 
 __global__ void __launch_bounds__(kThreads) k_split_df(long long n, const double* __restrict__ v, float* __restrict__ h,
                                                       float* __restrict__ l)
 {
+    pdl_wait();
     const long long i = (long long)blockIdx.x * kThreads + threadIdx.x;
     if (i < n) df_split(v[i], h[i], l[i]);
 }
@@ -780,6 +835,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_cg_step(long long n, double*
                                                             const double* __restrict__ num, const double* __restrict__ pden,
                                                             double* __restrict__ prr)
 {
+    pdl_wait();
     __shared__ double sh[33];
     const double den = reduce_partials(pden, sh);
     const double alpha = *num / den;
@@ -798,6 +854,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_cg_step(long long n, double*
 __global__ void __launch_bounds__(kReduceThreads) k_cg_direction(long long n, const double* __restrict__ z,
                                                                  const double* __restrict__ beta, double* __restrict__ d)
 {
+    pdl_wait();
     const double bt = *beta;
     for_each_element(n, [&](long long i) { return Pair2<double, double>{z[i], d[i]}; },
                      [&](long long i, const Pair2<double, double>& e) { d[i] = e.a + bt * e.b; });
@@ -806,6 +863,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_cg_direction(long long n, co
 __global__ void __launch_bounds__(kReduceThreads) k_finalize_norm(const double* __restrict__ prr, const double* __restrict__ bnorm,
                                                                   double* nr_out, double* hist, int* counter, int hist_len)
 {
+    pdl_wait();
     __shared__ double sh[33];
     const double rn = sqrt(reduce_partials(prr, sh));
     if (threadIdx.x == 0) {
@@ -820,6 +878,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_finalize_norm(const double* 
 
 __global__ void __launch_bounds__(kReduceThreads) k_sqrt_sum(const double* __restrict__ p, double* out)
 {
+    pdl_wait();
     __shared__ double sh[33];
     const double v = reduce_partials(p, sh);
     if (threadIdx.x == 0) *out = sqrt(v);
@@ -827,6 +886,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_sqrt_sum(const double* __res
 
 __global__ void __launch_bounds__(kReduceThreads) k_sum(const double* __restrict__ p, double* out)
 {
+    pdl_wait();
     __shared__ double sh[33];
     const double v = reduce_partials(p, sh);
     if (threadIdx.x == 0) *out = v;
@@ -834,6 +894,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_sum(const double* __restrict
 
 __global__ void __launch_bounds__(kReduceThreads) k_cg_beta(const double* __restrict__ p, double* rz, double* beta)
 {
+    pdl_wait();
     __shared__ double sh[33];
     const double v = reduce_partials(p, sh);
     if (threadIdx.x == 0) {
@@ -845,6 +906,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_cg_beta(const double* __rest
 template <class Tin, class Tout>
 __global__ void __launch_bounds__(kThreads) k_convert(long long n, const Tin* __restrict__ in, Tout* __restrict__ out)
 {
+    pdl_wait();
     const long long i = (long long)blockIdx.x * kThreads + threadIdx.x;
     if (i < n) out[i] = (Tout)in[i];
 }
@@ -853,6 +915,7 @@ template <class T>
 __global__ void __launch_bounds__(kThreads) k_permute(int nb, int bs, const int* __restrict__ perm,
                                                       const T* __restrict__ in, T* __restrict__ out, int gather)
 {
+    pdl_wait();
     const long long i = (long long)blockIdx.x * kThreads + threadIdx.x;
     if (i >= (long long)nb * bs) return;
     const int blk = (int)(i / bs), c = (int)(i - (long long)blk * bs);
@@ -891,11 +954,11 @@ template <class T, int BS, int G, int U>
 void spmv_u(const BsrView<T>& A, unsigned grid, int mode, const T* x, const T* aux, T* y, cudaStream_t s)
 {
     if (mode == kSpmvAssign)
-        k_bsr_spmv<T, BS, G, U, kSpmvAssign><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
+        pdl_launch(k_bsr_spmv<T, BS, G, U, kSpmvAssign>, grid, kThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
     else if (mode == kSpmvResidual)
-        k_bsr_spmv<T, BS, G, U, kSpmvResidual><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
+        pdl_launch(k_bsr_spmv<T, BS, G, U, kSpmvResidual>, grid, kThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
     else
-        k_bsr_spmv<T, BS, G, U, kSpmvAddTo><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
+        pdl_launch(k_bsr_spmv<T, BS, G, U, kSpmvAddTo>, grid, kThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
 }
 
 template <class T>
@@ -910,21 +973,28 @@ void launch_spmv(const BsrView<T>& A, int mode, const T* x, const T* aux, T* y, 
     g_kernel_launches++;
 }
 
+// The scaled residual needs G >= bs (lane r applies row r of D^-1); inside a template the other
+// shapes are discarded rather than instantiated.
+template <int BS, int G>
+void residual_dinv_shape(const BsrView<float>& A, unsigned grid, const float* dinv, long long dld, const float* x,
+                         const float* b, float* w, cudaStream_t s)
+{
+    if constexpr (G >= BS) {
+        if (A.unroll == 2)
+            pdl_launch(k_bsr_residual_dinv<float, BS, G, 2>, grid, kThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals,
+                       A.ld, dinv, dld, x, b, w);
+        else
+            pdl_launch(k_bsr_residual_dinv<float, BS, G, 1>, grid, kThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals,
+                       A.ld, dinv, dld, x, b, w);
+    }
+}
+
 void launch_residual_dinv(const BsrView<float>& A, const float* dinv, long long dld, const float* x, const float* b,
                           float* w, cudaStream_t s)
 {
     if (A.nbr == 0) return;
     const unsigned grid = grid_for((long long)A.nbr * A.lanes, kThreads);
-    FHG_DISPATCH_BS_G(A.bs, A.lanes, {
-        if constexpr (G >= BS) {
-            if (A.unroll == 2)
-                k_bsr_residual_dinv<float, BS, G, 2><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld,
-                                                                                dinv, dld, x, b, w);
-            else
-                k_bsr_residual_dinv<float, BS, G, 1><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld,
-                                                                                dinv, dld, x, b, w);
-        }
-    });
+    FHG_DISPATCH_BS_G(A.bs, A.lanes, { residual_dinv_shape<BS, G>(A, grid, dinv, dld, x, b, w, s); });
     g_kernel_launches++;
 }
 
@@ -936,10 +1006,10 @@ void launch_gs(const BsrView<T>& A, int row0, int row1, const T* dinv, long long
     const unsigned grid = grid_for((long long)(row1 - row0) * A.lanes, kThreads);
     FHG_DISPATCH_BS_G(A.bs, A.lanes, {
         if (A.unroll == 2)
-            k_bsr_gs<T, BS, G, 2><<<grid, kThreads, 0, s>>>(row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, b,
+            pdl_launch(k_bsr_gs<T, BS, G, 2>, grid, kThreads, 0, s, row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, b,
                                                             x, col_lo, col_hi);
         else
-            k_bsr_gs<T, BS, G, 1><<<grid, kThreads, 0, s>>>(row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, b,
+            pdl_launch(k_bsr_gs<T, BS, G, 1>, grid, kThreads, 0, s, row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, b,
                                                             x, col_lo, col_hi);
     });
     g_kernel_launches++;
@@ -952,7 +1022,7 @@ void launch_jacobi(const BsrView<T>& A, const T* dinv, long long dld, T omega, c
     if (A.nbr == 0) return;
     const unsigned grid = grid_for((long long)A.nbr * A.lanes, kThreads);
     FHG_DISPATCH_BS_G(A.bs, A.lanes, {
-        k_bsr_jacobi<T, BS, G><<<grid, kThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, omega, b,
+        pdl_launch(k_bsr_jacobi<T, BS, G>, grid, kThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, omega, b,
                                                          xold, xnew);
     });
     g_kernel_launches++;
@@ -962,7 +1032,7 @@ void launch_spmv_dots(const BsrView<double>& A, const double* d, const double* r
                       cudaStream_t s)
 {
     FHG_DISPATCH_BS_G(A.bs, A.lanes, {
-        k_bsr_spmv_dots<BS, G><<<kReduceCtas, kReduceThreads, 0, s>>>(A.nbr, A.rowptr, A.colidx, A.vals, A.ld, d, r,
+        pdl_launch(k_bsr_spmv_dots<BS, G>, kReduceCtas, kReduceThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals, A.ld, d, r,
                                                                       Ad, partials);
     });
     g_kernel_launches++;
@@ -971,13 +1041,13 @@ void launch_spmv_dots(const BsrView<double>& A, const double* d, const double* r
 template <class T>
 void launch_coarse(int n, const double* cinv, const T* b, T* x, cudaStream_t s)
 {
-    k_coarse<T><<<grid_for((long long)n * 32, kThreads), kThreads, 0, s>>>(n, cinv, b, x);
+    pdl_launch(k_coarse<T>, grid_for((long long)n * 32, kThreads), kThreads, 0, s, n, cinv, b, x);
     g_kernel_launches++;
 }
 
 void launch_dot(long long n, const double* a, const double* b, double* partials, cudaStream_t s)
 {
-    k_dot<<<kReduceCtas, kReduceThreads, 0, s>>>(n, a, b, partials);
+    pdl_launch(k_dot, kReduceCtas, kReduceThreads, 0, s, n, a, b, partials);
     g_kernel_launches++;
 }
 
@@ -985,7 +1055,7 @@ template <class T>
 void launch_dots3(long long n, int nq, const T* a0, const T* b0, const T* a1, const T* b1, const T* a2, const T* b2,
                   double* partials, cudaStream_t s)
 {
-    k_dots3<T><<<kReduceCtas, kReduceThreads, 0, s>>>(n, nq, a0, b0, a1 ? a1 : a0, b1 ? b1 : b0, a2 ? a2 : a0,
+    pdl_launch(k_dots3<T>, kReduceCtas, kReduceThreads, 0, s, n, nq, a0, b0, a1 ? a1 : a0, b1 ? b1 : b0, a2 ? a2 : a0,
                                                       b2 ? b2 : b0, partials);
     g_kernel_launches++;
 }
@@ -994,7 +1064,7 @@ template <class T>
 void launch_axpy(long long n, double alpha, const T* x, T* y, cudaStream_t s)
 {
     const long long blocks = std::min<long long>((n + 255) / 256, 4 * 152);
-    k_axpy<T><<<(unsigned)std::max<long long>(blocks, 1), 256, 0, s>>>(n, alpha, x, y);
+    pdl_launch(k_axpy<T>, (unsigned)std::max<long long>(blocks, 1), 256, 0, s, n, alpha, x, y);
     g_kernel_launches++;
 }
 
@@ -1002,7 +1072,7 @@ template <class T>
 void launch_lincomb(long long n, double a, const T* c, double b, const T* d, T* out, cudaStream_t s)
 {
     const long long blocks = std::min<long long>((n + 255) / 256, 4 * 152);
-    k_lincomb<T><<<(unsigned)std::max<long long>(blocks, 1), 256, 0, s>>>(n, a, c, b, d, out);
+    pdl_launch(k_lincomb<T>, (unsigned)std::max<long long>(blocks, 1), 256, 0, s, n, a, c, b, d, out);
     g_kernel_launches++;
 }
 
@@ -1018,7 +1088,7 @@ template void launch_lincomb<float>(long long, double, const float*, double, con
 void launch_fcg_direction(long long n, const double* z, const double* dp, const double* partials_zadp,
                           const double* dadp, double* d, cudaStream_t s)
 {
-    k_fcg_direction<<<kReduceCtas, kReduceThreads, 0, s>>>(n, z, dp, partials_zadp, dadp, d);
+    pdl_launch(k_fcg_direction, kReduceCtas, kReduceThreads, 0, s, n, z, dp, partials_zadp, dadp, d);
     g_kernel_launches++;
 }
 
@@ -1026,21 +1096,21 @@ void launch_krylov_step(long long n, double* x, double* r, const double* d, cons
                         const double* partials_num, const double* partials_den, double* den_out,
                         double* partials_rr, cudaStream_t s, float* r32)
 {
-    k_krylov_step<<<kReduceCtas, kReduceThreads, 0, s>>>(n, x, r, d, Ad, partials_num, partials_den, den_out,
+    pdl_launch(k_krylov_step, kReduceCtas, kReduceThreads, 0, s, n, x, r, d, Ad, partials_num, partials_den, den_out,
                                                          partials_rr, r32);
     g_kernel_launches++;
 }
 
 void launch_dot_mixed(long long n, const float* a, const double* b, double* partials, cudaStream_t s)
 {
-    k_dot_mixed<<<kReduceCtas, kReduceThreads, 0, s>>>(n, a, b, partials);
+    pdl_launch(k_dot_mixed, kReduceCtas, kReduceThreads, 0, s, n, a, b, partials);
     g_kernel_launches++;
 }
 
 void launch_fcg_direction_mixed(long long n, const float* z, const double* dp, const double* partials_zadp,
                                 const double* dadp, double* d, cudaStream_t s, float* dhi, float* dlo)
 {
-    k_fcg_direction_mixed<<<kReduceCtas, kReduceThreads, 0, s>>>(n, z, dp, partials_zadp, dadp, d, dhi, dlo);
+    pdl_launch(k_fcg_direction_mixed, kReduceCtas, kReduceThreads, 0, s, n, z, dp, partials_zadp, dadp, d, dhi, dlo);
     g_kernel_launches++;
 }
 
@@ -1051,7 +1121,7 @@ void launch_spmv_dots_df(const BsrView<float>& Ahi, const float* vlo, const floa
     // lane r writes output r: needs G >= bs (always true for G >= 4 and bs <= 4; bs = 6 uses 8)
     const int lanes = Ahi.lanes < Ahi.bs ? 8 : Ahi.lanes;
     FHG_DISPATCH_BS_G(Ahi.bs, lanes, {
-        k_bsr_spmv_dots_df<BS, G><<<kReduceCtas, kReduceThreads, 0, s>>>(Ahi.nbr, Ahi.rowptr, Ahi.colidx, Ahi.vals, vlo,
+        pdl_launch(k_bsr_spmv_dots_df<BS, G>, kReduceCtas, kReduceThreads, 0, s, Ahi.nbr, Ahi.rowptr, Ahi.colidx, Ahi.vals, vlo,
                                                                          Ahi.ld, dhi, dlo, rhi, rlo, Adhi, Adlo,
                                                                          partials);
     });
@@ -1060,14 +1130,14 @@ void launch_spmv_dots_df(const BsrView<float>& Ahi, const float* vlo, const floa
 
 void launch_dot_df(long long n, const float* z, const float* ah, const float* al, double* partials, cudaStream_t s)
 {
-    k_dot_df<<<kReduceCtas, kReduceThreads, 0, s>>>(n, z, ah, al, partials);
+    pdl_launch(k_dot_df, kReduceCtas, kReduceThreads, 0, s, n, z, ah, al, partials);
     g_kernel_launches++;
 }
 
 void launch_fcg_direction_df(long long n, const float* z, const float* dph, const float* dpl,
                              const double* partials_zadp, const double* dadp, float* dh, float* dl, cudaStream_t s)
 {
-    k_fcg_direction_df<<<kReduceCtas, kReduceThreads, 0, s>>>(n, z, dph, dpl, partials_zadp, dadp, dh, dl);
+    pdl_launch(k_fcg_direction_df, kReduceCtas, kReduceThreads, 0, s, n, z, dph, dpl, partials_zadp, dadp, dh, dl);
     g_kernel_launches++;
 }
 
@@ -1075,14 +1145,14 @@ void launch_krylov_step_df(long long n, double* x, float* rh, float* rl, const f
                            const float* Adh, const float* Adl, const double* partials_num,
                            const double* partials_den, double* den_out, double* partials_rr, cudaStream_t s)
 {
-    k_krylov_step_df<<<kReduceCtas, kReduceThreads, 0, s>>>(n, x, rh, rl, dh, dl, Adh, Adl, partials_num,
+    pdl_launch(k_krylov_step_df, kReduceCtas, kReduceThreads, 0, s, n, x, rh, rl, dh, dl, Adh, Adl, partials_num,
                                                             partials_den, den_out, partials_rr);
     g_kernel_launches++;
 }
 
 void launch_split_df(long long n, const double* v, float* h, float* l, cudaStream_t s)
 {
-    k_split_df<<<grid_for(n, kThreads), kThreads, 0, s>>>(n, v, h, l);
+    pdl_launch(k_split_df, grid_for(n, kThreads), kThreads, 0, s, n, v, h, l);
     g_kernel_launches++;
 }
 
@@ -1090,38 +1160,38 @@ void launch_split_df(long long n, const double* v, float* h, float* l, cudaStrea
 void launch_cg_step(long long n, double* x, double* r, const double* d, const double* Ad, const double* num,
                     const double* partials_den, double* partials_rr, cudaStream_t s)
 {
-    k_cg_step<<<kReduceCtas, kReduceThreads, 0, s>>>(n, x, r, d, Ad, num, partials_den, partials_rr);
+    pdl_launch(k_cg_step, kReduceCtas, kReduceThreads, 0, s, n, x, r, d, Ad, num, partials_den, partials_rr);
     g_kernel_launches++;
 }
 
 void launch_cg_direction(long long n, const double* z, const double* beta, double* d, cudaStream_t s)
 {
-    k_cg_direction<<<kReduceCtas, kReduceThreads, 0, s>>>(n, z, beta, d);
+    pdl_launch(k_cg_direction, kReduceCtas, kReduceThreads, 0, s, n, z, beta, d);
     g_kernel_launches++;
 }
 
 void launch_cg_beta(const double* partials, double* rz, double* beta, cudaStream_t s)
 {
-    k_cg_beta<<<1, kReduceThreads, 0, s>>>(partials, rz, beta);
+    pdl_launch(k_cg_beta, 1, kReduceThreads, 0, s, partials, rz, beta);
     g_kernel_launches++;
 }
 
 void launch_finalize_norm(const double* partials_rr, const double* bnorm, double* nr_out, double* hist, int* counter,
                           int hist_len, cudaStream_t s)
 {
-    k_finalize_norm<<<1, kReduceThreads, 0, s>>>(partials_rr, bnorm, nr_out, hist, counter, hist_len);
+    pdl_launch(k_finalize_norm, 1, kReduceThreads, 0, s, partials_rr, bnorm, nr_out, hist, counter, hist_len);
     g_kernel_launches++;
 }
 
 void launch_sqrt_sum(const double* partials, double* out, cudaStream_t s)
 {
-    k_sqrt_sum<<<1, kReduceThreads, 0, s>>>(partials, out);
+    pdl_launch(k_sqrt_sum, 1, kReduceThreads, 0, s, partials, out);
     g_kernel_launches++;
 }
 
 void launch_sum(const double* partials, double* out, cudaStream_t s)
 {
-    k_sum<<<1, kReduceThreads, 0, s>>>(partials, out);
+    pdl_launch(k_sum, 1, kReduceThreads, 0, s, partials, out);
     g_kernel_launches++;
 }
 
@@ -1129,7 +1199,7 @@ template <class Tin, class Tout>
 void launch_convert(long long n, const Tin* in, Tout* out, cudaStream_t s)
 {
     if (n == 0) return;
-    k_convert<Tin, Tout><<<grid_for(n, kThreads), kThreads, 0, s>>>(n, in, out);
+    pdl_launch(k_convert<Tin, Tout>, grid_for(n, kThreads), kThreads, 0, s, n, in, out);
     g_kernel_launches++;
 }
 
@@ -1137,7 +1207,7 @@ template <class T>
 void launch_permute(int nb, int bs, const int* perm, const T* in, T* out, bool gather, cudaStream_t s)
 {
     if (nb == 0) return;
-    k_permute<T><<<grid_for((long long)nb * bs, kThreads), kThreads, 0, s>>>(nb, bs, perm, in, out, gather ? 1 : 0);
+    pdl_launch(k_permute<T>, grid_for((long long)nb * bs, kThreads), kThreads, 0, s, nb, bs, perm, in, out, gather ? 1 : 0);
     g_kernel_launches++;
 }
 
@@ -1168,6 +1238,7 @@ namespace {
 __global__ void k_copy2(long long n, const double* __restrict__ a0, double* __restrict__ b0,
                         const double* __restrict__ a1, double* __restrict__ b1)
 {
+    pdl_wait();
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         b0[i] = a0[i];
         b1[i] = a1[i];
@@ -1176,6 +1247,7 @@ __global__ void k_copy2(long long n, const double* __restrict__ a0, double* __re
 
 __global__ void k_init_solve(double* scal, int* counter)
 {
+    pdl_wait();
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         scal[1] = 1.0;  // d.Ad of the (absent) previous direction
         scal[2] = 1.0;  // ||r|| / ||b||
@@ -1190,6 +1262,7 @@ __global__ void k_init_solve(double* scal, int* counter)
 __global__ void k_loop_control(const double* nr, const int* counter, double tol, int maxit,
                                cudaGraphConditionalHandle handle)
 {
+    pdl_wait();
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         const double v = *nr;
         const int it = *counter - 1;
@@ -1203,20 +1276,20 @@ __global__ void k_loop_control(const double* nr, const int* counter, double tol,
 void launch_copy2(long long n, const double* a0, double* b0, const double* a1, double* b1, cudaStream_t s)
 {
     const long long blocks = std::min<long long>((n + 255) / 256, 4 * 152);
-    k_copy2<<<(unsigned)std::max<long long>(blocks, 1), 256, 0, s>>>(n, a0, b0, a1, b1);
+    pdl_launch(k_copy2, (unsigned)std::max<long long>(blocks, 1), 256, 0, s, n, a0, b0, a1, b1);
     g_kernel_launches++;
 }
 
 void launch_init_solve(double* scal, int* counter, cudaStream_t s)
 {
-    k_init_solve<<<1, 32, 0, s>>>(scal, counter);
+    pdl_launch(k_init_solve, 1, 32, 0, s, scal, counter);
     g_kernel_launches++;
 }
 
 void launch_loop_control(const double* nr, const int* counter, double tol, int maxit, cudaGraphConditionalHandle h,
                          cudaStream_t s)
 {
-    k_loop_control<<<1, 32, 0, s>>>(nr, counter, tol, maxit, h);
+    pdl_launch(k_loop_control, 1, 32, 0, s, nr, counter, tol, maxit, h);
     g_kernel_launches++;
 }
 

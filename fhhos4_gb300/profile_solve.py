@@ -22,6 +22,7 @@ def main():
     ap.add_argument("--nu", default="2,2")
     ap.add_argument("--solves", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--autotune", type=int, default=1, help="0: default launch shapes (comparable across runs)")
     ap.add_argument("--step", choices=["", "learned_tcgen05", "learned_mma_sync", "gs_fp32", "outer_df"], default="")
     a = ap.parse_args()
 
@@ -43,7 +44,7 @@ def main():
     H.close()
     o = N.default_options()
     o.vcycle_precision = N.PRECISION["fp32"]
-    o.autotune = 1
+    o.autotune = a.autotune
     ctx.setup(len(As), o)
     npre, npost = (int(v) for v in a.nu.split(","))
     params = LN.load_params()[0]
