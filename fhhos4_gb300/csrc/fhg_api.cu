@@ -11,6 +11,7 @@
 #include "fhg_internal.h"
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -66,6 +67,7 @@ struct Level {
     DevBsr<double> A, Ahat, P, R;
     bool ahat_is_a = true;
     DevBsr<float> A32, P32, R32;
+    DevBsr<float> G32;          // FP32 GS operator: A's off-diagonal blocks in padded rows, when they fit
     DevBsr<float> Ahat_hi;      // level 0, FP32 V-cycle: outer operator as an FP32 pair (hi part)
     float* ahat_lo = nullptr;   // (lo part, same layout)
     double* dinv = nullptr;
@@ -622,6 +624,47 @@ int upload_bsr(fhg_ctx* ctx, const HostBsr& B, DevBsr<T>& D, const DevBsr<double
     return FHG_OK;
 }
 
+// The off-diagonal blocks of A in padded rows of W = max off-diagonal blocks per row slots (FP32,
+// entry-major, column -1 in empty slots, column order kept), for the GS sweeps: a row's blocks
+// start at row * W, so the sweep reads no row pointer before its blocks. Built when W <= 8 and the
+// padding adds at most half to the off-diagonal blocks (about 1% on a 64^3 tetrahedral mesh, more on
+// small meshes whose faces near the boundary have fewer neighbours); otherwise D stays empty and the
+// sweeps use A.
+int upload_offdiag_padded(fhg_ctx* ctx, const HostBsr& B, DevBsr<float>& D)
+{
+    D = DevBsr<float>();
+    int W = 0;
+    long long off = 0;
+    for (int i = 0; i < B.nbr; i++) {
+        int c = 0;
+        for (int p = B.rowptr[i]; p < B.rowptr[i + 1]; p++) c += B.colidx[p] != i;
+        W = std::max(W, c);
+        off += c;
+    }
+    const long long slots = (long long)B.nbr * W;
+    if (W == 0 || W > 8 || slots > off + off / 2 || slots > INT32_MAX) return FHG_OK;
+    const int bb = B.bs * B.bs;
+    const long long ld = round_up(slots, 32);
+    std::vector<int> col((size_t)slots, -1);
+    std::vector<float> soa((size_t)ld * bb, 0.f);
+    for (int i = 0; i < B.nbr; i++) {
+        long long q = (long long)i * W;
+        for (int p = B.rowptr[i]; p < B.rowptr[i + 1]; p++) {
+            if (B.colidx[p] == i) continue;
+            col[(size_t)q] = B.colidx[p];
+            for (int e = 0; e < bb; e++) soa[(size_t)e * ld + q] = (float)B.vals[(size_t)p * bb + e];
+            q++;
+        }
+    }
+    int rc;
+    if ((rc = upload(ctx, &D.colidx, col.data(), col.size()))) return rc;
+    if ((rc = upload(ctx, &D.vals, soa.data(), soa.size()))) return rc;
+    D.v.nbr = B.nbr; D.v.nbc = B.nbc; D.v.bs = B.bs; D.v.nnzb = slots; D.v.ld = ld; D.v.ell = W;
+    D.v.rowptr = nullptr; D.v.colidx = D.colidx; D.v.vals = D.vals;
+    D.v.lanes = W <= 4 ? 4 : 8;
+    return FHG_OK;
+}
+
 // Outer operator as an FP32 pair: hi = fl32(a), lo = fl32(a - hi), entry-major like upload_bsr.
 int upload_bsr_split(fhg_ctx* ctx, const HostBsr& B, DevBsr<float>& D, float** lo_out, const DevBsr<double>& share_index)
 {
@@ -726,6 +769,7 @@ template <> struct LevelVecs<double> {
     static const BsrView<double>& R(Level& L) { return L.R.v; }
     static const double* dinv(Level& L) { return L.dinv; }
     static double* k(Level& L, int i) { return L.kv64[i]; }
+    static const BsrView<double>& gs(Level& L) { return L.A.v; }
 };
 template <> struct LevelVecs<float> {
     static float* x(Level& L) { return L.x32; }
@@ -736,6 +780,8 @@ template <> struct LevelVecs<float> {
     static const BsrView<float>& R(Level& L) { return L.R32.v; }
     static const float* dinv(Level& L) { return L.dinv32; }
     static float* k(Level& L, int i) { return L.kv32[i]; }
+    // GS sweeps: the padded off-diagonal view when setup built one
+    static const BsrView<float>& gs(Level& L) { return L.G32.vals ? L.G32.v : L.A32.v; }
 };
 
 // `from_zero`: x holds zeros on entry (the pre-smoothing of a V-cycle), so the first GS sweep
@@ -746,16 +792,18 @@ void smooth(fhg_ctx* ctx, int l, int code, int iters, const T* b, T* x, bool fro
     Level& L = ctx->levels[l];
     using V = LevelVecs<T>;
     cudaStream_t s = ctx->stream;
-    BsrView<T> A = V::A(L);
-    if (L.gs_lanes) { A.lanes = L.gs_lanes; A.unroll = L.gs_unroll; }
+    BsrView<T> Ag = V::gs(L);   // GS sweeps (tuned shape)
+    if (L.gs_lanes) { Ag.lanes = L.gs_lanes; Ag.unroll = L.gs_unroll; }
+    BsrView<T> A = V::A(L);     // Jacobi (needs the diagonal blocks)
+    if (L.gs_lanes && Ag.ell == 0) { A.lanes = L.gs_lanes; A.unroll = L.gs_unroll; }
     auto forward = [&](bool zero) {
         for (int c = 0; c < L.ncolours; c++)
-            fhg::launch_gs<T>(A, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s, 0,
+            fhg::launch_gs<T>(Ag, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s, 0,
                               zero ? L.colour_start[c + 1] : 0x7fffffff);
     };
     auto backward = [&](bool zero) {
         for (int c = L.ncolours - 1; c >= 0; c--)
-            fhg::launch_gs<T>(A, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s,
+            fhg::launch_gs<T>(Ag, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s,
                               zero ? L.colour_start[c] : 0, 0x7fffffff);
     };
     for (int it = 0; it < iters; it++) {
@@ -1081,8 +1129,9 @@ int tune_level(fhg_ctx* ctx, int l)
     if (l < ctx->nlevels - 1) {
         Level& C = ctx->levels[l + 1];
         int g = A.lanes, gu = A.unroll;
+        if (V::gs(L).ell > 0) { g = V::gs(L).lanes; gu = 1; }
         rc = tune(ctx, bs, g, gu, [&](int G, int U) {
-            BsrView<T> v = A; v.lanes = G; v.unroll = U;
+            BsrView<T> v = V::gs(L); v.lanes = G; v.unroll = U;
             for (int c = 0; c < L.ncolours; c++)
                 fhg::launch_gs<T>(v, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, V::b(L), V::x(L), s);
         });
@@ -1116,9 +1165,37 @@ void free_graphs(fhg_ctx* ctx)
     ctx->graphs_l_built = 0;
 }
 
+// Device-side state of a level (the given host operators stay): cleared with the allocations so
+// that a later setup in another precision finds no pointer into freed memory.
+void reset_device_state(Level& L)
+{
+    L.A = DevBsr<double>();
+    L.Ahat = DevBsr<double>();
+    L.P = DevBsr<double>();
+    L.R = DevBsr<double>();
+    L.A32 = DevBsr<float>();
+    L.P32 = DevBsr<float>();
+    L.R32 = DevBsr<float>();
+    L.G32 = DevBsr<float>();
+    L.Ahat_hi = DevBsr<float>();
+    L.ahat_is_a = true;
+    L.ahat_lo = nullptr;
+    L.dinv = nullptr;
+    L.dinv32 = nullptr;
+    L.perm_d = nullptr;
+    L.x = L.b = L.r = nullptr;
+    L.x32 = L.b32 = L.r32 = nullptr;
+    for (int i = 0; i < 4; i++) { L.kv64[i] = nullptr; L.kv32[i] = nullptr; }
+    L.cinv = nullptr;
+    L.gs_lanes = 0;
+    L.gs_unroll = 1;
+    L.outer_lanes = 0;
+}
+
 void free_all(fhg_ctx* ctx)
 {
     free_graphs(ctx);
+    for (Level& L : ctx->levels) reset_device_state(L);
     ctx->nbr_d = nullptr; ctx->tfeat_d = nullptr; ctx->lw = nullptr; ctx->lstatus = nullptr;
     ctx->rlo = nullptr;
     ctx->lparams = nullptr; ctx->lwts = nullptr; ctx->lbias = nullptr;
@@ -1511,6 +1588,7 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         Ab[l] = HostBsr();
         if ((rc = upload_bsr<double>(ctx, Ap, L.A, nullptr))) return rc;
         if (fp32 && (rc = upload_bsr<float>(ctx, Ap, L.A32, &L.A))) return rc;
+        if (fp32 && l < nlevels - 1 && o.colouring && (rc = upload_offdiag_padded(ctx, Ap, L.G32))) return rc;
         if ((rc = upload(ctx, &L.perm_d, L.perm.data(), L.perm.size()))) return rc;
         if (l < nlevels - 1) {
             // Pre-inverted diagonal blocks (FP64, rounded for the FP32 copy).

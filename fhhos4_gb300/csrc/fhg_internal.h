@@ -22,6 +22,8 @@ struct BsrView {
     int unroll = 1;       // blocks per lane step in the row walk (1 or 2; 2 only for bs <= 3)
     long long nnzb = 0;   // stored blocks
     long long ld = 0;     // leading dimension of vals
+    int ell = 0;          // > 0: padded rows of `ell` slots, slot s of row i at i * ell + s, column -1
+                          // where empty, rowptr unused (the off-diagonal GS operator)
     const int* rowptr = nullptr;
     const int* colidx = nullptr;
     const T* vals = nullptr;
@@ -41,6 +43,7 @@ enum SpmvMode { kSpmvAssign = 0, kSpmvResidual = 1, kSpmvAddTo = 2 };
 template <class T>
 void launch_spmv(const BsrView<T>& A, int mode, const T* x, const T* aux, T* y, cudaStream_t s);
 // col_lo/col_hi: block columns outside [col_lo, col_hi) are skipped (zero-start sweeps).
+// A may be a padded (ell > 0) view of the off-diagonal blocks.
 template <class T>
 void launch_gs(const BsrView<T>& A, int row0, int row1, const T* dinv, long long dld,
                const T* b, T* x, cudaStream_t s, int col_lo = 0, int col_hi = 0x7fffffff);

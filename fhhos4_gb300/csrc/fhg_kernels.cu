@@ -278,13 +278,15 @@ __global__ void __launch_bounds__(kThreads) k_bsr_residual_dinv(int nbr, const i
 // Columns outside [col_lo, col_hi) are skipped: in a sweep that starts from x = 0 they hold
 // zeros not yet overwritten (later colours of a forward sweep, earlier ones of a backward
 // sweep), so skipping them changes no bit of the result and saves their loads. Block columns
-// are sorted, so the skipped ones form a head and a tail of each row.
+// are sorted, so the skipped ones form a head and a tail of each row. Padded slots (column -1 of
+// an ell view) are skipped the same way.
 template <class T, int BS, int G, int U>
 __global__ void __launch_bounds__(kThreads) k_bsr_gs(int row0, int row1, const int* __restrict__ rowptr,
                                                      const int* __restrict__ colidx,
                                                      const T* __restrict__ vals, long long ld,
                                                      const T* __restrict__ dinv, long long dld,
-                                                     const T* __restrict__ b, T* x, int col_lo, int col_hi)
+                                                     const T* __restrict__ b, T* x, int col_lo, int col_hi,
+                                                     int ell)
 {
     pdl_wait();
     const int lane = threadIdx.x & (G - 1);
@@ -307,7 +309,10 @@ __global__ void __launch_bounds__(kThreads) k_bsr_gs(int row0, int row1, const i
             if (col >= col_hi) return 2;
             return (col == row || col < col_lo) ? 0 : 1;
         };
-        accumulate_row<T, BS, G, U>(rowptr[row], rowptr[row + 1], lane, colidx, vals, ld, x, acc, sel);
+        // Padded rows (ell > 0) start at row * ell: no row-pointer load ahead of the walk.
+        const int p0 = ell > 0 ? row * ell : rowptr[row];
+        const int p1 = ell > 0 ? p0 + ell : rowptr[row + 1];
+        accumulate_row<T, BS, G, U>(p0, p1, lane, colidx, vals, ld, x, acc, sel);
     }
 #pragma unroll
     for (int r = 0; r < BS; r++) acc[r] = group_sum<G>(acc[r]);
@@ -1006,11 +1011,11 @@ void launch_gs(const BsrView<T>& A, int row0, int row1, const T* dinv, long long
     const unsigned grid = grid_for((long long)(row1 - row0) * A.lanes, kThreads);
     FHG_DISPATCH_BS_G(A.bs, A.lanes, {
         if (A.unroll == 2)
-            pdl_launch(k_bsr_gs<T, BS, G, 2>, grid, kThreads, 0, s, row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, b,
-                                                            x, col_lo, col_hi);
+            pdl_launch(k_bsr_gs<T, BS, G, 2>, grid, kThreads, 0, s, row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv,
+                       dld, b, x, col_lo, col_hi, A.ell);
         else
-            pdl_launch(k_bsr_gs<T, BS, G, 1>, grid, kThreads, 0, s, row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, b,
-                                                            x, col_lo, col_hi);
+            pdl_launch(k_bsr_gs<T, BS, G, 1>, grid, kThreads, 0, s, row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv,
+                       dld, b, x, col_lo, col_hi, A.ell);
     });
     g_kernel_launches++;
 }

@@ -219,6 +219,35 @@ def test_operators_of_every_level(case):
     assert np.linalg.norm(ys - O.spmv_sym_lower(A0, x)) <= 1e-13 * np.abs(A0).max() * np.linalg.norm(x) * 10
 
 
+def test_fp32_smoothers_of_every_level(case):
+    """FP32 GS sweeps (on the padded off-diagonal view where setup built one) and block Jacobi on
+    every smoothed level against the FP64 oracle in colour order, to FP32 accuracy."""
+    torch = pytest.importorskip("torch")
+    from fhhos4_gb300 import _native as N
+    solver = S().fcg_mg(case.As, case.Ps, case.bs, precision="fp32")
+    ctx = solver.Context()
+    rng = np.random.default_rng(11)
+    for l in range(case.levels - 1):
+        A = case.As[l]
+        n = A.shape[0]
+        s = scalar_perm(ctx.permutation(l, n // case.bs), case.bs)
+        Ap = O.as_csr(A[s][:, s])
+        x = rng.standard_normal(n).astype(np.float32).astype(np.float64)
+        b = rng.standard_normal(n).astype(np.float32).astype(np.float64)
+        xd = torch.tensor(x, dtype=torch.float32, device="cuda")
+        bd = torch.tensor(b, dtype=torch.float32, device="cuda")
+        out = torch.empty_like(xd)
+        for op, backward in ((N.OP_GS_FORWARD, False), (N.OP_GS_BACKWARD, True)):
+            ctx.apply_internal(l, op, "fp32", xd.data_ptr(), bd.data_ptr(), out.data_ptr())
+            ref = O.block_gs(Ap, case.bs, b, x, backward=backward)
+            g = out.cpu().numpy().astype(np.float64)
+            assert np.linalg.norm(g - ref) <= 2e-4 * np.linalg.norm(ref), (l, op)
+        ctx.apply_internal(l, N.OP_JACOBI, "fp32", xd.data_ptr(), bd.data_ptr(), out.data_ptr())
+        ref = O.block_jacobi(Ap, case.bs, 1.0, b, x)
+        g = out.cpu().numpy().astype(np.float64)
+        assert np.linalg.norm(g - ref) <= 2e-4 * np.linalg.norm(ref), l
+
+
 def test_kernel_launches_are_counted(case):
     solver, ctx = _ctx(case)
     before = ctx.kernel_launches()
@@ -254,6 +283,30 @@ def test_singular_diagonal_block_is_rejected():
     with pytest.raises(N.FhgError) as ei:
         S().fcg_mg([A] + c.As[1:], c.Ps, c.bs)
     assert ei.value.code == N.FHG_ERR_SINGULAR_BLOCK
+
+
+def test_fp64_setup_after_fp32_drops_the_fp32_operators():
+    """A context set up again in FP64 keeps no FP32 operator of its earlier FP32 setup: switching
+    its V-cycle to FP32 is refused (the FP32 data were freed with the first setup)."""
+    from fhhos4_gb300 import _native as N
+    c = _tiny()
+    ctx = N.Context(0)
+    for l, A in enumerate(c.As):
+        ctx.set_level(l, c.bs, A)
+    for l, P in enumerate(c.Ps):
+        ctx.set_prolongation(l, P)
+    o = N.default_options()
+    o.vcycle_precision = N.PRECISION["fp32"]
+    ctx.setup(len(c.As), o)
+    ctx.set_vcycle_precision("fp32")
+    o.vcycle_precision = N.PRECISION["fp64"]
+    ctx.setup(len(c.As), o)
+    with pytest.raises(N.FhgError) as ei:
+        ctx.set_vcycle_precision("fp32")
+    assert ei.value.code == N.FHG_ERR_NOT_READY
+    rc, x, hist, info = ctx.solve(c.b, 200)
+    assert rc == N.FHG_OK and info.normalized_residual < 1e-8
+    ctx.close()
 
 
 def test_invalid_inputs_are_rejected():
