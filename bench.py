@@ -407,6 +407,7 @@ def run_ours(args, dist: Dist):
         ctx.set_learned(params, "fallback")
     # Dominant kernel of the headline (FP32 V-cycle) solve: GS sweeps on level 0.
     ncol = info0["colours"]
+    gs_min_bytes = (nnzb0 - nb0) * (bs * bs * p32 + 4) + nb0 * bs * bs * p32 + 3 * n0 * p32
     dom = "bsr_gs_sweep_fp32"
     hbm, hbm_kind = measured_hbm_peak()
     traffic = committed_traffic().get(dom)
@@ -416,6 +417,11 @@ def run_ours(args, dist: Dist):
                 "traffic": traffic,
                 "algorithmic_bytes_per_launch": kernels[dom]["bytes"] / max(ncol, 1),
                 "launches_per_sweep": ncol,
+                # The sweep's own minimum: off-diagonal blocks with their column indices, D^-1, b,
+                # x read once and written once (the formula above also counts the diagonal blocks
+                # and row pointers, which the sweep does not read).
+                "min_bytes_per_launch": gs_min_bytes / max(ncol, 1),
+                "frac_min_bytes": round(gs_min_bytes / (kernels[dom]["ms"] * 1e-3) / 1e9 / hbm, 4),
                 "spmv_fp64_frac": round(kernels["bsr_spmv_fp64"]["gbs"] / hbm, 4),
                 "spmv_fp32_frac": round(kernels["bsr_spmv_fp32"]["gbs"] / hbm, 4)}
 

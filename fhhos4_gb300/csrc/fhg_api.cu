@@ -68,6 +68,7 @@ struct Level {
     bool ahat_is_a = true;
     DevBsr<float> A32, P32, R32;
     DevBsr<float> G32;          // FP32 GS operator: A's off-diagonal blocks in padded rows, when they fit
+    DevBsr<float> A32p, P32p;   // FP32 A and P in padded rows (all blocks), when they fit
     DevBsr<float> Ahat_hi;      // level 0, FP32 V-cycle: outer operator as an FP32 pair (hi part)
     float* ahat_lo = nullptr;   // (lo part, same layout)
     double* dinv = nullptr;
@@ -624,44 +625,49 @@ int upload_bsr(fhg_ctx* ctx, const HostBsr& B, DevBsr<T>& D, const DevBsr<double
     return FHG_OK;
 }
 
-// The off-diagonal blocks of A in padded rows of W = max off-diagonal blocks per row slots (FP32,
-// entry-major, column -1 in empty slots, column order kept), for the GS sweeps: a row's blocks
-// start at row * W, so the sweep reads no row pointer before its blocks. Built when W <= 8 and the
-// padding adds at most half to the off-diagonal blocks (about 1% on a 64^3 tetrahedral mesh, more on
-// small meshes whose faces near the boundary have fewer neighbours); otherwise D stays empty and the
-// sweeps use A.
-int upload_offdiag_padded(fhg_ctx* ctx, const HostBsr& B, DevBsr<float>& D)
+// A block operator in padded rows (FP32, entry-major, column order kept; empty slots hold zero
+// values and a column inside the operator: the row's own, skipped by a GS sweep as the diagonal,
+// for the off-diagonal view; the row's last stored column (0 for an empty row) otherwise, which a
+// product adds as an exact zero):
+// W = the most blocks of a row, row i's blocks at i * W, so a kernel reads no row pointer before
+// them. `offdiag`: only the off-diagonal blocks (the GS sweeps, which apply D^-1 instead). Built
+// when W <= max_w and the padding adds at most half to the stored blocks (about 1% for the
+// operators of a 64^3 tetrahedral mesh, more on small meshes whose faces near the boundary have
+// fewer neighbours); otherwise D stays empty and the kernels use the CSR form.
+int upload_padded(fhg_ctx* ctx, const HostBsr& B, DevBsr<float>& D, bool offdiag, int max_w)
 {
     D = DevBsr<float>();
     int W = 0;
-    long long off = 0;
+    long long kept = 0;
     for (int i = 0; i < B.nbr; i++) {
         int c = 0;
-        for (int p = B.rowptr[i]; p < B.rowptr[i + 1]; p++) c += B.colidx[p] != i;
+        for (int p = B.rowptr[i]; p < B.rowptr[i + 1]; p++) c += !(offdiag && B.colidx[p] == i);
         W = std::max(W, c);
-        off += c;
+        kept += c;
     }
     const long long slots = (long long)B.nbr * W;
-    if (W == 0 || W > 8 || slots > off + off / 2 || slots > INT32_MAX) return FHG_OK;
+    if (W == 0 || W > max_w || slots > kept + kept / 2 || slots > INT32_MAX) return FHG_OK;
     const int bb = B.bs * B.bs;
     const long long ld = round_up(slots, 32);
-    std::vector<int> col((size_t)slots, -1);
+    std::vector<int> col((size_t)slots);
     std::vector<float> soa((size_t)ld * bb, 0.f);
     for (int i = 0; i < B.nbr; i++) {
         long long q = (long long)i * W;
+        int last = 0;
         for (int p = B.rowptr[i]; p < B.rowptr[i + 1]; p++) {
-            if (B.colidx[p] == i) continue;
-            col[(size_t)q] = B.colidx[p];
+            if (offdiag && B.colidx[p] == i) continue;
+            col[(size_t)q] = last = B.colidx[p];
             for (int e = 0; e < bb; e++) soa[(size_t)e * ld + q] = (float)B.vals[(size_t)p * bb + e];
             q++;
         }
+        for (; q < (long long)(i + 1) * W; q++) col[(size_t)q] = offdiag ? i : last;
     }
     int rc;
     if ((rc = upload(ctx, &D.colidx, col.data(), col.size()))) return rc;
     if ((rc = upload(ctx, &D.vals, soa.data(), soa.size()))) return rc;
     D.v.nbr = B.nbr; D.v.nbc = B.nbc; D.v.bs = B.bs; D.v.nnzb = slots; D.v.ld = ld; D.v.ell = W;
     D.v.rowptr = nullptr; D.v.colidx = D.colidx; D.v.vals = D.vals;
-    D.v.lanes = W <= 4 ? 4 : 8;
+    D.v.lanes = W <= 4 ? 4 : (W <= 8 ? 8 : 16);
     return FHG_OK;
 }
 
@@ -770,18 +776,21 @@ template <> struct LevelVecs<double> {
     static const double* dinv(Level& L) { return L.dinv; }
     static double* k(Level& L, int i) { return L.kv64[i]; }
     static const BsrView<double>& gs(Level& L) { return L.A.v; }
+    static const BsrView<double>& Acsr(Level& L) { return L.A.v; }
 };
 template <> struct LevelVecs<float> {
     static float* x(Level& L) { return L.x32; }
     static float* b(Level& L) { return L.b32; }
     static float* r(Level& L) { return L.r32; }
-    static const BsrView<float>& A(Level& L) { return L.A32.v; }
-    static const BsrView<float>& P(Level& L) { return L.P32.v; }
+    // products with A and P: the padded views when setup built them
+    static const BsrView<float>& A(Level& L) { return L.A32p.vals ? L.A32p.v : L.A32.v; }
+    static const BsrView<float>& P(Level& L) { return L.P32p.vals ? L.P32p.v : L.P32.v; }
     static const BsrView<float>& R(Level& L) { return L.R32.v; }
     static const float* dinv(Level& L) { return L.dinv32; }
     static float* k(Level& L, int i) { return L.kv32[i]; }
     // GS sweeps: the padded off-diagonal view when setup built one
     static const BsrView<float>& gs(Level& L) { return L.G32.vals ? L.G32.v : L.A32.v; }
+    static const BsrView<float>& Acsr(Level& L) { return L.A32.v; }   // Jacobi: row pointers
 };
 
 // `from_zero`: x holds zeros on entry (the pre-smoothing of a V-cycle), so the first GS sweep
@@ -794,7 +803,7 @@ void smooth(fhg_ctx* ctx, int l, int code, int iters, const T* b, T* x, bool fro
     cudaStream_t s = ctx->stream;
     BsrView<T> Ag = V::gs(L);   // GS sweeps (tuned shape)
     if (L.gs_lanes) { Ag.lanes = L.gs_lanes; Ag.unroll = L.gs_unroll; }
-    BsrView<T> A = V::A(L);     // Jacobi (needs the diagonal blocks)
+    BsrView<T> A = V::Acsr(L);  // Jacobi (row pointers and the diagonal blocks)
     if (L.gs_lanes && Ag.ell == 0) { A.lanes = L.gs_lanes; A.unroll = L.gs_unroll; }
     auto forward = [&](bool zero) {
         for (int c = 0; c < L.ncolours; c++)
@@ -838,7 +847,7 @@ void learned_step(fhg_ctx* ctx, const float* b, float* x)
 {
     Level& L = ctx->levels[0];
     cudaStream_t s = ctx->stream;
-    fhg::launch_residual_dinv(L.A32.v, L.dinv32, L.nb, x, b, ctx->lw, s);
+    fhg::launch_residual_dinv(LevelVecs<float>::A(L), L.dinv32, L.nb, x, b, ctx->lw, s);
     fhg::launch_learned_apply(L.nb, L.bs, ctx->nbr_d, ctx->lw, ctx->tfeat_d, ctx->lwts, ctx->lbias, x, ctx->lstatus,
                               ctx->learned_kernel, s);
 }
@@ -1177,6 +1186,8 @@ void reset_device_state(Level& L)
     L.P32 = DevBsr<float>();
     L.R32 = DevBsr<float>();
     L.G32 = DevBsr<float>();
+    L.A32p = DevBsr<float>();
+    L.P32p = DevBsr<float>();
     L.Ahat_hi = DevBsr<float>();
     L.ahat_is_a = true;
     L.ahat_lo = nullptr;
@@ -1588,7 +1599,10 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         Ab[l] = HostBsr();
         if ((rc = upload_bsr<double>(ctx, Ap, L.A, nullptr))) return rc;
         if (fp32 && (rc = upload_bsr<float>(ctx, Ap, L.A32, &L.A))) return rc;
-        if (fp32 && l < nlevels - 1 && o.colouring && (rc = upload_offdiag_padded(ctx, Ap, L.G32))) return rc;
+        if (fp32 && l < nlevels - 1) {
+            if (o.colouring && (rc = upload_padded(ctx, Ap, L.G32, true, 8))) return rc;
+            if ((rc = upload_padded(ctx, Ap, L.A32p, false, 8))) return rc;
+        }
         if ((rc = upload(ctx, &L.perm_d, L.perm.data(), L.perm.size()))) return rc;
         if (l < nlevels - 1) {
             // Pre-inverted diagonal blocks (FP64, rounded for the FP32 copy).
@@ -1620,6 +1634,7 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
             if ((rc = upload_bsr<double>(ctx, Rp, L.R, nullptr))) return rc;
             if (fp32) {
                 if ((rc = upload_bsr<float>(ctx, Pp, L.P32, &L.P))) return rc;
+                if ((rc = upload_padded(ctx, Pp, L.P32p, false, 16))) return rc;
                 if ((rc = upload_bsr<float>(ctx, Rp, L.R32, &L.R))) return rc;
             }
         }
@@ -1687,10 +1702,10 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
             Level& L = ctx->levels[l];
             if (fp32) {
                 if ((rc = tune_level<float>(ctx, l))) return rc;
-                L.A.v.lanes = L.A32.v.lanes;
-                L.A.v.unroll = L.A32.v.unroll;
+                L.A.v.lanes = LevelVecs<float>::A(L).lanes;
+                L.A.v.unroll = LevelVecs<float>::A(L).unroll;
                 if (l < nlevels - 1) {
-                    L.P.v.lanes = L.P32.v.lanes; L.P.v.unroll = L.P32.v.unroll;
+                    L.P.v.lanes = LevelVecs<float>::P(L).lanes; L.P.v.unroll = LevelVecs<float>::P(L).unroll;
                     L.R.v.lanes = L.R32.v.lanes; L.R.v.unroll = L.R32.v.unroll;
                 }
             } else {

@@ -22,8 +22,9 @@ struct BsrView {
     int unroll = 1;       // blocks per lane step in the row walk (1 or 2; 2 only for bs <= 3)
     long long nnzb = 0;   // stored blocks
     long long ld = 0;     // leading dimension of vals
-    int ell = 0;          // > 0: padded rows of `ell` slots, slot s of row i at i * ell + s, column -1
-                          // where empty, rowptr unused (the off-diagonal GS operator)
+    int ell = 0;          // > 0: padded rows of `ell` slots, slot s of row i at i * ell + s, empty
+                          // slots with zero values and an in-range column, rowptr unused (accepted
+                          // by launch_spmv, launch_gs and launch_residual_dinv; Jacobi needs rowptr)
     const int* rowptr = nullptr;
     const int* colidx = nullptr;
     const T* vals = nullptr;

@@ -202,13 +202,28 @@ struct UseAll {
     __device__ __forceinline__ int operator()(int) const { return 1; }
 };
 
+// First and one-past-last stored position of a block row: padded views (ell > 0) put row i at
+// i * ell, with no row-pointer load ahead of the row walk. Their empty slots hold zero values and
+// a column inside the operator (the row's own in the off-diagonal GS view, where the sweep skips
+// it as the diagonal; a stored column of the row otherwise, where a product adds an exact zero).
+__device__ __forceinline__ void row_range(int row, int ell, const int* __restrict__ rowptr, int& p0, int& p1)
+{
+    if (ell > 0) {
+        p0 = row * ell;
+        p1 = p0 + ell;
+    } else {
+        p0 = rowptr[row];
+        p1 = rowptr[row + 1];
+    }
+}
+
 // ---------------------------------------------------------------------------
 // y = A x  |  y = aux - A x  |  y = aux + A x      (aux may alias y)
 template <class T, int BS, int G, int U, int MODE>
 __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int nbr, const int* __restrict__ rowptr,
                                                        const int* __restrict__ colidx,
                                                        const T* __restrict__ vals, long long ld,
-                                                       const T* __restrict__ x, const T* aux, T* y)
+                                                       const T* __restrict__ x, const T* aux, T* y, int ell)
 {
     pdl_wait();
     const int lane = threadIdx.x & (G - 1);
@@ -221,7 +236,11 @@ __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int nbr, const int* __res
     // before the row walk so that its latency overlaps it.
     T av = T(0);
     if (MODE != kSpmvAssign && G >= BS && row < nbr && lane < BS) av = aux[(long long)row * BS + lane];
-    if (row < nbr) accumulate_row<T, BS, G, U>(rowptr[row], rowptr[row + 1], lane, colidx, vals, ld, x, acc, UseAll());
+    if (row < nbr) {
+        int p0, p1;
+        row_range(row, ell, rowptr, p0, p1);
+        accumulate_row<T, BS, G, U>(p0, p1, lane, colidx, vals, ld, x, acc, UseAll());
+    }
 #pragma unroll
     for (int r = 0; r < BS; r++) acc[r] = group_sum<G>(acc[r]);
     if (row < nbr) {
@@ -246,7 +265,7 @@ __global__ void __launch_bounds__(kThreads) k_bsr_residual_dinv(int nbr, const i
                                                                 const T* __restrict__ vals, long long ld,
                                                                 const T* __restrict__ dinv, long long dld,
                                                                 const T* __restrict__ x, const T* __restrict__ b,
-                                                                T* __restrict__ w)
+                                                                T* __restrict__ w, int ell)
 {
     pdl_wait();
     const int lane = threadIdx.x & (G - 1);
@@ -261,7 +280,9 @@ __global__ void __launch_bounds__(kThreads) k_bsr_residual_dinv(int nbr, const i
         if (lane < BS)
 #pragma unroll
             for (int c = 0; c < BS; c++) dv[c] = dinv[(long long)(lane * BS + c) * dld + row];
-        accumulate_row<T, BS, G, U>(rowptr[row], rowptr[row + 1], lane, colidx, vals, ld, x, acc, UseAll());
+        int p0, p1;
+        row_range(row, ell, rowptr, p0, p1);
+        accumulate_row<T, BS, G, U>(p0, p1, lane, colidx, vals, ld, x, acc, UseAll());
     }
 #pragma unroll
     for (int r = 0; r < BS; r++) acc[r] = group_sum<G>(acc[r]);
@@ -278,8 +299,9 @@ __global__ void __launch_bounds__(kThreads) k_bsr_residual_dinv(int nbr, const i
 // Columns outside [col_lo, col_hi) are skipped: in a sweep that starts from x = 0 they hold
 // zeros not yet overwritten (later colours of a forward sweep, earlier ones of a backward
 // sweep), so skipping them changes no bit of the result and saves their loads. Block columns
-// are sorted, so the skipped ones form a head and a tail of each row. Padded slots (column -1 of
-// an ell view) are skipped the same way.
+// are sorted, so the skipped ones form a head and a tail of each row. The empty slots at the end
+// of a padded (ell) row hold the row's own column and are skipped as the diagonal is; a stop on a
+// column >= col_hi happens at a real block before them.
 template <class T, int BS, int G, int U>
 __global__ void __launch_bounds__(kThreads) k_bsr_gs(int row0, int row1, const int* __restrict__ rowptr,
                                                      const int* __restrict__ colidx,
@@ -309,9 +331,8 @@ __global__ void __launch_bounds__(kThreads) k_bsr_gs(int row0, int row1, const i
             if (col >= col_hi) return 2;
             return (col == row || col < col_lo) ? 0 : 1;
         };
-        // Padded rows (ell > 0) start at row * ell: no row-pointer load ahead of the walk.
-        const int p0 = ell > 0 ? row * ell : rowptr[row];
-        const int p1 = ell > 0 ? p0 + ell : rowptr[row + 1];
+        int p0, p1;
+        row_range(row, ell, rowptr, p0, p1);
         accumulate_row<T, BS, G, U>(p0, p1, lane, colidx, vals, ld, x, acc, sel);
     }
 #pragma unroll
@@ -959,11 +980,14 @@ template <class T, int BS, int G, int U>
 void spmv_u(const BsrView<T>& A, unsigned grid, int mode, const T* x, const T* aux, T* y, cudaStream_t s)
 {
     if (mode == kSpmvAssign)
-        pdl_launch(k_bsr_spmv<T, BS, G, U, kSpmvAssign>, grid, kThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
+        pdl_launch(k_bsr_spmv<T, BS, G, U, kSpmvAssign>, grid, kThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y,
+                   A.ell);
     else if (mode == kSpmvResidual)
-        pdl_launch(k_bsr_spmv<T, BS, G, U, kSpmvResidual>, grid, kThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
+        pdl_launch(k_bsr_spmv<T, BS, G, U, kSpmvResidual>, grid, kThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y,
+                   A.ell);
     else
-        pdl_launch(k_bsr_spmv<T, BS, G, U, kSpmvAddTo>, grid, kThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y);
+        pdl_launch(k_bsr_spmv<T, BS, G, U, kSpmvAddTo>, grid, kThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals, A.ld, x, aux, y,
+                   A.ell);
 }
 
 template <class T>
@@ -987,10 +1011,10 @@ void residual_dinv_shape(const BsrView<float>& A, unsigned grid, const float* di
     if constexpr (G >= BS) {
         if (A.unroll == 2)
             pdl_launch(k_bsr_residual_dinv<float, BS, G, 2>, grid, kThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals,
-                       A.ld, dinv, dld, x, b, w);
+                       A.ld, dinv, dld, x, b, w, A.ell);
         else
             pdl_launch(k_bsr_residual_dinv<float, BS, G, 1>, grid, kThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals,
-                       A.ld, dinv, dld, x, b, w);
+                       A.ld, dinv, dld, x, b, w, A.ell);
     }
 }
 
@@ -1024,7 +1048,7 @@ template <class T>
 void launch_jacobi(const BsrView<T>& A, const T* dinv, long long dld, T omega, const T* b, const T* xold, T* xnew,
                    cudaStream_t s)
 {
-    if (A.nbr == 0) return;
+    if (A.nbr == 0 || A.ell > 0) return;   // the Jacobi row walk needs the row pointers (callers pass A)
     const unsigned grid = grid_for((long long)A.nbr * A.lanes, kThreads);
     FHG_DISPATCH_BS_G(A.bs, A.lanes, {
         pdl_launch(k_bsr_jacobi<T, BS, G>, grid, kThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals, A.ld, dinv, dld, omega, b,
