@@ -68,7 +68,7 @@ struct Level {
     bool ahat_is_a = true;
     DevBsr<float> A32, P32, R32;
     DevBsr<float> G32;          // FP32 GS operator: A's off-diagonal blocks in padded rows, when they fit
-    DevBsr<float> A32p, P32p;   // FP32 A and P in padded rows (all blocks), when they fit
+    DevBsr<float> A32p;         // FP32 A in padded rows (all blocks), when they fit
     DevBsr<float> Ahat_hi;      // level 0, FP32 V-cycle: outer operator as an FP32 pair (hi part)
     float* ahat_lo = nullptr;   // (lo part, same layout)
     double* dinv = nullptr;
@@ -782,9 +782,11 @@ template <> struct LevelVecs<float> {
     static float* x(Level& L) { return L.x32; }
     static float* b(Level& L) { return L.b32; }
     static float* r(Level& L) { return L.r32; }
-    // products with A and P: the padded views when setup built them
+    // products with A: the padded view when setup built one
     static const BsrView<float>& A(Level& L) { return L.A32p.vals ? L.A32p.v : L.A32.v; }
-    static const BsrView<float>& P(Level& L) { return L.P32p.vals ? L.P32p.v : L.P32.v; }
+    // P stays CSR: at 64^3 its rows of up to 7 blocks pad by 29%, which costs what the saved
+    // row-pointer load gains (0.180 ms either way)
+    static const BsrView<float>& P(Level& L) { return L.P32.v; }
     static const BsrView<float>& R(Level& L) { return L.R32.v; }
     static const float* dinv(Level& L) { return L.dinv32; }
     static float* k(Level& L, int i) { return L.kv32[i]; }
@@ -1187,7 +1189,6 @@ void reset_device_state(Level& L)
     L.R32 = DevBsr<float>();
     L.G32 = DevBsr<float>();
     L.A32p = DevBsr<float>();
-    L.P32p = DevBsr<float>();
     L.Ahat_hi = DevBsr<float>();
     L.ahat_is_a = true;
     L.ahat_lo = nullptr;
@@ -1634,7 +1635,6 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
             if ((rc = upload_bsr<double>(ctx, Rp, L.R, nullptr))) return rc;
             if (fp32) {
                 if ((rc = upload_bsr<float>(ctx, Pp, L.P32, &L.P))) return rc;
-                if ((rc = upload_padded(ctx, Pp, L.P32p, false, 16))) return rc;
                 if ((rc = upload_bsr<float>(ctx, Rp, L.R32, &L.R))) return rc;
             }
         }
