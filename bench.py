@@ -54,7 +54,9 @@ def parse():
     ap.add_argument("--max-coarse-rows", type=int, default=1000)
     ap.add_argument("--galerkin", action="store_true", help="Galerkin coarse operators (the reference's -g 1)")
     ap.add_argument("--fast-smoothers", default="bgs,rbgs", help="pre,post smoothers of the fast (FP32) method")
-    ap.add_argument("--fast-nu", default="2,2", help="pre,post smoothing steps of the fast (FP32) method")
+    ap.add_argument("--fast-nu", default="3,3", help="pre,post smoothing steps of the fast (FP32) method")
+    ap.add_argument("--fast-coarse-nu", default="4,4",
+                    help="pre,post smoothing steps of the fast method on levels >= 1 (-1,-1: as --fast-nu)")
     ap.add_argument("--weights", default="", help="learned-step network (default: the committed one)")
     ap.add_argument("--no-learned", action="store_true", help="report the FP32 method as the headline")
     ap.add_argument("--batch", type=int, default=0,
@@ -251,6 +253,7 @@ def run_ours(args, dist: Dist):
     n0 = As[0].shape[0]
     fast_pre, fast_post = args.fast_smoothers.split(",")
     fast_npre, fast_npost = (int(v) for v in args.fast_nu.split(","))
+    fast_cpre, fast_cpost = (int(v) for v in args.fast_coarse_nu.split(","))
     ctx = N.Context(dev)
     t0 = time.perf_counter()
     for l, A in enumerate(As):
@@ -292,18 +295,20 @@ def run_ours(args, dist: Dist):
     params, wmeta = LN.load_params(args.weights or LN.DEFAULT_WEIGHTS)
     # the learned step exists for face blocks of 2..4 unknowns (k = 1 in 3D)
     have_learned = bs <= 4 and not args.no_learned
-    methods = {"plain": ("fp64", "bgs", "rbgs", 1, 1, False),
-               "fp64_fast": ("fp64", fast_pre, fast_post, fast_npre, fast_npost, False),
-               "fast": ("fp32", fast_pre, fast_post, fast_npre, fast_npost, False)}
+    fast_coarse = (fast_cpre, fast_cpost)
+    methods = {"plain": ("fp64", "bgs", "rbgs", 1, 1, (-1, -1), False),
+               "fp64_fast": ("fp64", fast_pre, fast_post, fast_npre, fast_npost, fast_coarse, False),
+               "fast": ("fp32", fast_pre, fast_post, fast_npre, fast_npost, fast_coarse, False)}
     if have_learned:
-        methods["learned"] = ("fp32", fast_pre, fast_post, fast_npre, fast_npost, True)
+        methods["learned"] = ("fp32", fast_pre, fast_post, fast_npre, fast_npost, fast_coarse, True)
     results = {}
     launches = {}
     clocks = {}
     solutions = {}
     learned_its = {}
-    for name, (prec, pre, post, npre, npost, use_learned) in methods.items():
+    for name, (prec, pre, post, npre, npost, coarse, use_learned) in methods.items():
         ctx.set_cycle(pre, post, npre, npost, 1)
+        ctx.set_coarse_smoothing(*coarse)
         ctx.set_vcycle_precision(prec)
         if use_learned:
             ctx.set_learned(params, "fallback")
@@ -328,7 +333,9 @@ def run_ours(args, dist: Dist):
         t_step = dist.max(float(np.mean(times)))
         solutions[name] = x_dev.cpu().numpy()
         results[name] = dict(s=t_step, iterations=iters[-1], true_rel_residual=true_residual(), final=float(hist[-1]),
-                             cycle=f"V({npre},{npost}) {pre}/{post}", vcycle_precision=prec)
+                             cycle=f"V({npre},{npost}) {pre}/{post}" + (
+                                 f", V({coarse[0]},{coarse[1]}) on levels >= 1" if min(coarse) >= 0 else ""),
+                             vcycle_precision=prec)
         if use_learned:
             results[name]["learned_iterations"] = info.learned_iterations
             results[name]["fallback_reference_rate"] = ctx.learned_reference_rate()
@@ -344,6 +351,7 @@ def run_ours(args, dist: Dist):
     head = "learned" if have_learned else "fast"
     # End to end through the public C ABI with pinned host buffers (H2D b, solve, D2H x), headline method.
     ctx.set_cycle(fast_pre, fast_post, fast_npre, fast_npost, 1)
+    ctx.set_coarse_smoothing(fast_cpre, fast_cpost)
     ctx.set_vcycle_precision("fp32")
     if head == "learned":
         ctx.set_learned(params, "fallback")

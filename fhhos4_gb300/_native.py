@@ -39,7 +39,7 @@ LEARNED_PARAMS = 24848
 # Every symbol include/fhg.h declares.
 EXPORTS = ["fhg_default_options", "fhg_create", "fhg_destroy", "fhg_last_error", "fhg_set_level",
            "fhg_set_prolongation", "fhg_setup", "fhg_solve", "fhg_solve_device", "fhg_apply",
-           "fhg_time_op", "fhg_set_cycle", "fhg_set_vcycle_precision", "fhg_level_info", "fhg_get_permutation",
+           "fhg_time_op", "fhg_set_cycle", "fhg_set_coarse_smoothing", "fhg_set_vcycle_precision", "fhg_level_info", "fhg_get_permutation",
            "fhg_kernel_launches", "fhg_residual_norm_noalloc", "fhg_set_face_tensors", "fhg_set_learned",
            "fhg_learned_reference_rate", "fhg_learned_features", "fhg_apply_internal", "fhg_net_num_params",
            "fhg_net_create", "fhg_net_destroy", "fhg_net_last_error", "fhg_net_set_params", "fhg_net_get_params",
@@ -61,7 +61,7 @@ class Options(C.Structure):
                 ("tolerance", C.c_double), ("max_iterations", C.c_int), ("vcycle_precision", C.c_int),
                 ("colouring", C.c_int), ("use_graphs", C.c_int), ("autotune", C.c_int),
                 ("max_coarse_rows", C.c_int), ("outer_split", C.c_int), ("w_loops", C.c_int),
-                ("galerkin", C.c_int)]
+                ("galerkin", C.c_int), ("coarse_pre_iterations", C.c_int), ("coarse_post_iterations", C.c_int)]
 
 
 class SolveInfo(C.Structure):
@@ -97,6 +97,7 @@ def load(path: str = LIB):
     lib.fhg_time_op.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_double)]
     lib.fhg_set_vcycle_precision.argtypes = [C.c_void_p, C.c_int]
     lib.fhg_set_cycle.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+    lib.fhg_set_coarse_smoothing.argtypes = [C.c_void_p, C.c_int, C.c_int]
     lib.fhg_level_info.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_longlong), P(C.c_int), P(C.c_int),
                                    P(C.c_longlong)]
     lib.fhg_get_permutation.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
@@ -208,6 +209,10 @@ class Context:
 
     def set_cycle(self, pre: str = "bgs", post: str = "rbgs", npre: int = 1, npost: int = 1, w_loops: int = 1):
         self._check(self.lib.fhg_set_cycle(self.h, SMOOTHERS[pre], SMOOTHERS[post], npre, npost, w_loops))
+
+    def set_coarse_smoothing(self, npre: int = -1, npost: int = -1):
+        """Smoothing steps on levels >= 1 (-1: those of level 0)."""
+        self._check(self.lib.fhg_set_coarse_smoothing(self.h, npre, npost))
 
     def set_vcycle_precision(self, precision: str):
         self._check(self.lib.fhg_set_vcycle_precision(self.h, PRECISION[precision]))

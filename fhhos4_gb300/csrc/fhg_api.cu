@@ -921,11 +921,16 @@ void mg_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
         return;
     }
     Level& C = ctx->levels[l + 1];
+    // Smoothing steps of this level: the coarse counts apply on levels >= 1 when set.
+    const int npre = l > 0 && ctx->opts.coarse_pre_iterations >= 0 ? ctx->opts.coarse_pre_iterations
+                                                                    : ctx->opts.pre_iterations;
+    const int npost = l > 0 && ctx->opts.coarse_post_iterations >= 0 ? ctx->opts.coarse_post_iterations
+                                                                      : ctx->opts.post_iterations;
     // A zero-start GS sweep writes every entry before any is read: no clearing needed then.
     const int pre = ctx->opts.pre_smoother;
-    const bool gs_zero = x_zero && is_gs(pre) && ctx->opts.pre_iterations > 0;
+    const bool gs_zero = x_zero && is_gs(pre) && npre > 0;
     if (x_zero && !gs_zero) cudaMemsetAsync(x, 0, sizeof(T) * (size_t)L.n, s);
-    smooth<T>(ctx, l, pre, ctx->opts.pre_iterations, b, x, gs_zero);
+    smooth<T>(ctx, l, pre, npre, b, x, gs_zero);
     fhg::launch_spmv<T>(V::A(L), fhg::kSpmvResidual, x, b, V::r(L), s);
     fhg::launch_spmv<T>(V::R(L), fhg::kSpmvAssign, V::r(L), nullptr, V::b(C), s);
     if (ctx->opts.w_loops == FHG_CYCLE_K && l + 1 < ctx->nlevels - 1) {
@@ -938,7 +943,7 @@ void mg_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
         }
     }
     fhg::launch_spmv<T>(V::P(L), fhg::kSpmvAddTo, V::x(C), x, x, s);
-    smooth<T>(ctx, l, ctx->opts.post_smoother, ctx->opts.post_iterations, b, x);
+    smooth<T>(ctx, l, ctx->opts.post_smoother, npost, b, x);
     if constexpr (std::is_same<T, float>::value) {
         if (l == 0 && ctx->learned_now) learned_step(ctx, b, x);
     }
@@ -1413,6 +1418,8 @@ void fhg_default_options(fhg_options* o)
     o->outer_split = 1;
     o->w_loops = 1;
     o->galerkin = 0;
+    o->coarse_pre_iterations = -1;
+    o->coarse_post_iterations = -1;
 }
 
 int fhg_create(fhg_ctx** out, int device)
@@ -1504,7 +1511,8 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
     if (opts) ctx->opts = *opts;
     fhg_options& o = ctx->opts;
     if (o.max_coarse_rows <= 0) o.max_coarse_rows = 8192;
-    if (o.max_iterations < 0 || o.pre_iterations < 0 || o.post_iterations < 0)
+    if (o.max_iterations < 0 || o.pre_iterations < 0 || o.post_iterations < 0 || o.coarse_pre_iterations < -1 ||
+        o.coarse_post_iterations < -1)
         return fail(ctx, FHG_ERR_INVALID_ARG, "negative iteration count");
     if (o.pre_smoother < 0 || o.pre_smoother > 6 || o.post_smoother < 0 || o.post_smoother > 6)
         return fail(ctx, FHG_ERR_INVALID_ARG, "unknown smoother code");
@@ -2026,6 +2034,21 @@ int fhg_set_cycle(fhg_ctx* ctx, int pre_smoother, int post_smoother, int pre_ite
     ctx->opts.pre_iterations = pre_iterations;
     ctx->opts.post_iterations = post_iterations;
     ctx->opts.w_loops = w_loops;
+    return FHG_OK;
+}
+
+int fhg_set_coarse_smoothing(fhg_ctx* ctx, int pre_iterations, int post_iterations)
+{
+    if (!ctx) return FHG_ERR_INVALID_ARG;
+    if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
+    if (pre_iterations < -1 || post_iterations < -1) return fail(ctx, FHG_ERR_INVALID_ARG, "negative iteration count");
+    if (ctx->opts.coarse_pre_iterations != pre_iterations || ctx->opts.coarse_post_iterations != post_iterations) {
+        free_graphs(ctx);
+        ctx->epoch++;
+        ctx->rho_plain = 0.0;
+        ctx->opts.coarse_pre_iterations = pre_iterations;
+        ctx->opts.coarse_post_iterations = post_iterations;
+    }
     return FHG_OK;
 }
 

@@ -23,6 +23,8 @@ def main():
     ap.add_argument("--solves", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--autotune", type=int, default=1, help="0: default launch shapes (comparable across runs)")
+    ap.add_argument("--coarse-nu", default="", help="pre,post smoothing steps on levels >= 1 (default: --nu)")
+    ap.add_argument("--levels", type=int, default=0, help="use the first N levels (the last one solved directly)")
     ap.add_argument("--step", choices=["", "learned_tcgen05", "learned_mma_sync", "gs_fp32", "outer_df"], default="")
     a = ap.parse_args()
 
@@ -42,10 +44,11 @@ def main():
         ctx.set_prolongation(l, P)
     ctx.set_face_tensors(H.face_tensors(0))
     H.close()
+    nlev = a.levels if a.levels > 0 else len(As)
     o = N.default_options()
     o.vcycle_precision = N.PRECISION["fp32"]
     o.autotune = a.autotune
-    ctx.setup(len(As), o)
+    ctx.setup(nlev, o)
     npre, npost = (int(v) for v in a.nu.split(","))
     params = LN.load_params()[0]
     if a.method == "plain":
@@ -53,6 +56,8 @@ def main():
         ctx.set_vcycle_precision("fp64")
     else:
         ctx.set_cycle("bgs", "rbgs", npre, npost, 1)
+        if a.coarse_nu:
+            ctx.set_coarse_smoothing(*(int(v) for v in a.coarse_nu.split(",")))
         if a.method == "learned" and bs <= 4:
             ctx.set_learned(params, "fallback")
     bd = torch.from_numpy(b).cuda()

@@ -85,6 +85,9 @@ class Multigrid(IterativeSolver):
         self.Colouring = True
         self.Autotune = False
         self.MaxCoarseRows = 8192
+        # smoothing steps on levels >= 1; -1: PreSmoothingIterations / PostSmoothingIterations
+        self.CoarsePreSmoothingIterations = -1
+        self.CoarsePostSmoothingIterations = -1
         self._As: List[sp.csr_matrix] = []
         self._Ps: List[sp.csr_matrix] = []
         self._nLevels = nLevels
@@ -152,6 +155,8 @@ class _KrylovOnGpu(IterativeSolver):
         o.outer_split = 1 if self.OuterSplit else 0
         o.w_loops = N.CYCLE_K if mg.Cycle == "K" else (mg.WLoops if mg.Cycle == "W" else 1)
         o.galerkin = 1 if mg.UseGalerkinOperator else 0
+        o.coarse_pre_iterations = mg.CoarsePreSmoothingIterations
+        o.coarse_post_iterations = mg.CoarsePostSmoothingIterations
         return o
 
     def Setup(self, A):
@@ -225,7 +230,8 @@ class ConjugateGradient(_KrylovOnGpu):
 
 def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: str = "bgs", post: str = "rbgs",
            precision: str = "fp64", krylov: str = "fcg", device: int = 0, autotune: bool = False,
-           use_graphs: bool = True, outer_split: bool = True, cycle: str = "V", galerkin: bool = False):
+           use_graphs: bool = True, outer_split: bool = True, cycle: str = "V", galerkin: bool = False,
+           nu=(1, 1), coarse_nu=(-1, -1)):
     """SolverFactory-style construction of "-s fcgmg -cycle V,1,1" (src/Solver/SolverFactory.h:156-200)."""
     mg = Multigrid(len(As))
     mg.SetHierarchy(As, Ps)
@@ -236,6 +242,8 @@ def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: st
     mg.Cycle = cycle
     mg.WLoops = 2 if cycle == "W" else 1
     mg.UseGalerkinOperator = galerkin
+    mg.PreSmoothingIterations, mg.PostSmoothingIterations = nu
+    mg.CoarsePreSmoothingIterations, mg.CoarsePostSmoothingIterations = coarse_nu
     solver = FlexibleConjugateGradient(1) if krylov == "fcg" else ConjugateGradient()
     solver.Precond = SolverPreconditioner(mg)
     solver.Tolerance = tol

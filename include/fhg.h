@@ -94,6 +94,10 @@ typedef struct {
     int galerkin;               /* Multigrid::UseGalerkinOperator ("-g 1", main.cpp:1307): coarse operators
                                    A_{l+1} = P_l^T A_l P_l formed at setup (Level.h:133-137); operators given
                                    for levels >= 1 are then not needed and are replaced */
+    int coarse_pre_iterations;  /* smoothing steps before the coarse correction on levels >= 1; -1 (the
+                                   default): pre_iterations, as the reference (one count for every level).
+                                   No counterpart in the reference. */
+    int coarse_post_iterations; /* the same after it; -1: post_iterations */
 } fhg_options;
 
 typedef struct {
@@ -167,6 +171,10 @@ int fhg_time_op(fhg_ctx* ctx, int level, int op, int precision, int warmup, int 
  * (src/Solver/Multigrid/Multigrid.h:19-26), without rebuilding the hierarchy. */
 int fhg_set_cycle(fhg_ctx* ctx, int pre_smoother, int post_smoother, int pre_iterations, int post_iterations,
                   int w_loops);
+
+/* Smoothing steps on levels >= 1 (-1: those of level 0, the reference's behaviour); cycles already
+ * captured in graphs are rebuilt. No counterpart in the reference. */
+int fhg_set_coarse_smoothing(fhg_ctx* ctx, int pre_iterations, int post_iterations);
 
 /* Switch the V-cycle precision of a set-up context (FP32 needs a setup with FHG_PREC_FP32,
  * which keeps both copies). The outer Krylov iteration stays FP64. */

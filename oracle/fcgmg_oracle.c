@@ -451,7 +451,11 @@ static void cycle(orc_mg* mg, int l, const double* b, double* x, int x_zero)
         return;
     }
     if (x_zero) memset(x, 0, sizeof(double) * (size_t)n);
-    smooth(mg, l, mg->opt->pre_smoother, mg->opt->pre_iterations, b, x);
+    const int npre = l > 0 && mg->opt->coarse_pre_iterations >= 0 ? mg->opt->coarse_pre_iterations
+                                                                  : mg->opt->pre_iterations;
+    const int npost = l > 0 && mg->opt->coarse_post_iterations >= 0 ? mg->opt->coarse_post_iterations
+                                                                    : mg->opt->post_iterations;
+    smooth(mg, l, mg->opt->pre_smoother, npre, b, x);
     orc_residual(&mg->A[l], b, x, mg->r[l]);
     orc_spmv(&mg->R[l], mg->r[l], mg->rc[l]);
     int nc = mg->A[l + 1].n_rows;
@@ -467,7 +471,7 @@ static void cycle(orc_mg* mg, int l, const double* b, double* x, int x_zero)
     }
     orc_spmv(&mg->P[l], mg->ec[l], mg->r[l]);
     for (int i = 0; i < n; i++) x[i] += mg->r[l][i];
-    smooth(mg, l, mg->opt->post_smoother, mg->opt->post_iterations, b, x);
+    smooth(mg, l, mg->opt->post_smoother, npost, b, x);
 }
 
 static void vcycle(orc_mg* mg, int l, const double* b, double* x) { cycle(mg, l, b, x, 1); }

@@ -33,6 +33,10 @@ typedef struct {
     double tolerance;
     int max_iterations;
     int w_loops;                       /* Multigrid::WLoops: 1 V-cycle, 2 W-cycle; ORC_CYCLE_K: K-cycle */
+    /* Smoothing steps on levels >= 1; -1: pre_iterations / post_iterations (the reference has one
+     * count for every level). An extension of the restatement with no counterpart in the
+     * reference, mirroring fhg_options.coarse_pre_iterations / coarse_post_iterations. */
+    int coarse_pre_iterations, coarse_post_iterations;
 } orc_options;
 #define ORC_CYCLE_K (-1)
 

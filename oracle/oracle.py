@@ -34,7 +34,8 @@ class _CSR(C.Structure):
 class _Opts(C.Structure):
     _fields_ = [("pre_smoother", C.c_int), ("post_smoother", C.c_int), ("omega", C.c_double),
                 ("pre_iterations", C.c_int), ("post_iterations", C.c_int), ("krylov", C.c_int),
-                ("tolerance", C.c_double), ("max_iterations", C.c_int), ("w_loops", C.c_int)]
+                ("tolerance", C.c_double), ("max_iterations", C.c_int), ("w_loops", C.c_int),
+                ("coarse_pre_iterations", C.c_int), ("coarse_post_iterations", C.c_int)]
 
 
 _lib = None
@@ -151,8 +152,9 @@ def last_timing():
 
 
 def fcgmg_solve(As, Ps, b, bs, pre="bgs", post="rbgs", krylov="fcg", tol=1e-8, maxit=200,
-                pre_iterations=1, post_iterations=1, cycle="V"):
-    """Returns (x, history, iterations, status)."""
+                pre_iterations=1, post_iterations=1, cycle="V", coarse_iterations=(-1, -1)):
+    """Returns (x, history, iterations, status). coarse_iterations: smoothing steps on levels >= 1
+    (-1: those of level 0, the reference's behaviour)."""
     keep: list = []
     nl = len(As)
     Aarr = (_CSR * nl)(*[_wrap(as_csr(A), keep) for A in As])
@@ -161,7 +163,8 @@ def fcgmg_solve(As, Ps, b, bs, pre="bgs", post="rbgs", krylov="fcg", tol=1e-8, m
     qc, om2 = SMOOTHER_CODES[post]
     opts = _Opts(pc, qc, om if pc == BJ else om2, pre_iterations, post_iterations,
                  KRYLOV_CG if krylov == "cg" else KRYLOV_FCG, tol, maxit,
-                 2 if cycle == "W" else (-1 if cycle == "K" else 1))
+                 2 if cycle == "W" else (-1 if cycle == "K" else 1), int(coarse_iterations[0]),
+                 int(coarse_iterations[1]))
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.zeros(As[0].shape[0])
     hist = np.zeros(maxit + 1)

@@ -106,6 +106,29 @@ def test_cycles_and_smoothers_match_reference(case, variant, pre, post, cycle):
     assert np.linalg.norm(x[sp_] - xr) / np.linalg.norm(xr) < X_RTOL
 
 
+@pytest.mark.parametrize("nu,coarse_nu", [((1, 1), (2, 2)), ((2, 2), (4, 3))])
+def test_coarse_smoothing_counts_match_the_oracle(case, nu, coarse_nu):
+    """Smoothing counts per level (levels >= 1 apart from level 0; no counterpart in the reference)
+    against the oracle extended the same way, on the colour-permuted hierarchy: exact iterations,
+    histories within the parity tolerance."""
+    Ac, Pc, bc = O.permute_hierarchy(case.As, case.Ps, case.b, case.bs, case.perms)
+    _, h_o, it_o, st = O.fcgmg_solve(Ac, Pc, bc, case.bs, pre_iterations=nu[0], post_iterations=nu[1],
+                                     coarse_iterations=coarse_nu)
+    assert st == 0
+    solver = S().fcg_mg(Ac, Pc, case.bs, nu=nu, coarse_nu=coarse_nu)
+    solver.Solve(bc)
+    assert solver.IterationCount == it_o
+    assert hist_close(solver.History, h_o)
+    # the setter on a context set up without coarse counts gives the same run
+    from fhhos4_gb300 import _native as N
+    plain = S().fcg_mg(Ac, Pc, case.bs, nu=nu)   # keeps its context alive
+    ctx = plain.Context()
+    ctx.set_coarse_smoothing(*coarse_nu)
+    rc, x, hist, info = ctx.solve(bc, 200)
+    assert rc == N.FHG_OK and info.iterations == it_o
+    assert hist_close(hist[: it_o + 1], h_o)
+
+
 def test_kcycle_with_fp32_vcycle_reaches_fp64_tolerance(case):
     """K-cycle with FP32 cycles inside the FP64 FCG: the FP64 true residual meets 1e-8 within a few
     iterations of the reference's FP64 K-cycle."""

@@ -76,6 +76,21 @@ def check_bj23_history(hist, ref):
     assert hist[-1] < 1e-8
 
 
+def test_coarse_smoothing_counts(case):
+    """Per-level smoothing counts (an extension with no counterpart in the reference): counts equal to
+    level 0's reproduce the reference run bit for bit; more coarse smoothing changes the history and
+    needs no more iterations."""
+    Ac, Pc, bc = O.permute_hierarchy(case.As, case.Ps, case.b, case.bs, case.perms)
+    _, h_ref, it_ref, _ = O.fcgmg_solve(Ac, Pc, bc, case.bs)
+    _, h_same, it_same, _ = O.fcgmg_solve(Ac, Pc, bc, case.bs, coarse_iterations=(1, 1))
+    assert it_same == it_ref and np.array_equal(h_same, h_ref)
+    _, h_more, it_more, st = O.fcgmg_solve(Ac, Pc, bc, case.bs, coarse_iterations=(3, 3))
+    assert st == 0 and h_more[-1] < 1e-8
+    assert it_more <= it_ref
+    if case.levels > 2:
+        assert not np.array_equal(h_more[: min(len(h_more), len(h_ref))], h_ref[: min(len(h_more), len(h_ref))])
+
+
 def test_colouring_is_the_committed_one(case):
     perms, _ = O.colour_perms(case.As, case.bs)
     for l in range(case.levels):
