@@ -77,7 +77,7 @@ class Field:
     """One coefficient field: hierarchy on a GPU context (FP32 V-cycle) plus its face tensors."""
 
     def __init__(self, spec: FieldSpec, device: int = 0, smoothers=("bgs", "rbgs"), nu=(1, 1), autotune=False,
-                 source: str = "sine"):
+                 source: str = "sine", coarse_nu=(-1, -1)):
         blocks = spec.checker_blocks or max(1, spec.n // 4)
         H = hho.Hierarchy(3, spec.n, spec.k, max_coarse_rows=spec.max_coarse_rows, source=source,
                           coefficient=spec.coefficient, contrast=spec.contrast, checker_blocks=blocks,
@@ -101,6 +101,7 @@ class Field:
         o.vcycle_precision = N.PRECISION["fp32"]
         o.pre_smoother, o.post_smoother = N.SMOOTHERS[smoothers[0]], N.SMOOTHERS[smoothers[1]]
         o.pre_iterations, o.post_iterations = nu
+        o.coarse_pre_iterations, o.coarse_post_iterations = coarse_nu
         o.autotune = 1 if autotune else 0
         ctx.setup(len(self.As), o)
         self.ctx = ctx
@@ -177,7 +178,7 @@ class TrainLog:
 def train(net: N.Net, fields: int = 64, n: int = 16, samples_per_field: int = 4, steps_per_sample: int = 1,
           lr: float = 2e-3, lr_min: float = 1e-4, weight_decay: float = 0.0, seed0: int = 1000, device: int = 0,
           spec_kw: Optional[dict] = None, log_every: int = 0, smoothers=("bgs", "rbgs"), nu=(1, 1),
-          identity_every: int = 0) -> TrainLog:
+          identity_every: int = 0, coarse_nu=(-1, -1)) -> TrainLog:
     """Stream `fields` seeded fields (seeds seed0, seed0+1, ...) and take Adam steps on their samples;
     identity_every = m > 0 makes every m-th field the identity coefficient instead."""
     log = TrainLog()
@@ -189,7 +190,7 @@ def train(net: N.Net, fields: int = 64, n: int = 16, samples_per_field: int = 4,
         if identity_every and fi % identity_every == identity_every - 1:
             kw["coefficient"] = "identity"
         spec = FieldSpec(n=n, seed=seed0 + fi, **kw)
-        f = Field(spec, device=device, smoothers=smoothers, nu=nu)
+        f = Field(spec, device=device, smoothers=smoothers, nu=nu, coarse_nu=coarse_nu)
         try:
             samples = make_samples(f, samples_per_field, seed=seed0 * 7919 + fi)
             for _ in range(steps_per_sample):
@@ -224,16 +225,20 @@ def _cli():
     ap.add_argument("--log-every", type=int, default=20)
     ap.add_argument("--nu", default="2,2", help="pre,post smoothing steps of the cycle the step corrects")
     ap.add_argument("--identity-every", type=int, default=4, help="every m-th field has K = I (0: none)")
+    ap.add_argument("--coarse-nu", default="-1,-1", help="pre,post smoothing steps on levels >= 1 (-1: as --nu)")
     a = ap.parse_args()
     nu = tuple(int(v) for v in a.nu.split(","))
+    coarse_nu = tuple(int(v) for v in a.coarse_nu.split(","))
     net = N.Net(0)
     p0 = load_params(a.init)[0] if a.init else init_params(a.seed)
     net.set_params(p0)
     log = train(net, fields=a.fields, n=a.n, samples_per_field=a.samples, steps_per_sample=a.repeat, lr=a.lr,
-                seed0=a.seed, log_every=a.log_every, nu=nu, identity_every=a.identity_every)
+                seed0=a.seed, log_every=a.log_every, nu=nu, identity_every=a.identity_every, coarse_nu=coarse_nu)
     meta = {"fields": a.fields, "n": a.n, "k": 1, "coefficient": "anisotropic diag(1,1,eps), eps log-U[1e-3,1], "
             "random rotation per 4^3 block" + (f"; every {a.identity_every}th field K = I" if a.identity_every else ""),
-            "cycle": f"V({nu[0]},{nu[1]}) bgs/rbgs", "samples_per_field": a.samples, "repeat": a.repeat, "lr": a.lr,
+            "cycle": f"V({nu[0]},{nu[1]}) bgs/rbgs" + (f", V({coarse_nu[0]},{coarse_nu[1]}) on levels >= 1"
+                                                       if min(coarse_nu) >= 0 else ""),
+            "init": os.path.basename(a.init) if a.init else "random", "samples_per_field": a.samples, "repeat": a.repeat, "lr": a.lr,
             "seed0": a.seed, "steps": log.steps, "seconds": round(log.seconds, 1),
             "first_mean_loss": float(np.mean(log.losses[:200])) if log.losses else None,
             "final_mean_loss": float(np.mean(log.losses[-200:])) if log.losses else None}

@@ -25,6 +25,7 @@ def main():
     ap.add_argument("--autotune", type=int, default=1, help="0: default launch shapes (comparable across runs)")
     ap.add_argument("--coarse-nu", default="", help="pre,post smoothing steps on levels >= 1 (default: --nu)")
     ap.add_argument("--levels", type=int, default=0, help="use the first N levels (the last one solved directly)")
+    ap.add_argument("--weights", default="", help="learned-step network (default: the committed one)")
     ap.add_argument("--step", choices=["", "learned_tcgen05", "learned_mma_sync", "gs_fp32", "outer_df"], default="")
     a = ap.parse_args()
 
@@ -50,7 +51,7 @@ def main():
     o.autotune = a.autotune
     ctx.setup(nlev, o)
     npre, npost = (int(v) for v in a.nu.split(","))
-    params = LN.load_params()[0]
+    params = LN.load_params(a.weights or LN.DEFAULT_WEIGHTS)[0]
     if a.method == "plain":
         ctx.set_cycle("bgs", "rbgs", 1, 1, 1)
         ctx.set_vcycle_precision("fp64")
