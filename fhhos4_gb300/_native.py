@@ -32,6 +32,7 @@ OP_SPMV, OP_RESIDUAL, OP_RESTRICT, OP_PROLONG_ADD = 0, 1, 2, 3
 OP_GS_FORWARD, OP_GS_BACKWARD, OP_JACOBI, OP_SYM_SPMV = 4, 5, 6, 7
 OP_COARSE_SOLVE, OP_VCYCLE, OP_VCYCLE_LEARNED, OP_LEARNED_STEP = 8, 9, 10, 11
 CYCLE_K = -1   # fhg_options.w_loops / set_cycle: the K-cycle
+GS_LAYOUT = {"auto": 0, "row": 1, "slot": 2}   # fhg_options.gs_layout
 LEARNED = {"off": 0, "fallback": 1, "always": 2}
 LEARNED_MMA_SYNC = 16
 LEARNED_PARAMS = 24848
@@ -61,7 +62,8 @@ class Options(C.Structure):
                 ("tolerance", C.c_double), ("max_iterations", C.c_int), ("vcycle_precision", C.c_int),
                 ("colouring", C.c_int), ("use_graphs", C.c_int), ("autotune", C.c_int),
                 ("max_coarse_rows", C.c_int), ("outer_split", C.c_int), ("w_loops", C.c_int),
-                ("galerkin", C.c_int), ("coarse_pre_iterations", C.c_int), ("coarse_post_iterations", C.c_int)]
+                ("galerkin", C.c_int), ("coarse_pre_iterations", C.c_int), ("coarse_post_iterations", C.c_int),
+                ("gs_layout", C.c_int)]
 
 
 class SolveInfo(C.Structure):

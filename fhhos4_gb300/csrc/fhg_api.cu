@@ -69,6 +69,8 @@ struct Level {
     DevBsr<float> A32, P32, R32;
     DevBsr<float> G32;          // FP32 GS operator: A's off-diagonal blocks in padded rows, when they fit
     DevBsr<float> A32p;         // FP32 A in padded rows (all blocks), when they fit
+    DevBsr<float> G32s;         // the GS view slot-major per colour (one thread per row), when built
+    bool gs_slot = false;       // the GS sweeps use G32s (setup: gs_layout or the autotuner)
     DevBsr<float> Ahat_hi;      // level 0, FP32 V-cycle: outer operator as an FP32 pair (hi part)
     float* ahat_lo = nullptr;   // (lo part, same layout)
     double* dinv = nullptr;
@@ -671,6 +673,54 @@ int upload_padded(fhg_ctx* ctx, const HostBsr& B, DevBsr<float>& D, bool offdiag
     return FHG_OK;
 }
 
+// The off-diagonal GS view slot-major per colour: slot s of row i of colour [c0, c1) at
+// c0 * W + s * (c1 - c0) + (i - c0) (W = the most off-diagonal blocks of a row, 4..8), so that a
+// sweep with one thread per row reads each slot of 32 consecutive rows as 32 consecutive words.
+// Empty slots hold the row's own column and zero values, as in upload_padded. Built only when W
+// is in 4..8 and the padding adds at most half; otherwise D stays empty.
+int upload_offdiag_slot_major(fhg_ctx* ctx, const HostBsr& B, const std::vector<int>& colour_start,
+                              DevBsr<float>& D)
+{
+    D = DevBsr<float>();
+    int W = 0;
+    long long kept = 0;
+    for (int i = 0; i < B.nbr; i++) {
+        int c = 0;
+        for (int p = B.rowptr[i]; p < B.rowptr[i + 1]; p++) c += B.colidx[p] != i;
+        W = std::max(W, c);
+        kept += c;
+    }
+    const long long slots = (long long)B.nbr * W;
+    if (W < 4 || W > 8 || slots > kept + kept / 2 || slots > INT32_MAX) return FHG_OK;
+    if (colour_start.empty() || colour_start.back() != B.nbr) return FHG_OK;
+    const int bb = B.bs * B.bs;
+    const long long ld = round_up(slots, 32);
+    std::vector<int> col((size_t)slots);
+    std::vector<float> soa((size_t)ld * bb, 0.f);
+    for (size_t c = 0; c + 1 < colour_start.size(); c++) {
+        const long long c0 = colour_start[c], nrc = colour_start[c + 1] - c0;
+        for (long long i = c0; i < c0 + nrc; i++) {
+            int k = 0;
+            for (int p = B.rowptr[i]; p < B.rowptr[i + 1]; p++) {
+                if (B.colidx[p] == i) continue;
+                const long long q = c0 * W + k * nrc + (i - c0);
+                col[(size_t)q] = B.colidx[p];
+                for (int e = 0; e < bb; e++) soa[(size_t)e * ld + q] = (float)B.vals[(size_t)p * bb + e];
+                k++;
+            }
+            for (; k < W; k++) col[(size_t)(c0 * W + k * nrc + (i - c0))] = (int)i;
+        }
+    }
+    int rc;
+    if ((rc = upload(ctx, &D.colidx, col.data(), col.size()))) return rc;
+    if ((rc = upload(ctx, &D.vals, soa.data(), soa.size()))) return rc;
+    D.v.nbr = B.nbr; D.v.nbc = B.nbc; D.v.bs = B.bs; D.v.nnzb = slots; D.v.ld = ld; D.v.ell = W;
+    D.v.slot_major = 1;
+    D.v.rowptr = nullptr; D.v.colidx = D.colidx; D.v.vals = D.vals;
+    D.v.lanes = 1;
+    return FHG_OK;
+}
+
 // Outer operator as an FP32 pair: hi = fl32(a), lo = fl32(a - hi), entry-major like upload_bsr.
 int upload_bsr_split(fhg_ctx* ctx, const HostBsr& B, DevBsr<float>& D, float** lo_out, const DevBsr<double>& share_index)
 {
@@ -791,7 +841,11 @@ template <> struct LevelVecs<float> {
     static const float* dinv(Level& L) { return L.dinv32; }
     static float* k(Level& L, int i) { return L.kv32[i]; }
     // GS sweeps: the padded off-diagonal view when setup built one
-    static const BsrView<float>& gs(Level& L) { return L.G32.vals ? L.G32.v : L.A32.v; }
+    static const BsrView<float>& gs(Level& L)
+    {
+        if (L.gs_slot && L.G32s.vals) return L.G32s.v;
+        return L.G32.vals ? L.G32.v : L.A32.v;
+    }
     static const BsrView<float>& Acsr(Level& L) { return L.A32.v; }   // Jacobi: row pointers
 };
 
@@ -1091,7 +1145,7 @@ int build_graphs(fhg_ctx* ctx, bool learned = false)
 // blocks per lane step U in {1, 2} (U = 2 for bs <= 3 only), timed with the launch that will
 // run; the fastest pair is kept. `run(G, U)` launches the operator once.
 template <class F>
-int tune(fhg_ctx* ctx, int bs, int& lanes, int& unroll, F run)
+int tune(fhg_ctx* ctx, int bs, int& lanes, int& unroll, F run, float* best_ms = nullptr)
 {
     // Three rounds over all candidates, each candidate's time the minimum over the rounds: a
     // single timing per candidate let one slow measurement decide, and the chosen shapes then
@@ -1124,6 +1178,26 @@ int tune(fhg_ctx* ctx, int bs, int& lanes, int& unroll, F run)
             if (t[U - 1][gi] < best) { best = t[U - 1][gi]; bestG = 4 << gi; bestU = U; }
     lanes = bestG;
     unroll = bestU;
+    if (best_ms) *best_ms = best;
+    return FHG_OK;
+}
+
+// Time `run` like one candidate of tune: minimum over three rounds of eight launches.
+template <class F>
+int time_candidate(fhg_ctx* ctx, F run, float* ms_out)
+{
+    float best = 1e30f;
+    for (int round = 0; round < 3; round++) {
+        for (int w = 0; w < 2; w++) run();
+        CK(cudaEventRecord(ctx->ev0, ctx->stream));
+        for (int r = 0; r < 8; r++) run();
+        CK(cudaEventRecord(ctx->ev1, ctx->stream));
+        CK(cudaEventSynchronize(ctx->ev1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        best = std::min(best, ms);
+    }
+    *ms_out = best;
     return FHG_OK;
 }
 
@@ -1145,15 +1219,33 @@ int tune_level(fhg_ctx* ctx, int l)
     if (l < ctx->nlevels - 1) {
         Level& C = ctx->levels[l + 1];
         int g = A.lanes, gu = A.unroll;
+        // the row-major sweep's launch shape first, then (gs_layout auto) the slot-major sweep
+        // against it
+        const bool forced_slot = L.gs_slot;
+        L.gs_slot = false;
+        float row_ms = 0.f;
         if (V::gs(L).ell > 0) { g = V::gs(L).lanes; gu = 1; }
         rc = tune(ctx, bs, g, gu, [&](int G, int U) {
             BsrView<T> v = V::gs(L); v.lanes = G; v.unroll = U;
             for (int c = 0; c < L.ncolours; c++)
                 fhg::launch_gs<T>(v, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, V::b(L), V::x(L), s);
-        });
+        }, &row_ms);
         if (rc) return rc;
         L.gs_lanes = g;
         L.gs_unroll = gu;
+        L.gs_slot = forced_slot;
+        if constexpr (std::is_same<T, float>::value) {
+            if (!forced_slot && L.G32s.vals && ctx->opts.gs_layout == FHG_GS_AUTO) {
+                float slot_ms = 0.f;
+                rc = time_candidate(ctx, [&]() {
+                    for (int c = 0; c < L.ncolours; c++)
+                        fhg::launch_gs<float>(L.G32s.v, L.colour_start[c], L.colour_start[c + 1], L.dinv32, L.nb,
+                                              L.b32, L.x32, s);
+                }, &slot_ms);
+                if (rc) return rc;
+                L.gs_slot = slot_ms < row_ms;
+            }
+        }
         BsrView<T>& P = const_cast<BsrView<T>&>(V::P(L));
         BsrView<T>& R = const_cast<BsrView<T>&>(V::R(L));
         CK(cudaMemsetAsync(V::x(C), 0, sizeof(T) * C.n, s));
@@ -1194,6 +1286,8 @@ void reset_device_state(Level& L)
     L.R32 = DevBsr<float>();
     L.G32 = DevBsr<float>();
     L.A32p = DevBsr<float>();
+    L.G32s = DevBsr<float>();
+    L.gs_slot = false;
     L.Ahat_hi = DevBsr<float>();
     L.ahat_is_a = true;
     L.ahat_lo = nullptr;
@@ -1420,6 +1514,7 @@ void fhg_default_options(fhg_options* o)
     o->galerkin = 0;
     o->coarse_pre_iterations = -1;
     o->coarse_post_iterations = -1;
+    o->gs_layout = FHG_GS_AUTO;
 }
 
 int fhg_create(fhg_ctx** out, int device)
@@ -1514,6 +1609,8 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
     if (o.max_iterations < 0 || o.pre_iterations < 0 || o.post_iterations < 0 || o.coarse_pre_iterations < -1 ||
         o.coarse_post_iterations < -1)
         return fail(ctx, FHG_ERR_INVALID_ARG, "negative iteration count");
+    if (o.gs_layout < FHG_GS_AUTO || o.gs_layout > FHG_GS_SLOT)
+        return fail(ctx, FHG_ERR_INVALID_ARG, "unknown GS layout %d", o.gs_layout);
     if (o.pre_smoother < 0 || o.pre_smoother > 6 || o.post_smoother < 0 || o.post_smoother > 6)
         return fail(ctx, FHG_ERR_INVALID_ARG, "unknown smoother code");
     if (o.w_loops < 1 && o.w_loops != FHG_CYCLE_K) o.w_loops = 1;
@@ -1611,6 +1708,11 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         if (fp32 && l < nlevels - 1) {
             if (o.colouring && (rc = upload_padded(ctx, Ap, L.G32, true, 8))) return rc;
             if ((rc = upload_padded(ctx, Ap, L.A32p, false, 8))) return rc;
+            // slot-major GS view: when forced, or for the autotuner to compare
+            if (o.colouring && (o.gs_layout == FHG_GS_SLOT || (o.gs_layout == FHG_GS_AUTO && o.autotune)) &&
+                (rc = upload_offdiag_slot_major(ctx, Ap, L.colour_start, L.G32s)))
+                return rc;
+            L.gs_slot = o.gs_layout == FHG_GS_SLOT && L.G32s.vals;
         }
         if ((rc = upload(ctx, &L.perm_d, L.perm.data(), L.perm.size()))) return rc;
         if (l < nlevels - 1) {

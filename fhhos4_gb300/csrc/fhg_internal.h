@@ -25,6 +25,8 @@ struct BsrView {
     int ell = 0;          // > 0: padded rows of `ell` slots, slot s of row i at i * ell + s, empty
                           // slots with zero values and an in-range column, rowptr unused (accepted
                           // by launch_spmv, launch_gs and launch_residual_dinv; Jacobi needs rowptr)
+    int slot_major = 0;   // with ell > 0 (GS views only): slot s of row i of a colour [c0, c1) at
+                          // c0 * ell + s * (c1 - c0) + (i - c0), swept one thread per row
     const int* rowptr = nullptr;
     const int* colidx = nullptr;
     const T* vals = nullptr;

@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <type_traits>
 #include <utility>
 
 namespace fhg {
@@ -359,6 +360,61 @@ __global__ void __launch_bounds__(kThreads) k_bsr_gs(int row0, int row1, const i
                 }
             }
         }
+    }
+}
+
+// One colour of block GS on a slot-major padded view (slot_major, ell = W): one thread per block
+// row. Slot s of row i of the colour [row0, row1) lives at row0 * W + s * (row1 - row0) + (i - row0),
+// so a warp's loads of one slot are 32 consecutive words. The W column indices, then the used
+// slots' values and x entries are loaded before the sums, so all of a row's loads are in flight
+// together; no lane reduction follows. The column rules are those of k_bsr_gs (empty slots hold
+// the row's own column). ZERO: a zero-start sweep, whose skipped blocks are not loaded; other
+// sweeps load every slot and drop the diagonal ones by a select.
+template <class T, int BS, int W, bool ZERO>
+__global__ void __launch_bounds__(kThreads, 2) k_bsr_gs_slot(int row0, int row1, const int* __restrict__ colidx,
+                                                            const T* __restrict__ vals, long long ld,
+                                                            const T* __restrict__ dinv, long long dld,
+                                                            const T* __restrict__ b, T* x, int col_lo, int col_hi)
+{
+    pdl_wait();
+    const int row = row0 + (int)(blockIdx.x * kThreads + threadIdx.x);
+    if (row >= row1) return;
+    const long long nrc = row1 - row0;
+    const long long base = (long long)row0 * W + (row - row0);
+    int col[W];
+#pragma unroll
+    for (int s = 0; s < W; s++) col[s] = colidx[base + s * nrc];
+    T bv[BS], dv[BS * BS];
+#pragma unroll
+    for (int c = 0; c < BS; c++) bv[c] = b[(long long)row * BS + c];
+#pragma unroll
+    for (int e = 0; e < BS * BS; e++) dv[e] = dinv[(long long)e * dld + row];
+    T acc[BS];
+#pragma unroll
+    for (int r = 0; r < BS; r++) acc[r] = T(0);
+#pragma unroll
+    for (int s = 0; s < W; s++) {
+        const int j = col[s];
+        const bool use = j != row && (!ZERO || (j >= col_lo && j < col_hi));
+        if (ZERO && !use) continue;
+        const long long p = base + s * nrc;
+        T xv[BS];
+#pragma unroll
+        for (int c = 0; c < BS; c++) xv[c] = x[(long long)j * BS + c];
+#pragma unroll
+        for (int r = 0; r < BS; r++)
+#pragma unroll
+            for (int c = 0; c < BS; c++) {
+                const T a = vals[(long long)(r * BS + c) * ld + p];
+                acc[r] = fma(use ? a : T(0), xv[c], acc[r]);
+            }
+    }
+#pragma unroll
+    for (int r = 0; r < BS; r++) {
+        T v = T(0);
+#pragma unroll
+        for (int c = 0; c < BS; c++) v = fma(dv[r * BS + c], bv[c] - acc[c], v);
+        x[(long long)row * BS + r] = v;
     }
 }
 
@@ -1027,11 +1083,58 @@ void launch_residual_dinv(const BsrView<float>& A, const float* dinv, long long 
     g_kernel_launches++;
 }
 
+// Slot-major sweeps: dispatch on the block size and the slot count W (4..8).
+template <int BS, int W>
+void gs_slot_shape(const BsrView<float>& A, unsigned grid, int row0, int row1, const float* dinv, long long dld,
+                   const float* b, float* x, cudaStream_t s, int col_lo, int col_hi)
+{
+    if (col_lo > 0 || col_hi < 0x7fffffff)
+        pdl_launch(k_bsr_gs_slot<float, BS, W, true>, grid, kThreads, 0, s, row0, row1, A.colidx, A.vals, A.ld, dinv,
+                   dld, b, x, col_lo, col_hi);
+    else
+        pdl_launch(k_bsr_gs_slot<float, BS, W, false>, grid, kThreads, 0, s, row0, row1, A.colidx, A.vals, A.ld, dinv,
+                   dld, b, x, col_lo, col_hi);
+}
+
+template <int BS>
+void gs_slot_w(const BsrView<float>& A, unsigned grid, int row0, int row1, const float* dinv, long long dld,
+               const float* b, float* x, cudaStream_t s, int col_lo, int col_hi)
+{
+    switch (A.ell) {
+    case 4: gs_slot_shape<BS, 4>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
+    case 5: gs_slot_shape<BS, 5>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
+    case 6: gs_slot_shape<BS, 6>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
+    case 7: gs_slot_shape<BS, 7>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
+    case 8: gs_slot_shape<BS, 8>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
+    default: break;   // setup builds slot-major views for W in 4..8 only
+    }
+}
+
+void launch_gs_slot(const BsrView<float>& A, int row0, int row1, const float* dinv, long long dld, const float* b,
+                    float* x, cudaStream_t s, int col_lo, int col_hi)
+{
+    const unsigned grid = grid_for((long long)(row1 - row0), kThreads);
+    switch (A.bs) {
+    case 2: gs_slot_w<2>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
+    case 3: gs_slot_w<3>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
+    case 4: gs_slot_w<4>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
+    case 6: gs_slot_w<6>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
+    default: break;
+    }
+}
+
 template <class T>
 void launch_gs(const BsrView<T>& A, int row0, int row1, const T* dinv, long long dld, const T* b, T* x, cudaStream_t s,
                int col_lo, int col_hi)
 {
     if (row1 <= row0) return;
+    if constexpr (std::is_same<T, float>::value) {
+        if (A.slot_major) {
+            launch_gs_slot(A, row0, row1, dinv, dld, b, x, s, col_lo, col_hi);
+            g_kernel_launches++;
+            return;
+        }
+    }
     const unsigned grid = grid_for((long long)(row1 - row0) * A.lanes, kThreads);
     FHG_DISPATCH_BS_G(A.bs, A.lanes, {
         if (A.unroll == 2)

@@ -88,6 +88,7 @@ class Multigrid(IterativeSolver):
         # smoothing steps on levels >= 1; -1: PreSmoothingIterations / PostSmoothingIterations
         self.CoarsePreSmoothingIterations = -1
         self.CoarsePostSmoothingIterations = -1
+        self.GsLayout = "auto"   # FP32 GS sweeps: "auto", "row" or "slot" (padded rows)
         self._As: List[sp.csr_matrix] = []
         self._Ps: List[sp.csr_matrix] = []
         self._nLevels = nLevels
@@ -157,6 +158,7 @@ class _KrylovOnGpu(IterativeSolver):
         o.galerkin = 1 if mg.UseGalerkinOperator else 0
         o.coarse_pre_iterations = mg.CoarsePreSmoothingIterations
         o.coarse_post_iterations = mg.CoarsePostSmoothingIterations
+        o.gs_layout = N.GS_LAYOUT[mg.GsLayout]
         return o
 
     def Setup(self, A):
@@ -231,7 +233,7 @@ class ConjugateGradient(_KrylovOnGpu):
 def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: str = "bgs", post: str = "rbgs",
            precision: str = "fp64", krylov: str = "fcg", device: int = 0, autotune: bool = False,
            use_graphs: bool = True, outer_split: bool = True, cycle: str = "V", galerkin: bool = False,
-           nu=(1, 1), coarse_nu=(-1, -1)):
+           nu=(1, 1), coarse_nu=(-1, -1), gs_layout: str = "auto"):
     """SolverFactory-style construction of "-s fcgmg -cycle V,1,1" (src/Solver/SolverFactory.h:156-200)."""
     mg = Multigrid(len(As))
     mg.SetHierarchy(As, Ps)
@@ -244,6 +246,7 @@ def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: st
     mg.UseGalerkinOperator = galerkin
     mg.PreSmoothingIterations, mg.PostSmoothingIterations = nu
     mg.CoarsePreSmoothingIterations, mg.CoarsePostSmoothingIterations = coarse_nu
+    mg.GsLayout = gs_layout
     solver = FlexibleConjugateGradient(1) if krylov == "fcg" else ConjugateGradient()
     solver.Precond = SolverPreconditioner(mg)
     solver.Tolerance = tol

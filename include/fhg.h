@@ -66,6 +66,11 @@ extern "C" {
                                     up to FP32 summation order) */
 #define FHG_LEARNED_PARAMS 24848  /* FP32 parameters: W1 128x48, b1 128, W2 128x128, b2 128, W3 16x128, b3 16 */
 
+/* fhg_options.gs_layout */
+#define FHG_GS_AUTO 0
+#define FHG_GS_ROW 1
+#define FHG_GS_SLOT 2
+
 typedef struct fhg_ctx fhg_ctx;
 
 typedef struct {
@@ -98,6 +103,9 @@ typedef struct {
                                    default): pre_iterations, as the reference (one count for every level).
                                    No counterpart in the reference. */
     int coarse_post_iterations; /* the same after it; -1: post_iterations */
+    int gs_layout;              /* FP32 GS sweeps: FHG_GS_AUTO (the autotuner picks row- or slot-major padded
+                                   rows; row-major without autotuning), FHG_GS_ROW, FHG_GS_SLOT. Same
+                                   arithmetic, different storage order and launch shape. */
 } fhg_options;
 
 typedef struct {

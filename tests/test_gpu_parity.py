@@ -165,6 +165,19 @@ def test_fp32_vcycle_reaches_fp64_tolerance(case, outer_split):
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-6
 
 
+def test_slot_major_gs_solve_tracks_row_major(case):
+    """The FP32 fast cycle with slot-major GS sweeps: the same arithmetic as the row-major sweeps up
+    to FP32 summation order, so the same iterations within one and the FP64 tolerance."""
+    kw = dict(precision="fp32", nu=(3, 3), coarse_nu=(4, 4))
+    a = S().fcg_mg(case.As, case.Ps, case.bs, gs_layout="row", **kw)
+    a.Solve(case.b)
+    b = S().fcg_mg(case.As, case.Ps, case.bs, gs_layout="slot", **kw)
+    xb = b.Solve(case.b)
+    assert abs(a.IterationCount - b.IterationCount) <= 1
+    assert b.History[-1] < 1e-8
+    assert true_rel_residual(case.As[0], case.b, xb) < 5e-8
+
+
 def test_double_fp32_outer_product_tracks_fp64(case):
     # The double-FP32 outer product (FP64-class accuracy, ~1e-14 relative per product) changes
     # the FP32-V-cycle solve at the FP32 rounding level of the V-cycle only: same iteration count
@@ -242,12 +255,13 @@ def test_operators_of_every_level(case):
     assert np.linalg.norm(ys - O.spmv_sym_lower(A0, x)) <= 1e-13 * np.abs(A0).max() * np.linalg.norm(x) * 10
 
 
-def test_fp32_smoothers_of_every_level(case):
-    """FP32 GS sweeps (on the padded off-diagonal view where setup built one) and block Jacobi on
-    every smoothed level against the FP64 oracle in colour order, to FP32 accuracy."""
+@pytest.mark.parametrize("layout", ["row", "slot"])
+def test_fp32_smoothers_of_every_level(case, layout):
+    """FP32 GS sweeps (on the padded off-diagonal view where setup built one, row- or slot-major) and
+    block Jacobi on every smoothed level against the FP64 oracle in colour order, to FP32 accuracy."""
     torch = pytest.importorskip("torch")
     from fhhos4_gb300 import _native as N
-    solver = S().fcg_mg(case.As, case.Ps, case.bs, precision="fp32")
+    solver = S().fcg_mg(case.As, case.Ps, case.bs, precision="fp32", gs_layout=layout)
     ctx = solver.Context()
     rng = np.random.default_rng(11)
     for l in range(case.levels - 1):
