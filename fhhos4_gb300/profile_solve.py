@@ -26,6 +26,7 @@ def main():
     ap.add_argument("--coarse-nu", default="", help="pre,post smoothing steps on levels >= 1 (default: --nu)")
     ap.add_argument("--levels", type=int, default=0, help="use the first N levels (the last one solved directly)")
     ap.add_argument("--weights", default="", help="learned-step network (default: the committed one)")
+    ap.add_argument("--gs-layout", default="auto", choices=["auto", "row", "slot"], help="FP32 GS sweep layout")
     ap.add_argument("--step", choices=["", "learned_tcgen05", "learned_mma_sync", "gs_fp32", "outer_df"], default="")
     a = ap.parse_args()
 
@@ -49,6 +50,7 @@ def main():
     o = N.default_options()
     o.vcycle_precision = N.PRECISION["fp32"]
     o.autotune = a.autotune
+    o.gs_layout = N.GS_LAYOUT[a.gs_layout]
     ctx.setup(nlev, o)
     npre, npost = (int(v) for v in a.nu.split(","))
     params = LN.load_params(a.weights or LN.DEFAULT_WEIGHTS)[0]
