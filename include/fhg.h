@@ -32,7 +32,7 @@ extern "C" {
 #define FHG_ERR_NOT_SPD (-5)          /* coarsest factorisation failed (EigenSparseCholesky.h:27-33) */
 #define FHG_ERR_DIVERGED (-6)         /* inf residual: "divergence of the solver" (IterativeSolver.h:237-238) */
 #define FHG_ERR_NAN (-7)              /* NaN residual: "the residual is NaN." (IterativeSolver.h:239-240) */
-#define FHG_ERR_TOO_LARGE (-8)        /* a size beyond what this build supports */
+#define FHG_ERR_TOO_LARGE (-8)        /* a size beyond what the library supports */
 #define FHG_ERR_UNSUPPORTED (-9)
 
 /* Smoother codes, as SmootherFactory::Create (src/Solver/Multigrid/SmootherFactory.h:37-100). */
