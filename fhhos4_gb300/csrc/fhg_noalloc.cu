@@ -1,23 +1,24 @@
 // fhg_residual_norm_noalloc: the residual 2-norm ||b - A x|| of a face-block system, computed
 // without allocating anything.
 //
-// Who needs it: callers that cannot call cudaMalloc when they check a solution - code running
-// while a stream is being captured into a CUDA graph (allocation is not allowed there), callers
-// that own every byte of device memory through their own pool or a fixed budget, and embedders
-// that must not let a library grow their footprint after start-up. They pass the operator, x, b
-// and a one-double output buffer, all in memory they own; the per-block partial sums this
+// Who needs it: callers that may not allocate device memory when they check a solution - a
+// serving process that reserved all of the GPU's memory for its own pool or budget at start-up,
+// an embedder that must not let a library grow its footprint after start-up, and latency-bound
+// loops that cannot afford cudaMalloc's device-wide synchronisation. They pass the operator, x,
+// b and a one-double output buffer, all in memory they own; the per-block partial sums this
 // reduction needs live in a fixed array compiled into the library instead of a temporary
 // allocation.
 //
 // The scratch array `g_residual_partials` below (FHG_NOALLOC_MAX_PARTIALS doubles, 1 MiB) is a
 // file-scope __device__ array: every GPU that loads the library holds it until the process
 // exits. Host code cannot pass its name to a kernel (the name is a host-side stand-in, not a
-// device address), so the first call on each device looks its device address up with
-// cudaGetSymbolAddress while that device is current and caches it; make that first call before
-// any stream capture. All calls share the array: a call overwrites the partial sums it uses
-// (nothing accumulates across calls, so nothing needs clearing), and two calls that overlap on
-// the GPU - on different streams, or from different host threads at once - race on it and must
-// be serialised by the caller.
+// device address), so the first call on each device (and the first call after that device's
+// context was replaced, e.g. by cudaDeviceReset) looks its device address up with
+// cudaGetSymbolAddress while that device is current and caches it with the context's id; make
+// that first call before any stream capture. All calls share the array: a call overwrites the
+// partial sums it uses (nothing accumulates across calls, so nothing needs clearing), and two
+// calls that overlap on the GPU - on different streams, or from different host threads at once -
+// race on it and must be serialised by the caller.
 #include "fhg.h"
 
 #include <cuda_runtime.h>
@@ -114,15 +115,50 @@ __global__ void __launch_bounds__(kThreads) k_residual_norm_finalize(const doubl
 
 std::mutex g_setup_mutex;
 double* g_partials_ptr[kMaxDevices] = {nullptr};
+unsigned long long g_partials_ctx[kMaxDevices] = {0};
 
-// Device address of the scratch array on `device` (must be current): looked up once per device.
+// Id of the current context (0 when none or when the driver cannot say), through the driver entry
+// points the runtime hands out, so that the library needs no link against libcuda.
+unsigned long long current_context_id()
+{
+    using GetCurrent = int (*)(void**);
+    using GetId = int (*)(void*, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        looked_up = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (GetCurrent)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (GetId)f;
+    }
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
+// Device address of the scratch array on `device` (must be current): looked up on the first call
+// on a device and again whenever the device's current context differs from the one it was looked
+// up in (a context id of 0, unknown, always looks it up).
 int scratch_address(int device, double** ptr)
 {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_partials_ptr[device]) {
+    const unsigned long long ctx = current_context_id();
+    if (!g_partials_ptr[device] || ctx == 0 || ctx != g_partials_ctx[device]) {
         void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_residual_partials) != cudaSuccess || !p) return FHG_ERR_CUDA;
+        if (cudaGetSymbolAddress(&p, g_residual_partials) != cudaSuccess || !p) {
+            g_partials_ptr[device] = nullptr;
+            return FHG_ERR_CUDA;
+        }
         g_partials_ptr[device] = (double*)p;
+        g_partials_ctx[device] = current_context_id();
     }
     *ptr = g_partials_ptr[device];
     return FHG_OK;
@@ -156,8 +192,11 @@ extern "C" int fhg_residual_norm_noalloc(int device, int n_block_rows, int block
     int previous = 0;
     if (cudaGetDevice(&previous) != cudaSuccess) return FHG_ERR_CUDA;
     if (previous != device && cudaSetDevice(device) != cudaSuccess) return FHG_ERR_CUDA;
+    // An error left pending by the caller's earlier work is reported, not cleared, and nothing is
+    // launched; after the launches, cudaGetLastError sees this call's own launch errors only.
+    int rc = cudaPeekAtLastError() == cudaSuccess ? FHG_OK : FHG_ERR_CUDA;
     double* partials = nullptr;
-    int rc = scratch_address(device, &partials);
+    if (rc == FHG_OK) rc = scratch_address(device, &partials);
     if (rc == FHG_OK) {
         cudaStream_t s = (cudaStream_t)stream;
         const unsigned grid = (unsigned)ctas;

@@ -1,8 +1,9 @@
-"""fhg_residual_norm_noalloc, the entry point for callers that cannot allocate device memory
-(for instance while a stream is being captured into a CUDA graph, or when all device memory is
-owned by the caller's own pool): it computes ||b - A x|| with its partial sums in a fixed array
-inside the library. Checked through the C ABI against the residual of the existing entry point
-fhg_apply(FHG_OP_RESIDUAL), within the operator tests' tolerance, on two calls in a row.
+"""fhg_residual_norm_noalloc, the entry point for callers that may not allocate device memory
+(a process whose GPU memory is all reserved by its own pool or budget, an embedder that must not
+grow its footprint, a latency-bound loop that cannot afford cudaMalloc's synchronisation): it
+computes ||b - A x|| with its partial sums in a fixed array inside the library. Checked through
+the C ABI against the residual of the existing entry point fhg_apply(FHG_OP_RESIDUAL) and against
+the host FP64 residual norm, within the operator tests' tolerance, on two calls in a row.
 Collected last on purpose (file name), and self-contained so that it passes alone as well."""
 import ctypes as C
 import importlib
@@ -73,8 +74,10 @@ def test_residual_norm_without_allocation_matches_existing_entry_point():
         assert rc == N.FHG_OK
         torch.cuda.synchronize()
         values.append(float(out.item()))
+    host = float(np.linalg.norm(b - A @ x))   # host FP64 residual of the same system
     for v in values:
         assert abs(v - ref) <= 1e-12 * ref
+        assert abs(v - host) <= 1e-12 * host
     assert values[0] == values[1]
 
     # sizes beyond the scratch array are rejected before anything is launched
