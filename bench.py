@@ -184,16 +184,24 @@ def committed_traffic():
 
 
 # --------------------------------------------------------------------------- workload
-def workload_config(args):
+def workload_config(args, unknowns=None, levels=None):
+    """The workload, identical in both arms (the problem and the stopping test; the solver method
+    of each arm is reported beside it, not in it)."""
     coef = "identity tensor" if args.coefficient == "identity" else (
         f"{args.coefficient} coefficient (contrast {args.contrast:g})")
     name = (f"{'3D tet' if args.dim == 3 else '2D tri'} {args.n}^{args.dim} HHO k={args.k} diffusion, {coef}, "
-            f"f={'sine' if args.source == 'sine' else '1'}, FCG(1)+geometric MG V(1,1) bgs/rbgs, tol 1e-8")
-    return {"workload": name, "dim": args.dim, "n": args.n, "k": args.k, "mesh": "stetra" if args.dim == 3 else "stri",
-            "krylov": "FCG(1)", "cycle": "V(1,1)", "smoothers": "bgs/rbgs (multicolour order)",
-            "coarse": "FP64 dense inverse of the coarsest operator",
-            "coarse_operators": "Galerkin P^T A P (-g 1)" if args.galerkin else "rediscretised (the reference default)",
-            "l2": "inputs larger than L2 (fine operator alone is > 1 GB)"}
+            f"f={'sine' if args.source == 'sine' else '1'}, solved to 1e-8 FP64 relative residual")
+    cfg = {"workload": name, "dim": args.dim, "n": args.n, "k": args.k, "mesh": "stetra" if args.dim == 3 else "stri",
+           "coefficient": args.coefficient, "source": args.source, "tolerance": 1e-8,
+           "coarse_operators": "Galerkin P^T A P (-g 1)" if args.galerkin else "rediscretised (the reference default)",
+           "max_coarse_rows": args.max_coarse_rows,
+           "l2": "inputs larger than L2 (fine operator alone is > 1 GB)" if args.n >= 48 else
+                 "operators of every level together larger than L2"}
+    if unknowns is not None:
+        cfg["unknowns"] = int(unknowns)
+    if levels is not None:
+        cfg["levels"] = int(levels)
+    return cfg
 
 
 def generate(args, keep=False):
@@ -460,10 +468,12 @@ def run_ours(args, dist: Dist):
         "dtype": "f64 (Krylov) / f32 (V-cycle)",
         "data": (f"synthetic: the reference's own {args.n}^{args.dim} HHO system ({args.coefficient} coefficient), "
                  "generated on the host"),
-        "config": dict(workload_config(args), parallelism=f"replicas x{dist.world}",
-                       method=(("learned correction + " if head == "learned" else "") +
-                               f"FP32 V-cycle {results[head]['cycle']} inside FP64 FCG(1), double-FP32 outer product"),
-                       unknowns=n0, levels=len(As), colours_level0=ncol),
+        "config": workload_config(args, n0, len(As)),
+        "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU",
+        "method": {"name": ("learned correction + " if head == "learned" else "") + "FP32 V-cycle inside FP64 FCG(1)",
+                   "krylov": "FCG(1), double-FP32 outer product, FP64 x and Krylov scalars",
+                   "cycle": results[head]["cycle"], "vcycle_precision": "fp32",
+                   "coarsest": "FP64 dense inverse of the coarsest operator", "colours_level0": ncol},
         "plain_fp64": dict(results["plain"], reference_iterations_colour_order=ref_col,
                            reference_iterations_natural_order=ref_nat),
         "fp64_fast_cycle": results["fp64_fast"],
@@ -560,7 +570,11 @@ def run_reference(args, dist: Dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
         "data": (f"synthetic: the reference's own {args.n}^{args.dim} HHO system ({args.coefficient} coefficient), "
                  "generated on the host"),
-        "config": dict(workload_config(args), parallelism="host cores", unknowns=n0),
+        "config": workload_config(args, n0, len(As)),
+        "parallelism": f"{threads} host threads",
+        "method": {"name": "plain FP64 FCG(1) + V(1,1) bgs/rbgs (the reference's method, natural block-GS order)",
+                   "krylov": "FCG(1)", "cycle": "V(1,1) bgs/rbgs", "vcycle_precision": "fp64",
+                   "coarsest": "FP64 direct solve"},
         "cpu_baseline": {"value": round(value, 4), "unit": "s", "cores": threads, "kind": "port",
                          "sample": (f"{it} FCG(1)+V(1,1) iterations (one per step) of the {n0}-unknown solve by the "
                                     f"oracle restatement of the reference (natural block-GS order, OpenMP "
@@ -575,6 +589,11 @@ def main():
     args = parse()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.gpus != world:
+        # one process per GPU: N > 1 runs under torchrun (WORLD_SIZE = N), never N in one process
+        sys.exit(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world}; run N > 1 as "
+                 f"python -m torch.distributed.run --nproc-per-node {args.gpus} bench.py --gpus {args.gpus}")
     dist = Dist()
     try:
         if args.impl == "reference":

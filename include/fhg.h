@@ -10,7 +10,7 @@
  * Every function returns FHG_OK (0) or a negative FHG_ERR_* code; the message of
  * the last failure is available from fhg_last_error(). The reference reports
  * errors through Utils::FatalError (print + exit, src/Utils/Utils.h:258-264); the
- * C++ adapter shown in INTEGRATION.md maps a nonzero status to that call.
+ * C++ adapter include/fhg_reference_adapter.hpp maps a nonzero status to that call.
  *
  * Matrices are scalar CSR with 32-bit indices and columns ascending within a
  * row, i.e. exactly the arrays of the reference's row-major Eigen SparseMatrix
@@ -200,20 +200,24 @@ int fhg_get_permutation(const fhg_ctx* ctx, int level, int* perm);
 long long fhg_kernel_launches(const fhg_ctx* ctx);
 
 /* Residual 2-norm ||b - A x|| of a face-block system, computed without allocating any memory.
- * No counterpart in the reference: it exists for callers that cannot call cudaMalloc when they
- * check a solution (while capturing a stream into a CUDA graph, or when every byte of device
- * memory is owned by the caller's own pool or budget). The caller passes, in device memory it
- * owns: the operator in libfhg's block layout (rowptr[n_block_rows+1], block colidx, values
- * entry-major: entry r*bs+c of block p at vals[(r*bs+c)*ld + p], ld >= number of blocks), x, b
- * (n_block_rows*block_size doubles each) and norm_out (one double, written on `stream`; NULL =
- * the default stream). `lanes` (4, 8, 16, 32) is the number of lanes per block row.
+ * No counterpart in the reference: it exists for callers that may not allocate device memory
+ * when they check a solution - a process that reserved all of the GPU's memory for its own pool
+ * or budget at start-up, an embedder that must not let a library grow its footprint, or a
+ * latency-bound loop that cannot afford cudaMalloc's device-wide synchronisation. The caller
+ * passes, in device memory it owns: the operator in libfhg's block layout (rowptr[n_block_rows+1],
+ * block colidx, values entry-major: entry r*bs+c of block p at vals[(r*bs+c)*ld + p], ld >= number
+ * of blocks), x, b (n_block_rows*block_size doubles each) and norm_out (one double, written on
+ * `stream`; NULL = the default stream). `lanes` (4, 8, 16, 32) is the number of lanes per block row.
  * The per-block partial sums live in a fixed array inside the library, FHG_NOALLOC_MAX_PARTIALS
  * doubles (1 MiB) on every GPU that loads it, held until the process exits; one partial sum per
  * 256/lanes block rows, so n_block_rows may be at most FHG_NOALLOC_MAX_PARTIALS*256/lanes
  * (4,194,304 block rows at 8 lanes): larger sizes return FHG_ERR_TOO_LARGE and launch nothing.
- * The first call on a device looks up the array's device address on that device (make it before
- * any stream capture). Calls share the array: two calls that overlap on the GPU race on it.
- * Makes the device current for the call and restores the caller's current device. */
+ * The first call on a device (and the first after that device's context was replaced, e.g. by
+ * cudaDeviceReset) looks up the array's device address in the current context: make it before
+ * any stream capture. Calls share the array and leave their partial sums in it: two calls that
+ * overlap on the GPU race on it. A CUDA error left pending by earlier work is returned as
+ * FHG_ERR_CUDA before anything is launched and is not cleared. Makes the device current for the
+ * call and restores the caller's current device. */
 #define FHG_NOALLOC_MAX_PARTIALS 131072
 int fhg_residual_norm_noalloc(int device, int n_block_rows, int block_size, int lanes,
                               const int* rowptr, const int* colidx, const double* vals, long long ld,
