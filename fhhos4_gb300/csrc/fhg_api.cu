@@ -861,15 +861,18 @@ void smooth(fhg_ctx* ctx, int l, int code, int iters, const T* b, T* x, bool fro
     if (L.gs_lanes) { Ag.lanes = L.gs_lanes; Ag.unroll = L.gs_unroll; }
     BsrView<T> A = V::Acsr(L);  // Jacobi (row pointers and the diagonal blocks)
     if (L.gs_lanes && Ag.ell == 0) { A.lanes = L.gs_lanes; A.unroll = L.gs_unroll; }
+    // Multigrid::RelaxationParameter: the GS codes become block SOR when it is not 1
+    // (SmootherFactory.h:37-100, BlockSOR.h:199-227).
+    const T w = T(ctx->opts.omega);
     auto forward = [&](bool zero) {
         for (int c = 0; c < L.ncolours; c++)
             fhg::launch_gs<T>(Ag, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s, 0,
-                              zero ? L.colour_start[c + 1] : 0x7fffffff);
+                              zero ? L.colour_start[c + 1] : 0x7fffffff, w);
     };
     auto backward = [&](bool zero) {
         for (int c = L.ncolours - 1; c >= 0; c--)
             fhg::launch_gs<T>(Ag, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, b, x, s,
-                              zero ? L.colour_start[c] : 0, 0x7fffffff);
+                              zero ? L.colour_start[c] : 0, 0x7fffffff, w);
     };
     for (int it = 0; it < iters; it++) {
         const bool zero = from_zero && it == 0;
@@ -980,9 +983,10 @@ void mg_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
                                                                     : ctx->opts.pre_iterations;
     const int npost = l > 0 && ctx->opts.coarse_post_iterations >= 0 ? ctx->opts.coarse_post_iterations
                                                                       : ctx->opts.post_iterations;
-    // A zero-start GS sweep writes every entry before any is read: no clearing needed then.
+    // A zero-start GS sweep writes every entry before any is read: no clearing needed then (block
+    // SOR reads the old value of the entry it writes, so it starts from cleared x).
     const int pre = ctx->opts.pre_smoother;
-    const bool gs_zero = x_zero && is_gs(pre) && npre > 0;
+    const bool gs_zero = x_zero && is_gs(pre) && npre > 0 && ctx->opts.omega == 1.0;
     if (x_zero && !gs_zero) cudaMemsetAsync(x, 0, sizeof(T) * (size_t)L.n, s);
     smooth<T>(ctx, l, pre, npre, b, x, gs_zero);
     fhg::launch_spmv<T>(V::A(L), fhg::kSpmvResidual, x, b, V::r(L), s);

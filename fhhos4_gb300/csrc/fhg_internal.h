@@ -46,10 +46,11 @@ enum SpmvMode { kSpmvAssign = 0, kSpmvResidual = 1, kSpmvAddTo = 2 };
 template <class T>
 void launch_spmv(const BsrView<T>& A, int mode, const T* x, const T* aux, T* y, cudaStream_t s);
 // col_lo/col_hi: block columns outside [col_lo, col_hi) are skipped (zero-start sweeps).
-// A may be a padded (ell > 0) view of the off-diagonal blocks.
+// A may be a padded (ell > 0) view of the off-diagonal blocks. omega != 1: block SOR,
+// x_i <- omega D_i^-1 (b_i - sum_{j != i} A_ij x_j) + (1 - omega) x_i.
 template <class T>
 void launch_gs(const BsrView<T>& A, int row0, int row1, const T* dinv, long long dld,
-               const T* b, T* x, cudaStream_t s, int col_lo = 0, int col_hi = 0x7fffffff);
+               const T* b, T* x, cudaStream_t s, int col_lo = 0, int col_hi = 0x7fffffff, T omega = T(1));
 template <class T>
 void launch_jacobi(const BsrView<T>& A, const T* dinv, long long dld, T omega, const T* b,
                    const T* xold, T* xnew, cudaStream_t s);

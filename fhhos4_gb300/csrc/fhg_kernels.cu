@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(kThreads) k_bsr_gs(int row0, int row1, const i
                                                      const T* __restrict__ vals, long long ld,
                                                      const T* __restrict__ dinv, long long dld,
                                                      const T* __restrict__ b, T* x, int col_lo, int col_hi,
-                                                     int ell)
+                                                     int ell, T omega)
 {
     pdl_wait();
     const int lane = threadIdx.x & (G - 1);
@@ -344,7 +344,10 @@ __global__ void __launch_bounds__(kThreads) k_bsr_gs(int row0, int row1, const i
                 T v = T(0);
 #pragma unroll
                 for (int c = 0; c < BS; c++) v = fma(dv[c], bv[c] - acc[c], v);
-                x[(long long)row * BS + lane] = v;
+                const long long i = (long long)row * BS + lane;
+                // block SOR: x_i <- omega D_i^-1 (b_i - sum_{j != i} A_ij x_j) + (1 - omega) x_i
+                if (omega != T(1)) v = fma(omega, v, (T(1) - omega) * x[i]);
+                x[i] = v;
             }
         } else {
             T t[BS];
@@ -356,7 +359,9 @@ __global__ void __launch_bounds__(kThreads) k_bsr_gs(int row0, int row1, const i
                     T v = T(0);
 #pragma unroll
                     for (int c = 0; c < BS; c++) v = fma(dinv[(long long)(r * BS + c) * dld + row], t[c], v);
-                    x[(long long)row * BS + r] = v;
+                    const long long i = (long long)row * BS + r;
+                    if (omega != T(1)) v = fma(omega, v, (T(1) - omega) * x[i]);
+                    x[i] = v;
                 }
             }
         }
@@ -374,7 +379,8 @@ template <class T, int BS, int W, bool ZERO>
 __global__ void __launch_bounds__(kThreads, 2) k_bsr_gs_slot(int row0, int row1, const int* __restrict__ colidx,
                                                             const T* __restrict__ vals, long long ld,
                                                             const T* __restrict__ dinv, long long dld,
-                                                            const T* __restrict__ b, T* x, int col_lo, int col_hi)
+                                                            const T* __restrict__ b, T* x, int col_lo, int col_hi,
+                                                            T omega)
 {
     pdl_wait();
     const int row = row0 + (int)(blockIdx.x * kThreads + threadIdx.x);
@@ -414,7 +420,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_bsr_gs_slot(int row0, int row1,
         T v = T(0);
 #pragma unroll
         for (int c = 0; c < BS; c++) v = fma(dv[r * BS + c], bv[c] - acc[c], v);
-        x[(long long)row * BS + r] = v;
+        const long long i = (long long)row * BS + r;
+        if (omega != T(1)) v = fma(omega, v, (T(1) - omega) * x[i]);   // block SOR
+        x[i] = v;
     }
 }
 
@@ -1086,51 +1094,51 @@ void launch_residual_dinv(const BsrView<float>& A, const float* dinv, long long 
 // Slot-major sweeps: dispatch on the block size and the slot count W (4..8).
 template <int BS, int W>
 void gs_slot_shape(const BsrView<float>& A, unsigned grid, int row0, int row1, const float* dinv, long long dld,
-                   const float* b, float* x, cudaStream_t s, int col_lo, int col_hi)
+                   const float* b, float* x, cudaStream_t s, int col_lo, int col_hi, float omega)
 {
     if (col_lo > 0 || col_hi < 0x7fffffff)
         pdl_launch(k_bsr_gs_slot<float, BS, W, true>, grid, kThreads, 0, s, row0, row1, A.colidx, A.vals, A.ld, dinv,
-                   dld, b, x, col_lo, col_hi);
+                   dld, b, x, col_lo, col_hi, omega);
     else
         pdl_launch(k_bsr_gs_slot<float, BS, W, false>, grid, kThreads, 0, s, row0, row1, A.colidx, A.vals, A.ld, dinv,
-                   dld, b, x, col_lo, col_hi);
+                   dld, b, x, col_lo, col_hi, omega);
 }
 
 template <int BS>
 void gs_slot_w(const BsrView<float>& A, unsigned grid, int row0, int row1, const float* dinv, long long dld,
-               const float* b, float* x, cudaStream_t s, int col_lo, int col_hi)
+               const float* b, float* x, cudaStream_t s, int col_lo, int col_hi, float omega)
 {
     switch (A.ell) {
-    case 4: gs_slot_shape<BS, 4>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
-    case 5: gs_slot_shape<BS, 5>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
-    case 6: gs_slot_shape<BS, 6>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
-    case 7: gs_slot_shape<BS, 7>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
-    case 8: gs_slot_shape<BS, 8>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
+    case 4: gs_slot_shape<BS, 4>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi, omega); break;
+    case 5: gs_slot_shape<BS, 5>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi, omega); break;
+    case 6: gs_slot_shape<BS, 6>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi, omega); break;
+    case 7: gs_slot_shape<BS, 7>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi, omega); break;
+    case 8: gs_slot_shape<BS, 8>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi, omega); break;
     default: break;   // setup builds slot-major views for W in 4..8 only
     }
 }
 
 void launch_gs_slot(const BsrView<float>& A, int row0, int row1, const float* dinv, long long dld, const float* b,
-                    float* x, cudaStream_t s, int col_lo, int col_hi)
+                    float* x, cudaStream_t s, int col_lo, int col_hi, float omega)
 {
     const unsigned grid = grid_for((long long)(row1 - row0), kThreads);
     switch (A.bs) {
-    case 2: gs_slot_w<2>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
-    case 3: gs_slot_w<3>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
-    case 4: gs_slot_w<4>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
-    case 6: gs_slot_w<6>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi); break;
+    case 2: gs_slot_w<2>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi, omega); break;
+    case 3: gs_slot_w<3>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi, omega); break;
+    case 4: gs_slot_w<4>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi, omega); break;
+    case 6: gs_slot_w<6>(A, grid, row0, row1, dinv, dld, b, x, s, col_lo, col_hi, omega); break;
     default: break;
     }
 }
 
 template <class T>
 void launch_gs(const BsrView<T>& A, int row0, int row1, const T* dinv, long long dld, const T* b, T* x, cudaStream_t s,
-               int col_lo, int col_hi)
+               int col_lo, int col_hi, T omega)
 {
     if (row1 <= row0) return;
     if constexpr (std::is_same<T, float>::value) {
         if (A.slot_major) {
-            launch_gs_slot(A, row0, row1, dinv, dld, b, x, s, col_lo, col_hi);
+            launch_gs_slot(A, row0, row1, dinv, dld, b, x, s, col_lo, col_hi, omega);
             g_kernel_launches++;
             return;
         }
@@ -1139,10 +1147,10 @@ void launch_gs(const BsrView<T>& A, int row0, int row1, const T* dinv, long long
     FHG_DISPATCH_BS_G(A.bs, A.lanes, {
         if (A.unroll == 2)
             pdl_launch(k_bsr_gs<T, BS, G, 2>, grid, kThreads, 0, s, row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv,
-                       dld, b, x, col_lo, col_hi, A.ell);
+                       dld, b, x, col_lo, col_hi, A.ell, omega);
         else
             pdl_launch(k_bsr_gs<T, BS, G, 1>, grid, kThreads, 0, s, row0, row1, A.rowptr, A.colidx, A.vals, A.ld, dinv,
-                       dld, b, x, col_lo, col_hi, A.ell);
+                       dld, b, x, col_lo, col_hi, A.ell, omega);
     });
     g_kernel_launches++;
 }
@@ -1346,9 +1354,9 @@ void launch_permute(int nb, int bs, const int* perm, const T* in, T* out, bool g
 template void launch_spmv<double>(const BsrView<double>&, int, const double*, const double*, double*, cudaStream_t);
 template void launch_spmv<float>(const BsrView<float>&, int, const float*, const float*, float*, cudaStream_t);
 template void launch_gs<double>(const BsrView<double>&, int, int, const double*, long long, const double*, double*,
-                                cudaStream_t, int, int);
+                                cudaStream_t, int, int, double);
 template void launch_gs<float>(const BsrView<float>&, int, int, const float*, long long, const float*, float*,
-                               cudaStream_t, int, int);
+                               cudaStream_t, int, int, float);
 template void launch_jacobi<double>(const BsrView<double>&, const double*, long long, double, const double*,
                                     const double*, double*, cudaStream_t);
 template void launch_jacobi<float>(const BsrView<float>&, const float*, long long, float, const float*, const float*,

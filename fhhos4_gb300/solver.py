@@ -30,6 +30,23 @@ import scipy.sparse as sp
 from . import _native as N
 
 
+# Smoother codes that SmootherFactory::Create (src/Solver/Multigrid/SmootherFactory.h:37-100) maps to
+# the same smoother as a GPU code: the block SOR names are the Gauss-Seidel codes (block SOR when
+# RelaxationParameter != 1, block GS when it is 1), and the hybrid chunk-parallel sweeps "hbgs" /
+# "hrbgs" (BlockGaussSeidel.h:124-185, whose result depends on the host thread schedule) run as
+# the multicolour parallel sweeps.
+SMOOTHER_ALIASES = {"bsor": "bgs", "rbsor": "rbgs", "sbsor": "sbgs", "absor": "abgs", "rabsor": "rabgs",
+                    "hbgs": "bgs", "hrbgs": "rbgs"}
+
+
+def smoother_code(code: str) -> int:
+    """libfhg's code of a reference smoother code; NotImplementedError for the others."""
+    code = SMOOTHER_ALIASES.get(code, code)
+    if code not in N.SMOOTHERS:
+        raise NotImplementedError(f"smoother '{code}' (GPU smoothers: {sorted(N.SMOOTHERS) + sorted(SMOOTHER_ALIASES)})")
+    return N.SMOOTHERS[code]
+
+
 def as_eigen_csr(A) -> sp.csr_matrix:
     """Row-major CSR with int32 indices, sorted and duplicate-free (Eigen compressed form)."""
     A = sp.csr_matrix(A)
@@ -110,8 +127,7 @@ class Multigrid(IterativeSolver):
         if self.Cycle == "W" and self.WLoops < 2:
             self.WLoops = 2
         for code in (self.PreSmootherCode, self.PostSmootherCode):
-            if code not in N.SMOOTHERS:
-                raise NotImplementedError(f"smoother '{code}' (GPU smoothers: {sorted(N.SMOOTHERS)})")
+            smoother_code(code)
         if self.VCyclePrecision not in N.PRECISION:
             raise ValueError(f"unknown precision {self.VCyclePrecision}")
 
@@ -141,8 +157,8 @@ class _KrylovOnGpu(IterativeSolver):
     def _options(self, mg: Multigrid) -> N.Options:
         o = N.default_options()
         o.krylov = N.KRYLOV[self._krylov]
-        o.pre_smoother = N.SMOOTHERS[mg.PreSmootherCode]
-        o.post_smoother = N.SMOOTHERS[mg.PostSmootherCode]
+        o.pre_smoother = smoother_code(mg.PreSmootherCode)
+        o.post_smoother = smoother_code(mg.PostSmootherCode)
         o.pre_iterations = mg.PreSmoothingIterations
         o.post_iterations = mg.PostSmoothingIterations
         o.omega = mg.RelaxationParameter
@@ -233,7 +249,7 @@ class ConjugateGradient(_KrylovOnGpu):
 def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: str = "bgs", post: str = "rbgs",
            precision: str = "fp64", krylov: str = "fcg", device: int = 0, autotune: bool = False,
            use_graphs: bool = True, outer_split: bool = True, cycle: str = "V", galerkin: bool = False,
-           nu=(1, 1), coarse_nu=(-1, -1), gs_layout: str = "auto"):
+           nu=(1, 1), coarse_nu=(-1, -1), gs_layout: str = "auto", omega: float = 1.0):
     """SolverFactory-style construction of "-s fcgmg -cycle V,1,1" (src/Solver/SolverFactory.h:156-200)."""
     mg = Multigrid(len(As))
     mg.SetHierarchy(As, Ps)
@@ -247,6 +263,7 @@ def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: st
     mg.PreSmoothingIterations, mg.PostSmoothingIterations = nu
     mg.CoarsePreSmoothingIterations, mg.CoarsePostSmoothingIterations = coarse_nu
     mg.GsLayout = gs_layout
+    mg.RelaxationParameter = omega
     solver = FlexibleConjugateGradient(1) if krylov == "fcg" else ConjugateGradient()
     solver.Precond = SolverPreconditioner(mg)
     solver.Tolerance = tol

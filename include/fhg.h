@@ -43,6 +43,11 @@ extern "C" {
 #define FHG_SMOOTHER_SBGS 4   /* "sbgs": symmetric block Gauss-Seidel (forward then backward) */
 #define FHG_SMOOTHER_ABGS 5   /* "abgs": alternating block Gauss-Seidel, forward first */
 #define FHG_SMOOTHER_RABGS 6  /* "rabgs": alternating block Gauss-Seidel, backward first */
+/* Block SOR: SmootherFactory builds BlockSOR (src/Solver/FixedPoint/BlockSOR.h:99-227) for the GS codes
+ * and their aliases "bsor", "rbsor", "sbsor", "absor", "rabsor" whenever the relaxation parameter is
+ * not 1; here the GS codes do the same with fhg_options.omega. The hybrid codes "hbgs" / "hrbgs"
+ * (chunk-parallel sweeps whose result depends on the host thread schedule, BlockGaussSeidel.h:124-185)
+ * map to FHG_SMOOTHER_BGS / FHG_SMOOTHER_RBGS, this library's parallel (multicolour) sweeps. */
 
 /* Krylov codes: "fcg" = FlexibleConjugateGradient(1) (src/Solver/Krylov/FlexibleConjugateGradient.h:21-25),
  * "cg" = ConjugateGradient (src/Solver/Krylov/ConjugateGradient.h:6-104). */
@@ -79,7 +84,8 @@ typedef struct {
     int post_smoother;          /* FHG_SMOOTHER_* (reference default "rbgs", ProgramArguments.h:68) */
     int pre_iterations;         /* Multigrid::PreSmoothingIterations */
     int post_iterations;        /* Multigrid::PostSmoothingIterations */
-    double omega;               /* Multigrid::RelaxationParameter (used by "bj") */
+    double omega;               /* Multigrid::RelaxationParameter: "bj"'s relaxation and, when not 1, block SOR
+                                   in place of every Gauss-Seidel code (SmootherFactory.h:37-100) */
     double tolerance;           /* IterativeSolver::Tolerance on ||r||/||b|| */
     int max_iterations;         /* IterativeSolver::MaxIterations */
     int vcycle_precision;       /* FHG_PREC_* */

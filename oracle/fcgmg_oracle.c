@@ -206,29 +206,43 @@ static void blockdiag_free(orc_blockdiag* D)
     free(D->lu); free(D->rp); free(D->cp);
 }
 
-static void gs_row(const orc_csr* A, const orc_blockdiag* D, const double* b, double* x, int ib)
+/* One block row of block Gauss-Seidel (BlockGaussSeidel.h:193-223) or, for omega != 1, of block
+ * SOR (BlockSOR.h:199-227: x_i = D_i^-1 (omega b_i + (1 - omega) D_i x_i - omega sum_{j != i} A_ij x_j),
+ * the smoother SmootherFactory.h:37-100 builds for the GS codes when the relaxation parameter is
+ * not 1). */
+static void gs_row(const orc_csr* A, const orc_blockdiag* D, const double* b, double* x, int ib, double omega)
 {
     int bs = D->bs;
     double t[64];
     for (int k = 0; k < bs; k++) {
         int i = ib * bs + k;
-        double v = b[i];
-        for (int p = A->rowptr[i]; p < A->rowptr[i + 1]; p++) {
-            int j = A->colidx[p];
-            if (j / bs != ib) v -= A->vals[p] * x[j];
+        if (omega == 1.0) {
+            double v = b[i];
+            for (int p = A->rowptr[i]; p < A->rowptr[i + 1]; p++) {
+                int j = A->colidx[p];
+                if (j / bs != ib) v -= A->vals[p] * x[j];
+            }
+            t[k] = v;
+        } else {
+            double v = omega * b[i];
+            for (int p = A->rowptr[i]; p < A->rowptr[i + 1]; p++) {
+                int j = A->colidx[p];
+                if (j / bs == ib) v += (1 - omega) * A->vals[p] * x[j];
+                else v += -omega * A->vals[p] * x[j];
+            }
+            t[k] = v;
         }
-        t[k] = v;
     }
     lu_solve(D->lu + (size_t)ib * bs * bs, bs, D->rp + (size_t)ib * bs, D->cp + (size_t)ib * bs, t, x + (size_t)ib * bs);
 }
 
-static void gs_sweep(const orc_csr* A, const orc_blockdiag* D, const double* b, double* x, int backward)
+static void gs_sweep(const orc_csr* A, const orc_blockdiag* D, const double* b, double* x, int backward, double omega)
 {
     int nb = D->nb;
     if (!backward)
-        for (int ib = 0; ib < nb; ib++) gs_row(A, D, b, x, ib);
+        for (int ib = 0; ib < nb; ib++) gs_row(A, D, b, x, ib, omega);
     else
-        for (int ib = nb - 1; ib >= 0; ib--) gs_row(A, D, b, x, ib);
+        for (int ib = nb - 1; ib >= 0; ib--) gs_row(A, D, b, x, ib, omega);
 }
 
 static void jacobi_sweep(const orc_csr* A, const orc_blockdiag* D, double omega, const double* b, double* x, double* xnew)
@@ -254,7 +268,7 @@ static void jacobi_sweep(const orc_csr* A, const orc_blockdiag* D, double omega,
 void orc_block_gs(const orc_csr* A, int bs, const double* b, double* x, int backward)
 {
     orc_blockdiag D;
-    if (blockdiag_setup(&D, A, bs) == 0) gs_sweep(A, &D, b, x, backward);
+    if (blockdiag_setup(&D, A, bs) == 0) gs_sweep(A, &D, b, x, backward, 1.0);
     blockdiag_free(&D);
 }
 
@@ -390,17 +404,18 @@ typedef struct {
  * forward/backward by iteration parity (IterationCount restarts at 0 in every Solve). */
 static void smooth(orc_mg* mg, int l, int code, int iters, const double* b, double* x)
 {
+    const double w = mg->opt->sor_omega;
     for (int s = 0; s < iters; s++) {
         switch (code) {
         case ORC_BJ: jacobi_sweep(&mg->A[l], &mg->D[l], mg->opt->omega, b, x, mg->tmp[l]); break;
-        case ORC_BGS_FORWARD: gs_sweep(&mg->A[l], &mg->D[l], b, x, 0); break;
-        case ORC_BGS_BACKWARD: gs_sweep(&mg->A[l], &mg->D[l], b, x, 1); break;
+        case ORC_BGS_FORWARD: gs_sweep(&mg->A[l], &mg->D[l], b, x, 0, w); break;
+        case ORC_BGS_BACKWARD: gs_sweep(&mg->A[l], &mg->D[l], b, x, 1, w); break;
         case ORC_BGS_SYMMETRIC:
-            gs_sweep(&mg->A[l], &mg->D[l], b, x, 0);
-            gs_sweep(&mg->A[l], &mg->D[l], b, x, 1);
+            gs_sweep(&mg->A[l], &mg->D[l], b, x, 0, w);
+            gs_sweep(&mg->A[l], &mg->D[l], b, x, 1, w);
             break;
-        case ORC_BGS_ALTERNATING_FORWARD_FIRST: gs_sweep(&mg->A[l], &mg->D[l], b, x, s % 2); break;
-        default: gs_sweep(&mg->A[l], &mg->D[l], b, x, 1 - s % 2); break;
+        case ORC_BGS_ALTERNATING_FORWARD_FIRST: gs_sweep(&mg->A[l], &mg->D[l], b, x, s % 2, w); break;
+        default: gs_sweep(&mg->A[l], &mg->D[l], b, x, 1 - s % 2, w); break;
         }
     }
 }

@@ -37,6 +37,10 @@ typedef struct {
      * count for every level). An extension of the restatement with no counterpart in the
      * reference, mirroring fhg_options.coarse_pre_iterations / coarse_post_iterations. */
     int coarse_pre_iterations, coarse_post_iterations;
+    /* Relaxation parameter of the Gauss-Seidel codes: 1 = block Gauss-Seidel, otherwise block SOR
+     * (SmootherFactory.h:37-100 turns bgs/rbgs/sbgs/abgs/rabgs and their bsor aliases into BlockSOR
+     * when Multigrid::RelaxationParameter != 1; BlockSOR.h:199-227). */
+    double sor_omega;
 } orc_options;
 #define ORC_CYCLE_K (-1)
 
@@ -49,7 +53,8 @@ void orc_spmv_sym_lower(const orc_csr* A, const double* x, double* y);
 /* Transpose (values and sorted column indices) into caller buffers sized n_cols+1 / nnz. */
 void orc_transpose(const orc_csr* A, int* rowptr_t, int* colidx_t, double* vals_t);
 
-/* One block Gauss-Seidel sweep in place (BlockGaussSeidel.h:75-123,193-223). */
+/* One block Gauss-Seidel sweep in place (BlockGaussSeidel.h:75-123,193-223); orc_options.sor_omega
+ * selects block SOR inside the multigrid cycle. */
 void orc_block_gs(const orc_csr* A, int bs, const double* b, double* x, int backward);
 /* One block Jacobi sweep in place (BlockJacobi.h:77-127). */
 void orc_block_jacobi(const orc_csr* A, int bs, double omega, const double* b, double* x);

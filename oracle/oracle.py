@@ -23,6 +23,9 @@ KRYLOV_FCG, KRYLOV_CG = 0, 1
 SMOOTHER_CODES = {"bgs": (BGS_FORWARD, 1.0), "rbgs": (BGS_BACKWARD, 1.0),
                   "bj": (BJ, 1.0), "bj23": (BJ, 2.0 / 3.0), "sbgs": (SBGS, 1.0),
                   "abgs": (ABGS, 1.0), "rabgs": (RABGS, 1.0)}
+# SmootherFactory.h:37-100: the block SOR codes are the Gauss-Seidel ones (BlockSOR when the
+# relaxation parameter is not 1, BlockGaussSeidel when it is).
+SOR_ALIASES = {"bsor": "bgs", "rbsor": "rbgs", "sbsor": "sbgs", "absor": "abgs", "rabsor": "rabgs"}
 
 
 class _CSR(C.Structure):
@@ -35,7 +38,7 @@ class _Opts(C.Structure):
     _fields_ = [("pre_smoother", C.c_int), ("post_smoother", C.c_int), ("omega", C.c_double),
                 ("pre_iterations", C.c_int), ("post_iterations", C.c_int), ("krylov", C.c_int),
                 ("tolerance", C.c_double), ("max_iterations", C.c_int), ("w_loops", C.c_int),
-                ("coarse_pre_iterations", C.c_int), ("coarse_post_iterations", C.c_int)]
+                ("coarse_pre_iterations", C.c_int), ("coarse_post_iterations", C.c_int), ("sor_omega", C.c_double)]
 
 
 _lib = None
@@ -152,19 +155,25 @@ def last_timing():
 
 
 def fcgmg_solve(As, Ps, b, bs, pre="bgs", post="rbgs", krylov="fcg", tol=1e-8, maxit=200,
-                pre_iterations=1, post_iterations=1, cycle="V", coarse_iterations=(-1, -1)):
+                pre_iterations=1, post_iterations=1, cycle="V", coarse_iterations=(-1, -1), omega=1.0):
     """Returns (x, history, iterations, status). coarse_iterations: smoothing steps on levels >= 1
-    (-1: those of level 0, the reference's behaviour)."""
+    (-1: those of level 0, the reference's behaviour). omega: Multigrid::RelaxationParameter, the
+    relaxation of "bj" and, when not 1, block SOR in place of the Gauss-Seidel codes
+    (SmootherFactory.h:37-100); "bj23" keeps 2/3."""
     keep: list = []
     nl = len(As)
     Aarr = (_CSR * nl)(*[_wrap(as_csr(A), keep) for A in As])
     Parr = (_CSR * max(nl - 1, 1))(*([_wrap(as_csr(P), keep) for P in Ps] or [_CSR()]))
+    pre, post = SOR_ALIASES.get(pre, pre), SOR_ALIASES.get(post, post)
     pc, om = SMOOTHER_CODES[pre]
     qc, om2 = SMOOTHER_CODES[post]
-    opts = _Opts(pc, qc, om if pc == BJ else om2, pre_iterations, post_iterations,
+    jac = om if pc == BJ else om2
+    if (pre == "bj" or post == "bj") and "bj23" not in (pre, post):
+        jac = omega
+    opts = _Opts(pc, qc, jac, pre_iterations, post_iterations,
                  KRYLOV_CG if krylov == "cg" else KRYLOV_FCG, tol, maxit,
                  2 if cycle == "W" else (-1 if cycle == "K" else 1), int(coarse_iterations[0]),
-                 int(coarse_iterations[1]))
+                 int(coarse_iterations[1]), float(omega))
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.zeros(As[0].shape[0])
     hist = np.zeros(maxit + 1)

@@ -12,7 +12,7 @@
 //         residual history captured through IterativeSolver::OnIterationEnd
 //         (src/Solver/IterativeSolver.h:224-227) and the solution x.
 //
-//   solve <dir> [--smoothers pre,post] [--krylov fcg|cg] [--cycle V|W] [--tol t] [--maxit m]
+//   solve <dir> [--smoothers pre,post] [--krylov fcg|cg] [--cycle V|W|K] [--tol t] [--maxit m] [--omega w]
 //         Reads a hierarchy (possibly re-ordered by the caller) from <dir>, feeds it
 //         to the reference's own Multigrid / BlockGaussSeidel / EigenSparseCholesky /
 //         FlexibleConjugateGradient classes through a Level subclass that only
@@ -281,7 +281,7 @@ protected:
 	Level* CreateCoarseLevel(Level* fineLevel, CoarseningType, int) override { return levels[fineLevel->Number + 1]; }
 };
 
-static int RunSolve(const std::string& dir, const std::string& pre, const std::string& post, const std::string& krylov, double tol, int maxit, char cycle)
+static int RunSolve(const std::string& dir, const std::string& pre, const std::string& post, const std::string& krylov, double tol, int maxit, char cycle, double omega)
 {
 	auto meta = ReadArray<int>(dir + "/levels.i32"); // [nLevels, blockSize]
 	int nLevels = meta[0], bs = meta[1];
@@ -306,7 +306,8 @@ static int RunSolve(const std::string& dir, const std::string& pre, const std::s
 	mg->PreSmoothingIterations = 1;
 	mg->PostSmoothingIterations = 1;
 	mg->BlockSizeForBlockSmoothers = bs;
-	mg->RelaxationParameter = 1;
+	// "-w": Multigrid::RelaxationParameter (bj, and block SOR for the GS codes when != 1)
+	mg->RelaxationParameter = omega;
 	mg->H_CS = H_CoarsStgy::StandardCoarsening;
 	mg->CoarseSolver = new EigenSparseCholesky();
 
@@ -353,7 +354,7 @@ int main(int argc, char** argv)
 	std::string mode = argv[1];
 	std::string pre = "bgs", post = "rbgs", krylov = "fcg";
 	char cycle = 'V';
-	double tol = 1e-8;
+	double tol = 1e-8, omega = 1.0;
 	int maxit = 200;
 	bool solve = true;
 	std::vector<std::string> pos;
@@ -363,6 +364,7 @@ int main(int argc, char** argv)
 		if (a == "--smoothers" && i + 1 < argc) ParseSmoothers(argv[++i], pre, post);
 		else if (a == "--krylov" && i + 1 < argc) krylov = argv[++i];
 		else if (a == "--tol" && i + 1 < argc) tol = atof(argv[++i]);
+		else if (a == "--omega" && i + 1 < argc) omega = atof(argv[++i]);
 		else if (a == "--maxit" && i + 1 < argc) maxit = atoi(argv[++i]);
 		else if (a == "--no-solve") solve = false;
 		else if (a == "--cycle" && i + 1 < argc) cycle = argv[++i][0];
@@ -377,7 +379,7 @@ int main(int argc, char** argv)
 		else rc = RunGen<3>(n, k, pos[3], pre, post, solve);
 	}
 	else if (mode == "solve" && pos.size() == 1)
-		rc = RunSolve(pos[0], pre, post, krylov, tol, maxit, cycle);
+		rc = RunSolve(pos[0], pre, post, krylov, tol, maxit, cycle, omega);
 	else
 		fprintf(stderr, "bad arguments\n");
 	std::cout.clear();

@@ -15,7 +15,9 @@ checkout by ``make -C oracle ref``) and stores, per case, in a compressed .npz:
 
 Only ``hist_*`` summaries are kept for the large cases (``--histories-only``).
 
-Usage:  python tests/golden/make_golden.py [case ...] [--histories-only | --add-k-cycle]
+``--add-sor`` adds the reference's block SOR (bsor/rbsor and sbsor, omega 1.2) to full cases.
+
+Usage:  python tests/golden/make_golden.py [case ...] [--histories-only | --add-k-cycle | --add-sor]
 """
 from __future__ import annotations
 
@@ -77,7 +79,7 @@ def ref_gen(dim, n, k, out):
     return meta, As, Ps, b, np.fromfile(f"{out}/history.f64"), np.fromfile(f"{out}/x.f64")
 
 
-def ref_solve(As, Ps, b, bs, work, smoothers="bgs,rbgs", krylov="fcg", cycle="V"):
+def ref_solve(As, Ps, b, bs, work, smoothers="bgs,rbgs", krylov="fcg", cycle="V", omega=1.0):
     os.makedirs(work, exist_ok=True)
     np.asarray([len(As), bs], dtype=np.int32).tofile(f"{work}/levels.i32")
     for l, A in enumerate(As):
@@ -85,8 +87,8 @@ def ref_solve(As, Ps, b, bs, work, smoothers="bgs,rbgs", krylov="fcg", cycle="V"
     for l, P in enumerate(Ps):
         dump_csr(f"{work}/L{l}_P", P)
     np.asarray(b, dtype=np.float64).tofile(f"{work}/b.f64")
-    subprocess.run([O.REF_DRIVER, "solve", work, "--smoothers", smoothers, "--krylov", krylov, "--cycle", cycle],
-                   check=True)
+    subprocess.run([O.REF_DRIVER, "solve", work, "--smoothers", smoothers, "--krylov", krylov, "--cycle", cycle,
+                    "--omega", repr(float(omega))], check=True)
     return np.fromfile(f"{work}/out_history.f64"), np.fromfile(f"{work}/out_x.f64")
 
 
@@ -134,6 +136,38 @@ def make_case(name, dim, n, k, histories_only=False):
               f"size={os.path.getsize(path)/1e6:.2f} MB", flush=True)
 
 
+# Block SOR fixtures: the reference's BlockSOR (BlockSOR.h:99-227) through the bsor/rbsor and
+# sbsor codes with relaxation parameter SOR_OMEGA, on the colour-permuted hierarchy.
+SOR_OMEGA = 1.2
+
+
+def _load_full(name):
+    path = os.path.join(GOLDEN, name + ".npz")
+    with np.load(path) as z:
+        data = {k: z[k] for k in z.files}
+    nl = int(data["levels"])
+    bs = int(data["block_size"])
+    As = [sp.csr_matrix((data[f"A{l}_data"], data[f"A{l}_indices"], data[f"A{l}_indptr"])) for l in range(nl)]
+    Ps = [sp.csr_matrix((data[f"P{l}_data"], data[f"P{l}_indices"], data[f"P{l}_indptr"]),
+                        shape=tuple(data[f"P{l}_shape"])) for l in range(nl - 1)]
+    perms = [data[f"perm{l}"] for l in range(nl)]
+    Ac, Pc, bc = O.permute_hierarchy(As, Ps, data["b"], bs, perms)
+    return path, data, bs, Ac, Pc, bc
+
+
+def add_sor(name):
+    """Add block SOR (bsor/rbsor and sbsor, omega = SOR_OMEGA) of the reference on the stored
+    colour-permuted hierarchy of a full case: hist_sor, x_sor, hist_ssor, x_ssor."""
+    path, data, bs, Ac, Pc, bc = _load_full(name)
+    with tempfile.TemporaryDirectory() as tmp:
+        hist_sor, x_sor = ref_solve(Ac, Pc, bc, bs, os.path.join(tmp, "sor"), smoothers="bsor,rbsor", omega=SOR_OMEGA)
+        hist_ssor, x_ssor = ref_solve(Ac, Pc, bc, bs, os.path.join(tmp, "ssor"), smoothers="sbsor,sbsor",
+                                      omega=SOR_OMEGA)
+    data.update(hist_sor=hist_sor, x_sor=x_sor, hist_ssor=hist_ssor, x_ssor=x_ssor, sor_omega=SOR_OMEGA)
+    np.savez_compressed(path, **data)
+    print(f"{name}: block SOR iterations {len(hist_sor) - 1}, symmetric {len(hist_ssor) - 1}", flush=True)
+
+
 def add_k_cycle(name):
     """Add the reference's K-cycle (FCG(1) + K,1,1, bgs/rbgs; Multigrid.h:523-537,611-656) on the
     stored colour-permuted hierarchy of a full case: hist_k, x_k."""
@@ -154,20 +188,25 @@ def add_k_cycle(name):
     print(f"{name}: K-cycle iterations {len(hist_k) - 1}", flush=True)
 
 
+def build_ref_driver():
+    """The reference harness, compiled from the read-only reference checkout (FHHOS4_REFERENCE)."""
+    ref = os.environ.get("FHHOS4_REFERENCE", "/root/reference")
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_ROOT={ref}"], check=True)
+
+
 def main(argv):
     histories_only = "--histories-only" in argv
-    if "--add-k-cycle" in argv:
-        if not os.path.exists(O.REF_DRIVER):
-            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
-        for name in [a for a in argv if not a.startswith("--")] or list(CASES):
-            add_k_cycle(name)
-        return
+    for flag, fn in (("--add-k-cycle", add_k_cycle), ("--add-sor", add_sor)):
+        if flag in argv:
+            build_ref_driver()
+            for name in [a for a in argv if not a.startswith("--")] or list(CASES):
+                fn(name)
+            return
     names = [a for a in argv if not a.startswith("--")]
     table = dict(CASES, **LARGE)
     if not names:
         names = list(CASES)
-    if not os.path.exists(O.REF_DRIVER):
-        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+    build_ref_driver()
     for name in names:
         dim, n, k = table[name]
         make_case(name, dim, n, k, histories_only or name in LARGE)

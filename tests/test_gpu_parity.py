@@ -106,6 +106,35 @@ def test_cycles_and_smoothers_match_reference(case, variant, pre, post, cycle):
     assert np.linalg.norm(x[sp_] - xr) / np.linalg.norm(xr) < X_RTOL
 
 
+@pytest.mark.parametrize("variant,pre,post", [("sor", "bsor", "rbsor"), ("ssor", "sbsor", "sbsor")])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_block_sor_matches_reference(case, variant, pre, post, precision):
+    """Block SOR, relaxation 1.2 (BlockSOR.h:99-227): FP64 at the reference's bar; the FP32 V-cycle
+    reaches the FP64 tolerance with the FP64 true residual."""
+    omega = float(case["sor_omega"])
+    solver = S().fcg_mg(case.As, case.Ps, case.bs, pre=pre, post=post, omega=omega, precision=precision)
+    x = solver.Solve(case.b)
+    ref = case[f"hist_{variant}"]
+    if precision == "fp32":
+        assert solver.History[-1] < 1e-8 and true_rel_residual(case.As[0], case.b, x) < 1e-8 * (1 + 1e-6)
+        assert solver.IterationCount <= len(ref) - 1 + 3
+        return
+    assert solver.IterationCount == len(ref) - 1
+    assert hist_close(solver.History, ref)
+    sp_ = scalar_perm(case.perms[0], case.bs)
+    xr = case[f"x_{variant}"]
+    assert np.linalg.norm(x[sp_] - xr) / np.linalg.norm(xr) < X_RTOL
+
+
+def test_hybrid_codes_run_the_parallel_sweeps(case):
+    """"hbgs"/"hrbgs" (the reference's chunk-parallel sweeps, schedule-dependent) run as the
+    multicolour sweeps: the same solve as bgs/rbgs."""
+    a = S().fcg_mg(case.As, case.Ps, case.bs, pre="hbgs", post="hrbgs")
+    b = S().fcg_mg(case.As, case.Ps, case.bs)
+    xa, xb = a.Solve(case.b), b.Solve(case.b)
+    assert a.IterationCount == b.IterationCount and np.array_equal(xa, xb)
+
+
 @pytest.mark.parametrize("nu,coarse_nu", [((1, 1), (2, 2)), ((2, 2), (4, 3))])
 def test_coarse_smoothing_counts_match_the_oracle(case, nu, coarse_nu):
     """Smoothing counts per level (levels >= 1 apart from level 0; no counterpart in the reference)

@@ -35,7 +35,10 @@ def test_unsupported_configurations_fail_loudly():
     with pytest.raises(NotImplementedError):
         mg._check_supported()
     mg.Cycle = "V"
-    mg.PreSmootherCode = "hbgs"
+    for code in ("hbgs", "hrbgs", "bsor", "rbsor", "sbsor", "absor", "rabsor"):
+        mg.PreSmootherCode = code       # aliases of the GPU Gauss-Seidel codes
+        mg._check_supported()
+    mg.PreSmootherCode = "gs"           # point (scalar) Gauss-Seidel: block size 1 only
     with pytest.raises(NotImplementedError):
         mg._check_supported()
     fcg = S.FlexibleConjugateGradient()

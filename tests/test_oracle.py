@@ -65,6 +65,19 @@ def test_colour_order_histories_match_reference(case, variant, smoothers, krylov
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < X_RTOL
 
 
+@pytest.mark.parametrize("variant,smoothers", [("sor", ("bsor", "rbsor")), ("ssor", ("sbsor", "sbsor"))])
+def test_block_sor_matches_reference(case, variant, smoothers):
+    """Block SOR (BlockSOR.h:99-227, relaxation 1.2) in colour order against the reference run."""
+    Ac, Pc, bc = O.permute_hierarchy(case.As, case.Ps, case.b, case.bs, case.perms)
+    x, hist, it, rc = O.fcgmg_solve(Ac, Pc, bc, case.bs, pre=smoothers[0], post=smoothers[1],
+                                    omega=float(case["sor_omega"]))
+    ref = case[f"hist_{variant}"]
+    assert rc == 0 and it == len(ref) - 1
+    assert hist_close(hist, ref), (hist, ref)
+    xr = case[f"x_{variant}"]
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < X_RTOL
+
+
 def check_bj23_history(hist, ref):
     """Block Jacobi with omega = 2/3 makes the V-cycle indefinite on these operators (the first
     FCG residual grows above 1), and FCG(1) then amplifies rounding differences by about 3x per
