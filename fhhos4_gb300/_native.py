@@ -26,7 +26,7 @@ FHG_ERR_UNSUPPORTED = -9
 
 SMOOTHERS = {"bgs": 0, "rbgs": 1, "bj": 2, "bj23": 3, "sbgs": 4, "abgs": 5, "rabgs": 6}
 KRYLOV = {"fcg": 0, "cg": 1}
-PRECISION = {"fp64": 0, "fp32": 1}
+PRECISION = {"fp64": 0, "fp32": 1, "df": 2}   # df: FP64-class V-cycle in FP32 pairs (FHG_PREC_DF)
 
 OP_SPMV, OP_RESIDUAL, OP_RESTRICT, OP_PROLONG_ADD = 0, 1, 2, 3
 OP_GS_FORWARD, OP_GS_BACKWARD, OP_JACOBI, OP_SYM_SPMV = 4, 5, 6, 7
@@ -63,7 +63,7 @@ class Options(C.Structure):
                 ("colouring", C.c_int), ("use_graphs", C.c_int), ("autotune", C.c_int),
                 ("max_coarse_rows", C.c_int), ("outer_split", C.c_int), ("w_loops", C.c_int),
                 ("galerkin", C.c_int), ("coarse_pre_iterations", C.c_int), ("coarse_post_iterations", C.c_int),
-                ("gs_layout", C.c_int)]
+                ("gs_layout", C.c_int), ("extra_precisions", C.c_int)]
 
 
 class SolveInfo(C.Structure):

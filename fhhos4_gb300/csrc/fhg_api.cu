@@ -24,6 +24,7 @@
 #include <vector>
 
 using fhg::BsrView;
+using fhg::dfl;
 
 namespace {
 
@@ -59,8 +60,13 @@ struct Level {
     HostCsr A_in, P_in;
     bool A_is_galerkin = false;    // A_in was computed as R A P by a setup with galerkin = 1
     int ncolours = 0;
-    int gs_lanes = 0;              // lanes per block row of the GS/Jacobi sweeps (0: those of A)
-    int gs_unroll = 1;             // blocks per lane step of the GS sweeps
+    // Launch shape of the GS/Jacobi sweeps per value type (index FHG_PREC_FP64 / FP32 / DF):
+    // lanes per block row (0: those of A), blocks per lane step, and whether the sweeps use the
+    // slot-major view (setup: gs_layout or the autotuner).
+    int gs_lanes[3] = {0, 0, 0};
+    int gs_unroll[3] = {1, 1, 1};
+    bool gs_slot[3] = {false, false, false};
+    bool prod_slot[3] = {false, false, false};  // products with A use the slot-major view
     int outer_lanes = 0;           // level 0: lanes of the FP64 outer product (0: those of its view)
     std::vector<int> colour_start;  // block-row offsets of every colour, ncolours + 1
     std::vector<int> perm;          // new block row -> given block row
@@ -70,7 +76,12 @@ struct Level {
     DevBsr<float> G32;          // FP32 GS operator: A's off-diagonal blocks in padded rows, when they fit
     DevBsr<float> A32p;         // FP32 A in padded rows (all blocks), when they fit
     DevBsr<float> G32s;         // the GS view slot-major per colour (one thread per row), when built
-    bool gs_slot = false;       // the GS sweeps use G32s (setup: gs_layout or the autotuner)
+    DevBsr<float> A32s;         // FP32 A slot-major (all blocks, one thread per row), when built
+    // FP32-pair copies (FHG_PREC_DF: FP64-class V-cycle on the FP32 pipe), same views as FP32
+    DevBsr<dfl> A2, P2, R2, G2, A2p, G2s, A2s;
+    dfl* dinv2 = nullptr;
+    dfl *x2 = nullptr, *b2 = nullptr, *r2 = nullptr;
+    dfl* kv2[4] = {nullptr, nullptr, nullptr, nullptr};
     DevBsr<float> Ahat_hi;      // level 0, FP32 V-cycle: outer operator as an FP32 pair (hi part)
     float* ahat_lo = nullptr;   // (lo part, same layout)
     double* dinv = nullptr;
@@ -107,6 +118,7 @@ struct fhg_ctx {
     // whose high part is the V-cycle input b32; d and Ad live as FP32 pairs in kz[p] and kAd[p]
     // (hi: n floats, then lo); x stays FP64 in kx.
     float* rlo = nullptr;
+    float* rhi = nullptr;        // the high part of r when the V-cycle is not FP32 (pair V-cycle)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     long long graph_kernels[2] = {0, 0};
     int graphs_built = 0;
@@ -636,9 +648,10 @@ int upload_bsr(fhg_ctx* ctx, const HostBsr& B, DevBsr<T>& D, const DevBsr<double
 // when W <= max_w and the padding adds at most half to the stored blocks (about 1% for the
 // operators of a 64^3 tetrahedral mesh, more on small meshes whose faces near the boundary have
 // fewer neighbours); otherwise D stays empty and the kernels use the CSR form.
-int upload_padded(fhg_ctx* ctx, const HostBsr& B, DevBsr<float>& D, bool offdiag, int max_w)
+template <class T>
+int upload_padded(fhg_ctx* ctx, const HostBsr& B, DevBsr<T>& D, bool offdiag, int max_w)
 {
-    D = DevBsr<float>();
+    D = DevBsr<T>();
     int W = 0;
     long long kept = 0;
     for (int i = 0; i < B.nbr; i++) {
@@ -652,14 +665,14 @@ int upload_padded(fhg_ctx* ctx, const HostBsr& B, DevBsr<float>& D, bool offdiag
     const int bb = B.bs * B.bs;
     const long long ld = round_up(slots, 32);
     std::vector<int> col((size_t)slots);
-    std::vector<float> soa((size_t)ld * bb, 0.f);
+    std::vector<T> soa((size_t)ld * bb, T(0));
     for (int i = 0; i < B.nbr; i++) {
         long long q = (long long)i * W;
         int last = 0;
         for (int p = B.rowptr[i]; p < B.rowptr[i + 1]; p++) {
             if (offdiag && B.colidx[p] == i) continue;
             col[(size_t)q] = last = B.colidx[p];
-            for (int e = 0; e < bb; e++) soa[(size_t)e * ld + q] = (float)B.vals[(size_t)p * bb + e];
+            for (int e = 0; e < bb; e++) soa[(size_t)e * ld + q] = (T)B.vals[(size_t)p * bb + e];
             q++;
         }
         for (; q < (long long)(i + 1) * W; q++) col[(size_t)q] = offdiag ? i : last;
@@ -678,10 +691,11 @@ int upload_padded(fhg_ctx* ctx, const HostBsr& B, DevBsr<float>& D, bool offdiag
 // sweep with one thread per row reads each slot of 32 consecutive rows as 32 consecutive words.
 // Empty slots hold the row's own column and zero values, as in upload_padded. Built only when W
 // is in 4..8 and the padding adds at most half; otherwise D stays empty.
+template <class T>
 int upload_offdiag_slot_major(fhg_ctx* ctx, const HostBsr& B, const std::vector<int>& colour_start,
-                              DevBsr<float>& D)
+                              DevBsr<T>& D)
 {
-    D = DevBsr<float>();
+    D = DevBsr<T>();
     int W = 0;
     long long kept = 0;
     for (int i = 0; i < B.nbr; i++) {
@@ -696,7 +710,7 @@ int upload_offdiag_slot_major(fhg_ctx* ctx, const HostBsr& B, const std::vector<
     const int bb = B.bs * B.bs;
     const long long ld = round_up(slots, 32);
     std::vector<int> col((size_t)slots);
-    std::vector<float> soa((size_t)ld * bb, 0.f);
+    std::vector<T> soa((size_t)ld * bb, T(0));
     for (size_t c = 0; c + 1 < colour_start.size(); c++) {
         const long long c0 = colour_start[c], nrc = colour_start[c + 1] - c0;
         for (long long i = c0; i < c0 + nrc; i++) {
@@ -705,11 +719,47 @@ int upload_offdiag_slot_major(fhg_ctx* ctx, const HostBsr& B, const std::vector<
                 if (B.colidx[p] == i) continue;
                 const long long q = c0 * W + k * nrc + (i - c0);
                 col[(size_t)q] = B.colidx[p];
-                for (int e = 0; e < bb; e++) soa[(size_t)e * ld + q] = (float)B.vals[(size_t)p * bb + e];
+                for (int e = 0; e < bb; e++) soa[(size_t)e * ld + q] = (T)B.vals[(size_t)p * bb + e];
                 k++;
             }
             for (; k < W; k++) col[(size_t)(c0 * W + k * nrc + (i - c0))] = (int)i;
         }
+    }
+    int rc;
+    if ((rc = upload(ctx, &D.colidx, col.data(), col.size()))) return rc;
+    if ((rc = upload(ctx, &D.vals, soa.data(), soa.size()))) return rc;
+    D.v.nbr = B.nbr; D.v.nbc = B.nbc; D.v.bs = B.bs; D.v.nnzb = slots; D.v.ld = ld; D.v.ell = W;
+    D.v.slot_major = 1;
+    D.v.rowptr = nullptr; D.v.colidx = D.colidx; D.v.vals = D.vals;
+    D.v.lanes = 1;
+    return FHG_OK;
+}
+
+// All of a block operator slot-major, for products (one thread per row): slot k of row i at
+// k * nbr + i (W = the most blocks of a row, 5..8), columns ascending; empty slots hold zero values
+// and the row's last stored column (an exact zero added). Built only when W is in 5..8 and the
+// padding adds at most half; otherwise D stays empty.
+template <class T>
+int upload_slot_major_all(fhg_ctx* ctx, const HostBsr& B, DevBsr<T>& D)
+{
+    D = DevBsr<T>();
+    int W = 0;
+    for (int i = 0; i < B.nbr; i++) W = std::max(W, B.rowptr[i + 1] - B.rowptr[i]);
+    const long long kept = B.nnzb();
+    const long long slots = (long long)B.nbr * W;
+    if (W < 5 || W > 8 || slots > kept + kept / 2 || slots > INT32_MAX) return FHG_OK;
+    const int bb = B.bs * B.bs;
+    const long long ld = round_up(slots, 32);
+    std::vector<int> col((size_t)slots);
+    std::vector<T> soa((size_t)ld * bb, T(0));
+    for (int i = 0; i < B.nbr; i++) {
+        int k = 0, last = i;
+        for (int p = B.rowptr[i]; p < B.rowptr[i + 1]; p++, k++) {
+            const long long q = (long long)k * B.nbr + i;
+            col[(size_t)q] = last = B.colidx[p];
+            for (int e = 0; e < bb; e++) soa[(size_t)e * ld + q] = (T)B.vals[(size_t)p * bb + e];
+        }
+        for (; k < W; k++) col[(size_t)((long long)k * B.nbr + i)] = last;
     }
     int rc;
     if ((rc = upload(ctx, &D.colidx, col.data(), col.size()))) return rc;
@@ -817,6 +867,7 @@ int upload_tensor_features(fhg_ctx* ctx)
 
 template <class T> struct LevelVecs;
 template <> struct LevelVecs<double> {
+    static constexpr int kPrec = FHG_PREC_FP64;
     static double* x(Level& L) { return L.x; }
     static double* b(Level& L) { return L.b; }
     static double* r(Level& L) { return L.r; }
@@ -829,24 +880,51 @@ template <> struct LevelVecs<double> {
     static const BsrView<double>& Acsr(Level& L) { return L.A.v; }
 };
 template <> struct LevelVecs<float> {
+    static constexpr int kPrec = FHG_PREC_FP32;
     static float* x(Level& L) { return L.x32; }
     static float* b(Level& L) { return L.b32; }
     static float* r(Level& L) { return L.r32; }
-    // products with A: the padded view when setup built one
-    static const BsrView<float>& A(Level& L) { return L.A32p.vals ? L.A32p.v : L.A32.v; }
+    // products with A: the slot-major or the row-major padded view when setup built one
+    static const BsrView<float>& A(Level& L)
+    {
+        if (L.prod_slot[kPrec] && L.A32s.vals) return L.A32s.v;
+        return L.A32p.vals ? L.A32p.v : L.A32.v;
+    }
     // P stays CSR: at 64^3 its rows of up to 7 blocks pad by 29%, which costs what the saved
     // row-pointer load gains (0.180 ms either way)
     static const BsrView<float>& P(Level& L) { return L.P32.v; }
     static const BsrView<float>& R(Level& L) { return L.R32.v; }
     static const float* dinv(Level& L) { return L.dinv32; }
     static float* k(Level& L, int i) { return L.kv32[i]; }
-    // GS sweeps: the padded off-diagonal view when setup built one
+    // GS sweeps: the slot-major or padded off-diagonal view when setup built one
     static const BsrView<float>& gs(Level& L)
     {
-        if (L.gs_slot && L.G32s.vals) return L.G32s.v;
+        if (L.gs_slot[kPrec] && L.G32s.vals) return L.G32s.v;
         return L.G32.vals ? L.G32.v : L.A32.v;
     }
     static const BsrView<float>& Acsr(Level& L) { return L.A32.v; }   // Jacobi: row pointers
+};
+// FP32 pairs: the FP32 V-cycle's views with 8-byte pair values (FP64-class arithmetic on the FP32 pipe).
+template <> struct LevelVecs<dfl> {
+    static constexpr int kPrec = FHG_PREC_DF;
+    static dfl* x(Level& L) { return L.x2; }
+    static dfl* b(Level& L) { return L.b2; }
+    static dfl* r(Level& L) { return L.r2; }
+    static const BsrView<dfl>& A(Level& L)
+    {
+        if (L.prod_slot[kPrec] && L.A2s.vals) return L.A2s.v;
+        return L.A2p.vals ? L.A2p.v : L.A2.v;
+    }
+    static const BsrView<dfl>& P(Level& L) { return L.P2.v; }
+    static const BsrView<dfl>& R(Level& L) { return L.R2.v; }
+    static const dfl* dinv(Level& L) { return L.dinv2; }
+    static dfl* k(Level& L, int i) { return L.kv2[i]; }
+    static const BsrView<dfl>& gs(Level& L)
+    {
+        if (L.gs_slot[kPrec] && L.G2s.vals) return L.G2s.v;
+        return L.G2.vals ? L.G2.v : L.A2.v;
+    }
+    static const BsrView<dfl>& Acsr(Level& L) { return L.A2.v; }
 };
 
 // `from_zero`: x holds zeros on entry (the pre-smoothing of a V-cycle), so the first GS sweep
@@ -857,10 +935,11 @@ void smooth(fhg_ctx* ctx, int l, int code, int iters, const T* b, T* x, bool fro
     Level& L = ctx->levels[l];
     using V = LevelVecs<T>;
     cudaStream_t s = ctx->stream;
+    constexpr int P = V::kPrec;
     BsrView<T> Ag = V::gs(L);   // GS sweeps (tuned shape)
-    if (L.gs_lanes) { Ag.lanes = L.gs_lanes; Ag.unroll = L.gs_unroll; }
+    if (L.gs_lanes[P]) { Ag.lanes = L.gs_lanes[P]; Ag.unroll = L.gs_unroll[P]; }
     BsrView<T> A = V::Acsr(L);  // Jacobi (row pointers and the diagonal blocks)
-    if (L.gs_lanes && Ag.ell == 0) { A.lanes = L.gs_lanes; A.unroll = L.gs_unroll; }
+    if (L.gs_lanes[P] && Ag.ell == 0) { A.lanes = L.gs_lanes[P]; A.unroll = L.gs_unroll[P]; }
     // Multigrid::RelaxationParameter: the GS codes become block SOR when it is not 1
     // (SmootherFactory.h:37-100, BlockSOR.h:199-227).
     const T w = T(ctx->opts.omega);
@@ -1018,6 +1097,10 @@ void precondition(fhg_ctx* ctx, const double* r, double* z)
         fhg::launch_convert<double, float>(L.n, r, L.b32, ctx->stream);
         vcycle<float>(ctx, 0, L.b32, L.x32);
         fhg::launch_convert<float, double>(L.n, L.x32, z, ctx->stream);
+    } else if (ctx->opts.vcycle_precision == FHG_PREC_DF) {
+        fhg::launch_convert<double, dfl>(L.n, r, L.b2, ctx->stream);
+        vcycle<dfl>(ctx, 0, L.b2, L.x2);
+        fhg::launch_convert<dfl, double>(L.n, L.x2, z, ctx->stream);
     } else {
         vcycle<double>(ctx, 0, r, z);
     }
@@ -1025,21 +1108,35 @@ void precondition(fhg_ctx* ctx, const double* r, double* z)
 
 double* part(fhg_ctx* ctx, int i) { return ctx->partials + (size_t)i * fhg::kReduceCtas; }
 
-// The outer iteration runs on FP32 pairs (double-FP32 outer product built at setup).
+// The outer iteration runs on FP32 pairs (double-FP32 outer product built at setup): with the FP32
+// V-cycle, and with the pair V-cycle.
 bool outer_df(const fhg_ctx* ctx)
 {
-    return ctx->opts.vcycle_precision == FHG_PREC_FP32 && ctx->opts.krylov == FHG_KRYLOV_FCG &&
+    const int p = ctx->opts.vcycle_precision;
+    return (p == FHG_PREC_FP32 || (p == FHG_PREC_DF && ctx->rhi)) && ctx->opts.krylov == FHG_KRYLOV_FCG &&
            ctx->levels[0].ahat_lo && ctx->rlo;
+}
+
+// High part of the outer residual pair: the FP32 V-cycle reads it as its right-hand side.
+float* outer_rh(fhg_ctx* ctx)
+{
+    return ctx->opts.vcycle_precision == FHG_PREC_DF ? ctx->rhi : ctx->levels[0].b32;
+}
+
+// The pair V-cycle's right-hand side (interleaved pairs of r), written with the outer residual.
+dfl* outer_r2(fhg_ctx* ctx)
+{
+    return ctx->opts.vcycle_precision == FHG_PREC_DF ? ctx->levels[0].b2 : nullptr;
 }
 
 // FP32 pair views of an n-long FP64 buffer (hi: first n floats, lo: next n).
 float* pair_hi(double* v) { return reinterpret_cast<float*>(v); }
 float* pair_lo(double* v, long long n) { return reinterpret_cast<float*>(v) + n; }
 
-// Start of a double-FP32 outer iteration: (b32, rlo) = r.
+// Start of a double-FP32 outer iteration: (rh, rlo) = r, and r as pairs for a pair V-cycle.
 void outer_df_start(fhg_ctx* ctx, const double* r)
 {
-    fhg::launch_split_df(ctx->levels[0].n, r, ctx->levels[0].b32, ctx->rlo, ctx->stream);
+    fhg::launch_split_df(ctx->levels[0].n, r, outer_rh(ctx), ctx->rlo, ctx->stream, outer_r2(ctx));
 }
 
 // One FCG(1) iteration (src/Solver/Krylov/FlexibleConjugateGradient.h:80-162), parity p
@@ -1055,15 +1152,25 @@ void fcg_iteration(fhg_ctx* ctx, int p)
     Level& L0 = ctx->levels[0];
     const bool fp32 = ctx->opts.vcycle_precision == FHG_PREC_FP32;
     if (outer_df(ctx)) {
-        // FP32 pairs for r, d, Ad: z = M r_hi (FP32 V-cycle), d = z - s dp, Ad = Â d, r -= alpha Ad
-        // with no FP64 instruction per element; x += alpha d in FP64.
-        vcycle<float>(ctx, 0, L0.b32, L0.x32);
+        // FP32 pairs for r, d, Ad: z = M r (FP32 V-cycle on r_hi, or the pair V-cycle on r),
+        // d = z - s dp, Ad = Â d, r -= alpha Ad with no FP64 instruction per element; x += alpha d in FP64.
+        const bool pv = ctx->opts.vcycle_precision == FHG_PREC_DF;
+        float* rh = outer_rh(ctx);
+        const float* z32 = nullptr;
+        const dfl* z2 = nullptr;
+        if (pv) {
+            vcycle<dfl>(ctx, 0, L0.b2, L0.x2);
+            z2 = L0.x2;
+        } else {
+            vcycle<float>(ctx, 0, L0.b32, L0.x32);
+            z32 = L0.x32;
+        }
         float *dh = pair_hi(z), *dl = pair_lo(z, n), *Adh = pair_hi(Ad), *Adl = pair_lo(Ad, n);
-        fhg::launch_dot_df(n, L0.x32, pair_hi(Adp), pair_lo(Adp, n), part(ctx, 0), s);
-        fhg::launch_fcg_direction_df(n, L0.x32, pair_hi(dp), pair_lo(dp, n), part(ctx, 0), ctx->scal + 1, dh, dl, s);
-        fhg::launch_spmv_dots_df(L0.Ahat_hi.v, L0.ahat_lo, dh, dl, L0.b32, ctx->rlo, Adh, Adl, part(ctx, 1), s);
-        fhg::launch_krylov_step_df(n, ctx->kx, L0.b32, ctx->rlo, dh, dl, Adh, Adl, part(ctx, 2),
-                                   part(ctx, 1), ctx->scal + 1, part(ctx, 3), s);
+        fhg::launch_dot_df(n, z32, pair_hi(Adp), pair_lo(Adp, n), part(ctx, 0), s, z2);
+        fhg::launch_fcg_direction_df(n, z32, pair_hi(dp), pair_lo(dp, n), part(ctx, 0), ctx->scal + 1, dh, dl, s, z2);
+        fhg::launch_spmv_dots_df(L0.Ahat_hi.v, L0.ahat_lo, dh, dl, rh, ctx->rlo, Adh, Adl, part(ctx, 1), s);
+        fhg::launch_krylov_step_df(n, ctx->kx, rh, ctx->rlo, dh, dl, Adh, Adl, part(ctx, 2), part(ctx, 1),
+                                   ctx->scal + 1, part(ctx, 3), s, outer_r2(ctx));
         fhg::launch_finalize_norm(part(ctx, 3), ctx->scal + 0, ctx->scal + 2, ctx->hist_d, ctx->counter_d,
                                   ctx->opts.max_iterations + 1, s);
         if (!ctx->device_loop) cudaMemcpyAsync(ctx->nr_host, ctx->scal + 2, sizeof(double), cudaMemcpyDeviceToHost, s);
@@ -1211,22 +1318,41 @@ int tune_level(fhg_ctx* ctx, int l)
     using V = LevelVecs<T>;
     Level& L = ctx->levels[l];
     cudaStream_t s = ctx->stream;
-    BsrView<T>& A = const_cast<BsrView<T>&>(V::A(L));
-    const int bs = A.bs;
+    const int bs = L.bs;
     CK(cudaMemsetAsync(V::x(L), 0, sizeof(T) * L.n, s));
     CK(cudaMemsetAsync(V::b(L), 0, sizeof(T) * L.n, s));
+    // Products with A: the row-major view's launch shape, then (layout auto) the slot-major view
+    // against it.
+    const bool forced_prod_slot = L.prod_slot[V::kPrec];
+    L.prod_slot[V::kPrec] = false;
+    BsrView<T>& A = const_cast<BsrView<T>&>(V::A(L));
+    float row_prod_ms = 0.f;
     int rc = tune(ctx, bs, A.lanes, A.unroll, [&](int G, int U) {
         BsrView<T> v = A; v.lanes = G; v.unroll = U;
         fhg::launch_spmv<T>(v, fhg::kSpmvResidual, V::x(L), V::b(L), V::r(L), s);
-    });
+    }, &row_prod_ms);
     if (rc) return rc;
+    L.prod_slot[V::kPrec] = forced_prod_slot;
+    if constexpr (!std::is_same<T, double>::value) {
+        const BsrView<T>* slot = nullptr;
+        if constexpr (std::is_same<T, float>::value) slot = L.A32s.vals ? &L.A32s.v : nullptr;
+        else slot = L.A2s.vals ? &L.A2s.v : nullptr;
+        if (!forced_prod_slot && slot && ctx->opts.gs_layout == FHG_GS_AUTO) {
+            float slot_ms = 0.f;
+            rc = time_candidate(ctx, [&]() { fhg::launch_spmv<T>(*slot, fhg::kSpmvResidual, V::x(L), V::b(L), V::r(L), s); },
+                                &slot_ms);
+            if (rc) return rc;
+            L.prod_slot[V::kPrec] = slot_ms < row_prod_ms;
+        }
+    }
     if (l < ctx->nlevels - 1) {
         Level& C = ctx->levels[l + 1];
         int g = A.lanes, gu = A.unroll;
         // the row-major sweep's launch shape first, then (gs_layout auto) the slot-major sweep
         // against it
-        const bool forced_slot = L.gs_slot;
-        L.gs_slot = false;
+        constexpr int PR = V::kPrec;
+        const bool forced_slot = L.gs_slot[PR];
+        L.gs_slot[PR] = false;
         float row_ms = 0.f;
         if (V::gs(L).ell > 0) { g = V::gs(L).lanes; gu = 1; }
         rc = tune(ctx, bs, g, gu, [&](int G, int U) {
@@ -1235,19 +1361,22 @@ int tune_level(fhg_ctx* ctx, int l)
                 fhg::launch_gs<T>(v, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb, V::b(L), V::x(L), s);
         }, &row_ms);
         if (rc) return rc;
-        L.gs_lanes = g;
-        L.gs_unroll = gu;
-        L.gs_slot = forced_slot;
-        if constexpr (std::is_same<T, float>::value) {
-            if (!forced_slot && L.G32s.vals && ctx->opts.gs_layout == FHG_GS_AUTO) {
+        L.gs_lanes[PR] = g;
+        L.gs_unroll[PR] = gu;
+        L.gs_slot[PR] = forced_slot;
+        if constexpr (!std::is_same<T, double>::value) {
+            const BsrView<T>* slot = nullptr;
+            if constexpr (std::is_same<T, float>::value) slot = L.G32s.vals ? &L.G32s.v : nullptr;
+            else slot = L.G2s.vals ? &L.G2s.v : nullptr;
+            if (!forced_slot && slot && ctx->opts.gs_layout == FHG_GS_AUTO) {
                 float slot_ms = 0.f;
                 rc = time_candidate(ctx, [&]() {
                     for (int c = 0; c < L.ncolours; c++)
-                        fhg::launch_gs<float>(L.G32s.v, L.colour_start[c], L.colour_start[c + 1], L.dinv32, L.nb,
-                                              L.b32, L.x32, s);
+                        fhg::launch_gs<T>(*slot, L.colour_start[c], L.colour_start[c + 1], V::dinv(L), L.nb,
+                                          V::b(L), V::x(L), s);
                 }, &slot_ms);
                 if (rc) return rc;
-                L.gs_slot = slot_ms < row_ms;
+                L.gs_slot[PR] = slot_ms < row_ms;
             }
         }
         BsrView<T>& P = const_cast<BsrView<T>&>(V::P(L));
@@ -1291,7 +1420,17 @@ void reset_device_state(Level& L)
     L.G32 = DevBsr<float>();
     L.A32p = DevBsr<float>();
     L.G32s = DevBsr<float>();
-    L.gs_slot = false;
+    L.A32s = DevBsr<float>();
+    L.A2 = DevBsr<dfl>();
+    L.P2 = DevBsr<dfl>();
+    L.R2 = DevBsr<dfl>();
+    L.G2 = DevBsr<dfl>();
+    L.A2p = DevBsr<dfl>();
+    L.G2s = DevBsr<dfl>();
+    L.A2s = DevBsr<dfl>();
+    L.dinv2 = nullptr;
+    L.x2 = L.b2 = L.r2 = nullptr;
+    for (int i = 0; i < 3; i++) { L.gs_slot[i] = false; L.prod_slot[i] = false; L.gs_lanes[i] = 0; L.gs_unroll[i] = 1; }
     L.Ahat_hi = DevBsr<float>();
     L.ahat_is_a = true;
     L.ahat_lo = nullptr;
@@ -1300,10 +1439,8 @@ void reset_device_state(Level& L)
     L.perm_d = nullptr;
     L.x = L.b = L.r = nullptr;
     L.x32 = L.b32 = L.r32 = nullptr;
-    for (int i = 0; i < 4; i++) { L.kv64[i] = nullptr; L.kv32[i] = nullptr; }
+    for (int i = 0; i < 4; i++) { L.kv64[i] = nullptr; L.kv32[i] = nullptr; L.kv2[i] = nullptr; }
     L.cinv = nullptr;
-    L.gs_lanes = 0;
-    L.gs_unroll = 1;
     L.outer_lanes = 0;
 }
 
@@ -1313,6 +1450,7 @@ void free_all(fhg_ctx* ctx)
     for (Level& L : ctx->levels) reset_device_state(L);
     ctx->nbr_d = nullptr; ctx->tfeat_d = nullptr; ctx->lw = nullptr; ctx->lstatus = nullptr;
     ctx->rlo = nullptr;
+    ctx->rhi = nullptr;
     ctx->lparams = nullptr; ctx->lwts = nullptr; ctx->lbias = nullptr;
     ctx->learned_mode = FHG_LEARNED_OFF;
     ctx->learned_now = false;
@@ -1436,8 +1574,10 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
             replacements++;
             CK(cudaMemcpyAsync(ctx->kr, ctx->kt, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
             CK(cudaMemcpyAsync(ctx->scal + 2, &true_rel, sizeof(double), cudaMemcpyHostToDevice, s));
-            if (outer_df(ctx)) fhg::launch_split_df(n, ctx->kr, L0.b32, ctx->rlo, s);
-            else fhg::launch_convert<double, float>(n, ctx->kr, L0.b32, s);
+            // the V-cycle's right-hand side: the FP32 pair of r, or r in FP32 (the FP64 and pair
+            // V-cycles without the split outer iteration read r itself)
+            if (outer_df(ctx)) outer_df_start(ctx, ctx->kr);
+            else if (fp32) fhg::launch_convert<double, float>(n, ctx->kr, L0.b32, s);
             CK(cudaStreamSynchronize(s));
             nr = true_rel;
             continue;
@@ -1519,6 +1659,7 @@ void fhg_default_options(fhg_options* o)
     o->coarse_pre_iterations = -1;
     o->coarse_post_iterations = -1;
     o->gs_layout = FHG_GS_AUTO;
+    o->extra_precisions = 0;
 }
 
 int fhg_create(fhg_ctx** out, int device)
@@ -1667,7 +1808,11 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
     if (LC.n > o.max_coarse_rows)
         return fail(ctx, FHG_ERR_TOO_LARGE, "coarsest level has %d rows, above the dense direct-solve limit %d", LC.n,
                     o.max_coarse_rows);
-    const bool fp32 = o.vcycle_precision == FHG_PREC_FP32;
+    if (o.vcycle_precision < FHG_PREC_FP64 || o.vcycle_precision > FHG_PREC_DF)
+        return fail(ctx, FHG_ERR_INVALID_ARG, "unknown V-cycle precision %d", o.vcycle_precision);
+    // Operator copies: FP64 always; FP32 and FP32 pairs for the V-cycle precision and the extra ones.
+    const bool fp32 = o.vcycle_precision == FHG_PREC_FP32 || (o.extra_precisions & (1 << FHG_PREC_FP32));
+    const bool pair = o.vcycle_precision == FHG_PREC_DF || (o.extra_precisions & (1 << FHG_PREC_DF));
     int rc;
 
     // Block structure, colouring and permutation of every level.
@@ -1709,14 +1854,24 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         Ab[l] = HostBsr();
         if ((rc = upload_bsr<double>(ctx, Ap, L.A, nullptr))) return rc;
         if (fp32 && (rc = upload_bsr<float>(ctx, Ap, L.A32, &L.A))) return rc;
+        if (pair && (rc = upload_bsr<dfl>(ctx, Ap, L.A2, &L.A))) return rc;
+        // slot-major views (GS sweeps and products): when forced, or for the autotuner to compare
+        const bool want_slot = o.colouring && (o.gs_layout == FHG_GS_SLOT || (o.gs_layout == FHG_GS_AUTO && o.autotune));
         if (fp32 && l < nlevels - 1) {
             if (o.colouring && (rc = upload_padded(ctx, Ap, L.G32, true, 8))) return rc;
             if ((rc = upload_padded(ctx, Ap, L.A32p, false, 8))) return rc;
-            // slot-major GS view: when forced, or for the autotuner to compare
-            if (o.colouring && (o.gs_layout == FHG_GS_SLOT || (o.gs_layout == FHG_GS_AUTO && o.autotune)) &&
-                (rc = upload_offdiag_slot_major(ctx, Ap, L.colour_start, L.G32s)))
-                return rc;
-            L.gs_slot = o.gs_layout == FHG_GS_SLOT && L.G32s.vals;
+            if (want_slot && (rc = upload_offdiag_slot_major(ctx, Ap, L.colour_start, L.G32s))) return rc;
+            if (want_slot && (rc = upload_slot_major_all(ctx, Ap, L.A32s))) return rc;
+            L.gs_slot[FHG_PREC_FP32] = o.gs_layout == FHG_GS_SLOT && L.G32s.vals;
+            L.prod_slot[FHG_PREC_FP32] = o.gs_layout == FHG_GS_SLOT && L.A32s.vals;
+        }
+        if (pair && l < nlevels - 1) {
+            if (o.colouring && (rc = upload_padded(ctx, Ap, L.G2, true, 8))) return rc;
+            if ((rc = upload_padded(ctx, Ap, L.A2p, false, 8))) return rc;
+            if (want_slot && (rc = upload_offdiag_slot_major(ctx, Ap, L.colour_start, L.G2s))) return rc;
+            if (want_slot && (rc = upload_slot_major_all(ctx, Ap, L.A2s))) return rc;
+            L.gs_slot[FHG_PREC_DF] = o.gs_layout == FHG_GS_SLOT && L.G2s.vals;
+            L.prod_slot[FHG_PREC_DF] = o.gs_layout == FHG_GS_SLOT && L.A2s.vals;
         }
         if ((rc = upload(ctx, &L.perm_d, L.perm.data(), L.perm.size()))) return rc;
         if (l < nlevels - 1) {
@@ -1738,6 +1893,11 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
                 std::vector<float> s32(soa.begin(), soa.end());
                 if ((rc = upload(ctx, &L.dinv32, s32.data(), s32.size()))) return rc;
             }
+            if (pair) {
+                std::vector<dfl> s2(soa.size());
+                for (size_t q = 0; q < soa.size(); q++) s2[q] = dfl(soa[q]);
+                if ((rc = upload(ctx, &L.dinv2, s2.data(), s2.size()))) return rc;
+            }
             // Transfers: P' = Pi_l P Pi_{l+1}^T, R' = P'^T.
             HostBsr Pb, Pp, Rp;
             csr_to_bsr(L.P_in, bs, Pb);
@@ -1750,6 +1910,10 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
             if (fp32) {
                 if ((rc = upload_bsr<float>(ctx, Pp, L.P32, &L.P))) return rc;
                 if ((rc = upload_bsr<float>(ctx, Rp, L.R32, &L.R))) return rc;
+            }
+            if (pair) {
+                if ((rc = upload_bsr<dfl>(ctx, Pp, L.P2, &L.P))) return rc;
+                if ((rc = upload_bsr<dfl>(ctx, Rp, L.R2, &L.R))) return rc;
             }
         }
         if (l == 0 && fp32 && nlevels > 1 && fhg::learned_supports(bs)) {
@@ -1767,7 +1931,7 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
             HostCsr S;
             symmetrise_lower(L.A_in, S);
             L.ahat_is_a = csr_equal(S, L.A_in);
-            const bool split = fp32 && o.outer_split;
+            const bool split = (fp32 || pair) && o.outer_split;
             if (!L.ahat_is_a) {
                 HostBsr Sb, Sp;
                 csr_to_bsr(S, bs, Sb);
@@ -1791,10 +1955,13 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         if ((rc = dalloc(ctx, &L.x, L.n)) || (rc = dalloc(ctx, &L.b, L.n)) || (rc = dalloc(ctx, &L.r, L.n))) return rc;
         if (fp32 && ((rc = dalloc(ctx, &L.x32, L.n)) || (rc = dalloc(ctx, &L.b32, L.n)) || (rc = dalloc(ctx, &L.r32, L.n))))
             return rc;
+        if (pair && ((rc = dalloc(ctx, &L.x2, L.n)) || (rc = dalloc(ctx, &L.b2, L.n)) || (rc = dalloc(ctx, &L.r2, L.n))))
+            return rc;
         if (l > 0 && l < nlevels - 1)  // K-cycle vectors (the K-cycle runs FCG on levels 1..L-2)
             for (int i = 0; i < 4; i++) {
                 if ((rc = dalloc(ctx, &L.kv64[i], L.n))) return rc;
                 if (fp32 && (rc = dalloc(ctx, &L.kv32[i], L.n))) return rc;
+                if (pair && (rc = dalloc(ctx, &L.kv2[i], L.n))) return rc;
             }
     }
     const long long n0 = ctx->levels[0].n;
@@ -1806,7 +1973,10 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         (rc = dalloc(ctx, &ctx->io, (size_t)2 * n0)))
         return rc;
     ctx->rlo = nullptr;
-    if (fp32 && o.outer_split && (rc = dalloc(ctx, &ctx->rlo, n0))) return rc;
+    ctx->rhi = nullptr;
+    if ((fp32 || pair) && o.outer_split && (rc = dalloc(ctx, &ctx->rlo, n0))) return rc;
+    // the high part of r: the FP32 V-cycle's right-hand side b32 itself; a buffer of its own otherwise
+    if (pair && o.outer_split && (rc = dalloc(ctx, &ctx->rhi, n0))) return rc;
     CK(cudaMallocHost(&ctx->nr_host, sizeof(double)));
 
     if (o.autotune) {
@@ -1814,17 +1984,26 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         // the same access pattern); the outer operators on their own launches.
         for (int l = 0; l < nlevels; l++) {
             Level& L = ctx->levels[l];
-            if (fp32) {
-                if ((rc = tune_level<float>(ctx, l))) return rc;
-                L.A.v.lanes = LevelVecs<float>::A(L).lanes;
-                L.A.v.unroll = LevelVecs<float>::A(L).unroll;
-                if (l < nlevels - 1) {
-                    L.P.v.lanes = LevelVecs<float>::P(L).lanes; L.P.v.unroll = LevelVecs<float>::P(L).unroll;
-                    L.R.v.lanes = L.R32.v.lanes; L.R.v.unroll = L.R32.v.unroll;
-                }
-            } else {
+            if (fp32 && (rc = tune_level<float>(ctx, l))) return rc;
+            if (pair && (rc = tune_level<dfl>(ctx, l))) return rc;
+            if (!fp32 && !pair) {
                 if ((rc = tune_level<double>(ctx, l))) return rc;
+                continue;
             }
+            // The FP64 copies take the shapes of the pair copies (same 8-byte values), else the FP32
+            // ones: the row-major views' lanes (a slot-major view runs one thread per row).
+            auto take = [&](const auto& A, const auto& P, const auto& R, int src) {
+                L.A.v.lanes = A.lanes;
+                L.A.v.unroll = A.unroll;
+                L.gs_lanes[FHG_PREC_FP64] = L.gs_lanes[src];
+                L.gs_unroll[FHG_PREC_FP64] = L.gs_unroll[src];
+                if (l < nlevels - 1) {
+                    L.P.v.lanes = P.lanes; L.P.v.unroll = P.unroll;
+                    L.R.v.lanes = R.lanes; L.R.v.unroll = R.unroll;
+                }
+            };
+            if (pair) take(L.A2p.vals ? L.A2p.v : L.A2.v, L.P2.v, L.R2.v, FHG_PREC_DF);
+            else take(L.A32p.vals ? L.A32p.v : L.A32.v, L.P32.v, L.R32.v, FHG_PREC_FP32);
         }
         Level& L0 = ctx->levels[0];
         BsrView<double>& Ah = L0.ahat_is_a ? L0.A.v : L0.Ahat.v;
@@ -2022,12 +2201,12 @@ static int time_op_t(fhg_ctx* ctx, int level, int op, int warmup, int reps, doub
     CK(cudaMemsetAsync(out, 0, sizeof(T) * mx, s));
     // Inputs: the level's last V-cycle vectors (finite, representative values), converted.
     const int la = op == FHG_OP_PROLONG_ADD ? lo : li;
-    if (sizeof(T) == sizeof(double)) {
+    if constexpr (std::is_same<T, double>::value) {
         CK(cudaMemcpyAsync(in, ctx->levels[li].x, sizeof(T) * ctx->levels[li].n, cudaMemcpyDeviceToDevice, s));
         CK(cudaMemcpyAsync(aux, ctx->levels[la].b, sizeof(T) * ctx->levels[la].n, cudaMemcpyDeviceToDevice, s));
     } else {
-        fhg::launch_convert<double, float>(ctx->levels[li].n, ctx->levels[li].x, (float*)in, s);
-        fhg::launch_convert<double, float>(ctx->levels[la].n, ctx->levels[la].b, (float*)aux, s);
+        fhg::launch_convert<double, T>(ctx->levels[li].n, ctx->levels[li].x, in, s);
+        fhg::launch_convert<double, T>(ctx->levels[la].n, ctx->levels[la].b, aux, s);
     }
     auto one = [&]() -> int {
         if (op == FHG_OP_GS_FORWARD || op == FHG_OP_GS_BACKWARD) {
@@ -2044,6 +2223,12 @@ static int time_op_t(fhg_ctx* ctx, int level, int op, int warmup, int reps, doub
             }
             if (op == FHG_OP_LEARNED_STEP) {
                 learned_step(ctx, aux, out);
+                return FHG_OK;
+            }
+        }
+        if constexpr (std::is_same<T, dfl>::value) {
+            if (op == FHG_OP_VCYCLE) {
+                vcycle<dfl>(ctx, 0, aux, out);
                 return FHG_OK;
             }
         }
@@ -2081,9 +2266,15 @@ int fhg_time_op(fhg_ctx* ctx, int level, int op, int precision, int warmup, int 
         if (rc == FHG_OK && op != FHG_OP_VCYCLE) rc = check_learned_status(ctx);
         return rc;
     }
+    if (op == FHG_OP_VCYCLE && precision == FHG_PREC_DF) {
+        if (level != 0 || !ctx->levels[0].A2.vals)
+            return fail(ctx, FHG_ERR_INVALID_ARG, "the pair V-cycle is timed on level 0 (pair copies built at setup)");
+        return time_op_t<dfl>(ctx, 0, op, warmup, reps, avg_ms);
+    }
     if (op == FHG_OP_SYM_SPMV || op == FHG_OP_VCYCLE) {
         Level& L0 = ctx->levels[0];
-        const bool split = op == FHG_OP_SYM_SPMV && precision == FHG_PREC_FP32;
+        // FP32 or DF: the outer operator in double-FP32 arithmetic (the one product both use)
+        const bool split = op == FHG_OP_SYM_SPMV && (precision == FHG_PREC_FP32 || precision == FHG_PREC_DF);
         if (precision != FHG_PREC_FP64 && !split) return fail(ctx, FHG_ERR_INVALID_ARG, "op %d is timed in FP64 only", op);
         if (split && (!L0.ahat_lo || !ctx->rlo))
             return fail(ctx, FHG_ERR_NOT_READY, "the double-FP32 outer operator was not built at setup");
@@ -2119,6 +2310,10 @@ int fhg_time_op(fhg_ctx* ctx, int level, int op, int precision, int warmup, int 
     if (precision == FHG_PREC_FP32) {
         if (!ctx->levels[0].A32.vals) return fail(ctx, FHG_ERR_NOT_READY, "FP32 operators were not built at setup");
         return time_op_t<float>(ctx, level, op, warmup, reps, avg_ms);
+    }
+    if (precision == FHG_PREC_DF) {
+        if (!ctx->levels[0].A2.vals) return fail(ctx, FHG_ERR_NOT_READY, "pair operators were not built at setup");
+        return time_op_t<dfl>(ctx, level, op, warmup, reps, avg_ms);
     }
     return time_op_t<double>(ctx, level, op, warmup, reps, avg_ms);
 }
@@ -2162,9 +2357,12 @@ int fhg_set_vcycle_precision(fhg_ctx* ctx, int precision)
 {
     if (!ctx) return FHG_ERR_INVALID_ARG;
     if (!ctx->ready) return fail(ctx, FHG_ERR_NOT_READY, "fhg_setup has not completed");
-    if (precision != FHG_PREC_FP64 && precision != FHG_PREC_FP32) return fail(ctx, FHG_ERR_INVALID_ARG, "unknown precision");
+    if (precision != FHG_PREC_FP64 && precision != FHG_PREC_FP32 && precision != FHG_PREC_DF)
+        return fail(ctx, FHG_ERR_INVALID_ARG, "unknown precision");
     if (precision == FHG_PREC_FP32 && !ctx->levels[0].A32.vals)
         return fail(ctx, FHG_ERR_NOT_READY, "FP32 operators were not built: set up with FHG_PREC_FP32");
+    if (precision == FHG_PREC_DF && !ctx->levels[0].A2.vals)
+        return fail(ctx, FHG_ERR_NOT_READY, "pair operators were not built: set up with FHG_PREC_DF");
     if (ctx->opts.vcycle_precision != precision) {
         free_graphs(ctx);
         ctx->epoch++;
@@ -2327,6 +2525,16 @@ int fhg_apply_internal(fhg_ctx* ctx, int level, int op, int precision, const voi
             return fail(ctx, FHG_ERR_INVALID_ARG, "the outer operator is FP64");
         } else {
             rc = apply_device_t<float>(ctx, level, op, (float*)in, (float*)aux, (float*)out);
+        }
+    } else if (precision == FHG_PREC_DF) {
+        if (!ctx->levels[0].A2.vals) return fail(ctx, FHG_ERR_NOT_READY, "pair operators were not built at setup");
+        if (op == FHG_OP_VCYCLE) {
+            if (level != 0) return fail(ctx, FHG_ERR_INVALID_ARG, "V-cycle starts on level 0");
+            vcycle<dfl>(ctx, 0, (const dfl*)in, (dfl*)out);
+        } else if (op == FHG_OP_SYM_SPMV || op == FHG_OP_VCYCLE_LEARNED || op == FHG_OP_LEARNED_STEP) {
+            return fail(ctx, FHG_ERR_INVALID_ARG, "op %d has no pair form", op);
+        } else {
+            rc = apply_device_t<dfl>(ctx, level, op, (dfl*)in, (dfl*)aux, (dfl*)out);
         }
     } else {
         return fail(ctx, FHG_ERR_INVALID_ARG, "unknown precision %d", precision);

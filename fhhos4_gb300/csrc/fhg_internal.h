@@ -7,6 +7,8 @@
 #include <atomic>
 #include <cstdint>
 
+#include "fhg_pair.h"
+
 namespace fhg {
 
 // Device block-sparse-row operator. Block values are stored entry-major
@@ -83,17 +85,21 @@ void launch_fcg_direction_mixed(long long n, const float* z, const double* dp, c
 void launch_spmv_dots_df(const BsrView<float>& Ahi, const float* vlo, const float* dhi, const float* dlo,
                          const float* rhi, const float* rlo, float* Adhi, float* Adlo, double* partials,
                          cudaStream_t s);
-// partials of z.Adp (z FP32).
-void launch_dot_df(long long n, const float* z, const float* ah, const float* al, double* partials, cudaStream_t s);
-// d = z - s dp, s = sum(partials_zadp) / *dadp.
+// partials of z.Adp (z FP32, or z2 non-null: the pair V-cycle's output as interleaved pairs).
+void launch_dot_df(long long n, const float* z, const float* ah, const float* al, double* partials, cudaStream_t s,
+                   const dfl* z2 = nullptr);
+// d = z - s dp, s = sum(partials_zadp) / *dadp (z as in launch_dot_df).
 void launch_fcg_direction_df(long long n, const float* z, const float* dph, const float* dpl,
-                             const double* partials_zadp, const double* dadp, float* dh, float* dl, cudaStream_t s);
-// As launch_krylov_step with r, d, Ad as pairs; rh doubles as the next V-cycle's FP32 right-hand side.
+                             const double* partials_zadp, const double* dadp, float* dh, float* dl, cudaStream_t s,
+                             const dfl* z2 = nullptr);
+// As launch_krylov_step with r, d, Ad as pairs; rh doubles as the next V-cycle's FP32 right-hand side,
+// r2 (optional) receives r as interleaved pairs, the pair V-cycle's right-hand side.
 void launch_krylov_step_df(long long n, double* x, float* rh, float* rl, const float* dh, const float* dl,
                            const float* Adh, const float* Adl, const double* partials_num,
-                           const double* partials_den, double* den_out, double* partials_rr, cudaStream_t s);
-// v -> (h, l).
-void launch_split_df(long long n, const double* v, float* h, float* l, cudaStream_t s);
+                           const double* partials_den, double* den_out, double* partials_rr, cudaStream_t s,
+                           dfl* r2 = nullptr);
+// v -> (h, l) and, optionally, v2 interleaved.
+void launch_split_df(long long n, const double* v, float* h, float* l, cudaStream_t s, dfl* v2 = nullptr);
 // ||r|| / ||b||: reduces partials_rr, divides by *bnorm, writes *nr_out and hist[*counter],
 // then ++*counter.
 void launch_finalize_norm(const double* partials_rr, const double* bnorm, double* nr_out,

@@ -106,6 +106,8 @@ class Multigrid(IterativeSolver):
         self.CoarsePreSmoothingIterations = -1
         self.CoarsePostSmoothingIterations = -1
         self.GsLayout = "auto"   # FP32 GS sweeps: "auto", "row" or "slot" (padded rows)
+        # further V-cycle precisions whose operator copies setup builds, to switch to later
+        self.ExtraPrecisions: List[str] = []
         self._As: List[sp.csr_matrix] = []
         self._Ps: List[sp.csr_matrix] = []
         self._nLevels = nLevels
@@ -175,6 +177,7 @@ class _KrylovOnGpu(IterativeSolver):
         o.coarse_pre_iterations = mg.CoarsePreSmoothingIterations
         o.coarse_post_iterations = mg.CoarsePostSmoothingIterations
         o.gs_layout = N.GS_LAYOUT[mg.GsLayout]
+        o.extra_precisions = sum(1 << N.PRECISION[p] for p in set(mg.ExtraPrecisions))
         return o
 
     def Setup(self, A):
@@ -249,7 +252,7 @@ class ConjugateGradient(_KrylovOnGpu):
 def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: str = "bgs", post: str = "rbgs",
            precision: str = "fp64", krylov: str = "fcg", device: int = 0, autotune: bool = False,
            use_graphs: bool = True, outer_split: bool = True, cycle: str = "V", galerkin: bool = False,
-           nu=(1, 1), coarse_nu=(-1, -1), gs_layout: str = "auto", omega: float = 1.0):
+           nu=(1, 1), coarse_nu=(-1, -1), gs_layout: str = "auto", omega: float = 1.0, extra=()):
     """SolverFactory-style construction of "-s fcgmg -cycle V,1,1" (src/Solver/SolverFactory.h:156-200)."""
     mg = Multigrid(len(As))
     mg.SetHierarchy(As, Ps)
@@ -264,6 +267,7 @@ def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: st
     mg.CoarsePreSmoothingIterations, mg.CoarsePostSmoothingIterations = coarse_nu
     mg.GsLayout = gs_layout
     mg.RelaxationParameter = omega
+    mg.ExtraPrecisions = list(extra)
     solver = FlexibleConjugateGradient(1) if krylov == "fcg" else ConjugateGradient()
     solver.Precond = SolverPreconditioner(mg)
     solver.Tolerance = tol

@@ -60,6 +60,12 @@ extern "C" {
 
 #define FHG_PREC_FP64 0
 #define FHG_PREC_FP32 1
+/* FP64-class V-cycle on the FP32 pipe: operators, inverted diagonal blocks and vectors as FP32
+ * pairs hi + lo (about 48 significant bits, a few units of 2^-47 per multiply-add), the outer FCG
+ * iteration in the same pair arithmetic with FP64 x and Krylov scalars, the reference's loop
+ * otherwise unchanged. GB300's FP64 pipe runs at 1/56 of its FP32 rate; with the pair values in
+ * the 8 bytes a double takes, the block products stay bound by HBM instead of the FP64 pipe. */
+#define FHG_PREC_DF 2
 
 /* Learned correction step of the FP32 V-cycle (no counterpart in the reference): off, on with
  * the fallback rule of fhg_set_learned, or on for every iteration. */
@@ -111,7 +117,11 @@ typedef struct {
     int coarse_post_iterations; /* the same after it; -1: post_iterations */
     int gs_layout;              /* FP32 GS sweeps: FHG_GS_AUTO (the autotuner picks row- or slot-major padded
                                    rows; row-major without autotuning), FHG_GS_ROW, FHG_GS_SLOT. Same
-                                   arithmetic, different storage order and launch shape. */
+                                   arithmetic, different storage order and launch shape; FHG_GS_SLOT also
+                                   makes the products with A use the slot-major view of all of A. */
+    int extra_precisions;       /* bit mask (1 << FHG_PREC_FP32, 1 << FHG_PREC_DF) of V-cycle precisions whose
+                                   operator copies setup also builds, besides vcycle_precision's, so that
+                                   fhg_set_vcycle_precision can switch to them (FP64 copies are always built) */
 } fhg_options;
 
 typedef struct {
@@ -174,8 +184,8 @@ int fhg_solve_device(fhg_ctx* ctx, const double* b_dev, double* x_dev, double* h
                                   fhg_apply_internal, fhg_time_op) */
 int fhg_apply(fhg_ctx* ctx, int level, int op, const double* in, const double* aux, double* out);
 
-/* Device timing of one operator (same ops; vectors left in device memory) in FHG_PREC_FP64 or
- * FHG_PREC_FP32 (the V-cycle copies): average ms per application over `reps` back-to-back
+/* Device timing of one operator (same ops; vectors left in device memory) in FHG_PREC_FP64,
+ * FHG_PREC_FP32 or FHG_PREC_DF (the V-cycle copies): average ms per application over `reps` back-to-back
  * applications after `warmup`, CUDA events on the context stream. A block-GS sweep is all of
  * its colour launches. */
 int fhg_time_op(fhg_ctx* ctx, int level, int op, int precision, int warmup, int reps, double* avg_ms);
@@ -190,8 +200,9 @@ int fhg_set_cycle(fhg_ctx* ctx, int pre_smoother, int post_smoother, int pre_ite
  * captured in graphs are rebuilt. No counterpart in the reference. */
 int fhg_set_coarse_smoothing(fhg_ctx* ctx, int pre_iterations, int post_iterations);
 
-/* Switch the V-cycle precision of a set-up context (FP32 needs a setup with FHG_PREC_FP32,
- * which keeps both copies). The outer Krylov iteration stays FP64. */
+/* Switch the V-cycle precision of a set-up context (FP32 and DF need their copies: a setup in that
+ * precision or with its bit in extra_precisions). The outer Krylov iteration keeps FP64 x and
+ * scalars. */
 int fhg_set_vcycle_precision(fhg_ctx* ctx, int precision);
 
 /* Sizes of level `level` after setup: block rows, stored blocks of A, colours, lanes per block row
@@ -260,8 +271,9 @@ int fhg_learned_reference_rate(fhg_ctx* ctx, double* rho);
 int fhg_learned_features(fhg_ctx* ctx, const float* r, void* features, float* scale);
 
 /* fhg_apply on DEVICE vectors in the context's colour numbering (fhg_get_permutation), in
- * FHG_PREC_FP64 (double) or FHG_PREC_FP32 (float, the V-cycle copies; FHG_OP_VCYCLE_LEARNED
- * applies the installed network). Returns after the stream has finished. */
+ * FHG_PREC_FP64 (double), FHG_PREC_FP32 (float, the V-cycle copies; FHG_OP_VCYCLE_LEARNED
+ * applies the installed network) or FHG_PREC_DF (interleaved FP32 pairs hi, lo: 8 bytes per value).
+ * Returns after the stream has finished. */
 int fhg_apply_internal(fhg_ctx* ctx, int level, int op, int precision, const void* in, const void* aux, void* out);
 
 /* Training of the network on the GPU (FP32 master weights, BF16 tensor-core forward and backward,

@@ -236,6 +236,94 @@ def test_autotuned_lanes_give_the_same_solve(case):
     assert hist_close(solver.History, ref)
 
 
+# ------------------------------------------------------- FP64-class V-cycle in FP32 pairs (df)
+DF_VARIANTS = [("colour", "bgs", "rbgs", "V", None), ("w", "bgs", "rbgs", "W", None),
+               ("sbgs", "sbgs", "sbgs", "V", None), ("abgs", "abgs", "rabgs", "V", None),
+               ("k", "bgs", "rbgs", "K", None), ("sor", "bsor", "rbsor", "V", "sor_omega")]
+
+
+@pytest.mark.parametrize("variant,pre,post,cycle,omega_key,layout",
+                         [v + ("auto",) for v in DF_VARIANTS] + [DF_VARIANTS[0] + ("slot",)])
+def test_df_vcycle_matches_reference(case, variant, pre, post, cycle, omega_key, layout):
+    """The pair V-cycle (FHG_PREC_DF: operators, D^-1 and vectors as FP32 pairs, the outer FCG in pair
+    arithmetic with FP64 x) at the reference's own bar: iteration counts exact, histories within
+    1e-10, x within 1e-10 (row-major views, and slot-major sweeps and products)."""
+    omega = float(case[omega_key]) if omega_key else 1.0
+    solver = S().fcg_mg(case.As, case.Ps, case.bs, pre=pre, post=post, cycle=cycle, omega=omega, precision="df",
+                        gs_layout=layout)
+    x = solver.Solve(case.b)
+    ref = case[f"hist_{variant}"]
+    assert solver.IterationCount == len(ref) - 1
+    # Absolute floor 2^6 times the FP64 one: pairs carry 47-48 bits, so a residual at the rounding
+    # level of an exact coarse solve (one-iteration cases) sits 64 times higher than in FP64.
+    h, r = np.asarray(solver.History), np.asarray(ref)
+    assert np.all(np.abs(h - r) <= 1e-10 * np.abs(r) + 64 * HIST_ATOL), (h, r)
+    sp_ = scalar_perm(case.perms[0], case.bs)
+    xr = case[f"x_{variant}"]
+    assert np.linalg.norm(x[sp_] - xr) / np.linalg.norm(xr) < X_RTOL
+
+
+def _pairs(torch, v):
+    """An FP64 vector as interleaved FP32 pairs (hi, lo) on the device."""
+    hi = v.astype(np.float32)
+    lo = (v - hi.astype(np.float64)).astype(np.float32)
+    return torch.tensor(np.stack([hi, lo], axis=1), device="cuda")
+
+
+def _unpair(t):
+    a = t.cpu().numpy().astype(np.float64)
+    return a[:, 0] + a[:, 1]
+
+
+@pytest.mark.parametrize("layout", ["row", "slot"])
+def test_df_operators_of_every_level(case, layout):
+    """Every pair operator of every level (row- or slot-major padded views) against the oracle in
+    FP64, to FP64-class accuracy."""
+    torch = pytest.importorskip("torch")
+    from fhhos4_gb300 import _native as N
+    solver = S().fcg_mg(case.As, case.Ps, case.bs, precision="df", gs_layout=layout)
+    ctx = solver.Context()
+    rng = np.random.default_rng(5)
+    tol = 1e-12
+    for l, A in enumerate(case.As):
+        n = A.shape[0]
+        s = scalar_perm(ctx.permutation(l, n // case.bs), case.bs)
+        Ap = O.as_csr(A[s][:, s])
+        x = rng.standard_normal(n)
+        b = rng.standard_normal(n)
+        xd, bd = _pairs(torch, x), _pairs(torch, b)
+        out = torch.zeros_like(xd)
+        scale = np.abs(A).max() * np.linalg.norm(x) + np.linalg.norm(b)
+        ctx.apply_internal(l, N.OP_SPMV, "df", xd.data_ptr(), None, out.data_ptr())
+        assert np.linalg.norm(_unpair(out) - O.spmv(Ap, x)) <= tol * scale, l
+        ctx.apply_internal(l, N.OP_RESIDUAL, "df", xd.data_ptr(), bd.data_ptr(), out.data_ptr())
+        assert np.linalg.norm(_unpair(out) - O.residual(Ap, b, x)) <= tol * scale, l
+        if l < case.levels - 1:
+            for op, backward in ((N.OP_GS_FORWARD, False), (N.OP_GS_BACKWARD, True)):
+                ctx.apply_internal(l, op, "df", xd.data_ptr(), bd.data_ptr(), out.data_ptr())
+                ref = O.block_gs(Ap, case.bs, b, x, backward=backward)
+                assert np.linalg.norm(_unpair(out) - ref) <= 1e-11 * np.linalg.norm(ref), (l, op)
+            ctx.apply_internal(l, N.OP_JACOBI, "df", xd.data_ptr(), bd.data_ptr(), out.data_ptr())
+            ref = O.block_jacobi(Ap, case.bs, 1.0, b, x)
+            assert np.linalg.norm(_unpair(out) - ref) <= 1e-11 * np.linalg.norm(ref), l
+            sc = scalar_perm(ctx.permutation(l + 1, case.As[l + 1].shape[0] // case.bs), case.bs)
+            Pp = O.as_csr(case.Ps[l][s][:, sc])
+            nc = Pp.shape[1]
+            rc = torch.zeros((nc, 2), dtype=torch.float32, device="cuda")
+            ctx.apply_internal(l, N.OP_RESTRICT, "df", xd.data_ptr(), None, rc.data_ptr())
+            ref = O.spmv(O.as_csr(Pp.T), x)
+            assert np.linalg.norm(_unpair(rc) - ref) <= tol * np.abs(Pp).max() * np.linalg.norm(x) * 10, l
+            e = rng.standard_normal(nc)
+            ed = _pairs(torch, e)
+            ctx.apply_internal(l, N.OP_PROLONG_ADD, "df", ed.data_ptr(), xd.data_ptr(), out.data_ptr())
+            ref = x + O.spmv(Pp, e)
+            assert np.linalg.norm(_unpair(out) - ref) <= tol * (np.linalg.norm(x) + np.abs(Pp).max() * np.linalg.norm(e)) * 10
+        else:
+            ctx.apply_internal(l, N.OP_COARSE_SOLVE, "df", bd.data_ptr(), None, out.data_ptr())
+            ref = np.linalg.solve(Ap.toarray(), b)
+            assert np.linalg.norm(_unpair(out) - ref) <= 1e-10 * np.linalg.norm(ref)
+
+
 # ---------------------------------------------------------------------------- kernels
 def _ctx(case):
     solver = S().fcg_mg(case.As, case.Ps, case.bs)
@@ -286,8 +374,9 @@ def test_operators_of_every_level(case):
 
 @pytest.mark.parametrize("layout", ["row", "slot"])
 def test_fp32_smoothers_of_every_level(case, layout):
-    """FP32 GS sweeps (on the padded off-diagonal view where setup built one, row- or slot-major) and
-    block Jacobi on every smoothed level against the FP64 oracle in colour order, to FP32 accuracy."""
+    """FP32 GS sweeps (on the padded off-diagonal view where setup built one, row- or slot-major), the
+    residual product (on the same layout's view of A) and block Jacobi on every smoothed level against
+    the FP64 oracle in colour order, to FP32 accuracy."""
     torch = pytest.importorskip("torch")
     from fhhos4_gb300 import _native as N
     solver = S().fcg_mg(case.As, case.Ps, case.bs, precision="fp32", gs_layout=layout)
@@ -308,6 +397,11 @@ def test_fp32_smoothers_of_every_level(case, layout):
             ref = O.block_gs(Ap, case.bs, b, x, backward=backward)
             g = out.cpu().numpy().astype(np.float64)
             assert np.linalg.norm(g - ref) <= 2e-4 * np.linalg.norm(ref), (l, op)
+        # products with A on the same layout's view
+        scale = np.abs(A).max() * np.linalg.norm(x) + np.linalg.norm(b)
+        ctx.apply_internal(l, N.OP_RESIDUAL, "fp32", xd.data_ptr(), bd.data_ptr(), out.data_ptr())
+        g = out.cpu().numpy().astype(np.float64)
+        assert np.linalg.norm(g - O.residual(Ap, b, x)) <= 1e-5 * scale, l
         ctx.apply_internal(l, N.OP_JACOBI, "fp32", xd.data_ptr(), bd.data_ptr(), out.data_ptr())
         ref = O.block_jacobi(Ap, case.bs, 1.0, b, x)
         g = out.cpu().numpy().astype(np.float64)

@@ -55,4 +55,4 @@ def test_hierarchy_shape_checks():
 def test_option_codes_match_header():
     assert N.SMOOTHERS == {"bgs": 0, "rbgs": 1, "bj": 2, "bj23": 3, "sbgs": 4, "abgs": 5, "rabgs": 6}
     assert N.KRYLOV == {"fcg": 0, "cg": 1}
-    assert N.PRECISION == {"fp64": 0, "fp32": 1}
+    assert N.PRECISION == {"fp64": 0, "fp32": 1, "df": 2}
