@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--source", default="sine", choices=["sine", "one"])
     ap.add_argument("--max-coarse-rows", type=int, default=1000)
     ap.add_argument("--galerkin", action="store_true", help="Galerkin coarse operators (the reference's -g 1)")
+    ap.add_argument("--replace-residual", action="store_true",
+                    help="residual replacement in every precision (FP64 true residual, compensated when it misses tol)")
     ap.add_argument("--fast-smoothers", default="bgs,rbgs", help="pre,post smoothers of the fast (FP32) method")
     ap.add_argument("--fast-nu", default="3,3", help="pre,post smoothing steps of the fast (FP32) method")
     ap.add_argument("--fast-coarse-nu", default="4,4",
@@ -273,6 +275,7 @@ def run_ours(args, dist: Dist):
     o.vcycle_precision = N.PRECISION["fp32"]   # keeps FP64 and FP32 copies
     o.extra_precisions = 1 << N.PRECISION["df"]   # and the FP32-pair copies (FP64-class V-cycle)
     o.galerkin = 1 if args.galerkin else 0
+    o.replace_residual = 1 if args.replace_residual else 0
     o.autotune = 1
     o.max_iterations = 200
     ctx.setup(len(As), o)

@@ -1564,12 +1564,23 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
         CK(cudaMemcpyAsync(h, ctx->scal, sizeof(h), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         true_rel = h[0] > 0 ? h[5] / h[0] : h[5];
-        // FP32 V-cycle: the recursive residual of the outer iteration can drift from the true one
-        // (the double-FP32 outer product loses digits to cancellation at high coefficient
-        // contrast). Residual replacement: r = b - A x in FP64 and the iteration continues (the
-        // direction recurrence is kept) until the true residual meets the tolerance. The FP64
-        // mode keeps the reference's loop unchanged.
-        if (fp32 && ctx->opts.krylov == FHG_KRYLOV_FCG && it < maxit && !(true_rel < ctx->opts.tolerance) &&
+        if (!(true_rel < ctx->opts.tolerance) && std::isfinite(true_rel)) {
+            // A plain FP64 evaluation of b - A x errs by up to u sum_j |a_ij x_j| per row, which at high
+            // coefficient contrast exceeds the tolerance: evaluate it again in compensated arithmetic
+            // (accurate to about one unit of each r_i) before judging the solve or replacing r.
+            fhg::launch_residual_comp(L0.A.v, ctx->kx, ctx->kb, ctx->kt, part(ctx, 0), s);
+            fhg::launch_sqrt_sum(part(ctx, 0), ctx->scal + 5, s);
+            CK(cudaMemcpyAsync(h, ctx->scal, sizeof(h), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            true_rel = h[0] > 0 ? h[5] / h[0] : h[5];
+        }
+        // FP32 V-cycle (and, with fhg_options.replace_residual, the FP64 ones): the recursive residual
+        // of the outer iteration can drift from the true one (the outer product loses digits to
+        // cancellation at high coefficient contrast). Residual replacement: r = b - A x and the
+        // iteration continues (the direction recurrence is kept) until the true residual meets the
+        // tolerance. Without the option the FP64 modes keep the reference's loop unchanged.
+        const bool replace = fp32 || ctx->opts.replace_residual;
+        if (replace && ctx->opts.krylov == FHG_KRYLOV_FCG && it < maxit && !(true_rel < ctx->opts.tolerance) &&
             replacements < 8) {
             replacements++;
             CK(cudaMemcpyAsync(ctx->kr, ctx->kt, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
@@ -1660,6 +1671,7 @@ void fhg_default_options(fhg_options* o)
     o->coarse_post_iterations = -1;
     o->gs_layout = FHG_GS_AUTO;
     o->extra_precisions = 0;
+    o->replace_residual = 0;
 }
 
 int fhg_create(fhg_ctx** out, int device)

@@ -63,6 +63,10 @@ void launch_spmv_dots(const BsrView<double>& A, const double* d, const double* r
 // x = Cinv b, Cinv dense n x n row-major FP64; b, x in T.
 template <class T>
 void launch_coarse(int n, const double* cinv, const T* b, T* x, cudaStream_t s);
+// r = b - A x in compensated (Dot2) FP64 summation, accurate to about one unit of r_i; partials of r.r.
+// A must be the CSR form (rowptr). enable (optional, device): the kernel returns at once if *enable == 0.
+void launch_residual_comp(const BsrView<double>& A, const double* x, const double* b, double* r, double* partials,
+                          cudaStream_t s, const int* enable = nullptr);
 // partials[0..kReduceCtas) of sum a_i b_i.
 void launch_dot(long long n, const double* a, const double* b, double* partials, cudaStream_t s);
 // FCG(1) direction: s = sum(partials_zadp) / *dadp; d = z - s * dp (d may alias z).

@@ -175,6 +175,61 @@ __global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots_df(int nbr, co
     }
 }
 
+// r = b - A x with compensated summation (Ogita, Rump and Oishi 2005, "Accurate sum and dot
+// product", Dot2): every product split exactly by an FMA (TwoProduct), the running sum kept exact by
+// TwoSum, the rounding errors summed apart and added once, so r_i carries an error of about one unit
+// of FP64 in r_i itself whatever the cancellation between b_i and the products (which bounds a plain
+// FP64 evaluation at u sum_j |a_ij x_j|). One thread per block row over a fixed grid; per-CTA
+// partials of sum r_i^2. FP64 pipe work of about ten operations per term: used only when the plain
+// FP64 true residual misses the tolerance. `enable` (optional, the device loop): run only if *enable.
+template <int BS>
+__global__ void __launch_bounds__(kReduceThreads) k_bsr_residual_comp(int nbr, const int* __restrict__ rowptr,
+                                                                      const int* __restrict__ colidx,
+                                                                      const double* __restrict__ vals, long long ld,
+                                                                      const double* __restrict__ x,
+                                                                      const double* __restrict__ b,
+                                                                      double* __restrict__ r,
+                                                                      double* __restrict__ partials,
+                                                                      const int* __restrict__ enable)
+{
+    pdl_wait();
+    if (enable && *enable == 0) return;
+    __shared__ double sh[33];
+    double rr = 0.0;
+    for (long long row = (long long)blockIdx.x * kReduceThreads + threadIdx.x; row < nbr; row += kRedStride) {
+        double sum[BS], err[BS];
+#pragma unroll
+        for (int k = 0; k < BS; k++) { sum[k] = b[row * BS + k]; err[k] = 0.0; }
+        for (int p = rowptr[row]; p < rowptr[row + 1]; p++) {
+            const long long col = colidx[p];
+            double xv[BS];
+#pragma unroll
+            for (int c = 0; c < BS; c++) xv[c] = x[col * BS + c];
+#pragma unroll
+            for (int k = 0; k < BS; k++)
+#pragma unroll
+                for (int c = 0; c < BS; c++) {
+                    const double a = vals[(long long)(k * BS + c) * ld + p];
+                    const double pr = a * xv[c];
+                    const double q = fma(a, xv[c], -pr);        // a x = pr + q exactly
+                    const double t = sum[k] - pr;                // TwoSum(sum, -pr)
+                    const double z = t - sum[k];
+                    const double e = (sum[k] - (t - z)) + (-pr - z);
+                    sum[k] = t;
+                    err[k] += e - q;
+                }
+        }
+#pragma unroll
+        for (int k = 0; k < BS; k++) {
+            const double v = sum[k] + err[k];
+            r[row * BS + k] = v;
+            rr = fma(v, v, rr);
+        }
+    }
+    rr = block_sum(rr, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = rr;
+}
+
 __global__ void __launch_bounds__(kReduceThreads) k_dot(long long n, const double* __restrict__ a,
                                                         const double* __restrict__ b, double* __restrict__ partials)
 {
@@ -515,6 +570,22 @@ void launch_spmv_dots(const BsrView<double>& A, const double* d, const double* r
         pdl_launch(k_bsr_spmv_dots<BS, G>, kReduceCtas, kReduceThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals, A.ld, d, r,
                                                                       Ad, partials);
     });
+    g_kernel_launches++;
+}
+
+void launch_residual_comp(const BsrView<double>& A, const double* x, const double* b, double* r, double* partials,
+                          cudaStream_t s, const int* enable)
+{
+    switch (A.bs) {
+    case 2: pdl_launch(k_bsr_residual_comp<2>, kReduceCtas, kReduceThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals,
+                       A.ld, x, b, r, partials, enable); break;
+    case 3: pdl_launch(k_bsr_residual_comp<3>, kReduceCtas, kReduceThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals,
+                       A.ld, x, b, r, partials, enable); break;
+    case 4: pdl_launch(k_bsr_residual_comp<4>, kReduceCtas, kReduceThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals,
+                       A.ld, x, b, r, partials, enable); break;
+    default: pdl_launch(k_bsr_residual_comp<6>, kReduceCtas, kReduceThreads, 0, s, A.nbr, A.rowptr, A.colidx, A.vals,
+                        A.ld, x, b, r, partials, enable); break;
+    }
     g_kernel_launches++;
 }
 

@@ -154,6 +154,9 @@ class _KrylovOnGpu(IterativeSolver):
         # FP32 V-cycle only: apply the outer operator in double-FP32 arithmetic (FP64-class
         # accuracy on the FP32 pipe) instead of native FP64.
         self.OuterSplit = True
+        # Residual replacement in every precision (the FP32 V-cycle always replaces); off keeps the
+        # reference's stopping loop in FP64.
+        self.ReplaceResidual = False
         self._ctx: Optional[N.Context] = None
 
     def _options(self, mg: Multigrid) -> N.Options:
@@ -172,6 +175,7 @@ class _KrylovOnGpu(IterativeSolver):
         o.autotune = 1 if mg.Autotune else 0
         o.max_coarse_rows = mg.MaxCoarseRows
         o.outer_split = 1 if self.OuterSplit else 0
+        o.replace_residual = 1 if self.ReplaceResidual else 0
         o.w_loops = N.CYCLE_K if mg.Cycle == "K" else (mg.WLoops if mg.Cycle == "W" else 1)
         o.galerkin = 1 if mg.UseGalerkinOperator else 0
         o.coarse_pre_iterations = mg.CoarsePreSmoothingIterations
@@ -213,6 +217,7 @@ class _KrylovOnGpu(IterativeSolver):
         rc, x, hist, info = self._ctx.solve(np.asarray(b, dtype=np.float64), self.MaxIterations)
         self.IterationCount = info.iterations
         self.SolveTimeMs = info.solve_ms
+        self.TrueRelativeResidual = info.true_relative_residual
         self.History = hist
         prev = -1.0
         rates: List[float] = []
@@ -252,7 +257,8 @@ class ConjugateGradient(_KrylovOnGpu):
 def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: str = "bgs", post: str = "rbgs",
            precision: str = "fp64", krylov: str = "fcg", device: int = 0, autotune: bool = False,
            use_graphs: bool = True, outer_split: bool = True, cycle: str = "V", galerkin: bool = False,
-           nu=(1, 1), coarse_nu=(-1, -1), gs_layout: str = "auto", omega: float = 1.0, extra=()):
+           nu=(1, 1), coarse_nu=(-1, -1), gs_layout: str = "auto", omega: float = 1.0, extra=(),
+           replace_residual: bool = False):
     """SolverFactory-style construction of "-s fcgmg -cycle V,1,1" (src/Solver/SolverFactory.h:156-200)."""
     mg = Multigrid(len(As))
     mg.SetHierarchy(As, Ps)
@@ -275,5 +281,6 @@ def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: st
     solver.Device = device
     solver.UseGraphs = use_graphs
     solver.OuterSplit = outer_split
+    solver.ReplaceResidual = replace_residual
     solver.Setup(As[0])
     return solver

@@ -122,6 +122,12 @@ typedef struct {
     int extra_precisions;       /* bit mask (1 << FHG_PREC_FP32, 1 << FHG_PREC_DF) of V-cycle precisions whose
                                    operator copies setup also builds, besides vcycle_precision's, so that
                                    fhg_set_vcycle_precision can switch to them (FP64 copies are always built) */
+    int replace_residual;       /* 1: residual replacement in every precision: when the recursive residual meets the
+                                   tolerance but the true one does not, r = b - A x and FCG continues (at most 8
+                                   times); 0 (default): only with the FP32 V-cycle, the FP64 modes keep the
+                                   reference's loop (IterativeSolver.h:224-247). The true residual that misses the
+                                   tolerance in FP64 is evaluated again in compensated arithmetic. No counterpart
+                                   in the reference. */
 } fhg_options;
 
 typedef struct {

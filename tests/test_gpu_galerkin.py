@@ -119,3 +119,22 @@ def test_high_contrast_checkerboard_converges_with_galerkin(precision):
         # FP32 V-cycle: residual replacement makes the FP64 true residual meet the tolerance
         assert fcg.IterationCount <= its_o + 40
         assert r < 1e-8 * (1 + 1e-6)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "df", "fp32"])
+def test_high_contrast_true_residual_meets_tolerance_with_replacement(precision):
+    """Checkerboard 1 / 1e6, k = 2: a plain FP64 evaluation of b - A x errs by about
+    u sum |a_ij x_j|, 2e7 times ||b|| here. With residual replacement on (and the true residual that
+    misses the tolerance evaluated again in compensated arithmetic), every precision returns an x
+    whose true residual, evaluated on the host in extended precision, meets 1e-8."""
+    from fhhos4_gb300 import solver as S
+    As, Ps, b, bs = _hier(8, 2, coefficient="checkerboard", contrast=1e6)
+    fcg = S.fcg_mg(As, Ps, bs, galerkin=True, precision=precision, maxit=300, replace_residual=True)
+    x = fcg.Solve(b)
+    A = As[0].tocsr()
+    Al = A.astype(np.longdouble)
+    r = np.asarray(b, dtype=np.longdouble) - Al @ np.asarray(x, dtype=np.longdouble)
+    true_ext = float(np.sqrt(np.sum(r * r)) / np.linalg.norm(b))
+    assert true_ext < 1e-8, true_ext
+    assert fcg.TrueRelativeResidual < 1e-8
+    assert abs(fcg.TrueRelativeResidual - true_ext) <= 0.05 * true_ext + 1e-12
