@@ -32,6 +32,7 @@
 #include <string>
 #include <thread>
 #include <unordered_map>
+#include <map>
 #include <vector>
 
 namespace {
@@ -454,8 +455,13 @@ struct CellBasis {
     Mat coef;  // nR x nR: phi_i = sum_j coef(i,j) m_j
     void eval_monomials(const double* x, double* m, double* gm /* nR x 3 or null */) const
     {
+        eval_monomials_at(x, xc.data(), m, gm);
+    }
+    // The same basis translated to centre c (elements of one class differ by a translation).
+    void eval_monomials_at(const double* x, const double* c, double* m, double* gm) const
+    {
         double y[3] = {0, 0, 0};
-        for (int d = 0; d < dim; d++) y[d] = (x[d] - xc[d]) / hs;
+        for (int d = 0; d < dim; d++) y[d] = (x[d] - c[d]) / hs;
         for (int j = 0; j < nR; j++) {
             const auto& e = ex[j];
             m[j] = ipow(y[0], e[0]) * ipow(y[1], e[1]) * ipow(y[2], e[2]);
@@ -471,10 +477,28 @@ struct CellBasis {
             }
         }
     }
-    void eval(const double* x, double* v, double* g) const
+    void eval(const double* x, double* v, double* g) const { eval_at(x, xc.data(), v, g); }
+    // Values of the first `count` basis functions only (the basis is hierarchical: phi_i combines
+    // monomials 0..i), centred at c.
+    void eval_first_at(const double* x, const double* c, int count, double* v) const
+    {
+        double y[3] = {0, 0, 0};
+        for (int d = 0; d < dim; d++) y[d] = (x[d] - c[d]) / hs;
+        double m[64];
+        for (int j = 0; j < count; j++) {
+            const auto& e = ex[j];
+            m[j] = ipow(y[0], e[0]) * ipow(y[1], e[1]) * ipow(y[2], e[2]);
+        }
+        for (int i = 0; i < count; i++) {
+            double s = 0;
+            for (int j = 0; j <= i; j++) s += coef(i, j) * m[j];
+            v[i] = s;
+        }
+    }
+    void eval_at(const double* x, const double* c, double* v, double* g) const
     {
         double m[64], gm[192];
-        eval_monomials(x, m, g ? gm : nullptr);
+        eval_monomials_at(x, c, m, g ? gm : nullptr);
         for (int i = 0; i < nR; i++) {
             double s = 0, gx = 0, gy = 0, gz = 0;
             for (int j = 0; j <= i; j++) {
@@ -632,6 +656,8 @@ struct ElementOps {
     std::vector<double> bT;    // nC: (f, c_j)_T
     std::vector<double> bF;    // nF nf: condensed RHS contribution
     std::vector<double> cell_rhs;  // nC: A_TT^{-1} b_T (cell unknowns = cell_rhs + solve_cells x_F)
+    Mat att_inv;  // nC x nC: A_TT^{-1}, for the source terms of the elements of this one's class
+    Mat atf;      // nC x nF nf: A_TF
     bool ok = true;
 };
 
@@ -876,7 +902,10 @@ ElementOps element_ops(const Mesh& M, int e, const Params& prm, const Rules& rul
     Mat X = Atf;  // A_TT^{-1} A_TF
     Mat rhsb(nC, 1);
     for (int j = 0; j < nC; j++) rhsb(j, 0) = O.bT[j];
-    if (!solve(Att, X) || !solve(Att, rhsb)) { O.ok = false; return O; }
+    O.att_inv = Mat(nC, nC);
+    for (int j = 0; j < nC; j++) O.att_inv(j, j) = 1.0;
+    if (!solve(Att, X) || !solve(Att, rhsb) || !solve(Att, O.att_inv)) { O.ok = false; return O; }
+    O.atf = Atf;
     O.schur = Mat(nFF, nFF);
     for (int i = 0; i < nFF; i++)
         for (int j = 0; j < nFF; j++) {
@@ -934,7 +963,14 @@ void parallel_for(size_t n, int threads, const std::function<void(size_t, size_t
 
 struct Level {
     Mesh mesh;
-    std::vector<ElementOps> ops;
+    // Element-local operators per class of elements that differ only by a translation (same vertex
+    // offsets, same face vertex orders, same diffusion tensor): the local matrices depend on nothing
+    // else, because every cell basis is centred on its element. The source term does depend on the
+    // position, so the condensed right-hand side and the cell part of the RHS are kept per element.
+    std::vector<ElementOps> cls_ops;
+    std::vector<int> cls;                 // element -> class
+    std::vector<double> bF_e;             // per element, nF nf: condensed RHS contribution (finest level)
+    std::vector<double> cell_rhs_e;       // per element, nC: A_TT^{-1} b_T (finest level)
     int n_rows = 0;
     std::vector<int> A_rowptr, A_colidx;
     std::vector<double> A_vals;
@@ -944,11 +980,105 @@ struct Level {
     int P_cols = 0;
 };
 
+// What element_ops depends on besides the element's position: the offsets of its vertices and of
+// every local face's vertices (in the face's own order, which fixes the face basis) from its first
+// vertex, in units of the mesh spacing h rounded to h / 4096, and the bits of its diffusion tensor.
+std::vector<long long> element_key(const Mesh& M, int e, double h)
+{
+    const int dim = M.dim;
+    std::vector<long long> key;
+    key.reserve(32);
+    const auto& v0 = M.vx[M.el[e][0]];
+    auto put = [&](int vi) {
+        for (int d = 0; d < dim; d++) key.push_back(std::llround((M.vx[vi][d] - v0[d]) / h * 4096.0));
+    };
+    for (int i = 1; i <= dim; i++) put(M.el[e][i]);
+    for (int lf = 0; lf <= dim; lf++)
+        for (int j = 0; j < dim; j++) put(M.fv[M.ef[e][lf]][j]);
+    for (int i = 0; i < 9; i++) {
+        long long bits;
+        std::memcpy(&bits, &M.K[e][i], sizeof(bits));
+        key.push_back(bits);
+    }
+    return key;
+}
+
+// The source terms of element e with its class's local operators O: b_T = (f, c_j)_T on the element's
+// own quadrature points and centred basis, cell_rhs = A_TT^{-1} b_T, bF = -A_FT A_TT^{-1} b_T.
+void element_rhs(const Mesh& M, int e, const Params& prm, const Rules& rules, const ElementOps& O, double* bF,
+                 double* cell_rhs)
+{
+    const int nC = O.nC, nFF = O.nF * O.nf;
+    const auto xc = centroid(M, e);
+    double bT[64] = {0};
+    const QPts QR = element_points(M, e, rules.cell_rhs);
+    double v[64];
+    for (size_t q = 0; q < QR.w.size(); q++) {
+        O.basis.eval_first_at(QR.x[q].data(), xc.data(), nC, v);
+        const double fv = source_value(prm, QR.x[q]);
+        for (int j = 0; j < nC; j++) bT[j] += QR.w[q] * fv * v[j];
+    }
+    for (int c = 0; c < nC; c++) {
+        double s = 0;
+        for (int j = 0; j < nC; j++) s += O.att_inv(c, j) * bT[j];
+        cell_rhs[c] = s;
+    }
+    for (int i = 0; i < nFF; i++) {
+        double s = 0;
+        for (int c = 0; c < nC; c++) s += O.atf(c, i) * cell_rhs[c];
+        bF[i] = -s;
+    }
+}
+
+// Element classes of a level, their local operators (computed once per class, in parallel), and on
+// the finest level every element's source terms.
+int element_classes(Level& L, const Params& prm, const Rules& rules, int threads, bool finest)
+{
+    const Mesh& M = L.mesh;
+    const size_t ne = M.el.size();
+    const double h = 1.0 / M.n;
+    std::vector<std::vector<long long>> keys(ne);
+    parallel_for(ne, threads, [&](size_t s, size_t e) {
+        for (size_t i = s; i < e; i++) keys[i] = element_key(M, (int)i, h);
+    });
+    std::map<std::vector<long long>, int> index;
+    std::vector<int> reps;
+    L.cls.assign(ne, 0);
+    for (size_t i = 0; i < ne; i++) {
+        auto it = index.find(keys[i]);
+        if (it == index.end()) {
+            it = index.emplace(std::move(keys[i]), (int)reps.size()).first;
+            reps.push_back((int)i);
+        }
+        L.cls[i] = it->second;
+    }
+    std::vector<std::vector<long long>>().swap(keys);
+    L.cls_ops.assign(reps.size(), ElementOps());
+    std::atomic<int> bad{0};
+    parallel_for(reps.size(), threads, [&](size_t s, size_t e) {
+        for (size_t c = s; c < e; c++) {
+            L.cls_ops[c] = element_ops(M, reps[c], prm, rules, true);
+            if (!L.cls_ops[c].ok) bad++;
+        }
+    });
+    if (bad) return -2;
+    if (finest) {
+        const int nC = L.cls_ops[0].nC, nFF = L.cls_ops[0].nF * L.cls_ops[0].nf;
+        L.bF_e.assign(ne * nFF, 0.0);
+        L.cell_rhs_e.assign(ne * nC, 0.0);
+        parallel_for(ne, threads, [&](size_t s, size_t e) {
+            for (size_t i = s; i < e; i++)
+                element_rhs(M, (int)i, prm, rules, L.cls_ops[L.cls[i]], &L.bF_e[i * nFF], &L.cell_rhs_e[i * nC]);
+        });
+    }
+    return 0;
+}
+
 // Global condensed operator and RHS of one level.
 void assemble(Level& L, const Params& prm, int threads, bool want_rhs)
 {
     Mesh& M = L.mesh;
-    const int nf = (int)L.ops[0].nf, nF = M.dim + 1;
+    const int nf = (int)L.cls_ops[0].nf, nF = M.dim + 1;
     const int nI = M.n_interior;
     L.n_rows = nI * nf;
     // Block pattern: faces of the elements of each interior face.
@@ -995,7 +1125,7 @@ void assemble(Level& L, const Params& prm, int threads, bool want_rhs)
             }
             for (int side = 0; side < 2; side++) {
                 const int el = side == 0 ? M.fe1[f] : M.fe2[f];
-                const ElementOps& O = L.ops[el];
+                const ElementOps& O = L.cls_ops[L.cls[el]];
                 int lfi = -1;
                 for (int lf = 0; lf < nF; lf++)
                     if (M.ef[el][lf] == f) lfi = lf;
@@ -1011,7 +1141,8 @@ void assemble(Level& L, const Params& prm, int threads, bool want_rhs)
                     }
                 }
                 if (want_rhs)
-                    for (int a = 0; a < nf; a++) L.b[(size_t)I * nf + a] += O.bF[lfi * nf + a];
+                    for (int a = 0; a < nf; a++)
+                        L.b[(size_t)I * nf + a] += L.bF_e[(size_t)el * nF * nf + lfi * nf + a];
             }
         }
     });
@@ -1022,7 +1153,7 @@ void prolongation(Level& F, const Level& C, const Params& prm, const Rules& rule
 {
     const Mesh& M = F.mesh;
     const Mesh& MC = C.mesh;
-    const int dim = M.dim, nf = C.ops[0].nf, nFc = dim + 1;
+    const int dim = M.dim, nf = C.cls_ops[0].nf, nFc = dim + 1;
     const int nI = M.n_interior;
     std::vector<int> face_of(nI);
     for (size_t f = 0; f < M.fv.size(); f++)
@@ -1083,13 +1214,14 @@ void prolongation(Level& F, const Level& C, const Params& prm, const Rules& rule
             const FaceBasis FB = face_basis(dim, prm.k, Q);
             const int nfq = (int)Q.w.size();
             for (int t = 0; t < nce; t++) {
-                const ElementOps& O = C.ops[ce[t]];
+                const ElementOps& O = C.cls_ops[C.cls[ce[t]]];
+                const auto xc = centroid(MC, ce[t]);
                 const int nR = O.nR;
                 // Trace of the coarse reconstruction basis on the fine face: M_f^{-1} (phi_a, r_j)_f
                 Mat m(nf, nR);
                 double v[64];
                 for (int q = 0; q < nfq; q++) {
-                    O.basis.eval(Q.x[q].data(), v, nullptr);
+                    O.basis.eval_at(Q.x[q].data(), xc.data(), v, nullptr);
                     for (int a = 0; a < nf; a++)
                         for (int j = 0; j < nR; j++) m(a, j) += Q.w[q] * FB.vals(a, q) * v[j];
                 }
@@ -1268,25 +1400,19 @@ int fhg_hho_create(fhg_hho** out, const fhg_hho_params* p)
     for (size_t l = 0; l + 1 < ns.size(); l++) link_coarse(H->levels[l].mesh, H->levels[l + 1].mesh);
     for (size_t l = 0; l < ns.size(); l++) {
         Level& L = H->levels[l];
-        const size_t ne = L.mesh.el.size();
-        L.ops.resize(ne);
-        std::atomic<int> bad{0};
-        const bool want_interp = l > 0;
-        parallel_for(ne, threads, [&](size_t s, size_t e) {
-            for (size_t i = s; i < e; i++) {
-                L.ops[i] = element_ops(L.mesh, (int)i, prm, rules, want_interp);
-                if (!L.ops[i].ok) bad++;
-            }
-        });
-        if (bad) { H->err = "singular local HHO system"; return -2; }
+        if (int rc = element_classes(L, prm, rules, threads, l == 0)) {
+            H->err = "singular local HHO system";
+            return rc;
+        }
         assemble(L, prm, threads, l == 0);
         if (l > 0) prolongation(H->levels[l - 1], L, prm, rules, threads);
-        if (l > 0) {
-            // fine-level element data no longer needed
-            std::vector<ElementOps>().swap(H->levels[l - 1].ops);
+        if (l > 1) {
+            // element data of levels above the finest no longer needed (the finest keeps it for
+            // the L2 error of a solution)
+            std::vector<ElementOps>().swap(H->levels[l - 1].cls_ops);
         }
     }
-    std::vector<ElementOps>().swap(H->levels.back().ops);
+    if (ns.size() > 1) std::vector<ElementOps>().swap(H->levels.back().cls_ops);
     H->rules = rules;
     return 0;
 }
@@ -1347,7 +1473,8 @@ int fhg_hho_l2_error(const fhg_hho* h, const double* x, double* rel_error)
         th.emplace_back([&, t]() {
             const size_t e0 = t * chunk, e1 = std::min(ne, e0 + chunk);
             for (size_t e = e0; e < e1; e++) {
-                const ElementOps O = element_ops(M, (int)e, h->prm, h->rules, true);
+                const ElementOps& O = L.cls_ops[L.cls[e]];
+                const auto xc = centroid(M, (int)e);
                 const int nC = O.nC, nR = O.nR, nFF = nF * nf;
                 std::vector<double> hyb(nC + nFF, 0.0);
                 for (int lf = 0; lf < nF; lf++) {
@@ -1356,7 +1483,7 @@ int fhg_hho_l2_error(const fhg_hho* h, const double* x, double* rel_error)
                     for (int a = 0; a < nf; a++) hyb[nC + lf * nf + a] = x[(size_t)g * nf + a];
                 }
                 for (int c = 0; c < nC; c++) {
-                    double v = O.cell_rhs[c];
+                    double v = L.cell_rhs_e[e * nC + c];
                     for (int j = 0; j < nFF; j++) v += O.solve_cells(c, j) * hyb[nC + j];
                     hyb[c] = v;
                 }
@@ -1366,7 +1493,7 @@ int fhg_hho_l2_error(const fhg_hho* h, const double* x, double* rel_error)
                 const QPts Q = element_points(M, (int)e, h->rules.cell_rhs);
                 double vals[64];
                 for (size_t q = 0; q < Q.w.size(); q++) {
-                    O.basis.eval(Q.x[q].data(), vals, nullptr);
+                    O.basis.eval_at(Q.x[q].data(), xc.data(), vals, nullptr);
                     double uh = 0;
                     for (int i = 0; i < nR; i++) uh += coef[i] * vals[i];
                     double u = 1.0;
