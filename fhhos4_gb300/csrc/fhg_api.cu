@@ -16,10 +16,13 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <type_traits>
 #include <vector>
 
@@ -1312,8 +1315,84 @@ int time_candidate(fhg_ctx* ctx, F run, float* ms_out)
     return FHG_OK;
 }
 
+// Launch shapes found by tune_level, per operator structure (value type, block size, block rows,
+// stored blocks of A and P, colours, padded widths): operators of identical structure (problems of one
+// mesh size and degree, whatever their coefficients) share the best shape, so a process that sets up
+// many of them times each structure once.
+struct TuneKey {
+    int prec, bs, nb, ncol, gs_w, prod_w, p_nbr, r_nbr;
+    long long nnzb, p_blocks;
+    bool operator<(const TuneKey& o) const
+    {
+        return std::tie(prec, bs, nb, ncol, gs_w, prod_w, p_nbr, r_nbr, nnzb, p_blocks) <
+               std::tie(o.prec, o.bs, o.nb, o.ncol, o.gs_w, o.prod_w, o.p_nbr, o.r_nbr, o.nnzb, o.p_blocks);
+    }
+};
+struct TuneShapes {
+    int a_lanes, a_unroll, gs_lanes, gs_unroll, p_lanes, p_unroll, r_lanes, r_unroll;
+    bool prod_slot, gs_slot;
+};
+std::mutex g_tune_mutex;
+std::map<TuneKey, TuneShapes> g_tune_cache;
+
+template <class T>
+int tune_level_uncached(fhg_ctx* ctx, int l);
+
 template <class T>
 int tune_level(fhg_ctx* ctx, int l)
+{
+    using V = LevelVecs<T>;
+    constexpr int PR = V::kPrec;
+    Level& L = ctx->levels[l];
+    const bool coarsest = l == ctx->nlevels - 1;
+    if (ctx->opts.gs_layout != FHG_GS_AUTO) return tune_level_uncached<T>(ctx, l);
+    // the key from the row-major views (what the uncached tuning starts from)
+    const bool ps0 = L.prod_slot[PR], gs0 = L.gs_slot[PR];
+    L.prod_slot[PR] = false;
+    L.gs_slot[PR] = false;
+    BsrView<T>& A = const_cast<BsrView<T>&>(V::A(L));
+    TuneKey key{PR, L.bs, L.nb, L.ncolours, V::gs(L).ell, A.ell, coarsest ? 0 : V::P(L).nbr,
+                coarsest ? 0 : V::R(L).nbr, A.nnzb, coarsest ? 0 : V::P(L).nnzb};
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            const TuneShapes& t = it->second;
+            A.lanes = t.a_lanes;
+            A.unroll = t.a_unroll;
+            L.prod_slot[PR] = t.prod_slot;
+            L.gs_lanes[PR] = t.gs_lanes;
+            L.gs_unroll[PR] = t.gs_unroll;
+            L.gs_slot[PR] = t.gs_slot;
+            if (!coarsest) {
+                BsrView<T>& P = const_cast<BsrView<T>&>(V::P(L));
+                BsrView<T>& R = const_cast<BsrView<T>&>(V::R(L));
+                P.lanes = t.p_lanes; P.unroll = t.p_unroll;
+                R.lanes = t.r_lanes; R.unroll = t.r_unroll;
+            }
+            return FHG_OK;
+        }
+    }
+    L.prod_slot[PR] = ps0;
+    L.gs_slot[PR] = gs0;
+    int rc = tune_level_uncached<T>(ctx, l);
+    if (rc) return rc;
+    const bool ps = L.prod_slot[PR];
+    L.prod_slot[PR] = false;
+    const BsrView<T>& Ar = V::A(L);
+    TuneShapes t{Ar.lanes, Ar.unroll, L.gs_lanes[PR], L.gs_unroll[PR], 0, 1, 0, 1, ps, L.gs_slot[PR]};
+    L.prod_slot[PR] = ps;
+    if (!coarsest) {
+        t.p_lanes = V::P(L).lanes; t.p_unroll = V::P(L).unroll;
+        t.r_lanes = V::R(L).lanes; t.r_unroll = V::R(L).unroll;
+    }
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[key] = t;
+    return FHG_OK;
+}
+
+template <class T>
+int tune_level_uncached(fhg_ctx* ctx, int l)
 {
     using V = LevelVecs<T>;
     Level& L = ctx->levels[l];

@@ -98,7 +98,10 @@ typedef struct {
     int colouring;              /* 1: greedy multicolour ordering (GPU-parallel GS); 0: keep the given order
                                    as colours of one block row each (sequential order, for small checks) */
     int use_graphs;             /* 1: capture one Krylov iteration in a CUDA graph */
-    int autotune;               /* 1: pick lanes-per-block-row of every operator by timing at setup */
+    int autotune;               /* 1: pick the launch shape of every operator by timing at setup (lanes per block row,
+                                   blocks per lane step, row- or slot-major padded views); with gs_layout auto the
+                                   shapes are kept per operator structure in the process, so operators of the same
+                                   sizes (problems of one mesh size and degree) are timed once */
     int max_coarse_rows;        /* dense coarsest solve limit (0: default 8192) */
     int outer_split;            /* FP32 V-cycle only: 1 = the outer FCG operator product in double-FP32
                                    arithmetic (FP32 pairs, ~2^-47 relative per term, on the FP32 pipe);
