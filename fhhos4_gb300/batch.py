@@ -14,6 +14,8 @@ coefficient patches (n = 48, 80, 112, ...), and FCG does not converge.
 """
 from __future__ import annotations
 
+import concurrent.futures as cf
+import os
 import time
 from dataclasses import dataclass
 from typing import List
@@ -38,21 +40,27 @@ def batched_specs(count: int, seed: int = 20261203, n_min: int = 32, n_max: int 
     return [ProblemSpec(int(rng.choice(ns)), int(rng.choice(ks)), int(rng.integers(1, 2 ** 62))) for _ in range(count)]
 
 
+def generate(spec: ProblemSpec, threads: int = 0):
+    """The host hierarchy of one problem: (block size, A_0, [P_l], b, levels)."""
+    H = hho.Hierarchy(2, spec.n, spec.k, source="modes", coefficient="lognormal_patches", contrast=1e3,
+                      checker_blocks=8, seed=spec.seed, max_coarse_rows=1000, threads=threads)
+    try:
+        return H.block_size, H.A(0), [H.P(l) for l in range(H.levels - 1)], H.b(), H.levels
+    finally:
+        H.close()
+
+
 class Problem:
     """One problem: its hierarchy on a set-up context; b uploaded to the context's device buffer."""
 
     def __init__(self, spec: ProblemSpec, device: int = 0, precision: str = "fp64", autotune: bool = True,
-                 tol: float = 1e-8, maxit: int = 200, keep_operator: bool = False):
-        H = hho.Hierarchy(2, spec.n, spec.k, source="modes", coefficient="lognormal_patches", contrast=1e3,
-                          checker_blocks=8, seed=spec.seed, max_coarse_rows=1000)
+                 tol: float = 1e-8, maxit: int = 200, keep_operator: bool = False, generated=None):
+        bs, A0, Ps, b, levels = generated if generated is not None else generate(spec)
         self.spec = spec
-        self.bs = H.block_size
-        A0 = H.A(0)
-        Ps = [H.P(l) for l in range(H.levels - 1)]
-        self.b = H.b()
+        self.bs = bs
+        self.b = b
         self.n = A0.shape[0]
-        self.levels = H.levels
-        H.close()
+        self.levels = levels
         ctx = N.Context(device)
         ctx.set_level(0, self.bs, A0)
         for l, P in enumerate(Ps):
@@ -83,7 +91,14 @@ def build(specs: List[ProblemSpec], device: int = 0, precision: str = "fp64", au
           keep_operator: bool = False):
     """Problems with b uploaded, and a Batch holding all of them. Returns (problems, batch, seconds)."""
     t0 = time.time()
-    probs = [Problem(s, device, precision, autotune, keep_operator=keep_operator) for s in specs]
+    # the host hierarchies in parallel, one generator thread each (ctypes releases the GIL), then
+    # the contexts one after another on the GPU
+    workers = max(1, min(len(specs), os.cpu_count() or 1))
+    with cf.ThreadPoolExecutor(workers) as ex:
+        gen = list(ex.map(lambda sp: generate(sp, threads=1), specs))
+    probs = [Problem(s, device, precision, autotune, keep_operator=keep_operator, generated=g)
+             for s, g in zip(specs, gen)]
+    del gen
     for p in probs:
         p.upload_b()
     batch = N.Batch(device)

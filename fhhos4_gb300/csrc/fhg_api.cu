@@ -115,6 +115,7 @@ struct fhg_ctx {
     double* scal = nullptr;      // [0]=bnorm [1]=dAdp [2]=nr [3]=rz [4]=beta
     double* hist_d = nullptr;
     int* counter_d = nullptr;
+    int* loop_state = nullptr;   // device-loop state (fhg::kLoop*): replacements left, go on, compensated check
     double* nr_host = nullptr;   // pinned
     double* io = nullptr;        // user-numbered I/O scratch (2 * n0)
     // Double-FP32 outer iteration (FP32 V-cycle with the split outer operator): the low part of r,
@@ -156,7 +157,8 @@ struct fhg_batch {
     std::string err;
     std::vector<fhg_ctx*> probs;
     std::vector<long long> epochs;     // setup epoch of every context when the graph was built
-    std::vector<long long> body_kernels;
+    std::vector<long long> body_kernels;   // per problem: kernels of one loop iteration
+    std::vector<long long> check_kernels;  // per problem: kernels of one true-residual check (IF body)
     long long fixed_kernels = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -2061,6 +2063,7 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         (rc = dalloc(ctx, &ctx->kAd[0], n0)) || (rc = dalloc(ctx, &ctx->kAd[1], n0)) ||
         (rc = dalloc(ctx, &ctx->partials, (size_t)8 * fhg::kReduceCtas)) || (rc = dalloc(ctx, &ctx->scal, 8)) ||
         (rc = dalloc(ctx, &ctx->hist_d, (size_t)o.max_iterations + 2)) || (rc = dalloc(ctx, &ctx->counter_d, 1)) ||
+        (rc = dalloc(ctx, &ctx->loop_state, 4)) ||
         (rc = dalloc(ctx, &ctx->io, (size_t)2 * n0)))
         return rc;
     ctx->rlo = nullptr;
@@ -2894,21 +2897,43 @@ void batch_prelude(fhg_ctx* ctx)
     }
     fhg::launch_dot(n, ctx->kb, ctx->kb, part(ctx, 0), s);
     fhg::launch_sqrt_sum(part(ctx, 0), ctx->scal + 0, s);
-    fhg::launch_init_solve(ctx->scal, ctx->counter_d, s);
+    // residual replacement in the device loop as in run_solve: with the FP32 V-cycle, or when asked
+    const bool replace = ctx->opts.krylov == FHG_KRYLOV_FCG &&
+                         (ctx->opts.vcycle_precision == FHG_PREC_FP32 || ctx->opts.replace_residual);
+    fhg::launch_init_solve(ctx->scal, ctx->counter_d, s, ctx->loop_state, replace ? 8 : 0);
     if (outer_df(ctx)) outer_df_start(ctx, ctx->kr);
     else if (ctx->opts.vcycle_precision == FHG_PREC_FP32) fhg::launch_convert<double, float>(n, ctx->kr, L0.b32, s);
 }
 
-// End of a solve: FP64 true residual into scal[5] (||b - A x||), x = Pi^T x'.
-void batch_epilogue(fhg_ctx* ctx)
+// The true residual t = b - A x on the device: FP64, and again in compensated arithmetic when the FP64
+// one misses the tolerance (run_solve's rule); scal[5] = ||t||. replace = 1 (inside the device loop):
+// r = t and go on while replacements are left, when the true residual misses the tolerance.
+void device_true_residual(fhg_ctx* ctx, int replace)
 {
     Level& L0 = ctx->levels[0];
     const long long n = L0.n;
     cudaStream_t s = ctx->stream;
+    const double tol = ctx->opts.tolerance;
     fhg::launch_spmv<double>(L0.A.v, fhg::kSpmvResidual, ctx->kx, ctx->kb, ctx->kt, s);
     fhg::launch_dot(n, ctx->kt, ctx->kt, part(ctx, 0), s);
-    fhg::launch_sqrt_sum(part(ctx, 0), ctx->scal + 5, s);
-    fhg::launch_permute<double>(L0.nb, L0.bs, L0.perm_d, ctx->kx, ctx->io + n, false, s);
+    fhg::launch_check_fp64(part(ctx, 0), ctx->scal, tol, ctx->loop_state, s);
+    fhg::launch_residual_comp(L0.A.v, ctx->kx, ctx->kb, ctx->kt, part(ctx, 1), s, ctx->loop_state + fhg::kLoopNeedComp);
+    fhg::launch_check_comp(part(ctx, 1), ctx->scal, tol, ctx->loop_state, replace, s);
+    if (replace) {
+        const bool df = outer_df(ctx);
+        fhg::launch_replace_apply(n, ctx->loop_state, ctx->kt, ctx->kr, df ? outer_rh(ctx) : nullptr,
+                                  df ? ctx->rlo : nullptr, df ? outer_r2(ctx) : nullptr,
+                                  !df && ctx->opts.vcycle_precision == FHG_PREC_FP32 ? L0.b32 : nullptr, s);
+    }
+}
+
+// End of a solve: the true residual into scal[5] (||b - A x||), x = Pi^T x'.
+void batch_epilogue(fhg_ctx* ctx)
+{
+    Level& L0 = ctx->levels[0];
+    const long long n = L0.n;
+    device_true_residual(ctx, 0);
+    fhg::launch_permute<double>(L0.nb, L0.bs, L0.perm_d, ctx->kx, ctx->io + n, false, ctx->stream);
 }
 
 // Capture `fn(ctx)` on the context's stream into `g` (a new graph when g is null, else the given
@@ -2932,6 +2957,7 @@ int batch_build(fhg_batch* batch)
     cudaGraph_t top = nullptr;
     BCK(cudaGraphCreate(&top, 0));
     batch->body_kernels.assign(batch->probs.size(), 0);
+    batch->check_kernels.assign(batch->probs.size(), 0);
     batch->fixed_kernels = 0;
     int rc = FHG_OK;
     for (size_t i = 0; i < batch->probs.size() && rc == FHG_OK; i++) {
@@ -2943,6 +2969,7 @@ int batch_build(fhg_batch* batch)
         e = capture(ctx, &pre, false, batch_prelude);
         if (e == cudaSuccess) e = cudaGraphAddChildGraphNode(&npre, top, nullptr, 0, pre);
         const long long k1 = fhg::g_kernel_launches.load();
+        long long kc0 = 0, kc1 = 0;
         cudaGraphConditionalHandle h = 0;
         if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, top, 1, cudaGraphCondAssignDefault);
         cudaGraphNodeParams cp = {};
@@ -2952,16 +2979,47 @@ int batch_build(fhg_batch* batch)
         cp.conditional.size = 1;
         if (e == cudaSuccess) e = cudaGraphAddNode(&nwhile, top, &npre, nullptr, 1, &cp);
         if (e == cudaSuccess) {
+            // Body: one FCG iteration, the stopping test, an IF node that checks the true residual once
+            // the recursive one meets the tolerance (replacing r when it misses), then the WHILE
+            // condition.
             cudaGraph_t body = cp.conditional.phGraph_out[0];
+            cudaGraph_t check_body = nullptr;
             ctx->device_loop = true;
             const double tol = ctx->opts.tolerance;
             const int maxit = ctx->opts.max_iterations;
-            e = capture(ctx, &body, true, [&](fhg_ctx* c) {
-                fcg_iteration(c, 0);
-                const long long n = c->levels[0].n;
-                fhg::launch_copy2(n, c->kz[0], c->kz[1], c->kAd[0], c->kAd[1], c->stream);
-                fhg::launch_loop_control(c->scal + 2, c->counter_d, tol, maxit, h, c->stream);
-            });
+            cudaGraphConditionalHandle hc = 0;
+            e = cudaGraphConditionalHandleCreate(&hc, body, 0, cudaGraphCondAssignDefault);
+            if (e == cudaSuccess)
+                e = capture(ctx, &body, true, [&](fhg_ctx* c) {
+                    fcg_iteration(c, 0);
+                    const long long n = c->levels[0].n;
+                    fhg::launch_copy2(n, c->kz[0], c->kz[1], c->kAd[0], c->kAd[1], c->stream);
+                    fhg::launch_loop_decide(c->scal + 2, c->counter_d, tol, maxit, c->loop_state, hc, c->stream);
+                    // the IF node, appended to the graph being captured
+                    cudaStreamCaptureStatus st;
+                    cudaGraph_t g = nullptr;
+                    const cudaGraphNode_t* deps = nullptr;
+                    size_t nd = 0;
+                    cudaError_t ce = cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, nullptr, &nd);
+                    std::vector<cudaGraphNode_t> dv;
+                    if (ce == cudaSuccess) dv.assign(deps, deps + nd);
+                    cudaGraphNodeParams ip = {};
+                    ip.type = cudaGraphNodeTypeConditional;
+                    ip.conditional.handle = hc;
+                    ip.conditional.type = cudaGraphCondTypeIf;
+                    ip.conditional.size = 1;
+                    cudaGraphNode_t nif = nullptr;
+                    if (ce == cudaSuccess) ce = cudaGraphAddNode(&nif, g, dv.data(), nullptr, dv.size(), &ip);
+                    if (ce == cudaSuccess)
+                        ce = cudaStreamUpdateCaptureDependencies(c->stream, &nif, nullptr, 1,
+                                                                 cudaStreamSetCaptureDependencies);
+                    if (ce == cudaSuccess) check_body = ip.conditional.phGraph_out[0];
+                    fhg::launch_loop_finish(c->loop_state, h, c->stream);
+                });
+            if (e == cudaSuccess && !check_body) e = cudaErrorStreamCaptureInvalidated;
+            kc0 = fhg::g_kernel_launches.load();
+            if (e == cudaSuccess) e = capture(ctx, &check_body, true, [&](fhg_ctx* c) { device_true_residual(c, 1); });
+            kc1 = fhg::g_kernel_launches.load();
             ctx->device_loop = false;
         }
         const long long k2 = fhg::g_kernel_launches.load();
@@ -2970,7 +3028,8 @@ int batch_build(fhg_batch* batch)
         const long long k3 = fhg::g_kernel_launches.load();
         fhg::g_kernel_launches -= (k3 - k0);  // captured, not executed
         batch->fixed_kernels += (k1 - k0) + (k3 - k2);
-        batch->body_kernels[i] = k2 - k1;
+        batch->body_kernels[i] = (k2 - k1) - (kc1 - kc0);
+        batch->check_kernels[i] = kc1 - kc0;
         if (pre) cudaGraphDestroy(pre);
         if (post) cudaGraphDestroy(post);
         if (e != cudaSuccess) rc = batch_fail(batch, FHG_ERR_CUDA, "problem %zu: graph construction: %s", i, cudaGetErrorString(e));
@@ -3067,10 +3126,16 @@ int fhg_batch_solve(fhg_batch* batch, fhg_solve_info* infos, double* elapsed_ms)
         fhg_ctx* c = batch->probs[i];
         double sc[6];
         int counter = 0;
+        int state[4] = {0, 0, 0, 0};
         BCK(cudaMemcpy(sc, c->scal, sizeof(sc), cudaMemcpyDeviceToHost));
         BCK(cudaMemcpy(&counter, c->counter_d, sizeof(int), cudaMemcpyDeviceToHost));
+        BCK(cudaMemcpy(state, c->loop_state, sizeof(state), cudaMemcpyDeviceToHost));
         const int its = counter - 1;
         kernels += (long long)its * batch->body_kernels[i];
+        // true-residual checks that ran: one per replacement, plus the last one when replacement is on
+        const bool replace = c->opts.krylov == FHG_KRYLOV_FCG &&
+                             (c->opts.vcycle_precision == FHG_PREC_FP32 || c->opts.replace_residual);
+        if (replace) kernels += (long long)(8 - state[fhg::kLoopReplaceLeft] + 1) * batch->check_kernels[i];
         int st = FHG_OK;
         if (std::isinf(sc[2])) st = FHG_ERR_DIVERGED;
         else if (std::isnan(sc[2])) st = FHG_ERR_NAN;

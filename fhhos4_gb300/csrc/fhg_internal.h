@@ -131,12 +131,22 @@ template <class T>
 void launch_axpy(long long n, double alpha, const T* x, T* y, cudaStream_t s);
 template <class T>
 void launch_lincomb(long long n, double a, const T* c, double b, const T* d, T* out, cudaStream_t s);
-// Device-side solve loop: b0 = a0 and b1 = a1; solve scalars and iteration counter at their start
-// values; the WHILE-node condition from ||r||/||b|| (nr), the counter, tol and maxit.
+// Device-side solve loop: b0 = a0 and b1 = a1; solve scalars, iteration counter and loop state at
+// their start values.
 void launch_copy2(long long n, const double* a0, double* b0, const double* a1, double* b1, cudaStream_t s);
-void launch_init_solve(double* scal, int* counter, cudaStream_t s);
-void launch_loop_control(const double* nr, const int* counter, double tol, int maxit, cudaGraphConditionalHandle h,
-                         cudaStream_t s);
+// Device-loop state per context (int[4]): replacements left, go on, compensated check needed.
+constexpr int kLoopReplaceLeft = 0, kLoopGo = 1, kLoopNeedComp = 2;
+void launch_init_solve(double* scal, int* counter, cudaStream_t s, int* state = nullptr, int replacements = 0);
+// After an iteration of the device loop: state[kLoopGo] and the IF condition `check` (true-residual check).
+void launch_loop_decide(const double* nr, const int* counter, double tol, int maxit, int* state,
+                        cudaGraphConditionalHandle check, cudaStream_t s);
+// True-residual checks (partials of r.r): FP64, then compensated when state[kLoopNeedComp].
+void launch_check_fp64(const double* partials, double* scal, double tol, int* state, cudaStream_t s);
+void launch_check_comp(const double* partials, double* scal, double tol, int* state, int replace, cudaStream_t s);
+void launch_replace_apply(long long n, const int* state, const double* t, double* r, float* rh, float* rl, dfl* r2,
+                          float* b32, cudaStream_t s);
+// The WHILE node's condition from state[kLoopGo].
+void launch_loop_finish(const int* state, cudaGraphConditionalHandle loop, cudaStream_t s);
 // gather: out[b*bs+c] = in[perm[b]*bs+c]; scatter: out[perm[b]*bs+c] = in[b*bs+c].
 template <class T>
 void launch_permute(int nb, int bs, const int* perm, const T* in, T* out, bool gather, cudaStream_t s);

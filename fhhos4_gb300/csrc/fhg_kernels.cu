@@ -752,7 +752,7 @@ __global__ void k_copy2(long long n, const double* __restrict__ a0, double* __re
     }
 }
 
-__global__ void k_init_solve(double* scal, int* counter)
+__global__ void k_init_solve(double* scal, int* counter, int* state, int replacements)
 {
     pdl_wait();
     if (threadIdx.x == 0 && blockIdx.x == 0) {
@@ -761,21 +761,104 @@ __global__ void k_init_solve(double* scal, int* counter)
         scal[3] = 0.0;
         scal[4] = 0.0;
         *counter = 1;
+        if (state) {
+            state[kLoopReplaceLeft] = replacements;
+            state[kLoopGo] = 1;
+            state[kLoopNeedComp] = 0;
+        }
     }
 }
 
-// Continue while iterations < maxit, ||r||/||b|| >= tol and finite (IterativeSolver's stopping
-// test, src/Solver/IterativeSolver.h:224-247). `counter` = iterations done + 1.
-__global__ void k_loop_control(const double* nr, const int* counter, double tol, int maxit,
-                               cudaGraphConditionalHandle handle)
+// After an iteration of the device loop (IterativeSolver's stopping test, IterativeSolver.h:224-247):
+// go on while iterations < maxit and ||r||/||b|| >= tol, finite; once the recursive residual meets
+// tol and replacements are left, set the IF node's condition so that the true residual is checked
+// (k_check_* decide then whether to stop or to replace r and go on).
+__global__ void k_loop_decide(const double* nr, const int* counter, double tol, int maxit, int* state,
+                              cudaGraphConditionalHandle check)
 {
     pdl_wait();
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         const double v = *nr;
         const int it = *counter - 1;
-        const bool go = it < maxit && v >= tol && isfinite(v);
-        cudaGraphSetConditional(handle, go ? 1u : 0u);
+        int go = 0, chk = 0;
+        if (isfinite(v) && it < maxit) {
+            if (!(v < tol)) go = 1;
+            else if (state[kLoopReplaceLeft] > 0) chk = 1;
+        }
+        state[kLoopGo] = go;
+        state[kLoopNeedComp] = 0;
+        cudaGraphSetConditional(check, chk ? 1u : 0u);
     }
+}
+
+// True residual from the FP64 evaluation (partials of r.r): it meets tol (stop), or it is evaluated
+// again in compensated arithmetic (state[kLoopNeedComp] = 1). scal[5] receives ||b - A x||.
+__global__ void __launch_bounds__(kReduceThreads) k_check_fp64(const double* __restrict__ p, double* scal, double tol,
+                                                               int* state)
+{
+    pdl_wait();
+    __shared__ double sh[33];
+    const double rn = sqrt(reduce_partials(p, sh));
+    if (threadIdx.x == 0) {
+        scal[5] = rn;
+        const double bn = scal[0];
+        const double tr = bn > 0.0 ? rn / bn : rn;
+        state[kLoopGo] = 0;
+        state[kLoopNeedComp] = (tr < tol) ? 0 : 1;
+    }
+}
+
+// After the compensated evaluation (when it ran): stop if the true residual meets tol, else replace
+// r (k_replace_apply) and go on while replacements are left. replace = 0: the epilogue's check only.
+__global__ void __launch_bounds__(kReduceThreads) k_check_comp(const double* __restrict__ p, double* scal, double tol,
+                                                               int* state, int replace)
+{
+    pdl_wait();
+    if (state[kLoopNeedComp] == 0) return;
+    __shared__ double sh[33];
+    const double rn = sqrt(reduce_partials(p, sh));
+    if (threadIdx.x == 0) {
+        scal[5] = rn;
+        const double bn = scal[0];
+        const double tr = bn > 0.0 ? rn / bn : rn;
+        if (replace && !(tr < tol) && isfinite(tr) && state[kLoopReplaceLeft] > 0) {
+            state[kLoopReplaceLeft]--;
+            state[kLoopGo] = 1;
+            scal[2] = tr;
+        } else {
+            state[kLoopGo] = 0;
+        }
+    }
+}
+
+// Residual replacement when state[kLoopGo]: r = t (the true residual) and the V-cycle's right-hand
+// side from it (FP32 pair (rh, rl) and optionally interleaved pairs r2, or FP32 b32).
+__global__ void __launch_bounds__(kReduceThreads) k_replace_apply(long long n, const int* __restrict__ state,
+                                                                  const double* __restrict__ t, double* __restrict__ r,
+                                                                  float* __restrict__ rh, float* __restrict__ rl,
+                                                                  dfl* __restrict__ r2, float* __restrict__ b32)
+{
+    pdl_wait();
+    if (state[kLoopGo] == 0) return;
+    for (long long i = (long long)blockIdx.x * kReduceThreads + threadIdx.x; i < n; i += kRedStride) {
+        const double v = t[i];
+        r[i] = v;
+        if (rh) {
+            float h, l;
+            df_split(v, h, l);
+            rh[i] = h;
+            rl[i] = l;
+            if (r2) r2[i] = dfl(h, l);
+        } else if (b32) {
+            b32[i] = (float)v;
+        }
+    }
+}
+
+__global__ void k_loop_finish(const int* state, cudaGraphConditionalHandle loop)
+{
+    pdl_wait();
+    if (threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(loop, state[kLoopGo] ? 1u : 0u);
 }
 
 }  // namespace
@@ -787,16 +870,42 @@ void launch_copy2(long long n, const double* a0, double* b0, const double* a1, d
     g_kernel_launches++;
 }
 
-void launch_init_solve(double* scal, int* counter, cudaStream_t s)
+void launch_init_solve(double* scal, int* counter, cudaStream_t s, int* state, int replacements)
 {
-    pdl_launch(k_init_solve, 1, 32, 0, s, scal, counter);
+    pdl_launch(k_init_solve, 1, 32, 0, s, scal, counter, state, replacements);
     g_kernel_launches++;
 }
 
-void launch_loop_control(const double* nr, const int* counter, double tol, int maxit, cudaGraphConditionalHandle h,
-                         cudaStream_t s)
+void launch_loop_decide(const double* nr, const int* counter, double tol, int maxit, int* state,
+                        cudaGraphConditionalHandle check, cudaStream_t s)
 {
-    pdl_launch(k_loop_control, 1, 32, 0, s, nr, counter, tol, maxit, h);
+    pdl_launch(k_loop_decide, 1, 32, 0, s, nr, counter, tol, maxit, state, check);
+    g_kernel_launches++;
+}
+
+void launch_check_fp64(const double* partials, double* scal, double tol, int* state, cudaStream_t s)
+{
+    pdl_launch(k_check_fp64, 1, kReduceThreads, 0, s, partials, scal, tol, state);
+    g_kernel_launches++;
+}
+
+void launch_check_comp(const double* partials, double* scal, double tol, int* state, int replace, cudaStream_t s)
+{
+    pdl_launch(k_check_comp, 1, kReduceThreads, 0, s, partials, scal, tol, state, replace);
+    g_kernel_launches++;
+}
+
+void launch_replace_apply(long long n, const int* state, const double* t, double* r, float* rh, float* rl, dfl* r2,
+                          float* b32, cudaStream_t s)
+{
+    pdl_launch(k_replace_apply, kReduceCtas, kReduceThreads, 0, s, n, state, t, r, rh, rl, r2, b32);
+    g_kernel_launches++;
+}
+
+// Launched without programmatic serialization: it follows a conditional node, not a kernel.
+void launch_loop_finish(const int* state, cudaGraphConditionalHandle loop, cudaStream_t s)
+{
+    k_loop_finish<<<1, 32, 0, s>>>(state, loop);
     g_kernel_launches++;
 }
 
