@@ -2999,8 +2999,9 @@ int batch_build(fhg_batch* batch)
                     cudaStreamCaptureStatus st;
                     cudaGraph_t g = nullptr;
                     const cudaGraphNode_t* deps = nullptr;
-                    size_t nd = 0;
-                    cudaError_t ce = cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, nullptr, &nd);
+                    const cudaGraphEdgeData* edges = nullptr;   // queried (a query without them can be lossy),
+                    size_t nd = 0;                              // then the IF node gets default full edges
+                    cudaError_t ce = cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &g, &deps, &edges, &nd);
                     std::vector<cudaGraphNode_t> dv;
                     if (ce == cudaSuccess) dv.assign(deps, deps + nd);
                     cudaGraphNodeParams ip = {};
