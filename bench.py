@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=0,
                     help="also run the batched workload: this many 2D problems in one graph launch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="only the headline (config 2): skip configs 3 and 5 and the 512-problem batch (config 4)")
     ap.add_argument("--cpu-sample-iterations", type=int, default=2)
     return ap.parse_args()
 
@@ -206,11 +208,22 @@ def workload_config(args, unknowns=None, levels=None):
     return cfg
 
 
+def checker_blocks(args):
+    """Blocks per direction of the coefficient field: 4 x 4 x 4 for the checkerboard, one block per
+    4^3 cubes for the rotated anisotropic tensor, 8 x 8 patches for the log-uniform field."""
+    if args.coefficient == "anisotropic":
+        return max(1, args.n // 4)
+    if args.coefficient == "lognormal_patches":
+        return 8
+    return 4
+
+
 def generate(args, keep=False):
     from fhhos4_gb300 import hho
     t0 = time.perf_counter()
     H = hho.Hierarchy(args.dim, args.n, args.k, coefficient=args.coefficient, contrast=args.contrast,
-                      source=args.source, max_coarse_rows=args.max_coarse_rows)
+                      source=args.source, max_coarse_rows=args.max_coarse_rows, checker_blocks=checker_blocks(args),
+                      seed=getattr(args, "seed", 20261203))
     As = [H.A(l) for l in range(H.levels)]
     Ps = [H.P(l) for l in range(H.levels - 1)]
     b = H.b()
@@ -253,6 +266,57 @@ def bytes_spmv(nnzb, nb_rows, n_in, n_out, bs, p, residual=False, add=False):
     return b
 
 
+def measure_methods(ctx, dist, dev, b_dev, x_dev, maxit, methods, warmup, steps, params=None, wmeta=None, bs=3):
+    """Solve b (resident on the device) with every method on one context: `warmup` untimed solves, then
+    `steps` timed ones (CUDA events on the library's stream, max over ranks). methods: name ->
+    (precision, pre, post, npre, npost, (coarse npre, coarse npost), learned)."""
+    import torch
+    results, launches, clocks, solutions = {}, {}, {}, {}
+    for name, (prec, pre, post, npre, npost, coarse, use_learned) in methods.items():
+        ctx.set_cycle(pre, post, npre, npost, 1)
+        ctx.set_coarse_smoothing(*coarse)
+        ctx.set_vcycle_precision(prec)
+        if use_learned:
+            ctx.set_learned(params, "fallback")
+        elif bs <= 4 and params is not None:
+            ctx.set_learned(None, "off")
+
+        def solve_device():
+            rc, hist, info = ctx.solve_device(b_dev.data_ptr(), x_dev.data_ptr(), maxit)
+            if rc != 0:
+                ctx._check(rc)
+            return hist, info
+
+        for _ in range(warmup):
+            solve_device()
+        dist.barrier()
+        torch.cuda.synchronize()
+        sampler = ClockSampler(dev)
+        sampler.start()
+        k0 = ctx.kernel_launches()
+        times, iters = [], []
+        for _ in range(steps):
+            hist, info = solve_device()
+            times.append(info.solve_ms / 1e3)
+            iters.append(info.iterations)
+        torch.cuda.synchronize()
+        launches[name] = ctx.kernel_launches() - k0
+        clocks[name] = sampler.stop()
+        dist.barrier()
+        t_step = dist.max(float(np.mean(times)))
+        solutions[name] = x_dev.cpu().numpy()
+        results[name] = dict(s=t_step, iterations=iters[-1], true_rel_residual=info.true_relative_residual,
+                             final=float(hist[-1]),
+                             cycle=f"V({npre},{npost}) {pre}/{post}" + (
+                                 f", V({coarse[0]},{coarse[1]}) on levels >= 1" if min(coarse) >= 0 else ""),
+                             vcycle_precision=prec)
+        if use_learned:
+            results[name]["learned_iterations"] = info.learned_iterations
+            results[name]["fallback_reference_rate"] = ctx.learned_reference_rate()
+            results[name]["network"] = wmeta
+    return results, launches, clocks, solutions
+
+
 def run_ours(args, dist: Dist):
     import torch
     from fhhos4_gb300 import _native as N
@@ -286,17 +350,6 @@ def run_ours(args, dist: Dist):
     x_dev = torch.empty_like(b_dev)
     torch.cuda.synchronize()
 
-    def solve_device():
-        rc, hist, info = ctx.solve_device(b_dev.data_ptr(), x_dev.data_ptr(), o.max_iterations)
-        if rc != 0:
-            ctx._check(rc)
-        return hist, info
-
-    def true_residual():
-        x = x_dev.cpu().numpy()
-        r = ctx.apply(0, N.OP_RESIDUAL, x, b, n0)
-        return float(np.linalg.norm(r) / np.linalg.norm(b))
-
     # Methods on the same hierarchy and context:
     #   plain        the reference's method, V(1,1) bgs/rbgs, in FP64-class arithmetic: the V-cycle and
     #                the outer FCG on FP32 pairs (FHG_PREC_DF, ~2^-47 per term on the FP32 pipe), x and
@@ -318,45 +371,8 @@ def run_ours(args, dist: Dist):
                "fast": ("fp32", fast_pre, fast_post, fast_npre, fast_npost, fast_coarse, False)}
     if have_learned:
         methods["learned"] = ("fp32", fast_pre, fast_post, fast_npre, fast_npost, fast_coarse, True)
-    results = {}
-    launches = {}
-    clocks = {}
-    solutions = {}
-    learned_its = {}
-    for name, (prec, pre, post, npre, npost, coarse, use_learned) in methods.items():
-        ctx.set_cycle(pre, post, npre, npost, 1)
-        ctx.set_coarse_smoothing(*coarse)
-        ctx.set_vcycle_precision(prec)
-        if use_learned:
-            ctx.set_learned(params, "fallback")
-        elif bs <= 4:
-            ctx.set_learned(None, "off")
-        for _ in range(args.warmup):
-            solve_device()
-        dist.barrier()
-        torch.cuda.synchronize()
-        sampler = ClockSampler(dev)
-        sampler.start()
-        k0 = ctx.kernel_launches()
-        times, iters = [], []
-        for _ in range(args.steps):
-            hist, info = solve_device()
-            times.append(info.solve_ms / 1e3)
-            iters.append(info.iterations)
-        torch.cuda.synchronize()
-        launches[name] = ctx.kernel_launches() - k0
-        clocks[name] = sampler.stop()
-        dist.barrier()
-        t_step = dist.max(float(np.mean(times)))
-        solutions[name] = x_dev.cpu().numpy()
-        results[name] = dict(s=t_step, iterations=iters[-1], true_rel_residual=true_residual(), final=float(hist[-1]),
-                             cycle=f"V({npre},{npost}) {pre}/{post}" + (
-                                 f", V({coarse[0]},{coarse[1]}) on levels >= 1" if min(coarse) >= 0 else ""),
-                             vcycle_precision=prec)
-        if use_learned:
-            results[name]["learned_iterations"] = info.learned_iterations
-            results[name]["fallback_reference_rate"] = ctx.learned_reference_rate()
-            results[name]["network"] = wmeta
+    results, launches, clocks, solutions = measure_methods(ctx, dist, dev, b_dev, x_dev, o.max_iterations, methods,
+                                                           args.warmup, args.steps, params, wmeta, bs)
     x64 = solutions["plain"]
     for name in methods:
         results[name]["rel_diff_vs_plain_fp64"] = float(np.linalg.norm(solutions[name] - x64) / np.linalg.norm(x64))
@@ -512,26 +528,31 @@ def run_ours(args, dist: Dist):
         "cpu_baseline": cpu,
     }
     ctx.close()
+    if not args.no_extra:
+        for name in EXTRA_CONFIGS:
+            line[name] = run_extra(args, dist, name)
+        args.batch = args.batch or 512
     if args.batch > 0:
-        line["batched"] = run_batched(args, dist)
+        line["config4_batched"] = run_batched(args, dist)
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
 
 
 def run_batched(args, dist: Dist):
-    """Many 2D problems of uneven size in one graph launch against the same problems solved one
-    after another (fhg_solve_device each)."""
+    """Config 4: many 2D problems of uneven size in one graph launch against the same problems solved
+    one after another (fhg_solve_device each), with the FP32 and the FP64-class (pair) V-cycles."""
     import torch
     from fhhos4_gb300 import batch as BT
     specs = BT.batched_specs(args.batch)
     t0 = time.perf_counter()
-    probs, batch, build_s = BT.build(specs, device=dist.local_rank, precision="fp32", autotune=True)
+    probs, batch, build_s = BT.build(specs, device=dist.local_rank, precision="fp32", autotune=True, extra=("df",))
     dofs = sum(p.n for p in probs)
     out = {"problems": len(probs), "unknowns": int(dofs), "n_range": [min(s.n for s in specs), max(s.n for s in specs)],
            "k_counts": {k: sum(1 for s in specs if s.k == k) for k in (1, 2, 3)},
-           "method": "V(1,1) bgs/rbgs inside FP64 FCG(1), Galerkin coarse operators, autotuned launch shapes",
+           "method": ("V(1,1) bgs/rbgs inside FP64 FCG(1), Galerkin coarse operators, autotuned launch shapes; "
+                      "residual replacement in the device loop (FP32); the FP64-class run keeps the reference loop"),
            "setup_s": round(time.perf_counter() - t0, 1)}
-    for prec in ("fp32", "fp64"):
+    for prec in ("fp32", "df"):
         for p in probs:
             p.ctx.set_vcycle_precision(prec)
             p.upload_b()
@@ -556,11 +577,109 @@ def run_batched(args, dist: Dist):
                      "speedup_batched_vs_sequential": round(seq_ms / batched_ms, 2),
                      "dofs_per_s": round(dofs / (batched_ms * 1e-3), 1), "iterations_min_max": [min(its), max(its)],
                      "true_rel_residual_median_worst": [trues[len(trues) // 2], trues[-1]],
-                     "problems_true_below_tol": sum(1 for t in trues if t < 1e-8), "status": rc}
+                     "problems_true_below_tol": sum(1 for t in trues if t < 1e-8), "status": rc,
+                     "timing": f"median of {max(3, args.steps // 2)} launches after 2 untimed ones"}
     batch.close()
     for p in probs:
         p.close()
     return out
+
+
+# The other configurations, measured in the same run beside the headline (config 2). Each is a
+# namespace of bench options and the methods it compares; every solve is judged by its true residual.
+EXTRA_CONFIGS = {
+    # Config 3: 48^3 tetrahedra, k = 2, 4x4x4 checkerboard 1 / 1e6, f = 1, Galerkin coarse operators,
+    # residual replacement in every precision (compensated true residual where FP64 misses 1e-8).
+    "config3": dict(dim=3, n=48, k=2, coefficient="checkerboard", contrast=1e6, source="one", max_coarse_rows=2000,
+                    galerkin=True, replace_residual=True,
+                    methods={"plain_fp64": ("df", "bgs", "rbgs", 1, 1, (-1, -1), False),
+                             "fp64_v22": ("df", "bgs", "rbgs", 2, 2, (-1, -1), False),
+                             "fp32_v22": ("fp32", "bgs", "rbgs", 2, 2, (-1, -1), False)}),
+    # Config 5: 32^3 tetrahedra, k = 1, diag(1, 1, eps) rotated per 4^3-cube block, eps log-uniform in
+    # [1e-3, 1], a field seed the network never saw; plain, FP32 fast cycle, and the learned step.
+    "config5": dict(dim=3, n=32, k=1, coefficient="anisotropic", contrast=1.0, source="one", max_coarse_rows=1000,
+                    galerkin=False, replace_residual=False, seed=987654321,
+                    methods={"plain_fp64": ("df", "bgs", "rbgs", 1, 1, (-1, -1), False),
+                             "fp32_fast": ("fp32", "bgs", "rbgs", 3, 3, (4, 4), False),
+                             "learned_fast": ("fp32", "bgs", "rbgs", 3, 3, (4, 4), True),
+                             "fp32_v22": ("fp32", "bgs", "rbgs", 2, 2, (-1, -1), False),
+                             "learned_v22": ("fp32", "bgs", "rbgs", 2, 2, (-1, -1), True)}),
+}
+CONFIG5_WEIGHTS = "learned_tet3d_k1_config5.npz"
+
+
+def run_extra(args, dist: Dist, name: str):
+    """One extra configuration: host hierarchy, set-up context (FP32, pair and FP64 copies, autotuned),
+    its methods timed (1 untimed and 2 timed solves each), true residuals, iterations."""
+    import copy
+    import torch
+    from fhhos4_gb300 import _native as N
+    from fhhos4_gb300 import learned as LN
+    spec = dict(EXTRA_CONFIGS[name])
+    methods = spec.pop("methods")
+    a = copy.copy(args)
+    for k, v in spec.items():
+        setattr(a, k, v)
+    dev = dist.local_rank
+    As, Ps, b, bs, gen_s, H = generate(a, keep=True)
+    ctx = N.Context(dev)
+    t0 = time.perf_counter()
+    for l, A in enumerate(As):
+        ctx.set_level(l, bs, A)
+    for l, P in enumerate(Ps):
+        ctx.set_prolongation(l, P)
+    ctx.set_face_tensors(H.face_tensors(0))
+    H.close()
+    o = N.default_options()
+    o.vcycle_precision = N.PRECISION["fp32"]
+    o.extra_precisions = 1 << N.PRECISION["df"]
+    o.galerkin = 1 if a.galerkin else 0
+    o.replace_residual = 1 if a.replace_residual else 0
+    o.autotune = 1
+    o.max_iterations = 300
+    ctx.setup(len(As), o)
+    setup_s = time.perf_counter() - t0
+    params = wmeta = None
+    if any(m[-1] for m in methods.values()):
+        path = os.path.join(LN.WEIGHTS_DIR, CONFIG5_WEIGHTS)
+        params, wmeta = LN.load_params(path if os.path.exists(path) else LN.DEFAULT_WEIGHTS)
+    b_dev = torch.from_numpy(b).to(f"cuda:{dev}")
+    x_dev = torch.empty_like(b_dev)
+    torch.cuda.synchronize()
+    results, launches, _, solutions = measure_methods(ctx, dist, dev, b_dev, x_dev, o.max_iterations, methods, 1, 2,
+                                                      params, wmeta, bs)
+    ctx.close()
+    n0 = As[0].shape[0]
+    ref = solutions[next(iter(methods))]
+    for m in methods:
+        results[m]["rel_diff_vs_plain_fp64"] = float(np.linalg.norm(solutions[m] - ref) / np.linalg.norm(ref))
+        results[m]["s"] = round(results[m]["s"], 5)
+        results[m]["meets_1e-8"] = bool(results[m]["true_rel_residual"] < 1e-8)
+    out = {"workload": workload_config(a, n0, len(As)), "methods": results,
+           "timing": "1 untimed and 2 timed solves per method, CUDA events, b resident in HBM",
+           "setup_s": {"hierarchy_generation": round(gen_s, 2), "gpu_setup": round(setup_s, 2)}}
+    if "learned_fast" in results:
+        out["learned_vs_fast"] = round(results["fp32_fast"]["s"] / results["learned_fast"]["s"], 3)
+        out["learned_vs_fast_v22"] = round(results["fp32_v22"]["s"] / results["learned_v22"]["s"], 3)
+        out["speedup_learned_vs_plain_fp64"] = round(results["plain_fp64"]["s"] / results["learned_fast"]["s"], 3)
+        out["energy_ratio_one_cycle"] = config5_energy_ratios(a, dev, params)
+    return out
+
+
+def config5_energy_ratios(a, dev, params, samples: int = 4):
+    """|e1|_A^2 / |e|_A^2 after one V(2,2) cycle, plain and with the learned step, for seeded errors
+    left by one plain cycle on the config-5 field (mean over `samples`)."""
+    from fhhos4_gb300 import learned as LN
+    f = LN.Field(LN.FieldSpec(n=a.n, seed=a.seed), device=dev, nu=(2, 2))
+    try:
+        f.ctx.set_learned(params, "always")
+        ss = LN.make_samples(f, samples, cycles=(1,), seed=4242)
+        plain = [LN.energy_ratio(f, e, False) for _, _, e in ss]
+        learned = [LN.energy_ratio(f, e, True) for _, _, e in ss]
+    finally:
+        f.close()
+    return {"cycle": "V(2,2) bgs/rbgs", "plain": round(float(np.mean(plain)), 4),
+            "learned": round(float(np.mean(learned)), 4), "samples": samples}
 
 
 def run_reference(args, dist: Dist):

@@ -54,7 +54,7 @@ class Problem:
     """One problem: its hierarchy on a set-up context; b uploaded to the context's device buffer."""
 
     def __init__(self, spec: ProblemSpec, device: int = 0, precision: str = "fp64", autotune: bool = True,
-                 tol: float = 1e-8, maxit: int = 200, keep_operator: bool = False, generated=None):
+                 tol: float = 1e-8, maxit: int = 200, keep_operator: bool = False, generated=None, extra=()):
         bs, A0, Ps, b, levels = generated if generated is not None else generate(spec)
         self.spec = spec
         self.bs = bs
@@ -68,6 +68,7 @@ class Problem:
         o = N.default_options()
         o.galerkin = 1
         o.vcycle_precision = N.PRECISION[precision]
+        o.extra_precisions = sum(1 << N.PRECISION[p] for p in set(extra))
         o.autotune = 1 if autotune else 0
         o.tolerance = tol
         o.max_iterations = maxit
@@ -88,7 +89,7 @@ class Problem:
 
 
 def build(specs: List[ProblemSpec], device: int = 0, precision: str = "fp64", autotune: bool = True,
-          keep_operator: bool = False):
+          keep_operator: bool = False, extra=()):
     """Problems with b uploaded, and a Batch holding all of them. Returns (problems, batch, seconds)."""
     t0 = time.time()
     # the host hierarchies in parallel, one generator thread each (ctypes releases the GIL), then
@@ -96,7 +97,7 @@ def build(specs: List[ProblemSpec], device: int = 0, precision: str = "fp64", au
     workers = max(1, min(len(specs), os.cpu_count() or 1))
     with cf.ThreadPoolExecutor(workers) as ex:
         gen = list(ex.map(lambda sp: generate(sp, threads=1), specs))
-    probs = [Problem(s, device, precision, autotune, keep_operator=keep_operator, generated=g)
+    probs = [Problem(s, device, precision, autotune, keep_operator=keep_operator, generated=g, extra=extra)
              for s, g in zip(specs, gen)]
     del gen
     for p in probs:
