@@ -73,22 +73,27 @@ class FieldSpec:
     max_coarse_rows: int = 1000
 
 
+def generate_field(spec: FieldSpec, source: str = "sine", threads: int = 0):
+    """The host hierarchy of a field: (block size, [A_l], [P_l], b, face tensors of level 0)."""
+    blocks = spec.checker_blocks or max(1, spec.n // 4)
+    H = hho.Hierarchy(3, spec.n, spec.k, max_coarse_rows=spec.max_coarse_rows, source=source,
+                      coefficient=spec.coefficient, contrast=spec.contrast, checker_blocks=blocks,
+                      eps_min=spec.eps_min, seed=spec.seed, threads=threads)
+    try:
+        return (H.block_size, [H.A(l) for l in range(H.levels)], [H.P(l) for l in range(H.levels - 1)], H.b(),
+                H.face_tensors(0))
+    finally:
+        H.close()
+
+
 class Field:
     """One coefficient field: hierarchy on a GPU context (FP32 V-cycle) plus its face tensors."""
 
     def __init__(self, spec: FieldSpec, device: int = 0, smoothers=("bgs", "rbgs"), nu=(1, 1), autotune=False,
-                 source: str = "sine", coarse_nu=(-1, -1)):
-        blocks = spec.checker_blocks or max(1, spec.n // 4)
-        H = hho.Hierarchy(3, spec.n, spec.k, max_coarse_rows=spec.max_coarse_rows, source=source,
-                          coefficient=spec.coefficient, contrast=spec.contrast, checker_blocks=blocks,
-                          eps_min=spec.eps_min, seed=spec.seed)
+                 source: str = "sine", coarse_nu=(-1, -1), generated=None):
         self.spec = spec
-        self.bs = H.block_size
-        self.As = [H.A(l) for l in range(H.levels)]
-        Ps = [H.P(l) for l in range(H.levels - 1)]
-        self.b = H.b()
-        self.tensors = H.face_tensors(0)
-        self.hierarchy = H
+        self.bs, self.As, Ps, self.b, self.tensors = generated if generated is not None else generate_field(spec, source)
+        self.hierarchy = None
         self.n = self.As[0].shape[0]
         self.nb = self.n // self.bs
         ctx = N.Context(device)
@@ -178,19 +183,38 @@ class TrainLog:
 def train(net: N.Net, fields: int = 64, n: int = 16, samples_per_field: int = 4, steps_per_sample: int = 1,
           lr: float = 2e-3, lr_min: float = 1e-4, weight_decay: float = 0.0, seed0: int = 1000, device: int = 0,
           spec_kw: Optional[dict] = None, log_every: int = 0, smoothers=("bgs", "rbgs"), nu=(1, 1),
-          identity_every: int = 0, coarse_nu=(-1, -1)) -> TrainLog:
+          identity_every: int = 0, coarse_nu=(-1, -1), sizes=None, prefetch: int = 0) -> TrainLog:
     """Stream `fields` seeded fields (seeds seed0, seed0+1, ...) and take Adam steps on their samples;
-    identity_every = m > 0 makes every m-th field the identity coefficient instead."""
+    identity_every = m > 0 makes every m-th field the identity coefficient instead. sizes: a list of
+    (n, count) replacing (n, fields), fields taken in that order. prefetch > 0: that many host
+    threads generate the next fields' hierarchies while the GPU trains on the current one."""
+    import concurrent.futures as cf
     log = TrainLog()
+    plan = [m for m, c in (sizes or [(n, fields)]) for _ in range(c)]
+    fields = len(plan)
     total = max(1, fields * samples_per_field * steps_per_sample)
     t0 = time.time()
     step = 0
+    specs = []
     for fi in range(fields):
         kw = dict(spec_kw or {})
         if identity_every and fi % identity_every == identity_every - 1:
             kw["coefficient"] = "identity"
-        spec = FieldSpec(n=n, seed=seed0 + fi, **kw)
-        f = Field(spec, device=device, smoothers=smoothers, nu=nu, coarse_nu=coarse_nu)
+        specs.append(FieldSpec(n=plan[fi], seed=seed0 + fi, **kw))
+    ex = cf.ThreadPoolExecutor(prefetch) if prefetch > 0 else None
+    futures = {}
+
+    def ahead(i):
+        if ex is not None:
+            for j in range(i, min(fields, i + 2 * prefetch)):
+                if j not in futures:
+                    futures[j] = ex.submit(generate_field, specs[j], "sine", 2)
+
+    for fi in range(fields):
+        spec = specs[fi]
+        ahead(fi)
+        gen = futures.pop(fi).result() if fi in futures else None
+        f = Field(spec, device=device, smoothers=smoothers, nu=nu, coarse_nu=coarse_nu, generated=gen)
         try:
             samples = make_samples(f, samples_per_field, seed=seed0 * 7919 + fi)
             for _ in range(steps_per_sample):
@@ -206,6 +230,8 @@ def train(net: N.Net, fields: int = 64, n: int = 16, samples_per_field: int = 4,
             recent = log.losses[-log_every * samples_per_field * steps_per_sample:]
             print(json.dumps({"fields": fi + 1, "mean_loss": float(np.mean(recent)),
                               "s": round(time.time() - t0, 1)}), flush=True)
+    if ex is not None:
+        ex.shutdown(wait=True, cancel_futures=True)
     log.steps = step
     log.seconds = time.time() - t0
     return log
@@ -226,15 +252,20 @@ def _cli():
     ap.add_argument("--nu", default="2,2", help="pre,post smoothing steps of the cycle the step corrects")
     ap.add_argument("--identity-every", type=int, default=4, help="every m-th field has K = I (0: none)")
     ap.add_argument("--coarse-nu", default="-1,-1", help="pre,post smoothing steps on levels >= 1 (-1: as --nu)")
+    ap.add_argument("--sizes", default="", help="n:count,... fields per mesh size in order (replaces --n/--fields)")
+    ap.add_argument("--prefetch", type=int, default=0, help="host threads generating the next fields ahead")
     a = ap.parse_args()
     nu = tuple(int(v) for v in a.nu.split(","))
     coarse_nu = tuple(int(v) for v in a.coarse_nu.split(","))
     net = N.Net(0)
     p0 = load_params(a.init)[0] if a.init else init_params(a.seed)
     net.set_params(p0)
+    sizes = [tuple(int(v) for v in t.split(":")) for t in a.sizes.split(",")] if a.sizes else None
     log = train(net, fields=a.fields, n=a.n, samples_per_field=a.samples, steps_per_sample=a.repeat, lr=a.lr,
-                seed0=a.seed, log_every=a.log_every, nu=nu, identity_every=a.identity_every, coarse_nu=coarse_nu)
-    meta = {"fields": a.fields, "n": a.n, "k": 1, "coefficient": "anisotropic diag(1,1,eps), eps log-U[1e-3,1], "
+                seed0=a.seed, log_every=a.log_every, nu=nu, identity_every=a.identity_every, coarse_nu=coarse_nu,
+                sizes=sizes, prefetch=a.prefetch)
+    meta = {"fields": log.fields, "n": a.n if not sizes else {str(m): c for m, c in sizes}, "k": 1,
+            "coefficient": "anisotropic diag(1,1,eps), eps log-U[1e-3,1], "
             "random rotation per 4^3 block" + (f"; every {a.identity_every}th field K = I" if a.identity_every else ""),
             "cycle": f"V({nu[0]},{nu[1]}) bgs/rbgs" + (f", V({coarse_nu[0]},{coarse_nu[1]}) on levels >= 1"
                                                        if min(coarse_nu) >= 0 else ""),
