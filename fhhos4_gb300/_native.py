@@ -63,7 +63,8 @@ class Options(C.Structure):
                 ("colouring", C.c_int), ("use_graphs", C.c_int), ("autotune", C.c_int),
                 ("max_coarse_rows", C.c_int), ("outer_split", C.c_int), ("w_loops", C.c_int),
                 ("galerkin", C.c_int), ("coarse_pre_iterations", C.c_int), ("coarse_post_iterations", C.c_int),
-                ("gs_layout", C.c_int), ("extra_precisions", C.c_int), ("replace_residual", C.c_int)]
+                ("gs_layout", C.c_int), ("extra_precisions", C.c_int), ("replace_residual", C.c_int),
+                ("fused_coarse", C.c_int)]
 
 
 class SolveInfo(C.Structure):

@@ -8,6 +8,7 @@
 // scalars on the device, one CUDA graph per iteration, one 8-byte read-back of the
 // normalised residual per iteration for the stopping test.
 #include "fhg.h"
+#include "fhg_coarse.h"
 #include "fhg_internal.h"
 
 #include <algorithm>
@@ -146,6 +147,7 @@ struct fhg_ctx {
     long long graph_l_kernels[2] = {0, 0};
     int graphs_l_built = 0;
     bool device_loop = false;          // capturing for the device-side loop: no host read-back
+    int fused_from = -1;               // first level of the coarse sub-cycle run as one cluster launch (-1: none)
     long long epoch = 0;               // incremented by every setup (batched graphs hold its buffers)
 };
 
@@ -1047,6 +1049,68 @@ void kcycle_fcg(fhg_ctx* ctx, int m, T* r, T* x)
     fhg::launch_lincomb<T>(n, alpha1 / rho1 - gamma * alpha2 / (rho1 * rho2), c, alpha2 / rho2, d, x, s);
 }
 
+// The coarse sub-cycle from level l down as one cluster launch (fhg_coarse.cu), when setup found the
+// levels small enough and the cycle is one it covers: GS / SOR smoothers, V or W cycle, FP32 or pair
+// values. Returns false when the caller must run the sub-cycle launch by launch.
+template <class T>
+bool fused_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
+{
+    if constexpr (std::is_same<T, double>::value) {
+        return false;
+    } else {
+        using V = LevelVecs<T>;
+        const fhg_options& o = ctx->opts;
+        if (!o.fused_coarse || l != ctx->fused_from || l <= 0 || o.w_loops == FHG_CYCLE_K || !is_gs(o.pre_smoother) ||
+            !is_gs(o.post_smoother))
+            return false;
+        Level& L0 = ctx->levels[l];
+        if (b != V::b(L0) || x != V::x(L0)) return false;
+        auto dir = [](int code) {
+            switch (code) {
+            case FHG_SMOOTHER_BGS: return fhg::kFusedForward;
+            case FHG_SMOOTHER_RBGS: return fhg::kFusedBackward;
+            case FHG_SMOOTHER_SBGS: return fhg::kFusedSymmetric;
+            case FHG_SMOOTHER_ABGS: return fhg::kFusedAlternatingForward;
+            default: return fhg::kFusedAlternatingBackward;
+            }
+        };
+        fhg::FusedCycle<T> P;
+        P.nlev = ctx->nlevels - l;
+        P.pre = dir(o.pre_smoother);
+        P.post = dir(o.post_smoother);
+        P.npre = o.coarse_pre_iterations >= 0 ? o.coarse_pre_iterations : o.pre_iterations;
+        P.npost = o.coarse_post_iterations >= 0 ? o.coarse_post_iterations : o.post_iterations;
+        P.w_loops = o.w_loops > 1 ? o.w_loops : 1;
+        P.x_zero = x_zero ? 1 : 0;
+        P.omega = T(o.omega);
+        for (int k = 0; k < P.nlev; k++) {
+            Level& L = ctx->levels[l + k];
+            fhg::FusedLevel<T>& F = P.lev[k];
+            F.nb = L.nb;
+            F.x = V::x(L);
+            F.b = V::b(L);
+            F.r = V::r(L);
+            if (l + k == ctx->nlevels - 1) {
+                P.n_coarse = L.n;
+                P.cinv = L.cinv;
+                continue;
+            }
+            F.ncol = L.ncolours;
+            for (int c = 0; c <= L.ncolours; c++) F.colour_start[c] = L.colour_start[c];
+            const BsrView<T>& A = V::Acsr(L);
+            F.a_rowptr = A.rowptr; F.a_colidx = A.colidx; F.a_vals = A.vals; F.a_ld = A.ld;
+            F.dinv = V::dinv(L);
+            const BsrView<T>& Pv = V::P(L);
+            F.p_rowptr = Pv.rowptr; F.p_colidx = Pv.colidx; F.p_vals = Pv.vals; F.p_ld = Pv.ld;
+            const BsrView<T>& Rv = V::R(L);
+            F.r_rowptr = Rv.rowptr; F.r_colidx = Rv.colidx; F.r_vals = Rv.vals; F.r_ld = Rv.ld;
+        }
+        if (fhg::launch_fused_cycle<T>(P, L0.bs, ctx->stream) != cudaSuccess) return false;
+        fhg::g_kernel_launches++;
+        return true;
+    }
+}
+
 // One multigrid cycle on level l (src/Solver/Multigrid/Multigrid.h:438-608): V for w_loops = 1,
 // W for 2 (the coarse correction repeated, except directly above the coarsest level), K for
 // FHG_CYCLE_K (kcycle_fcg on the coarser level unless that is the coarsest). x is the initial
@@ -1061,6 +1125,7 @@ void mg_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
         fhg::launch_coarse<T>(L.n, L.cinv, b, x, s);
         return;
     }
+    if (fused_cycle<T>(ctx, l, b, x, x_zero)) return;
     Level& C = ctx->levels[l + 1];
     // Smoothing steps of this level: the coarse counts apply on levels >= 1 when set.
     const int npre = l > 0 && ctx->opts.coarse_pre_iterations >= 0 ? ctx->opts.coarse_pre_iterations
@@ -1753,6 +1818,7 @@ void fhg_default_options(fhg_options* o)
     o->gs_layout = FHG_GS_AUTO;
     o->extra_precisions = 0;
     o->replace_residual = 0;
+    o->fused_coarse = 1;
 }
 
 int fhg_create(fhg_ctx** out, int device)
@@ -2072,6 +2138,15 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
     // the high part of r: the FP32 V-cycle's right-hand side b32 itself; a buffer of its own otherwise
     if (pair && o.outer_split && (rc = dalloc(ctx, &ctx->rhi, n0))) return rc;
     CK(cudaMallocHost(&ctx->nr_host, sizeof(double)));
+    // The coarse sub-cycle in one cluster launch from the first level (>= 1) from which every level is
+    // small (block rows, colours) and the levels fit the launch parameters.
+    ctx->fused_from = -1;
+    for (int l = 1; l + 1 < nlevels; l++) {
+        bool ok = nlevels - l <= fhg::kFusedMaxLevels;
+        for (int k = l; k < nlevels && ok; k++)
+            ok = ctx->levels[k].nb <= fhg::kFusedMaxRows && (k == nlevels - 1 || ctx->levels[k].ncolours <= fhg::kFusedMaxColours);
+        if (ok) { ctx->fused_from = l; break; }
+    }
 
     if (o.autotune) {
         // Tune in the precision the V-cycle runs in (the FP64 copies keep the FP32 choices,

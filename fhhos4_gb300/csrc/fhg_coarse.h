@@ -1,0 +1,60 @@
+// The coarse part of a multigrid cycle in one thread-block-cluster launch (fhg_coarse.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fhg_pair.h"
+
+namespace fhg {
+
+constexpr int kClusterCtas = 8;        // CTAs of the one cluster (the portable maximum)
+constexpr int kFusedThreads = 512;     // threads per CTA
+constexpr int kFusedMaxLevels = 6;     // levels of a fused sub-cycle, the coarsest included
+constexpr int kFusedMaxColours = 24;
+constexpr int kFusedMaxRows = 65536;   // block rows of the largest level a fused sub-cycle takes
+
+// Smoother directions of a fused sub-cycle (the GS codes; Jacobi is not fused).
+enum { kFusedForward = 0, kFusedBackward = 1, kFusedSymmetric = 2, kFusedAlternatingForward = 3,
+       kFusedAlternatingBackward = 4 };
+
+// One level of the sub-cycle in the launch parameters: A in CSR form (all blocks, entry-major values,
+// leading dimension a_ld), D^-1 entry-major (leading dimension nb), the colour offsets, P (this
+// level's rows, the next level's columns) and R = P^T (the next level's rows), and the level's x, b
+// and residual vectors. On the coarsest level only x and b are used.
+template <class T>
+struct FusedLevel {
+    int nb = 0, ncol = 0;
+    int colour_start[kFusedMaxColours + 1] = {};
+    const int* a_rowptr = nullptr;
+    const int* a_colidx = nullptr;
+    const T* a_vals = nullptr;
+    long long a_ld = 0;
+    const T* dinv = nullptr;
+    const int* p_rowptr = nullptr;
+    const int* p_colidx = nullptr;
+    const T* p_vals = nullptr;
+    long long p_ld = 0;
+    const int* r_rowptr = nullptr;
+    const int* r_colidx = nullptr;
+    const T* r_vals = nullptr;
+    long long r_ld = 0;
+    T* x = nullptr;
+    T* b = nullptr;
+    T* r = nullptr;
+};
+
+template <class T>
+struct FusedCycle {
+    int nlev = 0;                 // levels, the coarsest included (lev[nlev - 1])
+    int n_coarse = 0;             // unknowns of the coarsest level
+    const double* cinv = nullptr; // its dense FP64 inverse, row-major
+    int pre = 0, post = 1, npre = 1, npost = 1, w_loops = 1;
+    int x_zero = 1;               // x of the first level starts at zero
+    T omega = T(1);               // relaxation of the GS sweeps (block SOR when not 1)
+    FusedLevel<T> lev[kFusedMaxLevels];
+};
+
+template <class T>
+cudaError_t launch_fused_cycle(const FusedCycle<T>& P, int bs, cudaStream_t s);
+
+}  // namespace fhg

@@ -157,6 +157,8 @@ class _KrylovOnGpu(IterativeSolver):
         # Residual replacement in every precision (the FP32 V-cycle always replaces); off keeps the
         # reference's stopping loop in FP64.
         self.ReplaceResidual = False
+        # the coarse part of the cycle as one cluster launch where the levels are small (FP32 / DF)
+        self.FusedCoarse = True
         self._ctx: Optional[N.Context] = None
 
     def _options(self, mg: Multigrid) -> N.Options:
@@ -176,6 +178,7 @@ class _KrylovOnGpu(IterativeSolver):
         o.max_coarse_rows = mg.MaxCoarseRows
         o.outer_split = 1 if self.OuterSplit else 0
         o.replace_residual = 1 if self.ReplaceResidual else 0
+        o.fused_coarse = 1 if self.FusedCoarse else 0
         o.w_loops = N.CYCLE_K if mg.Cycle == "K" else (mg.WLoops if mg.Cycle == "W" else 1)
         o.galerkin = 1 if mg.UseGalerkinOperator else 0
         o.coarse_pre_iterations = mg.CoarsePreSmoothingIterations
@@ -258,7 +261,7 @@ def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: st
            precision: str = "fp64", krylov: str = "fcg", device: int = 0, autotune: bool = False,
            use_graphs: bool = True, outer_split: bool = True, cycle: str = "V", galerkin: bool = False,
            nu=(1, 1), coarse_nu=(-1, -1), gs_layout: str = "auto", omega: float = 1.0, extra=(),
-           replace_residual: bool = False):
+           replace_residual: bool = False, fused: bool = True):
     """SolverFactory-style construction of "-s fcgmg -cycle V,1,1" (src/Solver/SolverFactory.h:156-200)."""
     mg = Multigrid(len(As))
     mg.SetHierarchy(As, Ps)
@@ -282,5 +285,6 @@ def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: st
     solver.UseGraphs = use_graphs
     solver.OuterSplit = outer_split
     solver.ReplaceResidual = replace_residual
+    solver.FusedCoarse = fused
     solver.Setup(As[0])
     return solver

@@ -131,6 +131,11 @@ typedef struct {
                                    reference's loop (IterativeSolver.h:224-247). The true residual that misses the
                                    tolerance in FP64 is evaluated again in compensated arithmetic. No counterpart
                                    in the reference. */
+    int fused_coarse;           /* 1 (default): with GS / SOR smoothers and a V or W cycle in FP32 or DF, the cycle
+                                   below the first level from which every level has at most 65,536 block rows runs
+                                   as one thread-block-cluster launch (phases separated by the cluster barrier)
+                                   instead of one launch per colour and product; 0: launch by launch. Same
+                                   arithmetic up to the summation order of a row. */
 } fhg_options;
 
 typedef struct {

@@ -263,6 +263,26 @@ def test_df_vcycle_matches_reference(case, variant, pre, post, cycle, omega_key,
     assert np.linalg.norm(x[sp_] - xr) / np.linalg.norm(xr) < X_RTOL
 
 
+@pytest.mark.parametrize("precision,cycle,pre,post", [("fp32", "V", "bgs", "rbgs"), ("df", "V", "bgs", "rbgs"),
+                                                       ("df", "W", "sbgs", "sbgs"), ("fp32", "V", "bsor", "rbsor")])
+def test_fused_coarse_cycle_matches_launch_by_launch(case, precision, cycle, pre, post):
+    """The coarse sub-cycle as one cluster launch against the same cycle launched phase by phase:
+    the same arithmetic up to the summation order of a row, so FP64-class solves agree to 1e-10
+    (iterations equal) and FP32 solves take the same iterations within one and reach the tolerance."""
+    kw = dict(precision=precision, cycle=cycle, pre=pre, post=post, nu=(2, 2), coarse_nu=(3, 3),
+              omega=float(case["sor_omega"]) if pre == "bsor" else 1.0)
+    a = S().fcg_mg(case.As, case.Ps, case.bs, fused=True, **kw)
+    b = S().fcg_mg(case.As, case.Ps, case.bs, fused=False, **kw)
+    xa, xb = a.Solve(case.b), b.Solve(case.b)
+    if precision == "df":
+        assert a.IterationCount == b.IterationCount
+        assert np.all(np.abs(a.History - b.History) <= 1e-10 * np.abs(b.History) + 64 * HIST_ATOL)
+        assert np.linalg.norm(xa - xb) <= 1e-10 * np.linalg.norm(xb)
+    else:
+        assert abs(a.IterationCount - b.IterationCount) <= 1
+        assert true_rel_residual(case.As[0], case.b, xa) < 1e-8 * (1 + 1e-6)
+
+
 def _pairs(torch, v):
     """An FP64 vector as interleaved FP32 pairs (hi, lo) on the device."""
     hi = v.astype(np.float32)
