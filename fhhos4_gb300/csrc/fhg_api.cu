@@ -2147,6 +2147,10 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
             ok = ctx->levels[k].nb <= fhg::kFusedMaxRows && (k == nlevels - 1 || ctx->levels[k].ncolours <= fhg::kFusedMaxColours);
         if (ok) { ctx->fused_from = l; break; }
     }
+    // the cluster must fit on this device in every value type the context may run
+    if (ctx->fused_from >= 0 && ((fp32 && fhg::fused_cycle_clusters<float>(bs) < 1) ||
+                                 (pair && fhg::fused_cycle_clusters<dfl>(bs) < 1)))
+        ctx->fused_from = -1;
 
     if (o.autotune) {
         // Tune in the precision the V-cycle runs in (the FP64 copies keep the FP32 choices,

@@ -25,10 +25,12 @@ namespace fhg {
 
 namespace {
 
+// Every thread of the cluster arrives (release) and waits (acquire); the non-aligned form does not
+// require the threads of a warp to arrive together.
 __device__ __forceinline__ void cluster_sync()
 {
-    asm volatile("barrier.cluster.arrive.release.aligned;\n"
-                 "barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+    asm volatile("barrier.cluster.arrive.release;\n"
+                 "barrier.cluster.wait.acquire;\n" ::: "memory");
 }
 
 __device__ __forceinline__ void pdl_wait_coarse() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
@@ -201,6 +203,54 @@ __global__ void __launch_bounds__(kFusedThreads) k_fused_cycle(const __grid_cons
 
 }  // namespace
 
+namespace {
+
+template <class T>
+void fused_config(cudaLaunchConfig_t& cfg, cudaLaunchAttribute* attr, cudaStream_t s)
+{
+    cfg = {};
+    cfg.gridDim = dim3(kClusterCtas);
+    cfg.blockDim = dim3(kFusedThreads);
+    cfg.stream = s;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kClusterCtas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 2;
+}
+
+template <class T, int BS>
+int clusters_of()
+{
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[2];
+    fused_config<T>(cfg, attr, nullptr);
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k_fused_cycle<T, BS>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+}  // namespace
+
+template <class T>
+int fused_cycle_clusters(int bs)
+{
+    switch (bs) {
+    case 2: return clusters_of<T, 2>();
+    case 3: return clusters_of<T, 3>();
+    case 4: return clusters_of<T, 4>();
+    case 6: return clusters_of<T, 6>();
+    default: return 0;
+    }
+}
+
 template <class T>
 cudaError_t launch_fused_cycle(const FusedCycle<T>& P, int bs, cudaStream_t s)
 {
@@ -228,5 +278,7 @@ cudaError_t launch_fused_cycle(const FusedCycle<T>& P, int bs, cudaStream_t s)
 
 template cudaError_t launch_fused_cycle<float>(const FusedCycle<float>&, int, cudaStream_t);
 template cudaError_t launch_fused_cycle<dfl>(const FusedCycle<dfl>&, int, cudaStream_t);
+template int fused_cycle_clusters<float>(int);
+template int fused_cycle_clusters<dfl>(int);
 
 }  // namespace fhg

@@ -56,5 +56,8 @@ struct FusedCycle {
 
 template <class T>
 cudaError_t launch_fused_cycle(const FusedCycle<T>& P, int bs, cudaStream_t s);
+// Clusters of the fused kernel that fit on the current device at once (0: it cannot run here).
+template <class T>
+int fused_cycle_clusters(int bs);
 
 }  // namespace fhg
