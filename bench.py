@@ -168,6 +168,11 @@ class ClockSampler:
                 "samples": len(sm), "power_w_max": pmax}
 
 
+def log(msg: str):
+    """Progress of the bench on stderr (the JSON line alone goes to stdout)."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
 def measured_hbm_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -528,9 +533,12 @@ def run_ours(args, dist: Dist):
         "cpu_baseline": cpu,
     }
     ctx.close()
+    log(f"config 2 done: headline {value * 1e3:.2f} ms")
     if not args.no_extra:
         for name in EXTRA_CONFIGS:
+            t = time.perf_counter()
             line[name] = run_extra(args, dist, name)
+            log(f"{name} done in {time.perf_counter() - t:.1f} s")
         args.batch = args.batch or 512
     if args.batch > 0:
         line["config4_batched"] = run_batched(args, dist)
@@ -540,22 +548,24 @@ def run_ours(args, dist: Dist):
 
 def run_batched(args, dist: Dist):
     """Config 4: many 2D problems of uneven size in one graph launch against the same problems solved
-    one after another (fhg_solve_device each), with the FP32 and the FP64-class (pair) V-cycles."""
+    one after another (fhg_solve_device each), with the FP32 and the FP64-class (pair) V-cycles; the
+    contexts of one precision at a time (every problem's operators and views take device memory)."""
     import torch
     from fhhos4_gb300 import batch as BT
     specs = BT.batched_specs(args.batch)
     t0 = time.perf_counter()
-    probs, batch, build_s = BT.build(specs, device=dist.local_rank, precision="fp32", autotune=True, extra=("df",))
-    dofs = sum(p.n for p in probs)
-    out = {"problems": len(probs), "unknowns": int(dofs), "n_range": [min(s.n for s in specs), max(s.n for s in specs)],
+    gen = BT.generate_all(specs)
+    dofs = sum(g[1].shape[0] for g in gen)
+    out = {"problems": len(specs), "unknowns": int(dofs), "n_range": [min(s.n for s in specs), max(s.n for s in specs)],
            "k_counts": {k: sum(1 for s in specs if s.k == k) for k in (1, 2, 3)},
            "method": ("V(1,1) bgs/rbgs inside FP64 FCG(1), Galerkin coarse operators, autotuned launch shapes; "
                       "residual replacement in the device loop (FP32); the FP64-class run keeps the reference loop"),
-           "setup_s": round(time.perf_counter() - t0, 1)}
+           "host_generation_s": round(time.perf_counter() - t0, 1)}
+    log(f"config 4: {len(specs)} problems generated in {out['host_generation_s']} s")
     for prec in ("fp32", "df"):
-        for p in probs:
-            p.ctx.set_vcycle_precision(prec)
-            p.upload_b()
+        t1 = time.perf_counter()
+        probs, batch, build_s = BT.build(specs, device=dist.local_rank, precision=prec, autotune=True, generated=gen)
+        setup_s = time.perf_counter() - t1
         for _ in range(2):
             rc, infos, ms = batch.solve()
         times = []
@@ -578,10 +588,13 @@ def run_batched(args, dist: Dist):
                      "dofs_per_s": round(dofs / (batched_ms * 1e-3), 1), "iterations_min_max": [min(its), max(its)],
                      "true_rel_residual_median_worst": [trues[len(trues) // 2], trues[-1]],
                      "problems_true_below_tol": sum(1 for t in trues if t < 1e-8), "status": rc,
+                     "setup_s": round(setup_s, 1),
                      "timing": f"median of {max(3, args.steps // 2)} launches after 2 untimed ones"}
-    batch.close()
-    for p in probs:
-        p.close()
+        log(f"config 4 {prec}: setup {setup_s:.1f} s, batched {batched_ms:.1f} ms, sequential {seq_ms:.1f} ms")
+        batch.close()
+        for p in probs:
+            p.close()
+        del probs, batch
     return out
 
 

@@ -88,18 +88,22 @@ class Problem:
             self.ctx = None
 
 
-def build(specs: List[ProblemSpec], device: int = 0, precision: str = "fp64", autotune: bool = True,
-          keep_operator: bool = False, extra=()):
-    """Problems with b uploaded, and a Batch holding all of them. Returns (problems, batch, seconds)."""
-    t0 = time.time()
-    # the host hierarchies in parallel, one generator thread each (ctypes releases the GIL), then
-    # the contexts one after another on the GPU
+def generate_all(specs: List[ProblemSpec]):
+    """The host hierarchies of all problems, in parallel (one generator thread each; ctypes releases
+    the GIL)."""
     workers = max(1, min(len(specs), os.cpu_count() or 1))
     with cf.ThreadPoolExecutor(workers) as ex:
-        gen = list(ex.map(lambda sp: generate(sp, threads=1), specs))
+        return list(ex.map(lambda sp: generate(sp, threads=1), specs))
+
+
+def build(specs: List[ProblemSpec], device: int = 0, precision: str = "fp64", autotune: bool = True,
+          keep_operator: bool = False, extra=(), generated=None):
+    """Problems with b uploaded, and a Batch holding all of them. Returns (problems, batch, seconds).
+    generated: the hierarchies of generate_all(specs), reused; otherwise generated here."""
+    t0 = time.time()
+    gen = generated if generated is not None else generate_all(specs)
     probs = [Problem(s, device, precision, autotune, keep_operator=keep_operator, generated=g, extra=extra)
              for s, g in zip(specs, gen)]
-    del gen
     for p in probs:
         p.upload_b()
     batch = N.Batch(device)
