@@ -30,17 +30,25 @@ class GpuFcgMg : public IterativeSolver
 public:
     GpuFcgMg(Diffusion_HHO<Dim>* problem, const ProgramArguments& args, int blockSize, int device = 0)
     {
-        _mg = new MultigridForHHO<Dim>(problem, args.Solver.MG.Levels);
+        _opts = MapArguments(args);
+        _mg = new MultigridForHHO<Dim>(args.Solver.MG.Levels);
+        _mg->UseHigherOrderReconstruction = args.Solver.MG.UseHigherOrderReconstruction;
+        _mg->H_Prolongation = args.Solver.MG.GMG_H_Prolong;
+        _mg->UseHeterogeneousWeighting = args.Solver.MG.UseHeterogeneousWeighting;
+        _mg->InitializeWithProblem(problem);
         _mg->BlockSizeForBlockSmoothers = blockSize;
         _mg->MatrixMaxSizeForCoarsestLevel = args.Solver.MG.MatrixMaxSizeForCoarsestLevel;
+        _mg->UseGalerkinOperator = args.Solver.MG.UseGalerkinOperator;
         _mg->H_CS = args.Solver.MG.H_CS;
-        _mg->H_Prolongation = args.Solver.MG.GMG_H_Prolong;
+        _mg->FaceCoarseningStgy = args.Solver.MG.FaceCoarseningStgy;
+        _mg->BdryFaceCollapsing = args.Solver.MG.BoundaryFaceCollapsing;
+        _mg->NumberOfMeshes = args.Solver.MG.NumberOfMeshes;
+        _mg->CoarseningFactor = args.Solver.MG.CoarseningFactor;
         _mg->PreSmoothingIterations = 0;   // smoothers run on the GPU: no host smoother setup needed
         _mg->PostSmoothingIterations = 0;
         _mg->CoarseSolver = new EigenSparseCholesky();
-        fhg_default_options(&_opts);
-        _opts.pre_iterations = args.Solver.MG.PreSmoothingIterations;
-        _opts.post_iterations = args.Solver.MG.PostSmoothingIterations;
+        this->Tolerance = args.Solver.Tolerance;
+        this->MaxIterations = args.Solver.MaxIterations;
         Check(fhg_create(&_ctx, device));
     }
 
@@ -56,7 +64,7 @@ public:
     {
         IterativeSolver::Setup(A);
         _mg->Setup(A);
-        _opts.tolerance = this->Tolerance;
+        _opts.tolerance = this->Tolerance;   // the caller may have changed them after construction
         _opts.max_iterations = this->MaxIterations;
         Level* fine = _mg->*(&fhg_detail::MultigridFineLevel::_fineLevel);
         int l = 0;
@@ -103,5 +111,87 @@ private:
     {
         if (rc != FHG_OK)
             Utils::FatalError(std::string("GPU solver: ") + fhg_last_error(_ctx));
+    }
+
+    // The solver arguments the reference's SolverFactory reads for "-s fcgmg" / "-s cgmg"
+    // (SolverFactory.h:125-200, SetMultigridParameters SolverFactory.h:236-310), mapped to
+    // fhg_options; an argument the GPU path does not implement is an error, never ignored.
+public:
+    static fhg_options MapArguments(const ProgramArguments& args)
+    {
+        fhg_options o;
+        fhg_default_options(&o);
+        const SolverArguments& s = args.Solver;
+        const string& code = s.SolverCode;
+        const bool pc_mg = s.PreconditionerCode == "mg";
+        if (code == "fcgmg" || (code == "fcg" && pc_mg))
+            o.krylov = FHG_KRYLOV_FCG;
+        else if (code == "cgmg" || (code == "cg" && pc_mg))
+            o.krylov = FHG_KRYLOV_CG;
+        else
+            Utils::FatalError("GPU solver: solver code '" + code + "' (preconditioner '" + s.PreconditionerCode +
+                              "') is not supported; use fcgmg or cgmg");
+        if (s.StoppingCrit != StoppingCriteria::NormalizedResidual)
+            Utils::FatalError("GPU solver: only the normalized-residual stopping criterion is supported");
+        if (s.InitialGuessCode != "0")
+            Utils::FatalError("GPU solver: the initial guess must be \"0\"");
+        const MultigridArguments& mg = s.MG;
+        if (mg.CycleLetter == 'V')
+            o.w_loops = 1;
+        else if (mg.CycleLetter == 'W')
+            o.w_loops = mg.WLoops > 1 ? mg.WLoops : 2;
+        else if (mg.CycleLetter == 'K')
+            o.w_loops = FHG_CYCLE_K;
+        else
+            Utils::FatalError(std::string("GPU solver: multigrid cycle '") + mg.CycleLetter + "' is not supported");
+        if (mg.CoarseLevelChangeSmoothingCoeff != 0)
+            Utils::FatalError("GPU solver: level-dependent smoothing steps (-cycle V,a,b,+c) are not supported");
+        if (mg.CoarseSolverCode != "ch" && mg.CoarseSolverCode != "lu")
+            Utils::FatalError("GPU solver: coarse solver '" + mg.CoarseSolverCode +
+                              "' is not supported; the coarsest level is solved directly (ch / lu)");
+        o.galerkin = mg.UseGalerkinOperator ? 1 : 0;
+        o.pre_iterations = mg.PreSmoothingIterations;
+        o.post_iterations = mg.PostSmoothingIterations;
+        o.omega = s.RelaxationParameter;
+        o.tolerance = s.Tolerance;
+        o.max_iterations = s.MaxIterations;
+        o.pre_smoother = SmootherCode(mg.PreSmootherCode);
+        o.post_smoother = SmootherCode(PostSmootherName(mg));
+        return o;
+    }
+
+private:
+
+    // "<symmetric smoother>" resolved as SetMultigridParameters does (SolverFactory.h:258-283)
+    static string PostSmootherName(const MultigridArguments& mg)
+    {
+        const string& pre = mg.PreSmootherCode;
+        if (mg.PostSmootherCode != "<symmetric smoother>")
+            return mg.PostSmootherCode;
+        if (pre == "bj23" || pre == "bj" || pre == "sbgs")
+            return pre;
+        if (pre == "bgs")
+            return "rbgs";
+        if (pre == "hbgs")
+            return "hrbgs";
+        if (pre == "abgs" || pre == "asor")
+            return mg.PreSmoothingIterations % 2 == 0 ? pre : "r" + pre;
+        Utils::FatalError("GPU solver: no symmetric post-smoother for '" + pre + "'");
+        return pre;
+    }
+
+    // Block smoother codes of SmootherFactory::Create (SmootherFactory.h:37-100). The "hbgs" family
+    // maps to the multicolour sweeps; with RelaxationParameter != 1 the GS codes become block SOR.
+    static int SmootherCode(const string& c)
+    {
+        if (c == "bgs" || c == "bsor" || c == "hbgs") return FHG_SMOOTHER_BGS;
+        if (c == "rbgs" || c == "rbsor" || c == "hrbgs") return FHG_SMOOTHER_RBGS;
+        if (c == "sbgs" || c == "sbsor") return FHG_SMOOTHER_SBGS;
+        if (c == "abgs" || c == "absor") return FHG_SMOOTHER_ABGS;
+        if (c == "rabgs" || c == "rabsor") return FHG_SMOOTHER_RABGS;
+        if (c == "bj") return FHG_SMOOTHER_BJ;
+        if (c == "bj23") return FHG_SMOOTHER_BJ23;
+        Utils::FatalError("GPU solver: smoother '" + c + "' is not supported (block smoothers only)");
+        return -1;
     }
 };

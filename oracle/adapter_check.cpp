@@ -1,6 +1,7 @@
 // Compile-and-link check of include/fhg_reference_adapter.hpp against the reference headers
-// (no GPU needed: the program is built, not run, in environments without one). With a GPU it
-// solves the reference's 2D config-1 problem through the adapter and prints the iterations.
+// (TEST INFRASTRUCTURE). `adapter_check --map` needs no GPU: it prints the fhg_options the adapter
+// derives from several ProgramArguments settings. Without arguments (GPU needed) it solves the
+// reference's 2D config-1 problem through the adapter and prints the iterations.
 #include "ProgramArguments.h"
 #include "Discretizations/DG/Diffusion_DG.h"
 #include "TestCases/Diffusion/DiffTestCaseFactory.h"
@@ -12,9 +13,65 @@
 #include "Solver/SolverFactory.h"
 #include "fhg_reference_adapter.hpp"
 
-int main()
+static void print_options(const char* name, const ProgramArguments& a)
 {
+    const fhg_options o = GpuFcgMg<2>::MapArguments(a);
+    std::cout << name << " krylov=" << o.krylov << " pre=" << o.pre_smoother << " post=" << o.post_smoother
+              << " npre=" << o.pre_iterations << " npost=" << o.post_iterations << " omega=" << o.omega
+              << " w_loops=" << o.w_loops << " galerkin=" << o.galerkin << " tol=" << o.tolerance
+              << " maxit=" << o.max_iterations << std::endl;
+}
+
+static int map_check()
+{
+    ProgramArguments a;
+    a.Solver.SolverCode = "fcgmg";
+    print_options("default", a);
+    a.Solver.MG.PostSmootherCode = "<symmetric smoother>";
+    a.Solver.MG.PreSmootherCode = "abgs";
+    a.Solver.MG.PreSmoothingIterations = 3;
+    print_options("abgs3_symmetric", a);
+    a.Solver.MG.PreSmootherCode = "hbgs";
+    print_options("hbgs_symmetric", a);
+    ProgramArguments w;
+    w.Solver.SolverCode = "cg";
+    w.Solver.PreconditionerCode = "mg";
+    w.Solver.MG.CycleLetter = 'W';
+    w.Solver.MG.WLoops = 2;
+    w.Solver.MG.UseGalerkinOperator = true;
+    w.Solver.MG.PreSmootherCode = "bsor";
+    w.Solver.MG.PostSmootherCode = "rbsor";
+    w.Solver.RelaxationParameter = 1.2;
+    w.Solver.Tolerance = 1e-10;
+    w.Solver.MaxIterations = 50;
+    print_options("cg_w_sor", w);
+    ProgramArguments k;
+    k.Solver.SolverCode = "cgmg";
+    k.Solver.MG.CycleLetter = 'K';
+    k.Solver.MG.PreSmootherCode = "bj23";
+    k.Solver.MG.PostSmootherCode = "<symmetric smoother>";
+    print_options("cgmg_k_bj23", k);
+    return 0;
+}
+
+int main(int argc, char** argv)
+{
+    if (argc > 1 && std::string(argv[1]) == "--map")
+        return map_check();
+    if (argc > 2 && std::string(argv[1]) == "--reject")
+    {   // an unsupported setting: the mapping must end in Utils::FatalError
+        ProgramArguments a;
+        a.Solver.SolverCode = "fcgmg";
+        const std::string what(argv[2]);
+        if (what == "solver") a.Solver.SolverCode = "bicgstab";
+        if (what == "smoother") a.Solver.MG.PreSmootherCode = "gs";
+        if (what == "coarse") a.Solver.MG.CoarseSolverCode = "fcgmg";
+        if (what == "variable") a.Solver.MG.CoarseLevelChangeSmoothingCoeff = 1;
+        print_options("accepted", a);
+        return 0;
+    }
     ProgramArguments args;
+    args.Solver.SolverCode = "fcgmg";
     args.Problem.Dimension = 2;
     args.Problem.GeoCode = args.Problem.TestCaseCode = "square";
     args.Problem.BCCode = "d";

@@ -1,0 +1,55 @@
+"""The C++ adapter (include/fhg_reference_adapter.hpp) compiled against the reference's headers:
+ProgramArguments -> fhg_options as the reference's SolverFactory reads them (SolverFactory.h:125-200,
+236-310; SmootherFactory.h:37-100). CPU only: `adapter_check --map` makes no GPU call. Skipped
+where the reference checkout or libfhg.so is absent."""
+import os
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REFERENCE = os.environ.get("FHHOS4_REFERENCE", "/root/reference")
+LIB = os.path.join(ROOT, "fhhos4_gb300", "_build", "libfhg.so")
+
+
+def _mapped():
+    if not os.path.isdir(os.path.join(REFERENCE, "src", "Solver")):
+        pytest.skip("reference checkout not present")
+    if not os.path.exists(LIB):
+        pytest.skip("libfhg.so not built")
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "adapter", f"REF_ROOT={REFERENCE}"],
+                   check=True, timeout=600)
+    out = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "adapter_check"), "--map"], check=True,
+                         capture_output=True, text=True, timeout=60).stdout
+    rows = {}
+    for line in out.splitlines():
+        name, *kv = line.split()
+        rows[name] = {k: v for k, v in (x.split("=") for x in kv)}
+    return rows
+
+
+def test_adapter_argument_mapping():
+    m = _mapped()
+    # fcgmg defaults: V(1,1), bgs / rbgs, omega 1, tolerance 1e-8, 200 iterations (ProgramArguments.h:60-95)
+    assert m["default"] == dict(krylov="0", pre="0", post="1", npre="1", npost="1", omega="1", w_loops="1",
+                                galerkin="0", tol="1e-08", maxit="200")
+    # "<symmetric smoother>" after abgs with an odd step count is "rabgs" (SolverFactory.h:270-280)
+    assert (m["abgs3_symmetric"]["pre"], m["abgs3_symmetric"]["post"]) == ("5", "6")
+    # hbgs -> hrbgs, both the multicolour forward / backward sweeps
+    assert (m["hbgs_symmetric"]["pre"], m["hbgs_symmetric"]["post"]) == ("0", "1")
+    # cg + mg preconditioner, W-cycle, Galerkin, block SOR aliases with omega 1.2
+    w = m["cg_w_sor"]
+    assert (w["krylov"], w["w_loops"], w["galerkin"], w["pre"], w["post"], w["omega"]) == ("1", "2", "1", "0", "1", "1.2")
+    assert (w["tol"], w["maxit"]) == ("1e-10", "50")
+    # cgmg, K-cycle, bj23 symmetric post-smoother is bj23 itself
+    k = m["cgmg_k_bj23"]
+    assert (k["krylov"], k["w_loops"], k["pre"], k["post"]) == ("1", "-1", "3", "3")
+
+
+@pytest.mark.parametrize("what", ["solver", "smoother", "coarse", "variable"])
+def test_adapter_rejects_unsupported(what):
+    _mapped()
+    p = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "adapter_check"), "--reject", what],
+                       capture_output=True, text=True, timeout=60)
+    assert p.returncode != 0 and "accepted" not in p.stdout
+    assert "GPU solver" in p.stdout + p.stderr
