@@ -31,6 +31,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 
 namespace fhg {
 namespace {
@@ -1004,11 +1005,14 @@ int launch_learned_apply(int nb, int bs, const int* nbr, const float* w, const v
                          const float* bias, float* x, int* status, int kernel, cudaStream_t s)
 {
     // Persistent grids: as many CTAs as fit on the device at once, computed once per kernel, block
-    // size and device (the shared-memory attribute is set with it).
+    // size and device (the shared-memory attribute is set with it). Contexts on several host threads
+    // may launch at once: the table and the attribute calls are under one lock.
     static int grid_of[2][kMaxLearnedBs + 1][16] = {};
+    static std::mutex grid_mutex;
     int dev = 0;
     if (!learned_supports(bs) || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) return -1;
     const int kk = kernel == kLearnedKernelMmaSync ? 1 : 0;
+    std::unique_lock<std::mutex> grid_lock(grid_mutex);
     if (grid_of[kk][bs][dev] == 0) {
         // tcgen05: one CTA per SM (all 512 TMEM columns, four tile pipelines, 181 KB of shared
         // memory); mma.sync: two CTAs per SM (registers <= 128 per thread, 2 x 70 KB of shared
@@ -1034,15 +1038,17 @@ int launch_learned_apply(int nb, int bs, const int* nbr, const float* w, const v
         if (e != cudaSuccess || sms < 1) return -1;
         grid_of[kk][bs][dev] = (kk == 1 ? 2 : 1) * sms;
     }
+    const int grid_max = grid_of[kk][bs][dev];
+    grid_lock.unlock();
     if (kk == 1) {
         const int tiles = (nb + 15) / 16;
-        const int grid = std::min(grid_of[kk][bs][dev], (tiles + kApplyWarps - 1) / kApplyWarps);
+        const int grid = std::min(grid_max, (tiles + kApplyWarps - 1) / kApplyWarps);
         if (grid < 1) return 0;
         FHG_LEARNED_BS(bs, k_learned_apply<BS><<<grid, kApplyWarps * 32, kApplySmem, s>>>(
                                nb, nbr, w, (const bf16*)tfeat, (const bf16*)wts, bias, x));
     } else {
         const int tiles = (nb + kTcRows - 1) / kTcRows;
-        const int grid = std::min(grid_of[kk][bs][dev], (tiles + kTcSlots - 1) / kTcSlots);
+        const int grid = std::min(grid_max, (tiles + kTcSlots - 1) / kTcSlots);
         if (grid < 1) return 0;
         FHG_LEARNED_BS(bs, k_learned_apply_tc<BS><<<grid, kTcThreads, kTcSmem, s>>>(
                                nb, nbr, w, (const bf16*)tfeat, (const bf16*)wts, bias, x, status));
