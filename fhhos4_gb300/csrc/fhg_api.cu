@@ -147,7 +147,9 @@ struct fhg_ctx {
     long long graph_l_kernels[2] = {0, 0};
     int graphs_l_built = 0;
     bool device_loop = false;          // capturing for the device-side loop: no host read-back
-    int fused_from = -1;               // first level of the coarse sub-cycle run as one cluster launch (-1: none)
+    int fused_from[3] = {-1, -1, -1};  // per V-cycle precision: first level of the coarse sub-cycle run as
+                                       // one cluster launch (-1: none), and the cluster's CTAs
+    int fused_ctas[3] = {fhg::kClusterCtasPortable, fhg::kClusterCtasPortable, fhg::kClusterCtasPortable};
     long long epoch = 0;               // incremented by every setup (batched graphs hold its buffers)
 };
 
@@ -1049,6 +1051,15 @@ void kcycle_fcg(fhg_ctx* ctx, int m, T* r, T* x)
     fhg::launch_lincomb<T>(n, alpha1 / rho1 - gamma * alpha2 / (rho1 * rho2), c, alpha2 / rho2, d, x, s);
 }
 
+// Lanes of the fused kernel per block row of an operator: enough for the average row's blocks to be
+// loaded together, a power of two from 4 to 16.
+template <class T>
+int fused_lanes(const BsrView<T>& B)
+{
+    const double avg = B.nbr ? (double)B.nnzb / B.nbr : 1.0;
+    return avg <= 5.0 ? 4 : avg <= 12.0 ? 8 : 16;
+}
+
 // The coarse sub-cycle from level l down as one cluster launch (fhg_coarse.cu), when setup found the
 // levels small enough and the cycle is one it covers: GS / SOR smoothers, V or W cycle, FP32 or pair
 // values. Returns false when the caller must run the sub-cycle launch by launch.
@@ -1060,8 +1071,8 @@ bool fused_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
     } else {
         using V = LevelVecs<T>;
         const fhg_options& o = ctx->opts;
-        if (!o.fused_coarse || l != ctx->fused_from || l <= 0 || o.w_loops == FHG_CYCLE_K || !is_gs(o.pre_smoother) ||
-            !is_gs(o.post_smoother))
+        if (!o.fused_coarse || l != ctx->fused_from[V::kPrec] || l <= 0 || o.w_loops == FHG_CYCLE_K ||
+            !is_gs(o.pre_smoother) || !is_gs(o.post_smoother))
             return false;
         Level& L0 = ctx->levels[l];
         if (b != V::b(L0) || x != V::x(L0)) return false;
@@ -1104,11 +1115,142 @@ bool fused_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
             F.p_rowptr = Pv.rowptr; F.p_colidx = Pv.colidx; F.p_vals = Pv.vals; F.p_ld = Pv.ld;
             const BsrView<T>& Rv = V::R(L);
             F.r_rowptr = Rv.rowptr; F.r_colidx = Rv.colidx; F.r_vals = Rv.vals; F.r_ld = Rv.ld;
+            F.lanes = fused_lanes(A);
+            F.t_lanes = fused_lanes(Rv);
         }
-        if (fhg::launch_fused_cycle<T>(P, L0.bs, ctx->stream) != cudaSuccess) return false;
+        if (fhg::launch_fused_cycle<T>(P, L0.bs, ctx->fused_ctas[V::kPrec], ctx->stream) != cudaSuccess) return false;
         fhg::g_kernel_launches++;
         return true;
     }
+}
+
+// First level (>= 1, above the coarsest) from which every level has at most max_rows block rows and
+// at most kFusedMaxColours colours, within kFusedMaxLevels levels; -1 when there is none.
+int fused_first_level(const fhg_ctx* ctx, int max_rows)
+{
+    const int nlevels = ctx->nlevels;
+    for (int l = 1; l + 1 < nlevels; l++) {
+        bool ok = nlevels - l <= fhg::kFusedMaxLevels;
+        for (int k = l; k < nlevels && ok; k++)
+            ok = ctx->levels[k].nb <= max_rows &&
+                 (k == nlevels - 1 || ctx->levels[k].ncolours <= fhg::kFusedMaxColours);
+        if (ok) return l;
+    }
+    return -1;
+}
+
+// Timing-based choice of the coarse sub-cycle, kept per hierarchy structure and cycle in the process
+// (the same sizes, colours, block counts, smoothers and counts give the same choice).
+struct FusedKey {
+    std::vector<long long> sig;
+    bool operator<(const FusedKey& o) const { return sig < o.sig; }
+};
+std::mutex g_fused_mutex;
+std::map<FusedKey, std::pair<int, int>> g_fused_cache;
+
+template <class T>
+void mg_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero);
+
+// Time one cycle below level 0 (from level 1, x = 0) for launch by launch and for every eligible first
+// level of the fused sub-cycle with 8 and 16 CTAs; keep the fastest (ties: the earlier candidate).
+template <class T>
+int choose_fused(fhg_ctx* ctx)
+{
+    using V = LevelVecs<T>;
+    constexpr int PR = V::kPrec;
+    const fhg_options& o = ctx->opts;
+    const int nlevels = ctx->nlevels;
+    const int bs = ctx->levels[0].bs;
+    const int first = fused_first_level(ctx, fhg::kFusedMaxRows);
+    ctx->fused_from[PR] = -1;
+    ctx->fused_ctas[PR] = fhg::kClusterCtasPortable;
+    if (first < 0) return FHG_OK;
+    FusedKey key;
+    key.sig = {PR, bs, nlevels, o.pre_smoother, o.post_smoother, o.pre_iterations, o.post_iterations,
+               o.coarse_pre_iterations, o.coarse_post_iterations, o.w_loops, o.omega == 1.0 ? 1 : 0};
+    for (int l = 1; l < nlevels; l++) {
+        const Level& L = ctx->levels[l];
+        key.sig.push_back(L.nb);
+        key.sig.push_back(L.ncolours);
+        key.sig.push_back(V::Acsr(const_cast<Level&>(L)).nnzb);
+    }
+    {
+        std::lock_guard<std::mutex> lock(g_fused_mutex);
+        auto it = g_fused_cache.find(key);
+        if (it != g_fused_cache.end()) {
+            ctx->fused_from[PR] = it->second.first;
+            ctx->fused_ctas[PR] = it->second.second;
+            return FHG_OK;
+        }
+    }
+    Level& L1 = ctx->levels[1];
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemsetAsync(V::b(L1), 0, sizeof(T) * (size_t)L1.n, s));
+    auto time_cycle = [&](double* ms) -> int {
+        for (int w = 0; w < 2; w++) mg_cycle<T>(ctx, 1, V::b(L1), V::x(L1), true);
+        const int reps = 5;
+        CK(cudaEventRecord(ctx->ev0, s));
+        for (int r = 0; r < reps; r++) mg_cycle<T>(ctx, 1, V::b(L1), V::x(L1), true);
+        CK(cudaEventRecord(ctx->ev1, s));
+        CK(cudaEventSynchronize(ctx->ev1));
+        float t = 0;
+        CK(cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1));
+        *ms = t / reps;
+        return FHG_OK;
+    };
+    double best = 0.0;
+    int rc = time_cycle(&best);
+    if (rc) return rc;
+    int best_from = -1, best_ctas = fhg::kClusterCtasPortable;
+    for (int ctas : {fhg::kClusterCtasPortable, fhg::kClusterCtasLarge}) {
+        if (fhg::fused_cycle_clusters<T>(bs, ctas) < 1) continue;
+        for (int l = first; l + 1 < nlevels; l++) {
+            ctx->fused_from[PR] = l;
+            ctx->fused_ctas[PR] = ctas;
+            double ms = 0.0;
+            if ((rc = time_cycle(&ms))) break;
+            if (ms < best) {
+                best = ms;
+                best_from = l;
+                best_ctas = ctas;
+            }
+        }
+        if (rc) break;
+    }
+    ctx->fused_from[PR] = best_from;
+    ctx->fused_ctas[PR] = best_ctas;
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(g_fused_mutex);
+    g_fused_cache[key] = {best_from, best_ctas};
+    return FHG_OK;
+}
+
+// The coarse sub-cycle of every V-cycle precision the context holds: off, by timing (autotuning), or
+// from the first level of at most kFusedDefaultRows block rows with 8 CTAs. Called at setup and when
+// the cycle changes.
+int refresh_fused(fhg_ctx* ctx)
+{
+    const fhg_options& o = ctx->opts;
+    const int bs = ctx->levels[0].bs;
+    const bool fp32 = ctx->levels[0].A32.vals != nullptr, pair = ctx->levels[0].A2.vals != nullptr;
+    for (int p = 0; p < 3; p++) {
+        ctx->fused_from[p] = -1;
+        ctx->fused_ctas[p] = fhg::kClusterCtasPortable;
+    }
+    if (!o.fused_coarse || o.w_loops == FHG_CYCLE_K || !is_gs(o.pre_smoother) || !is_gs(o.post_smoother))
+        return FHG_OK;
+    int rc = FHG_OK;
+    if (o.autotune) {
+        if (fp32 && (rc = choose_fused<float>(ctx))) return rc;
+        if (pair && (rc = choose_fused<dfl>(ctx))) return rc;
+        return cudaStreamSynchronize(ctx->stream) == cudaSuccess ? FHG_OK
+                                                                 : fail(ctx, FHG_ERR_CUDA, "coarse sub-cycle timing failed");
+    }
+    const int first = fused_first_level(ctx, fhg::kFusedDefaultRows);
+    if (first < 0) return FHG_OK;
+    if (fp32 && fhg::fused_cycle_clusters<float>(bs, fhg::kClusterCtasPortable) >= 1) ctx->fused_from[FHG_PREC_FP32] = first;
+    if (pair && fhg::fused_cycle_clusters<dfl>(bs, fhg::kClusterCtasPortable) >= 1) ctx->fused_from[FHG_PREC_DF] = first;
+    return FHG_OK;
 }
 
 // One multigrid cycle on level l (src/Solver/Multigrid/Multigrid.h:438-608): V for w_loops = 1,
@@ -2138,20 +2280,6 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
     // the high part of r: the FP32 V-cycle's right-hand side b32 itself; a buffer of its own otherwise
     if (pair && o.outer_split && (rc = dalloc(ctx, &ctx->rhi, n0))) return rc;
     CK(cudaMallocHost(&ctx->nr_host, sizeof(double)));
-    // The coarse sub-cycle in one cluster launch from the first level (>= 1) from which every level is
-    // small (block rows, colours) and the levels fit the launch parameters.
-    ctx->fused_from = -1;
-    for (int l = 1; l + 1 < nlevels; l++) {
-        bool ok = nlevels - l <= fhg::kFusedMaxLevels;
-        for (int k = l; k < nlevels && ok; k++)
-            ok = ctx->levels[k].nb <= fhg::kFusedMaxRows && (k == nlevels - 1 || ctx->levels[k].ncolours <= fhg::kFusedMaxColours);
-        if (ok) { ctx->fused_from = l; break; }
-    }
-    // the cluster must fit on this device in every value type the context may run
-    if (ctx->fused_from >= 0 && ((fp32 && fhg::fused_cycle_clusters<float>(bs) < 1) ||
-                                 (pair && fhg::fused_cycle_clusters<dfl>(bs) < 1)))
-        ctx->fused_from = -1;
-
     if (o.autotune) {
         // Tune in the precision the V-cycle runs in (the FP64 copies keep the FP32 choices,
         // the same access pattern); the outer operators on their own launches.
@@ -2201,6 +2329,8 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
             L0.Ahat_hi.v.lanes = gd;
         }
     }
+    // the coarse sub-cycle: one cluster launch or launch by launch (timed when autotuning)
+    if ((rc = refresh_fused(ctx))) return rc;
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->ready = true;
     return FHG_OK;
@@ -2508,7 +2638,7 @@ int fhg_set_cycle(fhg_ctx* ctx, int pre_smoother, int post_smoother, int pre_ite
     ctx->opts.pre_iterations = pre_iterations;
     ctx->opts.post_iterations = post_iterations;
     ctx->opts.w_loops = w_loops;
-    return FHG_OK;
+    return refresh_fused(ctx);
 }
 
 int fhg_set_coarse_smoothing(fhg_ctx* ctx, int pre_iterations, int post_iterations)
@@ -2522,6 +2652,7 @@ int fhg_set_coarse_smoothing(fhg_ctx* ctx, int pre_iterations, int post_iteratio
         ctx->rho_plain = 0.0;
         ctx->opts.coarse_pre_iterations = pre_iterations;
         ctx->opts.coarse_post_iterations = post_iterations;
+        return refresh_fused(ctx);
     }
     return FHG_OK;
 }
@@ -2555,6 +2686,14 @@ int fhg_level_info(const fhg_ctx* ctx, int level, int* n_block_rows, long long* 
     if (n_colours) *n_colours = L.ncolours;
     if (lanes) *lanes = L.A.v.lanes;
     if (p_blocks) *p_blocks = L.p_blocks;
+    return FHG_OK;
+}
+
+int fhg_fused_coarse_info(const fhg_ctx* ctx, int precision, int* first_level, int* cluster_ctas)
+{
+    if (!ctx || !ctx->ready || precision < 0 || precision > 2) return FHG_ERR_INVALID_ARG;
+    if (first_level) *first_level = ctx->fused_from[precision];
+    if (cluster_ctas) *cluster_ctas = ctx->fused_ctas[precision];
     return FHG_OK;
 }
 

@@ -4,21 +4,27 @@
 // there is a long chain of short phases: every colour of every smoothing sweep, the residual, the
 // restriction, the coarsest solve, the prolongation. Launched one kernel per phase, each costs a
 // launch slot of a few microseconds while its work takes a fraction of that. Here one thread-block
-// cluster (kClusterCtas CTAs, co-scheduled by the hardware) runs the whole sub-cycle: every phase
+// cluster (8 or 16 CTAs, co-scheduled by the hardware) runs the whole sub-cycle: every phase
 // spreads its rows over all threads of the cluster, and phases are separated by the hardware
 // cluster barrier (barrier.cluster with release/acquire semantics at cluster scope, which orders the
 // global-memory writes of one phase before the reads of the next across the cluster's CTAs). The
 // barrier cannot wait forever: all CTAs of a cluster are resident together and every thread takes
 // the same path through the cycle.
 //
+// A block row is walked by a group of `lanes` threads (block p of the row by lane p mod lanes,
+// partial sums added by shuffles), so that the loads of a row's blocks are in flight together: one
+// thread per row waits for them one after another. The cycle runs as a loop over levels with a
+// count of coarse corrections per level (no device recursion, so the stack is fixed at compile time).
+//
 // The arithmetic is the multigrid cycle of Multigrid::MultigridCycle (src/Solver/Multigrid/
 // Multigrid.h:438-608) on the levels it covers: block Gauss-Seidel / SOR sweeps in colour order
 // (BlockGaussSeidel.h:84-120, BlockSOR.h:199-227), r = b - A x (Multigrid.h:478), R r (Level.h:139-143),
-// recursion (V, or W with WLoops), the coarsest dense solve, x += P e (Level.h:150-154, Multigrid.h:554).
-// Each row is summed block by block in column order by one thread; the FP32 and pair (dfl) value
-// types are instantiated.
+// the coarse correction (V, or W with WLoops: repeated on the same right-hand side, except directly
+// above the coarsest level), the coarsest dense solve, x += P e (Level.h:150-154, Multigrid.h:554).
+// The FP32 and pair (dfl) value types are instantiated.
 #include "fhg_coarse.h"
 
+#include <mutex>
 #include <type_traits>
 
 namespace fhg {
@@ -35,45 +41,94 @@ __device__ __forceinline__ void cluster_sync()
 
 __device__ __forceinline__ void pdl_wait_coarse() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
 
+// Sum over the g lanes of a group (g a power of two <= 32; every lane of the warp calls it).
+__device__ __forceinline__ float lanes_sum(float v, int g)
+{
+    for (int o = g >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, g);
+    return v;
+}
+
+__device__ __forceinline__ dfl lanes_sum(dfl v, int g)
+{
+    for (int o = g >> 1; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, v.h, o, g);
+        const float ol = __shfl_xor_sync(0xffffffffu, v.l, o, g);
+        df_add(v.h, v.l, oh, ol);
+    }
+    return v;
+}
+
+__device__ __forceinline__ double lanes_sum(double v, int g)
+{
+    for (int o = g >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, g);
+    return v;
+}
+
 template <class T>
 struct Ctx {
     const FusedCycle<T>& P;
     long long t, nthr;   // thread index within the cluster, threads of the cluster
 };
 
-// One colour [c0, c1) of a block GS / SOR sweep on level L.
+// Rows [r0, r1) of a phase, `g` lanes per row: calls f(i, valid, lane) in passes that every thread
+// of the cluster takes the same number of times (the shuffles of a group need all lanes of the warp).
+template <class T, class F>
+__device__ __forceinline__ void row_passes(const Ctx<T>& C, long long r0, long long r1, int g, F f)
+{
+    const long long gid = C.t / g, ngroups = C.nthr / g;
+    const int lane = (int)(C.t % g);
+    const long long passes = (r1 - r0 + ngroups - 1) / ngroups;
+    for (long long ps = 0; ps < passes; ps++) {
+        const long long i = r0 + ps * ngroups + gid;
+        f(i, i < r1, lane);
+    }
+}
+
+// acc = sum over the blocks of row i (the diagonal block left out when skip_diag) of A_ij x_j, walked
+// by the g lanes of a group and summed over them: every lane ends with the row's whole sum.
+template <class T, int BS>
+__device__ __forceinline__ void row_product(long long i, bool valid, int lane, int g, const int* __restrict__ rowptr,
+                                            const int* __restrict__ colidx, const T* __restrict__ vals, long long ld,
+                                            const T* x, bool skip_diag, T* acc)
+{
+#pragma unroll
+    for (int r = 0; r < BS; r++) acc[r] = T(0);
+    if (valid) {
+        const int p1 = rowptr[i + 1];
+        for (int p = rowptr[i] + lane; p < p1; p += g) {
+            const long long j = colidx[p];
+            if (skip_diag && j == i) continue;
+            T xv[BS];
+#pragma unroll
+            for (int c = 0; c < BS; c++) xv[c] = x[j * BS + c];
+#pragma unroll
+            for (int r = 0; r < BS; r++)
+#pragma unroll
+                for (int c = 0; c < BS; c++) acc[r] = fma(vals[(long long)(r * BS + c) * ld + p], xv[c], acc[r]);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < BS; r++) acc[r] = lanes_sum(acc[r], g);
+}
+
+// One colour [c0, c1) of a block GS / SOR sweep on level L: x_i <- D_i^-1 (b_i - sum_{j != i} A_ij x_j),
+// relaxed by omega; output r of a row written by lane r (lanes loop when BS > lanes).
 template <class T, int BS>
 __device__ void gs_colour(const Ctx<T>& C, const FusedLevel<T>& L, int c0, int c1)
 {
     const T w = C.P.omega;
-    for (long long i = c0 + C.t; i < c1; i += C.nthr) {
+    row_passes(C, c0, c1, L.lanes, [&](long long i, bool valid, int lane) {
         T acc[BS];
-#pragma unroll
-        for (int r = 0; r < BS; r++) acc[r] = T(0);
-        const int p1 = L.a_rowptr[i + 1];
-        for (int p = L.a_rowptr[i]; p < p1; p++) {
-            const long long j = L.a_colidx[p];
-            if (j == i) continue;
-            T xv[BS];
-#pragma unroll
-            for (int c = 0; c < BS; c++) xv[c] = L.x[j * BS + c];
-#pragma unroll
-            for (int r = 0; r < BS; r++)
-#pragma unroll
-                for (int c = 0; c < BS; c++) acc[r] = fma(L.a_vals[(long long)(r * BS + c) * L.a_ld + p], xv[c], acc[r]);
-        }
-        T t[BS];
-#pragma unroll
-        for (int c = 0; c < BS; c++) t[c] = L.b[i * BS + c] - acc[c];
-#pragma unroll
-        for (int r = 0; r < BS; r++) {
+        row_product<T, BS>(i, valid, lane, L.lanes, L.a_rowptr, L.a_colidx, L.a_vals, L.a_ld, L.x, true, acc);
+        if (!valid) return;
+        for (int r = lane; r < BS; r += L.lanes) {
             T v = T(0);
 #pragma unroll
-            for (int c = 0; c < BS; c++) v = fma(L.dinv[(long long)(r * BS + c) * L.nb + i], t[c], v);
+            for (int c = 0; c < BS; c++) v = fma(L.dinv[(long long)(r * BS + c) * L.nb + i], L.b[i * BS + c] - acc[c], v);
             if (w != T(1)) v = fma(w, v, (T(1) - w) * L.x[i * BS + r]);
             L.x[i * BS + r] = fin(v);
         }
-    }
+    });
     cluster_sync();
 }
 
@@ -103,50 +158,26 @@ __device__ void smooth(const Ctx<T>& C, const FusedLevel<T>& L, int code, int it
 template <class T, int BS>
 __device__ void residual(const Ctx<T>& C, const FusedLevel<T>& L)
 {
-    for (long long i = C.t; i < L.nb; i += C.nthr) {
+    row_passes(C, 0, L.nb, L.lanes, [&](long long i, bool valid, int lane) {
         T acc[BS];
-#pragma unroll
-        for (int r = 0; r < BS; r++) acc[r] = T(0);
-        const int p1 = L.a_rowptr[i + 1];
-        for (int p = L.a_rowptr[i]; p < p1; p++) {
-            const long long j = L.a_colidx[p];
-            T xv[BS];
-#pragma unroll
-            for (int c = 0; c < BS; c++) xv[c] = L.x[j * BS + c];
-#pragma unroll
-            for (int r = 0; r < BS; r++)
-#pragma unroll
-                for (int c = 0; c < BS; c++) acc[r] = fma(L.a_vals[(long long)(r * BS + c) * L.a_ld + p], xv[c], acc[r]);
-        }
-#pragma unroll
-        for (int r = 0; r < BS; r++) L.r[i * BS + r] = L.b[i * BS + r] - acc[r];
-    }
+        row_product<T, BS>(i, valid, lane, L.lanes, L.a_rowptr, L.a_colidx, L.a_vals, L.a_ld, L.x, false, acc);
+        if (!valid) return;
+        for (int r = lane; r < BS; r += L.lanes) L.r[i * BS + r] = L.b[i * BS + r] - acc[r];
+    });
     cluster_sync();
 }
 
 // out (rows of M) = M in, or out += M in: the transfers as block products over CSR operators.
 template <class T, int BS>
-__device__ void product(const Ctx<T>& C, int rows, const int* rowptr, const int* colidx, const T* vals, long long ld,
-                        const T* in, T* out, bool add)
+__device__ void product(const Ctx<T>& C, int rows, int g, const int* rowptr, const int* colidx, const T* vals,
+                        long long ld, const T* in, T* out, bool add)
 {
-    for (long long i = C.t; i < rows; i += C.nthr) {
+    row_passes(C, 0, rows, g, [&](long long i, bool valid, int lane) {
         T acc[BS];
-#pragma unroll
-        for (int r = 0; r < BS; r++) acc[r] = T(0);
-        const int p1 = rowptr[i + 1];
-        for (int p = rowptr[i]; p < p1; p++) {
-            const long long j = colidx[p];
-            T xv[BS];
-#pragma unroll
-            for (int c = 0; c < BS; c++) xv[c] = in[j * BS + c];
-#pragma unroll
-            for (int r = 0; r < BS; r++)
-#pragma unroll
-                for (int c = 0; c < BS; c++) acc[r] = fma(vals[(long long)(r * BS + c) * ld + p], xv[c], acc[r]);
-        }
-#pragma unroll
-        for (int r = 0; r < BS; r++) out[i * BS + r] = add ? out[i * BS + r] + acc[r] : fin(acc[r]);
-    }
+        row_product<T, BS>(i, valid, lane, g, rowptr, colidx, vals, ld, in, false, acc);
+        if (!valid) return;
+        for (int r = lane; r < BS; r += g) out[i * BS + r] = add ? out[i * BS + r] + acc[r] : fin(acc[r]);
+    });
     cluster_sync();
 }
 
@@ -157,63 +188,100 @@ __device__ void zero(const Ctx<T>& C, T* x, long long n)
     cluster_sync();
 }
 
-// The coarsest level: x = C^{-1} b, C^{-1} dense FP64 row-major, FP64 accumulation.
+// The coarsest level: x = C^{-1} b, C^{-1} dense FP64 row-major, FP64 accumulation; 8 lanes a row.
 template <class T>
 __device__ void coarse_solve(const Ctx<T>& C, const FusedLevel<T>& L)
 {
     const long long n = C.P.n_coarse;
-    for (long long i = C.t; i < n; i += C.nthr) {
-        const double* a = C.P.cinv + i * n;
+    row_passes(C, 0, n, 8, [&](long long i, bool valid, int lane) {
         double acc = 0.0;
-        for (long long j = 0; j < n; j++) acc = fma(a[j], (double)L.b[j], acc);
-        L.x[i] = T(acc);
-    }
+        if (valid) {
+            const double* a = C.P.cinv + i * n;
+            for (long long j = lane; j < n; j += 8) acc = fma(a[j], (double)L.b[j], acc);
+        }
+        acc = lanes_sum(acc, 8);
+        if (valid && lane == 0) L.x[i] = T(acc);
+    });
     cluster_sync();
 }
 
+// The cycle from lev[0] down: descend (zero x on a fresh level, pre-smooth, residual, restrict) to the
+// coarsest, solve there, then ascend (prolongate, post-smooth) until a level still owes a coarse
+// correction (W-cycle), from which the next descent starts with the coarser level's x kept.
 template <class T, int BS>
-__device__ void cycle(const Ctx<T>& C, int l, bool x_zero)
+__device__ void run_cycle(const Ctx<T>& C)
 {
-    const FusedLevel<T>& L = C.P.lev[l];
-    if (l == C.P.nlev - 1) {
-        coarse_solve(C, L);
-        return;
+    const FusedCycle<T>& P = C.P;
+    const int last = P.nlev - 1;
+    int done[kFusedMaxLevels];   // coarse corrections completed on each level of the current descent
+    int l = 0;
+    bool xz = P.x_zero != 0;
+    while (true) {
+        for (; l < last; l++) {
+            const FusedLevel<T>& L = P.lev[l];
+            const FusedLevel<T>& N = P.lev[l + 1];
+            if (xz) zero(C, L.x, (long long)L.nb * BS);
+            smooth<T, BS>(C, L, P.pre, P.npre);
+            residual<T, BS>(C, L);
+            product<T, BS>(C, N.nb, L.t_lanes, L.r_rowptr, L.r_colidx, L.r_vals, L.r_ld, L.r, N.b, false);
+            done[l] = 0;
+            xz = true;
+        }
+        coarse_solve(C, P.lev[last]);
+        bool again = false;
+        while (l > 0) {
+            l--;
+            done[l]++;
+            const int loops = (l + 1 == last || P.w_loops < 1) ? 1 : P.w_loops;
+            if (done[l] < loops) {
+                again = true;
+                break;
+            }
+            const FusedLevel<T>& L = P.lev[l];
+            const FusedLevel<T>& N = P.lev[l + 1];
+            product<T, BS>(C, L.nb, L.lanes, L.p_rowptr, L.p_colidx, L.p_vals, L.p_ld, N.x, L.x, true);
+            smooth<T, BS>(C, L, P.post, P.npost);
+        }
+        if (!again) return;
+        l++;          // the next coarse correction of level l - 1 starts on level l
+        xz = false;   // from the x the previous one left
     }
-    const FusedLevel<T>& N = C.P.lev[l + 1];
-    if (x_zero) zero(C, L.x, (long long)L.nb * BS);
-    smooth<T, BS>(C, L, C.P.pre, C.P.npre);
-    residual<T, BS>(C, L);
-    product<T, BS>(C, N.nb, L.r_rowptr, L.r_colidx, L.r_vals, L.r_ld, L.r, N.b, false);
-    const int loops = C.P.w_loops > 1 ? C.P.w_loops : 1;
-    for (int w = 0; w < loops; w++) {
-        cycle<T, BS>(C, l + 1, w == 0);
-        if (l + 1 == C.P.nlev - 1) break;
-    }
-    product<T, BS>(C, L.nb, L.p_rowptr, L.p_colidx, L.p_vals, L.p_ld, N.x, L.x, true);
-    smooth<T, BS>(C, L, C.P.post, C.P.npost);
 }
 
 template <class T, int BS>
-__global__ void __launch_bounds__(kFusedThreads) k_fused_cycle(const __grid_constant__ FusedCycle<T> P)
+__global__ void __launch_bounds__(kFusedThreads, 1) k_fused_cycle(const __grid_constant__ FusedCycle<T> P)
 {
     pdl_wait_coarse();
     const Ctx<T> C{P, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x};
-    cycle<T, BS>(C, 0, P.x_zero != 0);
+    run_cycle<T, BS>(C);
 }
 
-}  // namespace
-
-namespace {
+template <class T, int BS>
+void* kernel_of()
+{
+    return (void*)k_fused_cycle<T, BS>;
+}
 
 template <class T>
-void fused_config(cudaLaunchConfig_t& cfg, cudaLaunchAttribute* attr, cudaStream_t s)
+void* kernel_for(int bs)
+{
+    switch (bs) {
+    case 2: return kernel_of<T, 2>();
+    case 3: return kernel_of<T, 3>();
+    case 4: return kernel_of<T, 4>();
+    case 6: return kernel_of<T, 6>();
+    default: return nullptr;
+    }
+}
+
+void fused_config(cudaLaunchConfig_t& cfg, cudaLaunchAttribute* attr, int ctas, cudaStream_t s)
 {
     cfg = {};
-    cfg.gridDim = dim3(kClusterCtas);
+    cfg.gridDim = dim3(ctas);
     cfg.blockDim = dim3(kFusedThreads);
     cfg.stream = s;
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = kClusterCtas;
+    attr[0].val.clusterDim.x = ctas;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -222,51 +290,44 @@ void fused_config(cudaLaunchConfig_t& cfg, cudaLaunchAttribute* attr, cudaStream
     cfg.numAttrs = 2;
 }
 
-template <class T, int BS>
-int clusters_of()
+// Clusters above the portable size need the kernel's opt-in attribute, set once per kernel.
+std::mutex g_fused_attr_mutex;
+
+cudaError_t allow_large_clusters(const void* k)
 {
+    std::lock_guard<std::mutex> lock(g_fused_attr_mutex);
+    return cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+}
+
+}  // namespace
+
+template <class T>
+int fused_cycle_clusters(int bs, int ctas)
+{
+    const void* k = kernel_for<T>(bs);
+    if (!k || (ctas != kClusterCtasPortable && ctas != kClusterCtasLarge)) return 0;
+    if (ctas > kClusterCtasPortable && allow_large_clusters(k) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[2];
-    fused_config<T>(cfg, attr, nullptr);
+    fused_config(cfg, attr, ctas, nullptr);
     cfg.numAttrs = 1;
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, k_fused_cycle<T, BS>, &cfg) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveClusters(&n, k, &cfg) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
     return n;
 }
 
-}  // namespace
-
 template <class T>
-int fused_cycle_clusters(int bs)
+cudaError_t launch_fused_cycle(const FusedCycle<T>& P, int bs, int ctas, cudaStream_t s)
 {
-    switch (bs) {
-    case 2: return clusters_of<T, 2>();
-    case 3: return clusters_of<T, 3>();
-    case 4: return clusters_of<T, 4>();
-    case 6: return clusters_of<T, 6>();
-    default: return 0;
-    }
-}
-
-template <class T>
-cudaError_t launch_fused_cycle(const FusedCycle<T>& P, int bs, cudaStream_t s)
-{
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(kClusterCtas);
-    cfg.blockDim = dim3(kFusedThreads);
-    cfg.stream = s;
+    cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[2];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = kClusterCtas;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[1].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 2;
+    fused_config(cfg, attr, ctas, s);
     switch (bs) {
     case 2: return cudaLaunchKernelEx(&cfg, k_fused_cycle<T, 2>, P);
     case 3: return cudaLaunchKernelEx(&cfg, k_fused_cycle<T, 3>, P);
@@ -276,9 +337,9 @@ cudaError_t launch_fused_cycle(const FusedCycle<T>& P, int bs, cudaStream_t s)
     }
 }
 
-template cudaError_t launch_fused_cycle<float>(const FusedCycle<float>&, int, cudaStream_t);
-template cudaError_t launch_fused_cycle<dfl>(const FusedCycle<dfl>&, int, cudaStream_t);
-template int fused_cycle_clusters<float>(int);
-template int fused_cycle_clusters<dfl>(int);
+template cudaError_t launch_fused_cycle<float>(const FusedCycle<float>&, int, int, cudaStream_t);
+template cudaError_t launch_fused_cycle<dfl>(const FusedCycle<dfl>&, int, int, cudaStream_t);
+template int fused_cycle_clusters<float>(int, int);
+template int fused_cycle_clusters<dfl>(int, int);
 
 }  // namespace fhg

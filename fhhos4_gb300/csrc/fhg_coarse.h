@@ -7,11 +7,13 @@
 
 namespace fhg {
 
-constexpr int kClusterCtas = 8;        // CTAs of the one cluster (the portable maximum)
-constexpr int kFusedThreads = 512;     // threads per CTA
-constexpr int kFusedMaxLevels = 6;     // levels of a fused sub-cycle, the coarsest included
+constexpr int kClusterCtasPortable = 8;   // CTAs of the one cluster: the portable maximum, or
+constexpr int kClusterCtasLarge = 16;     // the non-portable one where the device runs it
+constexpr int kFusedThreads = 512;        // threads per CTA
+constexpr int kFusedMaxLevels = 6;        // levels of a fused sub-cycle, the coarsest included
 constexpr int kFusedMaxColours = 24;
-constexpr int kFusedMaxRows = 65536;   // block rows of the largest level a fused sub-cycle takes
+constexpr int kFusedMaxRows = 65536;      // block rows of the largest level a fused sub-cycle takes
+constexpr int kFusedDefaultRows = 8192;   // the same without timing at setup (autotuning off)
 
 // Smoother directions of a fused sub-cycle (the GS codes; Jacobi is not fused).
 enum { kFusedForward = 0, kFusedBackward = 1, kFusedSymmetric = 2, kFusedAlternatingForward = 3,
@@ -20,10 +22,11 @@ enum { kFusedForward = 0, kFusedBackward = 1, kFusedSymmetric = 2, kFusedAlterna
 // One level of the sub-cycle in the launch parameters: A in CSR form (all blocks, entry-major values,
 // leading dimension a_ld), D^-1 entry-major (leading dimension nb), the colour offsets, P (this
 // level's rows, the next level's columns) and R = P^T (the next level's rows), and the level's x, b
-// and residual vectors. On the coarsest level only x and b are used.
+// and residual vectors. `lanes` threads (4, 8 or 16) walk one block row of A, `t_lanes` one row of R.
+// On the coarsest level only x and b are used.
 template <class T>
 struct FusedLevel {
-    int nb = 0, ncol = 0;
+    int nb = 0, ncol = 0, lanes = 8, t_lanes = 8;
     int colour_start[kFusedMaxColours + 1] = {};
     const int* a_rowptr = nullptr;
     const int* a_colidx = nullptr;
@@ -54,10 +57,12 @@ struct FusedCycle {
     FusedLevel<T> lev[kFusedMaxLevels];
 };
 
+// One cluster of `ctas` CTAs (kClusterCtasPortable or kClusterCtasLarge).
 template <class T>
-cudaError_t launch_fused_cycle(const FusedCycle<T>& P, int bs, cudaStream_t s);
-// Clusters of the fused kernel that fit on the current device at once (0: it cannot run here).
+cudaError_t launch_fused_cycle(const FusedCycle<T>& P, int bs, int ctas, cudaStream_t s);
+// Clusters of `ctas` CTAs of the fused kernel that fit on the current device at once (0: it cannot
+// run here).
 template <class T>
-int fused_cycle_clusters(int bs);
+int fused_cycle_clusters(int bs, int ctas);
 
 }  // namespace fhg

@@ -132,10 +132,15 @@ typedef struct {
                                    tolerance in FP64 is evaluated again in compensated arithmetic. No counterpart
                                    in the reference. */
     int fused_coarse;           /* 1 (default): with GS / SOR smoothers and a V or W cycle in FP32 or DF, the cycle
-                                   below the first level from which every level has at most 65,536 block rows runs
-                                   as one thread-block-cluster launch (phases separated by the cluster barrier)
-                                   instead of one launch per colour and product; 0: launch by launch. Same
-                                   arithmetic up to the summation order of a row. */
+                                   below some level (>= 1) runs as one thread-block-cluster launch (8 or 16 CTAs,
+                                   phases separated by the cluster barrier) instead of one launch per colour and
+                                   product. With autotune, setup (and fhg_set_cycle / fhg_set_coarse_smoothing)
+                                   times one cycle below level 0 launch by launch and fused from every eligible
+                                   level (every level below it at most 65,536 block rows and 24 colours, at most
+                                   6 levels) and keeps the fastest, per precision and hierarchy structure;
+                                   without, it fuses from the first level of at most 8,192 block rows with 8
+                                   CTAs. 0: launch by launch. Same arithmetic up to the summation order of a
+                                   row. */
 } fhg_options;
 
 typedef struct {
@@ -223,6 +228,11 @@ int fhg_set_vcycle_precision(fhg_ctx* ctx, int precision);
  * of the A operator, stored blocks of P (0 on the coarsest). */
 int fhg_level_info(const fhg_ctx* ctx, int level, int* n_block_rows, long long* n_blocks,
                    int* n_colours, int* lanes, long long* p_blocks);
+
+/* The coarse sub-cycle of V-cycle precision `precision` (FHG_PREC_FP32 or FHG_PREC_DF) as the context
+ * runs it now: the first level of the one-launch sub-cycle (-1: launch by launch) and the CTAs of its
+ * cluster. No counterpart in the reference. */
+int fhg_fused_coarse_info(const fhg_ctx* ctx, int precision, int* first_level, int* cluster_ctas);
 
 /* The colour permutation of `level` after setup: perm[new_block_row] = given_block_row. */
 int fhg_get_permutation(const fhg_ctx* ctx, int level, int* perm);

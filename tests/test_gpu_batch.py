@@ -12,8 +12,10 @@ pytestmark = pytest.mark.gpu
 
 def _specs():
     from fhhos4_gb300.batch import ProblemSpec
+    # the last one has the deepest hierarchy of the batched workload (n = 256, k = 3: six levels, the
+    # coarse ones in one cluster launch inside the graph's loop body)
     return [ProblemSpec(32, 1, 11), ProblemSpec(48, 3, 12), ProblemSpec(64, 2, 13), ProblemSpec(80, 1, 14),
-            ProblemSpec(32, 2, 15), ProblemSpec(96, 3, 16)]
+            ProblemSpec(32, 2, 15), ProblemSpec(96, 3, 16), ProblemSpec(256, 3, 17)]
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])

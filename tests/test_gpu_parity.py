@@ -264,7 +264,8 @@ def test_df_vcycle_matches_reference(case, variant, pre, post, cycle, omega_key,
 
 
 @pytest.mark.parametrize("precision,cycle,pre,post", [("fp32", "V", "bgs", "rbgs"), ("df", "V", "bgs", "rbgs"),
-                                                       ("df", "W", "sbgs", "sbgs"), ("fp32", "V", "bsor", "rbsor")])
+                                                       ("df", "W", "sbgs", "sbgs"), ("fp32", "W", "bgs", "rbgs"),
+                                                       ("fp32", "V", "bsor", "rbsor")])
 def test_fused_coarse_cycle_matches_launch_by_launch(case, precision, cycle, pre, post):
     """The coarse sub-cycle as one cluster launch against the same cycle launched phase by phase:
     the same arithmetic up to the summation order of a row, so FP64-class solves agree to 1e-10
@@ -273,14 +274,43 @@ def test_fused_coarse_cycle_matches_launch_by_launch(case, precision, cycle, pre
               omega=float(case["sor_omega"]) if pre == "bsor" else 1.0)
     a = S().fcg_mg(case.As, case.Ps, case.bs, fused=True, **kw)
     b = S().fcg_mg(case.As, case.Ps, case.bs, fused=False, **kw)
-    xa, xb = a.Solve(case.b), b.Solve(case.b)
+    first, ctas = a._ctx.fused_coarse_info(precision)
+    if len(case.As) >= 3:
+        assert 1 <= first <= len(case.As) - 2 and ctas == 8
+    assert b._ctx.fused_coarse_info(precision)[0] == -1
+    _check_fused_pair(case.As[0], case.b, a, b, precision)
+
+
+def _check_fused_pair(A0, rhs, a, b, precision):
+    xa, xb = a.Solve(rhs), b.Solve(rhs)
     if precision == "df":
         assert a.IterationCount == b.IterationCount
         assert np.all(np.abs(a.History - b.History) <= 1e-10 * np.abs(b.History) + 64 * HIST_ATOL)
         assert np.linalg.norm(xa - xb) <= 1e-10 * np.linalg.norm(xb)
     else:
         assert abs(a.IterationCount - b.IterationCount) <= 1
-        assert true_rel_residual(case.As[0], case.b, xa) < 1e-8 * (1 + 1e-6)
+        assert true_rel_residual(A0, rhs, xa) < 1e-8 * (1 + 1e-6)
+
+
+@pytest.mark.parametrize("precision,cycle", [("fp32", "V"), ("df", "V"), ("df", "W")])
+def test_fused_coarse_cycle_deep_hierarchy(precision, cycle):
+    """A deep 2D hierarchy (n = 256, k = 3: six levels, Galerkin coarse operators, the largest
+    problem of the batched workload), fused from every eligible level and chosen by timing: the same
+    answers as launch by launch. The sub-cycle runs as a loop over levels with fixed stack use."""
+    from fhhos4_gb300 import batch as BT
+    bs, A0, Ps, b, levels = BT.generate(BT.ProblemSpec(256, 3, 4242))
+    As = [A0]
+    for P in Ps:
+        As.append((P.T @ As[-1] @ P).tocsr())
+    kw = dict(precision=precision, cycle=cycle, pre="bgs", post="rbgs", galerkin=True)
+    b_ = S().fcg_mg(As, Ps, bs, fused=False, **kw)
+    for autotune in (False, True):
+        a = S().fcg_mg(As, Ps, bs, fused=True, autotune=autotune, **kw)
+        first, ctas = a._ctx.fused_coarse_info(precision)
+        assert first == -1 or (1 <= first <= len(As) - 2 and ctas in (8, 16))
+        if not autotune:
+            assert first >= 1
+        _check_fused_pair(A0, b, a, b_, precision)
 
 
 def _pairs(torch, v):
