@@ -322,6 +322,29 @@ def measure_methods(ctx, dist, dev, b_dev, x_dev, maxit, methods, warmup, steps,
     return results, launches, clocks, solutions
 
 
+def gpu_post_processing(H, x, dev):
+    """Cell unknowns and the L2 error of the k+1 reconstruction of the headline solution on the GPU
+    (fhg_post_run), beside the host's evaluation of the same x."""
+    import torch
+    from fhhos4_gb300 import _native as N
+    t = H.post_tables()
+    post = N.Post(t, dev)
+    try:
+        xd = torch.from_numpy(x).to(f"cuda:{dev}")
+        cells = torch.empty(t["n_elements"] * t["n_cell"], dtype=torch.float64, device=f"cuda:{dev}")
+        post.run(xd.data_ptr(), cells.data_ptr(), "sine")
+        err, ms = post.run(xd.data_ptr(), cells.data_ptr(), "sine")
+    finally:
+        post.close()
+    t0 = time.perf_counter()
+    host = H.l2_error(x)
+    host_s = time.perf_counter() - t0
+    return {"what": "cell unknowns + k+1 reconstruction + relative L2 error vs the exact solution",
+            "l2_error_gpu": err, "l2_error_host": host, "gpu_ms": round(ms, 3), "host_s": round(host_s, 3),
+            "elements": int(t["n_elements"]), "element_classes": int(t["n_classes"]),
+            "quadrature_points": int(t["n_points"])}
+
+
 def run_ours(args, dist: Dist):
     import torch
     from fhhos4_gb300 import _native as N
@@ -383,6 +406,9 @@ def run_ours(args, dist: Dist):
         results[name]["rel_diff_vs_plain_fp64"] = float(np.linalg.norm(solutions[name] - x64) / np.linalg.norm(x64))
         if args.source == "sine" and H is not None:
             results[name]["l2_error_vs_exact"] = H.l2_error(solutions[name])
+    post_info = None
+    if args.source == "sine" and H is not None:
+        post_info = gpu_post_processing(H, solutions["learned" if have_learned else "fast"], dev)
     if H is not None:
         H.close()
 
@@ -530,6 +556,7 @@ def run_ours(args, dist: Dist):
         "gpu_launches": int(launches[head]),
         "clocks": clk,
         "setup_s": {"hierarchy_generation": round(gen_s, 2), "gpu_setup": round(setup_s, 2)},
+        "post_processing": post_info,
         "cpu_baseline": cpu,
     }
     ctx.close()

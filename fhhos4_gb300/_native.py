@@ -45,7 +45,8 @@ EXPORTS = ["fhg_default_options", "fhg_create", "fhg_destroy", "fhg_last_error",
            "fhg_learned_reference_rate", "fhg_learned_features", "fhg_apply_internal", "fhg_net_num_params",
            "fhg_net_create", "fhg_net_destroy", "fhg_net_last_error", "fhg_net_set_params", "fhg_net_get_params",
            "fhg_net_train_step", "fhg_io_buffers", "fhg_io_upload", "fhg_io_download", "fhg_batch_create", "fhg_batch_destroy", "fhg_batch_last_error",
-           "fhg_batch_add", "fhg_batch_solve"]
+           "fhg_batch_add", "fhg_batch_solve", "fhg_post_create", "fhg_post_run", "fhg_post_last_error",
+           "fhg_post_destroy"]
 
 FHG_NOALLOC_MAX_PARTIALS = 131072
 
@@ -134,6 +135,12 @@ def load(path: str = LIB):
     lib.fhg_batch_last_error.restype = C.c_char_p
     lib.fhg_batch_add.argtypes = [C.c_void_p, C.c_void_p]
     lib.fhg_batch_solve.argtypes = [C.c_void_p, C.c_void_p, P(C.c_double)]
+    lib.fhg_post_create.argtypes = [P(C.c_void_p)] + [C.c_int] * 8 + [C.c_void_p] * 9
+    lib.fhg_post_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, P(C.c_double), P(C.c_double)]
+    lib.fhg_post_last_error.argtypes = [C.c_void_p]
+    lib.fhg_post_last_error.restype = C.c_char_p
+    lib.fhg_post_destroy.argtypes = [C.c_void_p]
+    lib.fhg_post_destroy.restype = None
     _lib = lib
     return lib
 
@@ -317,6 +324,50 @@ class Batch:
     def close(self):
         if self.h:
             self.lib.fhg_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+EXACT = {"none": 0, "sine": 1}
+
+
+class Post:
+    """Owns one fhg_post: the finest level's element tables on a GPU, for cell-unknown recovery and
+    the L2 error of the k+1 reconstruction (tables as fhhos4_gb300.hho.Hierarchy.post_tables gives)."""
+
+    def __init__(self, tables: dict, device: int = 0):
+        self.lib = load()
+        self.h = C.c_void_p()
+        t = {k: np.ascontiguousarray(v) for k, v in tables.items() if isinstance(v, np.ndarray)}
+        self._keep = t
+        self.n_elements, self.n_cell = int(tables["n_elements"]), int(tables["n_cell"])
+        self._check(self.lib.fhg_post_create(
+            C.byref(self.h), device, int(tables["dim"]), self.n_elements, int(tables["n_classes"]), self.n_cell,
+            int(tables["n_face_dofs"]), int(tables["n_recon"]), int(tables["n_points"]),
+            ptr(t["elem_class"]), ptr(t["elem_faces"]), ptr(t["elem_centre"]), ptr(t["cell_rhs"]),
+            ptr(t["solve_cells"]), ptr(t["recon"]), ptr(t["weights"]), ptr(t["offsets"]), ptr(t["basis"])))
+
+    def _check(self, rc: int):
+        if rc != FHG_OK:
+            msg = self.lib.fhg_post_last_error(self.h).decode() if self.h else "no post-processing handle"
+            raise FhgError(rc, msg)
+
+    def run(self, x_faces_dev: int, x_cells_dev: int = 0, exact: str = "sine"):
+        """(relative L2 error or None, device ms) for the face solution at device address x_faces_dev;
+        cell unknowns written to x_cells_dev (n_elements x n_cell doubles) when given."""
+        err, ms = C.c_double(), C.c_double()
+        self._check(self.lib.fhg_post_run(self.h, C.c_void_p(x_faces_dev), C.c_void_p(x_cells_dev) if x_cells_dev else None,
+                                          EXACT[exact], C.byref(err), C.byref(ms)))
+        return (err.value if exact != "none" else None), ms.value
+
+    def close(self):
+        if self.h:
+            self.lib.fhg_post_destroy(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):

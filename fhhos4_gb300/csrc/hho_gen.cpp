@@ -1510,6 +1510,80 @@ int fhg_hho_l2_error(const fhg_hho* h, const double* x, double* rel_error)
     return 0;
 }
 
+// Sizes of the post-processing tables of the finest level (fhg_hho_post_tables).
+int fhg_hho_post_sizes(const fhg_hho* h, int* n_elements, int* n_classes, int* n_cell, int* n_face_dofs,
+                       int* n_recon, int* n_points)
+{
+    if (!h || h->levels.empty()) return -1;
+    const Level& L = h->levels[0];
+    const ElementOps& O = L.cls_ops[0];
+    if (n_elements) *n_elements = (int)L.mesh.el.size();
+    if (n_classes) *n_classes = (int)L.cls_ops.size();
+    if (n_cell) *n_cell = O.nC;
+    if (n_face_dofs) *n_face_dofs = O.nF * O.nf;
+    if (n_recon) *n_recon = O.nR;
+    if (n_points) *n_points = (int)h->rules.cell_rhs.w.size();
+    return 0;
+}
+
+// The finest level's data for recovering cell unknowns and evaluating the k+1 reconstruction
+// (Diffusion_HHO.h:855-912) element by element: per element its class, the unknown block of each
+// local face (-1: Dirichlet), its centroid (3 doubles) and A_TT^{-1} b_T; per class -A_TT^{-1} A_TF
+// (nC x nFF), the reconstruction [nR x (nC + nFF)], and at the cell quadrature points (the rule of
+// the L2 error) the weights, the offsets from the centroid (3 doubles each) and the reconstruction
+// basis values (nq x nR). Elements of one class differ by a translation, so the offsets, weights and
+// basis values of its first element serve them all.
+int fhg_hho_post_tables(const fhg_hho* h, int* elem_class, int* elem_faces, double* elem_centre, double* cell_rhs,
+                        double* solve_cells, double* recon, double* weights, double* offsets, double* basis)
+{
+    if (!h || h->levels.empty()) return -1;
+    const Level& L = h->levels[0];
+    const Mesh& M = L.mesh;
+    const int dim = M.dim, nF = dim + 1;
+    const size_t ne = M.el.size();
+    const size_t ncls = L.cls_ops.size();
+    const int nC = L.cls_ops[0].nC, nFF = nF * L.cls_ops[0].nf, nR = L.cls_ops[0].nR;
+    const size_t nq = h->rules.cell_rhs.w.size();
+    std::vector<long long> first(ncls, -1);
+    for (size_t e = 0; e < ne; e++) {
+        const int c = L.cls[e];
+        if (first[c] < 0) first[c] = (long long)e;
+        if (elem_class) elem_class[e] = c;
+        if (elem_faces)
+            for (int lf = 0; lf < nF; lf++) elem_faces[e * nF + lf] = M.number[M.ef[e][lf]];
+        if (elem_centre) {
+            const auto xc = centroid(M, (int)e);
+            for (int d = 0; d < 3; d++) elem_centre[e * 3 + d] = xc[d];
+        }
+        if (cell_rhs)
+            for (int c2 = 0; c2 < nC; c2++) cell_rhs[e * nC + c2] = L.cell_rhs_e[e * nC + c2];
+    }
+    for (size_t c = 0; c < ncls; c++) {
+        const ElementOps& O = L.cls_ops[c];
+        if (solve_cells)
+            for (int i = 0; i < nC; i++)
+                for (int j = 0; j < nFF; j++) solve_cells[(c * nC + i) * nFF + j] = O.solve_cells(i, j);
+        if (recon)
+            for (int i = 0; i < nR; i++)
+                for (int j = 0; j < nC + nFF; j++) recon[(c * nR + i) * (nC + nFF) + j] = O.P(i, j);
+        const int e = (int)first[c];
+        if (e < 0) continue;
+        const auto xc = centroid(M, e);
+        const QPts Q = element_points(M, e, h->rules.cell_rhs);
+        double vals[64];
+        for (size_t q = 0; q < nq; q++) {
+            if (weights) weights[c * nq + q] = Q.w[q];
+            if (offsets)
+                for (int d = 0; d < 3; d++) offsets[(c * nq + q) * 3 + d] = Q.x[q][d] - xc[d];
+            if (basis) {
+                O.basis.eval_at(Q.x[q].data(), xc.data(), vals, nullptr);
+                for (int i = 0; i < nR; i++) basis[(c * nq + q) * nR + i] = vals[i];
+            }
+        }
+    }
+    return 0;
+}
+
 int fhg_hho_rhs(const fhg_hho* h, const double** b)
 {
     if (!h || h->levels.empty()) return -1;

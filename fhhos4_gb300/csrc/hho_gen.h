@@ -49,6 +49,16 @@ int fhg_hho_rhs(const fhg_hho* h, const double** b);
 /* Relative L2 error of the reconstruction of face solution x (level-0 numbering) against the
  * exact solution of the sine source; -2 for sources without a closed form. */
 int fhg_hho_l2_error(const fhg_hho* h, const double* x, double* rel_error);
+/* Post-processing tables of the finest level: sizes (n_face_dofs = faces per element x face DOFs,
+ * n_points = cell quadrature points of the L2 error), then the arrays, each optional (null: skipped):
+ * elem_class[ne], elem_faces[ne * (dim + 1)] (unknown block or -1), elem_centre[ne * 3],
+ * cell_rhs[ne * n_cell] (A_TT^-1 b_T), and per class solve_cells[n_cell * n_face_dofs] (-A_TT^-1 A_TF),
+ * recon[n_recon * (n_cell + n_face_dofs)], weights[n_points], offsets[n_points * 3] (from the centroid),
+ * basis[n_points * n_recon]. */
+int fhg_hho_post_sizes(const fhg_hho* h, int* n_elements, int* n_classes, int* n_cell, int* n_face_dofs,
+                       int* n_recon, int* n_points);
+int fhg_hho_post_tables(const fhg_hho* h, int* elem_class, int* elem_faces, double* elem_centre, double* cell_rhs,
+                        double* solve_cells, double* recon, double* weights, double* offsets, double* basis);
 /* Diffusion tensors of the two elements of every unknown face of level `level` (both exist: the
  * unknowns are the interior faces): out[12*u .. 12*u+11] for face block u, element 1 then
  * element 2 (the face's own element order), each as (xx, yy, zz, xy, xz, yz) in 3D and

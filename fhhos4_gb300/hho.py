@@ -49,6 +49,8 @@ def lib():
         L.fhg_hho_rhs.argtypes = [C.c_void_p, P(P(C.c_double))]
         L.fhg_hho_l2_error.argtypes = [C.c_void_p, C.c_void_p, P(C.c_double)]
         L.fhg_hho_face_tensors.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.fhg_hho_post_sizes.argtypes = [C.c_void_p] + [P(C.c_int)] * 6
+        L.fhg_hho_post_tables.argtypes = [C.c_void_p] + [C.c_void_p] * 9
         _lib = L
     return _lib
 
@@ -74,6 +76,7 @@ class Hierarchy:
         p.contrast, p.checker_blocks, p.threads = contrast, checker_blocks, threads
         p.eps_min, p.seed = eps_min, seed
         self.h = C.c_void_p()
+        self.dim = dim
         rc = L.fhg_hho_create(C.byref(self.h), C.byref(p))
         if rc != 0:
             msg = L.fhg_hho_last_error(self.h).decode()
@@ -124,6 +127,26 @@ class Hierarchy:
         if lib().fhg_hho_face_tensors(self.h, l, C.c_void_p(out.ctypes.data)) != 0:
             raise RuntimeError("face_tensors failed")
         return out
+
+    def post_tables(self) -> dict:
+        """The finest level's element tables for post-processing (cell-unknown recovery and the L2 error
+        of the reconstruction; fhg_post_create takes them): sizes and arrays."""
+        sz = [C.c_int() for _ in range(6)]
+        if lib().fhg_hho_post_sizes(self.h, *[C.byref(v) for v in sz]) != 0:
+            raise RuntimeError("post_sizes failed")
+        ne, ncls, nC, nFF, nR, nq = (v.value for v in sz)
+        dim = self.dim
+        nF = dim + 1
+        t = dict(dim=dim, n_elements=ne, n_classes=ncls, n_cell=nC, n_face_dofs=nFF, n_recon=nR, n_points=nq,
+                 elem_class=np.zeros(ne, np.int32), elem_faces=np.zeros(ne * nF, np.int32),
+                 elem_centre=np.zeros(ne * 3), cell_rhs=np.zeros(ne * nC), solve_cells=np.zeros(ncls * nC * nFF),
+                 recon=np.zeros(ncls * nR * (nC + nFF)), weights=np.zeros(ncls * nq), offsets=np.zeros(ncls * nq * 3),
+                 basis=np.zeros(ncls * nq * nR))
+        names = ["elem_class", "elem_faces", "elem_centre", "cell_rhs", "solve_cells", "recon", "weights", "offsets",
+                 "basis"]
+        if lib().fhg_hho_post_tables(self.h, *[C.c_void_p(t[k].ctypes.data) for k in names]) != 0:
+            raise RuntimeError("post_tables failed")
+        return t
 
     def A_rows(self, l: int) -> int:
         n = C.c_int()

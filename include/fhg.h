@@ -336,6 +336,32 @@ int fhg_batch_add(fhg_batch* batch, fhg_ctx* ctx);
  * the launch (CUDA events on the batch's stream). */
 int fhg_batch_solve(fhg_batch* batch, fhg_solve_info* infos, double* elapsed_ms);
 
+/* ---- Post-processing of a face solution ----------------------------------------------------------
+ * Cell-unknown recovery x_T = A_TT^{-1} b_T - A_TT^{-1} A_TF x_F per element
+ * (Diffusion_HHO::HybridCoeffsBySolvingCellUnknowns, src/Discretizations/HHO/Diffusion_HHO.h:855-882),
+ * the k+1 reconstruction of [x_T; x_F] (ReconstructHigherOrderApproximationFromHybridCoeffs, :896-912)
+ * and its relative L2 error against a closed-form solution (Diffusion_HHO::L2Error, :120-150), on the
+ * GPU. The element tables are those of the finest level: per element its class, the unknown block of
+ * each local face (-1: Dirichlet), its centroid (3 doubles) and A_TT^{-1} b_T (n_cell); per class
+ * -A_TT^{-1} A_TF (n_cell x n_face_dofs, row-major), the reconstruction (n_recon x (n_cell +
+ * n_face_dofs)), and at n_points cell quadrature points their weights, offsets from the centroid (3
+ * doubles each) and reconstruction basis values (n_points x n_recon). A caller whose elements are not
+ * grouped in classes passes one class per element. */
+#define FHG_EXACT_NONE 0   /* no error evaluation: cell unknowns only */
+#define FHG_EXACT_SINE 1   /* u = prod_d sin(pi x_d), the solution of the "sine" test case source */
+typedef struct fhg_post fhg_post;
+int fhg_post_create(fhg_post** post, int device, int dim, int n_elements, int n_classes, int n_cell,
+                    int n_face_dofs, int n_recon, int n_points, const int* elem_class, const int* elem_faces,
+                    const double* elem_centre, const double* cell_rhs, const double* solve_cells,
+                    const double* recon, const double* weights, const double* offsets, const double* basis);
+/* x_faces: device face solution in the given numbering (fhg_solve's x); x_cells: device output
+ * (n_elements x n_cell) or null; rel_l2_error: host output with FHG_EXACT_SINE; elapsed_ms: device
+ * time (CUDA events) or null. */
+int fhg_post_run(fhg_post* post, const double* x_faces, double* x_cells, int exact, double* rel_l2_error,
+                 double* elapsed_ms);
+const char* fhg_post_last_error(const fhg_post* post);
+void fhg_post_destroy(fhg_post* post);
+
 #ifdef __cplusplus
 }
 #endif
