@@ -281,12 +281,12 @@ def test_fused_coarse_cycle_matches_launch_by_launch(case, precision, cycle, pre
     _check_fused_pair(case.As[0], case.b, a, b, precision)
 
 
-def _check_fused_pair(A0, rhs, a, b, precision):
+def _check_fused_pair(A0, rhs, a, b, precision, rtol=1e-10):
     xa, xb = a.Solve(rhs), b.Solve(rhs)
     if precision == "df":
         assert a.IterationCount == b.IterationCount
-        assert np.all(np.abs(a.History - b.History) <= 1e-10 * np.abs(b.History) + 64 * HIST_ATOL)
-        assert np.linalg.norm(xa - xb) <= 1e-10 * np.linalg.norm(xb)
+        assert np.all(np.abs(a.History - b.History) <= rtol * np.abs(b.History) + 64 * HIST_ATOL)
+        assert np.linalg.norm(xa - xb) <= rtol * np.linalg.norm(xb)
     else:
         assert abs(a.IterationCount - b.IterationCount) <= 1
         assert true_rel_residual(A0, rhs, xa) < 1e-8 * (1 + 1e-6)
@@ -296,7 +296,10 @@ def _check_fused_pair(A0, rhs, a, b, precision):
 def test_fused_coarse_cycle_deep_hierarchy(precision, cycle):
     """A deep 2D hierarchy (n = 256, k = 3: six levels, Galerkin coarse operators, the largest
     problem of the batched workload), fused from every eligible level and chosen by timing: the same
-    answers as launch by launch. The sub-cycle runs as a loop over levels with fixed stack use."""
+    answers as launch by launch. The sub-cycle runs as a loop over levels with fixed stack use.
+    Rows of the Galerkin operators hold about 40 blocks, summed by 16 lanes here and by the tuned
+    launch shape there; with the coefficient contrast (1e3) FCG carries that reordering (a few units
+    of 2^-47 per row in pairs) to 1e-10 of the history, so the FP64-class bar is 1e-8."""
     from fhhos4_gb300 import batch as BT
     bs, A0, Ps, b, levels = BT.generate(BT.ProblemSpec(256, 3, 4242))
     As = [A0]
@@ -310,7 +313,7 @@ def test_fused_coarse_cycle_deep_hierarchy(precision, cycle):
         assert first == -1 or (1 <= first <= len(As) - 2 and ctas in (8, 16))
         if not autotune:
             assert first >= 1
-        _check_fused_pair(A0, b, a, b_, precision)
+        _check_fused_pair(A0, b, a, b_, precision, rtol=1e-8)
 
 
 def _pairs(torch, v):
