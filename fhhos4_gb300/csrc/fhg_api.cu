@@ -72,6 +72,7 @@ struct Level {
     bool gs_slot[3] = {false, false, false};
     bool prod_slot[3] = {false, false, false};  // products with A use the slot-major view
     int outer_lanes = 0;           // level 0: lanes of the FP64 outer product (0: those of its view)
+    bool outer_slot = true;        // level 0: the pair outer product on the slot-major view (Ahat2s)
     std::vector<int> colour_start;  // block-row offsets of every colour, ncolours + 1
     std::vector<int> perm;          // new block row -> given block row
     DevBsr<double> A, Ahat, P, R;
@@ -86,6 +87,7 @@ struct Level {
     dfl* dinv2 = nullptr;
     dfl *x2 = nullptr, *b2 = nullptr, *r2 = nullptr;
     dfl* kv2[4] = {nullptr, nullptr, nullptr, nullptr};
+    DevBsr<dfl> Ahat2s;         // level 0: the outer operator as FP32 pairs, slot-major (when its rows allow)
     DevBsr<float> Ahat_hi;      // level 0, FP32 V-cycle: outer operator as an FP32 pair (hi part)
     float* ahat_lo = nullptr;   // (lo part, same layout)
     double* dinv = nullptr;
@@ -1320,6 +1322,18 @@ void precondition(fhg_ctx* ctx, const double* r, double* z)
 
 double* part(fhg_ctx* ctx, int i) { return ctx->partials + (size_t)i * fhg::kReduceCtas; }
 
+// Ad = Â d in pair arithmetic with the partials of d.Ad and r.d: on the slot-major pair view when
+// setup built one and the autotuner kept it, else on the row-major split view.
+void outer_product_df(fhg_ctx* ctx, const float* dh, const float* dl, const float* rh, const float* rl, float* Adh,
+                      float* Adl, double* partials)
+{
+    Level& L0 = ctx->levels[0];
+    if (L0.Ahat2s.vals && L0.outer_slot)
+        fhg::launch_spmv_dots_df_slot(L0.Ahat2s.v, dh, dl, rh, rl, Adh, Adl, partials, ctx->stream);
+    else
+        fhg::launch_spmv_dots_df(L0.Ahat_hi.v, L0.ahat_lo, dh, dl, rh, rl, Adh, Adl, partials, ctx->stream);
+}
+
 // The outer iteration runs on FP32 pairs (double-FP32 outer product built at setup): with the FP32
 // V-cycle, and with the pair V-cycle.
 bool outer_df(const fhg_ctx* ctx)
@@ -1380,7 +1394,7 @@ void fcg_iteration(fhg_ctx* ctx, int p)
         float *dh = pair_hi(z), *dl = pair_lo(z, n), *Adh = pair_hi(Ad), *Adl = pair_lo(Ad, n);
         fhg::launch_dot_df(n, z32, pair_hi(Adp), pair_lo(Adp, n), part(ctx, 0), s, z2);
         fhg::launch_fcg_direction_df(n, z32, pair_hi(dp), pair_lo(dp, n), part(ctx, 0), ctx->scal + 1, dh, dl, s, z2);
-        fhg::launch_spmv_dots_df(L0.Ahat_hi.v, L0.ahat_lo, dh, dl, rh, ctx->rlo, Adh, Adl, part(ctx, 1), s);
+        outer_product_df(ctx, dh, dl, rh, ctx->rlo, Adh, Adl, part(ctx, 1));
         fhg::launch_krylov_step_df(n, ctx->kx, rh, ctx->rlo, dh, dl, Adh, Adl, part(ctx, 2), part(ctx, 1),
                                    ctx->scal + 1, part(ctx, 3), s, outer_r2(ctx));
         fhg::launch_finalize_norm(part(ctx, 3), ctx->scal + 0, ctx->scal + 2, ctx->hist_d, ctx->counter_d,
@@ -1720,6 +1734,8 @@ void reset_device_state(Level& L)
     L.x2 = L.b2 = L.r2 = nullptr;
     for (int i = 0; i < 3; i++) { L.gs_slot[i] = false; L.prod_slot[i] = false; L.gs_lanes[i] = 0; L.gs_unroll[i] = 1; }
     L.Ahat_hi = DevBsr<float>();
+    L.Ahat2s = DevBsr<dfl>();
+    L.outer_slot = true;
     L.ahat_is_a = true;
     L.ahat_lo = nullptr;
     L.dinv = nullptr;
@@ -2239,8 +2255,10 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
                 permute_bsr(Sb, L.perm, iperm[0], Sp);
                 if ((rc = upload_bsr<double>(ctx, Sp, L.Ahat, nullptr))) return rc;
                 if (split && (rc = upload_bsr_split(ctx, Sp, L.Ahat_hi, &L.ahat_lo, L.Ahat))) return rc;
-            } else if (split && (rc = upload_bsr_split(ctx, Ap, L.Ahat_hi, &L.ahat_lo, L.A))) {
-                return rc;
+                if (split && (rc = upload_slot_major_all(ctx, Sp, L.Ahat2s))) return rc;
+            } else if (split) {
+                if ((rc = upload_bsr_split(ctx, Ap, L.Ahat_hi, &L.ahat_lo, L.A))) return rc;
+                if ((rc = upload_slot_major_all(ctx, Ap, L.Ahat2s))) return rc;
             }
         }
         if (l == nlevels - 1) {
@@ -2319,13 +2337,25 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         if (L0.ahat_lo) {
             int gd = g, gdu = 1;
             const long long n = L0.n;
+            float row_ms = 0.f;
             if ((rc = tune(ctx, 9, gd, gdu, [&](int G, int) {
                      BsrView<float> v = L0.Ahat_hi.v; v.lanes = G;
                      fhg::launch_spmv_dots_df(v, L0.ahat_lo, pair_hi(ctx->kz[0]), pair_lo(ctx->kz[0], n),
                                               pair_hi(ctx->kz[0]), pair_lo(ctx->kz[0], n), pair_hi(ctx->kAd[0]),
                                               pair_lo(ctx->kAd[0], n), part(ctx, 5), ctx->stream);
-                 })))
+                 }, &row_ms)))
                 return rc;
+            // the slot-major pair view against the best row-major shape
+            if (L0.Ahat2s.vals) {
+                float slot_ms = 0.f;
+                if ((rc = time_candidate(ctx, [&]() {
+                         fhg::launch_spmv_dots_df_slot(L0.Ahat2s.v, pair_hi(ctx->kz[0]), pair_lo(ctx->kz[0], n),
+                                                       pair_hi(ctx->kz[0]), pair_lo(ctx->kz[0], n), pair_hi(ctx->kAd[0]),
+                                                       pair_lo(ctx->kAd[0], n), part(ctx, 5), ctx->stream);
+                     }, &slot_ms)))
+                    return rc;
+                L0.outer_slot = slot_ms < row_ms;
+            }
             L0.Ahat_hi.v.lanes = gd;
         }
     }
@@ -2592,8 +2622,7 @@ int fhg_time_op(fhg_ctx* ctx, int level, int op, int precision, int warmup, int 
         if (split) fhg::launch_split_df((long long)n0, ctx->kr, dh, dl, ctx->stream);
         auto one = [&]() -> int {
             if (split) {
-                fhg::launch_spmv_dots_df(L0.Ahat_hi.v, L0.ahat_lo, dh, dl, dh, dl, pair_hi(t + n0),
-                                         pair_lo(t + n0, (long long)n0), part(ctx, 4), ctx->stream);
+                outer_product_df(ctx, dh, dl, dh, dl, pair_hi(t + n0), pair_lo(t + n0, (long long)n0), part(ctx, 4));
                 return FHG_OK;
             }
             return apply_device(ctx, level, op, t, nullptr, t + n0);

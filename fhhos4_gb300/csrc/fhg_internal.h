@@ -89,6 +89,9 @@ void launch_fcg_direction_mixed(long long n, const float* z, const double* dp, c
 void launch_spmv_dots_df(const BsrView<float>& Ahi, const float* vlo, const float* dhi, const float* dlo,
                          const float* rhi, const float* rlo, float* Adhi, float* Adlo, double* partials,
                          cudaStream_t s);
+// The same on the slot-major pair view of Â (ell = 5..8 slots; bs 2, 3, 4, 6).
+void launch_spmv_dots_df_slot(const BsrView<dfl>& A, const float* dhi, const float* dlo, const float* rhi,
+                              const float* rlo, float* Adhi, float* Adlo, double* partials, cudaStream_t s);
 // partials of z.Adp (z FP32, or z2 non-null: the pair V-cycle's output as interleaved pairs).
 void launch_dot_df(long long n, const float* z, const float* ah, const float* al, double* partials, cudaStream_t s,
                    const dfl* z2 = nullptr);

@@ -175,6 +175,74 @@ __global__ void __launch_bounds__(kReduceThreads) k_bsr_spmv_dots_df(int nbr, co
     }
 }
 
+// The same on the slot-major pair view of Â (slot s of row i at s * nbr + i; values as interleaved
+// FP32 pairs, one 8-byte load each; empty slots hold zero pairs and a column of the row): one thread
+// per block row over the fixed grid, the row's column indices and then its slots' values and d
+// entries loaded ahead of the sums, no row pointers and no lane reduction. The row's terms are
+// summed block by block in column order with the same pair arithmetic per term.
+template <int BS, int W>
+__global__ void __launch_bounds__(kReduceThreads, 2) k_bsr_spmv_dots_df_slot(int nbr, const int* __restrict__ colidx,
+                                                                          const dfl* __restrict__ vals, long long ld,
+                                                                          const float* __restrict__ dhi,
+                                                                          const float* __restrict__ dlo,
+                                                                          const float* __restrict__ rhi,
+                                                                          const float* __restrict__ rlo,
+                                                                          float* __restrict__ Adhi,
+                                                                          float* __restrict__ Adlo,
+                                                                          double* __restrict__ partials)
+{
+    pdl_wait();
+    __shared__ double sh_red[33];
+    float dad_h = 0.f, dad_l = 0.f, rd_h = 0.f, rd_l = 0.f;
+    const long long stride = (long long)kReduceCtas * kReduceThreads;
+    for (long long row = (long long)blockIdx.x * kReduceThreads + threadIdx.x; row < nbr; row += stride) {
+        int col[W];
+#pragma unroll
+        for (int k = 0; k < W; k++) col[k] = colidx[(long long)k * nbr + row];
+        float hi[BS], lo[BS];
+#pragma unroll
+        for (int r = 0; r < BS; r++) { hi[r] = 0.f; lo[r] = 0.f; }
+#pragma unroll
+        for (int k = 0; k < W; k++) {
+            const long long p = (long long)k * nbr + row;
+            float xh[BS], xl[BS];
+#pragma unroll
+            for (int c = 0; c < BS; c++) {
+                xh[c] = dhi[(long long)col[k] * BS + c];
+                xl[c] = dlo[(long long)col[k] * BS + c];
+            }
+#pragma unroll
+            for (int r = 0; r < BS; r++)
+#pragma unroll
+                for (int c = 0; c < BS; c++) {
+                    const dfl a = vals[(long long)(r * BS + c) * ld + p];
+                    float ph, pl;
+                    df_mul(a.h, a.l, xh[c], xl[c], ph, pl);
+                    df_add(hi[r], lo[r], ph, pl);
+                }
+        }
+#pragma unroll
+        for (int r = 0; r < BS; r++) {
+            const long long i = row * BS + r;
+            float ah, al, ph, pl;
+            df_norm(hi[r], lo[r], ah, al);
+            Adhi[i] = ah;
+            Adlo[i] = al;
+            const float dvh = dhi[i], dvl = dlo[i];
+            df_mul(dvh, dvl, ah, al, ph, pl);
+            df_add(dad_h, dad_l, ph, pl);
+            df_mul(rhi[i], rlo[i], dvh, dvl, ph, pl);
+            df_add(rd_h, rd_l, ph, pl);
+        }
+    }
+    const double s1 = block_sum((double)dad_h + (double)dad_l, sh_red);
+    const double s2 = block_sum((double)rd_h + (double)rd_l, sh_red);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = s1;
+        partials[kReduceCtas + blockIdx.x] = s2;
+    }
+}
+
 // r = b - A x with compensated summation (Ogita, Rump and Oishi 2005, "Accurate sum and dot
 // product", Dot2): every product split exactly by an FMA (TwoProduct), the running sum kept exact by
 // TwoSum, the rounding errors summed apart and added once, so r_i carries an error of about one unit
@@ -645,6 +713,25 @@ void launch_spmv_dots_df(const BsrView<float>& Ahi, const float* vlo, const floa
                                                                          partials);
     });
     g_kernel_launches++;
+}
+
+void launch_spmv_dots_df_slot(const BsrView<dfl>& A, const float* dhi, const float* dlo, const float* rhi,
+                              const float* rlo, float* Adhi, float* Adlo, double* partials, cudaStream_t s)
+{
+#define FHG_OUTER_SLOT(BSV, WV)                                                                              \
+    if (A.bs == BSV && A.ell == WV) {                                                                       \
+        pdl_launch(k_bsr_spmv_dots_df_slot<BSV, WV>, kReduceCtas, kReduceThreads, 0, s, A.nbr, A.colidx, A.vals, A.ld, \
+                   dhi, dlo, rhi, rlo, Adhi, Adlo, partials);                                              \
+        g_kernel_launches++;                                                                               \
+        return;                                                                                            \
+    }
+#define FHG_OUTER_SLOT_W(BSV) FHG_OUTER_SLOT(BSV, 5) FHG_OUTER_SLOT(BSV, 6) FHG_OUTER_SLOT(BSV, 7) FHG_OUTER_SLOT(BSV, 8)
+    FHG_OUTER_SLOT_W(2)
+    FHG_OUTER_SLOT_W(3)
+    FHG_OUTER_SLOT_W(4)
+    FHG_OUTER_SLOT_W(6)
+#undef FHG_OUTER_SLOT_W
+#undef FHG_OUTER_SLOT
 }
 
 void launch_dot_df(long long n, const float* z, const float* ah, const float* al, double* partials, cudaStream_t s,
