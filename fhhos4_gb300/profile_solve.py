@@ -4,8 +4,9 @@
 
 Setup (hierarchy generation, upload, autotuning) and warm-up solves run outside the range
 "solve"; `ncu --nvtx --nvtx-include "solve/" ...` then captures the launches of the timed solves
-only. `--step` instead applies one operator (the learned step, a forward GS sweep, the
-double-FP32 outer product) inside the range.
+only. `--step` instead applies one level-0 operator inside the range (the learned step, a forward
+GS sweep, the double-FP32 outer product, the SpMV in pair or native FP64 arithmetic, the FP32
+restriction or prolongation).
 """
 from __future__ import annotations
 
@@ -27,7 +28,8 @@ def main():
     ap.add_argument("--levels", type=int, default=0, help="use the first N levels (the last one solved directly)")
     ap.add_argument("--weights", default="", help="learned-step network (default: the committed one)")
     ap.add_argument("--gs-layout", default="auto", choices=["auto", "row", "slot"], help="FP32 GS sweep layout")
-    ap.add_argument("--step", choices=["", "learned_tcgen05", "learned_mma_sync", "gs_fp32", "outer_df"], default="")
+    ap.add_argument("--step", choices=["", "learned_tcgen05", "learned_mma_sync", "gs_fp32", "outer_df", "spmv_df",
+                                       "spmv_fp64", "restrict_fp32", "prolong_fp32"], default="")
     a = ap.parse_args()
 
     import torch
@@ -49,6 +51,7 @@ def main():
     nlev = a.levels if a.levels > 0 else len(As)
     o = N.default_options()
     o.vcycle_precision = N.PRECISION["fp32"]
+    o.extra_precisions = 1 << N.PRECISION["df"]   # the FP64-class pair copies as well
     o.autotune = a.autotune
     o.gs_layout = N.GS_LAYOUT[a.gs_layout]
     ctx.setup(nlev, o)
@@ -69,7 +72,9 @@ def main():
     out = {}
     if a.step:
         op, prec = {"learned_tcgen05": (N.OP_LEARNED_STEP, "fp32"), "learned_mma_sync": (N.OP_LEARNED_STEP, "fp32"),
-                    "gs_fp32": (N.OP_GS_FORWARD, "fp32"), "outer_df": (N.OP_SYM_SPMV, "fp32")}[a.step]
+                    "gs_fp32": (N.OP_GS_FORWARD, "fp32"), "outer_df": (N.OP_SYM_SPMV, "fp32"),
+                    "spmv_df": (N.OP_SPMV, "df"), "spmv_fp64": (N.OP_SPMV, "fp64"),
+                    "restrict_fp32": (N.OP_RESTRICT, "fp32"), "prolong_fp32": (N.OP_PROLONG_ADD, "fp32")}[a.step]
         if a.step.startswith("learned"):
             ctx.set_learned(params, "always", kernel=a.step.split("_", 1)[1])
         ctx.time_op(0, op, prec, warmup=a.warmup, reps=1)
