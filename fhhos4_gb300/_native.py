@@ -46,7 +46,8 @@ EXPORTS = ["fhg_default_options", "fhg_create", "fhg_destroy", "fhg_last_error",
            "fhg_net_create", "fhg_net_destroy", "fhg_net_last_error", "fhg_net_set_params", "fhg_net_get_params",
            "fhg_net_train_step", "fhg_io_buffers", "fhg_io_upload", "fhg_io_download", "fhg_batch_create", "fhg_batch_destroy", "fhg_batch_last_error",
            "fhg_batch_add", "fhg_batch_solve", "fhg_post_create", "fhg_post_run", "fhg_post_last_error",
-           "fhg_post_destroy"]
+           "fhg_post_destroy", "fhg_cond_create", "fhg_cond_run", "fhg_cond_result", "fhg_cond_download", "fhg_cond_last_error",
+           "fhg_cond_destroy"]
 
 FHG_NOALLOC_MAX_PARTIALS = 131072
 
@@ -141,6 +142,14 @@ def load(path: str = LIB):
     lib.fhg_post_last_error.restype = C.c_char_p
     lib.fhg_post_destroy.argtypes = [C.c_void_p]
     lib.fhg_post_destroy.restype = None
+    lib.fhg_cond_create.argtypes = [P(C.c_void_p)] + [C.c_int] * 7 + [C.c_void_p] * 5
+    lib.fhg_cond_run.argtypes = [C.c_void_p, P(C.c_longlong), P(C.c_double)]
+    lib.fhg_cond_result.argtypes = [C.c_void_p, P(C.c_void_p), P(C.c_void_p), P(C.c_void_p), P(C.c_void_p)]
+    lib.fhg_cond_download.argtypes = [C.c_void_p] + [C.c_void_p] * 4
+    lib.fhg_cond_last_error.argtypes = [C.c_void_p]
+    lib.fhg_cond_last_error.restype = C.c_char_p
+    lib.fhg_cond_destroy.argtypes = [C.c_void_p]
+    lib.fhg_cond_destroy.restype = None
     _lib = lib
     return lib
 
@@ -368,6 +377,54 @@ class Post:
     def close(self):
         if self.h:
             self.lib.fhg_post_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Condense:
+    """Owns one fhg_cond: static condensation and assembly of the finest face system on a GPU
+    (tables as fhhos4_gb300.hho.Hierarchy.condense_tables gives)."""
+
+    def __init__(self, tables: dict, device: int = 0):
+        self.lib = load()
+        self.h = C.c_void_p()
+        t = {k: np.ascontiguousarray(v) for k, v in tables.items() if isinstance(v, np.ndarray)}
+        self._keep = t
+        self.nf = int(tables["n_face_dofs"]) // (int(tables["dim"]) + 1)
+        self.n_face_blocks = int(tables["n_face_blocks"])
+        self._check(self.lib.fhg_cond_create(
+            C.byref(self.h), device, int(tables["dim"]), int(tables["n_elements"]), int(tables["n_classes"]),
+            int(tables["n_cell"]), int(tables["n_face_dofs"]), self.n_face_blocks, ptr(t["elem_class"]),
+            ptr(t["elem_faces"]), ptr(t["face_elems"]), ptr(t["local"]), ptr(t["b_cell"])))
+
+    def _check(self, rc: int):
+        if rc != FHG_OK:
+            msg = self.lib.fhg_cond_last_error(self.h).decode() if self.h else "no condensation handle"
+            raise FhgError(rc, msg)
+
+    def run(self):
+        """Condense and assemble on the device: (stored entries, device ms)."""
+        nnz, ms = C.c_longlong(), C.c_double()
+        self._check(self.lib.fhg_cond_run(self.h, C.byref(nnz), C.byref(ms)))
+        return nnz.value, ms.value
+
+    def result(self, nnz: int):
+        """The assembled system copied to the host: (scipy CSR A, b)."""
+        import scipy.sparse as sp
+        n = self.n_face_blocks * self.nf
+        rowptr, colidx = np.empty(n + 1, np.int32), np.empty(nnz, np.int32)
+        vals, b = np.empty(nnz), np.empty(n)
+        self._check(self.lib.fhg_cond_download(self.h, ptr(rowptr), ptr(colidx), ptr(vals), ptr(b)))
+        return sp.csr_matrix((vals, colidx, rowptr), shape=(n, n)), b
+
+    def close(self):
+        if self.h:
+            self.lib.fhg_cond_destroy(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):

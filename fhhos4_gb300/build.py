@@ -17,7 +17,7 @@ CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libfhg.so")
 HHO_LIB = os.path.join(OUT_DIR, "libfhg_hho.so")
-SOURCES = ["fhg_kernels.cu", "fhg_kernels_pair.cu", "fhg_coarse.cu", "fhg_api.cu", "fhg_noalloc.cu", "fhg_learned.cu", "fhg_post.cu"]
+SOURCES = ["fhg_kernels.cu", "fhg_kernels_pair.cu", "fhg_coarse.cu", "fhg_api.cu", "fhg_noalloc.cu", "fhg_learned.cu", "fhg_post.cu", "fhg_condense.cu"]
 HHO_SOURCES = ["hho_gen.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

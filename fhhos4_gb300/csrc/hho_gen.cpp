@@ -658,6 +658,7 @@ struct ElementOps {
     std::vector<double> cell_rhs;  // nC: A_TT^{-1} b_T (cell unknowns = cell_rhs + solve_cells x_F)
     Mat att_inv;  // nC x nC: A_TT^{-1}, for the source terms of the elements of this one's class
     Mat atf;      // nC x nF nf: A_TF
+    Mat local;    // (nC + nF nf)^2: the local operator before condensation (cells first, then faces)
     bool ok = true;
 };
 
@@ -881,6 +882,7 @@ ElementOps element_ops(const Mesh& M, int e, const Params& prm, const Rules& rul
     }
     O.A = Mat(nH, nH);
     for (size_t i = 0; i < O.A.a.size(); i++) O.A.a[i] = Acons.a[i] + Astab.a[i];
+    O.local = O.A;
     // Static condensation.
     const int nFF = nF * nf;
     Mat Att(nC, nC), Atf(nC, nFF);
@@ -971,6 +973,7 @@ struct Level {
     std::vector<int> cls;                 // element -> class
     std::vector<double> bF_e;             // per element, nF nf: condensed RHS contribution (finest level)
     std::vector<double> cell_rhs_e;       // per element, nC: A_TT^{-1} b_T (finest level)
+    std::vector<double> bT_e;             // per element, nC: b_T = (f, c_j)_T (finest level)
     int n_rows = 0;
     std::vector<int> A_rowptr, A_colidx;
     std::vector<double> A_vals;
@@ -1006,7 +1009,7 @@ std::vector<long long> element_key(const Mesh& M, int e, double h)
 // The source terms of element e with its class's local operators O: b_T = (f, c_j)_T on the element's
 // own quadrature points and centred basis, cell_rhs = A_TT^{-1} b_T, bF = -A_FT A_TT^{-1} b_T.
 void element_rhs(const Mesh& M, int e, const Params& prm, const Rules& rules, const ElementOps& O, double* bF,
-                 double* cell_rhs)
+                 double* cell_rhs, double* bT_out)
 {
     const int nC = O.nC, nFF = O.nF * O.nf;
     const auto xc = centroid(M, e);
@@ -1018,6 +1021,7 @@ void element_rhs(const Mesh& M, int e, const Params& prm, const Rules& rules, co
         const double fv = source_value(prm, QR.x[q]);
         for (int j = 0; j < nC; j++) bT[j] += QR.w[q] * fv * v[j];
     }
+    for (int j = 0; j < nC; j++) bT_out[j] = bT[j];
     for (int c = 0; c < nC; c++) {
         double s = 0;
         for (int j = 0; j < nC; j++) s += O.att_inv(c, j) * bT[j];
@@ -1066,9 +1070,11 @@ int element_classes(Level& L, const Params& prm, const Rules& rules, int threads
         const int nC = L.cls_ops[0].nC, nFF = L.cls_ops[0].nF * L.cls_ops[0].nf;
         L.bF_e.assign(ne * nFF, 0.0);
         L.cell_rhs_e.assign(ne * nC, 0.0);
+        L.bT_e.assign(ne * nC, 0.0);
         parallel_for(ne, threads, [&](size_t s, size_t e) {
             for (size_t i = s; i < e; i++)
-                element_rhs(M, (int)i, prm, rules, L.cls_ops[L.cls[i]], &L.bF_e[i * nFF], &L.cell_rhs_e[i * nC]);
+                element_rhs(M, (int)i, prm, rules, L.cls_ops[L.cls[i]], &L.bF_e[i * nFF], &L.cell_rhs_e[i * nC],
+                            &L.bT_e[i * nC]);
         });
     }
     return 0;
@@ -1581,6 +1587,42 @@ int fhg_hho_post_tables(const fhg_hho* h, int* elem_class, int* elem_faces, doub
             }
         }
     }
+    return 0;
+}
+
+// The finest level's inputs of static condensation (Diffusion_HHO.h:627-638): per class the local
+// operator before condensation, (nC + nFF)^2 row-major with the cell unknowns first; per element
+// b_T = (f, c_j)_T; and for every unknown face block I its two elements with the face's local index
+// in each, (e1, lf1, e2, lf2), in the order the assembly adds them.
+int fhg_hho_condense_tables(const fhg_hho* h, double* local, double* b_cell, int* face_elems)
+{
+    if (!h || h->levels.empty()) return -1;
+    const Level& L = h->levels[0];
+    const Mesh& M = L.mesh;
+    const int nF = M.dim + 1;
+    const int nH = L.cls_ops[0].nC + nF * L.cls_ops[0].nf;
+    if (local)
+        for (size_t c = 0; c < L.cls_ops.size(); c++) {
+            const Mat& A = L.cls_ops[c].local;
+            if (A.a.size() != (size_t)nH * nH) return -3;
+            for (int i = 0; i < nH; i++)
+                for (int j = 0; j < nH; j++) local[(c * nH + i) * nH + j] = A(i, j);
+        }
+    if (b_cell) std::copy(L.bT_e.begin(), L.bT_e.end(), b_cell);
+    if (face_elems)
+        for (size_t f = 0; f < M.fv.size(); f++) {
+            const int I = M.number[f];
+            if (I < 0) continue;
+            const int els[2] = {M.fe1[f], M.fe2[f]};
+            for (int side = 0; side < 2; side++) {
+                int lfi = -1;
+                if (els[side] >= 0)
+                    for (int lf = 0; lf < nF; lf++)
+                        if (M.ef[els[side]][lf] == (int)f) lfi = lf;
+                face_elems[(size_t)I * 4 + 2 * side] = els[side];
+                face_elems[(size_t)I * 4 + 2 * side + 1] = lfi;
+            }
+        }
     return 0;
 }
 

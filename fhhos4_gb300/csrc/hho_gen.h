@@ -59,6 +59,10 @@ int fhg_hho_post_sizes(const fhg_hho* h, int* n_elements, int* n_classes, int* n
                        int* n_recon, int* n_points);
 int fhg_hho_post_tables(const fhg_hho* h, int* elem_class, int* elem_faces, double* elem_centre, double* cell_rhs,
                         double* solve_cells, double* recon, double* weights, double* offsets, double* basis);
+/* Inputs of static condensation on the finest level: local[n_classes * nH * nH] (nH = n_cell +
+ * n_face_dofs; the local operator before condensation, cells first), b_cell[ne * n_cell] (b_T),
+ * face_elems[n_face_blocks * 4] = (e1, lf1, e2, lf2) per unknown face block, in assembly order. */
+int fhg_hho_condense_tables(const fhg_hho* h, double* local, double* b_cell, int* face_elems);
 /* Diffusion tensors of the two elements of every unknown face of level `level` (both exist: the
  * unknowns are the interior faces): out[12*u .. 12*u+11] for face block u, element 1 then
  * element 2 (the face's own element order), each as (xx, yy, zz, xy, xz, yz) in 3D and

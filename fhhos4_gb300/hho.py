@@ -51,6 +51,7 @@ def lib():
         L.fhg_hho_face_tensors.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         L.fhg_hho_post_sizes.argtypes = [C.c_void_p] + [P(C.c_int)] * 6
         L.fhg_hho_post_tables.argtypes = [C.c_void_p] + [C.c_void_p] * 9
+        L.fhg_hho_condense_tables.argtypes = [C.c_void_p] + [C.c_void_p] * 3
         _lib = L
     return _lib
 
@@ -146,6 +147,20 @@ class Hierarchy:
                  "basis"]
         if lib().fhg_hho_post_tables(self.h, *[C.c_void_p(t[k].ctypes.data) for k in names]) != 0:
             raise RuntimeError("post_tables failed")
+        return t
+
+    def condense_tables(self) -> dict:
+        """The finest level's inputs of static condensation (fhg_cond_create takes them): the post
+        tables' element classes and faces, per class the local operator before condensation, per
+        element b_T, per unknown face block its two elements and local face indices."""
+        t = self.post_tables()
+        nH = t["n_cell"] + t["n_face_dofs"]
+        nI = self.A_rows(0) // self.block_size
+        t.update(n_face_blocks=nI, local=np.zeros(t["n_classes"] * nH * nH),
+                 b_cell=np.zeros(t["n_elements"] * t["n_cell"]), face_elems=np.zeros(nI * 4, np.int32))
+        if lib().fhg_hho_condense_tables(self.h, C.c_void_p(t["local"].ctypes.data), C.c_void_p(t["b_cell"].ctypes.data),
+                                         C.c_void_p(t["face_elems"].ctypes.data)) != 0:
+            raise RuntimeError("condense_tables failed")
         return t
 
     def A_rows(self, l: int) -> int:

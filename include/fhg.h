@@ -362,6 +362,29 @@ int fhg_post_run(fhg_post* post, const double* x_faces, double* x_cells, int exa
 const char* fhg_post_last_error(const fhg_post* post);
 void fhg_post_destroy(fhg_post* post);
 
+/* ---- Static condensation and assembly of the finest face system -----------------------------------
+ * A = A_FF - A_TF^T A_TT^{-1} A_TF and b = -A_TF^T A_TT^{-1} b_T assembled over the interior faces
+ * (Diffusion_HHO::Assemble with static condensation, src/Discretizations/HHO/Diffusion_HHO.h:627-638),
+ * on the GPU in FP64. Inputs: per class the local operator before condensation ((n_cell +
+ * n_face_dofs)^2, row-major, cell unknowns first; one class per element when the elements are not
+ * grouped), per element its class, its faces' unknown blocks (-1: Dirichlet) and b_T (n_cell), per
+ * unknown face block its two elements with the face's local index in each, (e1, lf1, e2, lf2), in the
+ * order their contributions are added. fhg_cond_run condenses and assembles on the device and
+ * returns the number of stored entries; fhg_cond_result gives device pointers to the scalar CSR
+ * (rows face block * face DOFs + a: rowptr, colidx, vals) and b, valid until the next run or destroy,
+ * in the layout fhg_set_level takes. Every row is written by one thread in a fixed order (the result
+ * is bitwise reproducible). No counterpart in the reference's API: it replaces the host assembly. */
+typedef struct fhg_cond fhg_cond;
+int fhg_cond_create(fhg_cond** cond, int device, int dim, int n_elements, int n_classes, int n_cell,
+                    int n_face_dofs, int n_face_blocks, const int* elem_class, const int* elem_faces,
+                    const int* face_elems, const double* local, const double* b_cell);
+int fhg_cond_run(fhg_cond* cond, long long* n_entries, double* elapsed_ms);
+int fhg_cond_result(fhg_cond* cond, int** rowptr, int** colidx, double** vals, double** b);
+/* The same copied to host arrays (rows + 1, n_entries, n_entries, rows); null ones are skipped. */
+int fhg_cond_download(fhg_cond* cond, int* rowptr, int* colidx, double* vals, double* b);
+const char* fhg_cond_last_error(const fhg_cond* cond);
+void fhg_cond_destroy(fhg_cond* cond);
+
 #ifdef __cplusplus
 }
 #endif
