@@ -345,6 +345,26 @@ def gpu_post_processing(H, x, dev):
             "quadrature_points": int(t["n_points"])}
 
 
+def gpu_condensation(H, A0, b0, dev):
+    """The finest system condensed and assembled on the GPU (fhg_cond_run) from the element tables,
+    compared with the host assembly the solve uses."""
+    from fhhos4_gb300 import _native as N
+    t = H.condense_tables()
+    cond = N.Condense(t, dev)
+    try:
+        cond.run()
+        nnz, ms = cond.run()
+        A, b = cond.result(nnz)
+    finally:
+        cond.close()
+    same = bool(np.array_equal(A.indptr, A0.indptr) and np.array_equal(A.indices, A0.indices))
+    return {"what": "static condensation (per-class Schur complements) + assembly of A_0 and b on the GPU",
+            "gpu_ms": round(ms, 3), "same_structure": same,
+            "max_rel_diff_A": float(np.abs(A.data - A0.data).max() / np.abs(A0.data).max()) if same else None,
+            "max_rel_diff_b": float(np.abs(b - b0).max() / np.abs(b0).max()),
+            "element_classes": int(t["n_classes"]), "elements": int(t["n_elements"])}
+
+
 def run_ours(args, dist: Dist):
     import torch
     from fhhos4_gb300 import _native as N
@@ -406,9 +426,11 @@ def run_ours(args, dist: Dist):
         results[name]["rel_diff_vs_plain_fp64"] = float(np.linalg.norm(solutions[name] - x64) / np.linalg.norm(x64))
         if args.source == "sine" and H is not None:
             results[name]["l2_error_vs_exact"] = H.l2_error(solutions[name])
-    post_info = None
+    post_info = cond_info = None
     if args.source == "sine" and H is not None:
         post_info = gpu_post_processing(H, solutions["learned" if have_learned else "fast"], dev)
+    if H is not None:
+        cond_info = gpu_condensation(H, As[0], b, dev)
     if H is not None:
         H.close()
 
@@ -556,6 +578,7 @@ def run_ours(args, dist: Dist):
         "gpu_launches": int(launches[head]),
         "clocks": clk,
         "setup_s": {"hierarchy_generation": round(gen_s, 2), "gpu_setup": round(setup_s, 2)},
+        "condensation": cond_info,
         "post_processing": post_info,
         "cpu_baseline": cpu,
     }
