@@ -612,10 +612,18 @@ def run_batched(args, dist: Dist):
                       "residual replacement in the device loop (FP32); the FP64-class run keeps the reference loop"),
            "host_generation_s": round(time.perf_counter() - t0, 1)}
     log(f"config 4: {len(specs)} problems generated in {out['host_generation_s']} s")
+    from fhhos4_gb300 import _native as N
     for prec in ("fp32", "df"):
         t1 = time.perf_counter()
-        probs, batch, build_s = BT.build(specs, device=dist.local_rank, precision=prec, autotune=True, generated=gen)
+        try:
+            probs, batch, build_s = BT.build(specs, device=dist.local_rank, precision=prec, autotune=True, generated=gen)
+        except N.FhgError as e:   # reported, not fatal: the other precision and the rest of the line go on
+            out[prec] = {"error": str(e)}
+            log(f"config 4 {prec}: setup failed: {e}")
+            torch.cuda.empty_cache()
+            continue
         setup_s = time.perf_counter() - t1
+        device_gb = sum(p.ctx.device_bytes() for p in probs) / 1e9
         for _ in range(2):
             rc, infos, ms = batch.solve()
         times = []
@@ -631,6 +639,7 @@ def run_batched(args, dist: Dist):
             p.ctx.solve_device(bd.data_ptr(), xd.data_ptr(), 200)
             rc1, h, info = p.ctx.solve_device(bd.data_ptr(), xd.data_ptr(), 200)
             seq_ms += info.solve_ms
+            del bd, xd
         its = [i.iterations for i in infos]
         trues = sorted(i.true_relative_residual for i in infos)
         out[prec] = {"batched_ms": round(batched_ms, 2), "sequential_ms": round(seq_ms, 2),
@@ -638,13 +647,15 @@ def run_batched(args, dist: Dist):
                      "dofs_per_s": round(dofs / (batched_ms * 1e-3), 1), "iterations_min_max": [min(its), max(its)],
                      "true_rel_residual_median_worst": [trues[len(trues) // 2], trues[-1]],
                      "problems_true_below_tol": sum(1 for t in trues if t < 1e-8), "status": rc,
-                     "setup_s": round(setup_s, 1),
+                     "setup_s": round(setup_s, 1), "device_gb": round(device_gb, 1),
                      "timing": f"median of {max(3, args.steps // 2)} launches after 2 untimed ones"}
-        log(f"config 4 {prec}: setup {setup_s:.1f} s, batched {batched_ms:.1f} ms, sequential {seq_ms:.1f} ms")
+        log(f"config 4 {prec}: setup {setup_s:.1f} s ({device_gb:.1f} GB), batched {batched_ms:.1f} ms, "
+            f"sequential {seq_ms:.1f} ms")
         batch.close()
         for p in probs:
             p.close()
         del probs, batch
+        torch.cuda.empty_cache()
     return out
 
 

@@ -40,7 +40,7 @@ LEARNED_PARAMS = 24848
 # Every symbol include/fhg.h declares.
 EXPORTS = ["fhg_default_options", "fhg_create", "fhg_destroy", "fhg_last_error", "fhg_set_level",
            "fhg_set_prolongation", "fhg_setup", "fhg_solve", "fhg_solve_device", "fhg_apply",
-           "fhg_time_op", "fhg_set_cycle", "fhg_set_coarse_smoothing", "fhg_set_vcycle_precision", "fhg_level_info", "fhg_fused_coarse_info", "fhg_get_permutation",
+           "fhg_time_op", "fhg_set_cycle", "fhg_set_coarse_smoothing", "fhg_set_vcycle_precision", "fhg_level_info", "fhg_fused_coarse_info", "fhg_device_bytes", "fhg_get_permutation",
            "fhg_kernel_launches", "fhg_residual_norm_noalloc", "fhg_set_face_tensors", "fhg_set_learned",
            "fhg_learned_reference_rate", "fhg_learned_features", "fhg_apply_internal", "fhg_net_num_params",
            "fhg_net_create", "fhg_net_destroy", "fhg_net_last_error", "fhg_net_set_params", "fhg_net_get_params",
@@ -104,6 +104,8 @@ def load(path: str = LIB):
     lib.fhg_set_cycle.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
     lib.fhg_set_coarse_smoothing.argtypes = [C.c_void_p, C.c_int, C.c_int]
     lib.fhg_fused_coarse_info.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int)]
+    lib.fhg_device_bytes.argtypes = [C.c_void_p]
+    lib.fhg_device_bytes.restype = C.c_longlong
     lib.fhg_level_info.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_longlong), P(C.c_int), P(C.c_int),
                                    P(C.c_longlong)]
     lib.fhg_get_permutation.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
@@ -242,6 +244,10 @@ class Context:
         self._check(self.lib.fhg_level_info(self.h, level, C.byref(nb), C.byref(nbl), C.byref(nc), C.byref(lanes),
                                             C.byref(pb)))
         return dict(block_rows=nb.value, blocks=nbl.value, colours=nc.value, lanes=lanes.value, p_blocks=pb.value)
+
+    def device_bytes(self) -> int:
+        """Device memory the context holds, in bytes."""
+        return int(self.lib.fhg_device_bytes(self.h))
 
     def fused_coarse_info(self, precision: str):
         """(first level of the one-launch coarse sub-cycle or -1, CTAs of its cluster) as run now."""

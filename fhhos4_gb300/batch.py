@@ -97,13 +97,27 @@ def generate_all(specs: List[ProblemSpec]):
 
 
 def build(specs: List[ProblemSpec], device: int = 0, precision: str = "fp64", autotune: bool = True,
-          keep_operator: bool = False, extra=(), generated=None):
+          keep_operator: bool = False, extra=(), generated=None, threads: int = 0):
     """Problems with b uploaded, and a Batch holding all of them. Returns (problems, batch, seconds).
-    generated: the hierarchies of generate_all(specs), reused; otherwise generated here."""
+    generated: the hierarchies of generate_all(specs), reused; otherwise generated here. The contexts
+    are set up on `threads` host threads (default: up to 16; ctypes releases the GIL, the library
+    times one context at a time); on a failure every context made so far is closed and it re-raises."""
     t0 = time.time()
     gen = generated if generated is not None else generate_all(specs)
-    probs = [Problem(s, device, precision, autotune, keep_operator=keep_operator, generated=g, extra=extra)
-             for s, g in zip(specs, gen)]
+    workers = max(1, min(len(specs), threads or min(16, os.cpu_count() or 1)))
+    with cf.ThreadPoolExecutor(workers) as ex:
+        futs = [ex.submit(Problem, s, device, precision, autotune, keep_operator=keep_operator, generated=g, extra=extra)
+                for s, g in zip(specs, gen)]
+    probs, err = [], None
+    for f in futs:
+        try:
+            probs.append(f.result())
+        except Exception as e:  # noqa: BLE001 - closed below, then re-raised
+            err = err or e
+    if err is not None:
+        for p in probs:
+            p.close()
+        raise err
     for p in probs:
         p.upload_b()
     batch = N.Batch(device)

@@ -131,6 +131,7 @@ struct fhg_ctx {
     int graphs_built = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<void*> allocations;
+    std::vector<size_t> allocation_bytes;   // beside allocations, same order
     // Learned correction of the FP32 V-cycle on the finest level (built at setup when the
     // V-cycle is FP32 and bs <= 4; the network is installed with fhg_set_learned).
     int* nbr_d = nullptr;              // nb0 x 6 neighbour blocks by decreasing |A_ij|_F, -1 padded
@@ -218,8 +219,20 @@ int dalloc(fhg_ctx* ctx, T** p, size_t count)
     if (e != cudaSuccess)
         return fail(ctx, FHG_ERR_CUDA, "cudaMalloc(%zu bytes) failed: %s", count * sizeof(T), cudaGetErrorString(e));
     ctx->allocations.push_back(q);
+    ctx->allocation_bytes.push_back(count * sizeof(T));
     *p = (T*)q;
     return FHG_OK;
+}
+
+// Free one allocation of the context (null: nothing).
+void dfree(fhg_ctx* ctx, const void* q)
+{
+    if (!q) return;
+    auto it = std::find(ctx->allocations.begin(), ctx->allocations.end(), q);
+    if (it == ctx->allocations.end()) return;
+    ctx->allocation_bytes.erase(ctx->allocation_bytes.begin() + (it - ctx->allocations.begin()));
+    ctx->allocations.erase(it);
+    cudaFree(const_cast<void*>(q));
 }
 
 template <class T>
@@ -1227,11 +1240,54 @@ int choose_fused(fhg_ctx* ctx)
     return FHG_OK;
 }
 
+// Views the launch choices do not use, freed once setup has made them (each precision keeps the GS
+// view and the product view its sweeps and products run on, level 0 the outer operator's chosen
+// pair view): at 64^3 the padded and slot-major copies each take about the size of the FP32 operator.
+template <class T>
+void release_bsr(fhg_ctx* ctx, DevBsr<T>& D)
+{
+    dfree(ctx, D.vals);
+    if (D.owns_index) {
+        dfree(ctx, D.rowptr);
+        dfree(ctx, D.colidx);
+    }
+    D = DevBsr<T>();
+}
+
+void release_unused_views(fhg_ctx* ctx)
+{
+    for (int l = 0; l + 1 < ctx->nlevels; l++) {
+        Level& L = ctx->levels[l];
+        if (L.G32s.vals && L.gs_slot[FHG_PREC_FP32]) release_bsr(ctx, L.G32);
+        else if (L.G32s.vals) release_bsr(ctx, L.G32s);
+        if (L.A32s.vals && L.prod_slot[FHG_PREC_FP32]) release_bsr(ctx, L.A32p);
+        else if (L.A32s.vals) release_bsr(ctx, L.A32s);
+        if (L.G2s.vals && L.gs_slot[FHG_PREC_DF]) release_bsr(ctx, L.G2);
+        else if (L.G2s.vals) release_bsr(ctx, L.G2s);
+        if (L.A2s.vals && L.prod_slot[FHG_PREC_DF]) release_bsr(ctx, L.A2p);
+        else if (L.A2s.vals) release_bsr(ctx, L.A2s);
+    }
+    Level& L0 = ctx->levels[0];
+    if (L0.Ahat2s.vals && L0.outer_slot && L0.ahat_lo) {
+        dfree(ctx, L0.Ahat_hi.vals);
+        dfree(ctx, L0.ahat_lo);
+        L0.Ahat_hi = DevBsr<float>();
+        L0.ahat_lo = nullptr;
+    } else if (L0.Ahat2s.vals && !L0.outer_slot) {
+        release_bsr(ctx, L0.Ahat2s);
+    }
+}
+
+// Timing at setup (launch shapes, the coarse sub-cycle) runs one context at a time, so contexts set up
+// on several host threads do their host work concurrently without disturbing each other's timings.
+std::recursive_mutex g_timing_mutex;
+
 // The coarse sub-cycle of every V-cycle precision the context holds: off, by timing (autotuning), or
 // from the first level of at most kFusedDefaultRows block rows with 8 CTAs. Called at setup and when
 // the cycle changes.
 int refresh_fused(fhg_ctx* ctx)
 {
+    std::lock_guard<std::recursive_mutex> timing(g_timing_mutex);
     const fhg_options& o = ctx->opts;
     const int bs = ctx->levels[0].bs;
     const bool fp32 = ctx->levels[0].A32.vals != nullptr, pair = ctx->levels[0].A2.vals != nullptr;
@@ -1328,7 +1384,7 @@ void outer_product_df(fhg_ctx* ctx, const float* dh, const float* dl, const floa
                       float* Adl, double* partials)
 {
     Level& L0 = ctx->levels[0];
-    if (L0.Ahat2s.vals && L0.outer_slot)
+    if (L0.Ahat2s.vals && (L0.outer_slot || !L0.ahat_lo))
         fhg::launch_spmv_dots_df_slot(L0.Ahat2s.v, dh, dl, rh, rl, Adh, Adl, partials, ctx->stream);
     else
         fhg::launch_spmv_dots_df(L0.Ahat_hi.v, L0.ahat_lo, dh, dl, rh, rl, Adh, Adl, partials, ctx->stream);
@@ -1340,7 +1396,7 @@ bool outer_df(const fhg_ctx* ctx)
 {
     const int p = ctx->opts.vcycle_precision;
     return (p == FHG_PREC_FP32 || (p == FHG_PREC_DF && ctx->rhi)) && ctx->opts.krylov == FHG_KRYLOV_FCG &&
-           ctx->levels[0].ahat_lo && ctx->rlo;
+           (ctx->levels[0].ahat_lo || ctx->levels[0].Ahat2s.vals) && ctx->rlo;
 }
 
 // High part of the outer residual pair: the FP32 V-cycle reads it as its right-hand side.
@@ -1761,6 +1817,7 @@ void free_all(fhg_ctx* ctx)
     ctx->rho_plain = 0.0;
     for (void* p : ctx->allocations) cudaFree(p);
     ctx->allocations.clear();
+    ctx->allocation_bytes.clear();
     if (ctx->nr_host) { cudaFreeHost(ctx->nr_host); ctx->nr_host = nullptr; }
     ctx->ready = false;
 }
@@ -2298,6 +2355,8 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
     // the high part of r: the FP32 V-cycle's right-hand side b32 itself; a buffer of its own otherwise
     if (pair && o.outer_split && (rc = dalloc(ctx, &ctx->rhi, n0))) return rc;
     CK(cudaMallocHost(&ctx->nr_host, sizeof(double)));
+    std::unique_lock<std::recursive_mutex> timing(g_timing_mutex, std::defer_lock);
+    if (o.autotune) timing.lock();
     if (o.autotune) {
         // Tune in the precision the V-cycle runs in (the FP64 copies keep the FP32 choices,
         // the same access pattern); the outer operators on their own launches.
@@ -2361,6 +2420,8 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
     }
     // the coarse sub-cycle: one cluster launch or launch by launch (timed when autotuning)
     if ((rc = refresh_fused(ctx))) return rc;
+    if (timing.owns_lock()) timing.unlock();
+    release_unused_views(ctx);
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->ready = true;
     return FHG_OK;
@@ -2513,8 +2574,7 @@ int fhg_apply(fhg_ctx* ctx, int level, int op, const double* in, const double* a
         if (e != cudaSuccess) rc = fail(ctx, FHG_ERR_CUDA, "apply: %s", cudaGetErrorString(e));
     }
     cudaStreamSynchronize(s);
-    ctx->allocations.erase(std::find(ctx->allocations.begin(), ctx->allocations.end(), (void*)t));
-    cudaFree(t);
+    dfree(ctx, t);
     return rc;
 }
 
@@ -2578,8 +2638,7 @@ static int time_op_t(fhg_ctx* ctx, int level, int op, int warmup, int reps, doub
         *avg_ms = ms / reps;
     }
     cudaStreamSynchronize(s);
-    ctx->allocations.erase(std::find(ctx->allocations.begin(), ctx->allocations.end(), (void*)t));
-    cudaFree(t);
+    dfree(ctx, t);
     return rc;
 }
 
@@ -2609,7 +2668,7 @@ int fhg_time_op(fhg_ctx* ctx, int level, int op, int precision, int warmup, int 
         // FP32 or DF: the outer operator in double-FP32 arithmetic (the one product both use)
         const bool split = op == FHG_OP_SYM_SPMV && (precision == FHG_PREC_FP32 || precision == FHG_PREC_DF);
         if (precision != FHG_PREC_FP64 && !split) return fail(ctx, FHG_ERR_INVALID_ARG, "op %d is timed in FP64 only", op);
-        if (split && (!L0.ahat_lo || !ctx->rlo))
+        if (split && ((!L0.ahat_lo && !L0.Ahat2s.vals) || !ctx->rlo))
             return fail(ctx, FHG_ERR_NOT_READY, "the double-FP32 outer operator was not built at setup");
         const size_t n0 = L0.n;
         double* t = nullptr;
@@ -2635,8 +2694,7 @@ int fhg_time_op(fhg_ctx* ctx, int level, int op, int precision, int warmup, int 
         float ms = 0;
         CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
         *avg_ms = ms / reps;
-        ctx->allocations.erase(std::find(ctx->allocations.begin(), ctx->allocations.end(), (void*)t));
-        cudaFree(t);
+        dfree(ctx, t);
         return rc;
     }
     if (precision == FHG_PREC_FP32) {
@@ -2716,6 +2774,14 @@ int fhg_level_info(const fhg_ctx* ctx, int level, int* n_block_rows, long long* 
     if (lanes) *lanes = L.A.v.lanes;
     if (p_blocks) *p_blocks = L.p_blocks;
     return FHG_OK;
+}
+
+long long fhg_device_bytes(const fhg_ctx* ctx)
+{
+    if (!ctx) return -1;
+    long long total = 0;
+    for (size_t b : ctx->allocation_bytes) total += (long long)b;
+    return total;
 }
 
 int fhg_fused_coarse_info(const fhg_ctx* ctx, int precision, int* first_level, int* cluster_ctas)

@@ -237,6 +237,10 @@ int fhg_fused_coarse_info(const fhg_ctx* ctx, int precision, int* first_level, i
 /* The colour permutation of `level` after setup: perm[new_block_row] = given_block_row. */
 int fhg_get_permutation(const fhg_ctx* ctx, int level, int* perm);
 
+/* Device memory the context holds after setup, in bytes (its own allocations). No counterpart in the
+ * reference. */
+long long fhg_device_bytes(const fhg_ctx* ctx);
+
 /* Number of kernels this library has launched in this process (graph replays included). */
 long long fhg_kernel_launches(const fhg_ctx* ctx);
 
