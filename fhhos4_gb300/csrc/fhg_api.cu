@@ -1905,14 +1905,13 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
             if (learned) learned_its++;
             if (std::isinf(nr)) { status = fail(ctx, FHG_ERR_DIVERGED, "divergence of the solver"); break; }
             if (std::isnan(nr)) { status = fail(ctx, FHG_ERR_NAN, "the residual is NaN."); break; }
-            // Fallback rule: from the third iteration on, when the mean reduction of the last two
-            // iterations falls behind the plain method's calibrated per-iteration reduction by more
-            // than half of it in logarithmic terms (rho > rho_plain^(1/2): the margin absorbs how
-            // much the early iterations of one right-hand side differ from the calibration's), the
-            // remaining iterations use the plain V-cycle.
+            // Fallback rule: from the third iteration on, when the per-iteration residual reduction
+            // (the geometric mean over the last two iterations, which evens out FCG's alternation)
+            // falls behind the plain method's calibrated per-iteration reduction, the remaining
+            // iterations use the plain V-cycle.
             if (learned && ctx->learned_mode == FHG_LEARNED_FALLBACK && it >= 3 && ctx->rho_plain > 0.0) {
                 const double rho = std::sqrt(hist[it] / hist[it - 2]);
-                if (!(rho <= std::sqrt(ctx->rho_plain))) learned = false;
+                if (!(rho <= ctx->rho_plain)) learned = false;
             }
         }
         if (learned_its > 0 && status == FHG_OK) status = check_learned_status(ctx);

@@ -286,9 +286,9 @@ int fhg_set_face_tensors(fhg_ctx* ctx, int n_blocks, const double* tensors);
  * select the mode. Needs a setup with FHG_PREC_FP32, two levels or more and block size 2..4;
  * call after every fhg_setup. FHG_LEARNED_FALLBACK: from the third iteration of a solve on,
  * when the geometric mean rho of the last two residual reductions falls behind the plain
- * method's per-iteration reduction rho_p by more than half of it in log terms (rho > sqrt(rho_p);
- * rho_p measured once per cycle configuration on a seeded random right-hand side, before the
- * first solve's timed region), the remaining iterations use the plain V-cycle. */
+ * method's per-iteration reduction rho_p (rho > rho_p; rho_p measured once per cycle configuration
+ * on a seeded random right-hand side, before the first solve's timed region), the remaining
+ * iterations use the plain V-cycle. */
 int fhg_set_learned(fhg_ctx* ctx, const float* params, int n_params, int mode);
 
 /* The plain method's calibrated per-iteration reduction used by the fallback rule. */
