@@ -54,8 +54,9 @@ template <class T>
 struct DevBsr {
     BsrView<T> v;
     T* vals = nullptr;
-    int* rowptr = nullptr;
+    int* rowptr = nullptr;   // row pointers (CSR), or the row permutation of a jagged view
     int* colidx = nullptr;
+    int* jds_start = nullptr;  // slot offsets of a jagged view
     bool owns_index = true;
 };
 
@@ -84,6 +85,11 @@ struct Level {
     DevBsr<float> A32s;         // FP32 A slot-major (all blocks, one thread per row), when built
     // FP32-pair copies (FHG_PREC_DF: FP64-class V-cycle on the FP32 pipe), same views as FP32
     DevBsr<dfl> A2, P2, R2, G2, A2p, G2s, A2s;
+    // jagged (JDS) views of the transfers, levels 0 and 1 (the large ones), and whether the products
+    // use them (per V-cycle precision, chosen by timing at setup)
+    DevBsr<float> P32j, R32j;
+    DevBsr<dfl> P2j, R2j;
+    bool p_jds[3] = {false, false, false}, r_jds[3] = {false, false, false};
     dfl* dinv2 = nullptr;
     dfl *x2 = nullptr, *b2 = nullptr, *r2 = nullptr;
     dfl* kv2[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -795,6 +801,53 @@ int upload_slot_major_all(fhg_ctx* ctx, const HostBsr& B, DevBsr<T>& D)
     return FHG_OK;
 }
 
+// Jagged (JDS) view of a transfer operator: rows stably sorted by decreasing block count, slot s of
+// sorted row k at start[s] + k, values entry-major with no padding. Not built above 64 blocks a row.
+template <class T>
+int upload_jds(fhg_ctx* ctx, const HostBsr& B, DevBsr<T>& D)
+{
+    D = DevBsr<T>();
+    const int nbr = B.nbr;
+    int W = 0;
+    for (int i = 0; i < nbr; i++) W = std::max(W, B.rowptr[i + 1] - B.rowptr[i]);
+    if (nbr == 0 || W == 0 || W > 64) return FHG_OK;
+    std::vector<int> perm(nbr);
+    for (int i = 0; i < nbr; i++) perm[i] = i;
+    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) {
+        return B.rowptr[a + 1] - B.rowptr[a] > B.rowptr[b + 1] - B.rowptr[b];
+    });
+    std::vector<int> start(W + 1, 0);
+    for (int sl = 0; sl < W; sl++) {
+        int rows = 0;
+        while (rows < nbr && B.rowptr[perm[rows] + 1] - B.rowptr[perm[rows]] > sl) rows++;
+        start[sl + 1] = start[sl] + rows;
+    }
+    const long long nnzb = B.nnzb();
+    const int bb = B.bs * B.bs;
+    const long long ld = round_up(std::max<long long>(nnzb, 1), 32);
+    std::vector<int> col((size_t)nnzb);
+    std::vector<T> soa((size_t)ld * bb, T(0));
+    for (int sl = 0; sl < W; sl++)
+        for (int k = 0; k < start[sl + 1] - start[sl]; k++) {
+            const long long p = B.rowptr[perm[k]] + sl;
+            const long long q = start[sl] + k;
+            col[(size_t)q] = B.colidx[(size_t)p];
+            for (int e = 0; e < bb; e++) soa[(size_t)e * ld + q] = (T)B.vals[(size_t)p * bb + e];
+        }
+    int rc;
+    int *dperm = nullptr, *dstart = nullptr;
+    if ((rc = upload(ctx, &dperm, perm.data(), perm.size())) || (rc = upload(ctx, &dstart, start.data(), start.size())) ||
+        (rc = upload(ctx, &D.colidx, col.data(), col.size())) || (rc = upload(ctx, &D.vals, soa.data(), soa.size())))
+        return rc;
+    D.rowptr = dperm;   // owned with the view (freed with it): the permutation and the slot offsets
+    D.v.nbr = B.nbr; D.v.nbc = B.nbc; D.v.bs = B.bs; D.v.nnzb = nnzb; D.v.ld = ld;
+    D.v.rowptr = nullptr; D.v.colidx = D.colidx; D.v.vals = D.vals;
+    D.v.jds_perm = dperm; D.v.jds_start = dstart; D.v.jds_slots = W;
+    D.v.lanes = 1;
+    D.jds_start = dstart;
+    return FHG_OK;
+}
+
 // Outer operator as an FP32 pair: hi = fl32(a), lo = fl32(a - hi), entry-major like upload_bsr.
 int upload_bsr_split(fhg_ctx* ctx, const HostBsr& B, DevBsr<float>& D, float** lo_out, const DevBsr<double>& share_index)
 {
@@ -898,6 +951,8 @@ template <> struct LevelVecs<double> {
     static const BsrView<double>& A(Level& L) { return L.A.v; }
     static const BsrView<double>& P(Level& L) { return L.P.v; }
     static const BsrView<double>& R(Level& L) { return L.R.v; }
+    static const BsrView<double>& Pcsr(Level& L) { return L.P.v; }
+    static const BsrView<double>& Rcsr(Level& L) { return L.R.v; }
     static const double* dinv(Level& L) { return L.dinv; }
     static double* k(Level& L, int i) { return L.kv64[i]; }
     static const BsrView<double>& gs(Level& L) { return L.A.v; }
@@ -914,10 +969,12 @@ template <> struct LevelVecs<float> {
         if (L.prod_slot[kPrec] && L.A32s.vals) return L.A32s.v;
         return L.A32p.vals ? L.A32p.v : L.A32.v;
     }
-    // P stays CSR: at 64^3 its rows of up to 7 blocks pad by 29%, which costs what the saved
-    // row-pointer load gains (0.180 ms either way)
-    static const BsrView<float>& P(Level& L) { return L.P32.v; }
-    static const BsrView<float>& R(Level& L) { return L.R32.v; }
+    // transfers: the jagged view when setup kept it, else CSR (padded rows of P cost what the saved
+    // row-pointer load gains: its rows hold 1 to 7 blocks)
+    static const BsrView<float>& P(Level& L) { return L.p_jds[kPrec] && L.P32j.vals ? L.P32j.v : L.P32.v; }
+    static const BsrView<float>& R(Level& L) { return L.r_jds[kPrec] && L.R32j.vals ? L.R32j.v : L.R32.v; }
+    static const BsrView<float>& Pcsr(Level& L) { return L.P32.v; }
+    static const BsrView<float>& Rcsr(Level& L) { return L.R32.v; }
     static const float* dinv(Level& L) { return L.dinv32; }
     static float* k(Level& L, int i) { return L.kv32[i]; }
     // GS sweeps: the slot-major or padded off-diagonal view when setup built one
@@ -939,8 +996,10 @@ template <> struct LevelVecs<dfl> {
         if (L.prod_slot[kPrec] && L.A2s.vals) return L.A2s.v;
         return L.A2p.vals ? L.A2p.v : L.A2.v;
     }
-    static const BsrView<dfl>& P(Level& L) { return L.P2.v; }
-    static const BsrView<dfl>& R(Level& L) { return L.R2.v; }
+    static const BsrView<dfl>& P(Level& L) { return L.p_jds[kPrec] && L.P2j.vals ? L.P2j.v : L.P2.v; }
+    static const BsrView<dfl>& R(Level& L) { return L.r_jds[kPrec] && L.R2j.vals ? L.R2j.v : L.R2.v; }
+    static const BsrView<dfl>& Pcsr(Level& L) { return L.P2.v; }
+    static const BsrView<dfl>& Rcsr(Level& L) { return L.R2.v; }
     static const dfl* dinv(Level& L) { return L.dinv2; }
     static dfl* k(Level& L, int i) { return L.kv2[i]; }
     static const BsrView<dfl>& gs(Level& L)
@@ -1126,9 +1185,9 @@ bool fused_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
             const BsrView<T>& A = V::Acsr(L);
             F.a_rowptr = A.rowptr; F.a_colidx = A.colidx; F.a_vals = A.vals; F.a_ld = A.ld;
             F.dinv = V::dinv(L);
-            const BsrView<T>& Pv = V::P(L);
+            const BsrView<T>& Pv = V::Pcsr(L);
             F.p_rowptr = Pv.rowptr; F.p_colidx = Pv.colidx; F.p_vals = Pv.vals; F.p_ld = Pv.ld;
-            const BsrView<T>& Rv = V::R(L);
+            const BsrView<T>& Rv = V::Rcsr(L);
             F.r_rowptr = Rv.rowptr; F.r_colidx = Rv.colidx; F.r_vals = Rv.vals; F.r_ld = Rv.ld;
             F.lanes = fused_lanes(A);
             F.t_lanes = fused_lanes(Rv);
@@ -1250,6 +1309,7 @@ void release_bsr(fhg_ctx* ctx, DevBsr<T>& D)
     if (D.owns_index) {
         dfree(ctx, D.rowptr);
         dfree(ctx, D.colidx);
+        dfree(ctx, D.jds_start);
     }
     D = DevBsr<T>();
 }
@@ -1266,6 +1326,10 @@ void release_unused_views(fhg_ctx* ctx)
         else if (L.G2s.vals) release_bsr(ctx, L.G2s);
         if (L.A2s.vals && L.prod_slot[FHG_PREC_DF]) release_bsr(ctx, L.A2p);
         else if (L.A2s.vals) release_bsr(ctx, L.A2s);
+        if (L.P32j.vals && !L.p_jds[FHG_PREC_FP32]) release_bsr(ctx, L.P32j);
+        if (L.R32j.vals && !L.r_jds[FHG_PREC_FP32]) release_bsr(ctx, L.R32j);
+        if (L.P2j.vals && !L.p_jds[FHG_PREC_DF]) release_bsr(ctx, L.P2j);
+        if (L.R2j.vals && !L.r_jds[FHG_PREC_DF]) release_bsr(ctx, L.R2j);
     }
     Level& L0 = ctx->levels[0];
     if (L0.Ahat2s.vals && L0.outer_slot && L0.ahat_lo) {
@@ -1610,6 +1674,7 @@ struct TuneKey {
 struct TuneShapes {
     int a_lanes, a_unroll, gs_lanes, gs_unroll, p_lanes, p_unroll, r_lanes, r_unroll;
     bool prod_slot, gs_slot;
+    bool p_jds = false, r_jds = false;
 };
 std::mutex g_tune_mutex;
 std::map<TuneKey, TuneShapes> g_tune_cache;
@@ -1630,8 +1695,8 @@ int tune_level(fhg_ctx* ctx, int l)
     L.prod_slot[PR] = false;
     L.gs_slot[PR] = false;
     BsrView<T>& A = const_cast<BsrView<T>&>(V::A(L));
-    TuneKey key{PR, L.bs, L.nb, L.ncolours, V::gs(L).ell, A.ell, coarsest ? 0 : V::P(L).nbr,
-                coarsest ? 0 : V::R(L).nbr, A.nnzb, coarsest ? 0 : V::P(L).nnzb};
+    TuneKey key{PR, L.bs, L.nb, L.ncolours, V::gs(L).ell, A.ell, coarsest ? 0 : V::Pcsr(L).nbr,
+                coarsest ? 0 : V::Rcsr(L).nbr, A.nnzb, coarsest ? 0 : V::Pcsr(L).nnzb};
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         auto it = g_tune_cache.find(key);
@@ -1644,10 +1709,12 @@ int tune_level(fhg_ctx* ctx, int l)
             L.gs_unroll[PR] = t.gs_unroll;
             L.gs_slot[PR] = t.gs_slot;
             if (!coarsest) {
-                BsrView<T>& P = const_cast<BsrView<T>&>(V::P(L));
-                BsrView<T>& R = const_cast<BsrView<T>&>(V::R(L));
+                BsrView<T>& P = const_cast<BsrView<T>&>(V::Pcsr(L));
+                BsrView<T>& R = const_cast<BsrView<T>&>(V::Rcsr(L));
                 P.lanes = t.p_lanes; P.unroll = t.p_unroll;
                 R.lanes = t.r_lanes; R.unroll = t.r_unroll;
+                L.p_jds[PR] = t.p_jds;
+                L.r_jds[PR] = t.r_jds;
             }
             return FHG_OK;
         }
@@ -1662,8 +1729,10 @@ int tune_level(fhg_ctx* ctx, int l)
     TuneShapes t{Ar.lanes, Ar.unroll, L.gs_lanes[PR], L.gs_unroll[PR], 0, 1, 0, 1, ps, L.gs_slot[PR]};
     L.prod_slot[PR] = ps;
     if (!coarsest) {
-        t.p_lanes = V::P(L).lanes; t.p_unroll = V::P(L).unroll;
-        t.r_lanes = V::R(L).lanes; t.r_unroll = V::R(L).unroll;
+        t.p_lanes = V::Pcsr(L).lanes; t.p_unroll = V::Pcsr(L).unroll;
+        t.r_lanes = V::Rcsr(L).lanes; t.r_unroll = V::Rcsr(L).unroll;
+        t.p_jds = L.p_jds[PR];
+        t.r_jds = L.r_jds[PR];
     }
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     g_tune_cache[key] = t;
@@ -1737,19 +1806,50 @@ int tune_level_uncached(fhg_ctx* ctx, int l)
                 L.gs_slot[PR] = slot_ms < row_ms;
             }
         }
-        BsrView<T>& P = const_cast<BsrView<T>&>(V::P(L));
-        BsrView<T>& R = const_cast<BsrView<T>&>(V::R(L));
+        BsrView<T>& P = const_cast<BsrView<T>&>(V::Pcsr(L));
+        BsrView<T>& R = const_cast<BsrView<T>&>(V::Rcsr(L));
+        const bool forced_jds = ctx->opts.gs_layout == FHG_GS_SLOT;   // the jagged views, not compared
+        const bool pj0 = L.p_jds[V::kPrec], rj0 = L.r_jds[V::kPrec];
+        L.p_jds[V::kPrec] = false;
+        L.r_jds[V::kPrec] = false;
         CK(cudaMemsetAsync(V::x(C), 0, sizeof(T) * C.n, s));
+        float p_ms = 0.f, r_ms = 0.f;
         if ((rc = tune(ctx, bs, P.lanes, P.unroll, [&](int G, int U) {
                  BsrView<T> v = P; v.lanes = G; v.unroll = U;
                  fhg::launch_spmv<T>(v, fhg::kSpmvAddTo, V::x(C), V::r(L), V::r(L), s);
-             })))
+             }, &p_ms)))
             return rc;
         if ((rc = tune(ctx, bs, R.lanes, R.unroll, [&](int G, int U) {
                  BsrView<T> v = R; v.lanes = G; v.unroll = U;
                  fhg::launch_spmv<T>(v, fhg::kSpmvAssign, V::r(L), nullptr, V::b(C), s);
-             })))
+             }, &r_ms)))
             return rc;
+        // the jagged views against the best CSR shapes
+        if (forced_jds) {
+            L.p_jds[V::kPrec] = pj0;
+            L.r_jds[V::kPrec] = rj0;
+        } else if constexpr (!std::is_same<T, double>::value) {
+            const BsrView<T>* pj = nullptr;
+            const BsrView<T>* rj = nullptr;
+            if constexpr (std::is_same<T, float>::value) {
+                if (L.P32j.vals) pj = &L.P32j.v;
+                if (L.R32j.vals) rj = &L.R32j.v;
+            } else {
+                if (L.P2j.vals) pj = &L.P2j.v;
+                if (L.R2j.vals) rj = &L.R2j.v;
+            }
+            float ms = 0.f;
+            if (pj) {
+                if ((rc = time_candidate(ctx, [&]() { fhg::launch_spmv<T>(*pj, fhg::kSpmvAddTo, V::x(C), V::r(L), V::r(L), s); }, &ms)))
+                    return rc;
+                L.p_jds[V::kPrec] = ms < p_ms;
+            }
+            if (rj) {
+                if ((rc = time_candidate(ctx, [&]() { fhg::launch_spmv<T>(*rj, fhg::kSpmvAssign, V::r(L), nullptr, V::b(C), s); }, &ms)))
+                    return rc;
+                L.r_jds[V::kPrec] = ms < r_ms;
+            }
+        }
     }
     return FHG_OK;
 }
@@ -1786,6 +1886,11 @@ void reset_device_state(Level& L)
     L.A2p = DevBsr<dfl>();
     L.G2s = DevBsr<dfl>();
     L.A2s = DevBsr<dfl>();
+    L.P32j = DevBsr<float>();
+    L.R32j = DevBsr<float>();
+    L.P2j = DevBsr<dfl>();
+    L.R2j = DevBsr<dfl>();
+    for (int i = 0; i < 3; i++) { L.p_jds[i] = false; L.r_jds[i] = false; }
     L.dinv2 = nullptr;
     L.x2 = L.b2 = L.r2 = nullptr;
     for (int i = 0; i < 3; i++) { L.gs_slot[i] = false; L.prod_slot[i] = false; L.gs_lanes[i] = 0; L.gs_unroll[i] = 1; }
@@ -2287,6 +2392,18 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
             if (pair) {
                 if ((rc = upload_bsr<dfl>(ctx, Pp, L.P2, &L.P))) return rc;
                 if ((rc = upload_bsr<dfl>(ctx, Rp, L.R2, &L.R))) return rc;
+            }
+            // the jagged transfer views of the two largest levels: compared by the autotuner, or used
+            // with FHG_GS_SLOT
+            const bool want_jds = o.gs_layout == FHG_GS_SLOT || (o.gs_layout == FHG_GS_AUTO && o.autotune);
+            if (want_jds && l <= 1) {
+                if (fp32 && ((rc = upload_jds(ctx, Pp, L.P32j)) || (rc = upload_jds(ctx, Rp, L.R32j)))) return rc;
+                if (pair && ((rc = upload_jds(ctx, Pp, L.P2j)) || (rc = upload_jds(ctx, Rp, L.R2j)))) return rc;
+                if (o.gs_layout == FHG_GS_SLOT)
+                    for (int q : {FHG_PREC_FP32, FHG_PREC_DF}) {
+                        L.p_jds[q] = true;
+                        L.r_jds[q] = true;
+                    }
             }
         }
         if (l == 0 && fp32 && nlevels > 1 && fhg::learned_supports(bs)) {

@@ -273,6 +273,53 @@ __global__ void __launch_bounds__(kThreads) k_bsr_spmv(int nbr, const int* __res
     }
 }
 
+// y = M x | y = y + M x on the jagged view (rows sorted by decreasing block count, slot s of sorted
+// row k at start[s] + k): one thread per row, every slot's load of a warp is 32 consecutive blocks with
+// no padding, the sorted order ends a row's walk at its own length. The output row is scattered by
+// the permutation (the vectors of one level stay in L2). The row's blocks are summed in column order.
+constexpr int kMaxJdsSlots = 64;
+
+template <class T, int BS, int MODE>
+__global__ void __launch_bounds__(kThreads) k_bsr_spmv_jds(int nbr, int nslots, const int* __restrict__ perm,
+                                                           const int* __restrict__ start,
+                                                           const int* __restrict__ colidx,
+                                                           const T* __restrict__ vals, long long ld,
+                                                           const T* __restrict__ x, const T* aux, T* y)
+{
+    pdl_wait();
+    __shared__ int sh_start[kMaxJdsSlots + 1];
+    for (int i = threadIdx.x; i <= nslots; i += blockDim.x) sh_start[i] = start[i];
+    __syncthreads();
+    const int k = (int)(blockIdx.x * kThreads + threadIdx.x);
+    if (k >= nbr) return;
+    const long long row = perm[k];
+    T av[BS];
+    if (MODE != kSpmvAssign)
+#pragma unroll
+        for (int r = 0; r < BS; r++) av[r] = aux[row * BS + r];
+    T acc[BS];
+#pragma unroll
+    for (int r = 0; r < BS; r++) acc[r] = T(0);
+#pragma unroll 2
+    for (int sl = 0; sl < nslots; sl++) {
+        const int p = sh_start[sl] + k;
+        if (p >= sh_start[sl + 1]) break;
+        const long long col = colidx[p];
+        T xv[BS];
+#pragma unroll
+        for (int c = 0; c < BS; c++) xv[c] = x[col * BS + c];
+#pragma unroll
+        for (int r = 0; r < BS; r++)
+#pragma unroll
+            for (int c = 0; c < BS; c++) acc[r] = fma(vals[(long long)(r * BS + c) * ld + p], xv[c], acc[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < BS; r++) {
+        if (MODE == kSpmvAssign) y[row * BS + r] = fin(acc[r]);
+        else y[row * BS + r] = av[r] + acc[r];
+    }
+}
+
 // w = D^-1 (b - A x) (block-Jacobi-scaled residual, the learned step's input): the residual of a
 // row is reduced over the row's lanes, then lane r < BS applies row r of the row's D^-1.
 template <class T, int BS, int G, int U>
@@ -744,6 +791,29 @@ template <class T>
 void launch_spmv(const BsrView<T>& A, int mode, const T* x, const T* aux, T* y, cudaStream_t s)
 {
     if (A.nbr == 0) return;
+    if (A.jds_perm) {
+        // jagged views exist only for the transfers (assign, add-to) with at most kMaxJdsSlots blocks
+        // a row (setup builds no other); they have no row pointers to fall back on
+        if ((mode != kSpmvAssign && mode != kSpmvAddTo) || A.jds_slots > kMaxJdsSlots) return;
+        const unsigned grid = grid_for(A.nbr, kThreads);
+#define FHG_JDS_LAUNCH(BSV)                                                                                     \
+        if (mode == kSpmvAssign)                                                                                 \
+            pdl_launch(k_bsr_spmv_jds<T, BSV, kSpmvAssign>, grid, kThreads, 0, s, A.nbr, A.jds_slots, A.jds_perm, \
+                       A.jds_start, A.colidx, A.vals, A.ld, x, aux, y);                                          \
+        else                                                                                                     \
+            pdl_launch(k_bsr_spmv_jds<T, BSV, kSpmvAddTo>, grid, kThreads, 0, s, A.nbr, A.jds_slots, A.jds_perm,  \
+                       A.jds_start, A.colidx, A.vals, A.ld, x, aux, y);
+        switch (A.bs) {
+        case 2: FHG_JDS_LAUNCH(2) break;
+        case 3: FHG_JDS_LAUNCH(3) break;
+        case 4: FHG_JDS_LAUNCH(4) break;
+        case 6: FHG_JDS_LAUNCH(6) break;
+        default: break;
+        }
+#undef FHG_JDS_LAUNCH
+        g_kernel_launches++;
+        return;
+    }
     if constexpr (!std::is_same<T, double>::value) {
         if (A.slot_major) {   // FP32 and pair product views (no FP64 slot-major view is built)
             const unsigned grid = grid_for(A.nbr, kThreads);

@@ -32,6 +32,12 @@ struct BsrView {
     const int* rowptr = nullptr;
     const int* colidx = nullptr;
     const T* vals = nullptr;
+    // Jagged view (JDS, the transfer operators): rows sorted by decreasing block count, row
+    // jds_perm[k] in sorted place k, its slot s at jds_start[s] + k (jds_start[s + 1] - jds_start[s]
+    // rows have more than s blocks); no padding, rowptr unused; products only (assign, add-to).
+    const int* jds_perm = nullptr;
+    const int* jds_start = nullptr;
+    int jds_slots = 0;
 };
 
 // Fixed number of CTAs of the reduction kernels: the partial-sum arrays they write

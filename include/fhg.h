@@ -121,7 +121,9 @@ typedef struct {
     int gs_layout;              /* FP32 GS sweeps: FHG_GS_AUTO (the autotuner picks row- or slot-major padded
                                    rows; row-major without autotuning), FHG_GS_ROW, FHG_GS_SLOT. Same
                                    arithmetic, different storage order and launch shape; FHG_GS_SLOT also
-                                   makes the products with A use the slot-major view of all of A. */
+                                   makes the products with A use the slot-major view of all of A, and
+                                   the transfers of levels 0 and 1 their jagged views (rows sorted by
+                                   block count, one thread per row); the autotuner compares those too. */
     int extra_precisions;       /* bit mask (1 << FHG_PREC_FP32, 1 << FHG_PREC_DF) of V-cycle precisions whose
                                    operator copies setup also builds, besides vcycle_precision's, so that
                                    fhg_set_vcycle_precision can switch to them (FP64 copies are always built) */
