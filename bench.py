@@ -465,6 +465,11 @@ def run_ours(args, dist: Dist):
         e2e_times.append(time.perf_counter() - t)
     e2e_s = dist.max(float(np.mean(e2e_times)))
 
+    # Which part of the headline cycle runs as one cluster launch (chosen by timing at setup), and the
+    # context's device memory.
+    first, ctas = ctx.fused_coarse_info("fp32")
+    fused_info = {"first_level": first, "cluster_ctas": ctas, "device_gb": round(ctx.device_bytes() / 1e9, 2)}
+
     # Per-kernel device timing on level 0 (CUDA events on the library's stream).
     p32, p64 = 4, 8
     info1 = ctx.level_info(1) if len(As) > 1 else None
@@ -555,7 +560,8 @@ def run_ours(args, dist: Dist):
         "method": {"name": ("learned correction + " if head == "learned" else "") + "FP32 V-cycle inside FP64 FCG(1)",
                    "krylov": "FCG(1), double-FP32 outer product, FP64 x and Krylov scalars",
                    "cycle": results[head]["cycle"], "vcycle_precision": "fp32",
-                   "coarsest": "FP64 dense inverse of the coarsest operator", "colours_level0": ncol},
+                   "coarsest": "FP64 dense inverse of the coarsest operator", "colours_level0": ncol,
+                   "coarse_subcycle_one_launch": fused_info},
         "plain_fp64": dict(results["plain"], reference_iterations_colour_order=ref_col,
                            reference_iterations_natural_order=ref_nat,
                            arithmetic="FP64-class: FP32 pairs (~2^-47 per term) on the FP32 pipe, FP64 x"),
