@@ -67,6 +67,7 @@ class Problem:
             ctx.set_prolongation(l, P)
         o = N.default_options()
         o.galerkin = 1
+        o.replace_residual = 1   # every precision: the FP64 true residual must meet the tolerance
         o.vcycle_precision = N.PRECISION[precision]
         o.extra_precisions = sum(1 << N.PRECISION[p] for p in set(extra))
         o.autotune = 1 if autotune else 0

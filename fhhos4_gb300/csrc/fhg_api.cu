@@ -109,6 +109,9 @@ struct Level {
 
 }  // namespace
 
+// Iterations over which the learned step's residual reduction is compared with the plain method's.
+constexpr int kFallbackWindow = 4;
+
 struct fhg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -2010,12 +2013,13 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
             if (learned) learned_its++;
             if (std::isinf(nr)) { status = fail(ctx, FHG_ERR_DIVERGED, "divergence of the solver"); break; }
             if (std::isnan(nr)) { status = fail(ctx, FHG_ERR_NAN, "the residual is NaN."); break; }
-            // Fallback rule: from the third iteration on, when the per-iteration residual reduction
-            // (the geometric mean over the last two iterations, which evens out FCG's alternation)
-            // falls behind the plain method's calibrated per-iteration reduction, the remaining
-            // iterations use the plain V-cycle.
-            if (learned && ctx->learned_mode == FHG_LEARNED_FALLBACK && it >= 3 && ctx->rho_plain > 0.0) {
-                const double rho = std::sqrt(hist[it] / hist[it - 2]);
+            // Fallback rule: from the sixth iteration on, when the per-iteration residual reduction
+            // (the geometric mean over the last four iterations, which evens out FCG's irregular
+            // first iterations and its alternation) falls behind the plain method's calibrated
+            // per-iteration reduction, the remaining iterations use the plain V-cycle.
+            if (learned && ctx->learned_mode == FHG_LEARNED_FALLBACK && it >= kFallbackWindow + 2 &&
+                ctx->rho_plain > 0.0) {
+                const double rho = std::pow(hist[it] / hist[it - kFallbackWindow], 1.0 / kFallbackWindow);
                 if (!(rho <= ctx->rho_plain)) learned = false;
             }
         }

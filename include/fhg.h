@@ -286,8 +286,8 @@ int fhg_set_face_tensors(fhg_ctx* ctx, int n_blocks, const double* tensors);
 
 /* Install a network (params: FHG_LEARNED_PARAMS floats, host; NULL keeps the installed one) and
  * select the mode. Needs a setup with FHG_PREC_FP32, two levels or more and block size 2..4;
- * call after every fhg_setup. FHG_LEARNED_FALLBACK: from the third iteration of a solve on,
- * when the geometric mean rho of the last two residual reductions falls behind the plain
+ * call after every fhg_setup. FHG_LEARNED_FALLBACK: from the sixth iteration of a solve on,
+ * when the geometric mean rho of the last four residual reductions falls behind the plain
  * method's per-iteration reduction rho_p (rho > rho_p; rho_p measured once per cycle configuration
  * on a seeded random right-hand side, before the first solve's timed region), the remaining
  * iterations use the plain V-cycle. */
