@@ -286,9 +286,14 @@ __global__ void __launch_bounds__(kThreads) k_bsr_spmv_jds(int nbr, int nslots, 
                                                            const T* __restrict__ vals, long long ld,
                                                            const T* __restrict__ x, const T* aux, T* y)
 {
+    // Slots go in groups of kJdsGroup with every load of a group issued before its sums (predicated on
+    // the row's length, the sorted order making the valid slots a prefix), so that a row's loads are in
+    // flight together instead of one slot's after the other's.
+    constexpr int kBlockBytes = BS * BS * (int)sizeof(T);
+    constexpr int kJdsGroup = kBlockBytes <= 36 ? 4 : kBlockBytes <= 72 ? 2 : 1;   // registers: ~144 values
     pdl_wait();
-    __shared__ int sh_start[kMaxJdsSlots + 1];
-    for (int i = threadIdx.x; i <= nslots; i += blockDim.x) sh_start[i] = start[i];
+    __shared__ int sh_start[kMaxJdsSlots + kJdsGroup + 1];
+    for (int i = threadIdx.x; i <= nslots + kJdsGroup; i += blockDim.x) sh_start[i] = start[i < nslots ? i : nslots];
     __syncthreads();
     const int k = (int)(blockIdx.x * kThreads + threadIdx.x);
     if (k >= nbr) return;
@@ -300,18 +305,33 @@ __global__ void __launch_bounds__(kThreads) k_bsr_spmv_jds(int nbr, int nslots, 
     T acc[BS];
 #pragma unroll
     for (int r = 0; r < BS; r++) acc[r] = T(0);
-#pragma unroll 2
-    for (int sl = 0; sl < nslots; sl++) {
-        const int p = sh_start[sl] + k;
-        if (p >= sh_start[sl + 1]) break;
-        const long long col = colidx[p];
-        T xv[BS];
+    for (int s0 = 0; s0 < nslots; s0 += kJdsGroup) {
+        if (sh_start[s0] + k >= sh_start[s0 + 1]) break;   // the row has no slot s0
+        int col[kJdsGroup];
+        bool ok[kJdsGroup];
 #pragma unroll
-        for (int c = 0; c < BS; c++) xv[c] = x[col * BS + c];
+        for (int g = 0; g < kJdsGroup; g++) {
+            const int p = sh_start[s0 + g] + k;
+            ok[g] = s0 + g < nslots && p < sh_start[s0 + g + 1];
+            col[g] = ok[g] ? colidx[p] : 0;
+        }
+        T xv[kJdsGroup][BS], av2[kJdsGroup][BS * BS];
 #pragma unroll
-        for (int r = 0; r < BS; r++)
+        for (int g = 0; g < kJdsGroup; g++) {
+            const long long p = (long long)sh_start[s0 + g] + k;
 #pragma unroll
-            for (int c = 0; c < BS; c++) acc[r] = fma(vals[(long long)(r * BS + c) * ld + p], xv[c], acc[r]);
+            for (int c = 0; c < BS; c++) xv[g][c] = ok[g] ? x[(long long)col[g] * BS + c] : T(0);
+#pragma unroll
+            for (int e = 0; e < BS * BS; e++) av2[g][e] = ok[g] ? vals[(long long)e * ld + p] : T(0);
+        }
+#pragma unroll
+        for (int g = 0; g < kJdsGroup; g++) {
+            if (!ok[g]) continue;
+#pragma unroll
+            for (int r = 0; r < BS; r++)
+#pragma unroll
+                for (int c = 0; c < BS; c++) acc[r] = fma(av2[g][r * BS + c], xv[g][c], acc[r]);
+        }
     }
 #pragma unroll
     for (int r = 0; r < BS; r++) {
