@@ -1681,6 +1681,11 @@ struct TuneShapes {
 };
 std::mutex g_tune_mutex;
 std::map<TuneKey, TuneShapes> g_tune_cache;
+struct OuterChoice {
+    int lanes, df_lanes;
+    bool slot;
+};
+std::map<std::vector<long long>, OuterChoice> g_outer_cache;   // the outer operator's, per structure
 
 template <class T>
 int tune_level_uncached(fhg_ctx* ctx, int l);
@@ -2505,37 +2510,57 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         }
         Level& L0 = ctx->levels[0];
         BsrView<double>& Ah = L0.ahat_is_a ? L0.A.v : L0.Ahat.v;
-        int g = Ah.lanes, gu = 1;
-        CK(cudaMemsetAsync(ctx->kz[0], 0, sizeof(double) * L0.n, ctx->stream));
-        if ((rc = tune(ctx, 9, g, gu, [&](int G, int) {
-                 BsrView<double> v = Ah; v.lanes = G;
-                 fhg::launch_spmv_dots(v, ctx->kz[0], ctx->kz[0], ctx->kAd[0], part(ctx, 5), ctx->stream);
-             })))
-            return rc;
-        L0.outer_lanes = g;
-        if (L0.ahat_lo) {
-            int gd = g, gdu = 1;
-            const long long n = L0.n;
-            float row_ms = 0.f;
-            if ((rc = tune(ctx, 9, gd, gdu, [&](int G, int) {
-                     BsrView<float> v = L0.Ahat_hi.v; v.lanes = G;
-                     fhg::launch_spmv_dots_df(v, L0.ahat_lo, pair_hi(ctx->kz[0]), pair_lo(ctx->kz[0], n),
-                                              pair_hi(ctx->kz[0]), pair_lo(ctx->kz[0], n), pair_hi(ctx->kAd[0]),
-                                              pair_lo(ctx->kAd[0], n), part(ctx, 5), ctx->stream);
-                 }, &row_ms)))
-                return rc;
-            // the slot-major pair view against the best row-major shape
-            if (L0.Ahat2s.vals) {
-                float slot_ms = 0.f;
-                if ((rc = time_candidate(ctx, [&]() {
-                         fhg::launch_spmv_dots_df_slot(L0.Ahat2s.v, pair_hi(ctx->kz[0]), pair_lo(ctx->kz[0], n),
-                                                       pair_hi(ctx->kz[0]), pair_lo(ctx->kz[0], n), pair_hi(ctx->kAd[0]),
-                                                       pair_lo(ctx->kAd[0], n), part(ctx, 5), ctx->stream);
-                     }, &slot_ms)))
-                    return rc;
-                L0.outer_slot = slot_ms < row_ms;
+        // the outer operator's choices, kept per structure like the levels' shapes
+        const std::vector<long long> okey = {L0.bs, L0.nb, (long long)Ah.nnzb, L0.ahat_is_a ? 1 : 0,
+                                             L0.ahat_lo ? 1 : 0, L0.Ahat2s.vals ? 1 : 0, o.gs_layout};
+        bool cached = false;
+        if (o.gs_layout == FHG_GS_AUTO) {
+            std::lock_guard<std::mutex> lock(g_tune_mutex);
+            auto it = g_outer_cache.find(okey);
+            if (it != g_outer_cache.end()) {
+                L0.outer_lanes = it->second.lanes;
+                if (L0.ahat_lo) L0.Ahat_hi.v.lanes = it->second.df_lanes;
+                L0.outer_slot = it->second.slot;
+                cached = true;
             }
-            L0.Ahat_hi.v.lanes = gd;
+        }
+        if (!cached) {
+            int g = Ah.lanes, gu = 1;
+            CK(cudaMemsetAsync(ctx->kz[0], 0, sizeof(double) * L0.n, ctx->stream));
+            if ((rc = tune(ctx, 9, g, gu, [&](int G, int) {
+                     BsrView<double> v = Ah; v.lanes = G;
+                     fhg::launch_spmv_dots(v, ctx->kz[0], ctx->kz[0], ctx->kAd[0], part(ctx, 5), ctx->stream);
+                 })))
+                return rc;
+            L0.outer_lanes = g;
+            if (L0.ahat_lo) {
+                int gd = g, gdu = 1;
+                const long long n = L0.n;
+                float row_ms = 0.f;
+                if ((rc = tune(ctx, 9, gd, gdu, [&](int G, int) {
+                         BsrView<float> v = L0.Ahat_hi.v; v.lanes = G;
+                         fhg::launch_spmv_dots_df(v, L0.ahat_lo, pair_hi(ctx->kz[0]), pair_lo(ctx->kz[0], n),
+                                                  pair_hi(ctx->kz[0]), pair_lo(ctx->kz[0], n), pair_hi(ctx->kAd[0]),
+                                                  pair_lo(ctx->kAd[0], n), part(ctx, 5), ctx->stream);
+                     }, &row_ms)))
+                    return rc;
+                // the slot-major pair view against the best row-major shape
+                if (L0.Ahat2s.vals) {
+                    float slot_ms = 0.f;
+                    if ((rc = time_candidate(ctx, [&]() {
+                             fhg::launch_spmv_dots_df_slot(L0.Ahat2s.v, pair_hi(ctx->kz[0]), pair_lo(ctx->kz[0], n),
+                                                           pair_hi(ctx->kz[0]), pair_lo(ctx->kz[0], n), pair_hi(ctx->kAd[0]),
+                                                           pair_lo(ctx->kAd[0], n), part(ctx, 5), ctx->stream);
+                         }, &slot_ms)))
+                        return rc;
+                    L0.outer_slot = slot_ms < row_ms;
+                }
+                L0.Ahat_hi.v.lanes = gd;
+            }
+            if (o.gs_layout == FHG_GS_AUTO) {
+                std::lock_guard<std::mutex> lock(g_tune_mutex);
+                g_outer_cache[okey] = OuterChoice{L0.outer_lanes, L0.ahat_lo ? L0.Ahat_hi.v.lanes : 0, L0.outer_slot};
+            }
         }
     }
     // the coarse sub-cycle: one cluster launch or launch by launch (timed when autotuning)
