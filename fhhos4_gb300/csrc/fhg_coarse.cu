@@ -12,8 +12,9 @@
 // the same path through the cycle.
 //
 // A block row is walked by a group of `lanes` threads (block p of the row by lane p mod lanes,
-// partial sums added by shuffles), so that the loads of a row's blocks are in flight together: one
-// thread per row waits for them one after another. The cycle runs as a loop over levels with a
+// partial sums added by shuffles), and each group keeps up to four rows in flight (all their loads
+// issued before the sums), so that loads overlap: one thread per row waits for them one after another,
+// and a phase of a few rows per thread is a chain of memory round trips. The cycle runs as a loop over levels with a
 // count of coarse corrections per level (no device recursion, so the stack is fixed at compile time).
 //
 // The arithmetic is the multigrid cycle of Multigrid::MultigridCycle (src/Solver/Multigrid/
@@ -84,32 +85,78 @@ __device__ __forceinline__ void row_passes(const Ctx<T>& C, long long r0, long l
     }
 }
 
-// acc = sum over the blocks of row i (the diagonal block left out when skip_diag) of A_ij x_j, walked
-// by the g lanes of a group and summed over them: every lane ends with the row's whole sum.
-template <class T, int BS>
-__device__ __forceinline__ void row_product(long long i, bool valid, int lane, int g, const int* __restrict__ rowptr,
-                                            const int* __restrict__ colidx, const T* __restrict__ vals, long long ld,
-                                            const T* x, bool skip_diag, T* acc)
+// Rows [r0, r1) of a phase with `g` lanes per row and R rows per group in flight: in each pass a group
+// takes R rows, loads the row bounds of all R, then each step loads one block of every row (column
+// index, the x entries it names, the values) before any sum, so the loads of R rows overlap instead of
+// following one another. A row is summed block by block in each lane's order (blocks lane, lane + g,
+// ...), then over the lanes by shuffles. emit(i, lane, acc) runs for every valid row after the sums.
+template <class T, int BS, int R, class Emit>
+__device__ __forceinline__ void rows_multi(const Ctx<T>& C, long long r0, long long r1, int g,
+                                           const int* __restrict__ rowptr, const int* __restrict__ colidx,
+                                           const T* __restrict__ vals, long long ld, const T* x, bool skip_diag,
+                                           Emit emit)
 {
+    const long long gid = C.t / g, ngroups = C.nthr / g;
+    const int lane = (int)(C.t % g);
+    const long long span = ngroups * R;
+    const long long passes = (r1 - r0 + span - 1) / span;
+    for (long long ps = 0; ps < passes; ps++) {
+        int i[R];   // rows and columns fit in 32 bits (at most kFusedMaxRows block rows)
+        int p0[R], p1[R];
 #pragma unroll
-    for (int r = 0; r < BS; r++) acc[r] = T(0);
-    if (valid) {
-        const int p1 = rowptr[i + 1];
-        for (int p = rowptr[i] + lane; p < p1; p += g) {
-            const long long j = colidx[p];
-            if (skip_diag && j == i) continue;
-            T xv[BS];
-#pragma unroll
-            for (int c = 0; c < BS; c++) xv[c] = x[j * BS + c];
-#pragma unroll
-            for (int r = 0; r < BS; r++)
-#pragma unroll
-                for (int c = 0; c < BS; c++) acc[r] = fma(vals[(long long)(r * BS + c) * ld + p], xv[c], acc[r]);
+        for (int q = 0; q < R; q++) {
+            const long long iq = r0 + ps * span + (long long)q * ngroups + gid;
+            i[q] = (int)iq;
+            const bool v = iq < r1;
+            p0[q] = v ? rowptr[i[q]] : 0;
+            p1[q] = v ? rowptr[i[q] + 1] : 0;
         }
-    }
+        T acc[R][BS];
 #pragma unroll
-    for (int r = 0; r < BS; r++) acc[r] = lanes_sum(acc[r], g);
+        for (int q = 0; q < R; q++)
+#pragma unroll
+            for (int r = 0; r < BS; r++) acc[q][r] = T(0);
+        for (int base = lane;; base += g) {
+            bool ok[R], any = false;
+            int col[R];
+#pragma unroll
+            for (int q = 0; q < R; q++) {
+                ok[q] = p0[q] + base < p1[q];
+                any |= ok[q];
+                col[q] = ok[q] ? colidx[p0[q] + base] : 0;
+            }
+            if (!any) break;   // per lane; no shuffle inside the loop
+            T xv[R][BS], av[R][BS * BS];
+#pragma unroll
+            for (int q = 0; q < R; q++) {
+#pragma unroll
+                for (int c = 0; c < BS; c++) xv[q][c] = ok[q] ? x[(long long)col[q] * BS + c] : T(0);
+#pragma unroll
+                for (int e = 0; e < BS * BS; e++) av[q][e] = ok[q] ? vals[(long long)e * ld + p0[q] + base] : T(0);
+            }
+#pragma unroll
+            for (int q = 0; q < R; q++) {
+                if (!ok[q] || (skip_diag && col[q] == i[q])) continue;
+#pragma unroll
+                for (int r = 0; r < BS; r++)
+#pragma unroll
+                    for (int c = 0; c < BS; c++) acc[q][r] = fma(av[q][r * BS + c], xv[q][c], acc[q][r]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < R; q++)
+#pragma unroll
+            for (int r = 0; r < BS; r++) acc[q][r] = lanes_sum(acc[q][r], g);
+#pragma unroll
+        for (int q = 0; q < R; q++)
+            if (i[q] < r1) emit((long long)i[q], lane, acc[q]);
+    }
 }
+
+// Rows in flight per lane group, by the bytes of a block: what fits in 128 registers without spills.
+template <class T, int BS>
+constexpr int kRowsInFlight = BS * BS * (int)sizeof(T) <= 16 ? 4 : BS * BS * (int)sizeof(T) <= 36 ? 3
+                              : BS * BS * (int)sizeof(T) <= 72 ? 2 : 1;
 
 // One colour [c0, c1) of a block GS / SOR sweep on level L: x_i <- D_i^-1 (b_i - sum_{j != i} A_ij x_j),
 // relaxed by omega; output r of a row written by lane r (lanes loop when BS > lanes).
@@ -117,10 +164,8 @@ template <class T, int BS>
 __device__ void gs_colour(const Ctx<T>& C, const FusedLevel<T>& L, int c0, int c1)
 {
     const T w = C.P.omega;
-    row_passes(C, c0, c1, L.lanes, [&](long long i, bool valid, int lane) {
-        T acc[BS];
-        row_product<T, BS>(i, valid, lane, L.lanes, L.a_rowptr, L.a_colidx, L.a_vals, L.a_ld, L.x, true, acc);
-        if (!valid) return;
+    rows_multi<T, BS, kRowsInFlight<T, BS>>(C, c0, c1, L.lanes, L.a_rowptr, L.a_colidx, L.a_vals, L.a_ld, L.x, true,
+                                            [&](long long i, int lane, const T* acc) {
         for (int r = lane; r < BS; r += L.lanes) {
             T v = T(0);
 #pragma unroll
@@ -158,10 +203,8 @@ __device__ void smooth(const Ctx<T>& C, const FusedLevel<T>& L, int code, int it
 template <class T, int BS>
 __device__ void residual(const Ctx<T>& C, const FusedLevel<T>& L)
 {
-    row_passes(C, 0, L.nb, L.lanes, [&](long long i, bool valid, int lane) {
-        T acc[BS];
-        row_product<T, BS>(i, valid, lane, L.lanes, L.a_rowptr, L.a_colidx, L.a_vals, L.a_ld, L.x, false, acc);
-        if (!valid) return;
+    rows_multi<T, BS, kRowsInFlight<T, BS>>(C, 0, L.nb, L.lanes, L.a_rowptr, L.a_colidx, L.a_vals, L.a_ld, L.x, false,
+                                            [&](long long i, int lane, const T* acc) {
         for (int r = lane; r < BS; r += L.lanes) L.r[i * BS + r] = L.b[i * BS + r] - acc[r];
     });
     cluster_sync();
@@ -172,10 +215,8 @@ template <class T, int BS>
 __device__ void product(const Ctx<T>& C, int rows, int g, const int* rowptr, const int* colidx, const T* vals,
                         long long ld, const T* in, T* out, bool add)
 {
-    row_passes(C, 0, rows, g, [&](long long i, bool valid, int lane) {
-        T acc[BS];
-        row_product<T, BS>(i, valid, lane, g, rowptr, colidx, vals, ld, in, false, acc);
-        if (!valid) return;
+    rows_multi<T, BS, kRowsInFlight<T, BS>>(C, 0, rows, g, rowptr, colidx, vals, ld, in, false,
+                                            [&](long long i, int lane, const T* acc) {
         for (int r = lane; r < BS; r += g) out[i * BS + r] = add ? out[i * BS + r] + acc[r] : fin(acc[r]);
     });
     cluster_sync();
