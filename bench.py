@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
                     help="only the headline (config 2): skip configs 3 and 5 and the 512-problem batch (config 4)")
+    ap.add_argument("--extra", default="",
+                    help="only these extra configurations (comma-separated keys, e.g. config5); no batch unless --batch")
     ap.add_argument("--cpu-sample-iterations", type=int, default=2)
     return ap.parse_args()
 
@@ -592,11 +594,13 @@ def run_ours(args, dist: Dist):
     ctx.close()
     log(f"config 2 done: headline {value * 1e3:.2f} ms")
     if not args.no_extra:
-        for name in EXTRA_CONFIGS:
+        only = [n for n in args.extra.split(",") if n] if args.extra else list(EXTRA_CONFIGS)
+        for name in only:
             t = time.perf_counter()
             line[name] = run_extra(args, dist, name)
             log(f"{name} done in {time.perf_counter() - t:.1f} s")
-        args.batch = args.batch or 512
+        if not args.extra:
+            args.batch = args.batch or 512
     if args.batch > 0:
         line["config4_batched"] = run_batched(args, dist)
     if dist.rank == 0:
