@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
                     help="only the headline (config 2): skip configs 3 and 5 and the 512-problem batch (config 4)")
+    ap.add_argument("--batch-precisions", default="fp32",
+                    help="V-cycle precisions of the batched workload (fp32, df; each sets up all problems again)")
     ap.add_argument("--extra", default="",
                     help="only these extra configurations (comma-separated keys, e.g. config5); no batch unless --batch")
     ap.add_argument("--cpu-sample-iterations", type=int, default=2)
@@ -609,8 +611,9 @@ def run_ours(args, dist: Dist):
 
 def run_batched(args, dist: Dist):
     """Config 4: many 2D problems of uneven size in one graph launch against the same problems solved
-    one after another (fhg_solve_device each), with the FP32 and the FP64-class (pair) V-cycles; the
-    contexts of one precision at a time (every problem's operators and views take device memory)."""
+    one after another (fhg_solve_device each), in the V-cycle precisions of --batch-precisions (FP32
+    by default; df adds the FP64-class pair V-cycle, another full setup); the contexts of one
+    precision at a time (every problem's operators and views take device memory)."""
     import torch
     from fhhos4_gb300 import batch as BT
     specs = BT.batched_specs(args.batch)
@@ -624,7 +627,7 @@ def run_batched(args, dist: Dist):
            "host_generation_s": round(time.perf_counter() - t0, 1)}
     log(f"config 4: {len(specs)} problems generated in {out['host_generation_s']} s")
     from fhhos4_gb300 import _native as N
-    for prec in ("fp32", "df"):
+    for prec in [q for q in args.batch_precisions.split(",") if q]:
         t1 = time.perf_counter()
         try:
             probs, batch, build_s = BT.build(specs, device=dist.local_rank, precision=prec, autotune=True, generated=gen)
