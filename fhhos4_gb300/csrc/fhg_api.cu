@@ -109,8 +109,8 @@ struct Level {
 
 }  // namespace
 
-// First iteration at which the learned step's residual reduction is compared with the plain method's.
-constexpr int kFallbackStart = 4;
+// Iterations over which the learned step's residual reduction is compared with the plain method's.
+constexpr int kFallbackWindow = 4;
 
 struct fhg_ctx {
     int device = 0;
@@ -155,7 +155,6 @@ struct fhg_ctx {
     int learned_mode = FHG_LEARNED_OFF;
     bool learned_now = false;          // the cycle being launched or captured applies the step
     double rho_plain = 0.0;            // calibrated per-iteration reduction of the plain method
-    std::vector<double> plain_cum;     // its mean reduction per iteration over the first k iterations, [k]
     cudaGraphExec_t graph_l[2] = {nullptr, nullptr};
     long long graph_l_kernels[2] = {0, 0};
     int graphs_l_built = 0;
@@ -1929,7 +1928,6 @@ void free_all(fhg_ctx* ctx)
     ctx->learned_mode = FHG_LEARNED_OFF;
     ctx->learned_now = false;
     ctx->rho_plain = 0.0;
-    ctx->plain_cum.clear();
     for (void* p : ctx->allocations) cudaFree(p);
     ctx->allocations.clear();
     ctx->allocation_bytes.clear();
@@ -2020,16 +2018,14 @@ int run_solve(fhg_ctx* ctx, double* history, fhg_solve_info* info)
             if (learned) learned_its++;
             if (std::isinf(nr)) { status = fail(ctx, FHG_ERR_DIVERGED, "divergence of the solver"); break; }
             if (std::isnan(nr)) { status = fail(ctx, FHG_ERR_NAN, "the residual is NaN."); break; }
-            // Fallback rule: from the fourth iteration on, when the residual reduction per iteration so
-            // far ((r_k / r_0)^(1/k)) falls behind the plain method's over its first k iterations
-            // (calibrated; its last value beyond them), the remaining iterations use the plain
-            // V-cycle. Comparing like with like over the same iterations keeps FCG's irregular first
-            // iterations, which both methods share, from deciding alone.
-            if (learned && ctx->learned_mode == FHG_LEARNED_FALLBACK && it >= kFallbackStart &&
-                ctx->plain_cum.size() > 1 && hist[0] > 0.0) {
-                const double ref = ctx->plain_cum[std::min<size_t>(it, ctx->plain_cum.size() - 1)];
-                const double rho = std::pow(hist[it] / hist[0], 1.0 / it);
-                if (!(rho <= ref)) learned = false;
+            // Fallback rule: from the sixth iteration on, when the per-iteration residual reduction
+            // (the geometric mean over the last four iterations, which evens out FCG's irregular
+            // first iterations and its alternation) falls behind the plain method's calibrated
+            // per-iteration reduction, the remaining iterations use the plain V-cycle.
+            if (learned && ctx->learned_mode == FHG_LEARNED_FALLBACK && it >= kFallbackWindow + 2 &&
+                ctx->rho_plain > 0.0) {
+                const double rho = std::pow(hist[it] / hist[it - kFallbackWindow], 1.0 / kFallbackWindow);
+                if (!(rho <= ctx->rho_plain)) learned = false;
             }
         }
         if (learned_its > 0 && status == FHG_OK) status = check_learned_status(ctx);
@@ -2116,8 +2112,6 @@ int calibrate_plain(fhg_ctx* ctx)
     if (rc) return rc;
     const int k1 = std::min(info.iterations, K);
     ctx->rho_plain = k1 >= 4 && hist[2] > 0 ? std::pow(hist[k1] / hist[2], 1.0 / (k1 - 2)) : 0.0;
-    ctx->plain_cum.assign(1, 0.0);
-    for (int k = 1; k <= k1 && hist[0] > 0.0; k++) ctx->plain_cum.push_back(std::pow(hist[k] / hist[0], 1.0 / k));
     return FHG_OK;
 }
 
@@ -2871,7 +2865,6 @@ int fhg_set_cycle(fhg_ctx* ctx, int pre_smoother, int post_smoother, int pre_ite
     free_graphs(ctx);
     ctx->epoch++;          // batched graphs that captured the old cycle are rebuilt
     ctx->rho_plain = 0.0;  // the plain method's reduction is measured again for the new cycle
-    ctx->plain_cum.clear();
     ctx->opts.pre_smoother = pre_smoother;
     ctx->opts.post_smoother = post_smoother;
     ctx->opts.pre_iterations = pre_iterations;
@@ -2889,7 +2882,6 @@ int fhg_set_coarse_smoothing(fhg_ctx* ctx, int pre_iterations, int post_iteratio
         free_graphs(ctx);
         ctx->epoch++;
         ctx->rho_plain = 0.0;
-        ctx->plain_cum.clear();
         ctx->opts.coarse_pre_iterations = pre_iterations;
         ctx->opts.coarse_post_iterations = post_iterations;
         return refresh_fused(ctx);
@@ -2911,7 +2903,6 @@ int fhg_set_vcycle_precision(fhg_ctx* ctx, int precision)
         free_graphs(ctx);
         ctx->epoch++;
         ctx->rho_plain = 0.0;
-        ctx->plain_cum.clear();
         ctx->opts.vcycle_precision = precision;
     }
     return FHG_OK;
@@ -3025,7 +3016,6 @@ int fhg_set_learned(fhg_ctx* ctx, const float* params, int n_params, int mode)
     }
     ctx->learned_mode = mode;
     ctx->rho_plain = 0.0;
-    ctx->plain_cum.clear();
     ctx->epoch++;
     return FHG_OK;
 }

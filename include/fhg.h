@@ -286,11 +286,11 @@ int fhg_set_face_tensors(fhg_ctx* ctx, int n_blocks, const double* tensors);
 
 /* Install a network (params: FHG_LEARNED_PARAMS floats, host; NULL keeps the installed one) and
  * select the mode. Needs a setup with FHG_PREC_FP32, two levels or more and block size 2..4;
- * call after every fhg_setup. FHG_LEARNED_FALLBACK: from the fourth iteration k of a solve on,
- * when the residual reduction per iteration so far, (r_k / r_0)^(1/k), falls behind the plain
- * method's over its own first k iterations (calibrated once per cycle configuration on a seeded
- * random right-hand side, before the first solve's timed region; its last value for larger k), the
- * remaining iterations use the plain V-cycle. */
+ * call after every fhg_setup. FHG_LEARNED_FALLBACK: from the sixth iteration of a solve on,
+ * when the geometric mean rho of the last four residual reductions falls behind the plain
+ * method's per-iteration reduction rho_p (rho > rho_p; rho_p measured once per cycle configuration
+ * on a seeded random right-hand side, before the first solve's timed region), the remaining
+ * iterations use the plain V-cycle. */
 int fhg_set_learned(fhg_ctx* ctx, const float* params, int n_params, int mode);
 
 /* The plain method's calibrated per-iteration reduction (over its iterations 2 to 12). */

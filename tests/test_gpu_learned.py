@@ -247,7 +247,7 @@ def test_fallback_to_plain_cycle():
         rc, x, h, info = _solve(f, "fallback", bad)
         assert rc == 0 and h[-1] < 1e-8
         assert info.learned_iterations < info.iterations
-        assert info.learned_iterations <= 6   # the rule compares from the fourth iteration on
+        assert info.learned_iterations <= 7   # the rule looks back four iterations from the sixth
         rho = f.ctx.learned_reference_rate()
         assert 0.0 < rho < 1.0
     finally:
