@@ -65,11 +65,11 @@ def parse():
                     help="also run the batched workload: this many 2D problems in one graph launch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
-                    help="only the headline (config 2): skip configs 3 and 5 and the 512-problem batch (config 4)")
+                    help="only the headline (tet 64^3, k = 1): skip the other workloads and the 512-problem batch")
     ap.add_argument("--batch-precisions", default="fp32",
                     help="V-cycle precisions of the batched workload (fp32, df; each sets up all problems again)")
     ap.add_argument("--extra", default="",
-                    help="only these extra configurations (comma-separated keys, e.g. config5); no batch unless --batch")
+                    help="only these extra workloads (comma-separated keys, e.g. tet32_k1_anisotropic); no batch unless --batch")
     ap.add_argument("--cpu-sample-iterations", type=int, default=2)
     return ap.parse_args()
 
@@ -594,7 +594,7 @@ def run_ours(args, dist: Dist):
         "cpu_baseline": cpu,
     }
     ctx.close()
-    log(f"config 2 done: headline {value * 1e3:.2f} ms")
+    log(f"headline (tet 64^3, k = 1) done: {value * 1e3:.2f} ms")
     if not args.no_extra:
         only = [n for n in args.extra.split(",") if n] if args.extra else list(EXTRA_CONFIGS)
         for name in only:
@@ -604,13 +604,13 @@ def run_ours(args, dist: Dist):
         if not args.extra:
             args.batch = args.batch or 512
     if args.batch > 0:
-        line["config4_batched"] = run_batched(args, dist)
+        line["batched_2d_uneven"] = run_batched(args, dist)
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
 
 
 def run_batched(args, dist: Dist):
-    """Config 4: many 2D problems of uneven size in one graph launch against the same problems solved
+    """Many 2D problems of uneven size in one graph launch against the same problems solved
     one after another (fhg_solve_device each), in the V-cycle precisions of --batch-precisions (FP32
     by default; df adds the FP64-class pair V-cycle, another full setup); the contexts of one
     precision at a time (every problem's operators and views take device memory)."""
@@ -625,7 +625,7 @@ def run_batched(args, dist: Dist):
            "method": ("V(1,1) bgs/rbgs inside FP64 FCG(1), Galerkin coarse operators, autotuned launch shapes; "
                       "residual replacement in the device loop in both precisions (compensated true residual)"),
            "host_generation_s": round(time.perf_counter() - t0, 1)}
-    log(f"config 4: {len(specs)} problems generated in {out['host_generation_s']} s")
+    log(f"batched: {len(specs)} problems generated in {out['host_generation_s']} s")
     from fhhos4_gb300 import _native as N
     for prec in [q for q in args.batch_precisions.split(",") if q]:
         t1 = time.perf_counter()
@@ -633,7 +633,7 @@ def run_batched(args, dist: Dist):
             probs, batch, build_s = BT.build(specs, device=dist.local_rank, precision=prec, autotune=True, generated=gen)
         except N.FhgError as e:   # reported, not fatal: the other precision and the rest of the line go on
             out[prec] = {"error": str(e)}
-            log(f"config 4 {prec}: setup failed: {e}")
+            log(f"batched {prec}: setup failed: {e}")
             torch.cuda.empty_cache()
             continue
         setup_s = time.perf_counter() - t1
@@ -663,7 +663,7 @@ def run_batched(args, dist: Dist):
                      "problems_true_below_tol": sum(1 for t in trues if t < 1e-8), "status": rc,
                      "setup_s": round(setup_s, 1), "device_gb": round(device_gb, 1),
                      "timing": f"median of {max(3, args.steps // 2)} launches after 2 untimed ones"}
-        log(f"config 4 {prec}: setup {setup_s:.1f} s ({device_gb:.1f} GB), batched {batched_ms:.1f} ms, "
+        log(f"batched {prec}: setup {setup_s:.1f} s ({device_gb:.1f} GB), batched {batched_ms:.1f} ms, "
             f"sequential {seq_ms:.1f} ms")
         batch.close()
         for p in probs:
@@ -673,20 +673,20 @@ def run_batched(args, dist: Dist):
     return out
 
 
-# The other configurations, measured in the same run beside the headline (config 2). Each is a
+# The other workloads, measured in the same run beside the headline (tet 64^3, k = 1). Each is a
 # namespace of bench options and the methods it compares; every solve is judged by its true residual.
 EXTRA_CONFIGS = {
-    # Config 3: 48^3 tetrahedra, k = 2, 4x4x4 checkerboard 1 / 1e6, f = 1, Galerkin coarse operators,
+    # 48^3 tetrahedra, k = 2, 4x4x4 checkerboard 1 / 1e6, f = 1, Galerkin coarse operators,
     # residual replacement in every precision (compensated true residual where FP64 misses 1e-8).
-    "config3": dict(dim=3, n=48, k=2, coefficient="checkerboard", contrast=1e6, source="one", max_coarse_rows=2000,
+    "tet48_k2_checkerboard_1e6": dict(dim=3, n=48, k=2, coefficient="checkerboard", contrast=1e6, source="one", max_coarse_rows=2000,
                     galerkin=True, replace_residual=True,
                     methods={"plain_fp64": ("df", "bgs", "rbgs", 1, 1, (-1, -1), False),
                              "fp64_v22": ("df", "bgs", "rbgs", 2, 2, (-1, -1), False),
                              "fp32_v22": ("fp32", "bgs", "rbgs", 2, 2, (-1, -1), False)}),
-    # Config 5: 32^3 tetrahedra, k = 1, diag(1, 1, eps) rotated per 4^3-cube block, eps log-uniform in
+    # 32^3 tetrahedra, k = 1, diag(1, 1, eps) rotated per 4^3-cube block, eps log-uniform in
     # [1e-3, 1], a field seed the network never saw; plain, FP32 fast cycle, and the learned step (with the
     # fallback rule, and on every iteration).
-    "config5": dict(dim=3, n=32, k=1, coefficient="anisotropic", contrast=1.0, source="one", max_coarse_rows=1000,
+    "tet32_k1_anisotropic": dict(dim=3, n=32, k=1, coefficient="anisotropic", contrast=1.0, source="one", max_coarse_rows=1000,
                     galerkin=False, replace_residual=False, seed=987654321,
                     methods={"plain_fp64": ("df", "bgs", "rbgs", 1, 1, (-1, -1), False),
                              "fp32_fast": ("fp32", "bgs", "rbgs", 3, 3, (4, 4), False),
@@ -696,14 +696,14 @@ EXTRA_CONFIGS = {
                              "learned_v22": ("fp32", "bgs", "rbgs", 2, 2, (-1, -1), True)}),
     # The same field with Galerkin coarse operators (the reference's -g 1): rediscretised coarse
     # operators of the rotated anisotropic field make the V-cycle a weak preconditioner.
-    "config5_galerkin": dict(dim=3, n=32, k=1, coefficient="anisotropic", contrast=1.0, source="one",
+    "tet32_k1_anisotropic_galerkin": dict(dim=3, n=32, k=1, coefficient="anisotropic", contrast=1.0, source="one",
                              max_coarse_rows=1000, galerkin=True, replace_residual=False, seed=987654321,
                              methods={"plain_fp64": ("df", "bgs", "rbgs", 1, 1, (-1, -1), False),
                                       "fp32_fast": ("fp32", "bgs", "rbgs", 3, 3, (4, 4), False),
                                       "learned_fast": ("fp32", "bgs", "rbgs", 3, 3, (4, 4), True),
                                       "learned_fast_always": ("fp32", "bgs", "rbgs", 3, 3, (4, 4), "always")}),
 }
-CONFIG5_WEIGHTS = "learned_tet3d_k1_config5.npz"
+ANISO_WEIGHTS = "learned_tet3d_k1_aniso.npz"   # trained on fields of that anisotropic distribution
 
 
 def run_extra(args, dist: Dist, name: str):
@@ -739,7 +739,7 @@ def run_extra(args, dist: Dist, name: str):
     setup_s = time.perf_counter() - t0
     params = wmeta = None
     if any(m[-1] for m in methods.values()):
-        path = os.path.join(LN.WEIGHTS_DIR, CONFIG5_WEIGHTS)
+        path = os.path.join(LN.WEIGHTS_DIR, ANISO_WEIGHTS)
         params, wmeta = LN.load_params(path if os.path.exists(path) else LN.DEFAULT_WEIGHTS)
     b_dev = torch.from_numpy(b).to(f"cuda:{dev}")
     x_dev = torch.empty_like(b_dev)
@@ -763,13 +763,13 @@ def run_extra(args, dist: Dist, name: str):
             out["learned_vs_fast_v22"] = round(results["fp32_v22"]["s"] / results["learned_v22"]["s"], 3)
         out["speedup_learned_vs_plain_fp64"] = round(results["plain_fp64"]["s"] / results["learned_fast"]["s"], 3)
         if not a.galerkin:
-            out["energy_ratio_one_cycle"] = config5_energy_ratios(a, dev, params)
+            out["energy_ratio_one_cycle"] = aniso_energy_ratios(a, dev, params)
     return out
 
 
-def config5_energy_ratios(a, dev, params, samples: int = 4):
+def aniso_energy_ratios(a, dev, params, samples: int = 4):
     """|e1|_A^2 / |e|_A^2 after one V(2,2) cycle, plain and with the learned step, for seeded errors
-    left by one plain cycle on the config-5 field (mean over `samples`)."""
+    left by one plain cycle on the anisotropic 32^3 field (mean over `samples`)."""
     from fhhos4_gb300 import learned as LN
     f = LN.Field(LN.FieldSpec(n=a.n, seed=a.seed), device=dev, nu=(2, 2))
     try:

@@ -1,7 +1,7 @@
 // Compile-and-link check of include/fhg_reference_adapter.hpp against the reference headers
 // (TEST INFRASTRUCTURE). `adapter_check --map` needs no GPU: it prints the fhg_options the adapter
 // derives from several ProgramArguments settings. Without arguments (GPU needed) it solves the
-// reference's 2D config-1 problem through the adapter and prints the iterations.
+// reference's 2D problem on a 32 x 32 triangle mesh (k = 1) through the adapter and prints the iterations.
 #include "ProgramArguments.h"
 #include "Discretizations/DG/Diffusion_DG.h"
 #include "TestCases/Diffusion/DiffTestCaseFactory.h"

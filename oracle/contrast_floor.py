@@ -12,7 +12,7 @@ growing n it reports, with every residual evaluated in extended precision (numpy
   recursive residual at 1e-8, IterativeSolver.h:224-247), and the FP64 evaluation of that residual;
 * ratio: || |A| |fl64(x*)| || / ||b||, which scales the FP64 rounding of x into the residual.
 
-Usage: python oracle/config3_floor.py [n ...]   (default 8 12 16 20)
+Usage: python oracle/contrast_floor.py [n ...]   (default 8 12 16 20)
 """
 from __future__ import annotations
 
