@@ -9,10 +9,14 @@ multigrid V(1,1) cycle with block Gauss-Seidel (bgs/rbgs), coarsest direct solve
 reference's discretisation, validated against it) and uploaded once.
 
 One step = one complete solve to 1e-8 with b resident in HBM. `value` = seconds per solve of
-the fastest method that reaches 1e-8 FP64 relative residual (FP32 V-cycle inside FP64 FCG);
-the plain FP64 GPU solve (the reference's method, same iteration count) is reported beside it.
-`e2e` = the same solve through the C ABI with host buffers (H2D of b, D2H of x inside the
-timed region).
+the learned step + FP32 V-cycle inside the FP64-class FCG; the plain method (the reference's
+V(1,1), same iteration count) is reported beside it in FP32-pair (FP64-class) and native FP64
+arithmetic. `e2e` = the same solve through the C ABI with host buffers (H2D of b, D2H of x inside
+the timed region). Beside the headline, in the same line: the 48^3 k = 2 checkerboard (contrast
+1e6) workload, the 32^3 rotated-anisotropic workload (plain, FP32 and learned, with rediscretised
+and Galerkin coarse operators), the 512-problem batched workload (2D, uneven sizes, one graph
+launch), the GPU condensation and post-processing of the headline system; `--no-extra` and
+`--extra` select.
 
 --impl reference times the reference's CPU algorithm (the oracle restatement, natural block-GS
 order, OpenMP row-parallel products) on the host cores, one step = one FCG iteration, scaled
