@@ -1194,6 +1194,21 @@ bool fused_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
             F.r_rowptr = Rv.rowptr; F.r_colidx = Rv.colidx; F.r_vals = Rv.vals; F.r_ld = Rv.ld;
             F.lanes = fused_lanes(A);
             F.t_lanes = fused_lanes(Rv);
+            const BsrView<T>* G = nullptr;
+            const BsrView<T>* Ap = nullptr;
+            if constexpr (std::is_same<T, float>::value) {
+                if (L.G32.vals) G = &L.G32.v;
+                if (L.A32p.vals) Ap = &L.A32p.v;
+            } else {
+                if (L.G2.vals) G = &L.G2.v;
+                if (L.A2p.vals) Ap = &L.A2p.v;
+            }
+            if (G && G->ell > 0 && G->ell <= F.lanes) {
+                F.g_ell = G->ell; F.g_colidx = G->colidx; F.g_vals = G->vals; F.g_ld = G->ld;
+            }
+            if (Ap && Ap->ell > 0 && Ap->ell <= F.lanes) {
+                F.ap_ell = Ap->ell; F.ap_colidx = Ap->colidx; F.ap_vals = Ap->vals; F.ap_ld = Ap->ld;
+            }
         }
         if (fhg::launch_fused_cycle<T>(P, L0.bs, ctx->fused_ctas[V::kPrec], ctx->stream) != cudaSuccess) return false;
         fhg::g_kernel_launches++;
@@ -1321,13 +1336,15 @@ void release_unused_views(fhg_ctx* ctx)
 {
     for (int l = 0; l + 1 < ctx->nlevels; l++) {
         Level& L = ctx->levels[l];
-        if (L.G32s.vals && L.gs_slot[FHG_PREC_FP32]) release_bsr(ctx, L.G32);
+        // levels >= 1 keep their padded-row views: the one-launch coarse sub-cycle reads them
+        const bool keep_padded = l > 0;
+        if (L.G32s.vals && L.gs_slot[FHG_PREC_FP32]) { if (!keep_padded) release_bsr(ctx, L.G32); }
         else if (L.G32s.vals) release_bsr(ctx, L.G32s);
-        if (L.A32s.vals && L.prod_slot[FHG_PREC_FP32]) release_bsr(ctx, L.A32p);
+        if (L.A32s.vals && L.prod_slot[FHG_PREC_FP32]) { if (!keep_padded) release_bsr(ctx, L.A32p); }
         else if (L.A32s.vals) release_bsr(ctx, L.A32s);
-        if (L.G2s.vals && L.gs_slot[FHG_PREC_DF]) release_bsr(ctx, L.G2);
+        if (L.G2s.vals && L.gs_slot[FHG_PREC_DF]) { if (!keep_padded) release_bsr(ctx, L.G2); }
         else if (L.G2s.vals) release_bsr(ctx, L.G2s);
-        if (L.A2s.vals && L.prod_slot[FHG_PREC_DF]) release_bsr(ctx, L.A2p);
+        if (L.A2s.vals && L.prod_slot[FHG_PREC_DF]) { if (!keep_padded) release_bsr(ctx, L.A2p); }
         else if (L.A2s.vals) release_bsr(ctx, L.A2s);
         if (L.P32j.vals && !L.p_jds[FHG_PREC_FP32]) release_bsr(ctx, L.P32j);
         if (L.R32j.vals && !L.r_jds[FHG_PREC_FP32]) release_bsr(ctx, L.R32j);

@@ -91,7 +91,7 @@ __device__ __forceinline__ void row_passes(const Ctx<T>& C, long long r0, long l
 // following one another. A row is summed block by block in each lane's order (blocks lane, lane + g,
 // ...), then over the lanes by shuffles. emit(i, lane, acc) runs for every valid row after the sums.
 template <class T, int BS, int R, class Emit>
-__device__ __forceinline__ void rows_multi(const Ctx<T>& C, long long r0, long long r1, int g,
+__device__ __forceinline__ void rows_multi(const Ctx<T>& C, long long r0, long long r1, int g, int ell,
                                            const int* __restrict__ rowptr, const int* __restrict__ colidx,
                                            const T* __restrict__ vals, long long ld, const T* x, bool skip_diag,
                                            Emit emit)
@@ -108,8 +108,13 @@ __device__ __forceinline__ void rows_multi(const Ctx<T>& C, long long r0, long l
             const long long iq = r0 + ps * span + (long long)q * ngroups + gid;
             i[q] = (int)iq;
             const bool v = iq < r1;
-            p0[q] = v ? rowptr[i[q]] : 0;
-            p1[q] = v ? rowptr[i[q] + 1] : 0;
+            if (ell > 0) {   // padded rows: no row-pointer round trip
+                p0[q] = v ? i[q] * ell : 0;
+                p1[q] = v ? p0[q] + ell : 0;
+            } else {
+                p0[q] = v ? rowptr[i[q]] : 0;
+                p1[q] = v ? rowptr[i[q] + 1] : 0;
+            }
         }
         T acc[R][BS];
 #pragma unroll
@@ -164,7 +169,9 @@ template <class T, int BS>
 __device__ void gs_colour(const Ctx<T>& C, const FusedLevel<T>& L, int c0, int c1)
 {
     const T w = C.P.omega;
-    rows_multi<T, BS, kRowsInFlight<T, BS>>(C, c0, c1, L.lanes, L.a_rowptr, L.a_colidx, L.a_vals, L.a_ld, L.x, true,
+    const bool pad = L.g_ell > 0;
+    rows_multi<T, BS, kRowsInFlight<T, BS>>(C, c0, c1, L.lanes, L.g_ell, L.a_rowptr, pad ? L.g_colidx : L.a_colidx,
+                                            pad ? L.g_vals : L.a_vals, pad ? L.g_ld : L.a_ld, L.x, true,
                                             [&](long long i, int lane, const T* acc) {
         for (int r = lane; r < BS; r += L.lanes) {
             T v = T(0);
@@ -203,7 +210,9 @@ __device__ void smooth(const Ctx<T>& C, const FusedLevel<T>& L, int code, int it
 template <class T, int BS>
 __device__ void residual(const Ctx<T>& C, const FusedLevel<T>& L)
 {
-    rows_multi<T, BS, kRowsInFlight<T, BS>>(C, 0, L.nb, L.lanes, L.a_rowptr, L.a_colidx, L.a_vals, L.a_ld, L.x, false,
+    const bool pad = L.ap_ell > 0;
+    rows_multi<T, BS, kRowsInFlight<T, BS>>(C, 0, L.nb, L.lanes, L.ap_ell, L.a_rowptr, pad ? L.ap_colidx : L.a_colidx,
+                                            pad ? L.ap_vals : L.a_vals, pad ? L.ap_ld : L.a_ld, L.x, false,
                                             [&](long long i, int lane, const T* acc) {
         for (int r = lane; r < BS; r += L.lanes) L.r[i * BS + r] = L.b[i * BS + r] - acc[r];
     });
@@ -215,7 +224,7 @@ template <class T, int BS>
 __device__ void product(const Ctx<T>& C, int rows, int g, const int* rowptr, const int* colidx, const T* vals,
                         long long ld, const T* in, T* out, bool add)
 {
-    rows_multi<T, BS, kRowsInFlight<T, BS>>(C, 0, rows, g, rowptr, colidx, vals, ld, in, false,
+    rows_multi<T, BS, kRowsInFlight<T, BS>>(C, 0, rows, g, 0, rowptr, colidx, vals, ld, in, false,
                                             [&](long long i, int lane, const T* acc) {
         for (int r = lane; r < BS; r += g) out[i * BS + r] = add ? out[i * BS + r] + acc[r] : fin(acc[r]);
     });

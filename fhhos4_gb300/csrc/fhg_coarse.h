@@ -32,6 +32,16 @@ struct FusedLevel {
     const int* a_colidx = nullptr;
     const T* a_vals = nullptr;
     long long a_ld = 0;
+    // padded-row views when setup built them (row i's `ell` slots at i * ell, no row pointers): the
+    // off-diagonal blocks for the sweeps (empty slots: the row's own column) and all of A for the
+    // residual (empty slots: zero blocks)
+    int g_ell = 0, ap_ell = 0;
+    const int* g_colidx = nullptr;
+    const T* g_vals = nullptr;
+    long long g_ld = 0;
+    const int* ap_colidx = nullptr;
+    const T* ap_vals = nullptr;
+    long long ap_ld = 0;
     const T* dinv = nullptr;
     const int* p_rowptr = nullptr;
     const int* p_colidx = nullptr;
