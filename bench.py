@@ -367,10 +367,28 @@ def gpu_condensation(H, A0, b0, dev):
     finally:
         cond.close()
     same = bool(np.array_equal(A.indptr, A0.indptr) and np.array_equal(A.indices, A0.indices))
-    return {"what": "static condensation (per-class Schur complements) + assembly of A_0 and b on the GPU",
+    # the coarse levels' rediscretised operators the same way
+    coarse_ms, coarse_diff, coarse_same = 0.0, 0.0, True
+    for l in range(1, H.levels):
+        Al = H.A(l).tocsr()
+        c = N.Condense(H.level_tables(l), dev)
+        try:
+            nnz_l, ms_l = c.run()
+            Ag, _ = c.result(nnz_l)
+        finally:
+            c.close()
+        coarse_ms += ms_l
+        ok = bool(np.array_equal(Ag.indptr, Al.indptr) and np.array_equal(Ag.indices, Al.indices))
+        coarse_same &= ok
+        if ok:
+            coarse_diff = max(coarse_diff, float(np.abs(Ag.data - Al.data).max() / np.abs(Al.data).max()))
+    return {"what": "static condensation (per-class Schur complements) + assembly of A_0 and b on the GPU; "
+                    "the coarse levels' rediscretised operators the same way",
             "gpu_ms": round(ms, 3), "same_structure": same,
             "max_rel_diff_A": float(np.abs(A.data - A0.data).max() / np.abs(A0.data).max()) if same else None,
             "max_rel_diff_b": float(np.abs(b - b0).max() / np.abs(b0).max()),
+            "coarse_levels": H.levels - 1, "coarse_gpu_ms": round(coarse_ms, 3), "coarse_same_structure": coarse_same,
+            "coarse_max_rel_diff": coarse_diff if coarse_same else None,
             "element_classes": int(t["n_classes"]), "elements": int(t["n_elements"])}
 
 

@@ -974,6 +974,8 @@ struct Level {
     std::vector<double> bF_e;             // per element, nF nf: condensed RHS contribution (finest level)
     std::vector<double> cell_rhs_e;       // per element, nC: A_TT^{-1} b_T (finest level)
     std::vector<double> bT_e;             // per element, nC: b_T = (f, c_j)_T (finest level)
+    std::vector<double> cls_local;        // per class, the local operator before condensation (kept
+    int cls_nC = 0, cls_nFF = 0;          // when cls_ops is released), its cell and face unknowns
     int n_rows = 0;
     std::vector<int> A_rowptr, A_colidx;
     std::vector<double> A_vals;
@@ -1411,6 +1413,16 @@ int fhg_hho_create(fhg_hho** out, const fhg_hho_params* p)
             return rc;
         }
         assemble(L, prm, threads, l == 0);
+        {   // the local operators by class, for condensing this level elsewhere (fhg_hho_level_tables)
+            const ElementOps& O0 = L.cls_ops[0];
+            L.cls_nC = O0.nC;
+            L.cls_nFF = O0.nF * O0.nf;
+            const size_t nH = (size_t)L.cls_nC + L.cls_nFF;
+            L.cls_local.assign(L.cls_ops.size() * nH * nH, 0.0);
+            for (size_t c = 0; c < L.cls_ops.size(); c++)
+                if (L.cls_ops[c].local.a.size() == nH * nH)
+                    std::copy(L.cls_ops[c].local.a.begin(), L.cls_ops[c].local.a.end(), L.cls_local.begin() + c * nH * nH);
+        }
         if (l > 0) prolongation(H->levels[l - 1], L, prm, rules, threads);
         if (l > 1) {
             // element data of levels above the finest no longer needed (the finest keeps it for
@@ -1609,6 +1621,53 @@ int fhg_hho_condense_tables(const fhg_hho* h, double* local, double* b_cell, int
                 for (int j = 0; j < nH; j++) local[(c * nH + i) * nH + j] = A(i, j);
         }
     if (b_cell) std::copy(L.bT_e.begin(), L.bT_e.end(), b_cell);
+    if (face_elems)
+        for (size_t f = 0; f < M.fv.size(); f++) {
+            const int I = M.number[f];
+            if (I < 0) continue;
+            const int els[2] = {M.fe1[f], M.fe2[f]};
+            for (int side = 0; side < 2; side++) {
+                int lfi = -1;
+                if (els[side] >= 0)
+                    for (int lf = 0; lf < nF; lf++)
+                        if (M.ef[els[side]][lf] == (int)f) lfi = lf;
+                face_elems[(size_t)I * 4 + 2 * side] = els[side];
+                face_elems[(size_t)I * 4 + 2 * side + 1] = lfi;
+            }
+        }
+    return 0;
+}
+
+// Static-condensation inputs of level `level` (every level is rediscretised on its own mesh):
+// sizes, then per element its class and its faces' unknown blocks (-1: Dirichlet), per class the
+// local operator before condensation, per unknown face block its two elements and local faces.
+int fhg_hho_level_sizes(const fhg_hho* h, int level, int* n_elements, int* n_classes, int* n_cell, int* n_face_dofs,
+                        int* n_face_blocks)
+{
+    if (!h || level < 0 || level >= (int)h->levels.size()) return -1;
+    const Level& L = h->levels[level];
+    const size_t nH = (size_t)L.cls_nC + L.cls_nFF;
+    if (nH == 0) return -1;
+    if (n_elements) *n_elements = (int)L.mesh.el.size();
+    if (n_classes) *n_classes = (int)(L.cls_local.size() / (nH * nH));
+    if (n_cell) *n_cell = L.cls_nC;
+    if (n_face_dofs) *n_face_dofs = L.cls_nFF;
+    if (n_face_blocks) *n_face_blocks = L.mesh.n_interior;
+    return 0;
+}
+
+int fhg_hho_level_tables(const fhg_hho* h, int level, int* elem_class, int* elem_faces, double* local, int* face_elems)
+{
+    if (!h || level < 0 || level >= (int)h->levels.size()) return -1;
+    const Level& L = h->levels[level];
+    const Mesh& M = L.mesh;
+    const int nF = M.dim + 1;
+    for (size_t e = 0; e < M.el.size(); e++) {
+        if (elem_class) elem_class[e] = L.cls[e];
+        if (elem_faces)
+            for (int lf = 0; lf < nF; lf++) elem_faces[e * nF + lf] = M.number[M.ef[e][lf]];
+    }
+    if (local) std::copy(L.cls_local.begin(), L.cls_local.end(), local);
     if (face_elems)
         for (size_t f = 0; f < M.fv.size(); f++) {
             const int I = M.number[f];

@@ -63,6 +63,13 @@ int fhg_hho_post_tables(const fhg_hho* h, int* elem_class, int* elem_faces, doub
  * n_face_dofs; the local operator before condensation, cells first), b_cell[ne * n_cell] (b_T),
  * face_elems[n_face_blocks * 4] = (e1, lf1, e2, lf2) per unknown face block, in assembly order. */
 int fhg_hho_condense_tables(const fhg_hho* h, double* local, double* b_cell, int* face_elems);
+/* The same condensation inputs for any level (each level is rediscretised on its own mesh; no source
+ * term): sizes, then elem_class[ne], elem_faces[ne * (dim + 1)], local[n_classes * nH * nH],
+ * face_elems[n_face_blocks * 4]; null arrays are skipped. */
+int fhg_hho_level_sizes(const fhg_hho* h, int level, int* n_elements, int* n_classes, int* n_cell,
+                        int* n_face_dofs, int* n_face_blocks);
+int fhg_hho_level_tables(const fhg_hho* h, int level, int* elem_class, int* elem_faces, double* local,
+                         int* face_elems);
 /* Diffusion tensors of the two elements of every unknown face of level `level` (both exist: the
  * unknowns are the interior faces): out[12*u .. 12*u+11] for face block u, element 1 then
  * element 2 (the face's own element order), each as (xx, yy, zz, xy, xz, yz) in 3D and

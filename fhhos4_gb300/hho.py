@@ -52,6 +52,8 @@ def lib():
         L.fhg_hho_post_sizes.argtypes = [C.c_void_p] + [P(C.c_int)] * 6
         L.fhg_hho_post_tables.argtypes = [C.c_void_p] + [C.c_void_p] * 9
         L.fhg_hho_condense_tables.argtypes = [C.c_void_p] + [C.c_void_p] * 3
+        L.fhg_hho_level_sizes.argtypes = [C.c_void_p, C.c_int] + [P(C.c_int)] * 5
+        L.fhg_hho_level_tables.argtypes = [C.c_void_p, C.c_int] + [C.c_void_p] * 4
         _lib = L
     return _lib
 
@@ -161,6 +163,21 @@ class Hierarchy:
         if lib().fhg_hho_condense_tables(self.h, C.c_void_p(t["local"].ctypes.data), C.c_void_p(t["b_cell"].ctypes.data),
                                          C.c_void_p(t["face_elems"].ctypes.data)) != 0:
             raise RuntimeError("condense_tables failed")
+        return t
+
+    def level_tables(self, l: int) -> dict:
+        """Condensation inputs of level l (fhg_cond_create takes them; no source term, b_cell = 0)."""
+        sz = [C.c_int() for _ in range(5)]
+        if lib().fhg_hho_level_sizes(self.h, l, *[C.byref(v) for v in sz]) != 0:
+            raise RuntimeError("level_sizes failed")
+        ne, ncls, nC, nFF, nI = (v.value for v in sz)
+        nH, nF = nC + nFF, self.dim + 1
+        t = dict(dim=self.dim, n_elements=ne, n_classes=ncls, n_cell=nC, n_face_dofs=nFF, n_face_blocks=nI,
+                 elem_class=np.zeros(ne, np.int32), elem_faces=np.zeros(ne * nF, np.int32),
+                 local=np.zeros(ncls * nH * nH), face_elems=np.zeros(nI * 4, np.int32), b_cell=np.zeros(ne * nC))
+        if lib().fhg_hho_level_tables(self.h, l, *[C.c_void_p(t[k].ctypes.data)
+                                                   for k in ("elem_class", "elem_faces", "local", "face_elems")]) != 0:
+            raise RuntimeError("level_tables failed")
         return t
 
     def A_rows(self, l: int) -> int:

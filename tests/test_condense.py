@@ -1,7 +1,8 @@
-"""Static condensation and assembly of the finest face system (Diffusion_HHO.h:627-638): the
-generator's condensation tables condensed in numpy reproduce its assembled A_0 and b (which
-test_generator.py pins against the reference's own), the C ABI validates the tables before any
-device call, and the GPU's condensation and assembly give the same CSR structure and values."""
+"""Static condensation and assembly of the face systems (Diffusion_HHO.h:627-638): the generator's
+condensation tables condensed in numpy reproduce its assembled A_0 and b and every rediscretised
+coarse operator A_l (which test_generator.py pins against the reference's own), the C ABI validates
+the tables before any device call, and the GPU's condensation and assembly give the same CSR
+structure and values on every level."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -59,6 +60,18 @@ def test_tables_reproduce_host_assembly(dim, n, k):
     assert np.abs(b - b0).max() <= 1e-13 * np.abs(b0).max()
 
 
+@pytest.mark.parametrize("dim,n,k", [(3, 8, 1), (2, 16, 2)])
+def test_level_tables_reproduce_every_level(dim, n, k):
+    H = hho.Hierarchy(dim, n, k)
+    try:
+        for l in range(H.levels):
+            A, _ = numpy_condense(H.level_tables(l))
+            Al = H.A(l).tocsr()
+            assert abs(A - Al).max() <= 1e-13 * abs(Al).max(), l
+    finally:
+        H.close()
+
+
 def test_cond_create_validates_tables():
     """Inconsistent tables are refused with FHG_ERR_INVALID_ARG before any device call."""
     from fhhos4_gb300 import _native as N
@@ -102,6 +115,28 @@ def test_gpu_condensation_matches_host_assembly(dim, n, k):
         assert np.array_equal(A2.data, A.data) and np.array_equal(b2, b)
     finally:
         cond.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim,n,k", [(3, 16, 1), (2, 32, 2)])
+def test_gpu_rediscretisation_of_every_level(dim, n, k):
+    """Every level's operator condensed and assembled on the GPU from its element tables: the coarse
+    re-discretisation of LevelForHHO::SetupDiscretizedOperator (LevelForHHO.h:72-103)."""
+    from fhhos4_gb300 import _native as N
+    H = hho.Hierarchy(dim, n, k)
+    try:
+        for l in range(H.levels):
+            Al = H.A(l).tocsr()
+            cond = N.Condense(H.level_tables(l))
+            try:
+                nnz, _ = cond.run()
+                A, _ = cond.result(nnz)
+            finally:
+                cond.close()
+            assert np.array_equal(A.indptr, Al.indptr) and np.array_equal(A.indices, Al.indices), l
+            assert np.abs(A.data - Al.data).max() <= 1e-13 * np.abs(Al.data).max(), l
+    finally:
+        H.close()
 
 
 @pytest.mark.gpu
