@@ -56,3 +56,27 @@ def test_option_codes_match_header():
     assert N.SMOOTHERS == {"bgs": 0, "rbgs": 1, "bj": 2, "bj23": 3, "sbgs": 4, "abgs": 5, "rabgs": 6}
     assert N.KRYLOV == {"fcg": 0, "cg": 1}
     assert N.PRECISION == {"fp64": 0, "fp32": 1, "df": 2}
+
+
+def test_batched_workload_is_seeded_and_in_range():
+    """The batched workload: 2D problems with n a multiple of 16 in [32, 256], k in {1, 2, 3}, the
+    same draw for the same seed."""
+    from fhhos4_gb300 import batch as B
+    a, b = B.batched_specs(64), B.batched_specs(64)
+    assert [(s.n, s.k, s.seed) for s in a] == [(s.n, s.k, s.seed) for s in b]
+    assert all(32 <= s.n <= 256 and s.n % 16 == 0 and s.k in (1, 2, 3) for s in a)
+    assert len({s.seed for s in a}) == len(a)
+
+
+def test_bench_workloads_are_named_for_what_they_are():
+    """Every extra workload of the bench line carries its mesh, degree and coefficient in its key and
+    lists the methods it compares; the workload record of the line names sizes, not an index."""
+    import argparse
+    import bench
+    for key, spec in bench.EXTRA_CONFIGS.items():
+        assert key.startswith(f"tet{spec['n']}_k{spec['k']}_"), key
+        assert spec["methods"] and all(len(m) == 7 for m in spec["methods"].values())
+    args = argparse.Namespace(dim=3, n=64, k=1, coefficient="identity", contrast=1.0, source="sine",
+                              max_coarse_rows=1000, galerkin=False, checker_blocks=4, seed=0)
+    w = bench.workload_config(args, 9363456, 6)
+    assert "64^3" in w["workload"] and w["unknowns"] == 9363456
