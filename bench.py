@@ -494,8 +494,9 @@ def run_ours(args, dist: Dist):
 
     # Which part of the headline cycle runs as one cluster launch (chosen by timing at setup), and the
     # context's device memory.
-    first, ctas = ctx.fused_coarse_info("fp32")
-    fused_info = {"first_level": first, "cluster_ctas": ctas, "device_gb": round(ctx.device_bytes() / 1e9, 2)}
+    first, ctas, threads = ctx.fused_coarse_info("fp32")
+    fused_info = {"first_level": first, "cluster_ctas": ctas, "cta_threads": threads,
+                  "device_gb": round(ctx.device_bytes() / 1e9, 2)}
 
     # Per-kernel device timing on level 0 (CUDA events on the library's stream).
     p32, p64 = 4, 8

@@ -103,7 +103,7 @@ def load(path: str = LIB):
     lib.fhg_set_vcycle_precision.argtypes = [C.c_void_p, C.c_int]
     lib.fhg_set_cycle.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
     lib.fhg_set_coarse_smoothing.argtypes = [C.c_void_p, C.c_int, C.c_int]
-    lib.fhg_fused_coarse_info.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int)]
+    lib.fhg_fused_coarse_info.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int), P(C.c_int)]
     lib.fhg_device_bytes.argtypes = [C.c_void_p]
     lib.fhg_device_bytes.restype = C.c_longlong
     lib.fhg_level_info.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_longlong), P(C.c_int), P(C.c_int),
@@ -250,10 +250,12 @@ class Context:
         return int(self.lib.fhg_device_bytes(self.h))
 
     def fused_coarse_info(self, precision: str):
-        """(first level of the one-launch coarse sub-cycle or -1, CTAs of its cluster) as run now."""
-        first, ctas = C.c_int(), C.c_int()
-        self._check(self.lib.fhg_fused_coarse_info(self.h, PRECISION[precision], C.byref(first), C.byref(ctas)))
-        return first.value, ctas.value
+        """(first level of the one-launch coarse sub-cycle or -1, CTAs of its cluster, threads of a
+        CTA) as run now."""
+        first, ctas, threads = C.c_int(), C.c_int(), C.c_int()
+        self._check(self.lib.fhg_fused_coarse_info(self.h, PRECISION[precision], C.byref(first), C.byref(ctas),
+                                                   C.byref(threads)))
+        return first.value, ctas.value, threads.value
 
     def permutation(self, level: int, nb: int) -> np.ndarray:
         perm = np.empty(nb, dtype=np.int32)

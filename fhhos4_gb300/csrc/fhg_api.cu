@@ -162,6 +162,7 @@ struct fhg_ctx {
     int fused_from[3] = {-1, -1, -1};  // per V-cycle precision: first level of the coarse sub-cycle run as
                                        // one cluster launch (-1: none), and the cluster's CTAs
     int fused_ctas[3] = {fhg::kClusterCtasPortable, fhg::kClusterCtasPortable, fhg::kClusterCtasPortable};
+    int fused_threads[3] = {fhg::kFusedThreads, fhg::kFusedThreads, fhg::kFusedThreads};  // and its CTAs' threads
     long long epoch = 0;               // incremented by every setup (batched graphs hold its buffers)
 };
 
@@ -1210,7 +1211,9 @@ bool fused_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
                 F.ap_ell = Ap->ell; F.ap_colidx = Ap->colidx; F.ap_vals = Ap->vals; F.ap_ld = Ap->ld;
             }
         }
-        if (fhg::launch_fused_cycle<T>(P, L0.bs, ctx->fused_ctas[V::kPrec], ctx->stream) != cudaSuccess) return false;
+        if (fhg::launch_fused_cycle<T>(P, L0.bs, ctx->fused_ctas[V::kPrec], ctx->fused_threads[V::kPrec], ctx->stream) !=
+            cudaSuccess)
+            return false;
         fhg::g_kernel_launches++;
         return true;
     }
@@ -1237,14 +1240,18 @@ struct FusedKey {
     std::vector<long long> sig;
     bool operator<(const FusedKey& o) const { return sig < o.sig; }
 };
+struct FusedChoice {
+    int from = -1, ctas = fhg::kClusterCtasPortable, threads = fhg::kFusedThreads;
+};
 std::mutex g_fused_mutex;
-std::map<FusedKey, std::pair<int, int>> g_fused_cache;
+std::map<FusedKey, FusedChoice> g_fused_cache;
 
 template <class T>
 void mg_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero);
 
 // Time one cycle below level 0 (from level 1, x = 0) for launch by launch and for every eligible first
-// level of the fused sub-cycle with 8 and 16 CTAs; keep the fastest (ties: the earlier candidate).
+// level of the fused sub-cycle with 8 and 16 CTAs of 512 and 1024 threads; keep the fastest (ties: the
+// earlier candidate).
 template <class T>
 int choose_fused(fhg_ctx* ctx)
 {
@@ -1256,6 +1263,7 @@ int choose_fused(fhg_ctx* ctx)
     const int first = fused_first_level(ctx, fhg::kFusedMaxRows);
     ctx->fused_from[PR] = -1;
     ctx->fused_ctas[PR] = fhg::kClusterCtasPortable;
+    ctx->fused_threads[PR] = fhg::kFusedThreads;
     if (first < 0) return FHG_OK;
     FusedKey key;
     key.sig = {PR, bs, nlevels, o.pre_smoother, o.post_smoother, o.pre_iterations, o.post_iterations,
@@ -1270,8 +1278,9 @@ int choose_fused(fhg_ctx* ctx)
         std::lock_guard<std::mutex> lock(g_fused_mutex);
         auto it = g_fused_cache.find(key);
         if (it != g_fused_cache.end()) {
-            ctx->fused_from[PR] = it->second.first;
-            ctx->fused_ctas[PR] = it->second.second;
+            ctx->fused_from[PR] = it->second.from;
+            ctx->fused_ctas[PR] = it->second.ctas;
+            ctx->fused_threads[PR] = it->second.threads;
             return FHG_OK;
         }
     }
@@ -1293,27 +1302,31 @@ int choose_fused(fhg_ctx* ctx)
     double best = 0.0;
     int rc = time_cycle(&best);
     if (rc) return rc;
-    int best_from = -1, best_ctas = fhg::kClusterCtasPortable;
-    for (int ctas : {fhg::kClusterCtasPortable, fhg::kClusterCtasLarge}) {
-        if (fhg::fused_cycle_clusters<T>(bs, ctas) < 1) continue;
-        for (int l = first; l + 1 < nlevels; l++) {
-            ctx->fused_from[PR] = l;
-            ctx->fused_ctas[PR] = ctas;
-            double ms = 0.0;
-            if ((rc = time_cycle(&ms))) break;
-            if (ms < best) {
-                best = ms;
-                best_from = l;
-                best_ctas = ctas;
+    FusedChoice choice;
+    for (int threads : {fhg::kFusedThreads, fhg::kFusedThreadsWide}) {
+        for (int ctas : {fhg::kClusterCtasPortable, fhg::kClusterCtasLarge}) {
+            if (fhg::fused_cycle_clusters<T>(bs, ctas, threads) < 1) continue;
+            for (int l = first; l + 1 < nlevels; l++) {
+                ctx->fused_from[PR] = l;
+                ctx->fused_ctas[PR] = ctas;
+                ctx->fused_threads[PR] = threads;
+                double ms = 0.0;
+                if ((rc = time_cycle(&ms))) break;
+                if (ms < best) {
+                    best = ms;
+                    choice = {l, ctas, threads};
+                }
             }
+            if (rc) break;
         }
         if (rc) break;
     }
-    ctx->fused_from[PR] = best_from;
-    ctx->fused_ctas[PR] = best_ctas;
+    ctx->fused_from[PR] = choice.from;
+    ctx->fused_ctas[PR] = choice.ctas;
+    ctx->fused_threads[PR] = choice.threads;
     if (rc) return rc;
     std::lock_guard<std::mutex> lock(g_fused_mutex);
-    g_fused_cache[key] = {best_from, best_ctas};
+    g_fused_cache[key] = choice;
     return FHG_OK;
 }
 
@@ -1378,6 +1391,7 @@ int refresh_fused(fhg_ctx* ctx)
     for (int p = 0; p < 3; p++) {
         ctx->fused_from[p] = -1;
         ctx->fused_ctas[p] = fhg::kClusterCtasPortable;
+        ctx->fused_threads[p] = fhg::kFusedThreads;
     }
     if (!o.fused_coarse || o.w_loops == FHG_CYCLE_K || !is_gs(o.pre_smoother) || !is_gs(o.post_smoother))
         return FHG_OK;
@@ -1390,8 +1404,15 @@ int refresh_fused(fhg_ctx* ctx)
     }
     const int first = fused_first_level(ctx, fhg::kFusedDefaultRows);
     if (first < 0) return FHG_OK;
-    if (fp32 && fhg::fused_cycle_clusters<float>(bs, fhg::kClusterCtasPortable) >= 1) ctx->fused_from[FHG_PREC_FP32] = first;
-    if (pair && fhg::fused_cycle_clusters<dfl>(bs, fhg::kClusterCtasPortable) >= 1) ctx->fused_from[FHG_PREC_DF] = first;
+    const int threads = o.fused_coarse == 2 ? fhg::kFusedThreadsWide : fhg::kFusedThreads;
+    if (fp32 && fhg::fused_cycle_clusters<float>(bs, fhg::kClusterCtasPortable, threads) >= 1) {
+        ctx->fused_from[FHG_PREC_FP32] = first;
+        ctx->fused_threads[FHG_PREC_FP32] = threads;
+    }
+    if (pair && fhg::fused_cycle_clusters<dfl>(bs, fhg::kClusterCtasPortable, threads) >= 1) {
+        ctx->fused_from[FHG_PREC_DF] = first;
+        ctx->fused_threads[FHG_PREC_DF] = threads;
+    }
     return FHG_OK;
 }
 
@@ -2946,11 +2967,13 @@ long long fhg_device_bytes(const fhg_ctx* ctx)
     return total;
 }
 
-int fhg_fused_coarse_info(const fhg_ctx* ctx, int precision, int* first_level, int* cluster_ctas)
+int fhg_fused_coarse_info(const fhg_ctx* ctx, int precision, int* first_level, int* cluster_ctas,
+                          int* cta_threads)
 {
     if (!ctx || !ctx->ready || precision < 0 || precision > 2) return FHG_ERR_INVALID_ARG;
     if (first_level) *first_level = ctx->fused_from[precision];
     if (cluster_ctas) *cluster_ctas = ctx->fused_ctas[precision];
+    if (cta_threads) *cta_threads = ctx->fused_threads[precision];
     return FHG_OK;
 }
 

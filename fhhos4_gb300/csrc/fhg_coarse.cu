@@ -158,19 +158,21 @@ __device__ __forceinline__ void rows_multi(const Ctx<T>& C, long long r0, long l
     }
 }
 
-// Rows in flight per lane group, by the bytes of a block: what fits in 128 registers without spills.
-template <class T, int BS>
-constexpr int kRowsInFlight = BS * BS * (int)sizeof(T) <= 16 ? 4 : BS * BS * (int)sizeof(T) <= 36 ? 3
+// Rows in flight per lane group, by the bytes of a block: what fits in 128 registers (512-thread
+// CTAs) without spills; one row with 64 registers (1024-thread CTAs).
+template <class T, int BS, int THREADS>
+constexpr int kRowsInFlight = THREADS > kFusedThreads ? 1
+                              : BS * BS * (int)sizeof(T) <= 16 ? 4 : BS * BS * (int)sizeof(T) <= 36 ? 3
                               : BS * BS * (int)sizeof(T) <= 72 ? 2 : 1;
 
 // One colour [c0, c1) of a block GS / SOR sweep on level L: x_i <- D_i^-1 (b_i - sum_{j != i} A_ij x_j),
 // relaxed by omega; output r of a row written by lane r (lanes loop when BS > lanes).
-template <class T, int BS>
+template <class T, int BS, int TH>
 __device__ void gs_colour(const Ctx<T>& C, const FusedLevel<T>& L, int c0, int c1)
 {
     const T w = C.P.omega;
     const bool pad = L.g_ell > 0;
-    rows_multi<T, BS, kRowsInFlight<T, BS>>(C, c0, c1, L.lanes, L.g_ell, L.a_rowptr, pad ? L.g_colidx : L.a_colidx,
+    rows_multi<T, BS, kRowsInFlight<T, BS, TH>>(C, c0, c1, L.lanes, L.g_ell, L.a_rowptr, pad ? L.g_colidx : L.a_colidx,
                                             pad ? L.g_vals : L.a_vals, pad ? L.g_ld : L.a_ld, L.x, true,
                                             [&](long long i, int lane, const T* acc) {
         for (int r = lane; r < BS; r += L.lanes) {
@@ -184,34 +186,34 @@ __device__ void gs_colour(const Ctx<T>& C, const FusedLevel<T>& L, int c0, int c
     cluster_sync();
 }
 
-template <class T, int BS>
+template <class T, int BS, int TH>
 __device__ void sweep(const Ctx<T>& C, const FusedLevel<T>& L, bool backward)
 {
     if (!backward)
-        for (int c = 0; c < L.ncol; c++) gs_colour<T, BS>(C, L, L.colour_start[c], L.colour_start[c + 1]);
+        for (int c = 0; c < L.ncol; c++) gs_colour<T, BS, TH>(C, L, L.colour_start[c], L.colour_start[c + 1]);
     else
-        for (int c = L.ncol - 1; c >= 0; c--) gs_colour<T, BS>(C, L, L.colour_start[c], L.colour_start[c + 1]);
+        for (int c = L.ncol - 1; c >= 0; c--) gs_colour<T, BS, TH>(C, L, L.colour_start[c], L.colour_start[c + 1]);
 }
 
 // The smoother directions of BlockGaussSeidel::ExecuteOneIteration (alternating ones by iteration parity).
-template <class T, int BS>
+template <class T, int BS, int TH>
 __device__ void smooth(const Ctx<T>& C, const FusedLevel<T>& L, int code, int iters)
 {
     for (int it = 0; it < iters; it++) {
-        if (code == kFusedForward) sweep<T, BS>(C, L, false);
-        else if (code == kFusedBackward) sweep<T, BS>(C, L, true);
-        else if (code == kFusedSymmetric) { sweep<T, BS>(C, L, false); sweep<T, BS>(C, L, true); }
-        else if (code == kFusedAlternatingForward) sweep<T, BS>(C, L, it % 2 != 0);
-        else sweep<T, BS>(C, L, it % 2 == 0);
+        if (code == kFusedForward) sweep<T, BS, TH>(C, L, false);
+        else if (code == kFusedBackward) sweep<T, BS, TH>(C, L, true);
+        else if (code == kFusedSymmetric) { sweep<T, BS, TH>(C, L, false); sweep<T, BS, TH>(C, L, true); }
+        else if (code == kFusedAlternatingForward) sweep<T, BS, TH>(C, L, it % 2 != 0);
+        else sweep<T, BS, TH>(C, L, it % 2 == 0);
     }
 }
 
 // L.r = L.b - A x (all blocks, the diagonal included).
-template <class T, int BS>
+template <class T, int BS, int TH>
 __device__ void residual(const Ctx<T>& C, const FusedLevel<T>& L)
 {
     const bool pad = L.ap_ell > 0;
-    rows_multi<T, BS, kRowsInFlight<T, BS>>(C, 0, L.nb, L.lanes, L.ap_ell, L.a_rowptr, pad ? L.ap_colidx : L.a_colidx,
+    rows_multi<T, BS, kRowsInFlight<T, BS, TH>>(C, 0, L.nb, L.lanes, L.ap_ell, L.a_rowptr, pad ? L.ap_colidx : L.a_colidx,
                                             pad ? L.ap_vals : L.a_vals, pad ? L.ap_ld : L.a_ld, L.x, false,
                                             [&](long long i, int lane, const T* acc) {
         for (int r = lane; r < BS; r += L.lanes) L.r[i * BS + r] = L.b[i * BS + r] - acc[r];
@@ -220,11 +222,11 @@ __device__ void residual(const Ctx<T>& C, const FusedLevel<T>& L)
 }
 
 // out (rows of M) = M in, or out += M in: the transfers as block products over CSR operators.
-template <class T, int BS>
+template <class T, int BS, int TH>
 __device__ void product(const Ctx<T>& C, int rows, int g, const int* rowptr, const int* colidx, const T* vals,
                         long long ld, const T* in, T* out, bool add)
 {
-    rows_multi<T, BS, kRowsInFlight<T, BS>>(C, 0, rows, g, 0, rowptr, colidx, vals, ld, in, false,
+    rows_multi<T, BS, kRowsInFlight<T, BS, TH>>(C, 0, rows, g, 0, rowptr, colidx, vals, ld, in, false,
                                             [&](long long i, int lane, const T* acc) {
         for (int r = lane; r < BS; r += g) out[i * BS + r] = add ? out[i * BS + r] + acc[r] : fin(acc[r]);
     });
@@ -258,7 +260,7 @@ __device__ void coarse_solve(const Ctx<T>& C, const FusedLevel<T>& L)
 // The cycle from lev[0] down: descend (zero x on a fresh level, pre-smooth, residual, restrict) to the
 // coarsest, solve there, then ascend (prolongate, post-smooth) until a level still owes a coarse
 // correction (W-cycle), from which the next descent starts with the coarser level's x kept.
-template <class T, int BS>
+template <class T, int BS, int TH>
 __device__ void run_cycle(const Ctx<T>& C)
 {
     const FusedCycle<T>& P = C.P;
@@ -271,9 +273,9 @@ __device__ void run_cycle(const Ctx<T>& C)
             const FusedLevel<T>& L = P.lev[l];
             const FusedLevel<T>& N = P.lev[l + 1];
             if (xz) zero(C, L.x, (long long)L.nb * BS);
-            smooth<T, BS>(C, L, P.pre, P.npre);
-            residual<T, BS>(C, L);
-            product<T, BS>(C, N.nb, L.t_lanes, L.r_rowptr, L.r_colidx, L.r_vals, L.r_ld, L.r, N.b, false);
+            smooth<T, BS, TH>(C, L, P.pre, P.npre);
+            residual<T, BS, TH>(C, L);
+            product<T, BS, TH>(C, N.nb, L.t_lanes, L.r_rowptr, L.r_colidx, L.r_vals, L.r_ld, L.r, N.b, false);
             done[l] = 0;
             xz = true;
         }
@@ -289,8 +291,8 @@ __device__ void run_cycle(const Ctx<T>& C)
             }
             const FusedLevel<T>& L = P.lev[l];
             const FusedLevel<T>& N = P.lev[l + 1];
-            product<T, BS>(C, L.nb, L.lanes, L.p_rowptr, L.p_colidx, L.p_vals, L.p_ld, N.x, L.x, true);
-            smooth<T, BS>(C, L, P.post, P.npost);
+            product<T, BS, TH>(C, L.nb, L.lanes, L.p_rowptr, L.p_colidx, L.p_vals, L.p_ld, N.x, L.x, true);
+            smooth<T, BS, TH>(C, L, P.post, P.npost);
         }
         if (!again) return;
         l++;          // the next coarse correction of level l - 1 starts on level l
@@ -298,37 +300,39 @@ __device__ void run_cycle(const Ctx<T>& C)
     }
 }
 
-template <class T, int BS>
-__global__ void __launch_bounds__(kFusedThreads, 1) k_fused_cycle(const __grid_constant__ FusedCycle<T> P)
+template <class T, int BS, int TH>
+__global__ void __launch_bounds__(TH, 1) k_fused_cycle(const __grid_constant__ FusedCycle<T> P)
 {
     pdl_wait_coarse();
     const Ctx<T> C{P, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x};
-    run_cycle<T, BS>(C);
+    run_cycle<T, BS, TH>(C);
 }
 
-template <class T, int BS>
-void* kernel_of()
-{
-    return (void*)k_fused_cycle<T, BS>;
-}
-
-template <class T>
-void* kernel_for(int bs)
+template <class T, int TH>
+void* kernel_for_th(int bs)
 {
     switch (bs) {
-    case 2: return kernel_of<T, 2>();
-    case 3: return kernel_of<T, 3>();
-    case 4: return kernel_of<T, 4>();
-    case 6: return kernel_of<T, 6>();
+    case 2: return (void*)k_fused_cycle<T, 2, TH>;
+    case 3: return (void*)k_fused_cycle<T, 3, TH>;
+    case 4: return (void*)k_fused_cycle<T, 4, TH>;
+    case 6: return (void*)k_fused_cycle<T, 6, TH>;
     default: return nullptr;
     }
 }
 
-void fused_config(cudaLaunchConfig_t& cfg, cudaLaunchAttribute* attr, int ctas, cudaStream_t s)
+template <class T>
+void* kernel_for(int bs, int threads)
+{
+    if (threads == kFusedThreads) return kernel_for_th<T, kFusedThreads>(bs);
+    if (threads == kFusedThreadsWide) return kernel_for_th<T, kFusedThreadsWide>(bs);
+    return nullptr;
+}
+
+void fused_config(cudaLaunchConfig_t& cfg, cudaLaunchAttribute* attr, int ctas, int threads, cudaStream_t s)
 {
     cfg = {};
     cfg.gridDim = dim3(ctas);
-    cfg.blockDim = dim3(kFusedThreads);
+    cfg.blockDim = dim3(threads);
     cfg.stream = s;
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = ctas;
@@ -352,9 +356,9 @@ cudaError_t allow_large_clusters(const void* k)
 }  // namespace
 
 template <class T>
-int fused_cycle_clusters(int bs, int ctas)
+int fused_cycle_clusters(int bs, int ctas, int threads)
 {
-    const void* k = kernel_for<T>(bs);
+    const void* k = kernel_for<T>(bs, threads);
     if (!k || (ctas != kClusterCtasPortable && ctas != kClusterCtasLarge)) return 0;
     if (ctas > kClusterCtasPortable && allow_large_clusters(k) != cudaSuccess) {
         cudaGetLastError();
@@ -362,7 +366,7 @@ int fused_cycle_clusters(int bs, int ctas)
     }
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[2];
-    fused_config(cfg, attr, ctas, nullptr);
+    fused_config(cfg, attr, ctas, threads, nullptr);
     cfg.numAttrs = 1;
     int n = 0;
     if (cudaOccupancyMaxActiveClusters(&n, k, &cfg) != cudaSuccess) {
@@ -373,23 +377,20 @@ int fused_cycle_clusters(int bs, int ctas)
 }
 
 template <class T>
-cudaError_t launch_fused_cycle(const FusedCycle<T>& P, int bs, int ctas, cudaStream_t s)
+cudaError_t launch_fused_cycle(const FusedCycle<T>& P, int bs, int ctas, int threads, cudaStream_t s)
 {
+    const void* k = kernel_for<T>(bs, threads);
+    if (!k) return cudaErrorInvalidValue;
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[2];
-    fused_config(cfg, attr, ctas, s);
-    switch (bs) {
-    case 2: return cudaLaunchKernelEx(&cfg, k_fused_cycle<T, 2>, P);
-    case 3: return cudaLaunchKernelEx(&cfg, k_fused_cycle<T, 3>, P);
-    case 4: return cudaLaunchKernelEx(&cfg, k_fused_cycle<T, 4>, P);
-    case 6: return cudaLaunchKernelEx(&cfg, k_fused_cycle<T, 6>, P);
-    default: return cudaErrorInvalidValue;
-    }
+    fused_config(cfg, attr, ctas, threads, s);
+    void* args[] = {const_cast<FusedCycle<T>*>(&P)};
+    return cudaLaunchKernelExC(&cfg, k, args);
 }
 
-template cudaError_t launch_fused_cycle<float>(const FusedCycle<float>&, int, int, cudaStream_t);
-template cudaError_t launch_fused_cycle<dfl>(const FusedCycle<dfl>&, int, int, cudaStream_t);
-template int fused_cycle_clusters<float>(int, int);
-template int fused_cycle_clusters<dfl>(int, int);
+template cudaError_t launch_fused_cycle<float>(const FusedCycle<float>&, int, int, int, cudaStream_t);
+template cudaError_t launch_fused_cycle<dfl>(const FusedCycle<dfl>&, int, int, int, cudaStream_t);
+template int fused_cycle_clusters<float>(int, int, int);
+template int fused_cycle_clusters<dfl>(int, int, int);
 
 }  // namespace fhg

@@ -9,7 +9,8 @@ namespace fhg {
 
 constexpr int kClusterCtasPortable = 8;   // CTAs of the one cluster: the portable maximum, or
 constexpr int kClusterCtasLarge = 16;     // the non-portable one where the device runs it
-constexpr int kFusedThreads = 512;        // threads per CTA
+constexpr int kFusedThreads = 512;        // threads per CTA (128 registers, up to four rows in flight)
+constexpr int kFusedThreadsWide = 1024;   // or twice the warps per SM (64 registers, one row in flight)
 constexpr int kFusedMaxLevels = 6;        // levels of a fused sub-cycle, the coarsest included
 constexpr int kFusedMaxColours = 24;
 constexpr int kFusedMaxRows = 65536;      // block rows of the largest level a fused sub-cycle takes
@@ -67,12 +68,13 @@ struct FusedCycle {
     FusedLevel<T> lev[kFusedMaxLevels];
 };
 
-// One cluster of `ctas` CTAs (kClusterCtasPortable or kClusterCtasLarge).
+// One cluster of `ctas` CTAs (kClusterCtasPortable or kClusterCtasLarge) of `threads` threads
+// (kFusedThreads or kFusedThreadsWide).
 template <class T>
-cudaError_t launch_fused_cycle(const FusedCycle<T>& P, int bs, int ctas, cudaStream_t s);
-// Clusters of `ctas` CTAs of the fused kernel that fit on the current device at once (0: it cannot
-// run here).
+cudaError_t launch_fused_cycle(const FusedCycle<T>& P, int bs, int ctas, int threads, cudaStream_t s);
+// Clusters of `ctas` CTAs of `threads` threads of the fused kernel that fit on the current device at
+// once (0: it cannot run here).
 template <class T>
-int fused_cycle_clusters(int bs, int ctas);
+int fused_cycle_clusters(int bs, int ctas, int threads);
 
 }  // namespace fhg

@@ -157,7 +157,8 @@ class _KrylovOnGpu(IterativeSolver):
         # Residual replacement in every precision (the FP32 V-cycle always replaces); off keeps the
         # reference's stopping loop in FP64.
         self.ReplaceResidual = False
-        # the coarse part of the cycle as one cluster launch where the levels are small (FP32 / DF)
+        # the coarse part of the cycle as one cluster launch where the levels are small (FP32 / DF);
+        # "wide": the same with 1024-thread CTAs when the launch shape is not timed
         self.FusedCoarse = True
         self._ctx: Optional[N.Context] = None
 
@@ -178,7 +179,7 @@ class _KrylovOnGpu(IterativeSolver):
         o.max_coarse_rows = mg.MaxCoarseRows
         o.outer_split = 1 if self.OuterSplit else 0
         o.replace_residual = 1 if self.ReplaceResidual else 0
-        o.fused_coarse = 1 if self.FusedCoarse else 0
+        o.fused_coarse = 2 if self.FusedCoarse == "wide" else (1 if self.FusedCoarse else 0)
         o.w_loops = N.CYCLE_K if mg.Cycle == "K" else (mg.WLoops if mg.Cycle == "W" else 1)
         o.galerkin = 1 if mg.UseGalerkinOperator else 0
         o.coarse_pre_iterations = mg.CoarsePreSmoothingIterations

@@ -141,8 +141,10 @@ typedef struct {
                                    level (every level below it at most 65,536 block rows and 24 colours, at most
                                    6 levels) and keeps the fastest, per precision and hierarchy structure;
                                    without, it fuses from the first level of at most 8,192 block rows with 8
-                                   CTAs. 0: launch by launch. Same arithmetic up to the summation order of a
-                                   row. */
+                                   CTAs of 512 threads. Timing also tries CTAs of 1024 threads (twice the warps
+                                   per SM, one row in flight per lane group). 2: as 1, but without autotuning
+                                   the CTAs have 1024 threads. 0: launch by launch. Same arithmetic up to the
+                                   summation order of a row. */
 } fhg_options;
 
 typedef struct {
@@ -232,9 +234,10 @@ int fhg_level_info(const fhg_ctx* ctx, int level, int* n_block_rows, long long* 
                    int* n_colours, int* lanes, long long* p_blocks);
 
 /* The coarse sub-cycle of V-cycle precision `precision` (FHG_PREC_FP32 or FHG_PREC_DF) as the context
- * runs it now: the first level of the one-launch sub-cycle (-1: launch by launch) and the CTAs of its
- * cluster. No counterpart in the reference. */
-int fhg_fused_coarse_info(const fhg_ctx* ctx, int precision, int* first_level, int* cluster_ctas);
+ * runs it now: the first level of the one-launch sub-cycle (-1: launch by launch), the CTAs of its
+ * cluster and the threads of each CTA. Any pointer may be NULL. No counterpart in the reference. */
+int fhg_fused_coarse_info(const fhg_ctx* ctx, int precision, int* first_level, int* cluster_ctas,
+                          int* cta_threads);
 
 /* The colour permutation of `level` after setup: perm[new_block_row] = given_block_row. */
 int fhg_get_permutation(const fhg_ctx* ctx, int level, int* perm);

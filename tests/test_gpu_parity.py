@@ -267,18 +267,19 @@ def test_df_vcycle_matches_reference(case, variant, pre, post, cycle, omega_key,
                                                        ("df", "W", "sbgs", "sbgs"), ("fp32", "W", "bgs", "rbgs"),
                                                        ("fp32", "V", "bsor", "rbsor")])
 def test_fused_coarse_cycle_matches_launch_by_launch(case, precision, cycle, pre, post):
-    """The coarse sub-cycle as one cluster launch against the same cycle launched phase by phase:
-    the same arithmetic up to the summation order of a row, so FP64-class solves agree to 1e-10
+    """The coarse sub-cycle as one cluster launch (CTAs of 512 and of 1024 threads) against the same
+    cycle launched phase by phase: the same arithmetic up to the summation order of a row, so FP64-class solves agree to 1e-10
     (iterations equal) and FP32 solves take the same iterations within one and reach the tolerance."""
     kw = dict(precision=precision, cycle=cycle, pre=pre, post=post, nu=(2, 2), coarse_nu=(3, 3),
               omega=float(case["sor_omega"]) if pre == "bsor" else 1.0)
-    a = S().fcg_mg(case.As, case.Ps, case.bs, fused=True, **kw)
     b = S().fcg_mg(case.As, case.Ps, case.bs, fused=False, **kw)
-    first, ctas = a._ctx.fused_coarse_info(precision)
-    if len(case.As) >= 3:
-        assert 1 <= first <= len(case.As) - 2 and ctas == 8
     assert b._ctx.fused_coarse_info(precision)[0] == -1
-    _check_fused_pair(case.As[0], case.b, a, b, precision)
+    for fused, threads in ((True, 512), ("wide", 1024)):
+        a = S().fcg_mg(case.As, case.Ps, case.bs, fused=fused, **kw)
+        first, ctas, nthreads = a._ctx.fused_coarse_info(precision)
+        if len(case.As) >= 3:
+            assert 1 <= first <= len(case.As) - 2 and ctas == 8 and nthreads == threads
+        _check_fused_pair(case.As[0], case.b, a, b, precision)
 
 
 def _check_fused_pair(A0, rhs, a, b, precision, rtol=1e-10):
@@ -295,8 +296,8 @@ def _check_fused_pair(A0, rhs, a, b, precision, rtol=1e-10):
 @pytest.mark.parametrize("precision,cycle", [("fp32", "V"), ("df", "V"), ("df", "W")])
 def test_fused_coarse_cycle_deep_hierarchy(precision, cycle):
     """A deep 2D hierarchy (n = 256, k = 3: six levels, Galerkin coarse operators, the largest
-    problem of the batched workload), fused from every eligible level and chosen by timing: the same
-    answers as launch by launch. The sub-cycle runs as a loop over levels with fixed stack use.
+    problem of the batched workload), fused with CTAs of 512 and 1024 threads and chosen by timing:
+    the same answers as launch by launch. The sub-cycle runs as a loop over levels with fixed stack use.
     Rows of the Galerkin operators hold about 40 blocks, summed by 16 lanes here and by the tuned
     launch shape there; with the coefficient contrast (1e3) FCG carries that reordering (a few units
     of 2^-47 per row in pairs) to 1e-10 of the history, so the FP64-class bar is 1e-8."""
@@ -307,12 +308,12 @@ def test_fused_coarse_cycle_deep_hierarchy(precision, cycle):
         As.append((P.T @ As[-1] @ P).tocsr())
     kw = dict(precision=precision, cycle=cycle, pre="bgs", post="rbgs", galerkin=True)
     b_ = S().fcg_mg(As, Ps, bs, fused=False, **kw)
-    for autotune in (False, True):
-        a = S().fcg_mg(As, Ps, bs, fused=True, autotune=autotune, **kw)
-        first, ctas = a._ctx.fused_coarse_info(precision)
-        assert first == -1 or (1 <= first <= len(As) - 2 and ctas in (8, 16))
+    for fused, autotune in ((True, False), ("wide", False), (True, True)):
+        a = S().fcg_mg(As, Ps, bs, fused=fused, autotune=autotune, **kw)
+        first, ctas, threads = a._ctx.fused_coarse_info(precision)
+        assert first == -1 or (1 <= first <= len(As) - 2 and ctas in (8, 16) and threads in (512, 1024))
         if not autotune:
-            assert first >= 1
+            assert first >= 1 and threads == (1024 if fused == "wide" else 512)
         _check_fused_pair(A0, b, a, b_, precision, rtol=1e-8)
 
 
