@@ -105,6 +105,11 @@ struct Level {
     float* kv32[4] = {nullptr, nullptr, nullptr, nullptr};
     double* cinv = nullptr;  // coarsest only, n x n row-major
     long long p_blocks = 0;
+    // The transfer to the next level is the natural injection between face degrees (a p-multigrid
+    // level: same faces, the next level's block size smaller): no P / R operators, the map of block
+    // rows (this level's order -> the next level's) instead.
+    bool inject = false;
+    int* inj_map = nullptr;
 };
 
 }  // namespace
@@ -526,6 +531,50 @@ void symmetrise_lower(const HostCsr& A, HostCsr& S)
         S.rowptr[i + 1] = (int)S.colidx.size();
     }
     S.set = true;
+}
+
+// Whether P (scalar CSR, nb * nh rows) is the natural injection of P_LevelForHHO::SetupProlongation
+// (src/Solver/Multigrid/MultigridForHHO/P_MultigridForHHO.h:69-92) onto nl < nh unknowns per face:
+// row f * nh + i holds the single entry 1 at column f * nl + i for i < nl, and rows with i >= nl are
+// empty. nl is read from the column count.
+bool natural_injection(const HostCsr& P, int nh, int nb, int* nl_out)
+{
+    if (nb <= 0 || P.n_rows != nb * nh || P.n_cols % nb) return false;
+    const int nl = P.n_cols / nb;
+    if (nl <= 0 || nl >= nh) return false;
+    for (int f = 0; f < nb; f++)
+        for (int i = 0; i < nh; i++) {
+            const int r = f * nh + i;
+            const int len = P.rowptr[r + 1] - P.rowptr[r];
+            if (i >= nl ? len != 0
+                        : (len != 1 || P.colidx[P.rowptr[r]] != f * nl + i || P.vals[P.rowptr[r]] != 1.0))
+                return false;
+        }
+    *nl_out = nl;
+    return true;
+}
+
+// P^T A P for the natural injection: the leading nl x nl part of every nh x nh block of A, the
+// entries as they are (the Galerkin operator of a p-multigrid level, Level.h:133-137).
+void inject_galerkin(const HostCsr& A, int nh, int nl, HostCsr& C)
+{
+    const int nb = A.n_rows / nh;
+    C = HostCsr();
+    C.n_rows = C.n_cols = nb * nl;
+    C.rowptr.assign(1, 0);
+    for (int f = 0; f < nb; f++)
+        for (int i = 0; i < nl; i++) {
+            const int r = f * nh + i;
+            for (int p = A.rowptr[r]; p < A.rowptr[r + 1]; p++) {
+                const int c = A.colidx[p];
+                if (c % nh < nl) {
+                    C.colidx.push_back(c / nh * nl + c % nh);
+                    C.vals.push_back(A.vals[p]);
+                }
+            }
+            C.rowptr.push_back((int)C.colidx.size());
+        }
+    C.set = true;
 }
 
 bool csr_equal(const HostCsr& A, const HostCsr& B)
@@ -1220,15 +1269,16 @@ bool fused_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
 }
 
 // First level (>= 1, above the coarsest) from which every level has at most max_rows block rows and
-// at most kFusedMaxColours colours, within kFusedMaxLevels levels; -1 when there is none.
+// at most kFusedMaxColours colours, within kFusedMaxLevels levels, all of one block size and joined by
+// products with P (no natural injection); -1 when there is none.
 int fused_first_level(const fhg_ctx* ctx, int max_rows)
 {
     const int nlevels = ctx->nlevels;
     for (int l = 1; l + 1 < nlevels; l++) {
         bool ok = nlevels - l <= fhg::kFusedMaxLevels;
         for (int k = l; k < nlevels && ok; k++)
-            ok = ctx->levels[k].nb <= max_rows &&
-                 (k == nlevels - 1 || ctx->levels[k].ncolours <= fhg::kFusedMaxColours);
+            ok = ctx->levels[k].nb <= max_rows && ctx->levels[k].bs == ctx->levels[l].bs &&
+                 (k == nlevels - 1 || (ctx->levels[k].ncolours <= fhg::kFusedMaxColours && !ctx->levels[k].inject));
         if (ok) return l;
     }
     return -1;
@@ -1259,18 +1309,19 @@ int choose_fused(fhg_ctx* ctx)
     constexpr int PR = V::kPrec;
     const fhg_options& o = ctx->opts;
     const int nlevels = ctx->nlevels;
-    const int bs = ctx->levels[0].bs;
     const int first = fused_first_level(ctx, fhg::kFusedMaxRows);
     ctx->fused_from[PR] = -1;
     ctx->fused_ctas[PR] = fhg::kClusterCtasPortable;
     ctx->fused_threads[PR] = fhg::kFusedThreads;
     if (first < 0) return FHG_OK;
+    const int bs = ctx->levels[first].bs;   // every candidate level's (fused_first_level)
     FusedKey key;
-    key.sig = {PR, bs, nlevels, o.pre_smoother, o.post_smoother, o.pre_iterations, o.post_iterations,
+    key.sig = {PR, ctx->levels[0].bs, bs, nlevels, o.pre_smoother, o.post_smoother, o.pre_iterations, o.post_iterations,
                o.coarse_pre_iterations, o.coarse_post_iterations, o.w_loops, o.omega == 1.0 ? 1 : 0};
     for (int l = 1; l < nlevels; l++) {
         const Level& L = ctx->levels[l];
         key.sig.push_back(L.nb);
+        key.sig.push_back(L.bs);
         key.sig.push_back(L.ncolours);
         key.sig.push_back(V::Acsr(const_cast<Level&>(L)).nnzb);
     }
@@ -1386,7 +1437,6 @@ int refresh_fused(fhg_ctx* ctx)
 {
     std::lock_guard<std::recursive_mutex> timing(g_timing_mutex);
     const fhg_options& o = ctx->opts;
-    const int bs = ctx->levels[0].bs;
     const bool fp32 = ctx->levels[0].A32.vals != nullptr, pair = ctx->levels[0].A2.vals != nullptr;
     for (int p = 0; p < 3; p++) {
         ctx->fused_from[p] = -1;
@@ -1404,6 +1454,7 @@ int refresh_fused(fhg_ctx* ctx)
     }
     const int first = fused_first_level(ctx, fhg::kFusedDefaultRows);
     if (first < 0) return FHG_OK;
+    const int bs = ctx->levels[first].bs;
     const int threads = o.fused_coarse == 2 ? fhg::kFusedThreadsWide : fhg::kFusedThreads;
     if (fp32 && fhg::fused_cycle_clusters<float>(bs, fhg::kClusterCtasPortable, threads) >= 1) {
         ctx->fused_from[FHG_PREC_FP32] = first;
@@ -1414,6 +1465,28 @@ int refresh_fused(fhg_ctx* ctx)
         ctx->fused_threads[FHG_PREC_DF] = threads;
     }
     return FHG_OK;
+}
+
+// b_{l+1} = R_l r (Multigrid.h:491): the product with R_l, or the natural injection's restriction.
+template <class T>
+void restrict_to(fhg_ctx* ctx, int l, const T* r, T* bc)
+{
+    Level& L = ctx->levels[l];
+    if (L.inject)
+        fhg::launch_inject<T>(L.nb, L.bs, ctx->levels[l + 1].bs, L.inj_map, r, nullptr, bc, false, ctx->stream);
+    else
+        fhg::launch_spmv<T>(LevelVecs<T>::R(L), fhg::kSpmvAssign, r, nullptr, bc, ctx->stream);
+}
+
+// out = aux + P_l e (Multigrid.h:531-533), aux NULL reading as zero.
+template <class T>
+void prolong_add(fhg_ctx* ctx, int l, const T* e, const T* aux, T* out)
+{
+    Level& L = ctx->levels[l];
+    if (L.inject)
+        fhg::launch_inject<T>(L.nb, L.bs, ctx->levels[l + 1].bs, L.inj_map, e, aux, out, true, ctx->stream);
+    else
+        fhg::launch_spmv<T>(LevelVecs<T>::P(L), aux ? fhg::kSpmvAddTo : fhg::kSpmvAssign, e, aux, out, ctx->stream);
 }
 
 // One multigrid cycle on level l (src/Solver/Multigrid/Multigrid.h:438-608): V for w_loops = 1,
@@ -1444,7 +1517,7 @@ void mg_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
     if (x_zero && !gs_zero) cudaMemsetAsync(x, 0, sizeof(T) * (size_t)L.n, s);
     smooth<T>(ctx, l, pre, npre, b, x, gs_zero);
     fhg::launch_spmv<T>(V::A(L), fhg::kSpmvResidual, x, b, V::r(L), s);
-    fhg::launch_spmv<T>(V::R(L), fhg::kSpmvAssign, V::r(L), nullptr, V::b(C), s);
+    restrict_to<T>(ctx, l, V::r(L), V::b(C));
     if (ctx->opts.w_loops == FHG_CYCLE_K && l + 1 < ctx->nlevels - 1) {
         kcycle_fcg<T>(ctx, l + 1, V::b(C), V::x(C));
     } else {
@@ -1454,7 +1527,7 @@ void mg_cycle(fhg_ctx* ctx, int l, const T* b, T* x, bool x_zero)
             if (l + 1 == ctx->nlevels - 1) break;
         }
     }
-    fhg::launch_spmv<T>(V::P(L), fhg::kSpmvAddTo, V::x(C), x, x, s);
+    prolong_add<T>(ctx, l, V::x(C), x, x);
     smooth<T>(ctx, l, ctx->opts.post_smoother, npost, b, x);
     if constexpr (std::is_same<T, float>::value) {
         if (l == 0 && ctx->learned_now) learned_step(ctx, b, x);
@@ -1852,6 +1925,7 @@ int tune_level_uncached(fhg_ctx* ctx, int l)
                 L.gs_slot[PR] = slot_ms < row_ms;
             }
         }
+        if (L.inject) return FHG_OK;   // the natural injection has no launch shape
         BsrView<T>& P = const_cast<BsrView<T>&>(V::Pcsr(L));
         BsrView<T>& R = const_cast<BsrView<T>&>(V::Rcsr(L));
         const bool forced_jds = ctx->opts.gs_layout == FHG_GS_SLOT;   // the jagged views, not compared
@@ -1953,6 +2027,8 @@ void reset_device_state(Level& L)
     for (int i = 0; i < 4; i++) { L.kv64[i] = nullptr; L.kv32[i] = nullptr; L.kv2[i] = nullptr; }
     L.cinv = nullptr;
     L.outer_lanes = 0;
+    L.inject = false;
+    L.inj_map = nullptr;
 }
 
 void free_all(fhg_ctx* ctx)
@@ -2288,7 +2364,6 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
     if (nlevels <= 0 || nlevels > (int)ctx->levels.size())
         return fail(ctx, FHG_ERR_INVALID_ARG, "nlevels=%d but %zu levels were given", nlevels, ctx->levels.size());
     ctx->nlevels = nlevels;
-    const int bs = ctx->levels[0].bs;
     if (o.galerkin) {
         // Galerkin coarse operators A_{l+1} = R_l A_l P_l, R_l = P_l^T (Level::ComputeGalerkinOperator,
         // src/Solver/Multigrid/Level.h:133-137; "-g 1"), replacing any operator given for l >= 1.
@@ -2296,7 +2371,17 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         for (int l = 0; l + 1 < nlevels; l++) {
             Level& L = ctx->levels[l];
             Level& C = ctx->levels[l + 1];
+            const int bs = L.bs;
             if (!L.P_in.set) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d prolongation not set", l);
+            int nl = 0;
+            if (natural_injection(L.P_in, bs, L.nb, &nl)) {
+                inject_galerkin(L.A_in, bs, nl, C.A_in);
+                C.n = L.nb * nl;
+                C.bs = nl;
+                C.nb = L.nb;
+                C.A_is_galerkin = true;
+                continue;
+            }
             if (L.P_in.n_rows != L.n || L.P_in.n_cols % bs)
                 return fail(ctx, FHG_ERR_INVALID_ARG, "level %d prolongation is %dx%d for %d rows", l, L.P_in.n_rows,
                             L.P_in.n_cols, L.n);
@@ -2321,12 +2406,22 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
     for (int l = 0; l < nlevels; l++) {
         Level& L = ctx->levels[l];
         if (!L.A_in.set) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d operator not set", l);
-        if (L.bs != bs) return fail(ctx, FHG_ERR_UNSUPPORTED, "level %d block size %d differs from %d", l, L.bs, bs);
+        L.inject = false;
         if (l < nlevels - 1) {
+            const Level& C = ctx->levels[l + 1];
             if (!L.P_in.set) return fail(ctx, FHG_ERR_INVALID_ARG, "level %d prolongation not set", l);
-            if (L.P_in.n_rows != L.n || L.P_in.n_cols != ctx->levels[l + 1].n)
+            if (L.P_in.n_rows != L.n || L.P_in.n_cols != C.n)
                 return fail(ctx, FHG_ERR_INVALID_ARG, "level %d prolongation is %dx%d, expected %dx%d", l,
-                            L.P_in.n_rows, L.P_in.n_cols, L.n, ctx->levels[l + 1].n);
+                            L.P_in.n_rows, L.P_in.n_cols, L.n, C.n);
+            // A change of block size (p-coarsening) only through the natural injection.
+            if (C.bs != L.bs) {
+                int nl = 0;
+                if (C.nb != L.nb || !natural_injection(L.P_in, L.bs, L.nb, &nl) || nl != C.bs)
+                    return fail(ctx, FHG_ERR_UNSUPPORTED,
+                                "level %d block size %d differs from level %d's %d and the prolongation is not the "
+                                "natural injection between face degrees", l + 1, C.bs, l, L.bs);
+                L.inject = true;
+            }
         }
     }
     Level& LC = ctx->levels[nlevels - 1];
@@ -2344,7 +2439,7 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
     std::vector<HostBsr> Ab(nlevels);
     for (int l = 0; l < nlevels; l++) {
         Level& L = ctx->levels[l];
-        csr_to_bsr(L.A_in, bs, Ab[l]);
+        csr_to_bsr(L.A_in, L.bs, Ab[l]);
         L.perm.resize(L.nb);
         std::iota(L.perm.begin(), L.perm.end(), 0);
         if (l == nlevels - 1) {
@@ -2401,6 +2496,7 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
         if ((rc = upload(ctx, &L.perm_d, L.perm.data(), L.perm.size()))) return rc;
         if (l < nlevels - 1) {
             // Pre-inverted diagonal blocks (FP64, rounded for the FP32 copy).
+            const int bs = L.bs;
             const int bb = bs * bs;
             std::vector<double> inv((size_t)L.nb * bb);
             for (int I = 0; I < L.nb; I++) {
@@ -2423,37 +2519,45 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
                 for (size_t q = 0; q < soa.size(); q++) s2[q] = dfl(soa[q]);
                 if ((rc = upload(ctx, &L.dinv2, s2.data(), s2.size()))) return rc;
             }
-            // Transfers: P' = Pi_l P Pi_{l+1}^T, R' = P'^T.
-            HostBsr Pb, Pp, Rp;
-            csr_to_bsr(L.P_in, bs, Pb);
-            permute_bsr(Pb, L.perm, iperm[l + 1], Pp);
-            Pb = HostBsr();
-            transpose_bsr(Pp, Rp);
-            L.p_blocks = Pp.nnzb();
-            if ((rc = upload_bsr<double>(ctx, Pp, L.P, nullptr))) return rc;
-            if ((rc = upload_bsr<double>(ctx, Rp, L.R, nullptr))) return rc;
-            if (fp32) {
-                if ((rc = upload_bsr<float>(ctx, Pp, L.P32, &L.P))) return rc;
-                if ((rc = upload_bsr<float>(ctx, Rp, L.R32, &L.R))) return rc;
-            }
-            if (pair) {
-                if ((rc = upload_bsr<dfl>(ctx, Pp, L.P2, &L.P))) return rc;
-                if ((rc = upload_bsr<dfl>(ctx, Rp, L.R2, &L.R))) return rc;
-            }
-            // the jagged transfer views of the two largest levels: compared by the autotuner, or used
-            // with FHG_GS_SLOT
-            const bool want_jds = o.gs_layout == FHG_GS_SLOT || (o.gs_layout == FHG_GS_AUTO && o.autotune);
-            if (want_jds && l <= 1) {
-                if (fp32 && ((rc = upload_jds(ctx, Pp, L.P32j)) || (rc = upload_jds(ctx, Rp, L.R32j)))) return rc;
-                if (pair && ((rc = upload_jds(ctx, Pp, L.P2j)) || (rc = upload_jds(ctx, Rp, L.R2j)))) return rc;
-                if (o.gs_layout == FHG_GS_SLOT)
-                    for (int q : {FHG_PREC_FP32, FHG_PREC_DF}) {
-                        L.p_jds[q] = true;
-                        L.r_jds[q] = true;
-                    }
+            if (L.inject) {
+                // The natural injection: block row i of this level is block row map[i] of the next.
+                std::vector<int> map(L.nb);
+                for (int I = 0; I < L.nb; I++) map[I] = iperm[l + 1][L.perm[I]];
+                if ((rc = upload(ctx, &L.inj_map, map.data(), map.size()))) return rc;
+                L.p_blocks = 0;
+            } else {
+                // Transfers: P' = Pi_l P Pi_{l+1}^T, R' = P'^T.
+                HostBsr Pb, Pp, Rp;
+                csr_to_bsr(L.P_in, bs, Pb);
+                permute_bsr(Pb, L.perm, iperm[l + 1], Pp);
+                Pb = HostBsr();
+                transpose_bsr(Pp, Rp);
+                L.p_blocks = Pp.nnzb();
+                if ((rc = upload_bsr<double>(ctx, Pp, L.P, nullptr))) return rc;
+                if ((rc = upload_bsr<double>(ctx, Rp, L.R, nullptr))) return rc;
+                if (fp32) {
+                    if ((rc = upload_bsr<float>(ctx, Pp, L.P32, &L.P))) return rc;
+                    if ((rc = upload_bsr<float>(ctx, Rp, L.R32, &L.R))) return rc;
+                }
+                if (pair) {
+                    if ((rc = upload_bsr<dfl>(ctx, Pp, L.P2, &L.P))) return rc;
+                    if ((rc = upload_bsr<dfl>(ctx, Rp, L.R2, &L.R))) return rc;
+                }
+                // the jagged transfer views of the two largest levels: compared by the autotuner, or used
+                // with FHG_GS_SLOT
+                const bool want_jds = o.gs_layout == FHG_GS_SLOT || (o.gs_layout == FHG_GS_AUTO && o.autotune);
+                if (want_jds && l <= 1) {
+                    if (fp32 && ((rc = upload_jds(ctx, Pp, L.P32j)) || (rc = upload_jds(ctx, Rp, L.R32j)))) return rc;
+                    if (pair && ((rc = upload_jds(ctx, Pp, L.P2j)) || (rc = upload_jds(ctx, Rp, L.R2j)))) return rc;
+                    if (o.gs_layout == FHG_GS_SLOT)
+                        for (int q : {FHG_PREC_FP32, FHG_PREC_DF}) {
+                            L.p_jds[q] = true;
+                            L.r_jds[q] = true;
+                        }
+                }
             }
         }
-        if (l == 0 && fp32 && nlevels > 1 && fhg::learned_supports(bs)) {
+        if (l == 0 && fp32 && nlevels > 1 && fhg::learned_supports(L.bs)) {
             // Learned-step inputs: neighbour table, scratch and element-tensor features.
             std::vector<int> nbr;
             learned_neighbours(Ap, nbr);
@@ -2471,7 +2575,7 @@ int fhg_setup(fhg_ctx* ctx, int nlevels, const fhg_options* opts)
             const bool split = (fp32 || pair) && o.outer_split;
             if (!L.ahat_is_a) {
                 HostBsr Sb, Sp;
-                csr_to_bsr(S, bs, Sb);
+                csr_to_bsr(S, L.bs, Sb);
                 permute_bsr(Sb, L.perm, iperm[0], Sp);
                 if ((rc = upload_bsr<double>(ctx, Sp, L.Ahat, nullptr))) return rc;
                 if (split && (rc = upload_bsr_split(ctx, Sp, L.Ahat_hi, &L.ahat_lo, L.Ahat))) return rc;
@@ -2665,11 +2769,11 @@ static int apply_device_t(fhg_ctx* ctx, int level, int op, T* in, T* aux, T* out
     case FHG_OP_RESIDUAL: fhg::launch_spmv<T>(V::A(L), fhg::kSpmvResidual, in, aux, out, s); break;
     case FHG_OP_RESTRICT:
         if (coarsest) return fail(ctx, FHG_ERR_INVALID_ARG, "no restriction on the coarsest level");
-        fhg::launch_spmv<T>(V::R(L), fhg::kSpmvAssign, in, nullptr, out, s);
+        restrict_to<T>(ctx, level, in, out);
         break;
     case FHG_OP_PROLONG_ADD:
         if (coarsest) return fail(ctx, FHG_ERR_INVALID_ARG, "no prolongation on the coarsest level");
-        fhg::launch_spmv<T>(V::P(L), fhg::kSpmvAddTo, in, aux, out, s);
+        prolong_add<T>(ctx, level, in, aux, out);
         break;
     case FHG_OP_GS_FORWARD:
     case FHG_OP_GS_BACKWARD:

@@ -742,6 +742,39 @@ __global__ void __launch_bounds__(kThreads) k_permute(int nb, int bs, const int*
     else out[o] = in[i];
 }
 
+// The natural injection between two face degrees on the same faces (P_LevelForHHO::SetupProlongation,
+// src/Solver/Multigrid/MultigridForHHO/P_MultigridForHHO.h:69-92): fine face block i (nh unknowns)
+// is coarse block map[i] (nl < nh unknowns, the first nl functions of the hierarchical face basis).
+// Restriction by P^T: out[map[i] * nl + q] = in[i * nh + q] for q < nl.
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_inject_restrict(int nb, int nh, int nl, const int* __restrict__ map,
+                                                              const T* __restrict__ in, T* __restrict__ out)
+{
+    pdl_wait();
+    const long long i = (long long)blockIdx.x * kThreads + threadIdx.x;
+    if (i >= (long long)nb * nl) return;
+    const int blk = (int)(i / nl), q = (int)(i - (long long)blk * nl);
+    out[(long long)map[blk] * nl + q] = in[(long long)blk * nh + q];
+}
+
+// Prolongation by P: out[i * nh + q] = aux[i * nh + q] + (q < nl ? in[map[i] * nl + q] : 0), aux NULL
+// reading as zero; out may be aux. The one entry of P is 1, so this is the product's arithmetic.
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_inject_prolong(int nb, int nh, int nl, const int* __restrict__ map,
+                                                             const T* __restrict__ in, const T* aux, T* out)
+{
+    pdl_wait();
+    const long long i = (long long)blockIdx.x * kThreads + threadIdx.x;
+    if (i >= (long long)nb * nh) return;
+    const int blk = (int)(i / nh), q = (int)(i - (long long)blk * nh);
+    if (q < nl) {
+        const T e = in[(long long)map[blk] * nl + q];
+        out[i] = aux ? aux[i] + e : e;
+    } else {
+        out[i] = aux ? aux[i] : T(0);
+    }
+}
+
 inline unsigned grid_for(long long work, int per_cta)
 {
     long long g = (work + per_cta - 1) / per_cta;
@@ -980,6 +1013,20 @@ void launch_permute(int nb, int bs, const int* perm, const T* in, T* out, bool g
 {
     if (nb == 0) return;
     pdl_launch(k_permute<T>, grid_for((long long)nb * bs, kThreads), kThreads, 0, s, nb, bs, perm, in, out, gather ? 1 : 0);
+    g_kernel_launches++;
+}
+
+template <class T>
+void launch_inject(int nb, int nh, int nl, const int* map, const T* in, const T* aux, T* out, bool prolong,
+                   cudaStream_t s)
+{
+    if (nb == 0) return;
+    if (prolong)
+        pdl_launch(k_inject_prolong<T>, grid_for((long long)nb * nh, kThreads), kThreads, 0, s, nb, nh, nl, map, in,
+                   aux, out);
+    else
+        pdl_launch(k_inject_restrict<T>, grid_for((long long)nb * nl, kThreads), kThreads, 0, s, nb, nh, nl, map, in,
+                   out);
     g_kernel_launches++;
 }
 

@@ -159,6 +159,11 @@ void launch_loop_finish(const int* state, cudaGraphConditionalHandle loop, cudaS
 // gather: out[b*bs+c] = in[perm[b]*bs+c]; scatter: out[perm[b]*bs+c] = in[b*bs+c].
 template <class T>
 void launch_permute(int nb, int bs, const int* perm, const T* in, T* out, bool gather, cudaStream_t s);
+// The natural injection between face degrees (nh fine, nl coarse unknowns per face, fine block i ->
+// coarse block map[i]): prolong: out = aux + P in (aux may be NULL or out); else out = P^T in.
+template <class T>
+void launch_inject(int nb, int nh, int nl, const int* map, const T* in, const T* aux, T* out, bool prolong,
+                   cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Learned correction step (fhg_learned.cu)

@@ -821,6 +821,8 @@ template void launch_convert<double, float>(long long, const double*, float*, cu
 template void launch_convert<float, double>(long long, const float*, double*, cudaStream_t);
 template void launch_permute<double>(int, int, const int*, const double*, double*, bool, cudaStream_t);
 template void launch_permute<float>(int, int, const int*, const float*, float*, bool, cudaStream_t);
+template void launch_inject<double>(int, int, int, const int*, const double*, const double*, double*, bool, cudaStream_t);
+template void launch_inject<float>(int, int, int, const int*, const float*, const float*, float*, bool, cudaStream_t);
 
 
 // ---------------------------------------------------------------------------

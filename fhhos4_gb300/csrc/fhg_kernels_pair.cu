@@ -17,5 +17,6 @@ template void launch_jacobi<dfl>(const BsrView<dfl>&, const dfl*, long long, dfl
 template void launch_coarse<dfl>(int, const double*, const dfl*, dfl*, cudaStream_t);
 template void launch_convert<dfl, double>(long long, const dfl*, double*, cudaStream_t);
 template void launch_permute<dfl>(int, int, const int*, const dfl*, dfl*, bool, cudaStream_t);
+template void launch_inject<dfl>(int, int, int, const int*, const dfl*, const dfl*, dfl*, bool, cudaStream_t);
 
 }  // namespace fhg

@@ -206,3 +206,90 @@ def generate(dim: int, n: int, k: int = 1, **kw):
     bs = H.block_size
     H.close()
     return As, Ps, b, bs
+
+
+# ---------------------------------------------------------------------------
+# p-multigrid hierarchy (src/Solver/Multigrid/MultigridForHHO/P_MultigridForHHO.h)
+
+P_STRATEGIES = ("minus1", "minus2", "divide_by_2", "direct_to_low")
+
+
+def face_unknowns(dim: int, k: int) -> int:
+    """Face-basis functions of degree k (HHOParameters::nFaceUnknowns): k + 1 on edges, (k+1)(k+2)/2
+    on triangles."""
+    return k + 1 if dim == 2 else (k + 1) * (k + 2) // 2
+
+
+def natural_injection(n_faces: int, nh: int, nl: int) -> sp.csr_matrix:
+    """P_LevelForHHO::SetupProlongation (P_MultigridForHHO.h:69-92): on every face the nl functions of
+    the lower degree are the first nl of the nh of the higher one (hierarchical face bases), so P
+    holds a 1 at (f * nh + i, f * nl + i) for i < nl; R = P^T (P_MultigridForHHO.h:95-98)."""
+    f = np.arange(n_faces)[:, None]
+    i = np.arange(nl)[None, :]
+    rows, cols = (f * nh + i).ravel(), (f * nl + i).ravel()
+    return sp.csr_matrix((np.ones(rows.size), (rows, cols)), shape=(n_faces * nh, n_faces * nl))
+
+
+def p_degrees(dim: int, k: int, n_faces: int, strategy: str = "minus2", coarse_poly_degree: int = 1,
+              max_coarse_rows: int = 1000):
+    """Face degrees of the levels Multigrid::Setup creates with HP_CoarsStgy::P_only
+    (src/Solver/Multigrid/Multigrid.h:121-224, 353-361, 419-427): from k, a new level while the
+    current one has more than max_coarse_rows unknowns and a degree above coarse_poly_degree, its
+    degree lowered by P_CoarsStgy (Minus1, Minus2 by default, DivideBy2, DirectToLow) and never below
+    coarse_poly_degree (CoarsePolyDegree, 1 by default)."""
+    if strategy not in P_STRATEGIES:
+        raise ValueError(f"unknown p-coarsening strategy {strategy!r} ({', '.join(P_STRATEGIES)})")
+    if k <= coarse_poly_degree:
+        raise ValueError("p-coarsening cannot be performed because the polynomial degree of the fine level = "
+                         f"{coarse_poly_degree}")
+    degs = [k]
+    while n_faces * face_unknowns(dim, degs[-1]) > max_coarse_rows and degs[-1] > coarse_poly_degree:
+        d = degs[-1]
+        c = {"minus1": d - 1, "minus2": d - 2, "divide_by_2": d // 2, "direct_to_low": coarse_poly_degree}[strategy]
+        degs.append(max(c, coarse_poly_degree))
+    return degs
+
+
+def generate_p(dim: int, n: int, k: int, coarse_solver: str = "ch", strategy: str = "minus2",
+               coarse_poly_degree: int = 1, max_coarse_rows: int = 1000, **kw):
+    """The hierarchy of FCG with the p-multigrid preconditioner ("-s fcg -p p_mg", SolverFactory.h:201-211):
+    the p-levels on the fine mesh (face degrees from p_degrees, joined by the natural injection),
+    then, with the coarse solver "mg", the levels below the finest of the lowest degree's h-multigrid
+    (the coarse solver SolverFactory.h:289-309 builds for "-cs mg": one cycle with no pre-smoothing
+    and 3 (2D) or 6 (3D) post-smoothing steps). With "ch" (the default) the lowest degree is the
+    coarsest level, solved directly.
+
+    Returns (As, Ps, b, block_sizes, coarse_nu): coarse_nu is the pre and post smoothing of levels
+    >= 1 that reproduces the reference's cycle ((-1, -1): those of level 0)."""
+    if coarse_solver not in ("ch", "mg"):
+        raise ValueError("coarse solver 'ch' (direct) or 'mg' (one h-multigrid cycle)")
+    H = Hierarchy(dim, n, k, max_coarse_rows=max_coarse_rows, **kw)
+    try:
+        As, b, bss = [H.A(0)], H.b(), [H.block_size]
+    finally:
+        H.close()
+    n_faces = As[0].shape[0] // bss[0]
+    degs = p_degrees(dim, k, n_faces, strategy, coarse_poly_degree, max_coarse_rows)
+    if coarse_solver == "mg" and len(degs) > 2:
+        raise NotImplementedError("with the h-multigrid coarse solver the p-levels between the finest and the "
+                                  "lowest degree would need smoothing counts of their own")
+    if coarse_solver == "mg" and len(degs) == 1:
+        raise NotImplementedError("the fine level is already the lowest-degree level: the h-multigrid coarse "
+                                  "solver would smooth it with counts of its own")
+    Ps = []
+    for d in degs[1:]:
+        nl = face_unknowns(dim, d)
+        Ps.append(natural_injection(n_faces, bss[-1], nl))
+        bss.append(nl)
+        Hd = Hierarchy(dim, n, d, max_coarse_rows=max_coarse_rows, **kw)
+        try:
+            As.append(Hd.A(0))
+            if d == degs[-1] and coarse_solver == "mg":
+                for l in range(1, Hd.levels):
+                    Ps.append(Hd.P(l - 1))
+                    As.append(Hd.A(l))
+                    bss.append(nl)
+        finally:
+            Hd.close()
+    coarse_nu = (0, 3 if dim == 2 else 6) if coarse_solver == "mg" else (-1, -1)
+    return As, Ps, b, bss, coarse_nu

@@ -110,14 +110,21 @@ class Multigrid(IterativeSolver):
         self.ExtraPrecisions: List[str] = []
         self._As: List[sp.csr_matrix] = []
         self._Ps: List[sp.csr_matrix] = []
+        self._BlockSizes: Optional[List[int]] = None
         self._nLevels = nLevels
 
-    def SetHierarchy(self, As, Ps):
-        """A_0..A_{L-1} and P_0..P_{L-2} (P_l: level l rows, level l+1 columns), as built on the host."""
+    def SetHierarchy(self, As, Ps, block_sizes=None):
+        """A_0..A_{L-1} and P_0..P_{L-2} (P_l: level l rows, level l+1 columns), as built on the host.
+        block_sizes: one per level where they differ (a p-multigrid hierarchy, P_MultigridForHHO.h:
+        levels of lower face degree joined by the natural injection); None: BlockSizeForBlockSmoothers
+        on every level."""
         if len(Ps) != len(As) - 1:
             raise ValueError("need one prolongation per level except the coarsest")
+        if block_sizes is not None and len(block_sizes) != len(As):
+            raise ValueError("need one block size per level")
         self._As = [as_eigen_csr(A) for A in As]
         self._Ps = [as_eigen_csr(P) for P in Ps]
+        self._BlockSizes = None if block_sizes is None else [int(b) for b in block_sizes]
         self._nLevels = len(As)
 
     def NumberOfLevels(self) -> int:
@@ -203,11 +210,14 @@ class _KrylovOnGpu(IterativeSolver):
         bs = mg.BlockSizeForBlockSmoothers
         if bs <= 0:
             raise ValueError("BlockSizeForBlockSmoothers must be set (face DOFs)")
+        bss = mg._BlockSizes or [bs] * len(mg._As)
+        if bss[0] != bs:
+            raise ValueError("the finest level's block size is not BlockSizeForBlockSmoothers")
         if self._ctx is None:
             self._ctx = N.Context(self.Device)
         self._ctx.set_level(0, bs, self.Matrix)
         for l in range(1, len(mg._As)):
-            self._ctx.set_level(l, bs, mg._As[l])
+            self._ctx.set_level(l, bss[l], mg._As[l])
         for l, P in enumerate(mg._Ps):
             self._ctx.set_prolongation(l, P)
         self._ctx.setup(len(mg._As), self._options(mg))
@@ -258,15 +268,17 @@ class ConjugateGradient(_KrylovOnGpu):
     _krylov = "cg"
 
 
-def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: str = "bgs", post: str = "rbgs",
+def fcg_mg(As, Ps, block_size, tol: float = 1e-8, maxit: int = 200, pre: str = "bgs", post: str = "rbgs",
            precision: str = "fp64", krylov: str = "fcg", device: int = 0, autotune: bool = False,
            use_graphs: bool = True, outer_split: bool = True, cycle: str = "V", galerkin: bool = False,
            nu=(1, 1), coarse_nu=(-1, -1), gs_layout: str = "auto", omega: float = 1.0, extra=(),
-           replace_residual: bool = False, fused: bool = True):
-    """SolverFactory-style construction of "-s fcgmg -cycle V,1,1" (src/Solver/SolverFactory.h:156-200)."""
+           replace_residual: bool = False, fused: bool = True, colouring: bool = True):
+    """SolverFactory-style construction of "-s fcgmg -cycle V,1,1" (src/Solver/SolverFactory.h:156-200).
+    block_size: the face block size, or one per level (a p-multigrid hierarchy, hho.generate_p)."""
     mg = Multigrid(len(As))
-    mg.SetHierarchy(As, Ps)
-    mg.BlockSizeForBlockSmoothers = block_size
+    per_level = np.ndim(block_size) > 0
+    mg.SetHierarchy(As, Ps, list(block_size) if per_level else None)
+    mg.BlockSizeForBlockSmoothers = int(block_size[0]) if per_level else block_size
     mg.PreSmootherCode, mg.PostSmootherCode = pre, post
     mg.VCyclePrecision = precision
     mg.Autotune = autotune
@@ -278,6 +290,7 @@ def fcg_mg(As, Ps, block_size: int, tol: float = 1e-8, maxit: int = 200, pre: st
     mg.GsLayout = gs_layout
     mg.RelaxationParameter = omega
     mg.ExtraPrecisions = list(extra)
+    mg.Colouring = colouring
     solver = FlexibleConjugateGradient(1) if krylov == "fcg" else ConjugateGradient()
     solver.Precond = SolverPreconditioner(mg)
     solver.Tolerance = tol

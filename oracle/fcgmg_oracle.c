@@ -382,7 +382,7 @@ static void ldlt_solve(const orc_ldlt* F, const double* b, double* x)
 /* V-cycle and Krylov drivers                                                */
 
 typedef struct {
-    int nlevels, bs;
+    int nlevels;
     const orc_csr* A;
     const orc_csr* P;
     orc_csr* R;
@@ -503,10 +503,21 @@ int orc_fcgmg_solve(int nlevels, int bs, const orc_csr* A, const orc_csr* P,
                     const double* b, double* x, const orc_options* opt,
                     double* history, int* iterations)
 {
+    int* bs_l = (int*)malloc(sizeof(int) * (size_t)(nlevels > 0 ? nlevels : 1));
+    for (int l = 0; l < nlevels; l++) bs_l[l] = bs;
+    int rc = orc_fcgmg_solve_levels(nlevels, bs_l, A, P, b, x, opt, history, iterations);
+    free(bs_l);
+    return rc;
+}
+
+int orc_fcgmg_solve_levels(int nlevels, const int* bs, const orc_csr* A, const orc_csr* P,
+                           const double* b, double* x, const orc_options* opt,
+                           double* history, int* iterations)
+{
     const double t0 = now_s();
     orc_mg mg;
     memset(&mg, 0, sizeof(mg));
-    mg.nlevels = nlevels; mg.bs = bs; mg.A = A; mg.P = P; mg.opt = opt;
+    mg.nlevels = nlevels; mg.A = A; mg.P = P; mg.opt = opt;
     int rc = 0;
     mg.R = (orc_csr*)calloc((size_t)(nlevels > 1 ? nlevels - 1 : 1), sizeof(orc_csr));
     mg.D = (orc_blockdiag*)calloc((size_t)nlevels, sizeof(orc_blockdiag));
@@ -533,7 +544,7 @@ int orc_fcgmg_solve(int nlevels, int bs, const orc_csr* A, const orc_csr* P,
         orc_transpose(&P[l], rp, ci, va);
         mg.R[l].n_rows = P[l].n_cols; mg.R[l].n_cols = P[l].n_rows;
         mg.R[l].rowptr = rp; mg.R[l].colidx = ci; mg.R[l].vals = va;
-        if (blockdiag_setup(&mg.D[l], &A[l], bs)) rc = 2;
+        if (blockdiag_setup(&mg.D[l], &A[l], bs[l])) rc = 2;
         mg.r[l] = (double*)malloc(sizeof(double) * (size_t)A[l].n_rows);
         mg.tmp[l] = (double*)malloc(sizeof(double) * (size_t)A[l].n_rows);
         mg.rc[l] = (double*)malloc(sizeof(double) * (size_t)A[l + 1].n_rows);

@@ -74,6 +74,12 @@ void orc_colour_permutation(int nb, const int* colour, int ncolours, int* perm);
 int orc_fcgmg_solve(int nlevels, int bs, const orc_csr* A, const orc_csr* P,
                     const double* b, double* x, const orc_options* opt,
                     double* history, int* iterations);
+/* The same with a block size per level (bs[l]): the p-multigrid of P_MultigridForHHO, whose levels
+ * differ in face degree (src/Solver/Multigrid/MultigridForHHO/P_MultigridForHHO.h), P[l] the natural
+ * injection between them. */
+int orc_fcgmg_solve_levels(int nlevels, const int* bs, const orc_csr* A, const orc_csr* P,
+                           const double* b, double* x, const orc_options* opt,
+                           double* history, int* iterations);
 
 /* Wall seconds of the last orc_fcgmg_solve: setup (transposes, diagonal LU, coarse LDL^T)
  * and the Krylov iterations. */

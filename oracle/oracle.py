@@ -53,7 +53,8 @@ def build() -> str:
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
+        srcs = [os.path.join(HERE, f) for f in ("fcgmg_oracle.c", "fcgmg_oracle.h")]
+        if not os.path.exists(LIB_PATH) or any(os.path.getmtime(f) > os.path.getmtime(LIB_PATH) for f in srcs):
             build()
         _lib = C.CDLL(LIB_PATH)
     return _lib
@@ -156,8 +157,9 @@ def last_timing():
 
 def fcgmg_solve(As, Ps, b, bs, pre="bgs", post="rbgs", krylov="fcg", tol=1e-8, maxit=200,
                 pre_iterations=1, post_iterations=1, cycle="V", coarse_iterations=(-1, -1), omega=1.0):
-    """Returns (x, history, iterations, status). coarse_iterations: smoothing steps on levels >= 1
-    (-1: those of level 0, the reference's behaviour). omega: Multigrid::RelaxationParameter, the
+    """Returns (x, history, iterations, status). bs: the block size, or one per level (a p-multigrid
+    hierarchy, whose P between face degrees is the natural injection). coarse_iterations: smoothing
+    steps on levels >= 1 (-1: those of level 0, the reference's behaviour). omega: Multigrid::RelaxationParameter, the
     relaxation of "bj" and, when not 1, block SOR in place of the Gauss-Seidel codes
     (SmootherFactory.h:37-100); "bj23" keeps 2/3."""
     keep: list = []
@@ -178,7 +180,8 @@ def fcgmg_solve(As, Ps, b, bs, pre="bgs", post="rbgs", krylov="fcg", tol=1e-8, m
     x = np.zeros(As[0].shape[0])
     hist = np.zeros(maxit + 1)
     iters = C.c_int(0)
-    rc = lib().orc_fcgmg_solve(C.c_int(nl), C.c_int(bs), Aarr, Parr, _dptr(b), _dptr(x),
+    bs_l = np.ascontiguousarray(np.broadcast_to(np.asarray(bs, dtype=np.int32), (nl,)), dtype=np.int32)
+    rc = lib().orc_fcgmg_solve_levels(C.c_int(nl), _iptr(bs_l), Aarr, Parr, _dptr(b), _dptr(x),
                                C.byref(opts), _dptr(hist), C.byref(iters))
     return x, hist[: iters.value + 1].copy(), iters.value, rc
 
@@ -186,25 +189,30 @@ def fcgmg_solve(As, Ps, b, bs, pre="bgs", post="rbgs", krylov="fcg", tol=1e-8, m
 def permute_hierarchy(As, Ps, b, bs, perms):
     """Block-permute a hierarchy: A'_l = Pi_l A_l Pi_l^T, P'_l = Pi_l P_l Pi_{l+1}^T, b' = Pi_0 b.
 
-    perms[l][new_block] = old_block on level l.
+    perms[l][new_block] = old_block on level l; bs: the block size, or one per level.
     """
-    def scalar_perm(pb):
-        return (pb[:, None] * bs + np.arange(bs)[None, :]).ravel()
+    bs_l = np.broadcast_to(np.asarray(bs), (len(As),))
 
-    sps = [scalar_perm(np.asarray(p)) for p in perms]
+    def scalar_perm(pb, b):
+        return (pb[:, None] * b + np.arange(b)[None, :]).ravel()
+
+    sps = [scalar_perm(np.asarray(p), int(b)) for p, b in zip(perms, bs_l)]
     As2 = [as_csr(as_csr(A)[s][:, s]) for A, s in zip(As, sps)]
     Ps2 = [as_csr(as_csr(P)[sps[l]][:, sps[l + 1]]) for l, P in enumerate(Ps)]
     return As2, Ps2, np.asarray(b)[sps[0]]
 
 
 def colour_perms(As, bs):
-    """Greedy-colouring block permutation of every level (the coarsest stays natural)."""
+    """Greedy-colouring block permutation of every level (the coarsest stays natural); bs: the block
+    size, or one per level."""
     perms, ncol = [], []
+    bs_l = np.broadcast_to(np.asarray(bs), (len(As),))
     for l, A in enumerate(As):
-        nb = A.shape[0] // bs
+        b = int(bs_l[l])
+        nb = A.shape[0] // b
         if l == len(As) - 1:
             perms.append(np.arange(nb, dtype=np.int32)); ncol.append(0)
             continue
-        c, nc = greedy_colouring(A, bs)
+        c, nc = greedy_colouring(A, b)
         perms.append(colour_permutation(c, nc)); ncol.append(nc)
     return perms, ncol

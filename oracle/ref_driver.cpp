@@ -12,6 +12,14 @@
 //         residual history captured through IterativeSolver::OnIterationEnd
 //         (src/Solver/IterativeSolver.h:224-227) and the solution x.
 //
+//   genp  <dim> <n> <k> <outdir> [--coarse-solver ch|mg]
+//         The same pipeline with the p-multigrid preconditioner ("-s fcg -p p_mg", P_MultigridForHHO
+//         through SolverFactory.h:201-211, P_CS Minus2 and CoarsePolyDegree 1 as defaulted) and the
+//         coarse solver "-cs ch" (Cholesky of the lowest degree) or "-cs mg" (one h-multigrid cycle
+//         on it, SolverFactory.h:299-308). Dumps the p-levels' A and P (the natural injection),
+//         then, with "-cs mg", the levels of that coarse multigrid below its finest one, numbered on
+//         from the p-levels; the block size of every level; the history and x.
+//
 //   solve <dir> [--smoothers pre,post] [--krylov fcg|cg] [--cycle V|W|K] [--tol t] [--maxit m] [--omega w]
 //         Reads a hierarchy (possibly re-ordered by the caller) from <dir>, feeds it
 //         to the reference's own Multigrid / BlockGaussSeidel / EigenSparseCholesky /
@@ -119,7 +127,8 @@ static void ParseSmoothers(const std::string& s, std::string& pre, std::string& 
 // ---------------------------------------------------------------------------
 // gen: the reference pipeline end to end.
 template <int D>
-static int RunGen(int n, int k, const std::string& outdir, const std::string& pre, const std::string& post, bool solve)
+static int RunGen(int n, int k, const std::string& outdir, const std::string& pre, const std::string& post, bool solve,
+                  const std::string& precond = "mg", const std::string& coarseSolver = "ch")
 {
 	ProgramArguments args;
 	args.Problem.Dimension = D;
@@ -136,7 +145,7 @@ static int RunGen(int n, int k, const std::string& outdir, const std::string& pr
 	args.Discretization.FaceBasisCode = D == 2 ? "legendre" : "monomials";
 	args.Discretization.OrthogonalizeFaceBasesCode = D == 2 ? 0 : 1;
 	args.Solver.SolverCode = "fcg";
-	args.Solver.PreconditionerCode = "mg";
+	args.Solver.PreconditionerCode = precond;
 	args.Solver.Tolerance = 1e-8;
 	args.Solver.MaxIterations = 200;
 	args.Solver.PrintIterationResults = false;
@@ -146,7 +155,7 @@ static int RunGen(int n, int k, const std::string& outdir, const std::string& pr
 	args.Solver.MG.PostSmootherCode = post;
 	args.Solver.MG.PreSmoothingIterations = 1;
 	args.Solver.MG.PostSmoothingIterations = 1;
-	args.Solver.MG.CoarseSolverCode = "ch";
+	args.Solver.MG.CoarseSolverCode = coarseSolver;
 	args.Actions.LogAssembly = false;
 	Utils::ProgramArgs = args;
 	GaussLegendre::Init();
@@ -208,19 +217,43 @@ static int RunGen(int n, int k, const std::string& outdir, const std::string& pr
 	Multigrid* mg = dynamic_cast<Multigrid*>(PrecondSolver(fcg->Precond));
 	if (!mg) { fprintf(stderr, "unexpected preconditioner type\n"); return 3; }
 	int nLevels = 0;
+	std::vector<int> blockSizes;
+	Level* last = nullptr;
 	for (Level* l = MGFine(mg); l; l = l->CoarserLevel, nLevels++)
 	{
 		std::string p = outdir + "/L" + std::to_string(l->Number);
 		DumpCSR(p + "_A", *l->OperatorMatrix);
 		if (!l->IsCoarsestLevel())
 			DumpCSR(p + "_P", LevelP(l));
+		blockSizes.push_back(l->BlockSizeForBlockSmoothers());
+		last = l;
+	}
+	const int pLevels = nLevels;
+	// p-multigrid with an h-multigrid coarse solver: its levels below its finest (which is the
+	// lowest-degree p-level), numbered on.
+	if (Multigrid* inner = precond == "p_mg" ? dynamic_cast<Multigrid*>(mg->CoarseSolver) : nullptr)
+	{
+		Level* f = MGFine(inner);
+		if (f && !f->IsCoarsestLevel())
+			DumpCSR(outdir + "/L" + std::to_string(last->Number) + "_P", LevelP(f));
+		int number = last->Number;
+		for (Level* l = f ? f->CoarserLevel : nullptr; l; l = l->CoarserLevel, nLevels++)
+		{
+			std::string p = outdir + "/L" + std::to_string(++number);
+			DumpCSR(p + "_A", *l->OperatorMatrix);
+			if (!l->IsCoarsestLevel())
+				DumpCSR(p + "_P", LevelP(l));
+			blockSizes.push_back(l->BlockSizeForBlockSmoothers());
+		}
 	}
 	WriteArray(outdir + "/b.f64", pb->b.data(), (size_t)pb->b.rows());
+	WriteArray(outdir + "/block_sizes.i32", blockSizes.data(), blockSizes.size());
 
 	std::ostringstream meta;
 	meta << "{\"dim\": " << D << ", \"n\": " << n << ", \"k\": " << k << ", \"block_size\": " << bs
-	     << ", \"levels\": " << nLevels << ", \"pre\": \"" << pre << "\", \"post\": \"" << post << "\""
-	     << ", \"setup_s\": " << setupTimer.Elapsed().InSeconds();
+	     << ", \"levels\": " << nLevels << ", \"p_levels\": " << pLevels << ", \"pre\": \"" << pre
+	     << "\", \"post\": \"" << post << "\", \"precond\": \"" << precond << "\", \"coarse_solver\": \""
+	     << coarseSolver << "\", \"setup_s\": " << setupTimer.Elapsed().InSeconds();
 
 	if (solve)
 	{
@@ -357,6 +390,7 @@ int main(int argc, char** argv)
 	double tol = 1e-8, omega = 1.0;
 	int maxit = 200;
 	bool solve = true;
+	std::string coarseSolver = "ch";
 	std::vector<std::string> pos;
 	for (int i = 2; i < argc; i++)
 	{
@@ -368,6 +402,7 @@ int main(int argc, char** argv)
 		else if (a == "--maxit" && i + 1 < argc) maxit = atoi(argv[++i]);
 		else if (a == "--no-solve") solve = false;
 		else if (a == "--cycle" && i + 1 < argc) cycle = argv[++i][0];
+		else if (a == "--coarse-solver" && i + 1 < argc) coarseSolver = argv[++i];
 		else pos.push_back(a);
 	}
 	std::cout.setstate(std::ios_base::failbit); // the reference logs to stdout; keep it quiet
@@ -377,6 +412,12 @@ int main(int argc, char** argv)
 		int dim = atoi(pos[0].c_str()), n = atoi(pos[1].c_str()), k = atoi(pos[2].c_str());
 		if (dim == 2) rc = RunGen<2>(n, k, pos[3], pre, post, solve);
 		else rc = RunGen<3>(n, k, pos[3], pre, post, solve);
+	}
+	else if (mode == "genp" && pos.size() == 4)
+	{
+		int dim = atoi(pos[0].c_str()), n = atoi(pos[1].c_str()), k = atoi(pos[2].c_str());
+		if (dim == 2) rc = RunGen<2>(n, k, pos[3], pre, post, solve, "p_mg", coarseSolver);
+		else rc = RunGen<3>(n, k, pos[3], pre, post, solve, "p_mg", coarseSolver);
 	}
 	else if (mode == "solve" && pos.size() == 1)
 		rc = RunSolve(pos[0], pre, post, krylov, tol, maxit, cycle, omega);

@@ -17,6 +17,11 @@ Only ``hist_*`` summaries are kept for the large cases (``--histories-only``).
 
 ``--add-sor`` adds the reference's block SOR (bsor/rbsor and sbsor, omega 1.2) to full cases.
 
+``--p-multigrid`` writes the p-multigrid cases (``p_*.npz``): the reference's FCG with its
+p-multigrid preconditioner ("-s fcg -p p_mg", P_MultigridForHHO) with the coarse solvers "ch" and
+"mg" (``hist_ch``/``x_ch``, ``hist_mg``/``x_mg``), the block size of every level, and per level
+A_l v_l for a seeded v_l (``Av{l}``) with A_l's shape and entry count instead of A_l itself.
+
 Usage:  python tests/golden/make_golden.py [case ...] [--histories-only | --add-k-cycle | --add-sor]
 """
 from __future__ import annotations
@@ -188,6 +193,51 @@ def add_k_cycle(name):
     print(f"{name}: K-cycle iterations {len(hist_k) - 1}", flush=True)
 
 
+# name -> (dim, n, k): face degree k lowered to 1 on the same mesh (P_CS Minus2, CoarsePolyDegree 1)
+P_CASES = {
+    "p_tri2d_n16_k3": (2, 16, 3),    # block sizes 4 -> 2
+    "p_tet3d_n4_k2": (3, 4, 2),      # block sizes 6 -> 3
+}
+
+
+def probe_vector(l, n):
+    """The seeded vector the fixtures multiply level l's operator with."""
+    return np.random.default_rng(1000 + l).standard_normal(n)
+
+
+def make_p_case(name, dim, n, k):
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for cs in ("ch", "mg"):
+            d = os.path.join(tmp, cs)
+            os.makedirs(d)
+            subprocess.run([O.REF_DRIVER, "genp", str(dim), str(n), str(k), d, "--coarse-solver", cs], check=True)
+            meta = json.load(open(os.path.join(d, "meta.json")))
+            out[f"hist_{cs}"] = np.fromfile(f"{d}/history.f64")
+            out[f"x_{cs}"] = np.fromfile(f"{d}/x.f64")
+            out[f"levels_{cs}"] = meta["levels"]
+            if cs == "mg":
+                L = meta["levels"]
+                out["block_sizes"] = np.fromfile(f"{d}/block_sizes.i32", dtype=np.int32)
+                out["p_levels"] = meta["p_levels"]
+                out["b"] = np.fromfile(f"{d}/b.f64")
+                for l in range(L):
+                    A = load_csr(f"{d}/L{l}_A")
+                    out[f"A{l}_shape"] = np.asarray(A.shape, dtype=np.int64)
+                    out[f"A{l}_nnz"] = A.nnz
+                    out[f"Av{l}"] = A @ probe_vector(l, A.shape[0])
+                for l in range(L - 1):
+                    P = load_csr(f"{d}/L{l}_P")
+                    out[f"P{l}_shape"] = np.asarray(P.shape, dtype=np.int64)
+                    out[f"P{l}_nnz"] = P.nnz
+                    out[f"Pv{l}"] = P @ probe_vector(100 + l, P.shape[1])
+    out.update(dim=dim, n=n, k=k)
+    path = os.path.join(GOLDEN, name + ".npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: block sizes {[int(v) for v in out['block_sizes']]}, iterations ch/mg {len(out['hist_ch']) - 1}/"
+          f"{len(out['hist_mg']) - 1}, size={os.path.getsize(path) / 1e6:.2f} MB", flush=True)
+
+
 def build_ref_driver():
     """The reference harness, compiled from the read-only reference checkout (FHHOS4_REFERENCE)."""
     ref = os.environ.get("FHHOS4_REFERENCE", "/root/reference")
@@ -196,6 +246,11 @@ def build_ref_driver():
 
 def main(argv):
     histories_only = "--histories-only" in argv
+    if "--p-multigrid" in argv:
+        build_ref_driver()
+        for name in [a for a in argv if not a.startswith("--")] or list(P_CASES):
+            make_p_case(name, *P_CASES[name])
+        return
     for flag, fn in (("--add-k-cycle", add_k_cycle), ("--add-sor", add_sor)):
         if flag in argv:
             build_ref_driver()
