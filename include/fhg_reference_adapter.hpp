@@ -5,7 +5,9 @@
 //
 // GpuFcgMg<Dim> is an IterativeSolver (src/Solver/IterativeSolver.h:6-191): Setup(A) runs the
 // reference's own MultigridForHHO<Dim>::Setup on the host (src/Solver/Multigrid/Multigrid.h:88-313),
-// hands every level's operator and prolongation to the GPU and builds the device hierarchy;
+// or P_MultigridForHHO<Dim>'s for the p-multigrid preconditioner (with, for "-cs mg", the
+// MultigridForHHO coarse solver of the lowest degree SolverFactory.h:289-309 builds), hands every
+// level's operator, block size and prolongation to the GPU and builds the device hierarchy;
 // Solve(b, "0") runs FCG(1) + V-cycle entirely on the GPU (FlexibleConjugateGradient.h:47-171).
 // A nonzero status becomes Utils::FatalError (src/Utils/Utils.h:258-264), the reference's
 // error convention. No CPU fallback exists for the solve.
@@ -24,29 +26,50 @@ template <int Dim>
 class GpuFcgMg : public IterativeSolver
 {
     fhg_ctx* _ctx = nullptr;
-    MultigridForHHO<Dim>* _mg = nullptr;  // host-side hierarchy builder (reference code)
+    Multigrid* _mg = nullptr;  // host-side hierarchy builder (reference code)
+    bool _p = false;           // p-multigrid: P_MultigridForHHO, its levels' block sizes differ
     fhg_options _opts;
 
 public:
     GpuFcgMg(Diffusion_HHO<Dim>* problem, const ProgramArguments& args, int blockSize, int device = 0)
     {
         _opts = MapArguments(args);
-        _mg = new MultigridForHHO<Dim>(args.Solver.MG.Levels);
-        _mg->UseHigherOrderReconstruction = args.Solver.MG.UseHigherOrderReconstruction;
-        _mg->H_Prolongation = args.Solver.MG.GMG_H_Prolong;
-        _mg->UseHeterogeneousWeighting = args.Solver.MG.UseHeterogeneousWeighting;
-        _mg->InitializeWithProblem(problem);
-        _mg->BlockSizeForBlockSmoothers = blockSize;
-        _mg->MatrixMaxSizeForCoarsestLevel = args.Solver.MG.MatrixMaxSizeForCoarsestLevel;
-        _mg->UseGalerkinOperator = args.Solver.MG.UseGalerkinOperator;
-        _mg->H_CS = args.Solver.MG.H_CS;
-        _mg->FaceCoarseningStgy = args.Solver.MG.FaceCoarseningStgy;
-        _mg->BdryFaceCollapsing = args.Solver.MG.BoundaryFaceCollapsing;
-        _mg->NumberOfMeshes = args.Solver.MG.NumberOfMeshes;
-        _mg->CoarseningFactor = args.Solver.MG.CoarseningFactor;
-        _mg->PreSmoothingIterations = 0;   // smoothers run on the GPU: no host smoother setup needed
-        _mg->PostSmoothingIterations = 0;
-        _mg->CoarseSolver = new EigenSparseCholesky();
+        const MultigridArguments& m = args.Solver.MG;
+        _p = UsesPMultigrid(args.Solver);
+        if (_p)
+        {
+            // SolverFactory.h:201-211 with SetMultigridParameters; the coarse solver of "-cs mg" as
+            // SolverFactory.h:289-309 configures it (the other fields at their defaults), its
+            // problem set by P_MultigridForHHO::InitializeCoarseSolver
+            auto* pmg = new P_MultigridForHHO<Dim>(problem);
+            pmg->MatrixMaxSizeForCoarsestLevel = m.MatrixMaxSizeForCoarsestLevel;
+            pmg->UseGalerkinOperator = m.UseGalerkinOperator;
+            pmg->P_CS = m.P_CS;
+            pmg->HP_CS = HP_CoarsStgy::P_only;
+            pmg->PreSmoothingIterations = 0;   // smoothers run on the GPU: no host smoother setup needed
+            pmg->PostSmoothingIterations = 0;
+            if (m.CoarseSolverCode == "mg")
+            {
+                MultigridArguments c;
+                c.GMG_H_Prolong = m.GMG_H_Prolong;
+                c.H_CS = m.H_CS;
+                c.FaceCoarseningStgy = m.FaceCoarseningStgy;
+                auto* inner = new MultigridForHHO<Dim>(0);
+                ConfigureH(inner, c);
+                pmg->CoarseSolver = inner;
+            }
+            else
+                pmg->CoarseSolver = new EigenSparseCholesky();
+            _mg = pmg;
+        }
+        else
+        {
+            auto* mg = new MultigridForHHO<Dim>(m.Levels);
+            ConfigureH(mg, m);
+            mg->InitializeWithProblem(problem);
+            mg->BlockSizeForBlockSmoothers = blockSize;
+            _mg = mg;
+        }
         this->Tolerance = args.Solver.Tolerance;
         this->MaxIterations = args.Solver.MaxIterations;
         Check(fhg_create(&_ctx, device));
@@ -68,17 +91,30 @@ public:
         _opts.max_iterations = this->MaxIterations;
         Level* fine = _mg->*(&fhg_detail::MultigridFineLevel::_fineLevel);
         int l = 0;
+        Level* last = nullptr;
         for (Level* lev = fine; lev; lev = lev->CoarserLevel, l++)
         {
-            const SparseMatrix& Al = *lev->OperatorMatrix;
-            Check(fhg_set_level(_ctx, l, _mg->BlockSizeForBlockSmoothers, (int)Al.rows(), Al.outerIndexPtr(),
-                                Al.innerIndexPtr(), Al.valuePtr()));
-            if (!lev->IsCoarsestLevel())
+            SetLevel(l, lev, _p ? lev->BlockSizeForBlockSmoothers() : _mg->BlockSizeForBlockSmoothers);
+            last = lev;
+        }
+        // p-multigrid with the h-multigrid coarse solver: its levels below its finest (the lowest
+        // degree, already level l - 1) continue the hierarchy; its one cycle (no pre-smoothing,
+        // 3 / 6 post-smoothing steps) runs as the coarse part of the V-cycle.
+        if (Multigrid* inner = _p ? dynamic_cast<Multigrid*>(_mg->CoarseSolver) : nullptr)
+        {
+            if (l != 2)
+                Utils::FatalError("GPU solver: with '-cs mg' the p-multigrid must have exactly two levels (the "
+                                  "finest and the lowest degree): other levels would need smoothing counts of their own");
+            Level* f = inner->*(&fhg_detail::MultigridFineLevel::_fineLevel);
+            const int bs = last->BlockSizeForBlockSmoothers();
+            if (f && !f->IsCoarsestLevel())
             {
-                const SparseMatrix& P = lev->*(&fhg_detail::LevelProlongation::P);
-                Check(fhg_set_prolongation(_ctx, l, (int)P.rows(), (int)P.cols(), P.outerIndexPtr(),
+                const SparseMatrix& P = f->*(&fhg_detail::LevelProlongation::P);
+                Check(fhg_set_prolongation(_ctx, l - 1, (int)P.rows(), (int)P.cols(), P.outerIndexPtr(),
                                            P.innerIndexPtr(), P.valuePtr()));
             }
+            for (Level* lev = f ? f->CoarserLevel : nullptr; lev; lev = lev->CoarserLevel, l++)
+                SetLevel(l, lev, bs);
         }
         Check(fhg_setup(_ctx, l, &_opts));
     }
@@ -113,6 +149,46 @@ private:
             Utils::FatalError(std::string("GPU solver: ") + fhg_last_error(_ctx));
     }
 
+    // Level l of the device hierarchy: the level's operator with its block size, and its
+    // prolongation unless it is the coarsest.
+    void SetLevel(int l, Level* lev, int blockSize)
+    {
+        const SparseMatrix& Al = *lev->OperatorMatrix;
+        Check(fhg_set_level(_ctx, l, blockSize, (int)Al.rows(), Al.outerIndexPtr(), Al.innerIndexPtr(),
+                            Al.valuePtr()));
+        if (!lev->IsCoarsestLevel())
+        {
+            const SparseMatrix& P = lev->*(&fhg_detail::LevelProlongation::P);
+            Check(fhg_set_prolongation(_ctx, l, (int)P.rows(), (int)P.cols(), P.outerIndexPtr(), P.innerIndexPtr(),
+                                       P.valuePtr()));
+        }
+    }
+
+    // The h-multigrid fields SolverFactory sets for "-s mg" (SolverFactory.h:183-200, 236-256).
+    static void ConfigureH(MultigridForHHO<Dim>* mg, const MultigridArguments& m)
+    {
+        mg->UseHigherOrderReconstruction = m.UseHigherOrderReconstruction;
+        mg->H_Prolongation = m.GMG_H_Prolong;
+        mg->UseHeterogeneousWeighting = m.UseHeterogeneousWeighting;
+        mg->MatrixMaxSizeForCoarsestLevel = m.MatrixMaxSizeForCoarsestLevel;
+        mg->UseGalerkinOperator = m.UseGalerkinOperator;
+        mg->H_CS = m.H_CS;
+        mg->FaceCoarseningStgy = m.FaceCoarseningStgy;
+        mg->BdryFaceCollapsing = m.BoundaryFaceCollapsing;
+        mg->NumberOfMeshes = m.NumberOfMeshes;
+        mg->CoarseningFactor = m.CoarseningFactor;
+        mg->PreSmoothingIterations = 0;   // smoothers run on the GPU: no host smoother setup needed
+        mg->PostSmoothingIterations = 0;
+        mg->CoarseSolver = new EigenSparseCholesky();
+    }
+
+    // "-s fcgp_mg" / "-s cgp_mg" or "-s fcg|cg -p p_mg" (SolverFactory.h:125-181, 201-211)
+    static bool UsesPMultigrid(const SolverArguments& s)
+    {
+        return s.SolverCode == "fcgp_mg" || s.SolverCode == "cgp_mg" ||
+               ((s.SolverCode == "fcg" || s.SolverCode == "cg") && s.PreconditionerCode == "p_mg");
+    }
+
     // The solver arguments the reference's SolverFactory reads for "-s fcgmg" / "-s cgmg"
     // (SolverFactory.h:125-200, SetMultigridParameters SolverFactory.h:236-310), mapped to
     // fhg_options; an argument the GPU path does not implement is an error, never ignored.
@@ -123,14 +199,15 @@ public:
         fhg_default_options(&o);
         const SolverArguments& s = args.Solver;
         const string& code = s.SolverCode;
-        const bool pc_mg = s.PreconditionerCode == "mg";
-        if (code == "fcgmg" || (code == "fcg" && pc_mg))
+        const bool pc_mg = s.PreconditionerCode == "mg" || s.PreconditionerCode == "p_mg";
+        const bool p = UsesPMultigrid(s);
+        if (code == "fcgmg" || code == "fcgp_mg" || (code == "fcg" && pc_mg))
             o.krylov = FHG_KRYLOV_FCG;
-        else if (code == "cgmg" || (code == "cg" && pc_mg))
+        else if (code == "cgmg" || code == "cgp_mg" || (code == "cg" && pc_mg))
             o.krylov = FHG_KRYLOV_CG;
         else
             Utils::FatalError("GPU solver: solver code '" + code + "' (preconditioner '" + s.PreconditionerCode +
-                              "') is not supported; use fcgmg or cgmg");
+                              "') is not supported; use fcgmg, cgmg, fcgp_mg or cgp_mg");
         if (s.StoppingCrit != StoppingCriteria::NormalizedResidual)
             Utils::FatalError("GPU solver: only the normalized-residual stopping criterion is supported");
         if (s.InitialGuessCode != "0")
@@ -146,9 +223,19 @@ public:
             Utils::FatalError(std::string("GPU solver: multigrid cycle '") + mg.CycleLetter + "' is not supported");
         if (mg.CoarseLevelChangeSmoothingCoeff != 0)
             Utils::FatalError("GPU solver: level-dependent smoothing steps (-cycle V,a,b,+c) are not supported");
-        if (mg.CoarseSolverCode != "ch" && mg.CoarseSolverCode != "lu")
+        if (p && mg.CoarseSolverCode == "mg")
+        {
+            // one cycle of the lowest degree's h-multigrid (SolverFactory.h:299-308), V-cycle with no
+            // pre-smoothing and 3 (2D) or 6 (3D) post-smoothing steps
+            if (mg.CycleLetter != 'V')
+                Utils::FatalError("GPU solver: '-cs mg' under the p-multigrid needs a V-cycle");
+            o.coarse_pre_iterations = 0;
+            o.coarse_post_iterations = Dim == 2 ? 3 : 6;
+        }
+        else if (mg.CoarseSolverCode != "ch" && mg.CoarseSolverCode != "lu")
             Utils::FatalError("GPU solver: coarse solver '" + mg.CoarseSolverCode +
-                              "' is not supported; the coarsest level is solved directly (ch / lu)");
+                              "' is not supported; the coarsest level is solved directly (ch / lu)" +
+                              (p ? " or, under the p-multigrid, by one h-multigrid cycle (mg)" : ""));
         o.galerkin = mg.UseGalerkinOperator ? 1 : 0;
         o.pre_iterations = mg.PreSmoothingIterations;
         o.post_iterations = mg.PostSmoothingIterations;

@@ -19,7 +19,8 @@ static void print_options(const char* name, const ProgramArguments& a)
     std::cout << name << " krylov=" << o.krylov << " pre=" << o.pre_smoother << " post=" << o.post_smoother
               << " npre=" << o.pre_iterations << " npost=" << o.post_iterations << " omega=" << o.omega
               << " w_loops=" << o.w_loops << " galerkin=" << o.galerkin << " tol=" << o.tolerance
-              << " maxit=" << o.max_iterations << std::endl;
+              << " maxit=" << o.max_iterations << " cpre=" << o.coarse_pre_iterations
+              << " cpost=" << o.coarse_post_iterations << std::endl;
 }
 
 static int map_check()
@@ -51,6 +52,14 @@ static int map_check()
     k.Solver.MG.PreSmootherCode = "bj23";
     k.Solver.MG.PostSmootherCode = "<symmetric smoother>";
     print_options("cgmg_k_bj23", k);
+    ProgramArguments p;
+    p.Solver.SolverCode = "fcgp_mg";
+    print_options("fcgp_mg", p);
+    ProgramArguments q;
+    q.Solver.SolverCode = "cg";
+    q.Solver.PreconditionerCode = "p_mg";
+    q.Solver.MG.CoarseSolverCode = "mg";
+    print_options("cg_p_mg_cs_mg", q);
     return 0;
 }
 
@@ -67,6 +76,13 @@ int main(int argc, char** argv)
         if (what == "smoother") a.Solver.MG.PreSmootherCode = "gs";
         if (what == "coarse") a.Solver.MG.CoarseSolverCode = "fcgmg";
         if (what == "variable") a.Solver.MG.CoarseLevelChangeSmoothingCoeff = 1;
+        if (what == "coarse_mg") a.Solver.MG.CoarseSolverCode = "mg";   // only under the p-multigrid
+        if (what == "p_mg_w")
+        {
+            a.Solver.SolverCode = "fcgp_mg";
+            a.Solver.MG.CoarseSolverCode = "mg";
+            a.Solver.MG.CycleLetter = 'W';
+        }
         print_options("accepted", a);
         return 0;
     }

@@ -32,7 +32,7 @@ def test_adapter_argument_mapping():
     m = _mapped()
     # fcgmg defaults: V(1,1), bgs / rbgs, omega 1, tolerance 1e-8, 200 iterations (ProgramArguments.h:60-95)
     assert m["default"] == dict(krylov="0", pre="0", post="1", npre="1", npost="1", omega="1", w_loops="1",
-                                galerkin="0", tol="1e-08", maxit="200")
+                                galerkin="0", tol="1e-08", maxit="200", cpre="-1", cpost="-1")
     # "<symmetric smoother>" after abgs with an odd step count is "rabgs" (SolverFactory.h:270-280)
     assert (m["abgs3_symmetric"]["pre"], m["abgs3_symmetric"]["post"]) == ("5", "6")
     # hbgs -> hrbgs, both the multicolour forward / backward sweeps
@@ -44,9 +44,14 @@ def test_adapter_argument_mapping():
     # cgmg, K-cycle, bj23 symmetric post-smoother is bj23 itself
     k = m["cgmg_k_bj23"]
     assert (k["krylov"], k["w_loops"], k["pre"], k["post"]) == ("1", "-1", "3", "3")
+    # the p-multigrid preconditioner (SolverFactory.h:201-211): direct coarse solve by default; with
+    # "-cs mg" one h-multigrid cycle, V(0, 3) in 2D, below the lowest degree (SolverFactory.h:299-308)
+    assert m["fcgp_mg"] == dict(m["default"])
+    c = m["cg_p_mg_cs_mg"]
+    assert (c["krylov"], c["cpre"], c["cpost"], c["npre"], c["npost"]) == ("1", "0", "3", "1", "1")
 
 
-@pytest.mark.parametrize("what", ["solver", "smoother", "coarse", "variable"])
+@pytest.mark.parametrize("what", ["solver", "smoother", "coarse", "variable", "coarse_mg", "p_mg_w"])
 def test_adapter_rejects_unsupported(what):
     _mapped()
     p = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "adapter_check"), "--reject", what],
