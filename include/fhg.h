@@ -169,7 +169,12 @@ const char* fhg_last_error(const fhg_ctx* ctx);
  * (n_l x n_{l+1}, CSR) that LevelForHHO::SetupProlongation_H builds
  * (src/Solver/Multigrid/MultigridForHHO/LevelForHHO.h:182-213); R_l = P_l^T
  * (LevelForHHO.h:535-543). Replaces Level::Setup's operator/transfer setup
- * (src/Solver/Multigrid/Level.h:56-131). Copies the arrays. */
+ * (src/Solver/Multigrid/Level.h:56-131). Copies the arrays. block_size is the level's own
+ * (BlockSizeForBlockSmoothers): it may drop from one level to the next only where P_l is the
+ * natural injection between face degrees of the p-multigrid (P_LevelForHHO::SetupProlongation,
+ * src/Solver/Multigrid/MultigridForHHO/P_MultigridForHHO.h:69-92: the same faces, a 1 at
+ * (f * bs_l + i, f * bs_{l+1} + i) for i < bs_{l+1}); fhg_setup refuses any other change with
+ * FHG_ERR_UNSUPPORTED. */
 int fhg_set_level(fhg_ctx* ctx, int level, int block_size, int n,
                   const int* rowptr, const int* colidx, const double* vals);
 int fhg_set_prolongation(fhg_ctx* ctx, int level, int n_fine, int n_coarse,
