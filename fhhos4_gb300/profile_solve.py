@@ -6,12 +6,43 @@ Setup (hierarchy generation, upload, autotuning) and warm-up solves run outside 
 "solve"; `ncu --nvtx --nvtx-include "solve/" ...` then captures the launches of the timed solves
 only. `--step` instead applies one level-0 operator inside the range (the learned step, a forward
 GS sweep, the double-FP32 outer product, the SpMV in pair or native FP64 arithmetic, the FP32
-restriction or prolongation).
+restriction or prolongation). `--p-multigrid ch|mg` instead times FCG with the p-multigrid
+preconditioner against FCG with the h-multigrid one at the same degree (pair and FP32 V-cycles,
+default launch shapes) and prints one JSON line.
 """
 from __future__ import annotations
 
 import argparse
 import json
+
+
+def p_multigrid_timing(a):
+    """FCG(1) with the p-multigrid preconditioner of "-s fcgp_mg -cs <a.p_multigrid>" against FCG(1)
+    with the h-multigrid one (V(1,1) bgs/rbgs) on the same degree-k problem: the library's solve time
+    of the faster of two solves after one untimed, iterations and the FP64 true residual."""
+    import numpy as np
+    from . import hho
+    from . import solver as S
+    As, Ps, b, bss, cnu = hho.generate_p(a.dim, a.n, a.k, a.p_multigrid)
+    H = hho.Hierarchy(a.dim, a.n, a.k)
+    Ah, Ph = [H.A(l) for l in range(H.levels)], [H.P(l) for l in range(H.levels - 1)]
+    H.close()
+    out = {"workload": f"{a.dim}D n={a.n} k={a.k}", "unknowns": As[0].shape[0],
+           "p_mg": {"block_sizes": bss, "levels": [A.shape[0] for A in As], "coarse_solver": a.p_multigrid,
+                    "coarse_nu": list(cnu)},
+           "h_mg": {"levels": [A.shape[0] for A in Ah]}}
+    for name, (AA, PP, bb, cn) in (("p_mg", (As, Ps, bss, cnu)), ("h_mg", (Ah, Ph, bss[0], (-1, -1)))):
+        for prec in ("df", "fp32"):
+            s = S.fcg_mg(AA, PP, bb, coarse_nu=cn, precision=prec)
+            s.Solve(b)
+            ms = []
+            for _ in range(2):
+                x = s.Solve(b)
+                ms.append(s.SolveTimeMs)
+            out[name][prec] = {"ms": round(min(ms), 3), "iterations": s.IterationCount,
+                               "true_rel_residual": float(np.linalg.norm(b - As[0] @ x) / np.linalg.norm(b))}
+            s.Context().close()
+    print(json.dumps(out), flush=True)
 
 
 def main():
@@ -28,9 +59,14 @@ def main():
     ap.add_argument("--levels", type=int, default=0, help="use the first N levels (the last one solved directly)")
     ap.add_argument("--weights", default="", help="learned-step network (default: the committed one)")
     ap.add_argument("--gs-layout", default="auto", choices=["auto", "row", "slot"], help="FP32 GS sweep layout")
+    ap.add_argument("--p-multigrid", default="", choices=["", "ch", "mg"],
+                    help="compare FCG + p-multigrid (this coarse solver) with FCG + h-multigrid at --k")
     ap.add_argument("--step", choices=["", "learned_tcgen05", "learned_mma_sync", "gs_fp32", "outer_df", "spmv_df",
                                        "spmv_fp64", "restrict_fp32", "prolong_fp32"], default="")
     a = ap.parse_args()
+    if a.p_multigrid:
+        p_multigrid_timing(a)
+        return
 
     import torch
     from . import _native as N
