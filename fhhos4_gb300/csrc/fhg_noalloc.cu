@@ -14,8 +14,8 @@
 // exits. Host code cannot pass its name to a kernel (the name is a host-side stand-in, not a
 // device address), so the first call on each device (and the first call after that device's
 // context was replaced, e.g. by cudaDeviceReset) looks its device address up with
-// cudaGetSymbolAddress while that device is current and caches it with the context's id; make
-// that first call before any stream capture. All calls share the array: a call overwrites the
+// cudaGetSymbolAddress while that device is current and caches it with the context's id; later
+// calls make no runtime lookup. All calls share the array: a call overwrites the
 // partial sums it uses (nothing accumulates across calls, so nothing needs clearing), and two
 // calls that overlap on the GPU - on different streams, or from different host threads at once -
 // race on it and must be serialised by the caller.

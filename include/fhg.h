@@ -268,8 +268,8 @@ long long fhg_kernel_launches(const fhg_ctx* ctx);
  * 256/lanes block rows, so n_block_rows may be at most FHG_NOALLOC_MAX_PARTIALS*256/lanes
  * (4,194,304 block rows at 8 lanes): larger sizes return FHG_ERR_TOO_LARGE and launch nothing.
  * The first call on a device (and the first after that device's context was replaced, e.g. by
- * cudaDeviceReset) looks up the array's device address in the current context: make it before
- * any stream capture. Calls share the array and leave their partial sums in it: two calls that
+ * cudaDeviceReset) looks up the array's device address in the current context (cudaGetSymbolAddress);
+ * later calls reuse it. Calls share the array and leave their partial sums in it: two calls that
  * overlap on the GPU race on it. A CUDA error left pending by earlier work is returned as
  * FHG_ERR_CUDA before anything is launched and is not cleared. Makes the device current for the
  * call and restores the caller's current device. */
