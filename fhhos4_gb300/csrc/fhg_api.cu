@@ -1467,7 +1467,7 @@ int refresh_fused(fhg_ctx* ctx)
     return FHG_OK;
 }
 
-// b_{l+1} = R_l r (Multigrid.h:491): the product with R_l, or the natural injection's restriction.
+// b_{l+1} = R_l r (Multigrid.h:494): the product with R_l, or the natural injection's restriction.
 template <class T>
 void restrict_to(fhg_ctx* ctx, int l, const T* r, T* bc)
 {
@@ -1478,7 +1478,7 @@ void restrict_to(fhg_ctx* ctx, int l, const T* r, T* bc)
         fhg::launch_spmv<T>(LevelVecs<T>::R(L), fhg::kSpmvAssign, r, nullptr, bc, ctx->stream);
 }
 
-// out = aux + P_l e (Multigrid.h:531-533), aux NULL reading as zero.
+// out = aux + P_l e (Multigrid.h:554), aux NULL reading as zero.
 template <class T>
 void prolong_add(fhg_ctx* ctx, int l, const T* e, const T* aux, T* out)
 {
