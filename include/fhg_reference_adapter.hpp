@@ -28,9 +28,19 @@ class GpuFcgMg : public IterativeSolver
     fhg_ctx* _ctx = nullptr;
     Multigrid* _mg = nullptr;  // host-side hierarchy builder (reference code)
     bool _p = false;           // p-multigrid: P_MultigridForHHO, its levels' block sizes differ
+    int _device = 0;
     fhg_options _opts;
 
 public:
+    // One level of the hierarchy the reference's classes built: operator, prolongation to the next
+    // level (null on the coarsest) and block size.
+    struct HostLevel
+    {
+        const SparseMatrix* A;
+        const SparseMatrix* P;
+        int blockSize;
+    };
+
     GpuFcgMg(Diffusion_HHO<Dim>* problem, const ProgramArguments& args, int blockSize, int device = 0)
     {
         _opts = MapArguments(args);
@@ -72,7 +82,7 @@ public:
         }
         this->Tolerance = args.Solver.Tolerance;
         this->MaxIterations = args.Solver.MaxIterations;
-        Check(fhg_create(&_ctx, device));
+        _device = device;
     }
 
     ~GpuFcgMg()
@@ -86,37 +96,54 @@ public:
     void Setup(const SparseMatrix& A) override
     {
         IterativeSolver::Setup(A);
-        _mg->Setup(A);
+        BuildHostHierarchy(A);
         _opts.tolerance = this->Tolerance;   // the caller may have changed them after construction
         _opts.max_iterations = this->MaxIterations;
-        Level* fine = _mg->*(&fhg_detail::MultigridFineLevel::_fineLevel);
-        int l = 0;
-        Level* last = nullptr;
-        for (Level* lev = fine; lev; lev = lev->CoarserLevel, l++)
+        if (!_ctx)
+            Check(fhg_create(&_ctx, _device));
+        const std::vector<HostLevel> levels = Levels();
+        for (int l = 0; l < (int)levels.size(); l++)
         {
-            SetLevel(l, lev, _p ? lev->BlockSizeForBlockSmoothers() : _mg->BlockSizeForBlockSmoothers);
-            last = lev;
+            const HostLevel& L = levels[l];
+            Check(fhg_set_level(_ctx, l, L.blockSize, (int)L.A->rows(), L.A->outerIndexPtr(), L.A->innerIndexPtr(),
+                                L.A->valuePtr()));
+            if (L.P)
+                Check(fhg_set_prolongation(_ctx, l, (int)L.P->rows(), (int)L.P->cols(), L.P->outerIndexPtr(),
+                                           L.P->innerIndexPtr(), L.P->valuePtr()));
         }
-        // p-multigrid with the h-multigrid coarse solver: its levels below its finest (the lowest
-        // degree, already level l - 1) continue the hierarchy; its one cycle (no pre-smoothing,
-        // 3 / 6 post-smoothing steps) runs as the coarse part of the V-cycle.
+        Check(fhg_setup(_ctx, (int)levels.size(), &_opts));
+    }
+
+    // The reference's own multigrid setup on the host (no device call): MultigridForHHO's, or
+    // P_MultigridForHHO's with its coarse solver's.
+    void BuildHostHierarchy(const SparseMatrix& A) { _mg->Setup(A); }
+
+    // The levels the device hierarchy is made of, after BuildHostHierarchy. For the p-multigrid with
+    // the h-multigrid coarse solver, that solver's levels below its finest (the lowest degree, the
+    // last p-level) continue the hierarchy, and its one cycle (no pre-smoothing, 3 / 6 post-smoothing
+    // steps) runs as the coarse part of the V-cycle.
+    std::vector<HostLevel> Levels() const
+    {
+        std::vector<HostLevel> out;
+        Level* fine = _mg->*(&fhg_detail::MultigridFineLevel::_fineLevel);
+        for (Level* lev = fine; lev; lev = lev->CoarserLevel)
+            out.push_back({lev->OperatorMatrix, lev->IsCoarsestLevel() ? nullptr : &ProlongationOf(lev),
+                           _p ? lev->BlockSizeForBlockSmoothers() : _mg->BlockSizeForBlockSmoothers});
         if (Multigrid* inner = _p ? dynamic_cast<Multigrid*>(_mg->CoarseSolver) : nullptr)
         {
-            if (l != 2)
+            if (out.size() != 2)
                 Utils::FatalError("GPU solver: with '-cs mg' the p-multigrid must have exactly two levels (the "
                                   "finest and the lowest degree): other levels would need smoothing counts of their own");
             Level* f = inner->*(&fhg_detail::MultigridFineLevel::_fineLevel);
-            const int bs = last->BlockSizeForBlockSmoothers();
+            const int bs = out.back().blockSize;
             if (f && !f->IsCoarsestLevel())
             {
-                const SparseMatrix& P = f->*(&fhg_detail::LevelProlongation::P);
-                Check(fhg_set_prolongation(_ctx, l - 1, (int)P.rows(), (int)P.cols(), P.outerIndexPtr(),
-                                           P.innerIndexPtr(), P.valuePtr()));
+                out.back().P = &ProlongationOf(f);
+                for (Level* lev = f->CoarserLevel; lev; lev = lev->CoarserLevel)
+                    out.push_back({lev->OperatorMatrix, lev->IsCoarsestLevel() ? nullptr : &ProlongationOf(lev), bs});
             }
-            for (Level* lev = f ? f->CoarserLevel : nullptr; lev; lev = lev->CoarserLevel, l++)
-                SetLevel(l, lev, bs);
         }
-        Check(fhg_setup(_ctx, l, &_opts));
+        return out;
     }
 
     Vector Solve(const Vector& b, string initialGuessCode) override
@@ -149,20 +176,7 @@ private:
             Utils::FatalError(std::string("GPU solver: ") + fhg_last_error(_ctx));
     }
 
-    // Level l of the device hierarchy: the level's operator with its block size, and its
-    // prolongation unless it is the coarsest.
-    void SetLevel(int l, Level* lev, int blockSize)
-    {
-        const SparseMatrix& Al = *lev->OperatorMatrix;
-        Check(fhg_set_level(_ctx, l, blockSize, (int)Al.rows(), Al.outerIndexPtr(), Al.innerIndexPtr(),
-                            Al.valuePtr()));
-        if (!lev->IsCoarsestLevel())
-        {
-            const SparseMatrix& P = lev->*(&fhg_detail::LevelProlongation::P);
-            Check(fhg_set_prolongation(_ctx, l, (int)P.rows(), (int)P.cols(), P.outerIndexPtr(), P.innerIndexPtr(),
-                                       P.valuePtr()));
-        }
-    }
+    static const SparseMatrix& ProlongationOf(Level* lev) { return lev->*(&fhg_detail::LevelProlongation::P); }
 
     // The h-multigrid fields SolverFactory sets for "-s mg" (SolverFactory.h:183-200, 236-256).
     static void ConfigureH(MultigridForHHO<Dim>* mg, const MultigridArguments& m)

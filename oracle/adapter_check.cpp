@@ -1,7 +1,10 @@
 // Compile-and-link check of include/fhg_reference_adapter.hpp against the reference headers
 // (TEST INFRASTRUCTURE). `adapter_check --map` needs no GPU: it prints the fhg_options the adapter
-// derives from several ProgramArguments settings. Without arguments (GPU needed) it solves the
-// reference's 2D problem on a 32 x 32 triangle mesh (k = 1) through the adapter and prints the iterations.
+// derives from several ProgramArguments settings. `adapter_check --levels <dim> <n> <k> <solver>
+// <coarse solver>` needs no GPU either: it builds the reference's problem and the adapter's host
+// hierarchy and prints every level (rows, block size, prolongation shape) on stderr. Without arguments (GPU
+// needed) it solves the reference's 2D problem on a 32 x 32 triangle mesh (k = 1) through the
+// adapter and prints the iterations.
 #include "ProgramArguments.h"
 #include "Discretizations/DG/Diffusion_DG.h"
 #include "TestCases/Diffusion/DiffTestCaseFactory.h"
@@ -63,10 +66,63 @@ static int map_check()
     return 0;
 }
 
+// The reference's problem (Dirichlet, the built-in test case) on the in-house triangle or
+// tetrahedral mesh with the default bases of main.cpp:1703-1735, assembled.
+template <int D>
+static Diffusion_HHO<D>* make_problem(ProgramArguments& args, int n, int k)
+{
+    args.Problem.Dimension = D;
+    args.Problem.GeoCode = args.Problem.TestCaseCode = D == 2 ? "square" : "cube";
+    args.Problem.BCCode = "d";
+    args.Solver.MG.H_CS = H_CoarsStgy::StandardCoarsening;
+    args.Solver.MG.GMG_H_Prolong = GMG_H_Prolongation::CellInterp_Trace;
+    args.Actions.LogAssembly = false;
+    Utils::ProgramArgs = args;
+    GaussLegendre::Init();
+    auto* tc = DiffTestCaseFactory<D>::Create(args.Problem);
+    Mesh<D>* mesh;
+    if constexpr (D == 2)
+        mesh = new Square_TriangularMesh(n, n);
+    else
+        mesh = new Cube_CartesianTetrahedralMesh(n);
+    mesh->SetDiffusionField(&tc->DiffField);
+    mesh->SetBoundaryConditions(&tc->BC);
+    auto* rb = FunctionalBasisFactory<D>::Create("monomials", k + 1, false);
+    auto* cb = FunctionalBasisFactory<D>::Create("monomials", k, false);
+    auto* fb = FunctionalBasisFactory<D - 1>::Create(D == 2 ? "legendre" : "monomials", k, false);
+    auto* hho = new HHOParameters<D>(mesh, "hho", rb, cb, fb, 1, D == 2 ? 0 : 1);
+    auto* pb = new Diffusion_HHO<D>(mesh, tc, hho, true, false);
+    pb->Assemble(args.Actions, ExportModule(""));
+    return pb;
+}
+
+template <int D>
+static int levels_check(int n, int k, const std::string& solver, const std::string& coarse)
+{
+    ProgramArguments args;
+    args.Solver.SolverCode = solver;
+    args.Solver.MG.CoarseSolverCode = coarse;
+    Diffusion_HHO<D>* pb = make_problem<D>(args, n, k);
+    GpuFcgMg<D> s(pb, args, pb->HHO->nFaceUnknowns);
+    s.BuildHostHierarchy(pb->A);
+    const auto levels = s.Levels();
+    // on stderr: the reference logs its setup on stdout
+    for (size_t l = 0; l < levels.size(); l++)
+        std::cerr << "level" << l << " rows=" << levels[l].A->rows() << " bs=" << levels[l].blockSize
+                  << " p_rows=" << (levels[l].P ? levels[l].P->rows() : 0)
+                  << " p_cols=" << (levels[l].P ? levels[l].P->cols() : 0) << std::endl;
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
     if (argc > 1 && std::string(argv[1]) == "--map")
         return map_check();
+    if (argc > 6 && std::string(argv[1]) == "--levels")
+    {
+        const int dim = atoi(argv[2]), n = atoi(argv[3]), k = atoi(argv[4]);
+        return dim == 2 ? levels_check<2>(n, k, argv[5], argv[6]) : levels_check<3>(n, k, argv[5], argv[6]);
+    }
     if (argc > 2 && std::string(argv[1]) == "--reject")
     {   // an unsupported setting: the mapping must end in Utils::FatalError
         ProgramArguments a;
@@ -88,25 +144,8 @@ int main(int argc, char** argv)
     }
     ProgramArguments args;
     args.Solver.SolverCode = "fcgmg";
-    args.Problem.Dimension = 2;
-    args.Problem.GeoCode = args.Problem.TestCaseCode = "square";
-    args.Problem.BCCode = "d";
-    args.Solver.MG.H_CS = H_CoarsStgy::StandardCoarsening;
-    args.Solver.MG.GMG_H_Prolong = GMG_H_Prolongation::CellInterp_Trace;
-    args.Actions.LogAssembly = false;
-    Utils::ProgramArgs = args;
-    GaussLegendre::Init();
-    auto* tc = DiffTestCaseFactory<2>::Create(args.Problem);
-    Mesh<2>* mesh = new Square_TriangularMesh(32, 32);
-    mesh->SetDiffusionField(&tc->DiffField);
-    mesh->SetBoundaryConditions(&tc->BC);
-    auto* rb = FunctionalBasisFactory<2>::Create("monomials", 2, false);
-    auto* cb = FunctionalBasisFactory<2>::Create("monomials", 1, false);
-    auto* fb = FunctionalBasisFactory<1>::Create("legendre", 1, false);
-    auto* hho = new HHOParameters<2>(mesh, "hho", rb, cb, fb, 1, 0);
-    auto* pb = new Diffusion_HHO<2>(mesh, tc, hho, true, false);
-    pb->Assemble(args.Actions, ExportModule(""));
-    GpuFcgMg<2> solver(pb, args, fb->Size());
+    Diffusion_HHO<2>* pb = make_problem<2>(args, 32, 1);
+    GpuFcgMg<2> solver(pb, args, pb->HHO->nFaceUnknowns);
     solver.Tolerance = 1e-8;
     solver.Setup(pb->A);
     Vector x = solver.Solve(pb->b, "0");

@@ -58,3 +58,39 @@ def test_adapter_rejects_unsupported(what):
                        capture_output=True, text=True, timeout=60)
     assert p.returncode != 0 and "accepted" not in p.stdout
     assert "GPU solver" in p.stdout + p.stderr
+
+
+def _levels(*argv):
+    _mapped()
+    p = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "adapter_check"), "--levels", *map(str, argv)],
+                       check=True, capture_output=True, text=True, timeout=300)
+    rows = []
+    for line in p.stderr.splitlines():
+        if line.startswith("level"):
+            rows.append({k: int(v) for k, v in (x.split("=") for x in line.split()[1:])})
+    return rows
+
+
+@pytest.mark.parametrize("cs", ["ch", "mg"])
+def test_adapter_builds_the_p_multigrid_hierarchy(cs):
+    """The adapter's host side (no device call): the reference's P_MultigridForHHO levels (and, for
+    "-cs mg", its coarse multigrid's levels below the lowest degree) with their block sizes and
+    prolongations, the hierarchy hho.generate_p builds for the same problem."""
+    from fhhos4_gb300 import hho
+    got = _levels(2, 16, 3, "fcgp_mg", cs)
+    As, Ps, b, bss, _ = hho.generate_p(2, 16, 3, cs)
+    assert [r["rows"] for r in got] == [A.shape[0] for A in As]
+    assert [r["bs"] for r in got] == bss
+    assert [(r["p_rows"], r["p_cols"]) for r in got] == [P.shape for P in Ps] + [(0, 0)]
+
+
+def test_adapter_builds_the_h_multigrid_hierarchy():
+    from fhhos4_gb300 import hho
+    got = _levels(2, 32, 1, "fcgmg", "ch")
+    H = hho.Hierarchy(2, 32, 1)
+    try:
+        assert [r["rows"] for r in got] == [H.A_rows(l) for l in range(H.levels)]
+        assert all(r["bs"] == H.block_size for r in got)
+    finally:
+        H.close()
+
