@@ -65,6 +65,20 @@ def test_p_degrees_follow_the_reference_rule():
         hho.p_degrees(2, 1, big)
 
 
+def test_generate_p_refuses_what_the_cycle_cannot_express():
+    """With the h-multigrid coarse solver the composite hierarchy smooths every level below the
+    finest with the coarse solver's counts: that is the reference's cycle only with exactly two
+    p-levels."""
+    with pytest.raises(NotImplementedError, match="smoothing counts"):
+        hho.generate_p(2, 16, 3, "mg", strategy="minus1")          # degrees 3, 2, 1
+    with pytest.raises(NotImplementedError, match="lowest-degree"):
+        hho.generate_p(2, 4, 3, "mg")                              # already at most 1000 unknowns
+    with pytest.raises(ValueError):
+        hho.generate_p(2, 16, 3, "lu")
+    As, Ps, b, bss, cnu = hho.generate_p(2, 16, 3, "ch", strategy="minus1")
+    assert bss == [4, 3, 2] and cnu == (-1, -1) and len(Ps) == 2
+
+
 def test_natural_injection_structure():
     P = hho.natural_injection(5, 6, 3)
     assert P.shape == (30, 15) and P.nnz == 15 and np.all(P.data == 1.0)
