@@ -12,7 +12,7 @@
 //         residual history captured through IterativeSolver::OnIterationEnd
 //         (src/Solver/IterativeSolver.h:224-227) and the solution x.
 //
-//   genp  <dim> <n> <k> <outdir> [--coarse-solver ch|mg]
+//   genp  <dim> <n> <k> <outdir> [--coarse-solver ch|mg] [--p-cs minus1|minus2]
 //         The same pipeline with the p-multigrid preconditioner ("-s fcg -p p_mg", P_MultigridForHHO
 //         through SolverFactory.h:201-211, P_CS Minus2 and CoarsePolyDegree 1 as defaulted) and the
 //         coarse solver "-cs ch" (Cholesky of the lowest degree) or "-cs mg" (one h-multigrid cycle
@@ -128,7 +128,8 @@ static void ParseSmoothers(const std::string& s, std::string& pre, std::string& 
 // gen: the reference pipeline end to end.
 template <int D>
 static int RunGen(int n, int k, const std::string& outdir, const std::string& pre, const std::string& post, bool solve,
-                  const std::string& precond = "mg", const std::string& coarseSolver = "ch")
+                  const std::string& precond = "mg", const std::string& coarseSolver = "ch",
+                  P_CoarsStgy pcs = P_CoarsStgy::Minus2)
 {
 	ProgramArguments args;
 	args.Problem.Dimension = D;
@@ -156,6 +157,7 @@ static int RunGen(int n, int k, const std::string& outdir, const std::string& pr
 	args.Solver.MG.PreSmoothingIterations = 1;
 	args.Solver.MG.PostSmoothingIterations = 1;
 	args.Solver.MG.CoarseSolverCode = coarseSolver;
+	args.Solver.MG.P_CS = pcs;
 	args.Actions.LogAssembly = false;
 	Utils::ProgramArgs = args;
 	GaussLegendre::Init();
@@ -391,6 +393,7 @@ int main(int argc, char** argv)
 	int maxit = 200;
 	bool solve = true;
 	std::string coarseSolver = "ch";
+	P_CoarsStgy pcs = P_CoarsStgy::Minus2;
 	std::vector<std::string> pos;
 	for (int i = 2; i < argc; i++)
 	{
@@ -403,6 +406,7 @@ int main(int argc, char** argv)
 		else if (a == "--no-solve") solve = false;
 		else if (a == "--cycle" && i + 1 < argc) cycle = argv[++i][0];
 		else if (a == "--coarse-solver" && i + 1 < argc) coarseSolver = argv[++i];
+		else if (a == "--p-cs" && i + 1 < argc) pcs = std::string(argv[++i]) == "minus1" ? P_CoarsStgy::Minus1 : P_CoarsStgy::Minus2;
 		else pos.push_back(a);
 	}
 	std::cout.setstate(std::ios_base::failbit); // the reference logs to stdout; keep it quiet
@@ -416,8 +420,8 @@ int main(int argc, char** argv)
 	else if (mode == "genp" && pos.size() == 4)
 	{
 		int dim = atoi(pos[0].c_str()), n = atoi(pos[1].c_str()), k = atoi(pos[2].c_str());
-		if (dim == 2) rc = RunGen<2>(n, k, pos[3], pre, post, solve, "p_mg", coarseSolver);
-		else rc = RunGen<3>(n, k, pos[3], pre, post, solve, "p_mg", coarseSolver);
+		if (dim == 2) rc = RunGen<2>(n, k, pos[3], pre, post, solve, "p_mg", coarseSolver, pcs);
+		else rc = RunGen<3>(n, k, pos[3], pre, post, solve, "p_mg", coarseSolver, pcs);
 	}
 	else if (mode == "solve" && pos.size() == 1)
 		rc = RunSolve(pos[0], pre, post, krylov, tol, maxit, cycle, omega);

@@ -21,6 +21,8 @@ Only ``hist_*`` summaries are kept for the large cases (``--histories-only``).
 p-multigrid preconditioner ("-s fcg -p p_mg", P_MultigridForHHO) with the coarse solvers "ch" and
 "mg" (``hist_ch``/``x_ch``, ``hist_mg``/``x_mg``), the block size of every level, and per level
 A_l v_l for a seeded v_l (``Av{l}``) with A_l's shape and entry count instead of A_l itself.
+The 2D case also holds the strategy Minus1 with "ch" (degrees 3, 2, 1: ``hist_ch_minus1``,
+``x_ch_minus1``, ``block_sizes_ch_minus1``).
 
 Usage:  python tests/golden/make_golden.py [case ...] [--histories-only | --add-k-cycle | --add-sor]
 """
@@ -231,6 +233,14 @@ def make_p_case(name, dim, n, k):
                     out[f"P{l}_shape"] = np.asarray(P.shape, dtype=np.int64)
                     out[f"P{l}_nnz"] = P.nnz
                     out[f"Pv{l}"] = P @ probe_vector(100 + l, P.shape[1])
+        if dim == 2:
+            d = os.path.join(tmp, "minus1")
+            os.makedirs(d)
+            subprocess.run([O.REF_DRIVER, "genp", str(dim), str(n), str(k), d, "--coarse-solver", "ch",
+                            "--p-cs", "minus1"], check=True)
+            out["hist_ch_minus1"] = np.fromfile(f"{d}/history.f64")
+            out["x_ch_minus1"] = np.fromfile(f"{d}/x.f64")
+            out["block_sizes_ch_minus1"] = np.fromfile(f"{d}/block_sizes.i32", dtype=np.int32)
     out.update(dim=dim, n=n, k=k)
     path = os.path.join(GOLDEN, name + ".npz")
     np.savez_compressed(path, **out)

@@ -123,6 +123,22 @@ def test_oracle_p_multigrid_matches_reference(case, hierarchies, cs):
     assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < X_RTOL
 
 
+def test_oracle_three_p_levels_match_reference():
+    """P_CoarsStgy Minus1 with the direct coarse solver: face degrees 3, 2, 1 (block sizes 4, 3, 2),
+    two natural injections, every p-level smoothed V(1,1): the oracle against the reference's run."""
+    z = np.load(os.path.join(GOLDEN, "p_tri2d_n16_k3.npz"))
+    if "hist_ch_minus1" not in z.files:
+        pytest.skip("fixture without the Minus1 case")
+    As, Ps, b, bss, cnu = hho.generate_p(2, 16, 3, "ch", strategy="minus1")
+    assert bss == [int(v) for v in z["block_sizes_ch_minus1"]]
+    x, hist, it, rc = O.fcgmg_solve(As, Ps, z["b"], bss, coarse_iterations=cnu)
+    ref = z["hist_ch_minus1"]
+    assert rc == 0 and it == len(ref) - 1
+    assert hist_close(hist, ref), (hist, ref)
+    xr = z["x_ch_minus1"]
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < X_RTOL
+
+
 # ------------------------------------------------------------------------------------------ GPU
 def _solver():
     from fhhos4_gb300 import solver
