@@ -983,6 +983,12 @@ struct Level {
     std::vector<int> P_rowptr, P_colidx;
     std::vector<double> P_vals;
     int P_cols = 0;
+    // Tables of P (kept when asked for, fhg_hho_prolongation_tables): per unknown fine face its
+    // coarse elements (up to two, -1: none), their weights and contribution slots; per slot the
+    // nf x (dim + 1) nf contribution of a coarse element to a fine face.
+    std::vector<int> Pt_ce, Pt_slot;
+    std::vector<double> Pt_w, Pt_contrib;
+    int Pt_nslots = 0;
 };
 
 // What element_ops depends on besides the element's position: the offsets of its vertices and of
@@ -1156,8 +1162,9 @@ void assemble(Level& L, const Params& prm, int threads, bool want_rhs)
     });
 }
 
-// P (fine faces x coarse faces) of LevelForHHO::SetupProlongation_H with CellInterp_Trace.
-void prolongation(Level& F, const Level& C, const Params& prm, const Rules& rules, int threads)
+// P (fine faces x coarse faces) of LevelForHHO::SetupProlongation_H with CellInterp_Trace; with
+// `tables`, also the tables of P (Level::Pt_*).
+void prolongation(Level& F, const Level& C, const Params& prm, const Rules& rules, int threads, bool tables)
 {
     const Mesh& M = F.mesh;
     const Mesh& MC = C.mesh;
@@ -1177,6 +1184,23 @@ void prolongation(Level& F, const Level& C, const Params& prm, const Rules& rule
         ce[0] = M.coarser[e1]; w[0] = k1 / (k1 + k2);
         ce[1] = M.coarser[e2]; w[1] = k2 / (k1 + k2);
         nce = 2;
+    };
+    // The contribution of coarse element ce to the fine face of points Q and basis FB:
+    // M_f^{-1} (phi_a, r_j)_f (the trace of the coarse reconstruction basis on the fine face) times
+    // the coarse element's interpolation from its faces, nf x (nFc nf).
+    auto contribution = [&](const QPts& Q, const FaceBasis& FB, int ce) {
+        const ElementOps& O = C.cls_ops[C.cls[ce]];
+        const auto xc = centroid(MC, ce);
+        const int nR = O.nR, nfq = (int)Q.w.size();
+        Mat m(nf, nR);
+        double v[64];
+        for (int q = 0; q < nfq; q++) {
+            O.basis.eval_at(Q.x[q].data(), xc.data(), v, nullptr);
+            for (int a = 0; a < nf; a++)
+                for (int j = 0; j < nR; j++) m(a, j) += Q.w[q] * FB.vals(a, q) * v[j];
+        }
+        Mat tr = matmul(FB.mass_inv, m);
+        return matmul(tr, O.interp);
     };
     parallel_for(nI, threads, [&](size_t s, size_t e) {
         for (size_t I = s; I < e; I++) {
@@ -1220,21 +1244,8 @@ void prolongation(Level& F, const Level& C, const Params& prm, const Rules& rule
             double measure, diam;
             const QPts Q = face_points(M, f, rules.face, rules.face, measure, diam);
             const FaceBasis FB = face_basis(dim, prm.k, Q);
-            const int nfq = (int)Q.w.size();
             for (int t = 0; t < nce; t++) {
-                const ElementOps& O = C.cls_ops[C.cls[ce[t]]];
-                const auto xc = centroid(MC, ce[t]);
-                const int nR = O.nR;
-                // Trace of the coarse reconstruction basis on the fine face: M_f^{-1} (phi_a, r_j)_f
-                Mat m(nf, nR);
-                double v[64];
-                for (int q = 0; q < nfq; q++) {
-                    O.basis.eval_at(Q.x[q].data(), xc.data(), v, nullptr);
-                    for (int a = 0; a < nf; a++)
-                        for (int j = 0; j < nR; j++) m(a, j) += Q.w[q] * FB.vals(a, q) * v[j];
-                }
-                Mat tr = matmul(FB.mass_inv, m);
-                Mat contrib = matmul(tr, O.interp);  // nf x (nFc nf)
+                const Mat contrib = contribution(Q, FB, ce[t]);  // nf x (nFc nf)
                 for (int lf = 0; lf < nFc; lf++) {
                     const int g = MC.number[MC.ef[ce[t]][lf]];
                     if (g < 0) continue;
@@ -1246,6 +1257,56 @@ void prolongation(Level& F, const Level& C, const Params& prm, const Rules& rule
                     }
                 }
             }
+        }
+    });
+    if (!tables) return;
+    // A coarse element's contribution to a fine face depends only on the element's class and on
+    // where the face lies in it: the face's vertices, in the face's own order (which fixes its
+    // basis), relative to the element's first vertex, in units of the fine spacing rounded to 1/4096
+    // of it. One slot per such pair, computed once.
+    struct KeyHash {
+        size_t operator()(const std::array<long long, 10>& k) const
+        {
+            uint64_t hsh = 1469598103934665603ull;
+            for (long long v : k) hsh = (hsh ^ (uint64_t)v) * 1099511628211ull;
+            return (size_t)hsh;
+        }
+    };
+    std::unordered_map<std::array<long long, 10>, int, KeyHash> slot_of;
+    std::vector<std::pair<int, int>> reps;   // per slot: (fine face, coarse element)
+    F.Pt_ce.assign((size_t)nI * 2, -1);
+    F.Pt_slot.assign((size_t)nI * 2, -1);
+    F.Pt_w.assign((size_t)nI * 2, 0.0);
+    const double scale = 4096.0 * M.n;
+    for (int I = 0; I < nI; I++) {
+        const int f = face_of[I];
+        int ce[2], nce;
+        double w[2];
+        coarse_elems(f, ce, w, nce);
+        for (int t = 0; t < nce; t++) {
+            std::array<long long, 10> key{};
+            key[0] = C.cls[ce[t]];
+            const auto& x0 = MC.vx[MC.el[ce[t]][0]];
+            for (int v = 0; v < dim; v++)
+                for (int d = 0; d < dim; d++) key[1 + v * 3 + d] = std::llround((M.vx[M.fv[f][v]][d] - x0[d]) * scale);
+            const auto ins = slot_of.emplace(key, (int)reps.size());
+            if (ins.second) reps.emplace_back(f, ce[t]);
+            F.Pt_ce[(size_t)I * 2 + t] = ce[t];
+            F.Pt_w[(size_t)I * 2 + t] = w[t];
+            F.Pt_slot[(size_t)I * 2 + t] = ins.first->second;
+        }
+    }
+    const int ncc = nFc * nf;
+    F.Pt_nslots = (int)reps.size();
+    F.Pt_contrib.assign((size_t)reps.size() * nf * ncc, 0.0);
+    parallel_for(reps.size(), threads, [&](size_t s, size_t e) {
+        for (size_t r = s; r < e; r++) {
+            double measure, diam;
+            const QPts Q = face_points(M, reps[r].first, rules.face, rules.face, measure, diam);
+            const FaceBasis FB = face_basis(dim, prm.k, Q);
+            const Mat c = contribution(Q, FB, reps[r].second);
+            for (int a = 0; a < nf; a++)
+                for (int j = 0; j < ncc; j++) F.Pt_contrib[(r * nf + a) * ncc + j] = c(a, j);
         }
     });
 }
@@ -1423,7 +1484,7 @@ int fhg_hho_create(fhg_hho** out, const fhg_hho_params* p)
                 if (L.cls_ops[c].local.a.size() == nH * nH)
                     std::copy(L.cls_ops[c].local.a.begin(), L.cls_ops[c].local.a.end(), L.cls_local.begin() + c * nH * nH);
         }
-        if (l > 0) prolongation(H->levels[l - 1], L, prm, rules, threads);
+        if (l > 0) prolongation(H->levels[l - 1], L, prm, rules, threads, p->p_tables != 0);
         if (l > 1) {
             // element data of levels above the finest no longer needed (the finest keeps it for
             // the L2 error of a solution)
@@ -1453,6 +1514,39 @@ int fhg_hho_level(const fhg_hho* h, int l, int* n_rows, long long* nnz, const in
     if (rowptr) *rowptr = L.A_rowptr.data();
     if (colidx) *colidx = L.A_colidx.data();
     if (vals) *vals = L.A_vals.data();
+    return 0;
+}
+
+int fhg_hho_prolongation_table_sizes(const fhg_hho* h, int l, int* n_face_blocks, int* n_slots, int* n_coarse_elements,
+                                     int* block_size, int* faces_per_element)
+{
+    if (!h || l < 0 || l + 1 >= (int)h->levels.size()) return -1;
+    const Level& F = h->levels[l];
+    if (F.Pt_ce.empty()) return -2;
+    if (n_face_blocks) *n_face_blocks = F.mesh.n_interior;
+    if (n_slots) *n_slots = F.Pt_nslots;
+    if (n_coarse_elements) *n_coarse_elements = (int)h->levels[l + 1].mesh.el.size();
+    if (block_size) *block_size = h->block_size;
+    if (faces_per_element) *faces_per_element = F.mesh.dim + 1;
+    return 0;
+}
+
+int fhg_hho_prolongation_tables(const fhg_hho* h, int l, int* face_ce, double* face_w, int* face_slot,
+                                double* slot_contrib, int* coarse_elem_faces)
+{
+    if (!h || l < 0 || l + 1 >= (int)h->levels.size()) return -1;
+    const Level& F = h->levels[l];
+    if (F.Pt_ce.empty()) return -2;
+    if (face_ce) std::copy(F.Pt_ce.begin(), F.Pt_ce.end(), face_ce);
+    if (face_w) std::copy(F.Pt_w.begin(), F.Pt_w.end(), face_w);
+    if (face_slot) std::copy(F.Pt_slot.begin(), F.Pt_slot.end(), face_slot);
+    if (slot_contrib) std::copy(F.Pt_contrib.begin(), F.Pt_contrib.end(), slot_contrib);
+    if (coarse_elem_faces) {
+        const Mesh& MC = h->levels[l + 1].mesh;
+        const int nF = MC.dim + 1;
+        for (size_t e = 0; e < MC.el.size(); e++)
+            for (int lf = 0; lf < nF; lf++) coarse_elem_faces[e * nF + lf] = MC.number[MC.ef[e][lf]];
+    }
     return 0;
 }
 

@@ -31,6 +31,7 @@ typedef struct {
     int threads;          /* 0: all hardware threads */
     double eps_min;       /* FHG_HHO_ANISOTROPIC: smallest eps (1e-3) */
     unsigned long long seed; /* coefficient fields and random sources */
+    int p_tables;         /* 1: keep the tables of every P (fhg_hho_prolongation_tables); 0 (default) */
 } fhg_hho_params;
 
 typedef struct fhg_hho fhg_hho;
@@ -46,6 +47,19 @@ int fhg_hho_level(const fhg_hho* h, int level, int* n_rows, long long* nnz, cons
 int fhg_hho_prolongation(const fhg_hho* h, int level, int* n_rows, int* n_cols, long long* nnz,
                          const int** rowptr, const int** colidx, const double** vals);
 int fhg_hho_rhs(const fhg_hho* h, const double** b);
+/* The tables of P_l (kept with p_tables = 1; -2 otherwise), for assembling it elsewhere: a coarse
+ * element's contribution to a fine face depends only on the element's class and the face's place
+ * in it, so it is stored once per such slot. Sizes, then the arrays (each optional): face_ce and
+ * face_w [n_face_blocks * 2] (the unknown fine face's coarse elements, -1 for none, and their
+ * weights), face_slot [n_face_blocks * 2], slot_contrib [n_slots * bs * faces_per_element * bs]
+ * (row-major bs x faces_per_element*bs per slot), coarse_elem_faces [n_coarse_elements *
+ * faces_per_element] (coarse unknown blocks, -1: Dirichlet). P's block row of face I sums, over its
+ * coarse elements t, face_w * slot_contrib with column block lf of the slot going to coarse block
+ * coarse_elem_faces[ce][lf]. */
+int fhg_hho_prolongation_table_sizes(const fhg_hho* h, int level, int* n_face_blocks, int* n_slots,
+                                     int* n_coarse_elements, int* block_size, int* faces_per_element);
+int fhg_hho_prolongation_tables(const fhg_hho* h, int level, int* face_ce, double* face_w, int* face_slot,
+                                double* slot_contrib, int* coarse_elem_faces);
 /* Relative L2 error of the reconstruction of face solution x (level-0 numbering) against the
  * exact solution of the sine source; -2 for sources without a closed form. */
 int fhg_hho_l2_error(const fhg_hho* h, const double* x, double* rel_error);

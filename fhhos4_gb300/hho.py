@@ -22,7 +22,7 @@ class Params(C.Structure):
     _fields_ = [("dim", C.c_int), ("n", C.c_int), ("k", C.c_int), ("max_coarse_rows", C.c_int),
                 ("max_levels", C.c_int), ("source", C.c_int), ("coefficient", C.c_int), ("contrast", C.c_double),
                 ("checker_blocks", C.c_int), ("threads", C.c_int), ("eps_min", C.c_double),
-                ("seed", C.c_ulonglong)]
+                ("seed", C.c_ulonglong), ("p_tables", C.c_int)]
 
 
 _lib = None
@@ -69,7 +69,7 @@ class Hierarchy:
 
     def __init__(self, dim: int, n: int, k: int = 1, max_coarse_rows: int = 1000, max_levels: int = 0,
                  source: str = "sine", coefficient: str = "identity", contrast: float = 1.0, checker_blocks: int = 4,
-                 threads: int = 0, eps_min: float = 1e-3, seed: int = 20261203):
+                 threads: int = 0, eps_min: float = 1e-3, seed: int = 20261203, p_tables: bool = False):
         L = lib()
         p = Params()
         L.fhg_hho_default_params(C.byref(p))
@@ -78,6 +78,7 @@ class Hierarchy:
         p.source, p.coefficient = SOURCE[source], COEFFICIENT[coefficient]
         p.contrast, p.checker_blocks, p.threads = contrast, checker_blocks, threads
         p.eps_min, p.seed = eps_min, seed
+        p.p_tables = 1 if p_tables else 0
         self.h = C.c_void_p()
         self.dim = dim
         rc = L.fhg_hho_create(C.byref(self.h), C.byref(p))
@@ -104,6 +105,27 @@ class Hierarchy:
                                C.byref(va))
         return sp.csr_matrix((_arr(va, nnz.value, np.float64), _arr(ci, nnz.value, np.int32),
                               _arr(rp, nr.value + 1, np.int32)), shape=(nr.value, nc.value))
+
+    def prolongation_tables(self, l: int) -> dict:
+        """The tables of P_l (the hierarchy made with p_tables=True): per unknown fine face its coarse
+        elements `face_ce` (n, 2; -1: none), weights `face_w` and slots `face_slot`; per slot the
+        contribution `slot_contrib` (bs x faces_per_element*bs); per coarse element its unknown face
+        blocks `coarse_elem_faces` (-1: Dirichlet)."""
+        L = lib()
+        sz = [C.c_int() for _ in range(5)]
+        rc = L.fhg_hho_prolongation_table_sizes(self.h, l, *[C.byref(v) for v in sz])
+        if rc != 0:
+            raise RuntimeError("no prolongation tables (make the hierarchy with p_tables=True)" if rc == -2
+                               else "prolongation_table_sizes failed")
+        nI, ns, nce, bs, nF = (v.value for v in sz)
+        t = dict(n_face_blocks=nI, n_slots=ns, n_coarse_elements=nce, block_size=bs, faces_per_element=nF,
+                 face_ce=np.zeros((nI, 2), np.int32), face_w=np.zeros((nI, 2)), face_slot=np.zeros((nI, 2), np.int32),
+                 slot_contrib=np.zeros((ns, bs, nF * bs)), coarse_elem_faces=np.zeros((nce, nF), np.int32))
+        if L.fhg_hho_prolongation_tables(self.h, l, *[C.c_void_p(t[k].ctypes.data) for k in
+                                                      ("face_ce", "face_w", "face_slot", "slot_contrib",
+                                                       "coarse_elem_faces")]) != 0:
+            raise RuntimeError("prolongation_tables failed")
+        return t
 
     def b(self) -> np.ndarray:
         L = lib()
